@@ -1,0 +1,251 @@
+/*
+ * strobealign_gb300 -- C ABI of the GB300 (sm_103a) read-mapping library.
+ *
+ * The library is a drop-in for strobealign's per-read mapping path: index
+ * construction and StrobemerIndex lookups, NAM finding (seeding -> hits ->
+ * anchors -> collinear chaining), base-level extension (SSW-exact Smith-Waterman,
+ * Hamming fast path, mate rescue) and SAM / PAF / abundance output.  Every call
+ * returns an int32 status (SA_OK or a negative SA_ERR_*); it never aborts.  The
+ * message of the last failure on the calling thread is sa_last_error().
+ *
+ * Buffers passed in are borrowed for the duration of the call (the library copies
+ * what it keeps).  Output buffers returned through sa_output are owned by the
+ * library until sa_output_free().  Handles are not thread-safe unless stated.
+ *
+ * Reference interfaces each entry point replaces are cited as file:line of the
+ * strobealign source tree (Rust, v0.18.0-alpha).
+ */
+#ifndef STROBEALIGN_GB300_H
+#define STROBEALIGN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define SA_OK 0
+#define SA_ERR_INVALID (-1)      /* bad argument or parameter                 */
+#define SA_ERR_CUDA (-2)         /* CUDA runtime error or no usable device      */
+#define SA_ERR_OOM (-3)          /* device or host allocation failed            */
+#define SA_ERR_IO (-4)           /* file could not be read or written           */
+#define SA_ERR_STI_MISMATCH (-5) /* .sti magic/version/parameters differ        */
+#define SA_ERR_TIMEOUT (-6)      /* a bounded device wait gave up               */
+#define SA_ERR_CANCELLED (-7)    /* request cancelled                           */
+#define SA_ERR_FORMAT (-8)       /* malformed FASTA/FASTQ input                 */
+#define SA_ERR_BUSY (-9)         /* admission refused: not enough free memory   */
+
+/* Message describing the last failure on this thread (never NULL). */
+const char* sa_last_error(void);
+/* Library version string. */
+const char* sa_version(void);
+
+/* ---------------------------------------------------------------- parameters */
+/* SeedingParameters (src/seeding/parameters.rs:164-171; presets :102-159). */
+typedef struct {
+    uint32_t profile; /* Profile discriminant: 0 noisy, 1 r50, ... 7 r400 */
+    uint32_t k, s, t;
+    uint32_t w_min, w_max;
+    uint64_t q;
+    uint32_t max_dist;
+    uint32_t partial_orientation_pos;
+    uint64_t main_hash_mask;
+    uint64_t forward_main_hash_mask;
+} sa_seeding_params;
+
+/* SeedingParameters::new(read_length) (src/seeding/parameters.rs:181-221). */
+int32_t sa_seeding_params_from_read_length(size_t read_length, sa_seeding_params* out);
+
+/* ChainingParameters (src/chainer.rs:16-44), MappingParameters (src/mapper.rs:31-55),
+ * Scores (src/aligner.rs:11-30) and SAM output options (src/mapper.rs:87-112). */
+typedef struct {
+    uint32_t max_lookback;        /* 50 */
+    float diag_diff_penalty;      /* 0.1 */
+    float gap_length_penalty;     /* 0.05 */
+    float valid_score_threshold;  /* 0.7 */
+    uint32_t max_ref_gap;         /* 0 = read length */
+    float matches_weight;         /* 0.01 */
+    float max_diagonal_ratio;     /* 10.0 */
+} sa_chaining_params;
+
+enum { SA_MCS_ALWAYS = 0, SA_MCS_RESCUE = 1, SA_MCS_OFF = 2, SA_MCS_FIRST_STROBE = 3 };
+enum { SA_MODE_SAM = 0, SA_MODE_PAF = 1, SA_MODE_ABUNDANCE = 2 };
+
+typedef struct {
+    uint32_t max_secondary;  /* -N, 0 */
+    float dropoff_threshold; /* -S, 0.5 */
+    uint32_t rescue_distance;/* -R, 100 */
+    uint32_t max_tries;      /* -M, 20 */
+    uint32_t mcs_strategy;   /* SA_MCS_* */
+    uint32_t output_unmapped;/* !-U, 1 */
+    uint32_t use_ssw;        /* --ssw: single-end extension by SSW instead of piecewise */
+    int32_t xdrop;           /* 500 */
+    uint8_t match, mismatch, gap_open, gap_extend; /* 2 8 12 1 */
+    uint32_t end_bonus;      /* 10 */
+    uint32_t mode;           /* SA_MODE_* */
+    uint32_t eqx;            /* --eqx */
+    uint32_t details;        /* --details */
+    uint32_t fastq_comments; /* -C */
+    const char* rg_id;       /* RG:Z: value or NULL */
+    size_t chunk_size;       /* nucleotides per chunk (1000000) */
+} sa_mapping_params;
+
+/* Fill the reference's defaults. */
+void sa_chaining_params_default(sa_chaining_params* p);
+void sa_mapping_params_default(sa_mapping_params* p);
+
+/* ---------------------------------------------------------------- references */
+/* Reference contigs as PackedSeq (src/packed_seq.rs) plus names; read_fasta
+ * (src/io/fasta.rs:116-165). */
+typedef struct sa_refs sa_refs;
+int32_t sa_refs_from_fasta(const char* path, sa_refs** out);
+int32_t sa_refs_from_buffers(size_t n_contigs, const char* const* names, const char* const* seqs,
+                             const size_t* lens, sa_refs** out);
+size_t sa_refs_count(const sa_refs* refs);
+size_t sa_refs_total_length(const sa_refs* refs);
+/* SyncmerParameters::pick_bits (src/indexer.rs:294-300). */
+uint32_t sa_refs_pick_bits(const sa_refs* refs, const sa_seeding_params* p);
+void sa_refs_free(sa_refs* refs);
+
+/* ---------------------------------------------------------------- index */
+/* StrobemerIndex resident in device memory (src/index.rs:66-90). */
+typedef struct sa_index sa_index;
+
+typedef struct {
+    uint32_t bits;
+    uint32_t filter_cutoff;
+    uint64_t n_randstrobes;
+    uint64_t device_bytes;
+    sa_seeding_params params;
+} sa_index_info;
+
+/* make_index (src/indexer.rs:18-170) built on the GPU; bits < 0 picks
+ * automatically.  The sorted table and directory are identical to the reference's. */
+int32_t sa_index_build(const sa_refs* refs, const sa_seeding_params* p, int32_t bits, double filter_fraction,
+                       sa_index** out);
+/* read_index (src/index.rs:412-495) straight into device memory. */
+int32_t sa_index_read_sti(const char* path, const sa_seeding_params* p, int32_t bits, sa_index** out);
+/* StrobemerIndex::write (src/index.rs:374-409), .sti format version 7. */
+int32_t sa_index_write_sti(const sa_index* idx, const char* path);
+int32_t sa_index_get_info(const sa_index* idx, sa_index_info* out);
+/* Copy the sorted RefRandstrobe table (16 B each: u64 hash_offset, u32 position,
+ * u32 ref_index) and the (2^bits + 1) bucket starts to host memory. */
+int32_t sa_index_copy_to_host(const sa_index* idx, void* randstrobes, uint64_t* bucket_starts);
+
+/* Batched StrobemerIndex lookups (src/index.rs:127-205, :254-338).
+ * kind: 0 get_full_forward, 1 get_partial, 2 get_partial_forward.
+ * out_position[i] = table index of the first match or -1; out_count[i] (may be
+ * NULL) = get_count for the matched mask. Host buffers. */
+int32_t sa_index_lookup_batch(const sa_index* idx, const uint64_t* hashes, size_t n, int32_t kind,
+                              int64_t* out_position, uint32_t* out_count);
+void sa_index_free(sa_index* idx);
+
+/* ---------------------------------------------------------------- reads */
+/* A batch of reads in host memory.  Sequence i is seq[seq_offsets[i] ..
+ * seq_offsets[i+1]); qual (optional, same offsets), names and comments
+ * (optional) likewise.  For paired-end input, r1 and r2 batches have equal n. */
+typedef struct {
+    size_t n;
+    const char* seq;
+    const uint64_t* seq_offsets; /* n + 1 */
+    const char* qual;            /* NULL for FASTA input */
+    const char* names;
+    const uint64_t* name_offsets; /* n + 1 */
+    const char* comments;         /* NULL if none */
+    const uint64_t* comment_offsets;
+} sa_read_batch;
+
+/* Parse a FASTQ/FASTA read file (src/io/fastq.rs:19-100) into an owned batch. */
+typedef struct sa_reads sa_reads;
+int32_t sa_reads_from_file(const char* path, sa_reads** out);
+int32_t sa_reads_view(const sa_reads* reads, sa_read_batch* view);
+void sa_reads_free(sa_reads* reads);
+
+/* ---------------------------------------------------------------- stage entry points */
+/* randstrobes_query (src/seeding/mod.rs:19-75) for every read of the batch.
+ * Output arrays are sized by the caller: capacity entries each; per read r the
+ * forward randstrobes are at [out_offsets[2r], +out_counts[2r]) and the
+ * reverse-complement ones at [out_offsets[2r+1], +out_counts[2r+1]). */
+typedef struct {
+    uint64_t hash;
+    uint64_t hash_revcomp;
+    uint32_t start;
+    uint32_t end;
+} sa_query_randstrobe;
+int32_t sa_randstrobes_batch(const sa_index* idx, const sa_read_batch* reads, sa_query_randstrobe* out,
+                             size_t capacity, uint64_t* out_offsets, uint32_t* out_counts);
+
+/* get_nams_by_chaining (src/nam.rs:138-166) for every read; NAMs in the order the
+ * reference produces them (before sort_nams). */
+typedef struct {
+    uint32_t nam_id;
+    uint32_t ref_id;
+    uint32_t ref_start, ref_end;
+    uint32_t query_start, query_end;
+    uint32_t matching_bases;
+    uint32_t n_anchors;
+    float score;
+    uint32_t is_revcomp;
+} sa_nam;
+/* per-read statistics (NamDetails, src/details.rs:7-32) */
+typedef struct {
+    uint32_t full_not_found, full_filtered, full_found;
+    uint32_t partial_not_found, partial_filtered, partial_found;
+    uint32_t rescued;
+    uint32_t n_randstrobes, n_anchors, n_nams;
+    uint32_t both_orientations;
+} sa_nam_details;
+int32_t sa_nams_batch(const sa_index* idx, const sa_chaining_params* cp, const sa_mapping_params* mp,
+                      const sa_read_batch* reads, sa_nam* out, size_t capacity, uint64_t* out_offsets,
+                      uint32_t* out_counts, sa_nam_details* out_details);
+
+/* Aligner::align (src/aligner.rs:80-151) = ssw_align (ext/ssw/ssw.c:818-922) plus
+ * end-bonus extension, for independent (query, reference) pairs.  CIGAR ops use
+ * the reference encoding len << 4 | op (src/cigar.rs:5-16), =/X form. */
+typedef struct {
+    int32_t valid; /* 0 where the reference returns None */
+    uint32_t score;
+    uint32_t query_start, query_end, ref_start, ref_end;
+    uint32_t edit_distance;
+    uint32_t cigar_offset, cigar_len; /* into the cigar output array */
+} sa_alignment;
+int32_t sa_align_batch(const sa_mapping_params* mp, size_t n, const char* queries, const uint64_t* query_offsets,
+                       const char* refs, const uint64_t* ref_offsets, sa_alignment* out, uint32_t* cigar,
+                       size_t cigar_capacity);
+
+/* ---------------------------------------------------------------- mapping */
+typedef struct sa_mapper sa_mapper;
+/* The mapper keeps the index and per-batch arenas resident on the device. */
+int32_t sa_mapper_create(const sa_index* idx, const sa_refs* refs, const sa_chaining_params* cp,
+                         const sa_mapping_params* mp, sa_mapper** out);
+void sa_mapper_free(sa_mapper* m);
+
+typedef struct {
+    char* data;     /* SAM records (no header) / PAF lines; owned by the library */
+    size_t len;
+    uint64_t n_reads;
+    uint64_t n_mapped;
+    uint32_t n_waves;      /* extension waves the batch needed */
+    uint32_t n_gpu_launches;
+} sa_output;
+
+/* Map a batch (Mapper::map_chunk, src/main.rs:873-988).  The batch is cut into
+ * chunks exactly as the reference cuts its input (records until the nucleotide
+ * count exceeds chunk_size), each with a fresh RNG and insert-size estimate, so
+ * a batch that starts at the beginning of an input reproduces the reference's
+ * output bytes for those records.  r2 = NULL for single-end. */
+int32_t sa_map_batch(sa_mapper* m, const sa_read_batch* r1, const sa_read_batch* r2, sa_output* out);
+void sa_output_free(sa_output* out);
+/* Abundances accumulated over all batches (--aemb), one per contig, already
+ * divided by the contig length (src/main.rs:990-1001). */
+int32_t sa_mapper_abundances(const sa_mapper* m, double* out, size_t n);
+/* SAM header (src/io/sam.rs:176-200); cmd_line NULL omits the @PG line. */
+int32_t sa_sam_header(const sa_refs* refs, const char* cmd_line, const char* rg_id, const char* const* rg_fields,
+                      size_t n_rg_fields, sa_output* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STROBEALIGN_GB300_H */

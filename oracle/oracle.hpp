@@ -1,0 +1,320 @@
+// Oracle: a sequential CPU restatement of strobealign's per-read mapping path.
+//
+// TEST INFRASTRUCTURE ONLY.  Nothing in the product (strobealign_gb300/) links,
+// loads or calls this code; only tests/, __graft_entry__.smoke() and the
+// cpu_baseline leg of bench.py use it, and only as the checker / the timed CPU
+// baseline.  Each function cites the reference file:line it restates (paths are
+// relative to the strobealign source tree).
+//
+// Parity pins: tests/golden/ holds the reference's own phiX goldens
+// (tests/phix.{se,pe,tags}.sam, phix.{se,mcsrescue.se}.paf, phix.abun.{se,pe}.txt)
+// and the SSW restatement is fuzzed against the reference's compiled
+// ext/ssw/ssw.c (oracle/_ref/, built only where the reference tree is present).
+// Two third-party behaviours are restated from their published algorithms and
+// are "parity unpinned": fastrand 2.3.0 (wyrand + Lemire bounded ints, used only
+// to break ties) and block-aligner 0.5.1 (single-end piecewise extension).
+#pragma once
+#include <cstdint>
+#include <cstddef>
+#include <string>
+#include <vector>
+#include <optional>
+#include <utility>
+
+namespace oracle {
+
+// ---------------------------------------------------------------- sequences
+// src/packed_seq.rs:1-126 -- 2-bit reference, 32 nt per u64, LSB first;
+// non-ACGTU bytes become a position hash (packed_seq.rs:56-59).
+struct PackedSeq {
+    std::vector<uint64_t> data;
+    size_t len = 0;
+    void push(uint8_t c);
+    uint8_t bits(size_t i) const { return (uint8_t)((data[i >> 5] >> ((i & 31) * 2)) & 3); }
+    uint8_t decode_at(size_t i) const { return "ACGT"[bits(i)]; }
+    std::string decode(size_t start, size_t end) const;
+};
+
+struct RefSeq {
+    std::string name;
+    PackedSeq seq;
+};
+
+std::string reverse_complement(const std::string& s);  // src/revcomp.rs:1-29
+uint64_t xxh64(uint64_t x);                             // src/seeding/hash.rs:9-27
+
+// ---------------------------------------------------------------- parameters
+// src/seeding/parameters.rs:92-327
+struct SeedingParameters {
+    int profile = 5;  // Profile enum discriminant (Noisy=0, R50=1 ... R400=7)
+    size_t k = 20, s = 16, t = 3;
+    size_t w_min = 5, w_max = 11;
+    uint64_t q = 255;
+    uint32_t max_dist = 80;
+    uint64_t main_hash_mask = 0xFFFFFFFFFC000000ULL;
+    uint64_t forward_main_hash_mask = 0;
+    uint32_t partial_orientation_pos = 25;
+    static SeedingParameters from_read_length(size_t read_length);
+    void finish_masks();
+};
+
+struct Syncmer {
+    uint64_t hash;
+    bool is_forward;
+    size_t position;
+};
+
+struct QueryRandstrobe {
+    uint64_t hash, hash_revcomp;
+    size_t start, end;
+};
+
+std::vector<Syncmer> syncmers_of_read(const std::string& seq, const SeedingParameters& p);
+std::vector<Syncmer> syncmers_of_ref(const PackedSeq& seq, const SeedingParameters& p);
+void randstrobes_query(const std::string& seq, const SeedingParameters& p,
+                       std::vector<QueryRandstrobe> out[2]);
+
+// ---------------------------------------------------------------- index
+// src/index.rs:15-110
+constexpr uint64_t REF_RANDSTROBE_HASH_MASK = 0xFFFFFFFFFFFFFF00ULL;
+struct RefRandstrobe {
+    uint64_t hash_offset;
+    uint32_t position;
+    uint32_t ref_index;
+    uint64_t hash() const { return hash_offset & REF_RANDSTROBE_HASH_MASK; }
+    uint32_t offset() const { return (uint32_t)(hash_offset & 0xFF); }
+};
+static_assert(sizeof(RefRandstrobe) == 16, "RefRandstrobe must be 16 bytes");
+
+struct Index {
+    SeedingParameters params;
+    uint8_t bits = 0;
+    size_t filter_cutoff = 0;
+    std::vector<RefRandstrobe> randstrobes;
+    std::vector<uint64_t> bucket_starts;
+
+    // sentinel SIZE_MAX means "not found"
+    size_t get_masked_from(uint64_t hash, uint64_t mask, size_t start_position, bool has_start) const;
+    size_t get_full_forward(uint64_t h) const { return get_masked_from(h, REF_RANDSTROBE_HASH_MASK, 0, false); }
+    size_t get_partial(uint64_t h) const { return get_masked_from(h, params.main_hash_mask, 0, false); }
+    size_t get_partial_forward_from(uint64_t h, size_t pos) const {
+        return get_masked_from(h, params.forward_main_hash_mask, pos, true);
+    }
+    size_t get_count(size_t position, uint64_t mask) const;
+    size_t get_count_full_forward(size_t pos) const { return get_count(pos, REF_RANDSTROBE_HASH_MASK); }
+    size_t get_count_partial(size_t pos) const { return get_count(pos, params.main_hash_mask); }
+    size_t get_count_full(size_t pos, uint64_t hash_revcomp) const;
+    bool is_too_frequent_forward(size_t pos, size_t cutoff) const;
+    bool is_too_frequent(size_t pos, size_t cutoff, uint64_t hash_revcomp) const;
+    bool is_too_frequent_partial(size_t pos, size_t cutoff) const;
+};
+
+uint8_t pick_bits(const std::vector<RefSeq>& refs, const SeedingParameters& p);
+Index make_index(const std::vector<RefSeq>& refs, const SeedingParameters& p, uint8_t bits,
+                 double filter_fraction);
+bool write_sti(const Index& idx, const std::string& path);
+int read_sti(const std::string& path, const SeedingParameters& p, uint8_t bits, Index& out);
+
+// ---------------------------------------------------------------- hits, chains
+enum class Mcs { Always = 0, Rescue = 1, Off = 2, FirstStrobe = 3 };
+
+struct HitsDetails {
+    size_t full_not_found = 0, full_filtered = 0, full_found = 0;
+    size_t partial_not_found = 0, partial_filtered = 0, partial_found = 0;
+    size_t rescued = 0;
+    size_t total_hits() const { return partial_filtered + partial_found + full_filtered + full_found; }
+    size_t total_found() const { return full_found + partial_found; }
+    bool is_better_than(const HitsDetails& o) const {
+        size_t total = full_found + full_filtered, other = o.full_found + o.full_filtered;
+        return total >= other * 2 && total > other + 5;
+    }
+    void add(const HitsDetails& o);
+};
+
+struct Hit {
+    size_t query_start, query_end, position;
+    uint64_t hash, hash_revcomp;
+    bool is_partial, is_filtered;
+};
+
+struct Anchor {
+    size_t ref_id, ref_start, query_start;
+    bool operator<(const Anchor& o) const {
+        if (ref_id != o.ref_id) return ref_id < o.ref_id;
+        if (ref_start != o.ref_start) return ref_start < o.ref_start;
+        return query_start < o.query_start;
+    }
+    bool operator==(const Anchor& o) const {
+        return ref_id == o.ref_id && ref_start == o.ref_start && query_start == o.query_start;
+    }
+};
+
+struct ChainingParameters {
+    size_t max_lookback = 50;
+    float diag_diff_penalty = 0.1f;
+    float gap_length_penalty = 0.05f;
+    float valid_score_threshold = 0.7f;
+    size_t max_ref_gap = 0;  // 0 = read length (Option::None)
+    bool has_max_ref_gap = false;
+    float matches_weight = 0.01f;
+    float max_diagonal_ratio = 10.0f;
+};
+
+struct Nam {
+    size_t nam_id = 0, ref_start = 0, ref_end = 0, query_start = 0, query_end = 0;
+    size_t matching_bases = 0, ref_id = 0;
+    float score = 0;
+    bool is_revcomp = false;
+    std::vector<Anchor> anchors;
+    size_t projected_ref_start() const { return ref_start > query_start ? ref_start - query_start : 0; }
+};
+
+struct NamDetails {
+    HitsDetails hits;
+    size_t n_reads = 0, n_randstrobes = 0, n_anchors = 0, n_nams = 0;
+    bool both_orientations = false;
+    void add(const NamDetails& o);
+};
+
+struct Details {
+    NamDetails nam;
+    size_t inconsistent_nams = 0, mate_rescue = 0, tried_alignment = 0, gapped = 0, best_alignments = 0;
+    void add(const Details& o);
+};
+
+float chaining_score(size_t dq, size_t dr, size_t k, const ChainingParameters& cp);
+
+void find_hits(const std::vector<QueryRandstrobe>& qr, const Index& idx, Mcs mcs, size_t filter_cutoff,
+               size_t rescue_distance, HitsDetails& details, std::vector<Hit>& hits);
+std::vector<Anchor> hits_to_anchors(const std::vector<Hit>& hits, const Index& idx);
+std::vector<Nam> get_nams_by_chaining(const std::string& seq, const Index& idx, const ChainingParameters& cp,
+                                      size_t rescue_distance, Mcs mcs, NamDetails& details);
+
+// fastrand 2.3.0 restated (wyrand); parity unpinned (see header)
+struct Rng {
+    uint64_t state;
+    explicit Rng(uint64_t seed) : state(seed) {}
+    uint64_t gen_u64();
+    uint32_t gen_mod_u32(uint32_t n);
+    uint64_t gen_mod_u64(uint64_t n);
+    uint32_t u32_below(uint32_t n) { return gen_mod_u32(n); }  // u32(..n), n >= 1
+    size_t usize_below(size_t n) { return (size_t)gen_mod_u64((uint64_t)n); }
+    template <class T> void shuffle(T* items, size_t n) {
+        for (size_t i = 1; i < n; i++) {
+            size_t j = (size_t)gen_mod_u64((uint64_t)(i + 1));
+            std::swap(items[i], items[j]);
+        }
+    }
+};
+
+void sort_nams(std::vector<Nam>& nams, Rng& rng);
+
+// ---------------------------------------------------------------- alignment
+enum CigarOp : uint8_t { OP_M = 0, OP_I = 1, OP_D = 2, OP_N = 3, OP_S = 4, OP_H = 5, OP_P = 6, OP_EQ = 7, OP_X = 8 };
+struct Cigar {
+    std::vector<uint32_t> ops;  // len << 4 | op  (src/cigar.rs:68-75)
+    void push(uint8_t op, size_t len);
+    void extend(const Cigar& o) { for (uint32_t v : o.ops) push(v & 15, v >> 4); }
+    Cigar reversed() const;
+    Cigar with_m() const;
+    Cigar with_eqx(const std::string& q, const std::string& r) const;
+    size_t edit_distance() const;
+    std::string str() const;
+};
+
+struct AlignmentInfo {
+    Cigar cigar;
+    size_t edit_distance = 0, ref_start = 0, ref_end = 0, query_start = 0, query_end = 0;
+    uint32_t score = 0;
+};
+
+struct Scores {
+    uint8_t match = 2, mismatch = 8, gap_open = 12, gap_extend = 1;
+    uint32_t end_bonus = 10;
+};
+
+// Restated SSW (ext/ssw/ssw.c:163-922) with the exact striped semantics.
+struct SswResult {
+    uint16_t score1 = 0;
+    int32_t ref_begin1 = -1, ref_end1 = -1, read_begin1 = -1, read_end1 = -1;
+    std::vector<uint32_t> cigar;  // M/I/D ops
+    uint16_t flag = 0;
+};
+SswResult ssw_align(const int8_t* read, int32_t read_len, const int8_t* ref, int32_t ref_len,
+                    const int8_t* mat, int32_t n, uint8_t gap_open, uint8_t gap_extend);
+std::vector<int8_t> ssw_translate(const std::string& s);  // src/ssw.rs:8-25
+
+std::optional<AlignmentInfo> ssw_aligner_align(const std::string& query, const std::string& ref, const Scores& sc);
+std::optional<AlignmentInfo> aligner_align(const std::string& query, const std::string& ref, const Scores& sc);
+std::optional<AlignmentInfo> hamming_align(const std::string& query, const std::string& ref, uint8_t match,
+                                           uint8_t mismatch, uint32_t end_bonus);
+AlignmentInfo hamming_align_global(const std::string& query, const std::string& ref, uint8_t match, uint8_t mismatch);
+void highest_scoring_segment(const std::string& q, const std::string& r, uint8_t match, uint8_t mismatch,
+                             uint32_t end_bonus, size_t& start, size_t& end, uint32_t& score);
+
+// ---------------------------------------------------------------- mapping
+struct MappingParameters {
+    size_t max_secondary = 0;
+    float dropoff_threshold = 0.5f;
+    size_t rescue_distance = 100;
+    size_t max_tries = 20;
+    Mcs mcs = Mcs::Always;
+    bool output_unmapped = true;
+    bool use_ssw = false;
+    int32_t xdrop = 500;
+};
+
+struct SequenceRecord {
+    std::string name;
+    int end = 0;  // 0 none, 1 '/1', 2 '/2'
+    std::string comment;
+    bool has_comment = false;
+    std::string seq;
+    std::string qual;
+    bool has_qual = false;
+};
+
+struct SamOptions {
+    bool eqx = false, details = false, fastq_comments = false;
+    std::string rg_id;
+    bool has_rg = false;
+};
+
+struct InsertSizeDistribution {
+    size_t sample_size = 0;
+    float mu = 300.0f, sigma = 100.0f, variance = 10000.0f, sse = 10000.0f;
+    void update(size_t insert_size);
+};
+
+struct Context {
+    const std::vector<RefSeq>* refs;
+    const Index* index;
+    MappingParameters mp;
+    ChainingParameters cp;
+    Scores sc;
+    SamOptions so;
+};
+
+std::string align_single_end_read(const SequenceRecord& r, const Context& ctx, Rng& rng, Details& det);
+std::string align_paired_end_read(const SequenceRecord& r1, const SequenceRecord& r2, const Context& ctx,
+                                  InsertSizeDistribution& isd, Rng& rng, Details& det);
+std::string map_single_end_read(const SequenceRecord& r, const Context& ctx, Rng& rng, Details& det);
+std::string map_paired_end_read(const SequenceRecord& r1, const SequenceRecord& r2, const Context& ctx,
+                                InsertSizeDistribution& isd, Rng& rng, Details& det);
+void abundances_single_end_read(const SequenceRecord& r, const Context& ctx, std::vector<double>& ab, Rng& rng);
+void abundances_paired_end_read(const SequenceRecord& r1, const SequenceRecord& r2, const Context& ctx,
+                                std::vector<double>& ab, InsertSizeDistribution& isd, Rng& rng);
+
+// Piecewise single-end extension (src/piecewisealigner.rs); block-aligner restated.
+void remove_spurious_anchors(std::vector<Anchor>& anchors);
+std::optional<AlignmentInfo> extend_piecewise(const std::string& query, const std::string& ref,
+                                              const std::vector<Anchor>& anchors, size_t padding, size_t k,
+                                              const Scores& sc, int32_t xdrop);
+
+// ---------------------------------------------------------------- io
+bool read_fasta(const std::string& path, std::vector<RefSeq>& out, std::string& err);
+bool read_fastq_file(const std::string& path, std::vector<SequenceRecord>& out, std::string& err);
+std::string sam_header(const std::vector<RefSeq>& refs, const std::string* cmd_line, const std::string& version,
+                       const std::string* rg_id, const std::vector<std::string>& rg_fields);
+
+}  // namespace oracle

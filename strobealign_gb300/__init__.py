@@ -1,0 +1,387 @@
+"""strobealign_gb300: strobealign's per-read mapping path on one GB300 GPU.
+
+Python face of the C ABI (include/strobealign_gb300.h), mirroring the reference's
+library surface:
+
+* ``SeedingParameters.from_read_length`` -- SeedingParameters::new (src/seeding/parameters.rs)
+* ``References`` -- reference contigs (src/io/fasta.rs, src/packed_seq.rs)
+* ``StrobemerIndex.build`` / ``.read_sti`` / ``.write_sti`` / lookups -- make_index
+  (src/indexer.rs) and StrobemerIndex (src/index.rs)
+* ``randstrobes_batch`` / ``nams_batch`` / ``align_batch`` -- randstrobes_query,
+  get_nams_by_chaining, Aligner::align for whole batches
+* ``Mapper.map`` -- align_single_end_read / align_paired_end_read /
+  map_*_read / abundances_*_read (src/mapper.rs, src/maponly.rs) per chunk as
+  Mapper::map_chunk does (src/main.rs)
+
+All compute runs on the GPU through the compiled library; nothing here falls
+back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+
+MODE_SAM, MODE_PAF, MODE_ABUNDANCE = 0, 1, 2
+MCS = {"always": 0, "rescue": 1, "off": 2, "first-strobe": 3}
+
+
+def lib() -> C.CDLL:
+    return L.load()
+
+
+def _p(arr, ctype):
+    return arr.ctypes.data_as(C.POINTER(ctype))
+
+
+class SeedingParameters:
+    """SeedingParameters (src/seeding/parameters.rs:164-221)."""
+
+    def __init__(self, c: L.SeedingParams):
+        self.c = c
+
+    @classmethod
+    def from_read_length(cls, read_length: int) -> "SeedingParameters":
+        c = L.SeedingParams()
+        L.check(lib().sa_seeding_params_from_read_length(read_length, C.byref(c)))
+        return cls(c)
+
+    def __getattr__(self, name):
+        return getattr(self.c, name)
+
+
+class References:
+    """Reference contigs held as 2-bit PackedSeq on the host (uploaded by the index/mapper)."""
+
+    def __init__(self, handle: int):
+        self.h = C.c_void_p(handle)
+
+    @classmethod
+    def from_fasta(cls, path: str) -> "References":
+        h = C.c_void_p()
+        L.check(lib().sa_refs_from_fasta(str(path).encode(), C.byref(h)))
+        return cls(h.value)
+
+    @classmethod
+    def from_sequences(cls, names: list[str], seqs: list[bytes | str]) -> "References":
+        n = len(names)
+        bn = [x.encode() for x in names]
+        bs = [s.encode() if isinstance(s, str) else bytes(s) for s in seqs]
+        an = (C.c_char_p * n)(*bn)
+        aseq = (C.c_char_p * n)(*bs)
+        alen = (C.c_size_t * n)(*[len(s) for s in bs])
+        h = C.c_void_p()
+        L.check(lib().sa_refs_from_buffers(n, an, aseq, alen, C.byref(h)))
+        r = cls(h.value)
+        r._keep = (bn, bs)
+        return r
+
+    def __len__(self):
+        return lib().sa_refs_count(self.h)
+
+    @property
+    def total_length(self) -> int:
+        return lib().sa_refs_total_length(self.h)
+
+    def pick_bits(self, params: SeedingParameters) -> int:
+        return lib().sa_refs_pick_bits(self.h, C.byref(params.c))
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().sa_refs_free(self.h)
+            self.h = C.c_void_p()
+
+
+RS_DTYPE = np.dtype([("hash_offset", "<u8"), ("position", "<u4"), ("ref_index", "<u4")])
+
+
+class StrobemerIndex:
+    """Device-resident StrobemerIndex (src/index.rs:66-338)."""
+
+    FULL_FORWARD, PARTIAL, PARTIAL_FORWARD = 0, 1, 2
+
+    def __init__(self, handle: int, params: SeedingParameters):
+        self.h = C.c_void_p(handle)
+        self.params = params
+
+    @classmethod
+    def build(cls, refs: References, params: SeedingParameters, bits: int = -1,
+              filter_fraction: float = 0.0002) -> "StrobemerIndex":
+        h = C.c_void_p()
+        L.check(lib().sa_index_build(refs.h, C.byref(params.c), bits, filter_fraction, C.byref(h)))
+        return cls(h.value, params)
+
+    @classmethod
+    def read_sti(cls, path: str, params: SeedingParameters, bits: int = -1) -> "StrobemerIndex":
+        h = C.c_void_p()
+        L.check(lib().sa_index_read_sti(str(path).encode(), C.byref(params.c), bits, C.byref(h)))
+        return cls(h.value, params)
+
+    def write_sti(self, path: str) -> None:
+        L.check(lib().sa_index_write_sti(self.h, str(path).encode()))
+
+    @property
+    def info(self) -> L.IndexInfo:
+        i = L.IndexInfo()
+        L.check(lib().sa_index_get_info(self.h, C.byref(i)))
+        return i
+
+    @property
+    def filter_cutoff(self) -> int:
+        return self.info.filter_cutoff
+
+    @property
+    def bits(self) -> int:
+        return self.info.bits
+
+    def __len__(self):
+        return self.info.n_randstrobes
+
+    def to_host(self) -> tuple[np.ndarray, np.ndarray]:
+        info = self.info
+        rs = np.zeros(info.n_randstrobes, dtype=RS_DTYPE)
+        bs = np.zeros((1 << info.bits) + 1, dtype=np.uint64)
+        L.check(lib().sa_index_copy_to_host(self.h, rs.ctypes.data_as(C.c_void_p), _p(bs, C.c_uint64)))
+        return rs, bs
+
+    def lookup(self, hashes, kind: int = 0, counts: bool = False):
+        """get_full_forward / get_partial / get_partial_forward for many hashes at once."""
+        h = np.ascontiguousarray(hashes, dtype=np.uint64)
+        pos = np.zeros(h.size, dtype=np.int64)
+        cnt = np.zeros(h.size, dtype=np.uint32) if counts else None
+        L.check(lib().sa_index_lookup_batch(self.h, _p(h, C.c_uint64), h.size, kind, _p(pos, C.c_int64),
+                                            _p(cnt, C.c_uint32) if counts else None))
+        return (pos, cnt) if counts else pos
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().sa_index_free(self.h)
+            self.h = C.c_void_p()
+
+
+@dataclass
+class Reads:
+    """A batch of reads as concatenated buffers (the C ABI's sa_read_batch)."""
+
+    seq: bytes
+    seq_offsets: np.ndarray
+    names: bytes
+    name_offsets: np.ndarray
+    qual: bytes | None = None
+    comments: bytes | None = None
+    comment_offsets: np.ndarray | None = None
+
+    @classmethod
+    def from_lists(cls, names, seqs, quals=None, comments=None) -> "Reads":
+        bs = [s.encode() if isinstance(s, str) else bytes(s) for s in seqs]
+        bn = [x.encode() if isinstance(x, str) else bytes(x) for x in names]
+        so = np.zeros(len(bs) + 1, dtype=np.uint64)
+        so[1:] = np.cumsum([len(s) for s in bs])
+        no = np.zeros(len(bn) + 1, dtype=np.uint64)
+        no[1:] = np.cumsum([len(s) for s in bn])
+        q = None
+        if quals is not None:
+            q = b"".join(x.encode() if isinstance(x, str) else bytes(x) for x in quals)
+        cm = co = None
+        if comments is not None:
+            bc = [(c or "").encode() if isinstance(c or "", str) else bytes(c) for c in comments]
+            co = np.zeros(len(bc) + 1, dtype=np.uint64)
+            co[1:] = np.cumsum([len(s) for s in bc])
+            cm = b"".join(bc)
+        return cls(b"".join(bs), so, b"".join(bn), no, q, cm, co)
+
+    @classmethod
+    def from_arrays(cls, seq: np.ndarray, seq_offsets: np.ndarray, names: bytes, name_offsets: np.ndarray,
+                    qual: bytes | None = None) -> "Reads":
+        return cls(seq.tobytes() if isinstance(seq, np.ndarray) else seq, np.ascontiguousarray(seq_offsets, np.uint64),
+                   names, np.ascontiguousarray(name_offsets, np.uint64), qual)
+
+    @classmethod
+    def from_file(cls, path: str) -> "Reads":
+        h = C.c_void_p()
+        L.check(lib().sa_reads_from_file(str(path).encode(), C.byref(h)))
+        try:
+            v = L.ReadBatch()
+            L.check(lib().sa_reads_view(h, C.byref(v)))
+            n = v.n
+            so = np.ctypeslib.as_array(v.seq_offsets, shape=(n + 1,)).copy()
+            no = np.ctypeslib.as_array(v.name_offsets, shape=(n + 1,)).copy()
+            co = np.ctypeslib.as_array(v.comment_offsets, shape=(n + 1,)).copy()
+            seq = C.string_at(v.seq, int(so[-1])) if so[-1] else b""
+            names = C.string_at(v.names, int(no[-1])) if no[-1] else b""
+            qual = C.string_at(v.qual, int(so[-1])) if v.qual else None
+            comments = C.string_at(v.comments, int(co[-1])) if co[-1] else b""
+            return cls(seq, so, names, no, qual, comments, co)
+        finally:
+            lib().sa_reads_free(h)
+
+    def __len__(self):
+        return len(self.seq_offsets) - 1
+
+    def c(self) -> L.ReadBatch:
+        b = L.ReadBatch()
+        self._bufs = [self.seq, self.names, self.qual, self.comments]
+        b.n = len(self)
+        b.seq = C.cast(C.c_char_p(self.seq), C.c_void_p)
+        b.seq_offsets = _p(self.seq_offsets, C.c_uint64)
+        b.qual = C.cast(C.c_char_p(self.qual), C.c_void_p) if self.qual is not None else None
+        b.names = C.cast(C.c_char_p(self.names), C.c_void_p)
+        b.name_offsets = _p(self.name_offsets, C.c_uint64)
+        if self.comments is not None and self.comment_offsets is not None:
+            b.comments = C.cast(C.c_char_p(self.comments), C.c_void_p)
+            b.comment_offsets = _p(self.comment_offsets, C.c_uint64)
+        return b
+
+
+def chaining_defaults() -> L.ChainingParams:
+    c = L.ChainingParams()
+    lib().sa_chaining_params_default(C.byref(c))
+    return c
+
+
+def mapping_defaults(**kw) -> L.MappingParams:
+    m = L.MappingParams()
+    lib().sa_mapping_params_default(C.byref(m))
+    for k, v in kw.items():
+        if k == "rg_id":
+            v = v.encode() if isinstance(v, str) else v
+        if k == "mcs_strategy" and isinstance(v, str):
+            v = MCS[v]
+        setattr(m, k, v)
+    return m
+
+
+def randstrobes_batch(index: StrobemerIndex, reads: Reads):
+    """randstrobes_query for each read: list of (forward, reverse-complement) arrays."""
+    n = len(reads)
+    cap = int(reads.seq_offsets[-1]) * 2 + 1
+    out = (L.QueryRandstrobe * cap)()
+    offs = np.zeros(2 * n, dtype=np.uint64)
+    cnt = np.zeros(2 * n, dtype=np.uint32)
+    b = reads.c()
+    L.check(lib().sa_randstrobes_batch(index.h, C.byref(b), out, cap, _p(offs, C.c_uint64), _p(cnt, C.c_uint32)))
+    arr = np.ctypeslib.as_array(out).view(np.dtype([("hash", "<u8"), ("hash_revcomp", "<u8"), ("start", "<u4"),
+                                                     ("end", "<u4")]))
+    return [(arr[offs[2 * r]:offs[2 * r] + cnt[2 * r]].copy(), arr[offs[2 * r + 1]:offs[2 * r + 1] + cnt[2 * r + 1]].copy())
+            for r in range(n)]
+
+
+NAM_DTYPE = np.dtype([("nam_id", "<u4"), ("ref_id", "<u4"), ("ref_start", "<u4"), ("ref_end", "<u4"),
+                      ("query_start", "<u4"), ("query_end", "<u4"), ("matching_bases", "<u4"),
+                      ("n_anchors", "<u4"), ("score", "<f4"), ("is_revcomp", "<u4")])
+DETAILS_DTYPE = np.dtype([(n, "<u4") for n in ("full_not_found", "full_filtered", "full_found", "partial_not_found",
+                                               "partial_filtered", "partial_found", "rescued", "n_randstrobes",
+                                               "n_anchors", "n_nams", "both_orientations")])
+
+
+def nams_batch(index: StrobemerIndex, reads: Reads, chaining: L.ChainingParams | None = None,
+               mapping: L.MappingParams | None = None):
+    """get_nams_by_chaining for each read: NAM arrays sorted by score (stable), and details."""
+    n = len(reads)
+    cap = max(1, int(reads.seq_offsets[-1]) * 4)
+    out = np.zeros(cap, dtype=NAM_DTYPE)
+    offs = np.zeros(n, dtype=np.uint64)
+    cnt = np.zeros(n, dtype=np.uint32)
+    det = np.zeros(n, dtype=DETAILS_DTYPE)
+    b = reads.c()
+    cpar = chaining or chaining_defaults()
+    mpar = mapping or mapping_defaults()
+    L.check(lib().sa_nams_batch(index.h, C.byref(cpar), C.byref(mpar), C.byref(b),
+                                out.ctypes.data_as(C.POINTER(L.Nam)), cap, _p(offs, C.c_uint64), _p(cnt, C.c_uint32),
+                                det.ctypes.data_as(C.POINTER(L.NamDetails))))
+    return [out[offs[r]:offs[r] + cnt[r]].copy() for r in range(n)], det
+
+
+ALN_DTYPE = np.dtype([("valid", "<i4"), ("score", "<u4"), ("query_start", "<u4"), ("query_end", "<u4"),
+                      ("ref_start", "<u4"), ("ref_end", "<u4"), ("edit_distance", "<u4"), ("cigar_offset", "<u4"),
+                      ("cigar_len", "<u4")])
+CIGAR_OPS = "MIDNSHP=X"
+
+
+def cigar_str(ops) -> str:
+    return "".join(f"{int(v) >> 4}{CIGAR_OPS[int(v) & 15]}" for v in ops)
+
+
+def align_batch(queries, refs, mapping: L.MappingParams | None = None):
+    """Aligner::align (SSW + end bonus) for (query, reference) pairs.  Returns a list of
+    dicts, or None where the reference returns None."""
+    bq = [q.encode() if isinstance(q, str) else bytes(q) for q in queries]
+    br = [r.encode() if isinstance(r, str) else bytes(r) for r in refs]
+    n = len(bq)
+    qo = np.zeros(n + 1, dtype=np.uint64)
+    qo[1:] = np.cumsum([len(x) for x in bq])
+    ro = np.zeros(n + 1, dtype=np.uint64)
+    ro[1:] = np.cumsum([len(x) for x in br])
+    out = np.zeros(max(n, 1), dtype=ALN_DTYPE)
+    cap = int(qo[-1] * 2 + ro[-1] + 4 * n + 8)
+    cig = np.zeros(cap, dtype=np.uint32)
+    Q, R = b"".join(bq), b"".join(br)
+    m = mapping or mapping_defaults()
+    L.check(lib().sa_align_batch(C.byref(m), n, C.c_char_p(Q), _p(qo, C.c_uint64), C.c_char_p(R),
+                                 _p(ro, C.c_uint64), out.ctypes.data_as(C.POINTER(L.AlignmentC)),
+                                 _p(cig, C.c_uint32), cap))
+    res = []
+    for i in range(n):
+        a = out[i]
+        if not a["valid"]:
+            res.append(None)
+            continue
+        ops = cig[a["cigar_offset"]:a["cigar_offset"] + a["cigar_len"]]
+        res.append(dict(score=int(a["score"]), query_start=int(a["query_start"]), query_end=int(a["query_end"]),
+                        ref_start=int(a["ref_start"]), ref_end=int(a["ref_end"]),
+                        edit_distance=int(a["edit_distance"]), cigar=cigar_str(ops)))
+    return res
+
+
+class Mapper:
+    """Maps batches of reads; keeps the index and its device arenas resident."""
+
+    def __init__(self, index: StrobemerIndex, refs: References, chaining: L.ChainingParams | None = None,
+                 mapping: L.MappingParams | None = None, **kw):
+        self.index, self.refs = index, refs
+        self.cp = chaining or chaining_defaults()
+        self.mp = mapping or mapping_defaults(**kw)
+        h = C.c_void_p()
+        L.check(lib().sa_mapper_create(index.h, refs.h, C.byref(self.cp), C.byref(self.mp), C.byref(h)))
+        self.h = h
+        self.last = None
+
+    def map(self, r1: Reads, r2: Reads | None = None) -> bytes:
+        o = L.Output()
+        b1 = r1.c()
+        b2 = r2.c() if r2 is not None else None
+        L.check(lib().sa_map_batch(self.h, C.byref(b1), C.byref(b2) if b2 is not None else None, C.byref(o)))
+        try:
+            data = C.string_at(o.data, o.len) if o.len else b""
+            self.last = dict(n_reads=o.n_reads, n_mapped=o.n_mapped, n_waves=o.n_waves,
+                             n_gpu_launches=o.n_gpu_launches)
+            return data
+        finally:
+            lib().sa_output_free(C.byref(o))
+
+    def abundances(self) -> np.ndarray:
+        n = len(self.refs)
+        out = np.zeros(n, dtype=np.float64)
+        L.check(lib().sa_mapper_abundances(self.h, _p(out, C.c_double), n))
+        return out
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().sa_mapper_free(self.h)
+            self.h = C.c_void_p()
+
+
+def sam_header(refs: References, cmd_line: str | None = None, rg_id: str | None = None,
+               rg_fields: list[str] = ()) -> bytes:
+    o = L.Output()
+    f = [x.encode() for x in rg_fields]
+    arr = (C.c_char_p * max(1, len(f)))(*f)
+    L.check(lib().sa_sam_header(refs.h, cmd_line.encode() if cmd_line else None, rg_id.encode() if rg_id else None,
+                                arr, len(f), C.byref(o)))
+    try:
+        return C.string_at(o.data, o.len)
+    finally:
+        lib().sa_output_free(C.byref(o))

@@ -1,0 +1,71 @@
+// Extension pipeline (extend.cu): extend_seed / rescue_align / Aligner::align for a
+// list of jobs.
+#pragma once
+#include "pipeline.h"
+
+namespace sa {
+
+struct AlignScores {
+    uint8_t match, mismatch, gap_open, gap_extend;
+    uint32_t end_bonus;
+};
+
+// Per-job device-side description of the work (filled by the prepare kernel).
+struct PrepRec {
+    uint32_t type;        // 0 none, 1 hamming, 2 ssw
+    uint32_t read;
+    uint32_t rc;          // query is the read's reverse complement
+    uint32_t qlen;
+    uint32_t ref_id;
+    uint32_t wstart, wlen;  // reference window (contig coordinates)
+    uint64_t arena_off;   // query bytes then window bytes
+    uint64_t cigar_off;   // first op of this job's CIGAR
+    uint64_t h_off;       // banded-DP scratch (ints)
+    uint32_t cigar_cap;
+    uint32_t pad_;
+};
+
+// SSW task state (ext/ssw/ssw.c:818-922 results).
+struct SswTask {
+    uint32_t job;
+    int32_t score1;
+    int32_t ref_end1, read_end1;
+    int32_t ref_begin1, read_begin1;
+    int32_t word;
+    int32_t flag;
+    int32_t band_width;
+    uint32_t raw_len;
+    uint64_t dir_off;
+    uint64_t raw_off;
+};
+
+struct ExtWorkspace {
+    DevBuf<ExtJob> jobs;
+    DevBuf<ExtResult> results;
+    DevBuf<PrepRec> prep;
+    DevBuf<uint64_t> sizes;     // 3 per job: arena bytes, cigar ops, h ints
+    DevBuf<uint64_t> offs;      // 3 per job (+3)
+    DevBuf<uint8_t> arena;
+    DevBuf<uint32_t> cigar;
+    DevBuf<int32_t> hscratch;
+    DevBuf<SswTask> tasks;
+    DevBuf<uint32_t> counters;  // [0] n_tasks [1] n_word [2] n_rev_byte [3] n_rev_word
+    DevBuf<uint32_t> list_word, list_rev_byte, list_rev_word;
+    DevBuf<uint64_t> dir_size, dir_off;
+    DevBuf<uint8_t> dir;
+    DevBuf<uint64_t> raw_size, raw_off;
+    DevBuf<uint32_t> raw;
+    DevBuf<uint8_t> cub_tmp;
+    // host mirrors
+    std::vector<ExtResult> h_results;
+    std::vector<uint32_t> h_cigar;
+    uint64_t total_cigar = 0;
+};
+
+// Runs jobs (already in ws.jobs, n of them) against the reads in nws.seq/nws.off.
+// Results and CIGARs are copied back into ws.h_results / ws.h_cigar.  Returns the
+// number of kernel launches.
+uint32_t run_extension(const DevRefs& refs, const NamWorkspace& nws, uint32_t k, const AlignScores& sc, uint32_t n,
+                       ExtWorkspace& ws, uint32_t max_qlen, cudaStream_t st);
+
+}  // namespace sa

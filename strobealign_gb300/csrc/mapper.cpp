@@ -1,0 +1,229 @@
+// Batch driver: Mapper::map_chunk (src/main.rs:873-988) for a whole batch on one
+// GPU.  NAMs for every read come from one pass of the device pipeline; the
+// sequential per-chunk policy then consumes extension results produced in waves:
+// wave 0 extends each read's best NAMs speculatively, and every later wave runs
+// exactly the jobs that chunks stopped on (plus their likely successors).
+#include <chrono>
+#include <cstring>
+
+#include "mapper.h"
+
+namespace sa {
+
+Mapper::Mapper(const sa_index* idx, const sa_refs* refs, const sa_chaining_params& cp, const sa_mapping_params& mp)
+    : idx_(idx), refs_(refs), cp_(cp), mp_(mp) {
+    if (mp.rg_id) rg_id_ = mp.rg_id;
+    SA_CUDA(cudaSetDevice(idx->device));
+    SA_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    const auto& cs = refs->contigs;
+    const uint32_t nc = (uint32_t)cs.size();
+    std::vector<uint64_t> woff(nc);
+    std::vector<uint32_t> clen(nc);
+    uint64_t nw = 0;
+    for (uint32_t c = 0; c < nc; c++) {
+        woff[c] = nw;
+        nw += cs[c].words.size() + 1;
+        clen[c] = (uint32_t)cs[c].len;
+        max_contig_len_ = std::max<uint32_t>(max_contig_len_, clen[c]);
+        contigs_.push_back(ContigInfo{&cs[c].name, cs[c].len});
+    }
+    std::vector<uint64_t> hw(nw, 0);
+    for (uint32_t c = 0; c < nc; c++) std::copy(cs[c].words.begin(), cs[c].words.end(), hw.begin() + woff[c]);
+    d_words_.reserve(nw);
+    d_woff_.reserve(nc);
+    d_clen_.reserve(nc);
+    SA_CUDA(cudaMemcpy(d_words_.p, hw.data(), nw * 8, cudaMemcpyHostToDevice));
+    SA_CUDA(cudaMemcpy(d_woff_.p, woff.data(), nc * 8, cudaMemcpyHostToDevice));
+    SA_CUDA(cudaMemcpy(d_clen_.p, clen.data(), nc * 4, cudaMemcpyHostToDevice));
+    refs_view_ = DevRefs{d_words_.p, d_woff_.p, d_clen_.p, nc};
+    abundances_.assign(nc, 0.0);
+    pcfg_.mp = mp_;
+    pcfg_.rg_id = rg_id_;
+    pcfg_.has_rg = mp.rg_id != nullptr;
+    pcfg_.k = idx->sp.k;
+    if (!mp_.use_ssw && mp_.mode == SA_MODE_SAM) {
+        // single-end piecewise extension (block-aligner) has no device implementation; paired-end
+        // extension always uses SSW in the reference (src/mapper.rs:860-870)
+        single_end_piecewise_ = true;
+    }
+}
+
+Mapper::~Mapper() {
+    if (st_) cudaStreamDestroy(st_);
+}
+
+void Mapper::upload_reads(const std::vector<ReadView>& reads) {
+    uint64_t total = 0;
+    for (auto& r : reads) {
+        if (r.len > MAX_READ_LEN)
+            throw Error(SA_ERR_INVALID, "read longer than " + std::to_string(MAX_READ_LEN) + " nt");
+        total += r.len;
+    }
+    const uint32_t n = (uint32_t)reads.size();
+    h_seq_.reserve(total + 16);
+    h_off_.reserve((size_t)n + 1);
+    uint64_t o = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        h_off_.p[i] = o;
+        std::memcpy(h_seq_.p + o, reads[i].seq, reads[i].len);
+        o += reads[i].len;
+    }
+    h_off_.p[n] = o;
+    nws_.seq.reserve(total + 16);
+    nws_.off.reserve((size_t)n + 1);
+    SA_CUDA(cudaMemcpyAsync(nws_.seq.p, h_seq_.p, total, cudaMemcpyHostToDevice, st_));
+    SA_CUDA(cudaMemcpyAsync(nws_.off.p, h_off_.p, ((size_t)n + 1) * 8, cudaMemcpyHostToDevice, st_));
+    total_bases_ = total;
+    n_reads_ = n;
+    h2d_bytes_ += total + ((size_t)n + 1) * 8;
+}
+
+void Mapper::nams_for_reads(uint32_t& launches) {
+    NamConfig cfg;
+    cfg.cp = ChainParams{cp_.max_lookback, cp_.diag_diff_penalty, cp_.gap_length_penalty, cp_.valid_score_threshold,
+                         cp_.max_ref_gap, cp_.matches_weight, cp_.max_diagonal_ratio};
+    cfg.mcs = mp_.mcs_strategy;
+    cfg.rescue_distance = mp_.rescue_distance;
+    launches += run_nam_pipeline(idx_->view(), refs_view_, cfg, n_reads_, total_bases_, max_contig_len_,
+                                 (uint32_t)refs_->contigs.size(), nws_, st_);
+    const uint64_t tn = nws_.last_total_nams;
+    h_nam_off_.resize((size_t)n_reads_ + 1);
+    h_nams_.resize(tn);
+    h_details_.resize(n_reads_);
+    SA_CUDA(cudaMemcpyAsync(h_nam_off_.data(), nws_.nam_off.p, ((size_t)n_reads_ + 1) * 8, cudaMemcpyDeviceToHost, st_));
+    if (tn) SA_CUDA(cudaMemcpyAsync(h_nams_.data(), nws_.nams.p, tn * sizeof(NamRec), cudaMemcpyDeviceToHost, st_));
+    SA_CUDA(cudaMemcpyAsync(h_details_.data(), nws_.details.p, (size_t)n_reads_ * sizeof(NamDetailsRec),
+                            cudaMemcpyDeviceToHost, st_));
+    SA_CUDA(cudaStreamSynchronize(st_));
+    d2h_bytes_ += ((size_t)n_reads_ + 1) * 8 + tn * sizeof(NamRec) + (size_t)n_reads_ * sizeof(NamDetailsRec);
+}
+
+uint32_t Mapper::run_wave(ResultStore& store, uint32_t max_qlen) {
+    const uint32_t nj = (uint32_t)store.pending.size();
+    if (!nj) return 0;
+    ews_.jobs.reserve(nj);
+    SA_CUDA(cudaMemcpyAsync(ews_.jobs.p, store.pending.data(), (size_t)nj * sizeof(ExtJob), cudaMemcpyHostToDevice,
+                            st_));
+    h2d_bytes_ += (size_t)nj * sizeof(ExtJob);
+    AlignScores sc{mp_.match, mp_.mismatch, mp_.gap_open, mp_.gap_extend, mp_.end_bonus};
+    uint32_t launches = run_extension(refs_view_, nws_, idx_->sp.k, sc, nj, ews_, max_qlen, st_);
+    d2h_bytes_ += (size_t)nj * sizeof(ExtResult) + ews_.total_cigar * 4;
+    const uint32_t base_res = (uint32_t)store.results.size();
+    const uint64_t base_cig = store.cigar.size();
+    store.cigar.insert(store.cigar.end(), ews_.h_cigar.begin(), ews_.h_cigar.end());
+    for (uint32_t j = 0; j < nj; j++) {
+        ExtResult r = ews_.h_results[j];
+        r.cigar_offset = (uint32_t)(base_cig + r.cigar_offset);
+        store.results.push_back(r);
+        const ExtJob& jb = store.pending[j];
+        store.per_read[jb.read][jb.tag].result = base_res + j;
+    }
+    store.pending.clear();
+    jobs_run_ += nj;
+    return launches;
+}
+
+void Mapper::map(const sa_read_batch* r1, const sa_read_batch* r2, sa_output* out) {
+    if (single_end_piecewise_ && !r2)
+        throw Error(SA_ERR_INVALID,
+                    "single-end SAM output needs use_ssw=1: the piecewise (block-aligner) extension is not "
+                    "implemented on the GPU");
+    auto t0 = std::chrono::steady_clock::now();
+    const bool paired = r2 != nullptr;
+    if (paired && r2->n != r1->n) throw Error(SA_ERR_INVALID, "r1 and r2 batches differ in size");
+    const uint64_t nrec = r1->n;
+    BatchView bv;
+    bv.paired = paired;
+    bv.reads.resize(paired ? 2 * nrec : nrec);
+    auto view = [](const sa_read_batch* b, uint64_t i) {
+        ReadView v;
+        v.seq = b->seq + b->seq_offsets[i];
+        v.len = (uint32_t)(b->seq_offsets[i + 1] - b->seq_offsets[i]);
+        v.qual = b->qual ? b->qual + b->seq_offsets[i] : nullptr;
+        v.name = b->names + b->name_offsets[i];
+        v.name_len = (uint32_t)(b->name_offsets[i + 1] - b->name_offsets[i]);
+        v.comment = nullptr;
+        v.comment_len = 0;
+        if (b->comments && b->comment_offsets && b->comment_offsets[i + 1] > b->comment_offsets[i]) {
+            v.comment = b->comments + b->comment_offsets[i];
+            v.comment_len = (uint32_t)(b->comment_offsets[i + 1] - b->comment_offsets[i]);
+        }
+        return v;
+    };
+    uint32_t max_qlen = 1;
+    for (uint64_t i = 0; i < nrec; i++) {
+        if (paired) {
+            bv.reads[2 * i] = view(r1, i);
+            bv.reads[2 * i + 1] = view(r2, i);
+        } else {
+            bv.reads[i] = view(r1, i);
+        }
+    }
+    for (auto& r : bv.reads) max_qlen = std::max(max_qlen, r.len);
+    uint32_t launches = 0;
+    h2d_bytes_ = d2h_bytes_ = 0;
+    jobs_run_ = 0;
+    upload_reads(bv.reads);
+    nams_for_reads(launches);
+    bv.nams = h_nams_.data();
+    bv.nam_off = h_nam_off_.data();
+    bv.details = h_details_.data();
+    // chunks (src/main.rs:591-604)
+    std::vector<ChunkState> chunks;
+    for (uint64_t i = 0; i < nrec;) {
+        uint64_t nt = 0, j = i;
+        while (j < nrec) {
+            nt += bv.reads[paired ? 2 * j : j].len + (paired ? bv.reads[2 * j + 1].len : 0);
+            j++;
+            if (nt > mp_.chunk_size) break;
+        }
+        ChunkState cs;
+        cs.first = cs.next = i;
+        cs.end = j;
+        chunks.push_back(std::move(cs));
+        i = j;
+    }
+    ResultStore store;
+    store.per_read.resize(bv.reads.size());
+    Policy policy(pcfg_, contigs_, bv, store, &abundances_);
+    policy.seed_requests(0, nrec);
+    uint32_t waves = 0;
+    for (;;) {
+        if (!store.pending.empty()) {
+            launches += run_wave(store, max_qlen);
+            waves++;
+        }
+        bool all_done = true;
+        for (auto& c : chunks)
+            if (!c.done) {
+                policy.run_chunk(c);
+                all_done = all_done && c.done;
+            }
+        if (all_done) break;
+        if (store.pending.empty()) throw Error(SA_ERR_INVALID, "internal: chunk stalled without a pending request");
+    }
+    size_t total_len = 0;
+    uint64_t mapped = 0;
+    for (auto& c : chunks) {
+        total_len += c.out.size();
+        mapped += c.mapped;
+    }
+    out->data = (char*)std::malloc(total_len + 1);
+    if (!out->data) throw Error(SA_ERR_OOM, "output allocation failed");
+    size_t o = 0;
+    for (auto& c : chunks) {
+        std::memcpy(out->data + o, c.out.data(), c.out.size());
+        o += c.out.size();
+    }
+    out->data[total_len] = 0;
+    out->len = total_len;
+    out->n_reads = bv.reads.size();
+    out->n_mapped = mapped;
+    out->n_waves = waves;
+    out->n_gpu_launches = launches;
+    last_launches_ = launches;
+    last_waves_ = waves;
+    last_seconds_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace sa

@@ -1,0 +1,66 @@
+// Batch driver state behind sa_mapper.
+#pragma once
+#include "policy.h"
+
+namespace sa {
+
+class Mapper {
+  public:
+    Mapper(const sa_index* idx, const sa_refs* refs, const sa_chaining_params& cp, const sa_mapping_params& mp);
+    ~Mapper();
+    void map(const sa_read_batch* r1, const sa_read_batch* r2, sa_output* out);
+    const std::vector<double>& abundances() const { return abundances_; }
+    const DevRefs& refs_view() const { return refs_view_; }
+    NamWorkspace& nam_ws() { return nws_; }
+    ExtWorkspace& ext_ws() { return ews_; }
+    cudaStream_t stream() const { return st_; }
+    void upload_reads(const std::vector<ReadView>& reads);
+    void nams_for_reads(uint32_t& launches);
+    uint32_t n_reads() const { return n_reads_; }
+    uint64_t total_bases() const { return total_bases_; }
+    const std::vector<NamRec>& host_nams() const { return h_nams_; }
+    const std::vector<uint64_t>& host_nam_off() const { return h_nam_off_; }
+    const std::vector<NamDetailsRec>& host_details() const { return h_details_; }
+    uint64_t h2d_bytes() const { return h2d_bytes_; }
+    uint64_t d2h_bytes() const { return d2h_bytes_; }
+    uint32_t last_launches() const { return last_launches_; }
+    uint32_t last_waves() const { return last_waves_; }
+    uint64_t jobs_run() const { return jobs_run_; }
+
+  private:
+    uint32_t run_wave(ResultStore& store, uint32_t max_qlen);
+
+    const sa_index* idx_;
+    const sa_refs* refs_;
+    sa_chaining_params cp_;
+    sa_mapping_params mp_;
+    std::string rg_id_;
+    PolicyConfig pcfg_;
+    cudaStream_t st_ = nullptr;
+    DevBuf<uint64_t> d_words_, d_woff_;
+    DevBuf<uint32_t> d_clen_;
+    DevRefs refs_view_{};
+    uint32_t max_contig_len_ = 0;
+    std::vector<ContigInfo> contigs_;
+    std::vector<double> abundances_;
+    bool single_end_piecewise_ = false;
+    NamWorkspace nws_;
+    ExtWorkspace ews_;
+    PinnedBuf<uint8_t> h_seq_;
+    PinnedBuf<uint64_t> h_off_;
+    std::vector<uint64_t> h_nam_off_;
+    std::vector<NamRec> h_nams_;
+    std::vector<NamDetailsRec> h_details_;
+    uint32_t n_reads_ = 0;
+    uint64_t total_bases_ = 0;
+    uint64_t h2d_bytes_ = 0, d2h_bytes_ = 0;
+    uint32_t last_launches_ = 0, last_waves_ = 0;
+    uint64_t jobs_run_ = 0;
+    double last_seconds_ = 0;
+};
+
+}  // namespace sa
+
+struct sa_mapper {
+    sa::Mapper* m;
+};

@@ -1,0 +1,862 @@
+// NAM finding on the GPU: the reference's get_nams_by_chaining (src/nam.rs:138-166)
+// for a whole batch of reads, one launch per stage:
+//
+//   k_seed          warp per read: canonical syncmers + forward / reverse-complement
+//                   randstrobes (src/seeding/{syncmers,strobes,mod}.rs)
+//   k_hits          warp per read: index probes with the repeat filter, global and
+//                   local rescue, orientation choice (src/hit.rs, src/chainer.rs:205-216)
+//   k_anchors       warp per read: anchor count, then fill (src/chainer.rs:304-384)
+//   segmented sort  (ref_id, ref_start, query_start) packed in a u64 key
+//   k_chain         warp per read-orientation: dedup, collinear chaining DP with the
+//                   reference's early-break rules evaluated as a warp prefix-max, chain
+//                   extraction (src/chainer.rs:85-180, 386-449)
+//   k_nam_compact   warp per read: NAM ids in push order, stable sort by score
+//                   (src/nam.rs:168-170)
+//
+// Floating point follows the reference exactly: f32 with explicit round-to-nearest
+// intrinsics (no contraction) and log2(d + 1) from a table built with the host's
+// log2f, the function the reference calls.
+#include <cub/cub.cuh>
+
+#include <cmath>
+
+#include "index_device.cuh"
+#include "pipeline.h"
+
+namespace sa {
+
+namespace {
+
+constexpr uint32_t FULL = 0xffffffffu;
+constexpr int WARPS_PER_BLOCK = 8;
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
+__device__ __forceinline__ uint32_t lanemask_lt() { return (1u << lane_id()) - 1; }
+
+__device__ __forceinline__ uint8_t nt_code(uint8_t c) {
+    switch (c) {
+        case 'A': case 'a': return 0;
+        case 'C': case 'c': return 1;
+        case 'G': case 'g': return 2;
+        case 'T': case 't': case 'U': case 'u': return 3;
+        default: return 4;
+    }
+}
+
+// ------------------------------------------------------------------ seeding
+// src/seeding/syncmers.rs:171-237: a syncmer at p requires an N-free k-mer window
+// and the (t-1)-th of its k-s+1 s-mer hashes to equal their minimum.
+__global__ void __launch_bounds__(256) k_seed(const uint8_t* __restrict__ seq, const uint64_t* __restrict__ off,
+                                              uint32_t n, SeedParams p, uint64_t* syn_hash, uint32_t* syn_pos,
+                                              uint64_t* qr_hash, uint64_t* qr_hash_rc, uint32_t* qr_start,
+                                              uint32_t* qr_end, uint64_t total, uint32_t* n_rs) {
+    extern __shared__ uint8_t smem[];
+    uint8_t* codes = smem + (threadIdx.x / 32) * MAX_READ_LEN;
+    const uint32_t lane = lane_id();
+    const uint32_t span = p.k - p.s, step = 32 - span;
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t r = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; r < n; r += nwarps) {
+        const uint64_t o = off[r];
+        const uint32_t L = (uint32_t)(off[r + 1] - o);
+        for (uint32_t i = lane; i < L; i += 32) codes[i] = nt_code(seq[o + i]);
+        __syncwarp();
+        uint32_t nsyn = 0;
+        for (uint32_t c = 0; L >= p.k && c + p.k <= L; c += step) {
+            const uint32_t q = c + lane;
+            bool v = q + p.s <= L;
+            uint64_t fw = 0, rc = 0;
+            if (v) {
+                for (uint32_t b = 0; b < p.s; b++) {
+                    uint32_t cc = codes[q + b];
+                    if (cc > 3) { v = false; break; }
+                    fw = (fw << 2) | cc;
+                    rc |= (uint64_t)(3 - cc) << (2 * b);
+                }
+            }
+            uint64_t hs = v ? xxh64_u64(fw < rc ? fw : rc) : 0;
+            bool ok = true;
+            uint64_t mn = UINT64_MAX, ht = 0;
+            for (uint32_t d = 0; d <= span; d++) {
+                uint64_t h = __shfl_down_sync(FULL, hs, d);
+                bool vv = __shfl_down_sync(FULL, v, d);
+                ok = ok && vv;
+                mn = h < mn ? h : mn;
+                if (d == p.t - 1) ht = h;
+            }
+            const uint32_t pos = c + lane;
+            bool is_syn = lane < step && pos + p.k <= L && ok && ht == mn;
+            uint64_t kh = 0;
+            uint32_t fwd = 0;
+            if (is_syn) {
+                uint64_t kf = 0, kr = 0;
+                for (uint32_t b = 0; b < p.k; b++) {
+                    uint32_t cc = codes[pos + b];
+                    kf = (kf << 2) | cc;
+                    kr |= (uint64_t)(3 - cc) << (2 * b);
+                }
+                kh = xxh64_u64(kf < kr ? kf : kr);
+                fwd = kf <= kr;
+            }
+            uint32_t bal = __ballot_sync(FULL, is_syn);
+            if (is_syn) {
+                uint32_t idx = nsyn + __popc(bal & lanemask_lt());
+                syn_hash[o + idx] = kh;
+                syn_pos[o + idx] = (pos << 1) | fwd;
+            }
+            nsyn += __popc(bal);
+        }
+        __syncwarp();
+        const uint32_t nr = L < p.w_max ? 0 : nsyn;
+        // forward randstrobes (src/seeding/strobes.rs:145-176)
+        for (uint32_t i = lane; i < nr; i += 32) {
+            uint64_t h1 = syn_hash[o + i];
+            uint32_t p1 = syn_pos[o + i];
+            uint32_t pos1 = p1 >> 1;
+            uint64_t best = UINT64_MAX;
+            uint64_t h2 = h1;
+            uint32_t p2 = p1;
+            for (uint32_t j = i + p.w_min; j <= i + p.w_max && j < nsyn; j++) {
+                uint32_t pj = syn_pos[o + j];
+                if ((pj >> 1) > pos1 + p.max_dist) break;
+                uint64_t hj = syn_hash[o + j];
+                uint64_t ones = (uint64_t)__popcll((h1 ^ hj) & p.q);
+                if (ones < best) { best = ones; h2 = hj; p2 = pj; }
+            }
+            uint64_t f1 = p1 & 1, f2 = p2 & 1;
+            qr_hash[o + i] = randstrobe_hash(h1, h2, f1, f2, p);
+            qr_hash_rc[o + i] = randstrobe_hash(h2, h1, f1 ^ 1, f2 ^ 1, p);
+            qr_start[o + i] = pos1;
+            qr_end[o + i] = (p2 >> 1) + p.k;
+        }
+        // reverse-complement randstrobes from the reversed syncmer list (src/seeding/mod.rs:53-73)
+        for (uint32_t ir = lane; ir < nr; ir += 32) {
+            uint32_t i = nsyn - 1 - ir;
+            uint64_t h1 = syn_hash[o + i];
+            uint32_t p1 = syn_pos[o + i];
+            uint32_t pos1 = L - (p1 >> 1) - p.k;
+            uint32_t f1 = (p1 & 1) ^ 1;
+            uint64_t best = UINT64_MAX;
+            uint64_t h2 = h1;
+            uint32_t pos2 = pos1, f2 = f1;
+            for (uint32_t d = p.w_min; d <= p.w_max && d <= i; d++) {
+                uint32_t j = i - d;
+                uint32_t pj = syn_pos[o + j];
+                uint32_t posj = L - (pj >> 1) - p.k;
+                if (posj > pos1 + p.max_dist) break;
+                uint64_t hj = syn_hash[o + j];
+                uint64_t ones = (uint64_t)__popcll((h1 ^ hj) & p.q);
+                if (ones < best) { best = ones; h2 = hj; pos2 = posj; f2 = (pj & 1) ^ 1; }
+            }
+            qr_hash[total + o + ir] = randstrobe_hash(h1, h2, f1, f2, p);
+            qr_hash_rc[total + o + ir] = randstrobe_hash(h2, h1, f1 ^ 1, f2 ^ 1, p);
+            qr_start[total + o + ir] = pos1;
+            qr_end[total + o + ir] = pos2 + p.k;
+        }
+        if (lane == 0) {
+            n_rs[2 * r] = nr;
+            n_rs[2 * r + 1] = nr;
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------ hits
+struct HitsCounts {
+    uint32_t fnf, ff, ffound, pnf, pf, pfound, rescued;
+};
+
+__device__ __forceinline__ uint32_t warp_sum(uint32_t v) {
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(FULL, v, d);
+    return v;
+}
+
+// count used by rescue_least_frequent (src/hit.rs:96-107), cached per hit
+__device__ __forceinline__ uint32_t hit_count(const DevIndex& ix, uint64_t pos, uint32_t info, uint64_t hash_rc) {
+    if (info & 2) return idx_get_count(ix, pos, ix.p.main_mask);
+    return idx_count_full(ix, pos, hash_rc);
+}
+
+// rescue_least_frequent (src/hit.rs:88-125) over hits [s, e) of one read-orientation.
+// Whole warp participates; returns the number rescued (valid in all lanes).
+__device__ uint32_t warp_rescue_least_frequent(const DevIndex& ix, uint32_t s, uint32_t e, uint32_t to_rescue,
+                                               uint32_t threshold, const uint64_t* hit_pos, uint32_t* hit_info,
+                                               uint32_t* cache, const uint64_t* rs_hash_rc) {
+    for (uint32_t h = s + lane_id(); h < e; h += 32) {
+        if (cache[h] == 0xffffffffu) {
+            uint32_t info = hit_info[h];
+            cache[h] = hit_count(ix, hit_pos[h], info, rs_hash_rc[info >> 3]);
+        }
+    }
+    __syncwarp();
+    uint32_t rescued = 0;
+    if (lane_id() == 0) {
+        // stable ascending sort by count == pick (count, index) in lexicographic order
+        uint32_t pc = 0, pi = 0;
+        bool have_prev = false;
+        for (uint32_t t = 0; t < to_rescue; t++) {
+            uint32_t bc = 0xffffffffu, bi = 0xffffffffu;
+            for (uint32_t h = s; h < e; h++) {
+                uint32_t c = cache[h];
+                if (c > threshold) continue;
+                if (have_prev && (c < pc || (c == pc && h <= pi))) continue;
+                if (c < bc || (c == bc && h < bi)) { bc = c; bi = h; }
+            }
+            if (bi == 0xffffffffu) break;
+            uint32_t info = hit_info[bi];
+            rescued += (info >> 2) & 1;
+            hit_info[bi] = info & ~4u;
+            pc = bc;
+            pi = bi;
+            have_prev = true;
+        }
+    }
+    __syncwarp();
+    return __shfl_sync(FULL, rescued, 0);
+}
+
+// find_hits (src/hit.rs:129-333) for both orientations of each read, then the
+// orientation heuristic (src/chainer.rs:205-216, src/hit.rs:76-81).
+__global__ void __launch_bounds__(256) k_hits(DevIndex ix, const uint64_t* __restrict__ off, uint32_t n,
+                                              uint64_t total, uint32_t mcs, uint32_t rescue_distance,
+                                              const uint64_t* qr_hash, const uint64_t* qr_hash_rc,
+                                              const uint32_t* qr_start, const uint32_t* qr_end,
+                                              const uint32_t* n_rs, uint64_t* hit_pos, uint32_t* hit_info,
+                                              uint32_t* cache, uint32_t* n_hits, uint8_t* orient,
+                                              NamDetailsRec* details) {
+    const uint32_t lane = lane_id();
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
+    const uint32_t cutoff = ix.filter_cutoff;
+    for (uint32_t r = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; r < n; r += nwarps) {
+        const uint64_t o = off[r];
+        HitsCounts hc[2];
+        for (int ori = 0; ori < 2; ori++) {
+            const uint64_t b = ori * total + o;
+            const uint32_t nr = n_rs[2 * r + ori];
+            uint32_t nh = 0;
+            uint32_t fnf = 0, ff = 0, ffound = 0, pnf = 0, pf = 0, pfound = 0;
+            const bool do_full = mcs != SA_MCS_FIRST_STROBE;
+            // pass 1: full lookups (with partial fallback under MCS always)
+            if (do_full) {
+                for (uint32_t c = 0; c < nr; c += 32) {
+                    uint32_t i = c + lane;
+                    bool is_hit = false, partial = false, filtered = false;
+                    uint64_t pos = UINT64_MAX;
+                    if (i < nr) {
+                        uint64_t h = qr_hash[b + i];
+                        pos = idx_full_forward(ix, h);
+                        if (pos != UINT64_MAX) {
+                            is_hit = true;
+                            filtered = idx_too_frequent(ix, pos, cutoff, qr_hash_rc[b + i]);
+                            if (filtered) ff++;
+                            else ffound++;
+                        } else {
+                            fnf++;
+                            if (mcs == SA_MCS_ALWAYS) {
+                                pos = idx_get_masked_from(ix, h, ix.p.main_mask, false, 0);
+                                if (pos != UINT64_MAX) {
+                                    is_hit = partial = true;
+                                    filtered = idx_too_frequent_partial(ix, pos, cutoff);
+                                    if (filtered) pf++;
+                                    else pfound++;
+                                } else {
+                                    pnf++;
+                                }
+                            }
+                        }
+                    }
+                    uint32_t bal = __ballot_sync(FULL, is_hit);
+                    if (is_hit) {
+                        uint32_t idx = nh + __popc(bal & lanemask_lt());
+                        hit_pos[b + idx] = pos;
+                        hit_info[b + idx] = (i << 3) | (filtered ? 4u : 0u) | (partial ? 2u : 0u) | 1u;
+                        cache[b + idx] = 0xffffffffu;
+                    }
+                    nh += __popc(bal);
+                }
+            }
+            uint32_t full_hits = warp_sum(ff + ffound);
+            bool partial_pass = mcs == SA_MCS_FIRST_STROBE || (mcs == SA_MCS_RESCUE && full_hits == 0);
+            if (partial_pass) {
+                for (uint32_t c = 0; c < nr; c += 32) {
+                    uint32_t i = c + lane;
+                    bool is_hit = false, filtered = false;
+                    uint64_t pos = UINT64_MAX;
+                    if (i < nr) {
+                        pos = idx_get_masked_from(ix, qr_hash[b + i], ix.p.main_mask, false, 0);
+                        if (pos != UINT64_MAX) {
+                            is_hit = true;
+                            filtered = idx_too_frequent_partial(ix, pos, cutoff);
+                            if (filtered) pf++;
+                            else pfound++;
+                        } else {
+                            pnf++;
+                        }
+                    }
+                    uint32_t bal = __ballot_sync(FULL, is_hit);
+                    if (is_hit) {
+                        uint32_t idx = nh + __popc(bal & lanemask_lt());
+                        hit_pos[b + idx] = pos;
+                        hit_info[b + idx] = (i << 3) | (filtered ? 4u : 0u) | 2u | 1u;
+                        cache[b + idx] = 0xffffffffu;
+                    }
+                    nh += __popc(bal);
+                }
+            }
+            __syncwarp();
+            HitsCounts d;
+            d.fnf = warp_sum(fnf);
+            d.ff = warp_sum(ff);
+            d.ffound = warp_sum(ffound);
+            d.pnf = warp_sum(pnf);
+            d.pf = warp_sum(pf);
+            d.pfound = warp_sum(pfound);
+            d.rescued = 0;
+            // rescue (src/hit.rs:270-304)
+            uint32_t total_hits = d.pf + d.pfound + d.ff + d.ffound;
+            uint32_t nonrep = d.ffound + d.pfound;
+            float frac = total_hits > 0 ? __fdiv_rn(__uint2float_rn(nonrep), __uint2float_rn(total_hits)) : 1.0f;
+            if (rescue_distance > 0) {
+                if (frac < 0.7f && nonrep < 5)
+                    d.rescued += warp_rescue_least_frequent(ix, 0, nh, 5, 1000, hit_pos + b, hit_info + b, cache + b,
+                                                            qr_hash_rc + b);
+                // local rescue over filtered stretches (src/hit.rs:232-268); an interval is
+                // processed as soon as it is found, which only touches hits already scanned
+                uint32_t scan = 0, last_unf = 0, first_f = 0;
+                for (;;) {
+                    uint32_t is = 0, ie = 0, tr = 0, found = 0;
+                    if (lane == 0) {
+                        while (scan < nh) {
+                            uint32_t h = scan++;
+                            uint32_t info = hit_info[b + h];
+                            if (info & 4) continue;
+                            uint32_t qs = qr_start[b + (info >> 3)];
+                            bool iv = qs > last_unf + rescue_distance;
+                            if (iv) { is = first_f; ie = h; tr = (qs - last_unf) / rescue_distance; found = 1; }
+                            last_unf = qs;
+                            first_f = h + 1;
+                            if (iv) break;
+                        }
+                        if (!found && scan == nh && nh > 0 && scan != 0xffffffffu) {
+                            uint32_t lq = qr_start[b + (hit_info[b + nh - 1] >> 3)];
+                            uint32_t diff = lq - last_unf;
+                            if (diff > rescue_distance) { is = first_f; ie = nh; tr = diff / rescue_distance; found = 1; }
+                            scan = 0xffffffffu;
+                        }
+                    }
+                    found = __shfl_sync(FULL, found, 0);
+                    if (!found) break;
+                    is = __shfl_sync(FULL, is, 0);
+                    ie = __shfl_sync(FULL, ie, 0);
+                    tr = __shfl_sync(FULL, tr, 0);
+                    d.rescued += warp_rescue_least_frequent(ix, is, ie, tr, 10000, hit_pos + b, hit_info + b,
+                                                            cache + b, qr_hash_rc + b);
+                }
+            }
+            hc[ori] = d;
+            if (lane == 0) n_hits[2 * r + ori] = nh;
+        }
+        if (lane == 0) {
+            uint32_t t0 = hc[0].ffound + hc[0].ff, t1 = hc[1].ffound + hc[1].ff;
+            bool b0 = t0 >= t1 * 2 && t0 > t1 + 5;
+            bool b1 = t1 >= t0 * 2 && t1 > t0 + 5;
+            uint8_t m = b0 ? 1 : b1 ? 2 : 3;
+            orient[r] = m;
+            NamDetailsRec dr;
+            dr.full_not_found = hc[0].fnf + hc[1].fnf;
+            dr.full_filtered = hc[0].ff + hc[1].ff;
+            dr.full_found = hc[0].ffound + hc[1].ffound;
+            dr.partial_not_found = hc[0].pnf + hc[1].pnf;
+            dr.partial_filtered = hc[0].pf + hc[1].pf;
+            dr.partial_found = hc[0].pfound + hc[1].pfound;
+            dr.rescued = hc[0].rescued + hc[1].rescued;
+            dr.n_randstrobes = n_rs[2 * r] + n_rs[2 * r + 1];
+            dr.n_anchors = 0;
+            dr.n_nams = 0;
+            dr.both_orientations = m == 3;
+            details[r] = dr;
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------ anchors
+struct AnchorPack {
+    uint32_t qbits, pbits;
+    __device__ __forceinline__ uint64_t key(uint32_t ref_id, uint32_t ref_start, uint32_t qs) const {
+        return ((uint64_t)ref_id << (pbits + qbits)) | ((uint64_t)ref_start << qbits) | qs;
+    }
+};
+
+// add_to_anchors_full / add_to_anchors_partial (src/chainer.rs:304-366): counts when
+// out == nullptr, otherwise writes the anchors
+__device__ __forceinline__ uint32_t hit_anchors(const DevIndex& ix, uint64_t pos, uint32_t info, uint64_t hash,
+                                                uint32_t qs, uint32_t qe, AnchorPack ap, uint64_t* out) {
+    const uint32_t k = ix.p.k;
+    uint32_t cnt = 0;
+    if (info & 2) {
+        uint64_t e = idx_get_masked_from(ix, hash, ix.p.fwd_main_mask, true, pos);
+        if (e == UINT64_MAX) return 0;
+        uint64_t fh = load_rs(ix.rs, e).hash_offset & ix.p.fwd_main_mask;
+        for (uint64_t i = e; i < ix.n; i++) {
+            RefRandstrobe rr = load_rs(ix.rs, i);
+            if ((rr.hash_offset & ix.p.fwd_main_mask) != fh) break;
+            if (out) out[cnt] = ap.key(rr.ref_index, rr.position, qs);
+            cnt++;
+        }
+    } else {
+        uint64_t fh = load_hash(ix.rs, pos);
+        uint32_t minld = 0xffffffffu;
+        const uint32_t ql = qe - qs;
+        for (uint64_t i = pos; i < ix.n; i++) {
+            RefRandstrobe rr = load_rs(ix.rs, i);
+            if (rs_hash(rr) != fh) break;
+            uint32_t rl = (uint32_t)(rr.hash_offset & 0xff) + k;
+            uint32_t ld = ql > rl ? ql - rl : rl - ql;
+            if (ld <= minld) {
+                if (out) {
+                    out[cnt] = ap.key(rr.ref_index, rr.position, qs);
+                    out[cnt + 1] = ap.key(rr.ref_index, rr.position + rl - k, qe - k);
+                }
+                cnt += 2;
+                minld = ld;
+            }
+        }
+    }
+    return cnt;
+}
+
+__device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, uint32_t& total) {
+    uint32_t x = v;
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t y = __shfl_up_sync(FULL, x, d);
+        if (lane_id() >= (uint32_t)d) x += y;
+    }
+    total = __shfl_sync(FULL, x, 31);
+    return x - v;
+}
+
+template <bool FILL>
+__global__ void __launch_bounds__(256) k_anchors(DevIndex ix, const uint64_t* __restrict__ off, uint32_t n,
+                                                 uint64_t total, const uint64_t* qr_hash, const uint32_t* qr_start,
+                                                 const uint32_t* qr_end, const uint64_t* hit_pos,
+                                                 const uint32_t* hit_info, const uint32_t* n_hits,
+                                                 const uint8_t* orient, uint32_t* hit_anchors_n, uint64_t* seg_count,
+                                                 const uint64_t* seg_off, uint64_t* anchors, AnchorPack ap,
+                                                 NamDetailsRec* details) {
+    const uint32_t lane = lane_id();
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t r = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; r < n; r += nwarps) {
+        const uint64_t o = off[r];
+        const uint8_t m = orient[r];
+        uint32_t read_total = 0;
+        for (int ori = 0; ori < 2; ori++) {
+            const uint64_t b = ori * total + o;
+            const uint32_t nh = (m >> ori) & 1 ? n_hits[2 * r + ori] : 0;
+            uint64_t acc = FILL ? seg_off[2 * r + ori] : 0;
+            uint32_t sum = 0;
+            for (uint32_t c = 0; c < nh; c += 32) {
+                uint32_t h = c + lane;
+                uint32_t cnt = 0;
+                uint32_t info = 0;
+                if (h < nh) {
+                    info = hit_info[b + h];
+                    if (!(info & 4)) {
+                        if (FILL) cnt = hit_anchors_n[b + h];
+                        else {
+                            uint32_t ri = info >> 3;
+                            uint32_t qs = qr_start[b + ri];
+                            uint32_t qe = (info & 2) ? qs + ix.p.k : qr_end[b + ri];
+                            cnt = hit_anchors(ix, hit_pos[b + h], info, qr_hash[b + ri], qs, qe, ap, nullptr);
+                            hit_anchors_n[b + h] = cnt;
+                        }
+                    }
+                }
+                uint32_t tot;
+                uint32_t ex = warp_excl_scan(cnt, tot);
+                if (FILL && cnt) {
+                    uint32_t ri = info >> 3;
+                    uint32_t qs = qr_start[b + ri];
+                    uint32_t qe = (info & 2) ? qs + ix.p.k : qr_end[b + ri];
+                    hit_anchors(ix, hit_pos[b + h], info, qr_hash[b + ri], qs, qe, ap, anchors + acc + ex);
+                }
+                acc += tot;
+                sum += tot;
+            }
+            if (!FILL && lane == 0) seg_count[2 * r + ori] = sum;
+            read_total += sum;
+        }
+        if (!FILL && lane == 0) details[r].n_anchors = read_total;
+    }
+}
+
+// ------------------------------------------------------------------ chaining
+struct ChainCtx {
+    ChainParams cp;
+    uint32_t k;
+    const float* lut;
+};
+
+// compute_score (src/chainer.rs:286-302)
+__device__ __forceinline__ float chain_score(uint32_t dq, uint32_t dr, const ChainCtx& c) {
+    uint32_t dd = dr > dq ? dr - dq : dq - dr;
+    uint32_t dg = dq < dr ? dq : dr;
+    float score = __uint2float_rn(c.k < dg ? c.k : dg);
+    uint32_t dg2 = dg > c.k ? dg - c.k : 0;
+    float lin = __fadd_rn(__fmul_rn(c.cp.diag_diff_penalty, __uint2float_rn(dd)),
+                          __fmul_rn(c.cp.gap_length_penalty, __uint2float_rn(dg2)));
+    float lg = dd >= 1 ? __ldg(c.lut + (dd < LOG2_LUT_SIZE ? dd : LOG2_LUT_SIZE - 1)) : 0.0f;
+    return __fsub_rn(score, __fadd_rn(lin, __fmul_rn(0.5f, lg)));
+}
+
+__global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off, uint32_t n, const uint64_t* seg_off,
+                                               const uint64_t* sorted, uint64_t* dedup, float* dp, uint32_t* pred,
+                                               uint32_t* aux, uint64_t total_anchors, AnchorPack ap, ChainCtx cc,
+                                               NamRec* nam_out, uint32_t* nam_seg_count) {
+    const uint32_t lane = lane_id();
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
+    const uint64_t qmask = (1ULL << ap.qbits) - 1, pmask = (1ULL << ap.pbits) - 1;
+    for (uint32_t sg = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; sg < 2 * n; sg += nwarps) {
+        const uint64_t b = seg_off[sg], e = seg_off[sg + 1];
+        const uint32_t r = sg >> 1;
+        const uint32_t read_len = (uint32_t)(off[r + 1] - off[r]);
+        // dedup (src/chainer.rs:228-229)
+        uint32_t N = 0;
+        for (uint64_t c = b; c < e; c += 32) {
+            uint64_t i = c + lane;
+            bool keep = false;
+            uint64_t key = 0;
+            if (i < e) {
+                key = sorted[i];
+                keep = i == b || sorted[i - 1] != key;
+            }
+            uint32_t bal = __ballot_sync(FULL, keep);
+            if (keep) dedup[b + N + __popc(bal & lanemask_lt())] = key;
+            N += __popc(bal);
+        }
+        __syncwarp();
+        if (N == 0) {
+            if (lane == 0) nam_seg_count[sg] = 0;
+            continue;
+        }
+        const uint32_t max_ref_gap = cc.cp.max_ref_gap ? cc.cp.max_ref_gap : read_len;
+        const float kf = __uint2float_rn(cc.k);
+        float best_score = 0.0f;
+        uint32_t best_index = 0xffffffffu;
+        for (uint32_t i = 0; i < N; i++) {
+            const uint64_t ki = dedup[b + i];
+            const uint32_t ri = (uint32_t)(ki >> (ap.pbits + ap.qbits)), rsi = (uint32_t)((ki >> ap.qbits) & pmask),
+                           qi = (uint32_t)(ki & qmask);
+            const uint32_t lookup_end = i > cc.cp.max_lookback ? i - cc.cp.max_lookback : 0;
+            float cur = kf;  // dp[i] as the reference's downward scan leaves it
+            uint32_t cur_pred = 0xffffffffu;
+            bool stop = false;
+            // candidates j = i-1, i-2, ... in chunks of 32, lane t handles j = i-1-(base+t)
+            for (uint32_t base = 0; !stop && base < i - lookup_end; base += 32) {
+                const uint32_t t = base + lane;
+                bool in = t < i - lookup_end;
+                uint32_t j = i - 1 - t;
+                bool hard = false, valid = false, diag = false;
+                float val = 0.0f;
+                if (in) {
+                    const uint64_t kj = dedup[b + j];
+                    const uint32_t rj = (uint32_t)(kj >> (ap.pbits + ap.qbits)),
+                                   rsj = (uint32_t)((kj >> ap.qbits) & pmask), qj = (uint32_t)(kj & qmask);
+                    if (rj != ri) hard = true;
+                    else if (qi >= qj) {
+                        uint32_t dq = qi - qj, dr = rsi - rsj;
+                        if (dr >= max_ref_gap) hard = true;
+                        else {
+                            uint32_t mx = dq > dr ? dq : dr, mn = dq < dr ? dq : dr;
+                            float ratio = __fdiv_rn(__uint2float_rn(mx), __uint2float_rn(mn));
+                            if (!(ratio > cc.cp.max_diagonal_ratio)) {
+                                valid = true;
+                                diag = dq == dr;
+                                val = __fadd_rn(dp[b + j], chain_score(dq, dr, cc));
+                            }
+                        }
+                    }
+                }
+                uint32_t hb = __ballot_sync(FULL, hard);
+                uint32_t lim = hb ? (uint32_t)(__ffs(hb) - 1) : 32;  // lanes >= lim are not reached
+                if (lane >= lim) valid = false;
+                // exclusive prefix max of val over valid lanes in scan order
+                float x = valid ? val : -INFINITY;
+                float incl = x;
+                for (int d = 1; d < 32; d <<= 1) {
+                    float y = __shfl_up_sync(FULL, incl, d);
+                    if (lane >= (uint32_t)d) incl = fmaxf(incl, y);
+                }
+                float excl = __shfl_up_sync(FULL, incl, 1);
+                if (lane == 0) excl = -INFINITY;
+                float before = fmaxf(cur, excl);
+                bool upd = valid && val >= before;
+                uint32_t ub = __ballot_sync(FULL, upd);
+                uint32_t sb = __ballot_sync(FULL, upd && diag);
+                uint32_t reach = lim;
+                if (sb) {
+                    uint32_t sl = (uint32_t)(__ffs(sb) - 1);
+                    reach = sl + 1;
+                    stop = true;
+                }
+                if (hb) stop = true;
+                uint32_t um = ub & (reach >= 32 ? FULL : ((1u << reach) - 1));
+                if (um) {
+                    uint32_t last = 31 - __clz(um);
+                    float lv = __shfl_sync(FULL, val, last);
+                    cur = lv;
+                    cur_pred = i - 1 - (base + last);
+                }
+            }
+            // re-check of the best chain end (src/chainer.rs:150-165)
+            if (best_index != 0xffffffffu) {
+                const uint64_t kb = dedup[b + best_index];
+                const uint32_t rb = (uint32_t)(kb >> (ap.pbits + ap.qbits)), rsb = (uint32_t)((kb >> ap.qbits) & pmask),
+                               qb = (uint32_t)(kb & qmask);
+                if (rb == ri && qi > qb) {
+                    uint32_t dq = qi - qb, dr = rsi - rsb;
+                    uint32_t mx = dq > dr ? dq : dr, mn = dq < dr ? dq : dr;
+                    float ratio = __fdiv_rn(__uint2float_rn(mx), __uint2float_rn(mn));
+                    if (dr < max_ref_gap && dr > 0 && ratio <= cc.cp.max_diagonal_ratio) {
+                        float ns = __fadd_rn(dp[b + best_index], chain_score(dq, dr, cc));
+                        if (ns > cur) {
+                            cur = ns;
+                            cur_pred = best_index;
+                        }
+                    }
+                }
+            }
+            if (lane == 0) {
+                dp[b + i] = cur;
+                pred[b + i] = cur_pred;
+            }
+            if (cur > best_score) {
+                best_score = cur;
+                best_index = i;
+            }
+            __syncwarp();
+        }
+        // extract_chains (src/chainer.rs:386-449)
+        const float valid_score = __fmul_rn(best_score, cc.cp.valid_score_threshold);
+        uint32_t* cand = aux + b;
+        uint32_t* sorted_c = aux + total_anchors + b;
+        uint32_t* used = aux + 2 * total_anchors + b;
+        uint32_t M = 0;
+        for (uint32_t c = 0; c < N; c += 32) {
+            uint32_t i = c + lane;
+            bool take = i < N && dp[b + i] >= valid_score;
+            uint32_t bal = __ballot_sync(FULL, take);
+            if (take) cand[M + __popc(bal & lanemask_lt())] = i;
+            if (i < N) used[i] = 0;
+            M += __popc(bal);
+        }
+        __syncwarp();
+        for (uint32_t c = lane; c < M; c += 32) {
+            uint32_t ci = cand[c];
+            float s = dp[b + ci];
+            uint32_t rank = 0;
+            for (uint32_t u = 0; u < M; u++) {
+                float su = dp[b + cand[u]];
+                rank += (su > s) || (su == s && u < c);
+            }
+            sorted_c[rank] = ci;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            uint32_t nn = 0;
+            NamRec* outp = nam_out + b;
+            for (uint32_t c = 0; c < M; c++) {
+                uint32_t i = sorted_c[c];
+                if (used[i]) continue;
+                uint32_t j = i;
+                bool overlaps = false;
+                uint32_t nanch = 1;
+                const uint64_t ki = dedup[b + i];
+                uint32_t matching = cc.k;
+                uint32_t cov = (uint32_t)((ki >> ap.qbits) & pmask);
+                while (pred[b + j] != 0xffffffffu) {
+                    j = pred[b + j];
+                    if (used[j]) { overlaps = true; break; }
+                    nanch++;
+                    used[j] = 1;
+                    uint32_t rsj = (uint32_t)((dedup[b + j] >> ap.qbits) & pmask);
+                    uint32_t d = cov > rsj ? cov - rsj : 0;
+                    matching += d < cc.k ? d : cc.k;
+                    cov = rsj;
+                }
+                if (overlaps) continue;
+                const uint64_t kf2 = dedup[b + j];
+                NamRec nr;
+                nr.nam_id = nn;
+                nr.query_start = (uint32_t)(kf2 & qmask);
+                nr.query_end = (uint32_t)(ki & qmask) + cc.k;
+                nr.ref_start = (uint32_t)((kf2 >> ap.qbits) & pmask);
+                nr.ref_end = (uint32_t)((ki >> ap.qbits) & pmask) + cc.k;
+                nr.matching_bases = matching;
+                nr.ref_id = (uint32_t)(ki >> (ap.pbits + ap.qbits));
+                nr.score = __fadd_rn(dp[b + i], __fmul_rn(__uint2float_rn(nanch), cc.cp.matches_weight));
+                nr.is_revcomp = sg & 1;
+                nr.n_anchors = nanch;
+                outp[nn++] = nr;
+            }
+            nam_seg_count[sg] = nn;
+        }
+        __syncwarp();
+    }
+}
+
+// NAM ids in push order (forward chains first), then a stable sort by score,
+// descending (src/nam.rs:168-170; the tie shuffle is applied by the host policy)
+__global__ void __launch_bounds__(256) k_nam_compact(uint32_t n, const uint64_t* seg_off, const NamRec* scratch,
+                                                     const uint32_t* nam_seg_count, const uint64_t* nam_off,
+                                                     NamRec* out, NamDetailsRec* details) {
+    const uint32_t lane = lane_id();
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t r = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; r < n; r += nwarps) {
+        const uint32_t c0 = nam_seg_count[2 * r], c1 = nam_seg_count[2 * r + 1], c = c0 + c1;
+        const NamRec* s0 = scratch + seg_off[2 * r];
+        const NamRec* s1 = scratch + seg_off[2 * r + 1];
+        const uint64_t ob = nam_off[r];
+        for (uint32_t t = lane; t < c; t += 32) {
+            NamRec nr = t < c0 ? s0[t] : s1[t - c0];
+            float s = nr.score;
+            uint32_t rank = 0;
+            for (uint32_t u = 0; u < c; u++) {
+                float su = u < c0 ? s0[u].score : s1[u - c0].score;
+                rank += (su > s) || (su == s && u < t);
+            }
+            nr.nam_id = t;
+            out[ob + rank] = nr;
+        }
+        if (lane == 0) details[r].n_nams = c;
+    }
+}
+
+__global__ void k_nam_counts(uint32_t n, const uint32_t* nam_seg_count, uint64_t* nam_count) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+        nam_count[r] = (uint64_t)nam_seg_count[2 * r] + nam_seg_count[2 * r + 1];
+}
+
+inline unsigned warps_grid(uint64_t items) {
+    uint64_t blocks = (items + WARPS_PER_BLOCK - 1) / WARPS_PER_BLOCK;
+    if (blocks > 152ULL * 32) blocks = 152ULL * 32;
+    return (unsigned)(blocks ? blocks : 1);
+}
+
+uint32_t ceil_log2(uint64_t v) {
+    uint32_t b = 0;
+    while ((1ULL << b) < v) b++;
+    return b;
+}
+
+template <class T>
+void cub_excl_sum(NamWorkspace& ws, const T* in, T* out, uint64_t n, cudaStream_t st) {
+    size_t tmp = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tmp, in, out, (int64_t)n, st);
+    ws.cub_tmp.reserve(tmp);
+    cub::DeviceScan::ExclusiveSum(ws.cub_tmp.p, tmp, in, out, (int64_t)n, st);
+}
+
+}  // namespace
+
+uint32_t run_seeding(const SeedParams& sp, uint32_t n, uint64_t total, NamWorkspace& ws, cudaStream_t st) {
+    ws.syn_hash.reserve(total);
+    ws.syn_pos.reserve(total);
+    ws.qr_hash.reserve(2 * total);
+    ws.qr_hash_rc.reserve(2 * total);
+    ws.qr_start.reserve(2 * total);
+    ws.qr_end.reserve(2 * total);
+    ws.n_rs.reserve(2 * (size_t)n);
+    size_t smem = WARPS_PER_BLOCK * MAX_READ_LEN;
+    k_seed<<<warps_grid(n), 32 * WARPS_PER_BLOCK, smem, st>>>(ws.seq.p, ws.off.p, n, sp, ws.syn_hash.p, ws.syn_pos.p,
+                                                              ws.qr_hash.p, ws.qr_hash_rc.p, ws.qr_start.p,
+                                                              ws.qr_end.p, total, ws.n_rs.p);
+    SA_CUDA(cudaGetLastError());
+    return 1;
+}
+
+uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConfig& cfg, uint32_t n, uint64_t total,
+                          uint32_t max_contig_len, uint32_t n_contigs, NamWorkspace& ws, cudaStream_t st) {
+    (void)refs;
+    uint32_t launches = 0;
+    if (!ws.log2_lut.p) {
+        std::vector<float> lut(LOG2_LUT_SIZE);
+        for (uint32_t d = 0; d < LOG2_LUT_SIZE; d++) lut[d] = std::log2((float)d + 1.0f);
+        ws.log2_lut.reserve(LOG2_LUT_SIZE);
+        SA_CUDA(cudaMemcpy(ws.log2_lut.p, lut.data(), LOG2_LUT_SIZE * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    AnchorPack ap;
+    ap.qbits = ceil_log2((uint64_t)MAX_READ_LEN + 1);
+    ap.pbits = ceil_log2((uint64_t)max_contig_len + 1);
+    uint32_t rbits = ceil_log2((uint64_t)n_contigs);
+    if (ap.qbits + ap.pbits + rbits > 64) throw Error(SA_ERR_INVALID, "contig count/length too large for anchor keys");
+    launches += run_seeding(ix.p, n, total, ws, st);
+    ws.hit_pos.reserve(2 * total);
+    ws.hit_info.reserve(2 * total);
+    ws.hit_count_cache.reserve(2 * total);
+    ws.n_hits.reserve(2 * (size_t)n);
+    ws.orient.reserve(n);
+    ws.details.reserve(n);
+    k_hits<<<warps_grid(n), 32 * WARPS_PER_BLOCK, 0, st>>>(
+        ix, ws.off.p, n, total, cfg.mcs, cfg.rescue_distance, ws.qr_hash.p, ws.qr_hash_rc.p, ws.qr_start.p,
+        ws.qr_end.p, ws.n_rs.p, ws.hit_pos.p, ws.hit_info.p, ws.hit_count_cache.p, ws.n_hits.p, ws.orient.p,
+        ws.details.p);
+    launches++;
+    ws.hit_anchors.reserve(2 * total);
+    ws.seg_count.reserve(2 * (size_t)n + 1);
+    ws.seg_off.reserve(2 * (size_t)n + 1);
+    k_anchors<false><<<warps_grid(n), 32 * WARPS_PER_BLOCK, 0, st>>>(
+        ix, ws.off.p, n, total, ws.qr_hash.p, ws.qr_start.p, ws.qr_end.p, ws.hit_pos.p, ws.hit_info.p, ws.n_hits.p,
+        ws.orient.p, ws.hit_anchors.p, ws.seg_count.p, nullptr, nullptr, ap, ws.details.p);
+    launches++;
+    SA_CUDA(cudaMemsetAsync(ws.seg_count.p + 2 * (size_t)n, 0, 8, st));
+    cub_excl_sum(ws, ws.seg_count.p, ws.seg_off.p, 2 * (uint64_t)n + 1, st);
+    launches++;
+    uint64_t total_anchors = 0;
+    SA_CUDA(cudaMemcpyAsync(&total_anchors, ws.seg_off.p + 2 * (size_t)n, 8, cudaMemcpyDeviceToHost, st));
+    SA_CUDA(cudaStreamSynchronize(st));
+    ws.anchors.reserve(total_anchors);
+    ws.anchors_sorted.reserve(total_anchors);
+    k_anchors<true><<<warps_grid(n), 32 * WARPS_PER_BLOCK, 0, st>>>(
+        ix, ws.off.p, n, total, ws.qr_hash.p, ws.qr_start.p, ws.qr_end.p, ws.hit_pos.p, ws.hit_info.p, ws.n_hits.p,
+        ws.orient.p, ws.hit_anchors.p, nullptr, ws.seg_off.p, ws.anchors.p, ap, ws.details.p);
+    launches++;
+    if (total_anchors) {
+        size_t tmp = 0;
+        cub::DeviceSegmentedSort::SortKeys(nullptr, tmp, ws.anchors.p, ws.anchors_sorted.p, (int64_t)total_anchors,
+                                           (int64_t)(2 * (uint64_t)n), ws.seg_off.p, ws.seg_off.p + 1, st);
+        ws.cub_tmp.reserve(tmp);
+        cub::DeviceSegmentedSort::SortKeys(ws.cub_tmp.p, tmp, ws.anchors.p, ws.anchors_sorted.p,
+                                           (int64_t)total_anchors, (int64_t)(2 * (uint64_t)n), ws.seg_off.p,
+                                           ws.seg_off.p + 1, st);
+        launches++;
+    }
+    ws.dp.reserve(total_anchors);
+    ws.pred.reserve(total_anchors);
+    ws.aux.reserve(3 * total_anchors);
+    ws.nam_scratch.reserve(total_anchors);
+    ws.nam_seg_count.reserve(2 * (size_t)n);
+    ChainCtx cc{cfg.cp, ix.p.k, ws.log2_lut.p};
+    k_chain<<<warps_grid(2 * (uint64_t)n), 32 * WARPS_PER_BLOCK, 0, st>>>(
+        ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p, total_anchors, ap,
+        cc, ws.nam_scratch.p, ws.nam_seg_count.p);
+    launches++;
+    ws.nam_count.reserve((size_t)n + 1);
+    ws.nam_off.reserve((size_t)n + 1);
+    k_nam_counts<<<(n + 255) / 256 + 1, 256, 0, st>>>(n, ws.nam_seg_count.p, ws.nam_count.p);
+    SA_CUDA(cudaMemsetAsync(ws.nam_count.p + n, 0, 8, st));
+    cub_excl_sum(ws, ws.nam_count.p, ws.nam_off.p, (uint64_t)n + 1, st);
+    launches += 2;
+    uint64_t total_nams = 0;
+    SA_CUDA(cudaMemcpyAsync(&total_nams, ws.nam_off.p + n, 8, cudaMemcpyDeviceToHost, st));
+    SA_CUDA(cudaStreamSynchronize(st));
+    ws.nams.reserve(total_nams);
+    k_nam_compact<<<warps_grid(n), 32 * WARPS_PER_BLOCK, 0, st>>>(n, ws.seg_off.p, ws.nam_scratch.p,
+                                                                  ws.nam_seg_count.p, ws.nam_off.p, ws.nams.p,
+                                                                  ws.details.p);
+    launches++;
+    SA_CUDA(cudaGetLastError());
+    ws.last_total_nams = total_nams;
+    return launches;
+}
+
+}  // namespace sa

@@ -1,0 +1,149 @@
+// Host-side mapping policy: the sequential, per-chunk part of the reference's
+// mapping (src/mapper.rs, src/maponly.rs) that consumes GPU NAMs and GPU
+// extension results.  Missing extension results raise Miss; the batch driver then
+// runs another extension wave and resumes the chunk at the read that missed.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "extend.h"
+
+namespace sa {
+
+// fastrand 2.3.0 (wyrand + Lemire bounded integers), the RNG the reference seeds
+// per chunk (src/main.rs:878) and draws from on ties (src/shuffle.rs:21,
+// src/mapper.rs:461,716).
+struct Rng {
+    uint64_t state = 0;
+    uint64_t gen_u64();
+    uint32_t gen_mod_u32(uint32_t n);
+    uint64_t gen_mod_u64(uint64_t n);
+};
+
+// InsertSizeDistribution (src/insertsize.rs:1-50)
+struct InsertSize {
+    uint64_t sample_size = 0;
+    float mu = 300.0f, sigma = 100.0f, variance = 10000.0f, sse = 10000.0f;
+    void update(uint64_t insert_size);
+};
+
+struct Details {
+    NamDetailsRec nam{};
+    uint32_t inconsistent_nams = 0, mate_rescue = 0, tried_alignment = 0, gapped = 0, best_alignments = 0;
+};
+
+struct Alignment {
+    uint32_t reference_id = 0, ref_start = 0, edit_distance = 0, soft_clip_left = 0, soft_clip_right = 0;
+    uint32_t score = 0, length = 0;
+    bool is_revcomp = false, gapped = false;
+    const uint32_t* cigar = nullptr;
+    uint32_t cigar_len = 0;
+    uint32_t global_edit_distance() const { return edit_distance + soft_clip_left + soft_clip_right; }
+};
+
+struct JobKey {
+    uint32_t kind, a, b, c, d;
+    bool operator==(const JobKey& o) const {
+        return kind == o.kind && a == o.a && b == o.b && c == o.c && d == o.d;
+    }
+};
+
+struct Miss {};
+
+// Extension results of one batch, accumulated over waves.
+struct ResultStore {
+    struct Entry {
+        JobKey key;
+        uint32_t result;  // index into results, or UINT32_MAX while pending
+    };
+    std::vector<std::vector<Entry>> per_read;
+    std::vector<ExtResult> results;
+    std::vector<uint32_t> cigar;
+    std::vector<ExtJob> pending;  // requests of the wave being assembled
+};
+
+struct ReadView {
+    const char* seq;
+    uint32_t len;
+    const char* qual;  // nullptr if absent
+    const char* name;
+    uint32_t name_len;
+    const char* comment;  // nullptr if absent
+    uint32_t comment_len;
+};
+
+struct PolicyConfig {
+    sa_mapping_params mp;
+    std::string rg_id;
+    bool has_rg = false;
+    uint32_t k = 0;
+};
+
+struct ContigInfo {
+    const std::string* name;
+    uint64_t len;
+};
+
+// Per-read inputs the policy reads
+struct BatchView {
+    std::vector<ReadView> reads;         // device read order (pairs interleaved)
+    const NamRec* nams = nullptr;
+    const uint64_t* nam_off = nullptr;
+    const NamDetailsRec* details = nullptr;
+    bool paired = false;
+};
+
+struct ChunkState {
+    uint64_t first = 0, next = 0, end = 0;  // record range [first, end), cursor next
+    Rng rng;
+    InsertSize isd;
+    std::string out;
+    uint64_t mapped = 0;
+    bool done = false;
+};
+
+class Policy {
+  public:
+    Policy(const PolicyConfig& cfg, const std::vector<ContigInfo>& contigs, const BatchView& bv, ResultStore& store,
+           std::vector<double>* abundances)
+        : cfg_(cfg), contigs_(contigs), bv_(bv), store_(store), ab_(abundances) {}
+    // Advance one chunk as far as the available results allow.
+    void run_chunk(ChunkState& cs);
+    // Speculative first-wave requests for every read of the batch.
+    void seed_requests(uint64_t first_record, uint64_t end_record);
+
+  private:
+    const PolicyConfig& cfg_;
+    const std::vector<ContigInfo>& contigs_;
+    const BatchView& bv_;
+    ResultStore& store_;
+    std::vector<double>* ab_;
+
+    void want(uint32_t read, const ExtJob& job, const JobKey& key);
+    const ExtResult* lookup(uint32_t read, const JobKey& key) const;
+    const ExtResult& get(uint32_t read, const ExtJob& job, const JobKey& key);
+
+    void se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mapped);
+    void pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out, uint64_t& mapped);
+    void paf_se(uint64_t rec, Rng& rng, std::string& out);
+    void paf_pe(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out);
+    void aemb_se(uint64_t rec, Rng& rng);
+    void aemb_pe(uint64_t rec, Rng& rng, InsertSize& isd);
+
+  public:
+    // helpers used by the implementation file
+    std::vector<NamRec> sorted_nams(uint32_t read, Rng& rng) const;
+    ExtJob nam_job(uint32_t read, const NamRec& n, uint32_t kind) const;
+    static JobKey nam_key(const NamRec& n, uint32_t kind) { return JobKey{kind, n.nam_id, 0, 0, 0}; }
+    Alignment to_alignment(const ExtResult& r, uint32_t ref_id) const;
+    const PolicyConfig& cfg() const { return cfg_; }
+    const std::vector<ContigInfo>& contigs() const { return contigs_; }
+    const BatchView& bv() const { return bv_; }
+    // extend_seed with the given consistency semantics; applies the flip to nam
+    bool extend(uint32_t read, NamRec& nam, uint32_t kind, Alignment& out, bool& consistent);
+    bool rescue(uint32_t read, const NamRec& mate, float mu, float sigma, Alignment& out);
+    void want_nam(uint32_t read, const NamRec& n, uint32_t kind);
+};
+
+}  // namespace sa

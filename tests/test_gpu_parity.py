@@ -1,0 +1,258 @@
+"""GPU parity: each stage of the CUDA path against the oracle, and whole-run SAM /
+PAF / abundance bytes against the reference's goldens and the oracle."""
+import os
+import random
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle_lib import OracleIndex, aligner_oracle, randstrobes_oracle, run_oracle_cli
+
+pytestmark = pytest.mark.gpu
+
+RG = ["--rg-id=1", "--rg=SM:sample", "--rg=LB:library"]
+
+
+@pytest.fixture(scope="module")
+def sa():
+    import strobealign_gb300 as sa
+    return sa
+
+
+@pytest.fixture(scope="module")
+def synth(tmp_path_factory):
+    from strobealign_gb300 import synthetic as syn
+    d = tmp_path_factory.mktemp("synth")
+    g = syn.make_genome(21, 400_000, 3, gc=0.41, segdup_fraction=0.10, segdup_div=0.02)
+    fa = str(d / "ref.fa")
+    g.write_fasta(fa)
+    r1, r2 = syn.make_paired_end(22, g, 3000, 150, 300, 30, 0.01, 0.002, rescue_fraction=0.03)
+    f1, f2 = str(d / "r1.fq"), str(d / "r2.fq")
+    r1.write_fastq(f1)
+    r2.write_fastq(f2)
+    se = syn.make_single_end(23, g, 2000, (50, 500), 0.015, 0.002)
+    fse = str(d / "se.fq")
+    se.write_fastq(fse)
+    return dict(dir=d, fa=fa, f1=f1, f2=f2, fse=fse, genome=g)
+
+
+def _index(sa, fa, read_length=150):
+    refs = sa.References.from_fasta(fa)
+    p = sa.SeedingParameters.from_read_length(read_length)
+    return refs, sa.StrobemerIndex.build(refs, p)
+
+
+@pytest.mark.parametrize("which,read_length", [("phix", 150), ("phix", 300), ("synth", 150), ("synth", 250)])
+def test_index_identical_to_oracle(sa, synth, which, read_length):
+    fa = str(GOLDEN / "phix.fasta") if which == "phix" else synth["fa"]
+    refs, idx = _index(sa, fa, read_length)
+    rs, bs = idx.to_host()
+    o = OracleIndex(fa, read_length)
+    ors, obs = o.arrays()
+    n, bits, cutoff = o.info()
+    assert idx.bits == bits and idx.filter_cutoff == cutoff and len(rs) == n
+    assert (rs["hash_offset"] == ors["hash_offset"]).all()
+    assert (rs["position"] == ors["position"]).all() and (rs["ref_index"] == ors["ref_index"]).all()
+    assert (bs == obs).all()
+
+
+def test_index_lookups(sa, synth):
+    refs, idx = _index(sa, synth["fa"])
+    rs, bs = idx.to_host()
+    h = rs["hash_offset"] & np.uint64(0xFFFFFFFFFFFFFF00)
+    rng = np.random.default_rng(5)
+    q = np.concatenate([h[rng.integers(0, len(h), 2000)], rng.integers(0, 2**63, 2000, dtype=np.uint64)])
+    pos, cnt = idx.lookup(q, kind=0, counts=True)
+    first = np.searchsorted(h, q, side="left")
+    last = np.searchsorted(h, q, side="right")
+    found = first < last
+    assert (pos[found] == first[found]).all() and (pos[~found] == -1).all()
+    # the count is bounded by the bucket (src/index.rs:272-295)
+    assert (cnt[found] == (last - first)[found]).all()
+
+
+def _reads_with_edge_cases(synth):
+    rnd = random.Random(3)
+    g = synth["genome"].seqs[0].tobytes()
+    names, seqs = [], []
+    for i in range(300):
+        L = rnd.choice([0, 5, 10, 15, 20, 21, 30, 50, 100, 150, 151, 250, 500, 1000])
+        p = rnd.randint(0, len(g) - L - 1)
+        s = bytearray(g[p:p + L])
+        if rnd.random() < 0.3 and L > 4:
+            for _ in range(rnd.randint(1, 3)):
+                s[rnd.randrange(L)] = ord("N")
+        if rnd.random() < 0.1 and L:
+            s = bytearray(b"A" * L)  # homopolymer: every window is a syncmer
+        names.append(f"e{i}")
+        seqs.append(bytes(s))
+    return names, seqs
+
+
+@pytest.mark.parametrize("read_length", [150, 250])
+def test_randstrobes_identical_to_oracle(sa, synth, read_length):
+    refs, idx = _index(sa, synth["fa"], read_length)
+    names, seqs = _reads_with_edge_cases(synth)
+    got = sa.randstrobes_batch(idx, sa.Reads.from_lists(names, seqs))
+    for s, (f, r) in zip(seqs, got):
+        of, orc = randstrobes_oracle(s, read_length)
+        for a, b in ((f, of), (r, orc)):
+            assert len(a) == len(b), s
+            if len(a):
+                assert (a["hash"] == b[:, 0]).all() and (a["hash_revcomp"] == b[:, 1]).all()
+                assert (a["start"] == b[:, 2]).all() and (a["end"] == b[:, 3]).all()
+
+
+def _nam_rows(arr):
+    return [(int(x["nam_id"]), int(x["ref_id"]), int(x["ref_start"]), int(x["ref_end"]), int(x["query_start"]),
+             int(x["query_end"]), int(x["matching_bases"]), int(x["n_anchors"]),
+             np.float32(x["score"]).view(np.uint32), int(x["is_revcomp"])) for x in arr]
+
+
+@pytest.mark.parametrize("mcs", ["always", "rescue", "off", "first-strobe"])
+def test_nams_identical_to_oracle(sa, synth, mcs):
+    refs, idx = _index(sa, synth["fa"])
+    reads = sa.Reads.from_file(synth["f1"])
+    names, seqs = _reads_with_edge_cases(synth)
+    batch_seqs = [reads.seq[reads.seq_offsets[i]:reads.seq_offsets[i + 1]] for i in range(600)] + seqs
+    rb = sa.Reads.from_lists([f"n{i}" for i in range(len(batch_seqs))], batch_seqs)
+    nams, det = sa.nams_batch(idx, rb, mapping=sa.mapping_defaults(mcs_strategy=mcs))
+    o = OracleIndex(synth["fa"], 150)
+    mcs_i = sa.MCS[mcs]
+    for i, s in enumerate(batch_seqs):
+        rows, od = o.nams(bytes(s), mcs_i)
+        want = [r[:8] + (np.float32(r[8]).view(np.uint32), r[9]) for r in rows]
+        assert _nam_rows(nams[i]) == want, (i, s)
+        for k, v in od.items():
+            assert det[i][k] == v, (i, k)
+
+
+def test_align_batch_identical_to_oracle(sa):
+    rnd = random.Random(11)
+    qs, rs = [], []
+    for _ in range(1500):
+        L = rnd.choice([1, 10, 17, 50, 100, 150, 200, 300, 500])
+        q = bytes(rnd.choice(b"ACGT") for _ in range(L))
+        if rnd.random() < 0.1 and L > 3:
+            q = q[:L // 2] + b"N" + q[L // 2 + 1:]
+        core = bytearray()
+        for c in q:
+            x = rnd.random()
+            if x < 0.03:
+                core.append(rnd.choice(b"ACGT"))
+            elif x < 0.04:
+                pass
+            elif x < 0.05:
+                core += bytes([c, rnd.choice(b"ACGT")])
+            else:
+                core.append(c)
+        r = bytes(rnd.choice(b"ACGT") for _ in range(rnd.randint(0, 30))) + bytes(core) + \
+            bytes(rnd.choice(b"ACGT") for _ in range(rnd.randint(0, 30)))
+        if rnd.random() < 0.05:
+            r = bytes(rnd.choice(b"ACGT") for _ in range(rnd.randint(1, 80)))
+        qs.append(q)
+        rs.append(r)
+    got = sa.align_batch(qs, rs)
+    for q, r, g in zip(qs, rs, got):
+        assert g == aligner_oracle(q, r), (q, r)
+
+
+def _map_files(sa, fa, files, read_length=None, header=True, **kw):
+    refs = sa.References.from_fasta(fa)
+    r1 = sa.Reads.from_file(files[0])
+    if read_length is None:
+        n = min(500, len(r1))
+        read_length = int(r1.seq_offsets[n] // n) if n else 0
+    idx = sa.StrobemerIndex.build(refs, sa.SeedingParameters.from_read_length(read_length))
+    rg = kw.pop("rg", None)
+    m = sa.Mapper(idx, refs, **kw)
+    r2 = sa.Reads.from_file(files[1]) if len(files) > 1 else None
+    body = m.map(r1, r2)
+    if kw.get("mode", 0) == sa.MODE_ABUNDANCE:
+        ab = m.abundances()
+        lens = [len(s) for s in _fasta_lengths(fa)]
+        return "".join(f"{n}\t{a / L:.6f}\n" for n, a, L in zip(_fasta_names(fa), ab, lens)).encode()
+    if header and kw.get("mode", 0) == sa.MODE_SAM:
+        return sa.sam_header(refs, rg_id=rg[0] if rg else None, rg_fields=rg[1] if rg else ()) + body
+    return body
+
+
+def _fasta_names(fa):
+    return [l[1:].split()[0].decode() for l in open(fa, "rb") if l.startswith(b">")]
+
+
+def _fasta_lengths(fa):
+    seqs, cur = [], None
+    for l in open(fa, "rb"):
+        if l.startswith(b">"):
+            cur = []
+            seqs.append(cur)
+        else:
+            cur.append(l.strip())
+    return [b"".join(c) for c in seqs]
+
+
+def test_phix_paired_end_golden(sa):
+    got = _map_files(sa, str(GOLDEN / "phix.fasta"), [str(GOLDEN / "phix.1.fastq"), str(GOLDEN / "phix.2.fastq")],
+                     eqx=1, rg_id="1", rg=("1", ["SM:sample", "LB:library"]))
+    assert got == (GOLDEN / "phix.pe.sam").read_bytes()
+
+
+def test_phix_tags_golden(sa):
+    got = _map_files(sa, str(GOLDEN / "phix.fasta"), [str(GOLDEN / "phix.tags.fastq")], use_ssw=1,
+                     fastq_comments=1, rg_id="1", rg=("1", ["SM:sample", "LB:library"]))
+    assert got == (GOLDEN / "phix.tags.sam").read_bytes()
+
+
+def test_phix_single_end_ssw_matches_oracle(sa):
+    want = run_oracle_cli(["--chunk-size=3", "--no-PG", "--eqx", "--ssw", "phix.fasta", "phix.1.fastq"], cwd=GOLDEN)
+    got = _map_files(sa, str(GOLDEN / "phix.fasta"), [str(GOLDEN / "phix.1.fastq")], eqx=1, use_ssw=1, chunk_size=3)
+    assert got == want
+
+
+def test_phix_paf_and_abundance_goldens(sa):
+    got = _map_files(sa, str(GOLDEN / "phix.fasta"), [str(GOLDEN / "phix.1.fastq")], mode=sa.MODE_PAF)
+    assert b"".join(got.splitlines(keepends=True)[-11:]) == (GOLDEN / "phix.se.paf").read_bytes()
+    got = _map_files(sa, str(GOLDEN / "phix.fasta"), [str(GOLDEN / "phix.1.fastq")], mode=sa.MODE_PAF,
+                     mcs_strategy="rescue")
+    assert b"".join(got.splitlines(keepends=True)[-11:]) == (GOLDEN / "phix.mcsrescue.se.paf").read_bytes()
+    got = _map_files(sa, str(GOLDEN / "phix.fasta"), [str(GOLDEN / "phix.1.fastq")], mode=sa.MODE_ABUNDANCE)
+    assert got == (GOLDEN / "phix.abun.se.txt").read_bytes()
+    got = _map_files(sa, str(GOLDEN / "phix.fasta"), [str(GOLDEN / "phix.1.fastq"), str(GOLDEN / "phix.2.fastq")],
+                     mode=sa.MODE_ABUNDANCE)
+    assert got == (GOLDEN / "phix.abun.pe.txt").read_bytes()
+
+
+def _first_diff(a: bytes, b: bytes) -> str:
+    la, lb = a.splitlines(), b.splitlines()
+    for i in range(min(len(la), len(lb))):
+        if la[i] != lb[i]:
+            return f"line {i}:\n gpu    {la[i][:300]!r}\n oracle {lb[i][:300]!r}"
+    return f"lengths {len(la)} vs {len(lb)}"
+
+
+def test_synthetic_paired_end_sam_matches_oracle(sa, synth):
+    want = run_oracle_cli(["--no-PG", "--eqx", synth["fa"], synth["f1"], synth["f2"]])
+    got = _map_files(sa, synth["fa"], [synth["f1"], synth["f2"]], eqx=1)
+    assert got == want, _first_diff(got, want)
+
+
+def test_synthetic_paired_end_small_chunks_matches_oracle(sa, synth):
+    # many chunks: the per-chunk RNG and insert-size restarts are exercised
+    want = run_oracle_cli(["--no-PG", "--chunk-size=20000", synth["fa"], synth["f1"], synth["f2"]])
+    got = _map_files(sa, synth["fa"], [synth["f1"], synth["f2"]], chunk_size=20000)
+    assert got == want, _first_diff(got, want)
+
+
+def test_synthetic_single_end_ssw_matches_oracle(sa, synth):
+    want = run_oracle_cli(["--no-PG", "--eqx", "--ssw", synth["fa"], synth["fse"]])
+    got = _map_files(sa, synth["fa"], [synth["fse"]], eqx=1, use_ssw=1)
+    assert got == want, _first_diff(got, want)
+
+
+def test_synthetic_paf_matches_oracle(sa, synth):
+    want = run_oracle_cli(["-x", synth["fa"], synth["f1"], synth["f2"]])
+    got = _map_files(sa, synth["fa"], [synth["f1"], synth["f2"]], mode=sa.MODE_PAF)
+    assert got == want, _first_diff(got, want)
