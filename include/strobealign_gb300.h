@@ -239,8 +239,24 @@ typedef struct {
 int32_t sa_map_batch(sa_mapper* m, const sa_read_batch* r1, const sa_read_batch* r2, sa_output* out);
 void sa_output_free(sa_output* out);
 /* Abundances accumulated over all batches (--aemb), one per contig, already
- * divided by the contig length (src/main.rs:990-1001). */
+ * divided by the contig length as output_abundances does (src/main.rs:990-1001). */
 int32_t sa_mapper_abundances(const sa_mapper* m, double* out, size_t n);
+/* Two-step form of sa_map_batch: upload a batch to the device, then map it.  The
+ * host buffers of the batch must stay valid until the last sa_map_uploaded call
+ * (names, qualities and comments are read from them when records are written).
+ * Mapping the same uploaded batch again reproduces the same bytes. */
+int32_t sa_mapper_upload(sa_mapper* m, const sa_read_batch* r1, const sa_read_batch* r2);
+int32_t sa_map_uploaded(sa_mapper* m, sa_output* out);
+
+/* Stage timings and counters of the last mapped batch. */
+typedef struct {
+    double seconds_upload, seconds_nams, seconds_extension, seconds_policy, seconds_total;
+    uint64_t n_jobs, n_waves, n_launches;
+    uint64_t h2d_bytes, d2h_bytes;
+    uint64_t n_nams, n_anchors;
+} sa_mapper_stats;
+int32_t sa_mapper_get_stats(const sa_mapper* m, sa_mapper_stats* out);
+
 /* SAM header (src/io/sam.rs:176-200); cmd_line NULL omits the @PG line. */
 int32_t sa_sam_header(const sa_refs* refs, const char* cmd_line, const char* rg_id, const char* const* rg_fields,
                       size_t n_rg_fields, sa_output* out);

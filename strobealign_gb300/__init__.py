@@ -362,6 +362,29 @@ class Mapper:
         finally:
             lib().sa_output_free(C.byref(o))
 
+    def upload(self, r1: Reads, r2: Reads | None = None) -> None:
+        """Copy a batch to the device; map it with map_uploaded()."""
+        self._b1 = r1.c()
+        self._b2 = r2.c() if r2 is not None else None
+        self._keep = (r1, r2)
+        L.check(lib().sa_mapper_upload(self.h, C.byref(self._b1),
+                                       C.byref(self._b2) if self._b2 is not None else None))
+
+    def map_uploaded(self) -> bytes:
+        o = L.Output()
+        L.check(lib().sa_map_uploaded(self.h, C.byref(o)))
+        try:
+            self.last = dict(n_reads=o.n_reads, n_mapped=o.n_mapped, n_waves=o.n_waves,
+                             n_gpu_launches=o.n_gpu_launches)
+            return C.string_at(o.data, o.len) if o.len else b""
+        finally:
+            lib().sa_output_free(C.byref(o))
+
+    def stats(self) -> dict:
+        s = L.MapperStats()
+        L.check(lib().sa_mapper_get_stats(self.h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in L.MapperStats._fields_}
+
     def abundances(self) -> np.ndarray:
         n = len(self.refs)
         out = np.zeros(n, dtype=np.float64)

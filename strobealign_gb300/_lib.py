@@ -72,6 +72,12 @@ class Output(C.Structure):
                 ("n_gpu_launches", u32)]
 
 
+class MapperStats(C.Structure):
+    _fields_ = [("seconds_upload", f64), ("seconds_nams", f64), ("seconds_extension", f64),
+                ("seconds_policy", f64), ("seconds_total", f64), ("n_jobs", u64), ("n_waves", u64),
+                ("n_launches", u64), ("h2d_bytes", u64), ("d2h_bytes", u64), ("n_nams", u64), ("n_anchors", u64)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "sa_last_error": (cp, []),
@@ -105,6 +111,9 @@ SIGNATURES = {
     "sa_output_free": (None, [P(Output)]),
     "sa_mapper_abundances": (i32, [vp, P(f64), sz]),
     "sa_sam_header": (i32, [vp, cp, cp, P(cp), sz, P(Output)]),
+    "sa_mapper_upload": (i32, [vp, P(ReadBatch), P(ReadBatch)]),
+    "sa_map_uploaded": (i32, [vp, P(Output)]),
+    "sa_mapper_get_stats": (i32, [vp, P(MapperStats)]),
 }
 
 _lib = None

@@ -388,8 +388,34 @@ int32_t sa_mapper_abundances(const sa_mapper* m, double* out, size_t n) {
     SA_TRY
     require(m && out, "null argument");
     const auto& ab = m->m->abundances();
+    const auto& cs = m->m->contig_lengths();
     require(n >= ab.size(), "output too small");
-    for (size_t i = 0; i < ab.size(); i++) out[i] = ab[i];
+    for (size_t i = 0; i < ab.size(); i++) out[i] = ab[i] / (double)cs[i];
+    return SA_OK;
+    SA_CATCH
+}
+
+int32_t sa_mapper_upload(sa_mapper* m, const sa_read_batch* r1, const sa_read_batch* r2) {
+    SA_TRY
+    require(m && r1, "null argument");
+    m->m->upload(r1, r2);
+    return SA_OK;
+    SA_CATCH
+}
+
+int32_t sa_map_uploaded(sa_mapper* m, sa_output* out) {
+    SA_TRY
+    require(m && out, "null argument");
+    std::memset(out, 0, sizeof(*out));
+    m->m->map_uploaded(out);
+    return SA_OK;
+    SA_CATCH
+}
+
+int32_t sa_mapper_get_stats(const sa_mapper* m, sa_mapper_stats* out) {
+    SA_TRY
+    require(m && out, "null argument");
+    *out = m->m->stats();
     return SA_OK;
     SA_CATCH
 }

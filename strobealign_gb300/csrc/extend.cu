@@ -161,10 +161,13 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
 struct CigarWriter {
     uint32_t* out;
     uint32_t n;
+    uint32_t cap;
+    bool overflow;
     __device__ void push(uint32_t op, uint32_t len) {
         if (len == 0) return;
         if (n > 0 && (out[n - 1] & 15) == op) out[n - 1] += len << 4;
-        else out[n++] = (len << 4) | op;
+        else if (n < cap) out[n++] = (len << 4) | op;
+        else overflow = true;
     }
 };
 
@@ -195,7 +198,7 @@ __global__ void k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict
                 be = L;
                 bs = start;
             }
-            CigarWriter w{cigar + p.cigar_off, 0};
+            CigarWriter w{cigar + p.cigar_off, 0, p.cigar_cap, false};
             uint32_t mm = 0;
             for (uint32_t i = bs; i < be; i++) {
                 bool eq = read_char(s, L, i, p.rc) == ref_base(R, p.ref_id, p.wstart + i);
@@ -203,7 +206,7 @@ __global__ void k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict
                 w.push(eq ? 7u : 8u, 1);
             }
             ExtResult r = res[t];
-            r.valid = 1;
+            r.valid = w.overflow ? 0 : 1;
             r.score = (uint32_t)best;
             r.edit_distance = mm;
             r.ref_start = p.wstart + bs;
@@ -654,7 +657,7 @@ __global__ void k_finalize(const SswTask* tasks, const uint32_t* n_tasks_ptr, co
             else { fscore -= sc.mismatch; fed++; }
         }
         bool take_front = fq == 0 && fscore + (int32_t)sc.end_bonus > score;
-        CigarWriter w{cigar + p.cigar_off, 0};
+        CigarWriter w{cigar + p.cigar_off, 0, p.cigar_cap, false};
         if (take_front && qs > 0) {
             for (uint32_t a = fq; a < qs; a++) w.push(q[a] == rf[fr + (a - fq)] ? 7u : 8u, 1);
         }
@@ -708,7 +711,7 @@ __global__ void k_finalize(const SswTask* tasks, const uint32_t* n_tasks_ptr, co
             score = bscore + (int32_t)sc.end_bonus;
             edits = bed;
         }
-        r.valid = 1;
+        r.valid = w.overflow ? 0 : 1;
         r.score = (uint32_t)score;
         r.edit_distance = edits;
         r.ref_start = p.wstart + a_rs;
@@ -719,11 +722,6 @@ __global__ void k_finalize(const SswTask* tasks, const uint32_t* n_tasks_ptr, co
         r.cigar_len = w.n;
         res[tk.job] = r;
     }
-}
-
-__global__ void k_set_cigar_offsets(ExtResult* res, const PrepRec* prep, uint32_t n) {
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
-        if (res[t].valid) res[t].cigar_offset = (uint32_t)prep[t].cigar_off;
 }
 
 inline unsigned grid1(uint64_t n, unsigned block = 256) {

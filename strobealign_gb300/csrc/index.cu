@@ -131,12 +131,24 @@ struct RsDecomposer {
     }
 };
 
-// bucket_starts[x] = first entry whose top `bits` bits are >= x (src/indexer.rs:82-124)
+// Bucket directory exactly as src/indexer.rs:82-124 fills it: bucket_starts[0] = 0,
+// and for x >= 1 the first position p >= 1 that starts a new hash with top bits
+// >= x (N if none).  Entry 0 only ever starts bucket 0, so when the smallest hash
+// has top bits t > 0, buckets 1..t begin at the end of its run.
 __global__ void k_buckets(const RefRandstrobe* rs, uint64_t n, uint32_t bits, uint64_t* buckets) {
-    uint64_t nb = (1ULL << bits) + 1;
+    const uint64_t nb = (1ULL << bits) + 1;
+    const uint64_t h0 = n ? rs_hash(rs[0]) : 0;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i <= n; i += (uint64_t)gridDim.x * blockDim.x) {
-        int64_t lo = i == 0 ? -1 : (int64_t)(rs_hash(rs[i - 1]) >> (64 - bits));
-        int64_t hi = i == n ? (int64_t)nb - 1 : (int64_t)(rs_hash(rs[i]) >> (64 - bits));
+        int64_t lo, hi;
+        if (i == 0) {
+            lo = -1;
+            hi = n == 0 ? (int64_t)nb - 1 : 0;
+        } else {
+            uint64_t hp = rs_hash(rs[i - 1]);
+            if (i < n && rs_hash(rs[i]) == hp) continue;  // not the start of a new hash
+            lo = hp == h0 ? 0 : (int64_t)(hp >> (64 - bits));
+            hi = i == n ? (int64_t)nb - 1 : (int64_t)(rs_hash(rs[i]) >> (64 - bits));
+        }
         for (int64_t x = lo + 1; x <= hi; x++) buckets[x] = i;
     }
 }

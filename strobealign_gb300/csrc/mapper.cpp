@@ -123,7 +123,7 @@ uint32_t Mapper::run_wave(ResultStore& store, uint32_t max_qlen) {
     return launches;
 }
 
-void Mapper::map(const sa_read_batch* r1, const sa_read_batch* r2, sa_output* out) {
+void Mapper::upload(const sa_read_batch* r1, const sa_read_batch* r2) {
     if (single_end_piecewise_ && !r2)
         throw Error(SA_ERR_INVALID,
                     "single-end SAM output needs use_ssw=1: the piecewise (block-aligner) extension is not "
@@ -132,9 +132,9 @@ void Mapper::map(const sa_read_batch* r1, const sa_read_batch* r2, sa_output* ou
     const bool paired = r2 != nullptr;
     if (paired && r2->n != r1->n) throw Error(SA_ERR_INVALID, "r1 and r2 batches differ in size");
     const uint64_t nrec = r1->n;
-    BatchView bv;
-    bv.paired = paired;
-    bv.reads.resize(paired ? 2 * nrec : nrec);
+    bv_ = BatchView();
+    bv_.paired = paired;
+    bv_.reads.resize(paired ? 2 * nrec : nrec);
     auto view = [](const sa_read_batch* b, uint64_t i) {
         ReadView v;
         v.seq = b->seq + b->seq_offsets[i];
@@ -150,21 +150,46 @@ void Mapper::map(const sa_read_batch* r1, const sa_read_batch* r2, sa_output* ou
         }
         return v;
     };
-    uint32_t max_qlen = 1;
     for (uint64_t i = 0; i < nrec; i++) {
         if (paired) {
-            bv.reads[2 * i] = view(r1, i);
-            bv.reads[2 * i + 1] = view(r2, i);
+            bv_.reads[2 * i] = view(r1, i);
+            bv_.reads[2 * i + 1] = view(r2, i);
         } else {
-            bv.reads[i] = view(r1, i);
+            bv_.reads[i] = view(r1, i);
         }
     }
-    for (auto& r : bv.reads) max_qlen = std::max(max_qlen, r.len);
+    max_qlen_ = 1;
+    for (auto& r : bv_.reads) max_qlen_ = std::max(max_qlen_, r.len);
+    h2d_bytes_ = 0;
+    upload_reads(bv_.reads);
+    SA_CUDA(cudaStreamSynchronize(st_));
+    have_batch_ = true;
+    stats_.seconds_upload = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void Mapper::map(const sa_read_batch* r1, const sa_read_batch* r2, sa_output* out) {
+    auto t0 = std::chrono::steady_clock::now();
+    upload(r1, r2);
+    uint64_t h2d = h2d_bytes_;
+    double tu = stats_.seconds_upload;
+    map_uploaded(out);
+    stats_.seconds_upload = tu;
+    stats_.h2d_bytes += h2d;
+    stats_.seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void Mapper::map_uploaded(sa_output* out) {
+    if (!have_batch_) throw Error(SA_ERR_INVALID, "no uploaded batch");
+    auto t0 = std::chrono::steady_clock::now();
+    BatchView& bv = bv_;
+    const bool paired = bv.paired;
+    const uint64_t nrec = paired ? bv.reads.size() / 2 : bv.reads.size();
     uint32_t launches = 0;
     h2d_bytes_ = d2h_bytes_ = 0;
     jobs_run_ = 0;
-    upload_reads(bv.reads);
+    t_ext_ = 0;
     nams_for_reads(launches);
+    auto t1 = std::chrono::steady_clock::now();
     bv.nams = h_nams_.data();
     bv.nam_off = h_nam_off_.data();
     bv.details = h_details_.data();
@@ -189,8 +214,11 @@ void Mapper::map(const sa_read_batch* r1, const sa_read_batch* r2, sa_output* ou
     policy.seed_requests(0, nrec);
     uint32_t waves = 0;
     for (;;) {
+        if (waves > 1000000) throw Error(SA_ERR_INVALID, "internal: extension waves do not converge");
         if (!store.pending.empty()) {
-            launches += run_wave(store, max_qlen);
+            auto tw = std::chrono::steady_clock::now();
+            launches += run_wave(store, max_qlen_);
+            t_ext_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - tw).count();
             waves++;
         }
         bool all_done = true;
@@ -223,7 +251,19 @@ void Mapper::map(const sa_read_batch* r1, const sa_read_batch* r2, sa_output* ou
     out->n_gpu_launches = launches;
     last_launches_ = launches;
     last_waves_ = waves;
-    last_seconds_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    auto t2 = std::chrono::steady_clock::now();
+    last_seconds_ = std::chrono::duration<double>(t2 - t0).count();
+    stats_.seconds_nams = std::chrono::duration<double>(t1 - t0).count();
+    stats_.seconds_extension = t_ext_;
+    stats_.seconds_policy = std::chrono::duration<double>(t2 - t1).count() - t_ext_;
+    stats_.seconds_total = last_seconds_;
+    stats_.n_jobs = jobs_run_;
+    stats_.n_waves = waves;
+    stats_.n_launches = launches;
+    stats_.h2d_bytes = h2d_bytes_;
+    stats_.d2h_bytes = d2h_bytes_ + total_len;
+    stats_.n_nams = h_nams_.size();
+    stats_.n_anchors = 0;
 }
 
 }  // namespace sa

@@ -9,7 +9,15 @@ class Mapper {
     Mapper(const sa_index* idx, const sa_refs* refs, const sa_chaining_params& cp, const sa_mapping_params& mp);
     ~Mapper();
     void map(const sa_read_batch* r1, const sa_read_batch* r2, sa_output* out);
+    void upload(const sa_read_batch* r1, const sa_read_batch* r2);
+    void map_uploaded(sa_output* out);
+    const sa_mapper_stats& stats() const { return stats_; }
     const std::vector<double>& abundances() const { return abundances_; }
+    std::vector<uint64_t> contig_lengths() const {
+        std::vector<uint64_t> v;
+        for (auto& c : contigs_) v.push_back(c.len);
+        return v;
+    }
     const DevRefs& refs_view() const { return refs_view_; }
     NamWorkspace& nam_ws() { return nws_; }
     ExtWorkspace& ext_ws() { return ews_; }
@@ -29,6 +37,11 @@ class Mapper {
 
   private:
     uint32_t run_wave(ResultStore& store, uint32_t max_qlen);
+    BatchView bv_;
+    bool have_batch_ = false;
+    uint32_t max_qlen_ = 1;
+    sa_mapper_stats stats_{};
+    double t_ext_ = 0;
 
     const sa_index* idx_;
     const sa_refs* refs_;
