@@ -1,0 +1,306 @@
+#!/usr/bin/env python3
+"""Aligned reads/s of strobealign's paired-end mapping path on GB300.
+
+Workload: 50 Mbp synthetic reference in 20 contigs (GC 41%, 10% of it 2 kbp segmental
+copies at 2% divergence), 1M read pairs 2x150 bp, insert N(300, 30), 1% substitutions,
+0.1% indels, 2% of pairs with one mate too mutated to seed (mate rescue).  Seeded
+generators (strobealign_gb300.synthetic) stand in for the reference's read sets.
+
+One step maps the whole batch: NAM finding, SSW-exact extension waves and SAM record
+formatting, chunked as the reference chunks its input.  `value` is measured with the
+reads already resident in device memory (sa_map_uploaded); `e2e` maps from host
+buffers through sa_map_batch (reads copied to the device, NAMs and alignments copied
+back, SAM bytes returned to the caller).  Index (160 MB) + reads (300 MB) exceed the
+129 MB L2, so no flush is done between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun each rank maps its own replica of the workload (no data exchange:
+chunks are independent), and rank 0 prints one JSON line with the aggregate rate
+over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "aligned reads/s on 1 GB300 (bit-exact SAM), served vs plain; p50/p99 latency"
+WORKLOAD = "paired-end repetitive: 50 Mbp / 20 contigs, 1M pairs 2x150 bp, insert N(300,30), 1% sub, 0.1% indel"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload (1.0 = full)")
+    ap.add_argument("--cpu-sample-pairs", type=int, default=20000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload(scale: float):
+    from strobealign_gb300 import synthetic as syn
+    g = syn.make_genome(2, int(50_000_000 * scale), 20, gc=0.41, segdup_fraction=0.10, segdup_len=2000,
+                        segdup_div=0.02)
+    r1, r2 = syn.make_paired_end(102, g, int(1_000_000 * scale), 150, 300, 30, 0.01, 0.001, rescue_fraction=0.02)
+    return g, r1, r2
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.f = None
+
+    def __enter__(self):
+        try:
+            self.f = tempfile.TemporaryFile(mode="w+")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.f:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f:
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(g, r1, r2, pairs: int, threads: int) -> dict:
+    """The oracle (C++ restatement of the reference's CPU path) on a bounded sample,
+    all host threads; index build excluded from the rate."""
+    from oracle import build as oracle_build
+    from strobealign_gb300 import synthetic as syn
+    oracle_build.build()
+    pairs = min(pairs, len(r1))
+    with tempfile.TemporaryDirectory() as d:
+        fa, f1, f2 = os.path.join(d, "ref.fa"), os.path.join(d, "r1.fq"), os.path.join(d, "r2.fq")
+        g.write_fasta(fa)
+        for rs, f in ((r1, f1), (r2, f2)):
+            sub = syn.ReadSet(rs.seq[:int(rs.offsets[pairs])], rs.offsets[:pairs + 1], rs.names,
+                              rs.name_offsets[:pairs + 1], rs.qual)
+            sub.write_fastq(f)
+        r = subprocess.run([str(oracle_build.cli_path()), "-t", str(threads), "--timing", "-o", os.path.join(d, "o.sam"),
+                            fa, f1, f2], capture_output=True, text=True, check=True)
+    line = [l for l in r.stderr.splitlines() if l.startswith("oracle_timing")][-1]
+    kv = dict(x.split("=") for x in line.split()[1:])
+    map_s = float(kv["map_s"])
+    return {"value": 2 * pairs / map_s, "unit": "reads/s", "cores": threads, "kind": "port",
+            "sample": f"{pairs} pairs of the same workload, index build excluded ({float(kv['index_s']):.1f} s)",
+            "seconds": map_s}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    g, r1, r2 = workload(args.scale)
+    for _ in range(args.warmup):
+        cpu_baseline(g, r1, r2, min(2000, args.cpu_sample_pairs), threads)
+    vals, secs = [], []
+    for _ in range(args.steps):
+        b = cpu_baseline(g, r1, r2, args.cpu_sample_pairs, threads)
+        vals.append(b["value"])
+        secs.append(b["seconds"])
+    value = statistics.median(vals)
+    out = {"metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1000 * statistics.median(secs), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+           "impl": "reference",
+           "config": {"workload": WORKLOAD, "scale": args.scale, "sample_pairs": args.cpu_sample_pairs},
+           "cpu_baseline": {"value": value, "unit": "reads/s", "cores": threads, "kind": "port",
+                            "sample": f"{args.cpu_sample_pairs} pairs per step; the Rust reference cannot be built "
+                                      "(no cargo); the oracle restates its CPU path"},
+           "e2e": {"value": value, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_info()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+    import torch
+    torch.cuda.set_device(local)
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+    import strobealign_gb300 as sa
+
+    g, r1, r2 = workload(args.scale)
+    refs = sa.References.from_sequences(g.names, [s.tobytes() for s in g.seqs])
+    params = sa.SeedingParameters.from_read_length(150)
+    t = time.time()
+    index = sa.StrobemerIndex.build(refs, params)
+    torch.cuda.synchronize()
+    index_s = time.time() - t
+    R1 = sa.Reads.from_arrays(r1.seq, r1.offsets, r1.names, r1.name_offsets, r1.qual)
+    R2 = sa.Reads.from_arrays(r2.seq, r2.offsets, r2.names, r2.name_offsets, r2.qual)
+    n_reads = 2 * len(R1)
+    mapper = sa.Mapper(index, refs)
+    mapper.upload(R1, R2)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if pg:
+            pg.barrier()
+
+    for _ in range(max(3, args.warmup)):
+        mapper.map_uploaded()
+    # timed region: reads resident in device memory
+    mapper.set_profiling(True)
+    kern = {}
+    launches = 0
+    barrier()
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            out = mapper.map_uploaded()
+            st = mapper.stats()
+            launches += int(st["n_launches"])
+            for k, v in st["kernel_ms"].items():
+                kern.setdefault(k, [0.0, 0])
+                kern[k][0] += v
+                kern[k][1] += int(st["kernel_launches"][k])
+        ev1.record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+    mapper.set_profiling(False)
+    ev_ms = ev0.elapsed_time(ev1)
+    elapsed = max(wall, ev_ms / 1000.0)
+    if pg:
+        tt = torch.tensor([elapsed], device="cuda")
+        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+        elapsed = float(tt.item())
+    value = ws * n_reads * args.steps / elapsed
+    sam_bytes = len(out)
+    # end to end: host buffers in, SAM bytes out, every step
+    h2d = d2h = 0
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        mapper.map(R1, R2)
+        st = mapper.stats()
+        h2d, d2h = int(st["h2d_bytes"]), int(st["d2h_bytes"])
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if pg:
+        tt = torch.tensor([e2e_s], device="cuda")
+        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e = ws * n_reads * args.steps / e2e_s
+    if rank != 0:
+        pg.destroy_process_group()
+        return
+    # roofline of the dominant stage, from the CUDA-event times of the timed steps
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    total_ms = sum(v[0] for v in kern.values())
+    dom = max(kern, key=lambda k: kern[k][0]) if kern else None
+    shares = {k: round(v[0] / total_ms, 4) for k, v in kern.items() if total_ms and v[0] > 0}
+    roofline = roofline_for(dom, kern, st, peaks, clk.summary()) if dom else None
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline(g, r1, r2, args.cpu_sample_pairs, os.cpu_count() or 1)
+        except Exception as e:  # reported, never fatal for the GPU line
+            cpu = {"value": None, "error": str(e)[:200]}
+    out = {
+        "metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": 1000 * elapsed / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "scale": args.scale, "reads_per_step": n_reads,
+                   "l2": "no flush: index 160 MB + reads 300 MB exceed the 129 MB L2",
+                   "form": "plain (one launch per stage, extension waves)", "sam_bytes_per_step": sam_bytes,
+                   "index_build_s": round(index_s, 3)},
+        "e2e": {"value": e2e, "unit": "reads/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "stage_share": shares,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(out), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+def roofline_for(dom, kern, st, peaks, clocks) -> dict:
+    """achieved/peak of the dominant stage.  Lookup (hits) is HBM-bound: algorithmic
+    bytes are the 32-byte sectors of index directory and table the reference's probe
+    sequence touches.  Extension (sw_*) is integer-ALU bound: cells = query x window
+    of each striped pass, against 152 SMs x 128 INT32 lanes x SM clock / 11 ops per cell."""
+    ms, n = kern[dom]
+    avg_s = ms / 1000.0 / max(n, 1)
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    if dom in ("sw_byte", "sw_word"):
+        c = st["sw_cells"]
+        cells = (c["forward_byte"] + c["reverse_byte"]) if dom == "sw_byte" else (c["forward_word"] + c["reverse_word"])
+        cells_per_launch = cells / max(1, st["kernel_launches"][dom])
+        clock = (clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)) * 1e6
+        peak_gcups = 152 * 128 * clock / 11 / 1e9
+        achieved = cells_per_launch / avg_s / 1e9
+        return {"kernel": dom, "bound": "int32", "achieved": achieved, "peak": peak_gcups, "unit": "GCUPS",
+                "frac": achieved / peak_gcups, "traffic": None, "avg_launch_ms": avg_s * 1000,
+                "peak_source": "152 SMs x 128 INT32 lanes x median SM clock under load / 11 ops per cell"}
+    return {"kernel": dom, "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None,
+            "traffic": None, "avg_launch_ms": avg_s * 1000}
+
+
+if __name__ == "__main__":
+    main()

@@ -254,8 +254,18 @@ typedef struct {
     uint64_t n_jobs, n_waves, n_launches;
     uint64_t h2d_bytes, d2h_bytes;
     uint64_t n_nams, n_anchors;
+    /* per-stage device time (CUDA events on the mapper's stream) when profiling is
+     * on: seed, hits, anchors, sort, chain, other NAM, prepare, fill, SW byte,
+     * SW word, banded traceback, finalize, other extension */
+    double kernel_ms[16];
+    uint64_t kernel_launches[16];
+    /* Smith-Waterman cells (query x reference) of the striped passes: forward byte,
+     * forward word (byte overflow reruns), reverse byte, reverse word */
+    uint64_t sw_cells[4];
 } sa_mapper_stats;
 int32_t sa_mapper_get_stats(const sa_mapper* m, sa_mapper_stats* out);
+/* Record CUDA events around each stage's launches (off by default). */
+int32_t sa_mapper_set_profiling(sa_mapper* m, int32_t enable);
 
 /* SAM header (src/io/sam.rs:176-200); cmd_line NULL omits the @PG line. */
 int32_t sa_sam_header(const sa_refs* refs, const char* cmd_line, const char* rg_id, const char* const* rg_fields,

@@ -383,7 +383,14 @@ class Mapper:
     def stats(self) -> dict:
         s = L.MapperStats()
         L.check(lib().sa_mapper_get_stats(self.h, C.byref(s)))
-        return {f: getattr(s, f) for f, _ in L.MapperStats._fields_}
+        d = {f: getattr(s, f) for f, _ in L.MapperStats._fields_ if not f.startswith("kernel_")}
+        d["kernel_ms"] = {n: s.kernel_ms[i] for i, n in enumerate(L.KERNEL_SLOTS)}
+        d["kernel_launches"] = {n: s.kernel_launches[i] for i, n in enumerate(L.KERNEL_SLOTS)}
+        d["sw_cells"] = dict(zip(("forward_byte", "forward_word", "reverse_byte", "reverse_word"), list(s.sw_cells)))
+        return d
+
+    def set_profiling(self, on: bool = True) -> None:
+        L.check(lib().sa_mapper_set_profiling(self.h, 1 if on else 0))
 
     def abundances(self) -> np.ndarray:
         n = len(self.refs)

@@ -75,7 +75,12 @@ class Output(C.Structure):
 class MapperStats(C.Structure):
     _fields_ = [("seconds_upload", f64), ("seconds_nams", f64), ("seconds_extension", f64),
                 ("seconds_policy", f64), ("seconds_total", f64), ("n_jobs", u64), ("n_waves", u64),
-                ("n_launches", u64), ("h2d_bytes", u64), ("d2h_bytes", u64), ("n_nams", u64), ("n_anchors", u64)]
+                ("n_launches", u64), ("h2d_bytes", u64), ("d2h_bytes", u64), ("n_nams", u64), ("n_anchors", u64),
+                ("kernel_ms", f64 * 16), ("kernel_launches", u64 * 16), ("sw_cells", u64 * 4)]
+
+
+KERNEL_SLOTS = ["seed", "hits", "anchors", "sort", "chain", "nams_other", "prepare", "fill", "sw_byte", "sw_word",
+                "banded_traceback", "finalize", "ext_other"]
 
 
 # name -> (restype, argtypes)
@@ -114,6 +119,7 @@ SIGNATURES = {
     "sa_mapper_upload": (i32, [vp, P(ReadBatch), P(ReadBatch)]),
     "sa_map_uploaded": (i32, [vp, P(Output)]),
     "sa_mapper_get_stats": (i32, [vp, P(MapperStats)]),
+    "sa_mapper_set_profiling": (i32, [vp, i32]),
 }
 
 _lib = None

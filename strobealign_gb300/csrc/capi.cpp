@@ -32,7 +32,7 @@ void index_extent_gpu(const sa_index& idx, uint32_t& max_pos, uint32_t& max_ref,
 void extension_init_tables();
 uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64_t* off, const uint8_t* raw_refs,
                            const uint64_t* raw_off, uint32_t k, const AlignScores& sc, uint32_t n, ExtWorkspace& ws,
-                           uint32_t max_qlen, cudaStream_t st);
+                           uint32_t max_qlen, cudaStream_t st, KernelTimers* kt = nullptr);
 
 }  // namespace sa
 
@@ -408,6 +408,14 @@ int32_t sa_map_uploaded(sa_mapper* m, sa_output* out) {
     require(m && out, "null argument");
     std::memset(out, 0, sizeof(*out));
     m->m->map_uploaded(out);
+    return SA_OK;
+    SA_CATCH
+}
+
+int32_t sa_mapper_set_profiling(sa_mapper* m, int32_t enable) {
+    SA_TRY
+    require(m, "null argument");
+    m->m->set_profiling(enable != 0);
     return SA_OK;
     SA_CATCH
 }

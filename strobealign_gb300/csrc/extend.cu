@@ -66,7 +66,8 @@ __device__ bool shared_substring(const DevRefs& R, uint32_t ref_id, uint32_t ws,
 
 __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict__ seq,
                           const uint64_t* __restrict__ off, DevRefs R, uint32_t k, const uint8_t* raw_refs,
-                          const uint64_t* raw_off, ExtResult* res, PrepRec* prep, uint64_t* sizes) {
+                          const uint64_t* raw_off, ExtResult* res, PrepRec* prep, uint64_t* sz_arena,
+                          uint64_t* sz_cigar, uint64_t* sz_h) {
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         ExtJob jb = jobs[t];
         const uint8_t* s = seq + off[jb.read];
@@ -151,9 +152,9 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
         p.cigar_cap = (uint32_t)cap;
         res[t] = r;
         prep[t] = p;
-        sizes[3 * t] = ab;
-        sizes[3 * t + 1] = cap;
-        sizes[3 * t + 2] = hs;
+        sz_arena[t] = ab;
+        sz_cigar[t] = cap;
+        sz_h[t] = hs;
     }
 }
 
@@ -173,13 +174,13 @@ struct CigarWriter {
 
 __global__ void k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict__ seq, const uint64_t* __restrict__ off,
                        DevRefs R, const uint8_t* raw_refs, const uint64_t* raw_off, AlignScores sc, PrepRec* prep,
-                       const uint64_t* offs, uint8_t* arena, uint32_t* cigar, ExtResult* res, SswTask* tasks,
-                       uint32_t* counters) {
+                       const uint64_t* off_arena, const uint64_t* off_cigar, const uint64_t* off_h, uint8_t* arena,
+                       uint32_t* cigar, ExtResult* res, SswTask* tasks, uint32_t* counters) {
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         PrepRec p = prep[t];
-        p.arena_off = offs[3 * t];
-        p.cigar_off = offs[3 * t + 1];
-        p.h_off = offs[3 * t + 2];
+        p.arena_off = off_arena[t];
+        p.cigar_off = off_cigar[t];
+        p.h_off = off_h[t];
         prep[t] = p;
         const uint8_t* s = seq + off[p.read];
         const uint32_t L = p.qlen;
@@ -227,6 +228,7 @@ __global__ void k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict
                 for (uint32_t i = 0; i < p.wlen; i++) w[i] = ref_base(R, p.ref_id, p.wstart + i);
             }
             uint32_t ti = atomicAdd(&counters[0], 1u);
+            atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8), (unsigned long long)L * p.wlen);
             SswTask tk{};
             tk.job = t;
             tk.ref_begin1 = -1;
@@ -423,6 +425,8 @@ __global__ void __launch_bounds__(128) k_sw(SswTask* tasks, const uint32_t* list
             if (gl == 0) {
                 if (!WORD && e.score == 255) {
                     list_word[atomicAdd(&counters[1], 1u)] = ti;
+                    atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8) + 1,
+                              (unsigned long long)p.qlen * p.wlen);
                 } else {
                     tk.score1 = e.score;
                     tk.ref_end1 = e.ref;
@@ -448,6 +452,9 @@ __global__ void __launch_bounds__(128) k_sw(SswTask* tasks, const uint32_t* list
                 tk.ref_begin1 = e.ref;
                 tk.read_begin1 = tk.read_end1 - e.read;
                 tk.flag = tk.score1 > e.score ? 2 : 0;
+                if (tk.ref_end1 >= 0)
+                    atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8) + 2 + (WORD ? 1 : 0),
+                              (unsigned long long)(tk.read_end1 + 1) * (unsigned long long)(tk.ref_end1 + 1));
                 tasks[ti] = tk;
             }
         }
@@ -724,6 +731,24 @@ __global__ void k_finalize(const SswTask* tasks, const uint32_t* n_tasks_ptr, co
     }
 }
 
+__global__ void k_cigar_used(const ExtResult* res, uint32_t n, uint64_t* used) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+        used[t] = res[t].valid ? res[t].cigar_len : 0;
+}
+
+// copy each valid job's CIGAR into a compact array and point the result at it
+__global__ void k_cigar_gather(ExtResult* res, uint32_t n, const uint32_t* cigar, const uint64_t* off,
+                               uint32_t* compact) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        ExtResult r = res[t];
+        if (!r.valid) continue;
+        const uint64_t o = off[t];
+        for (uint32_t i = 0; i < r.cigar_len; i++) compact[o + i] = cigar[r.cigar_offset + i];
+        r.cigar_offset = (uint32_t)o;
+        res[t] = r;
+    }
+}
+
 inline unsigned grid1(uint64_t n, unsigned block = 256) {
     uint64_t g = (n + block - 1) / block;
     if (g > 152ULL * 16) g = 152ULL * 16;
@@ -763,36 +788,38 @@ void extension_init_tables() { init_tables(); }
 
 uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64_t* off, const uint8_t* raw_refs,
                            const uint64_t* raw_off, uint32_t k, const AlignScores& sc, uint32_t n, ExtWorkspace& ws,
-                           uint32_t max_qlen, cudaStream_t st) {
+                           uint32_t max_qlen, cudaStream_t st, KernelTimers* kt) {
     init_tables();
+    KernelTimers none;
+    if (!kt) kt = &none;
     uint32_t launches = 0;
     ws.results.reserve(n);
     ws.prep.reserve(n);
-    ws.sizes.reserve(3 * (size_t)n + 3);
-    ws.offs.reserve(3 * (size_t)n + 3);
-    ws.counters.reserve(8);
+    ws.sizes.reserve(3 * ((size_t)n + 1));
+    ws.offs.reserve(3 * ((size_t)n + 1));
+    ws.counters.reserve(16);
     if (n == 0) {
         ws.h_results.clear();
         ws.h_cigar.clear();
         return 0;
     }
-    SA_CUDA(cudaMemsetAsync(ws.counters.p, 0, 8 * sizeof(uint32_t), st));
+    uint64_t* sz[3] = {ws.sizes.p, ws.sizes.p + n + 1, ws.sizes.p + 2 * ((size_t)n + 1)};
+    uint64_t* of[3] = {ws.offs.p, ws.offs.p + n + 1, ws.offs.p + 2 * ((size_t)n + 1)};
+    SA_CUDA(cudaMemsetAsync(ws.counters.p, 0, 16 * sizeof(uint32_t), st));
+    kt->begin(KS_PREPARE, st);
     k_prepare<<<grid1(n), 256, 0, st>>>(ws.jobs.p, n, seq, off, refs, k, raw_refs, raw_off, ws.results.p, ws.prep.p,
-                                        ws.sizes.p);
+                                        sz[0], sz[1], sz[2]);
+    kt->end(st);
     launches++;
-    SA_CUDA(cudaMemsetAsync(ws.sizes.p + 3 * (size_t)n, 0, 3 * 8, st));
-    // three interleaved exclusive scans: arena bytes, cigar ops, h ints
-    std::vector<uint64_t> hsz(3 * (size_t)n + 3);
-    SA_CUDA(cudaMemcpyAsync(hsz.data(), ws.sizes.p, hsz.size() * 8, cudaMemcpyDeviceToHost, st));
+    // exclusive scans of arena bytes, CIGAR capacity and banded-DP scratch per job
+    uint64_t tot[3];
+    for (int c = 0; c < 3; c++) {
+        SA_CUDA(cudaMemsetAsync(sz[c] + n, 0, 8, st));
+        excl_sum(ws, sz[c], of[c], (uint64_t)n + 1, st);
+        SA_CUDA(cudaMemcpyAsync(&tot[c], of[c] + n, 8, cudaMemcpyDeviceToHost, st));
+    }
+    launches += 3;
     SA_CUDA(cudaStreamSynchronize(st));
-    uint64_t tot[3] = {0, 0, 0};
-    for (size_t t = 0; t <= n; t++)
-        for (int c = 0; c < 3; c++) {
-            uint64_t v = hsz[3 * t + c];
-            hsz[3 * t + c] = tot[c];
-            tot[c] += v;
-        }
-    SA_CUDA(cudaMemcpyAsync(ws.offs.p, hsz.data(), hsz.size() * 8, cudaMemcpyHostToDevice, st));
     ws.arena.reserve(tot[0] + 16);
     ws.cigar.reserve(tot[1] + 1);
     ws.hscratch.reserve(tot[2] + 1);
@@ -800,8 +827,10 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
     ws.list_word.reserve(n);
     ws.list_rev_byte.reserve(n);
     ws.list_rev_word.reserve(n);
-    k_fill<<<grid1(n), 256, 0, st>>>(ws.jobs.p, n, seq, off, refs, raw_refs, raw_off, sc, ws.prep.p, ws.offs.p,
-                                     ws.arena.p, ws.cigar.p, ws.results.p, ws.tasks.p, ws.counters.p);
+    kt->begin(KS_FILL, st);
+    k_fill<<<grid1(n), 256, 0, st>>>(ws.jobs.p, n, seq, off, refs, raw_refs, raw_off, sc, ws.prep.p, of[0], of[1],
+                                     of[2], ws.arena.p, ws.cigar.p, ws.results.p, ws.tasks.p, ws.counters.p);
+    kt->end(st);
     launches++;
     uint32_t cnt[4];
     SA_CUDA(cudaMemcpyAsync(cnt, ws.counters.p, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
@@ -825,27 +854,37 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
             return (unsigned)(b ? b : 1);
         };
         // forward byte pass over all tasks
+        kt->begin(KS_SW_BYTE, st);
         k_sw<false><<<blocks_for(n_tasks, tpb / 16), tpb, smem_b, st>>>(
             ws.tasks.p, nullptr, nullptr, n_tasks, ws.prep.p, ws.arena.p, sc, bias, 0, seg_b, ws.counters.p,
             ws.list_word.p, ws.list_rev_byte.p, ws.list_rev_word.p);
+        kt->end(st);
         // forward word pass over the overflowed tasks
+        kt->begin(KS_SW_WORD, st);
         k_sw<true><<<blocks_for(n_tasks, tpb / 8), tpb, smem_w, st>>>(
             ws.tasks.p, ws.list_word.p, ws.counters.p + 1, 0, ws.prep.p, ws.arena.p, sc, bias, 0, seg_w,
             ws.counters.p, ws.list_word.p, ws.list_rev_byte.p, ws.list_rev_word.p);
+        kt->end(st);
         // reverse passes
+        kt->begin(KS_SW_BYTE, st);
         k_sw<false><<<blocks_for(n_tasks, tpb / 16), tpb, smem_b, st>>>(
             ws.tasks.p, ws.list_rev_byte.p, ws.counters.p + 2, 0, ws.prep.p, ws.arena.p, sc, bias, 1, seg_b,
             ws.counters.p, ws.list_word.p, ws.list_rev_byte.p, ws.list_rev_word.p);
+        kt->end(st);
+        kt->begin(KS_SW_WORD, st);
         k_sw<true><<<blocks_for(n_tasks, tpb / 8), tpb, smem_w, st>>>(
             ws.tasks.p, ws.list_rev_word.p, ws.counters.p + 3, 0, ws.prep.p, ws.arena.p, sc, bias, 1, seg_w,
             ws.counters.p, ws.list_word.p, ws.list_rev_byte.p, ws.list_rev_word.p);
+        kt->end(st);
         launches += 4;
         ws.dir_size.reserve((size_t)n_tasks + 1);
         ws.dir_off.reserve((size_t)n_tasks + 1);
         ws.raw_size.reserve((size_t)n_tasks + 1);
         ws.raw_off.reserve((size_t)n_tasks + 1);
+        kt->begin(KS_BAND, st);
         k_band_width<<<grid1(n_tasks, 128), 128, 0, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p,
                                                           ws.hscratch.p, sc, ws.dir_size.p, ws.raw_size.p);
+        kt->end(st);
         launches++;
         SA_CUDA(cudaMemsetAsync(ws.dir_size.p + n_tasks, 0, 8, st));
         SA_CUDA(cudaMemsetAsync(ws.raw_size.p + n_tasks, 0, 8, st));
@@ -859,27 +898,43 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
         ws.dir.reserve(dtot + 16);
         ws.raw.reserve(rtot + 1);
         SA_CUDA(cudaMemsetAsync(ws.dir.p, 0, dtot + 16, st));
+        kt->begin(KS_BAND, st);
         k_band_trace<<<grid1(n_tasks, 128), 128, 0, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p,
                                                           ws.hscratch.p, sc, ws.dir_off.p, ws.dir.p, ws.raw_off.p,
                                                           ws.raw.p);
+        kt->end(st);
+        kt->begin(KS_FINALIZE, st);
         k_finalize<<<grid1(n_tasks, 128), 128, 0, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p,
                                                         ws.raw_off.p, ws.raw.p, sc, ws.cigar.p, ws.results.p);
+        kt->end(st);
         launches += 2;
     }
+    // compact the CIGARs that were written and copy back results + used ops only
+    k_cigar_used<<<grid1(n), 256, 0, st>>>(ws.results.p, n, sz[0]);
+    SA_CUDA(cudaMemsetAsync(sz[0] + n, 0, 8, st));
+    excl_sum(ws, sz[0], of[0], (uint64_t)n + 1, st);
+    uint64_t used = 0;
+    SA_CUDA(cudaMemcpyAsync(&used, of[0] + n, 8, cudaMemcpyDeviceToHost, st));
+    SA_CUDA(cudaStreamSynchronize(st));
+    ws.raw.reserve(std::max<uint64_t>(used, 1));  // reused as the compact CIGAR buffer
+    k_cigar_gather<<<grid1(n), 256, 0, st>>>(ws.results.p, n, ws.cigar.p, of[0], ws.raw.p);
+    launches += 3;
     SA_CUDA(cudaGetLastError());
     ws.h_results.resize(n);
-    ws.h_cigar.resize(tot[1]);
+    ws.h_cigar.resize(used);
     SA_CUDA(cudaMemcpyAsync(ws.h_results.data(), ws.results.p, (size_t)n * sizeof(ExtResult), cudaMemcpyDeviceToHost,
                             st));
-    if (tot[1]) SA_CUDA(cudaMemcpyAsync(ws.h_cigar.data(), ws.cigar.p, tot[1] * 4, cudaMemcpyDeviceToHost, st));
+    if (used) SA_CUDA(cudaMemcpyAsync(ws.h_cigar.data(), ws.raw.p, used * 4, cudaMemcpyDeviceToHost, st));
+    SA_CUDA(cudaMemcpyAsync(ws.cells, ws.counters.p + 8, 4 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
     SA_CUDA(cudaStreamSynchronize(st));
+    tot[1] = used;
     ws.total_cigar = tot[1];
     return launches;
 }
 
 uint32_t run_extension(const DevRefs& refs, const NamWorkspace& nws, uint32_t k, const AlignScores& sc, uint32_t n,
-                       ExtWorkspace& ws, uint32_t max_qlen, cudaStream_t st) {
-    return run_extension_raw(refs, nws.seq.p, nws.off.p, nullptr, nullptr, k, sc, n, ws, max_qlen, st);
+                       ExtWorkspace& ws, uint32_t max_qlen, cudaStream_t st, KernelTimers* kt) {
+    return run_extension_raw(refs, nws.seq.p, nws.off.p, nullptr, nullptr, k, sc, n, ws, max_qlen, st, kt);
 }
 
 }  // namespace sa

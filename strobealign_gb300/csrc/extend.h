@@ -60,12 +60,13 @@ struct ExtWorkspace {
     std::vector<ExtResult> h_results;
     std::vector<uint32_t> h_cigar;
     uint64_t total_cigar = 0;
+    uint64_t cells[4] = {0, 0, 0, 0};  // SW cells: forward byte, forward word, reverse byte, reverse word
 };
 
 // Runs jobs (already in ws.jobs, n of them) against the reads in nws.seq/nws.off.
 // Results and CIGARs are copied back into ws.h_results / ws.h_cigar.  Returns the
 // number of kernel launches.
 uint32_t run_extension(const DevRefs& refs, const NamWorkspace& nws, uint32_t k, const AlignScores& sc, uint32_t n,
-                       ExtWorkspace& ws, uint32_t max_qlen, cudaStream_t st);
+                       ExtWorkspace& ws, uint32_t max_qlen, cudaStream_t st, KernelTimers* kt = nullptr);
 
 }  // namespace sa

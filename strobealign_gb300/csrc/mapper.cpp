@@ -3,8 +3,10 @@
 // sequential per-chunk policy then consumes extension results produced in waves:
 // wave 0 extends each read's best NAMs speculatively, and every later wave runs
 // exactly the jobs that chunks stopped on (plus their likely successors).
+#include <atomic>
 #include <chrono>
 #include <cstring>
+#include <thread>
 
 #include "mapper.h"
 
@@ -85,7 +87,7 @@ void Mapper::nams_for_reads(uint32_t& launches) {
     cfg.mcs = mp_.mcs_strategy;
     cfg.rescue_distance = mp_.rescue_distance;
     launches += run_nam_pipeline(idx_->view(), refs_view_, cfg, n_reads_, total_bases_, max_contig_len_,
-                                 (uint32_t)refs_->contigs.size(), nws_, st_);
+                                 (uint32_t)refs_->contigs.size(), nws_, st_, &kt_);
     const uint64_t tn = nws_.last_total_nams;
     h_nam_off_.resize((size_t)n_reads_ + 1);
     h_nams_.resize(tn);
@@ -106,8 +108,9 @@ uint32_t Mapper::run_wave(ResultStore& store, uint32_t max_qlen) {
                             st_));
     h2d_bytes_ += (size_t)nj * sizeof(ExtJob);
     AlignScores sc{mp_.match, mp_.mismatch, mp_.gap_open, mp_.gap_extend, mp_.end_bonus};
-    uint32_t launches = run_extension(refs_view_, nws_, idx_->sp.k, sc, nj, ews_, max_qlen, st_);
+    uint32_t launches = run_extension(refs_view_, nws_, idx_->sp.k, sc, nj, ews_, max_qlen, st_, &kt_);
     d2h_bytes_ += (size_t)nj * sizeof(ExtResult) + ews_.total_cigar * 4;
+    for (int c = 0; c < 4; c++) sw_cells_[c] += ews_.cells[c];
     const uint32_t base_res = (uint32_t)store.results.size();
     const uint64_t base_cig = store.cigar.size();
     store.cigar.insert(store.cigar.end(), ews_.h_cigar.begin(), ews_.h_cigar.end());
@@ -188,6 +191,8 @@ void Mapper::map_uploaded(sa_output* out) {
     h2d_bytes_ = d2h_bytes_ = 0;
     jobs_run_ = 0;
     t_ext_ = 0;
+    kt_.reset();
+    for (int c = 0; c < 4; c++) sw_cells_[c] = 0;
     nams_for_reads(launches);
     auto t1 = std::chrono::steady_clock::now();
     bv.nams = h_nams_.data();
@@ -210,8 +215,29 @@ void Mapper::map_uploaded(sa_output* out) {
     }
     ResultStore store;
     store.per_read.resize(bv.reads.size());
-    Policy policy(pcfg_, contigs_, bv, store, &abundances_);
-    policy.seed_requests(0, nrec);
+    // chunks are independent (fresh RNG and insert-size state); policy passes run them
+    // on all host threads, requests are merged in chunk order
+    const unsigned nthreads = std::max(1u, std::min<unsigned>(policy_threads_, (unsigned)chunks.size()));
+    auto parallel = [&](auto&& fn) {
+        std::atomic<size_t> next{0};
+        auto worker = [&]() {
+            Policy policy(pcfg_, contigs_, bv, store);
+            for (;;) {
+                size_t c = next.fetch_add(1);
+                if (c >= chunks.size()) break;
+                fn(policy, chunks[c]);
+            }
+        };
+        std::vector<std::thread> th;
+        for (unsigned t = 1; t < nthreads; t++) th.emplace_back(worker);
+        worker();
+        for (auto& t : th) t.join();
+        for (auto& c : chunks) {
+            store.pending.insert(store.pending.end(), c.pending.begin(), c.pending.end());
+            c.pending.clear();
+        }
+    };
+    parallel([](Policy& p, ChunkState& c) { p.seed_requests(c); });
     uint32_t waves = 0;
     for (;;) {
         if (waves > 1000000) throw Error(SA_ERR_INVALID, "internal: extension waves do not converge");
@@ -221,15 +247,16 @@ void Mapper::map_uploaded(sa_output* out) {
             t_ext_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - tw).count();
             waves++;
         }
+        parallel([](Policy& p, ChunkState& c) {
+            if (!c.done) p.run_chunk(c);
+        });
         bool all_done = true;
-        for (auto& c : chunks)
-            if (!c.done) {
-                policy.run_chunk(c);
-                all_done = all_done && c.done;
-            }
+        for (auto& c : chunks) all_done = all_done && c.done;
         if (all_done) break;
         if (store.pending.empty()) throw Error(SA_ERR_INVALID, "internal: chunk stalled without a pending request");
     }
+    for (auto& c : chunks)
+        for (auto& a : c.abundance) abundances_[a.first] += a.second;
     size_t total_len = 0;
     uint64_t mapped = 0;
     for (auto& c : chunks) {
@@ -261,9 +288,15 @@ void Mapper::map_uploaded(sa_output* out) {
     stats_.n_waves = waves;
     stats_.n_launches = launches;
     stats_.h2d_bytes = h2d_bytes_;
-    stats_.d2h_bytes = d2h_bytes_ + total_len;
+    stats_.d2h_bytes = d2h_bytes_;
     stats_.n_nams = h_nams_.size();
     stats_.n_anchors = 0;
+    kt_.collect();
+    for (int c = 0; c < 4; c++) stats_.sw_cells[c] = sw_cells_[c];
+    for (int i = 0; i < 16; i++) {
+        stats_.kernel_ms[i] = i < KS_COUNT ? kt_.ms[i] : 0.0;
+        stats_.kernel_launches[i] = i < KS_COUNT ? kt_.launches[i] : 0;
+    }
 }
 
 }  // namespace sa

@@ -1,5 +1,7 @@
 // Batch driver state behind sa_mapper.
 #pragma once
+#include <thread>
+
 #include "policy.h"
 
 namespace sa {
@@ -34,6 +36,8 @@ class Mapper {
     uint32_t last_launches() const { return last_launches_; }
     uint32_t last_waves() const { return last_waves_; }
     uint64_t jobs_run() const { return jobs_run_; }
+    void set_policy_threads(unsigned n) { policy_threads_ = n ? n : 1; }
+    void set_profiling(bool on) { kt_.enabled = on; }
 
   private:
     uint32_t run_wave(ResultStore& store, uint32_t max_qlen);
@@ -42,6 +46,9 @@ class Mapper {
     uint32_t max_qlen_ = 1;
     sa_mapper_stats stats_{};
     double t_ext_ = 0;
+    KernelTimers kt_;
+    uint64_t sw_cells_[4] = {0, 0, 0, 0};
+    unsigned policy_threads_ = std::max(1u, std::thread::hardware_concurrency());
 
     const sa_index* idx_;
     const sa_refs* refs_;

@@ -758,7 +758,10 @@ void cub_excl_sum(NamWorkspace& ws, const T* in, T* out, uint64_t n, cudaStream_
 
 }  // namespace
 
-uint32_t run_seeding(const SeedParams& sp, uint32_t n, uint64_t total, NamWorkspace& ws, cudaStream_t st) {
+uint32_t run_seeding(const SeedParams& sp, uint32_t n, uint64_t total, NamWorkspace& ws, cudaStream_t st,
+                     KernelTimers* kt) {
+    KernelTimers none;
+    if (!kt) kt = &none;
     ws.syn_hash.reserve(total);
     ws.syn_pos.reserve(total);
     ws.qr_hash.reserve(2 * total);
@@ -767,16 +770,21 @@ uint32_t run_seeding(const SeedParams& sp, uint32_t n, uint64_t total, NamWorksp
     ws.qr_end.reserve(2 * total);
     ws.n_rs.reserve(2 * (size_t)n);
     size_t smem = WARPS_PER_BLOCK * MAX_READ_LEN;
+    kt->begin(KS_SEED, st);
     k_seed<<<warps_grid(n), 32 * WARPS_PER_BLOCK, smem, st>>>(ws.seq.p, ws.off.p, n, sp, ws.syn_hash.p, ws.syn_pos.p,
                                                               ws.qr_hash.p, ws.qr_hash_rc.p, ws.qr_start.p,
                                                               ws.qr_end.p, total, ws.n_rs.p);
+    kt->end(st);
     SA_CUDA(cudaGetLastError());
     return 1;
 }
 
 uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConfig& cfg, uint32_t n, uint64_t total,
-                          uint32_t max_contig_len, uint32_t n_contigs, NamWorkspace& ws, cudaStream_t st) {
+                          uint32_t max_contig_len, uint32_t n_contigs, NamWorkspace& ws, cudaStream_t st,
+                          KernelTimers* kt) {
     (void)refs;
+    KernelTimers none;
+    if (!kt) kt = &none;
     uint32_t launches = 0;
     if (!ws.log2_lut.p) {
         std::vector<float> lut(LOG2_LUT_SIZE);
@@ -789,24 +797,28 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     ap.pbits = ceil_log2((uint64_t)max_contig_len + 1);
     uint32_t rbits = ceil_log2((uint64_t)n_contigs);
     if (ap.qbits + ap.pbits + rbits > 64) throw Error(SA_ERR_INVALID, "contig count/length too large for anchor keys");
-    launches += run_seeding(ix.p, n, total, ws, st);
+    launches += run_seeding(ix.p, n, total, ws, st, kt);
     ws.hit_pos.reserve(2 * total);
     ws.hit_info.reserve(2 * total);
     ws.hit_count_cache.reserve(2 * total);
     ws.n_hits.reserve(2 * (size_t)n);
     ws.orient.reserve(n);
     ws.details.reserve(n);
+    kt->begin(KS_HITS, st);
     k_hits<<<warps_grid(n), 32 * WARPS_PER_BLOCK, 0, st>>>(
         ix, ws.off.p, n, total, cfg.mcs, cfg.rescue_distance, ws.qr_hash.p, ws.qr_hash_rc.p, ws.qr_start.p,
         ws.qr_end.p, ws.n_rs.p, ws.hit_pos.p, ws.hit_info.p, ws.hit_count_cache.p, ws.n_hits.p, ws.orient.p,
         ws.details.p);
+    kt->end(st);
     launches++;
     ws.hit_anchors.reserve(2 * total);
     ws.seg_count.reserve(2 * (size_t)n + 1);
     ws.seg_off.reserve(2 * (size_t)n + 1);
+    kt->begin(KS_ANCHORS, st);
     k_anchors<false><<<warps_grid(n), 32 * WARPS_PER_BLOCK, 0, st>>>(
         ix, ws.off.p, n, total, ws.qr_hash.p, ws.qr_start.p, ws.qr_end.p, ws.hit_pos.p, ws.hit_info.p, ws.n_hits.p,
         ws.orient.p, ws.hit_anchors.p, ws.seg_count.p, nullptr, nullptr, ap, ws.details.p);
+    kt->end(st);
     launches++;
     SA_CUDA(cudaMemsetAsync(ws.seg_count.p + 2 * (size_t)n, 0, 8, st));
     cub_excl_sum(ws, ws.seg_count.p, ws.seg_off.p, 2 * (uint64_t)n + 1, st);
@@ -816,18 +828,22 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     SA_CUDA(cudaStreamSynchronize(st));
     ws.anchors.reserve(total_anchors);
     ws.anchors_sorted.reserve(total_anchors);
+    kt->begin(KS_ANCHORS, st);
     k_anchors<true><<<warps_grid(n), 32 * WARPS_PER_BLOCK, 0, st>>>(
         ix, ws.off.p, n, total, ws.qr_hash.p, ws.qr_start.p, ws.qr_end.p, ws.hit_pos.p, ws.hit_info.p, ws.n_hits.p,
         ws.orient.p, ws.hit_anchors.p, nullptr, ws.seg_off.p, ws.anchors.p, ap, ws.details.p);
+    kt->end(st);
     launches++;
     if (total_anchors) {
         size_t tmp = 0;
+        kt->begin(KS_SORT, st);
         cub::DeviceSegmentedSort::SortKeys(nullptr, tmp, ws.anchors.p, ws.anchors_sorted.p, (int64_t)total_anchors,
                                            (int64_t)(2 * (uint64_t)n), ws.seg_off.p, ws.seg_off.p + 1, st);
         ws.cub_tmp.reserve(tmp);
         cub::DeviceSegmentedSort::SortKeys(ws.cub_tmp.p, tmp, ws.anchors.p, ws.anchors_sorted.p,
                                            (int64_t)total_anchors, (int64_t)(2 * (uint64_t)n), ws.seg_off.p,
                                            ws.seg_off.p + 1, st);
+        kt->end(st);
         launches++;
     }
     ws.dp.reserve(total_anchors);
@@ -836,9 +852,11 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     ws.nam_scratch.reserve(total_anchors);
     ws.nam_seg_count.reserve(2 * (size_t)n);
     ChainCtx cc{cfg.cp, ix.p.k, ws.log2_lut.p};
+    kt->begin(KS_CHAIN, st);
     k_chain<<<warps_grid(2 * (uint64_t)n), 32 * WARPS_PER_BLOCK, 0, st>>>(
         ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p, total_anchors, ap,
         cc, ws.nam_scratch.p, ws.nam_seg_count.p);
+    kt->end(st);
     launches++;
     ws.nam_count.reserve((size_t)n + 1);
     ws.nam_off.reserve((size_t)n + 1);

@@ -1,6 +1,7 @@
 // Device pipelines: NAM finding (nams.cu) and extension (extend.cu).
 #pragma once
 #include "host_state.h"
+#include "ktimer.h"
 
 namespace sa {
 
@@ -58,9 +59,11 @@ struct NamConfig {
 // NAMs (stable-sorted by score, descending) in ws.nams at ws.nam_off, and per-read
 // statistics in ws.details.  Returns the number of kernel launches issued.
 uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConfig& cfg, uint32_t n, uint64_t total,
-                          uint32_t max_contig_len, uint32_t n_contigs, NamWorkspace& ws, cudaStream_t st);
+                          uint32_t max_contig_len, uint32_t n_contigs, NamWorkspace& ws, cudaStream_t st,
+                          KernelTimers* kt = nullptr);
 
 // Randstrobes only (stage entry point).
-uint32_t run_seeding(const SeedParams& sp, uint32_t n, uint64_t total, NamWorkspace& ws, cudaStream_t st);
+uint32_t run_seeding(const SeedParams& sp, uint32_t n, uint64_t total, NamWorkspace& ws, cudaStream_t st,
+                     KernelTimers* kt = nullptr);
 
 }  // namespace sa

@@ -461,7 +461,7 @@ void Policy::want(uint32_t read, const ExtJob& job, const JobKey& key) {
     v.push_back(ResultStore::Entry{key, UINT32_MAX});
     ExtJob j = job;
     j.tag = (uint32_t)(v.size() - 1);
-    store_.pending.push_back(j);
+    cur_->pending.push_back(j);
 }
 
 const ExtResult& Policy::get(uint32_t read, const ExtJob& job, const JobKey& key) {
@@ -1135,7 +1135,7 @@ void Policy::aemb_se(uint64_t rec, Rng& rng) {
     size_t nb = 0;
     while (nb < nams.size() && nams[nb].score == nams[0].score) nb++;
     double w = (double)bv_.reads[rec].len / (double)nb;
-    for (size_t i = 0; i < nb; i++) (*ab_)[nams[i].ref_id] += w;
+    for (size_t i = 0; i < nb; i++) add_abundance(nams[i].ref_id, w);
 }
 
 // src/maponly.rs:198-261
@@ -1153,8 +1153,8 @@ void Policy::aemb_pe(uint64_t rec, Rng& rng, InsertSize& isd) {
         while (nb < pairs.size() && pairs[nb].score == js) nb++;
         double w1 = (double)bv_.reads[a].len / (double)nb, w2 = (double)bv_.reads[b].len / (double)nb;
         for (size_t i = 0; i < nb; i++) {
-            (*ab_)[pairs[i].n1.ref_id] += w1;
-            (*ab_)[pairs[i].n2.ref_id] += w2;
+            add_abundance(pairs[i].n1.ref_id, w1);
+            add_abundance(pairs[i].n2.ref_id, w2);
         }
     } else {
         const std::vector<NamRec>* lists[2] = {&n1, &n2};
@@ -1164,16 +1164,17 @@ void Policy::aemb_pe(uint64_t rec, Rng& rng, InsertSize& isd) {
             size_t nb = 0;
             while (nb < n.size() && n[nb].score == n[0].score) nb++;
             double w = (double)lens[t] / (double)nb;
-            for (size_t i = 0; i < nb; i++) (*ab_)[n[i].ref_id] += w;
+            for (size_t i = 0; i < nb; i++) add_abundance(n[i].ref_id, w);
         }
     }
 }
 
 // ------------------------------------------------------------------ chunk driver
-void Policy::seed_requests(uint64_t first, uint64_t end) {
+void Policy::seed_requests(ChunkState& cs) {
     if (cfg_.mp.mode != SA_MODE_SAM) return;
+    cur_ = &cs;
     const bool paired = bv_.paired;
-    for (uint64_t rec = first; rec < end; rec++) {
+    for (uint64_t rec = cs.first; rec < cs.end; rec++) {
         for (int m = 0; m < (paired ? 2 : 1); m++) {
             uint32_t read = paired ? (uint32_t)(2 * rec + m) : (uint32_t)rec;
             const NamRec* n = bv_.nams + bv_.nam_off[read];
@@ -1190,29 +1191,51 @@ void Policy::seed_requests(uint64_t first, uint64_t end) {
 }
 
 void Policy::run_chunk(ChunkState& cs) {
+    cur_ = &cs;
+    auto one = [&](uint64_t rec, Rng& rng, InsertSize& isd, std::string& out, uint64_t& mapped) {
+        switch (cfg_.mp.mode) {
+            case SA_MODE_SAM:
+                if (bv_.paired) pe_record(rec, rng, isd, out, mapped);
+                else se_record(rec, rng, out, mapped);
+                break;
+            case SA_MODE_PAF:
+                if (bv_.paired) paf_pe(rec, rng, isd, out);
+                else paf_se(rec, rng, out);
+                break;
+            default:
+                if (bv_.paired) aemb_pe(rec, rng, isd);
+                else aemb_se(rec, rng);
+                break;
+        }
+    };
     while (cs.next < cs.end) {
         Rng rng = cs.rng;
         InsertSize isd = cs.isd;
-        size_t out_len = cs.out.size();
+        size_t out_len = cs.out.size(), ab_len = cs.abundance.size();
         uint64_t mapped = 0;
-        std::vector<double> ab_save;
         try {
-            switch (cfg_.mp.mode) {
-                case SA_MODE_SAM:
-                    if (bv_.paired) pe_record(cs.next, rng, isd, cs.out, mapped);
-                    else se_record(cs.next, rng, cs.out, mapped);
-                    break;
-                case SA_MODE_PAF:
-                    if (bv_.paired) paf_pe(cs.next, rng, isd, cs.out);
-                    else paf_se(cs.next, rng, cs.out);
-                    break;
-                default:
-                    if (bv_.paired) aemb_pe(cs.next, rng, isd);
-                    else aemb_se(cs.next, rng);
-                    break;
-            }
+            one(cs.next, rng, isd, cs.out, mapped);
         } catch (const Miss&) {
             cs.out.resize(out_len);
+            cs.abundance.resize(ab_len);
+            // look ahead: later reads of the chunk with the best-known state
+            speculative_ = true;
+            Rng srng = cs.rng;
+            InsertSize sisd = cs.isd;
+            std::string scratch;
+            for (uint64_t rec = cs.next + 1; rec < cs.end; rec++) {
+                Rng r2 = srng;
+                InsertSize i2 = sisd;
+                uint64_t m2 = 0;
+                try {
+                    one(rec, r2, i2, scratch, m2);
+                    srng = r2;
+                    sisd = i2;
+                } catch (const Miss&) {
+                }
+                scratch.clear();
+            }
+            speculative_ = false;
             return;
         }
         cs.rng = rng;

@@ -101,24 +101,31 @@ struct ChunkState {
     std::string out;
     uint64_t mapped = 0;
     bool done = false;
+    std::vector<ExtJob> pending;                          // requests raised by this chunk
+    std::vector<std::pair<uint32_t, double>> abundance;   // (contig, weight) in read order
 };
 
 class Policy {
   public:
-    Policy(const PolicyConfig& cfg, const std::vector<ContigInfo>& contigs, const BatchView& bv, ResultStore& store,
-           std::vector<double>* abundances)
-        : cfg_(cfg), contigs_(contigs), bv_(bv), store_(store), ab_(abundances) {}
-    // Advance one chunk as far as the available results allow.
+    Policy(const PolicyConfig& cfg, const std::vector<ContigInfo>& contigs, const BatchView& bv, ResultStore& store)
+        : cfg_(cfg), contigs_(contigs), bv_(bv), store_(store) {}
+    // Advance one chunk as far as the available results allow.  On a miss, the
+    // rest of the chunk is evaluated speculatively (state copies, output dropped)
+    // so that the jobs of later reads join the next wave.
     void run_chunk(ChunkState& cs);
-    // Speculative first-wave requests for every read of the batch.
-    void seed_requests(uint64_t first_record, uint64_t end_record);
+    // Speculative first-wave requests for the reads of one chunk.
+    void seed_requests(ChunkState& cs);
 
   private:
     const PolicyConfig& cfg_;
     const std::vector<ContigInfo>& contigs_;
     const BatchView& bv_;
     ResultStore& store_;
-    std::vector<double>* ab_;
+    ChunkState* cur_ = nullptr;
+    bool speculative_ = false;
+    void add_abundance(uint32_t ref_id, double w) {
+        if (!speculative_) cur_->abundance.emplace_back(ref_id, w);
+    }
 
     void want(uint32_t read, const ExtJob& job, const JobKey& key);
     const ExtResult* lookup(uint32_t read, const JobKey& key) const;
