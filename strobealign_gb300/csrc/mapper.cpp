@@ -1,11 +1,16 @@
 // Batch driver: Mapper::map_chunk (src/main.rs:873-988) for a whole batch on one
 // GPU.  NAMs for every read come from one pass of the device pipeline; the
 // sequential per-chunk policy then consumes extension results produced in waves:
-// wave 0 extends each read's best NAMs speculatively, and every later wave runs
-// exactly the jobs that chunks stopped on (plus their likely successors).
-#include <atomic>
+// the first requests of a chunk extend each read's best NAMs speculatively, and
+// later ones are exactly the jobs the chunk stopped on (plus their likely
+// successors).  Waves are batched continuously across chunks (Mapper::schedule).
+#include <algorithm>
 #include <chrono>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
+#include <exception>
+#include <mutex>
 #include <thread>
 
 #include "mapper.h"
@@ -100,28 +105,26 @@ void Mapper::nams_for_reads(uint32_t& launches) {
     d2h_bytes_ += ((size_t)n_reads_ + 1) * 8 + tn * sizeof(NamRec) + (size_t)n_reads_ * sizeof(NamDetailsRec);
 }
 
-uint32_t Mapper::run_wave(ResultStore& store, uint32_t max_qlen) {
-    const uint32_t nj = (uint32_t)store.pending.size();
+uint32_t Mapper::run_wave(ResultStore& store, const std::vector<ExtJob>& jobs, uint32_t max_qlen) {
+    const uint32_t nj = (uint32_t)jobs.size();
     if (!nj) return 0;
     ews_.jobs.reserve(nj);
-    SA_CUDA(cudaMemcpyAsync(ews_.jobs.p, store.pending.data(), (size_t)nj * sizeof(ExtJob), cudaMemcpyHostToDevice,
-                            st_));
+    SA_CUDA(cudaMemcpyAsync(ews_.jobs.p, jobs.data(), (size_t)nj * sizeof(ExtJob), cudaMemcpyHostToDevice, st_));
     h2d_bytes_ += (size_t)nj * sizeof(ExtJob);
     AlignScores sc{mp_.match, mp_.mismatch, mp_.gap_open, mp_.gap_extend, mp_.end_bonus};
     uint32_t launches = run_extension(refs_view_, nws_, idx_->sp.k, sc, nj, ews_, max_qlen, st_, &kt_);
     d2h_bytes_ += (size_t)nj * sizeof(ExtResult) + ews_.total_cigar * 4;
     for (int c = 0; c < 4; c++) sw_cells_[c] += ews_.cells[c];
-    const uint32_t base_res = (uint32_t)store.results.size();
-    const uint64_t base_cig = store.cigar.size();
-    store.cigar.insert(store.cigar.end(), ews_.h_cigar.begin(), ews_.h_cigar.end());
+    store.cigars.emplace_back(ews_.h_cigar.begin(), ews_.h_cigar.end());
+    const uint32_t* cig = store.cigars.back().data();
     for (uint32_t j = 0; j < nj; j++) {
-        ExtResult r = ews_.h_results[j];
-        r.cigar_offset = (uint32_t)(base_cig + r.cigar_offset);
+        StoredResult r;
+        static_cast<ExtResult&>(r) = ews_.h_results[j];
+        r.cigar = cig + r.cigar_offset;
         store.results.push_back(r);
-        const ExtJob& jb = store.pending[j];
-        store.per_read[jb.read][jb.tag].result = base_res + j;
+        const ExtJob& jb = jobs[j];
+        store.per_read[jb.read][jb.tag].result = &store.results.back();
     }
-    store.pending.clear();
     jobs_run_ += nj;
     return launches;
 }
@@ -181,6 +184,127 @@ void Mapper::map(const sa_read_batch* r1, const sa_read_batch* r2, sa_output* ou
     stats_.seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
+// Continuous batching of extension work.  Chunks are independent (fresh RNG and
+// insert-size state, src/main.rs:878-880), so policy threads run whichever chunks
+// have their results, while this thread gathers the requests of the chunks that
+// stopped on a miss into the next extension wave.  A wave starts once enough jobs
+// are waiting, or as soon as no policy thread could add more.  Which jobs share a
+// wave depends on timing; results do not (each job is a pure function of its
+// inputs, and the output of every chunk depends only on the results it reads).
+uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, ResultStore& store, uint32_t& launches) {
+    const size_t nchunks = chunks.size();
+    const unsigned nthreads = std::max(1u, std::min<unsigned>(policy_threads_, (unsigned)nchunks));
+    std::mutex mu;
+    std::condition_variable cv_work, cv_ext;
+    std::deque<size_t> ready;       // chunks that can run
+    std::vector<size_t> waiting;    // chunks whose requests are not yet in a wave
+    size_t waiting_jobs = 0, n_done = 0;
+    unsigned running = 0;
+    std::exception_ptr err;
+    bool stop = false;
+    for (size_t c = 0; c < nchunks; c++) ready.push_back(c);
+    std::vector<bool> is_seeded(nchunks, false);
+
+    auto worker = [&]() {
+        Policy policy(pcfg_, contigs_, bv_, store);
+        std::unique_lock<std::mutex> lk(mu);
+        for (;;) {
+            cv_work.wait(lk, [&] { return stop || !ready.empty(); });
+            if (stop) return;
+            const size_t c = ready.front();
+            ready.pop_front();
+            running++;
+            const bool first = !is_seeded[c];
+            is_seeded[c] = true;
+            lk.unlock();
+            ChunkState& cs = chunks[c];
+            try {
+                if (first)
+                    policy.seed_requests(cs);
+                else
+                    policy.run_chunk(cs);
+            } catch (...) {
+                lk.lock();
+                if (!err) err = std::current_exception();
+                stop = true;
+                running--;
+                cv_work.notify_all();
+                cv_ext.notify_all();
+                return;
+            }
+            lk.lock();
+            running--;
+            if (!first && cs.done) {
+                n_done++;
+            } else if (cs.pending.empty()) {
+                // nothing requested: a seeded chunk runs at once; a stalled one is a bug
+                if (!first) {
+                    if (!err)
+                        err = std::make_exception_ptr(
+                            Error(SA_ERR_INVALID, "internal: chunk stalled without a pending request"));
+                    stop = true;
+                    cv_work.notify_all();
+                } else {
+                    ready.push_back(c);
+                    cv_work.notify_one();
+                }
+            } else {
+                waiting.push_back(c);
+                waiting_jobs += cs.pending.size();
+            }
+            cv_ext.notify_one();
+        }
+    };
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nthreads; t++) th.emplace_back(worker);
+
+    uint32_t waves = 0;
+    std::vector<ExtJob> jobs;
+    std::vector<size_t> batch;
+    try {
+        std::unique_lock<std::mutex> lk(mu);
+        for (;;) {
+            // start a wave when the policy threads cannot add more, or enough has queued
+            cv_ext.wait(lk, [&] {
+                if (stop || n_done == nchunks) return true;
+                if (waiting.empty()) return false;
+                const bool idle = running == 0 && ready.empty();
+                return idle || waiting_jobs >= wave_min_jobs_;
+            });
+            if (stop || n_done == nchunks) break;
+            batch.swap(waiting);
+            waiting.clear();
+            waiting_jobs = 0;
+            lk.unlock();
+            // chunk order inside a wave keeps waves reproducible for a given grouping
+            std::sort(batch.begin(), batch.end());
+            jobs.clear();
+            for (size_t c : batch) {
+                jobs.insert(jobs.end(), chunks[c].pending.begin(), chunks[c].pending.end());
+                chunks[c].pending.clear();
+            }
+            if (waves > 1000000) throw Error(SA_ERR_INVALID, "internal: extension waves do not converge");
+            auto tw = std::chrono::steady_clock::now();
+            launches += run_wave(store, jobs, max_qlen_);
+            t_ext_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - tw).count();
+            waves++;
+            lk.lock();
+            for (size_t c : batch) ready.push_back(c);
+            cv_work.notify_all();
+        }
+        stop = true;
+        cv_work.notify_all();
+    } catch (...) {
+        std::lock_guard<std::mutex> g(mu);
+        if (!err) err = std::current_exception();
+        stop = true;
+        cv_work.notify_all();
+    }
+    for (auto& t : th) t.join();
+    if (err) std::rethrow_exception(err);
+    return waves;
+}
+
 void Mapper::map_uploaded(sa_output* out) {
     if (!have_batch_) throw Error(SA_ERR_INVALID, "no uploaded batch");
     auto t0 = std::chrono::steady_clock::now();
@@ -215,46 +339,7 @@ void Mapper::map_uploaded(sa_output* out) {
     }
     ResultStore store;
     store.per_read.resize(bv.reads.size());
-    // chunks are independent (fresh RNG and insert-size state); policy passes run them
-    // on all host threads, requests are merged in chunk order
-    const unsigned nthreads = std::max(1u, std::min<unsigned>(policy_threads_, (unsigned)chunks.size()));
-    auto parallel = [&](auto&& fn) {
-        std::atomic<size_t> next{0};
-        auto worker = [&]() {
-            Policy policy(pcfg_, contigs_, bv, store);
-            for (;;) {
-                size_t c = next.fetch_add(1);
-                if (c >= chunks.size()) break;
-                fn(policy, chunks[c]);
-            }
-        };
-        std::vector<std::thread> th;
-        for (unsigned t = 1; t < nthreads; t++) th.emplace_back(worker);
-        worker();
-        for (auto& t : th) t.join();
-        for (auto& c : chunks) {
-            store.pending.insert(store.pending.end(), c.pending.begin(), c.pending.end());
-            c.pending.clear();
-        }
-    };
-    parallel([](Policy& p, ChunkState& c) { p.seed_requests(c); });
-    uint32_t waves = 0;
-    for (;;) {
-        if (waves > 1000000) throw Error(SA_ERR_INVALID, "internal: extension waves do not converge");
-        if (!store.pending.empty()) {
-            auto tw = std::chrono::steady_clock::now();
-            launches += run_wave(store, max_qlen_);
-            t_ext_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - tw).count();
-            waves++;
-        }
-        parallel([](Policy& p, ChunkState& c) {
-            if (!c.done) p.run_chunk(c);
-        });
-        bool all_done = true;
-        for (auto& c : chunks) all_done = all_done && c.done;
-        if (all_done) break;
-        if (store.pending.empty()) throw Error(SA_ERR_INVALID, "internal: chunk stalled without a pending request");
-    }
+    const uint32_t waves = schedule(chunks, store, launches);
     for (auto& c : chunks)
         for (auto& a : c.abundance) abundances_[a.first] += a.second;
     size_t total_len = 0;
@@ -282,7 +367,7 @@ void Mapper::map_uploaded(sa_output* out) {
     last_seconds_ = std::chrono::duration<double>(t2 - t0).count();
     stats_.seconds_nams = std::chrono::duration<double>(t1 - t0).count();
     stats_.seconds_extension = t_ext_;
-    stats_.seconds_policy = std::chrono::duration<double>(t2 - t1).count() - t_ext_;
+    stats_.seconds_policy = std::max(0.0, std::chrono::duration<double>(t2 - t1).count() - t_ext_);
     stats_.seconds_total = last_seconds_;
     stats_.n_jobs = jobs_run_;
     stats_.n_waves = waves;

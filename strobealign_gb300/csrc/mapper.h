@@ -38,9 +38,11 @@ class Mapper {
     uint64_t jobs_run() const { return jobs_run_; }
     void set_policy_threads(unsigned n) { policy_threads_ = n ? n : 1; }
     void set_profiling(bool on) { kt_.enabled = on; }
+    void set_wave_min_jobs(uint64_t n) { wave_min_jobs_ = n; }
 
   private:
-    uint32_t run_wave(ResultStore& store, uint32_t max_qlen);
+    uint32_t run_wave(ResultStore& store, const std::vector<ExtJob>& jobs, uint32_t max_qlen);
+    uint32_t schedule(std::vector<ChunkState>& chunks, ResultStore& store, uint32_t& launches);
     BatchView bv_;
     bool have_batch_ = false;
     uint32_t max_qlen_ = 1;
@@ -49,6 +51,7 @@ class Mapper {
     KernelTimers kt_;
     uint64_t sw_cells_[4] = {0, 0, 0, 0};
     unsigned policy_threads_ = std::max(1u, std::thread::hardware_concurrency());
+    uint64_t wave_min_jobs_ = 32768;
 
     const sa_index* idx_;
     const sa_refs* refs_;

@@ -433,21 +433,21 @@ void add_details(Details& a, const Details& b) {
 }  // namespace
 
 // ------------------------------------------------------------------ result access
-const ExtResult* Policy::lookup(uint32_t read, const JobKey& key) const {
+const StoredResult* Policy::lookup(uint32_t read, const JobKey& key) const {
     const auto& v = store_.per_read[read];
-    auto find = [&](const JobKey& k) -> const ExtResult* {
+    auto find = [&](const JobKey& k) -> const StoredResult* {
         for (auto& e : v)
-            if (e.key == k && e.result != UINT32_MAX) return &store_.results[e.result];
+            if (e.key == k && e.result) return e.result;
         return nullptr;
     };
-    if (const ExtResult* r = find(key)) return r;
+    if (const StoredResult* r = find(key)) return r;
     // extend_seed after is_consistent and after reverse_nam_if_needed coincide whenever
     // the latter does not flip the NAM
     if (key.kind == JOB_EXTEND_FULL) {
-        const ExtResult* f = find(JobKey{JOB_EXTEND_FAST, key.a, 0, 0, 0});
+        const StoredResult* f = find(JobKey{JOB_EXTEND_FAST, key.a, 0, 0, 0});
         if (f && f->consistent) return f;
     } else if (key.kind == JOB_EXTEND_FAST) {
-        const ExtResult* f = find(JobKey{JOB_EXTEND_FULL, key.a, 0, 0, 0});
+        const StoredResult* f = find(JobKey{JOB_EXTEND_FULL, key.a, 0, 0, 0});
         if (f && !f->flipped) return f;
     }
     return nullptr;
@@ -458,14 +458,14 @@ void Policy::want(uint32_t read, const ExtJob& job, const JobKey& key) {
     auto& v = store_.per_read[read];
     for (auto& e : v)
         if (e.key == key) return;  // pending
-    v.push_back(ResultStore::Entry{key, UINT32_MAX});
+    v.push_back(ResultStore::Entry{key, nullptr});
     ExtJob j = job;
     j.tag = (uint32_t)(v.size() - 1);
     cur_->pending.push_back(j);
 }
 
-const ExtResult& Policy::get(uint32_t read, const ExtJob& job, const JobKey& key) {
-    if (const ExtResult* r = lookup(read, key)) return *r;
+const StoredResult& Policy::get(uint32_t read, const ExtJob& job, const JobKey& key) {
+    if (const StoredResult* r = lookup(read, key)) return *r;
     want(read, job, key);
     throw Miss{};
 }
@@ -491,7 +491,7 @@ ExtJob Policy::nam_job(uint32_t read, const NamRec& cur, uint32_t kind) const {
 
 void Policy::want_nam(uint32_t read, const NamRec& n, uint32_t kind) { want(read, nam_job(read, n, kind), nam_key(n, kind)); }
 
-Alignment Policy::to_alignment(const ExtResult& r, uint32_t ref_id) const {
+Alignment Policy::to_alignment(const StoredResult& r, uint32_t ref_id) const {
     Alignment a;
     a.reference_id = ref_id;
     a.ref_start = r.ref_start;
@@ -502,13 +502,13 @@ Alignment Policy::to_alignment(const ExtResult& r, uint32_t ref_id) const {
     a.length = r.length;
     a.is_revcomp = r.is_revcomp != 0;
     a.gapped = r.gapped != 0;
-    a.cigar = store_.cigar.data() + r.cigar_offset;
+    a.cigar = r.cigar;
     a.cigar_len = r.cigar_len;
     return a;
 }
 
 bool Policy::extend(uint32_t read, NamRec& nam, uint32_t kind, Alignment& out, bool& consistent) {
-    const ExtResult& r = get(read, nam_job(read, nam, kind), nam_key(nam, kind));
+    const StoredResult& r = get(read, nam_job(read, nam, kind), nam_key(nam, kind));
     consistent = r.consistent != 0;
     if (kind == JOB_EXTEND_FULL) {
         nam.is_revcomp = r.nam_is_revcomp;
@@ -550,7 +550,7 @@ bool Policy::rescue(uint32_t read, const NamRec& mate, float mu, float sigma, Al
     j.ref_end = (uint32_t)re;
     j.is_revcomp = rc;
     j.use_ssw = 1;
-    const ExtResult& r = get(read, j, JobKey{JOB_RESCUE, mate.ref_id, (uint32_t)rs, (uint32_t)re, rc ? 1u : 0u});
+    const StoredResult& r = get(read, j, JobKey{JOB_RESCUE, mate.ref_id, (uint32_t)rs, (uint32_t)re, rc ? 1u : 0u});
     if (!r.valid) return false;
     out = to_alignment(r, mate.ref_id);
     return true;
@@ -577,7 +577,7 @@ void Policy::se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mappe
     Details details;
     details.nam = bv_.details[read];
     if (nams.empty()) {
-        if (cfg_.mp.output_unmapped) format_sam(unmapped_record(rv, details), cfg_, out);
+        if (cfg_.mp.output_unmapped && !speculative_) format_sam(unmapped_record(rv, details), cfg_, out);
         return;
     }
     const float nam_max = nams[0].score;
@@ -633,11 +633,11 @@ void Policy::se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mappe
         if (cfg_.mp.max_secondary > 0) alignments.push_back(a);
     }
     if (!have_best) {
-        if (cfg_.mp.output_unmapped) format_sam(unmapped_record(rv, details), cfg_, out);
+        if (cfg_.mp.output_unmapped && !speculative_) format_sam(unmapped_record(rv, details), cfg_, out);
         return;
     }
     uint8_t mapq = (uint8_t)((60 * (best_score - second) + best_score - 1) / best_score);
-    format_sam(mapped_record(*this, best, rv, mapq, false, details), cfg_, out);
+    if (!speculative_) format_sam(mapped_record(*this, best, rv, mapq, false, details), cfg_, out);
     mapped++;
     if (cfg_.mp.max_secondary > 0) {
         alignments[best_index] = alignments.back();
@@ -649,7 +649,7 @@ void Policy::se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mappe
             const Alignment& a = alignments[t];
             uint32_t d = a.score > best_score ? a.score - best_score : 0;
             if (d > lim) break;
-            format_sam(mapped_record(*this, a, rv, mapq, true, details), cfg_, out);
+            if (!speculative_) format_sam(mapped_record(*this, a, rv, mapq, true, details), cfg_, out);
         }
     }
 }
@@ -816,7 +816,7 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
                     } else {
                         NamRec other = *nm[1 - i];
                         // reverse_nam_if_needed on the partner, then rescue from it
-                        const ExtResult& fr = get(rd[1 - i], nam_job(rd[1 - i], other, JOB_EXTEND_FULL),
+                        const StoredResult& fr = get(rd[1 - i], nam_job(rd[1 - i], other, JOB_EXTEND_FULL),
                                                   nam_key(other, JOB_EXTEND_FULL));
                         det[1 - i].inconsistent_nams += !fr.consistent;
                         other.is_revcomp = fr.nam_is_revcomp;
@@ -947,7 +947,7 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
     }
     if (!cfg_.mp.output_unmapped && recs.size() >= 2 && !recs[0].is_mapped() && !recs[1].is_mapped()) recs.clear();
     for (auto& r : recs) {
-        format_sam(r, cfg_, out);
+        if (!speculative_) format_sam(r, cfg_, out);
         mapped += r.is_mapped();
     }
 }
@@ -1218,12 +1218,14 @@ void Policy::run_chunk(ChunkState& cs) {
         } catch (const Miss&) {
             cs.out.resize(out_len);
             cs.abundance.resize(ab_len);
-            // look ahead: later reads of the chunk with the best-known state
+            // look ahead: later reads of the chunk with the best-known state; after the
+            // first lookahead only the reads that missed in the previous one are revisited
             speculative_ = true;
             Rng srng = cs.rng;
             InsertSize sisd = cs.isd;
             std::string scratch;
-            for (uint64_t rec = cs.next + 1; rec < cs.end; rec++) {
+            std::vector<uint64_t> todo;
+            auto visit = [&](uint64_t rec) {
                 Rng r2 = srng;
                 InsertSize i2 = sisd;
                 uint64_t m2 = 0;
@@ -1232,9 +1234,17 @@ void Policy::run_chunk(ChunkState& cs) {
                     srng = r2;
                     sisd = i2;
                 } catch (const Miss&) {
+                    todo.push_back(rec);
                 }
-                scratch.clear();
+            };
+            if (!cs.lookahead_started) {
+                for (uint64_t rec = cs.next + 1; rec < cs.end; rec++) visit(rec);
+                cs.lookahead_started = true;
+            } else {
+                for (uint64_t rec : cs.lookahead_todo)
+                    if (rec > cs.next) visit(rec);
             }
+            cs.lookahead_todo.swap(todo);
             speculative_ = false;
             return;
         }

@@ -4,6 +4,7 @@
 // runs another extension wave and resumes the chunk at the read that missed.
 #pragma once
 #include <cstdint>
+#include <deque>
 #include <string>
 #include <vector>
 
@@ -51,16 +52,25 @@ struct JobKey {
 
 struct Miss {};
 
-// Extension results of one batch, accumulated over waves.
+// One extension result as the host keeps it: the device record plus the address
+// of its CIGAR in the wave's host copy.
+struct StoredResult : ExtResult {
+    const uint32_t* cigar = nullptr;
+};
+
+// Extension results of one batch, accumulated over waves.  Storage is stable:
+// waves append (deque elements never move), so policy threads keep reading the
+// results they hold while the extension thread appends the next wave.  An entry of
+// per_read[r] is written only by the thread that runs the chunk owning read r, or
+// by the extension thread while that chunk waits for the wave.
 struct ResultStore {
     struct Entry {
         JobKey key;
-        uint32_t result;  // index into results, or UINT32_MAX while pending
+        const StoredResult* result;  // nullptr while pending
     };
     std::vector<std::vector<Entry>> per_read;
-    std::vector<ExtResult> results;
-    std::vector<uint32_t> cigar;
-    std::vector<ExtJob> pending;  // requests of the wave being assembled
+    std::deque<StoredResult> results;
+    std::deque<std::vector<uint32_t>> cigars;  // one per wave
 };
 
 struct ReadView {
@@ -103,6 +113,8 @@ struct ChunkState {
     bool done = false;
     std::vector<ExtJob> pending;                          // requests raised by this chunk
     std::vector<std::pair<uint32_t, double>> abundance;   // (contig, weight) in read order
+    bool lookahead_started = false;
+    std::vector<uint64_t> lookahead_todo;                 // reads that missed in the last lookahead
 };
 
 class Policy {
@@ -128,8 +140,8 @@ class Policy {
     }
 
     void want(uint32_t read, const ExtJob& job, const JobKey& key);
-    const ExtResult* lookup(uint32_t read, const JobKey& key) const;
-    const ExtResult& get(uint32_t read, const ExtJob& job, const JobKey& key);
+    const StoredResult* lookup(uint32_t read, const JobKey& key) const;
+    const StoredResult& get(uint32_t read, const ExtJob& job, const JobKey& key);
 
     void se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mapped);
     void pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out, uint64_t& mapped);
@@ -143,7 +155,7 @@ class Policy {
     std::vector<NamRec> sorted_nams(uint32_t read, Rng& rng) const;
     ExtJob nam_job(uint32_t read, const NamRec& n, uint32_t kind) const;
     static JobKey nam_key(const NamRec& n, uint32_t kind) { return JobKey{kind, n.nam_id, 0, 0, 0}; }
-    Alignment to_alignment(const ExtResult& r, uint32_t ref_id) const;
+    Alignment to_alignment(const StoredResult& r, uint32_t ref_id) const;
     const PolicyConfig& cfg() const { return cfg_; }
     const std::vector<ContigInfo>& contigs() const { return contigs_; }
     const BatchView& bv() const { return bv_; }
