@@ -177,6 +177,48 @@ typedef struct {
 int32_t sa_randstrobes_batch(const sa_index* idx, const sa_read_batch* reads, sa_query_randstrobe* out,
                              size_t capacity, uint64_t* out_offsets, uint32_t* out_counts);
 
+/* Allocation-free seeding.  No counterpart in the reference: it computes what
+ * sa_randstrobes_batch computes, for reads already in device memory, into device
+ * buffers the caller owns, and allocates nothing (no cudaMalloc/cudaFree, no
+ * pinned or pooled memory).  It is for callers that cannot allocate on the device
+ * at this point: cudaMalloc and cudaFree synchronise the whole device, which
+ * stalls a caller keeping other streams busy, and a caller that has reserved all
+ * device memory up front (index, batches, a memory pool of its own) has none left
+ * to give.
+ *
+ * The syncmer scratch is a static device array of SA_RANDSTROBES_NOALLOC_MAX_BASES
+ * bases (12 bytes per base, 12 MiB), one per device, so a batch holds at most that
+ * many bases; larger batches are rejected with SA_ERR_INVALID.  Nothing needs to
+ * start at zero, neither the scratch nor the output buffers.
+ *
+ * Calls share the one scratch array of their device: two calls whose kernels
+ * overlap in time on the same device (different streams, or different host
+ * threads) race and corrupt each other's results.  Serialise them, e.g. on one
+ * stream.
+ *
+ * The first call on each device looks up the scratch address
+ * (cudaGetSymbolAddress; this may load the library's device code), so make that
+ * call outside any stream capture; a call with n_reads = 0 does only this setup
+ * and launches nothing.  Later calls only launch.
+ *
+ * Runs on the calling thread's current device, asynchronously on `stream` (a
+ * cudaStream_t; NULL = legacy default stream).  idx supplies only the seeding
+ * parameters.  Device inputs: d_seq (total_bases bytes of ASCII bases),
+ * d_seq_offsets (n_reads + 1 values, d_seq_offsets[0] = 0, read r is
+ * [d_seq_offsets[r], d_seq_offsets[r+1])).  Device outputs, 2 * total_bases
+ * entries each: the forward randstrobes of read r at
+ * [d_seq_offsets[r], + d_counts[2r]) and the reverse-complement ones at
+ * [total_bases + d_seq_offsets[r], + d_counts[2r+1]), with the values of the
+ * hash / hash_revcomp / start / end fields of sa_query_randstrobe.  A read whose
+ * offsets decrease, end past total_bases or span more than 2048 bases gets
+ * d_counts = UINT32_MAX in both orientations.  Only argument errors are reported
+ * by the return value; kernel results are ready when the stream reaches them. */
+#define SA_RANDSTROBES_NOALLOC_MAX_BASES 1048576u
+int32_t sa_randstrobes_device_noalloc(const sa_index* idx, const uint8_t* d_seq, const uint64_t* d_seq_offsets,
+                                      uint32_t n_reads, uint64_t total_bases, uint64_t* d_hash,
+                                      uint64_t* d_hash_revcomp, uint32_t* d_start, uint32_t* d_end,
+                                      uint32_t* d_counts, void* stream);
+
 /* get_nams_by_chaining (src/nam.rs:138-166) for every read; NAMs in the order the
  * reference produces them (before sort_nams). */
 typedef struct {

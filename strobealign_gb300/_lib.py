@@ -107,6 +107,7 @@ SIGNATURES = {
     "sa_reads_view": (i32, [vp, P(ReadBatch)]),
     "sa_reads_free": (None, [vp]),
     "sa_randstrobes_batch": (i32, [vp, P(ReadBatch), P(QueryRandstrobe), sz, P(u64), P(u32)]),
+    "sa_randstrobes_device_noalloc": (i32, [vp, vp, vp, u32, u64, vp, vp, vp, vp, vp, vp]),
     "sa_nams_batch": (i32, [vp, P(ChainingParams), P(MappingParams), P(ReadBatch), P(Nam), sz, P(u64), P(u32),
                             P(NamDetails)]),
     "sa_align_batch": (i32, [P(MappingParams), sz, vp, P(u64), vp, P(u64), P(AlignmentC), P(u32), sz]),

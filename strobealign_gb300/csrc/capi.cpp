@@ -493,6 +493,20 @@ int32_t sa_randstrobes_batch(const sa_index* idx, const sa_read_batch* reads, sa
     SA_CATCH
 }
 
+// Allocation-free seeding: the checked seeding kernel on caller-owned device
+// buffers with the syncmer scratch in a static device array.
+int32_t sa_randstrobes_device_noalloc(const sa_index* idx, const uint8_t* d_seq, const uint64_t* d_seq_offsets,
+                                      uint32_t n_reads, uint64_t total_bases, uint64_t* d_hash,
+                                      uint64_t* d_hash_revcomp, uint32_t* d_start, uint32_t* d_end,
+                                      uint32_t* d_counts, void* stream) {
+    SA_TRY
+    require(idx != nullptr, "null index");
+    run_seeding_noalloc(idx->sp, d_seq, d_seq_offsets, n_reads, total_bases, d_hash, d_hash_revcomp, d_start, d_end,
+                        d_counts, (cudaStream_t)stream);
+    return SA_OK;
+    SA_CATCH
+}
+
 int32_t sa_nams_batch(const sa_index* idx, const sa_chaining_params* cp, const sa_mapping_params* mp,
                       const sa_read_batch* reads, sa_nam* out, size_t capacity, uint64_t* out_offsets,
                       uint32_t* out_counts, sa_nam_details* out_details) {

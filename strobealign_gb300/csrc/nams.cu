@@ -19,6 +19,8 @@
 #include <cub/cub.cuh>
 
 #include <cmath>
+#include <mutex>
+#include <string>
 
 #include "index_device.cuh"
 #include "pipeline.h"
@@ -46,6 +48,10 @@ __device__ __forceinline__ uint8_t nt_code(uint8_t c) {
 // ------------------------------------------------------------------ seeding
 // src/seeding/syncmers.rs:171-237: a syncmer at p requires an N-free k-mer window
 // and the (t-1)-th of its k-s+1 s-mer hashes to equal their minimum.
+// CHECKED (offsets supplied by a caller, not built here): a read whose offsets are
+// decreasing, end past `total` or span more than MAX_READ_LEN gets the count
+// UINT32_MAX in both orientations and is not touched otherwise.
+template <bool CHECKED>
 __global__ void __launch_bounds__(256) k_seed(const uint8_t* __restrict__ seq, const uint64_t* __restrict__ off,
                                               uint32_t n, SeedParams p, uint64_t* syn_hash, uint32_t* syn_pos,
                                               uint64_t* qr_hash, uint64_t* qr_hash_rc, uint32_t* qr_start,
@@ -57,6 +63,16 @@ __global__ void __launch_bounds__(256) k_seed(const uint8_t* __restrict__ seq, c
     const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
     for (uint32_t r = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; r < n; r += nwarps) {
         const uint64_t o = off[r];
+        if (CHECKED) {
+            const uint64_t e = off[r + 1];
+            if (e < o || e > total || e - o > MAX_READ_LEN) {
+                if (lane == 0) {
+                    n_rs[2 * r] = UINT32_MAX;
+                    n_rs[2 * r + 1] = UINT32_MAX;
+                }
+                continue;
+            }
+        }
         const uint32_t L = (uint32_t)(off[r + 1] - o);
         for (uint32_t i = lane; i < L; i += 32) codes[i] = nt_code(seq[o + i]);
         __syncwarp();
@@ -771,12 +787,55 @@ uint32_t run_seeding(const SeedParams& sp, uint32_t n, uint64_t total, NamWorksp
     ws.n_rs.reserve(2 * (size_t)n);
     size_t smem = WARPS_PER_BLOCK * MAX_READ_LEN;
     kt->begin(KS_SEED, st);
-    k_seed<<<warps_grid(n), 32 * WARPS_PER_BLOCK, smem, st>>>(ws.seq.p, ws.off.p, n, sp, ws.syn_hash.p, ws.syn_pos.p,
-                                                              ws.qr_hash.p, ws.qr_hash_rc.p, ws.qr_start.p,
-                                                              ws.qr_end.p, total, ws.n_rs.p);
+    k_seed<false><<<warps_grid(n), 32 * WARPS_PER_BLOCK, smem, st>>>(ws.seq.p, ws.off.p, n, sp, ws.syn_hash.p,
+                                                                     ws.syn_pos.p, ws.qr_hash.p, ws.qr_hash_rc.p,
+                                                                     ws.qr_start.p, ws.qr_end.p, total, ws.n_rs.p);
     kt->end(st);
     SA_CUDA(cudaGetLastError());
     return 1;
+}
+
+// Syncmer scratch of the allocation-free seeding entry point: hashes (8 bytes per
+// base) then positions (4 bytes per base) for at most
+// SA_RANDSTROBES_NOALLOC_MAX_BASES bases.  One copy per device, shared by every
+// call on that device.  Nothing in it needs to start at zero: each read writes
+// its own syncmer slots before reading them.
+static __device__ __align__(256) uint8_t g_seed_scratch[(size_t)SA_RANDSTROBES_NOALLOC_MAX_BASES * 12];
+
+void run_seeding_noalloc(const SeedParams& sp, const uint8_t* seq, const uint64_t* off, uint32_t n, uint64_t total,
+                         uint64_t* qr_hash, uint64_t* qr_hash_rc, uint32_t* qr_start, uint32_t* qr_end,
+                         uint32_t* counts, cudaStream_t st) {
+    if (total > SA_RANDSTROBES_NOALLOC_MAX_BASES)
+        throw Error(SA_ERR_INVALID, "batch has " + std::to_string(total) + " bases; the allocation-free seeding "
+                                    "entry point takes at most " +
+                                        std::to_string((uint64_t)SA_RANDSTROBES_NOALLOC_MAX_BASES));
+    // scratch address per device, looked up on the first call on that device
+    constexpr int MAX_DEVICES = 64;
+    static std::mutex mu;
+    static uint8_t* scratch[MAX_DEVICES] = {};
+    int dev = 0;
+    SA_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= MAX_DEVICES) throw Error(SA_ERR_CUDA, "device ordinal out of range");
+    uint8_t* base;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        if (!scratch[dev]) {
+            // loads the kernel too, so that later calls only launch
+            cudaFuncAttributes fa;
+            SA_CUDA(cudaFuncGetAttributes(&fa, k_seed<true>));
+            SA_CUDA(cudaGetSymbolAddress((void**)&scratch[dev], g_seed_scratch));
+        }
+        base = scratch[dev];
+    }
+    if (!n) return;
+    if (!off || !counts || (total && (!seq || !qr_hash || !qr_hash_rc || !qr_start || !qr_end)))
+        throw Error(SA_ERR_INVALID, "null device pointer");
+    uint64_t* syn_hash = reinterpret_cast<uint64_t*>(base);
+    uint32_t* syn_pos = reinterpret_cast<uint32_t*>(base + (size_t)SA_RANDSTROBES_NOALLOC_MAX_BASES * 8);
+    const size_t smem = WARPS_PER_BLOCK * MAX_READ_LEN;
+    k_seed<true><<<warps_grid(n), 32 * WARPS_PER_BLOCK, smem, st>>>(seq, off, n, sp, syn_hash, syn_pos, qr_hash,
+                                                                    qr_hash_rc, qr_start, qr_end, total, counts);
+    SA_CUDA(cudaGetLastError());
 }
 
 uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConfig& cfg, uint32_t n, uint64_t total,

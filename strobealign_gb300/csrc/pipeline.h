@@ -65,5 +65,10 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
 // Randstrobes only (stage entry point).
 uint32_t run_seeding(const SeedParams& sp, uint32_t n, uint64_t total, NamWorkspace& ws, cudaStream_t st,
                      KernelTimers* kt = nullptr);
+// Seeding with the syncmer scratch in a static device array and every other buffer
+// supplied by the caller (k_seed<true>); allocates nothing.
+void run_seeding_noalloc(const SeedParams& sp, const uint8_t* seq, const uint64_t* off, uint32_t n, uint64_t total,
+                         uint64_t* qr_hash, uint64_t* qr_hash_rc, uint32_t* qr_start, uint32_t* qr_end,
+                         uint32_t* counts, cudaStream_t st);
 
 }  // namespace sa
