@@ -283,6 +283,45 @@ void sa_output_free(sa_output* out);
 /* Abundances accumulated over all batches (--aemb), one per contig, already
  * divided by the contig length as output_abundances does (src/main.rs:990-1001). */
 int32_t sa_mapper_abundances(const sa_mapper* m, double* out, size_t n);
+/* ---------------------------------------------------------------- serving
+ * Continuous batching of mapping requests (the reference maps one input stream
+ * per process; a session serves many).  A request is a read batch; the session
+ * copies it, admits it onto the device when its reads fit in the in-flight read
+ * arena, and maps it as its own chunk stream (src/main.rs:591-604,873-988), so
+ * its output is byte-identical to sa_map_batch on the same records, whatever else
+ * is in flight.  Requests admitted together share extension waves.
+ * submit/poll/wait may be called from any thread. */
+typedef struct sa_session sa_session;
+typedef struct {
+    uint64_t max_inflight_bases;    /* device read arena in bases; 0 = 2^30 */
+    uint32_t max_inflight_requests; /* 0 = no limit */
+    uint32_t policy_threads;        /* host threads for the mapping policy; 0 = all */
+} sa_session_params;
+typedef struct {
+    double seconds_queued;  /* submit -> admitted */
+    double seconds_service; /* admitted -> done */
+    double seconds_total;   /* submit -> done */
+    uint64_t n_reads;
+    uint32_t n_waves; /* extension waves the request took part in */
+} sa_request_stats;
+void sa_session_params_default(sa_session_params* p);
+int32_t sa_session_create(const sa_index* idx, const sa_refs* refs, const sa_chaining_params* cp,
+                          const sa_mapping_params* mp, const sa_session_params* sp, sa_session** out);
+/* Copies the batch and queues it; r2 = NULL for single-end.  SA_ERR_INVALID if the
+ * request can never fit in the arena. */
+int32_t sa_session_submit(sa_session* s, const sa_read_batch* r1, const sa_read_batch* r2, uint64_t* ticket);
+/* *done = 1 once the request's output is ready. */
+int32_t sa_session_poll(sa_session* s, uint64_t ticket, int32_t* done);
+/* Waits up to timeout_ms (< 0: no limit; SA_ERR_TIMEOUT when it runs out) and
+ * hands over the request's output (release with sa_output_free).  stats may be
+ * NULL.  In abundance mode abundances (n_abundances >= contig count) receives the
+ * request's per-contig abundances divided by contig length; it may be NULL
+ * otherwise.  The ticket is invalid afterwards. */
+int32_t sa_session_wait(sa_session* s, uint64_t ticket, int64_t timeout_ms, sa_output* out, sa_request_stats* stats,
+                        double* abundances, size_t n_abundances);
+/* Finishes the admitted requests, cancels the queued ones, frees the session. */
+void sa_session_free(sa_session* s);
+
 /* Two-step form of sa_map_batch: upload a batch to the device, then map it.  The
  * host buffers of the batch must stay valid until the last sa_map_uploaded call
  * (names, qualities and comments are read from them when records are written).
@@ -301,9 +340,11 @@ typedef struct {
      * SW word, banded traceback, finalize, other extension */
     double kernel_ms[16];
     uint64_t kernel_launches[16];
-    /* Smith-Waterman cells (query x reference) of the striped passes: forward byte,
-     * forward word (byte overflow reruns), reverse byte, reverse word */
-    uint64_t sw_cells[4];
+    /* Smith-Waterman cells (query x reference).  [0]: canonical cells, |query| x
+     * |reference window| once per SSW call.  [1..4]: cells the striped passes
+     * computed (up to an early stop): forward byte, forward word (byte overflow
+     * reruns), reverse byte, reverse word */
+    uint64_t sw_cells[5];
 } sa_mapper_stats;
 int32_t sa_mapper_get_stats(const sa_mapper* m, sa_mapper_stats* out);
 /* Record CUDA events around each stage's launches (off by default). */

@@ -24,6 +24,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib as L
+from ._lib import SaError  # noqa: F401  (raised by every entry point)
 
 MODE_SAM, MODE_PAF, MODE_ABUNDANCE = 0, 1, 2
 MCS = {"always": 0, "rescue": 1, "off": 2, "first-strobe": 3}
@@ -386,7 +387,8 @@ class Mapper:
         d = {f: getattr(s, f) for f, _ in L.MapperStats._fields_ if not f.startswith("kernel_")}
         d["kernel_ms"] = {n: s.kernel_ms[i] for i, n in enumerate(L.KERNEL_SLOTS)}
         d["kernel_launches"] = {n: s.kernel_launches[i] for i, n in enumerate(L.KERNEL_SLOTS)}
-        d["sw_cells"] = dict(zip(("forward_byte", "forward_word", "reverse_byte", "reverse_word"), list(s.sw_cells)))
+        d["sw_cells"] = dict(zip(("canonical", "forward_byte", "forward_word", "reverse_byte", "reverse_word"),
+                                 list(s.sw_cells)))
         return d
 
     def set_profiling(self, on: bool = True) -> None:
@@ -402,6 +404,65 @@ class Mapper:
         if getattr(self, "h", None) and self.h.value:
             lib().sa_mapper_free(self.h)
             self.h = C.c_void_p()
+
+
+class Session:
+    """Serving session: requests are mapped with continuous batching on the GPU.
+
+    Each request is mapped as its own chunk stream, so its bytes equal
+    Mapper.map on the same records alone."""
+
+    def __init__(self, index: StrobemerIndex, refs: References, chaining: L.ChainingParams | None = None,
+                 mapping: L.MappingParams | None = None, max_inflight_bases: int = 0, max_inflight_requests: int = 0,
+                 policy_threads: int = 0, **kw):
+        self.index, self.refs = index, refs
+        self.cp = chaining or chaining_defaults()
+        self.mp = mapping or mapping_defaults(**kw)
+        sp = L.SessionParams()
+        lib().sa_session_params_default(C.byref(sp))
+        if max_inflight_bases:
+            sp.max_inflight_bases = max_inflight_bases
+        sp.max_inflight_requests = max_inflight_requests
+        sp.policy_threads = policy_threads
+        h = C.c_void_p()
+        L.check(lib().sa_session_create(index.h, refs.h, C.byref(self.cp), C.byref(self.mp), C.byref(sp),
+                                        C.byref(h)))
+        self.h = h
+
+    def submit(self, r1: Reads, r2: Reads | None = None) -> int:
+        b1 = r1.c()
+        b2 = r2.c() if r2 is not None else None
+        t = C.c_uint64()
+        L.check(lib().sa_session_submit(self.h, C.byref(b1), C.byref(b2) if b2 is not None else None, C.byref(t)))
+        return t.value
+
+    def poll(self, ticket: int) -> bool:
+        d = C.c_int32()
+        L.check(lib().sa_session_poll(self.h, ticket, C.byref(d)))
+        return bool(d.value)
+
+    def wait(self, ticket: int, timeout_ms: int = -1, abundances: bool = False):
+        """(output bytes, stats dict[, abundances])"""
+        o = L.Output()
+        st = L.RequestStats()
+        ab = np.zeros(len(self.refs), dtype=np.float64) if abundances else None
+        L.check(lib().sa_session_wait(self.h, ticket, timeout_ms, C.byref(o), C.byref(st),
+                                      _p(ab, C.c_double) if ab is not None else None, len(ab) if ab is not None else 0))
+        try:
+            data = C.string_at(o.data, o.len) if o.len else b""
+        finally:
+            lib().sa_output_free(C.byref(o))
+        stats = {f: getattr(st, f) for f, _ in L.RequestStats._fields_}
+        stats["n_mapped"] = o.n_mapped
+        return (data, stats, ab) if abundances else (data, stats)
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().sa_session_free(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        self.close()
 
 
 def sam_header(refs: References, cmd_line: str | None = None, rg_id: str | None = None,

@@ -72,11 +72,20 @@ class Output(C.Structure):
                 ("n_gpu_launches", u32)]
 
 
+class SessionParams(C.Structure):
+    _fields_ = [("max_inflight_bases", u64), ("max_inflight_requests", u32), ("policy_threads", u32)]
+
+
+class RequestStats(C.Structure):
+    _fields_ = [("seconds_queued", f64), ("seconds_service", f64), ("seconds_total", f64), ("n_reads", u64),
+                ("n_waves", u32)]
+
+
 class MapperStats(C.Structure):
     _fields_ = [("seconds_upload", f64), ("seconds_nams", f64), ("seconds_extension", f64),
                 ("seconds_policy", f64), ("seconds_total", f64), ("n_jobs", u64), ("n_waves", u64),
                 ("n_launches", u64), ("h2d_bytes", u64), ("d2h_bytes", u64), ("n_nams", u64), ("n_anchors", u64),
-                ("kernel_ms", f64 * 16), ("kernel_launches", u64 * 16), ("sw_cells", u64 * 4)]
+                ("kernel_ms", f64 * 16), ("kernel_launches", u64 * 16), ("sw_cells", u64 * 5)]
 
 
 KERNEL_SLOTS = ["seed", "hits", "anchors", "sort", "chain", "nams_other", "prepare", "fill", "sw_byte", "sw_word",
@@ -85,6 +94,12 @@ KERNEL_SLOTS = ["seed", "hits", "anchors", "sort", "chain", "nams_other", "prepa
 
 # name -> (restype, argtypes)
 SIGNATURES = {
+    "sa_session_params_default": (None, [P(SessionParams)]),
+    "sa_session_create": (i32, [vp, vp, P(ChainingParams), P(MappingParams), P(SessionParams), P(vp)]),
+    "sa_session_submit": (i32, [vp, P(ReadBatch), P(ReadBatch), P(u64)]),
+    "sa_session_poll": (i32, [vp, u64, P(i32)]),
+    "sa_session_wait": (i32, [vp, u64, i64, P(Output), P(RequestStats), P(f64), sz]),
+    "sa_session_free": (None, [vp]),
     "sa_last_error": (cp, []),
     "sa_version": (cp, []),
     "sa_seeding_params_from_read_length": (i32, [sz, P(SeedingParams)]),

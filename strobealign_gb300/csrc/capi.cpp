@@ -7,6 +7,7 @@
 #include <fstream>
 
 #include "mapper.h"
+#include "session.h"
 
 namespace sa {
 
@@ -30,9 +31,6 @@ SeedParams to_seed_params(const sa_seeding_params& p) {
 
 void index_extent_gpu(const sa_index& idx, uint32_t& max_pos, uint32_t& max_ref, cudaStream_t st);
 void extension_init_tables();
-uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64_t* off, const uint8_t* raw_refs,
-                           const uint64_t* raw_off, uint32_t k, const AlignScores& sc, uint32_t n, ExtWorkspace& ws,
-                           uint32_t max_qlen, cudaStream_t st, KernelTimers* kt = nullptr);
 
 }  // namespace sa
 
@@ -619,3 +617,98 @@ int32_t sa_align_batch(const sa_mapping_params* mp, size_t n, const char* querie
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- serving
+void sa_session_params_default(sa_session_params* p) {
+    if (!p) return;
+    p->max_inflight_bases = 1ull << 30;
+    p->max_inflight_requests = 0;
+    p->policy_threads = 0;
+}
+
+int32_t sa_session_create(const sa_index* idx, const sa_refs* refs, const sa_chaining_params* cp,
+                          const sa_mapping_params* mp, const sa_session_params* sp, sa_session** out) {
+    SA_TRY
+    require(idx && refs && out, "null argument");
+    sa_chaining_params c;
+    sa_mapping_params m;
+    if (cp) c = *cp;
+    else sa_chaining_params_default(&c);
+    if (mp) m = *mp;
+    else sa_mapping_params_default(&m);
+    require(c.max_lookback <= 1024, "max_lookback above 1024 is not supported");
+    require(c.max_ref_gap < LOG2_LUT_SIZE, "max_ref_gap too large");
+    SessionConfig sc;
+    if (sp) {
+        sc.max_inflight_bases = sp->max_inflight_bases;
+        sc.max_inflight_requests = sp->max_inflight_requests;
+        sc.policy_threads = sp->policy_threads;
+    }
+    auto* s = new sa_session{nullptr};
+    try {
+        s->s = new Session(idx, refs, c, m, sc);
+    } catch (...) {
+        delete s;
+        throw;
+    }
+    *out = s;
+    return SA_OK;
+    SA_CATCH
+}
+
+int32_t sa_session_submit(sa_session* s, const sa_read_batch* r1, const sa_read_batch* r2, uint64_t* ticket) {
+    SA_TRY
+    require(s && r1 && ticket, "null argument");
+    *ticket = s->s->submit(r1, r2);
+    return SA_OK;
+    SA_CATCH
+}
+
+int32_t sa_session_poll(sa_session* s, uint64_t ticket, int32_t* done) {
+    SA_TRY
+    require(s && done, "null argument");
+    *done = s->s->poll(ticket);
+    return SA_OK;
+    SA_CATCH
+}
+
+int32_t sa_session_wait(sa_session* s, uint64_t ticket, int64_t timeout_ms, sa_output* out, sa_request_stats* stats,
+                        double* abundances, size_t n_abundances) {
+    SA_TRY
+    require(s && out, "null argument");
+    std::unique_ptr<Request> r;
+    if (!s->s->wait(ticket, timeout_ms, r)) throw Error(SA_ERR_TIMEOUT, "request not finished within the timeout");
+    out->data = (char*)std::malloc(r->out.size() + 1);
+    if (!out->data) throw Error(SA_ERR_OOM, "output allocation failed");
+    std::memcpy(out->data, r->out.data(), r->out.size());
+    out->data[r->out.size()] = 0;
+    out->len = r->out.size();
+    out->n_reads = r->n_reads;
+    out->n_mapped = r->mapped;
+    out->n_waves = r->waves;
+    out->n_gpu_launches = 0;
+    if (stats) {
+        auto sec = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+            return std::chrono::duration<double>(b - a).count();
+        };
+        stats->seconds_queued = sec(r->t_submit, r->t_admit);
+        stats->seconds_service = sec(r->t_admit, r->t_done);
+        stats->seconds_total = sec(r->t_submit, r->t_done);
+        stats->n_reads = r->n_reads;
+        stats->n_waves = r->waves;
+    }
+    if (abundances) {
+        const auto& cs = s->s->contigs();
+        require(n_abundances >= cs.size(), "abundance output too small");
+        for (size_t i = 0; i < cs.size(); i++)
+            abundances[i] = i < r->abundance.size() ? r->abundance[i] / (double)cs[i].len : 0.0;
+    }
+    return SA_OK;
+    SA_CATCH
+}
+
+void sa_session_free(sa_session* s) {
+    if (!s) return;
+    delete s->s;
+    delete s;
+}

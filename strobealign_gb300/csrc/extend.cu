@@ -26,6 +26,8 @@ __constant__ uint8_t c_ssw_code[256];   // src/ssw.rs:8-25
 __constant__ uint8_t c_comp[256];       // src/revcomp.rs:5-22
 
 constexpr uint32_t FULLM = 0xffffffffu;
+// SswTask::raw_off of a task whose banded traceback runs on the per-thread path
+constexpr uint64_t RAW_FALLBACK = ~0ull;
 
 __device__ __forceinline__ uint8_t ref_base(const DevRefs& R, uint32_t c, uint64_t i) {
     uint64_t w = __ldg(R.words + R.word_off[c] + (i >> 5));
@@ -46,28 +48,102 @@ __device__ bool nam_consistent(const DevRefs& R, const uint8_t* s, uint32_t L, u
     return true;
 }
 
-// has_shared_substring (src/mapper.rs:1157-1168)
-__device__ bool shared_substring(const DevRefs& R, uint32_t ref_id, uint32_t ws, uint32_t wl, const uint8_t* s,
-                                 uint32_t L, bool rc, uint32_t k) {
-    uint32_t sub = 2 * k / 3, step = k / 3;
-    uint32_t lim = L > sub ? L - sub : 0;
-    if (step == 0) step = 1;
-    for (uint32_t i = 0; i < lim; i += step) {
-        if (sub == 0) return true;
-        if (wl < sub) continue;
-        for (uint32_t p = 0; p + sub <= wl; p++) {
-            uint32_t t = 0;
-            while (t < sub && ref_base(R, ref_id, ws + p + t) == read_char(s, L, i + t, rc)) t++;
-            if (t == sub) return true;
+// has_shared_substring (src/mapper.rs:1157-1168), warp per rescue job: the
+// window's substrings of length 2k/3 go into a shared-memory hash set (2-bit
+// codes, the window read straight from the packed reference), then every read
+// substring starting at a multiple of k/3 is looked up.  A read substring holding
+// anything but A/C/G/T never matches (the window decodes to A/C/G/T only).  Jobs
+// without a shared substring are dropped (type 0, nothing to extend).
+constexpr uint32_t RESCUE_TAB_MAX = 4096;  // > 2 * (2000 - sub + 1) slots
+constexpr unsigned long long RESCUE_EMPTY = ~0ull;
+
+__device__ __forceinline__ uint32_t rescue_slot(uint64_t v, uint32_t bits) {
+    return (uint32_t)((v * 0x9E3779B97F4A7C15ull) >> (64 - bits));
+}
+
+__global__ void __launch_bounds__(64) k_rescue_filter(const uint32_t* __restrict__ list,
+                                                      const uint32_t* __restrict__ n_list,
+                                                      const uint8_t* __restrict__ seq, const uint64_t* __restrict__ off,
+                                                      DevRefs R, uint32_t k, PrepRec* prep, uint64_t* sz_arena,
+                                                      uint64_t* sz_cigar, uint64_t* sz_h) {
+    extern __shared__ unsigned long long rescue_tab[];
+    const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31, wpb = blockDim.x / 32;
+    unsigned long long* tab = rescue_tab + warp * RESCUE_TAB_MAX;
+    const uint32_t n = *n_list;
+    const uint32_t sub = 2 * k / 3;
+    const uint32_t step = k / 3 ? k / 3 : 1;
+    const uint64_t mask = (1ull << (2 * sub)) - 1;  // sub <= 21 for k <= 32
+    for (uint32_t li = blockIdx.x * wpb + warp; li < n; li += gridDim.x * wpb) {
+        const uint32_t t = list[li];
+        const PrepRec p = prep[t];
+        const uint8_t* s = seq + off[p.read];
+        const uint32_t L = p.qlen;
+        const uint32_t lim = L > sub ? L - sub : 0;
+        bool found;
+        if (lim == 0) {
+            found = false;
+        } else if (sub == 0) {
+            found = true;
+        } else if (p.wlen < sub) {
+            found = false;
+        } else {
+            const uint32_t entries = p.wlen - sub + 1;
+            uint32_t bits = 6;
+            while ((1u << bits) < 2 * entries) bits++;
+            const uint32_t size = 1u << bits;
+            for (uint32_t i = lane; i < size; i += 32) tab[i] = RESCUE_EMPTY;
+            __syncwarp();
+            const uint64_t* words = R.words + R.word_off[p.ref_id];
+            for (uint32_t q = lane; q < entries; q += 32) {
+                const uint64_t x = (uint64_t)p.wstart + q;
+                const uint64_t w0 = __ldg(words + (x >> 5)), w1 = __ldg(words + (x >> 5) + 1);
+                const uint32_t sh = (uint32_t)(x & 31) * 2;
+                uint64_t v = sh ? (w0 >> sh) | (w1 << (64 - sh)) : w0;
+                v &= mask;
+                uint32_t h = rescue_slot(v, bits);
+                for (;;) {
+                    const unsigned long long prev = atomicCAS(&tab[h], RESCUE_EMPTY, (unsigned long long)v);
+                    if (prev == RESCUE_EMPTY || prev == v) break;
+                    h = (h + 1) & (size - 1);
+                }
+            }
+            __syncwarp();
+            bool hit = false;
+            for (uint32_t i = lane * step; i < lim && !hit; i += 32 * step) {
+                uint64_t v = 0;
+                bool ok = true;
+                for (uint32_t j = 0; j < sub; j++) {
+                    const uint8_t c = read_char(s, L, i + j, p.rc);
+                    const uint32_t code = c == 'A' ? 0 : c == 'C' ? 1 : c == 'G' ? 2 : c == 'T' ? 3 : 4;
+                    if (code > 3) { ok = false; break; }
+                    v |= (uint64_t)code << (2 * j);
+                }
+                if (!ok) continue;
+                uint32_t h = rescue_slot(v, bits);
+                for (;;) {
+                    const unsigned long long e = tab[h];
+                    if (e == v) { hit = true; break; }
+                    if (e == RESCUE_EMPTY) break;
+                    h = (h + 1) & (size - 1);
+                }
+            }
+            found = __any_sync(FULLM, hit);
+            __syncwarp();
+        }
+        if (!found && lane == 0) {
+            prep[t].type = 0;
+            prep[t].cigar_cap = 0;
+            sz_arena[t] = 0;
+            sz_cigar[t] = 0;
+            sz_h[t] = 0;
         }
     }
-    return false;
 }
 
 __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict__ seq,
                           const uint64_t* __restrict__ off, DevRefs R, uint32_t k, const uint8_t* raw_refs,
                           const uint64_t* raw_off, ExtResult* res, PrepRec* prep, uint64_t* sz_arena,
-                          uint64_t* sz_cigar, uint64_t* sz_h) {
+                          uint64_t* sz_cigar, uint64_t* sz_h, uint32_t* rescue_list, uint32_t* n_rescue) {
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         ExtJob jb = jobs[t];
         const uint8_t* s = seq + off[jb.read];
@@ -133,8 +209,9 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
             r.gapped = 1;
             p.wstart = jb.ref_start;
             p.wlen = jb.ref_end - jb.ref_start;
-            p.type = 0;
-            if (p.wlen <= 2000 && L > 0 && shared_substring(R, jb.ref_id, p.wstart, p.wlen, s, L, rc, k)) p.type = 2;
+            // extended only if has_shared_substring holds (k_rescue_filter)
+            p.type = (p.wlen <= 2000 && L > 0) ? 2 : 0;
+            if (p.type == 2) rescue_list[atomicAdd(n_rescue, 1u)] = t;
         } else {  // JOB_ALIGN: raw reference bytes
             p.rc = 0;
             p.wstart = 0;
@@ -231,6 +308,7 @@ __global__ void k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict
             atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8), (unsigned long long)L * p.wlen);
             SswTask tk{};
             tk.job = t;
+            tk.raw_off = RAW_FALLBACK;
             tk.ref_begin1 = -1;
             tk.read_begin1 = -1;
             tasks[ti] = tk;
@@ -265,6 +343,7 @@ struct Lanes<true> {
 
 struct EndPos {
     int score, ref, read;
+    int cols;  // reference columns processed
 };
 
 // One striped pass (sw_sse2_byte / sw_sse2_word).  The G lanes of a group hold one
@@ -288,7 +367,9 @@ __device__ EndPos sw_pass(const uint8_t* q, int qlen, bool q_rev, const uint8_t*
     int max = 0, end_ref = WORD ? 0 : -1, end_read = qlen - 1;
     int vMaxScore = 0, vMaxMark = 0;
     bool overflow = false;
+    int cols = 0;
     for (int tt = 0; tt < rlen; tt++) {
+        cols = tt + 1;
         const int i = r_rev ? rlen - 1 - tt : tt;
         const int rb = c_ssw_code[r[i]];
         int last = H[(seg - 1) * G + gl];
@@ -386,6 +467,7 @@ __device__ EndPos sw_pass(const uint8_t* q, int qlen, bool q_rev, const uint8_t*
     }
     (void)overflow;
     EndPos res;
+    res.cols = cols;
     res.score = WORD ? max : (max + bias >= 255 ? 255 : max);
     res.ref = end_ref;
     res.read = end_read;
@@ -423,10 +505,10 @@ __global__ void __launch_bounds__(128) k_sw(SswTask* tasks, const uint32_t* list
             EndPos e = sw_pass<WORD>(q, (int)p.qlen, false, r, (int)p.wlen, false, WORD ? 65535 : 255, sc, bias, H, E,
                                      qc, mask, gl);
             if (gl == 0) {
+                atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8) + 1 + (WORD ? 1 : 0),
+                          (unsigned long long)p.qlen * (unsigned long long)e.cols);
                 if (!WORD && e.score == 255) {
                     list_word[atomicAdd(&counters[1], 1u)] = ti;
-                    atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8) + 1,
-                              (unsigned long long)p.qlen * p.wlen);
                 } else {
                     tk.score1 = e.score;
                     tk.ref_end1 = e.ref;
@@ -444,6 +526,7 @@ __global__ void __launch_bounds__(128) k_sw(SswTask* tasks, const uint32_t* list
                 e.score = 0;
                 e.ref = -1;
                 e.read = tk.read_end1;
+                e.cols = 0;
             } else {
                 e = sw_pass<WORD>(q, tk.read_end1 + 1, true, r, tk.ref_end1 + 1, true, tk.score1, sc, bias, H, E, qc,
                                   mask, gl);
@@ -452,13 +535,503 @@ __global__ void __launch_bounds__(128) k_sw(SswTask* tasks, const uint32_t* list
                 tk.ref_begin1 = e.ref;
                 tk.read_begin1 = tk.read_end1 - e.read;
                 tk.flag = tk.score1 > e.score ? 2 : 0;
-                if (tk.ref_end1 >= 0)
-                    atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8) + 2 + (WORD ? 1 : 0),
-                              (unsigned long long)(tk.read_end1 + 1) * (unsigned long long)(tk.ref_end1 + 1));
+                atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8) + 3 + (WORD ? 1 : 0),
+                          (unsigned long long)(tk.read_end1 + 1) * (unsigned long long)e.cols);
                 tasks[ti] = tk;
             }
         }
         __syncwarp(mask);
+    }
+}
+
+// ------------------------------------------------------------------ striped SW, registers
+// The same striped passes with each lane's segment column of H and E in registers
+// (SEG >= segLen rows per lane, the loops unrolled) and the striped query profile
+// (ext/ssw/ssw.c:114-146 qP_byte / qP_word) as signed bytes in shared memory, one
+// 32-bit word per four rows.  Scores are plain ints: byte mode without
+// saturation equals ssw.c's biased u8 arithmetic until the column max reaches
+// 255 - bias, and that column ends the byte pass as an overflow in both forms;
+// word scores never reach the i16 limits (|score| <= 2 x 2048 x 127).
+template <int G, int SEG>
+__device__ EndPos sw_pass_reg(const uint8_t* q, int qlen, bool q_rev, const uint8_t* r, int rlen, bool r_rev,
+                              bool check_term, int terminate, const AlignScores& sc, int bias, bool byte_mode,
+                              uint32_t* prof, unsigned mask, int gl) {
+    constexpr int SEGW = (SEG + 3) / 4;
+    const int seg = (qlen + G - 1) / G;
+    const int gO = sc.gap_open, gE = sc.gap_extend;
+    const int match = sc.match, mism = -(int)sc.mismatch;
+    // prof[(b * G + gl) * SEGW + w]: rows gl*seg + 4w .. 4w+3 against reference code b (4 = N)
+    for (int b = 0; b < 5; b++) {
+        for (int w = 0; w < SEGW; w++) {
+            uint32_t word = 0;
+            for (int x = 0; x < 4; x++) {
+                const int j = 4 * w + x, pos = gl * seg + j;
+                int s = 0;
+                if (j < seg && pos < qlen) {
+                    const int code = c_ssw_code[q_rev ? q[qlen - 1 - pos] : q[pos]];
+                    s = (code == b && b < 4) ? match : mism;
+                }
+                word |= (uint32_t)(uint8_t)(int8_t)s << (8 * x);
+            }
+            prof[(b * G + gl) * SEGW + w] = word;
+        }
+    }
+    __syncwarp(mask);
+    int H[SEG], E[SEG];
+#pragma unroll
+    for (int j = 0; j < SEG; j++) {
+        H[j] = 0;
+        E[j] = 0;
+    }
+    int max = 0, end_ref = byte_mode ? -1 : 0, end_read = qlen - 1;
+    int vMaxScore = 0, vMaxMark = 0, cols = 0;
+    int rb_next = rlen > 0 ? c_ssw_code[r[r_rev ? rlen - 1 : 0]] : 0;
+    for (int tt = 0; tt < rlen; tt++) {
+        cols = tt + 1;
+        const int i = r_rev ? rlen - 1 - tt : tt;
+        const int rb = rb_next;
+        if (tt + 1 < rlen) rb_next = c_ssw_code[r[r_rev ? rlen - 2 - tt : tt + 1]];
+        uint32_t P[SEGW];
+        const uint32_t* pp = prof + (rb * G + gl) * SEGW;
+#pragma unroll
+        for (int w = 0; w < SEGW; w++) P[w] = pp[w];
+        int last = H[0];
+#pragma unroll
+        for (int j = 1; j < SEG; j++)
+            if (j < seg) last = H[j];
+        int vH = __shfl_up_sync(mask, last, 1, G);
+        if (gl == 0) vH = 0;
+        int vF = 0, vMaxCol = 0;
+#pragma unroll
+        for (int j = 0; j < SEG; j++) {
+            if (j >= seg) break;
+            const int m = (int)(int8_t)(uint8_t)(P[j >> 2] >> (8 * (j & 3)));
+            const int e = E[j];
+            int h = vH + m;
+            h = h > e ? h : e;
+            h = h > vF ? h : vF;
+            vMaxCol = vMaxCol > h ? vMaxCol : h;
+            vH = H[j];
+            H[j] = h;
+            int hg = h - gO;
+            hg = hg > 0 ? hg : 0;
+            const int e2 = e - gE;
+            E[j] = e2 > hg ? e2 : hg;
+            const int f2 = vF - gE;
+            vF = f2 > hg ? f2 : hg;
+        }
+        // lazy-F (ext/ssw/ssw.c:285-299 / :491-502)
+        for (int kk = 0; kk < G; kk++) {
+            vF = __shfl_up_sync(mask, vF, 1, G);
+            if (gl == 0) vF = 0;
+            bool done = false;
+#pragma unroll
+            for (int j = 0; j < SEG; j++) {
+                if (j >= seg) break;
+                int h = H[j] > vF ? H[j] : vF;
+                vMaxCol = vMaxCol > h ? vMaxCol : h;
+                H[j] = h;
+                int hg = h - gO;
+                hg = hg > 0 ? hg : 0;
+                vF = vF - gE > 0 ? vF - gE : 0;
+                if (__all_sync(mask, vF <= hg)) {
+                    done = true;
+                    break;
+                }
+            }
+            if (done) break;
+        }
+        vMaxScore = vMaxScore > vMaxCol ? vMaxScore : vMaxCol;
+        if (__any_sync(mask, vMaxScore != vMaxMark)) {
+            vMaxMark = vMaxScore;
+            int temp = vMaxScore;
+            for (int d = G / 2; d > 0; d >>= 1) {
+                const int o = __shfl_xor_sync(mask, temp, d, G);
+                temp = temp > o ? temp : o;
+            }
+            if (temp > max) {
+                max = temp;
+                if (byte_mode && max + bias >= 255) break;
+                end_ref = i;
+                int best = 0x7fffffff;
+#pragma unroll
+                for (int j = 0; j < SEG; j++) {
+                    if (j >= seg) break;
+                    if (H[j] == max) {
+                        const int pos = gl * seg + j;
+                        best = pos < best ? pos : best;
+                    }
+                }
+                for (int d = G / 2; d > 0; d >>= 1) {
+                    const int o = __shfl_xor_sync(mask, best, d, G);
+                    best = best < o ? best : o;
+                }
+                end_read = best < qlen - 1 ? best : qlen - 1;
+            }
+        }
+        if (check_term) {
+            int cm = vMaxCol;
+            for (int d = G / 2; d > 0; d >>= 1) {
+                const int o = __shfl_xor_sync(mask, cm, d, G);
+                cm = cm > o ? cm : o;
+            }
+            if (cm == terminate) break;
+        }
+    }
+    EndPos res;
+    res.cols = cols;
+    res.score = !byte_mode ? max : (max + bias >= 255 ? 255 : max);
+    res.ref = end_ref;
+    res.read = end_read;
+    return res;
+}
+
+// k_sw with sw_pass_reg: the forward pass never meets its terminate value (byte
+// mode stops on overflow first, word scores stay below 65535), so only the reverse
+// pass checks it.
+template <bool WORD, int SEG>
+__global__ void __launch_bounds__(128) k_swr(SswTask* tasks, const uint32_t* list, const uint32_t* n_list_ptr,
+                                             uint32_t n_list_host, const PrepRec* prep, const uint8_t* arena,
+                                             AlignScores sc, int bias, int pass, uint32_t* counters,
+                                             uint32_t* list_word, uint32_t* list_rev_byte, uint32_t* list_rev_word) {
+    constexpr int G = Lanes<WORD>::G;
+    constexpr int SEGW = (SEG + 3) / 4;
+    extern __shared__ __align__(16) uint32_t prof_smem[];
+    const uint32_t n_list = n_list_ptr ? *n_list_ptr : n_list_host;
+    const int lane = threadIdx.x & 31;
+    const int grp_in_warp = lane / G, gl = lane % G;
+    const unsigned mask = (G == 32 ? FULLM : ((1u << G) - 1) << (grp_in_warp * G));
+    const int groups_per_block = blockDim.x / G;
+    const int grp = threadIdx.x / G;
+    uint32_t* prof = prof_smem + grp * (5 * G * SEGW);
+    for (uint32_t base = blockIdx.x * groups_per_block; base < n_list; base += gridDim.x * groups_per_block) {
+        const uint32_t li = base + grp;
+        if (li >= n_list) continue;  // whole group idles together
+        const uint32_t ti = list ? list[li] : li;
+        SswTask tk = tasks[ti];
+        const PrepRec p = prep[tk.job];
+        const uint8_t* q = arena + p.arena_off;
+        const uint8_t* r = q + p.qlen;
+        if (pass == 0) {
+            EndPos e = sw_pass_reg<G, SEG>(q, (int)p.qlen, false, r, (int)p.wlen, false, false, 0, sc, bias, !WORD,
+                                           prof, mask, gl);
+            if (gl == 0) {
+                atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8) + 1 + (WORD ? 1 : 0),
+                          (unsigned long long)p.qlen * (unsigned long long)e.cols);
+                if (!WORD && e.score == 255) {
+                    list_word[atomicAdd(&counters[1], 1u)] = ti;
+                } else {
+                    tk.score1 = e.score;
+                    tk.ref_end1 = e.ref;
+                    tk.read_end1 = e.read;
+                    tk.word = WORD;
+                    tasks[ti] = tk;
+                    if (WORD) list_rev_word[atomicAdd(&counters[3], 1u)] = ti;
+                    else list_rev_byte[atomicAdd(&counters[2], 1u)] = ti;
+                }
+            }
+        } else {
+            EndPos e;
+            if (tk.ref_end1 < 0) {
+                e.score = 0;
+                e.ref = -1;
+                e.read = tk.read_end1;
+                e.cols = 0;
+            } else {
+                e = sw_pass_reg<G, SEG>(q, tk.read_end1 + 1, true, r, tk.ref_end1 + 1, true, true, tk.score1, sc, bias,
+                                        !WORD, prof, mask, gl);
+            }
+            if (gl == 0) {
+                tk.ref_begin1 = e.ref;
+                tk.read_begin1 = tk.read_end1 - e.read;
+                tk.flag = tk.score1 > e.score ? 2 : 0;
+                atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8) + 3 + (WORD ? 1 : 0),
+                          (unsigned long long)(tk.read_end1 + 1) * (unsigned long long)e.cols);
+                tasks[ti] = tk;
+            }
+        }
+        __syncwarp(mask);
+    }
+}
+
+// ------------------------------------------------------------------ fused SSW, warp per task
+// ssw_align's search for both ends (ext/ssw/ssw.c:818-888) for one task per warp,
+// in one launch: the byte pass, the word rerun when the byte pass overflows, then
+// the reverse pass in the mode that produced the score.
+//
+// Layout: NL SSE lanes (16 byte, 8 word) of segLen = ceil(L / NL) rows each, as
+// in the library.  A lane's rows are split over S = 32 / NL threads in
+// consecutive blocks of R = ceil(segLen / S) rows, so thread (l, s) holds rows
+// l*segLen + s*R ... in registers and the 32 threads hold the query in order.
+//
+// Within a column the F recurrence is rewritten as vF' = max(vF - gE, a) with
+// a = max(max(vH + m, E) - gO, 0); this equals the library's update whenever
+// gap_open >= gap_extend (the term H - gO that vF itself feeds never exceeds
+// vF - gE).  It is linear in the max-plus sense, so each thread scans its own rows
+// and a max-plus scan over the S threads of a lane supplies the F entering each
+// block.  The lazy-F pass has a closed form (below), and the column maximum
+// bookkeeping (vMaxScore / vMaxMark) reduces to "the running maximum grew in this
+// column".
+__device__ __forceinline__ int warp_max32(int v) {
+    for (int d = 16; d > 0; d >>= 1) {
+        const int o = __shfl_xor_sync(FULLM, v, d);
+        v = v > o ? v : o;
+    }
+    return v;
+}
+__device__ __forceinline__ int warp_min32(int v) {
+    for (int d = 16; d > 0; d >>= 1) {
+        const int o = __shfl_xor_sync(FULLM, v, d);
+        v = v < o ? v : o;
+    }
+    return v;
+}
+
+template <int NL, int RMAX>
+__device__ __noinline__ EndPos ssw_warp_pass(const uint8_t* q, int qlen, bool q_rev, const uint8_t* r, int rlen, bool r_rev,
+                                bool check_term, int terminate, const AlignScores& sc, int bias, uint32_t* prof) {
+    constexpr int S = 32 / NL;
+    constexpr int RW = (RMAX + 3) / 4;
+    constexpr bool BYTE = NL == 16;
+    if (qlen <= 0) {
+        EndPos z;
+        z.score = 0;
+        z.ref = BYTE ? -1 : 0;
+        z.read = qlen - 1;
+        z.cols = 0;
+        return z;
+    }
+    const int tau = threadIdx.x & 31, l = tau / S, s = tau % S;
+    const int seg = (qlen + NL - 1) / NL;
+    const int R = (seg + S - 1) / S;
+    const int j0 = s * R;
+    int nr = seg - j0;
+    nr = nr < 0 ? 0 : (nr > R ? R : nr);
+    const int s_last = (seg - 1) / R;
+    // owner of the row before this thread's first row (row l*seg + j0 - 1)
+    const int pred = s > 0 ? tau - 1 : (l > 0 ? (l - 1) * S + s_last : 0);
+    const int src_last = l > 0 ? (l - 1) * S + s_last : 0;
+    const int gO = sc.gap_open, gE = sc.gap_extend;
+    const int match = sc.match, mism = -(int)sc.mismatch;
+    // prof[(b * 32 + tau) * RW + w]: this thread's rows j0 + 4w .. 4w+3 against reference code b (4 = N)
+    for (int b = 0; b < 5; b++)
+        for (int w = 0; w < RW; w++) {
+            uint32_t word = 0;
+            for (int y = 0; y < 4; y++) {
+                const int rr = 4 * w + y, pos = l * seg + j0 + rr;
+                int sv = 0;
+                if (rr < nr && pos < qlen) {
+                    const int code = c_ssw_code[q_rev ? q[qlen - 1 - pos] : q[pos]];
+                    sv = (code == b && b < 4) ? match : mism;
+                }
+                word |= (uint32_t)(uint8_t)(int8_t)sv << (8 * y);
+            }
+            prof[(b * 32 + tau) * RW + w] = word;
+        }
+    __syncwarp();
+    int H[RMAX], E[RMAX];
+#pragma unroll
+    for (int rr = 0; rr < RMAX; rr++) {
+        H[rr] = 0;
+        E[rr] = 0;
+    }
+    int max = 0, end_ref = BYTE ? -1 : 0, end_read = qlen - 1, cols = 0;
+    int rb_next = rlen > 0 ? c_ssw_code[r[r_rev ? rlen - 1 : 0]] : 0;
+    for (int tt = 0; tt < rlen; tt++) {
+        cols = tt + 1;
+        const int i = r_rev ? rlen - 1 - tt : tt;
+        const int rb = rb_next;
+        if (tt + 1 < rlen) rb_next = c_ssw_code[r[r_rev ? rlen - 2 - tt : tt + 1]];
+        uint32_t P[RW];
+        const uint32_t* pp = prof + (rb * 32 + tau) * RW;
+#pragma unroll
+        for (int w = 0; w < RW; w++) P[w] = pp[w];
+        int lastH = H[0];
+#pragma unroll
+        for (int rr = 1; rr < RMAX; rr++)
+            if (rr < nr) lastH = H[rr];
+        int vH = __shfl_sync(FULLM, lastH, pred);
+        if (tau == 0) vH = 0;
+        // main pass, part 1: diagonal + E candidates and the local F scan (F entering
+        // this thread's first row taken as 0)
+        int A[RMAX], F[RMAX];
+        int f = 0;
+#pragma unroll
+        for (int rr = 0; rr < RMAX; rr++) {
+            if (rr >= nr) break;
+            const int m = (int)(int8_t)(uint8_t)(P[rr >> 2] >> (8 * (rr & 3)));
+            const int e = E[rr];
+            int x = vH + m;
+            x = x > e ? x : e;
+            A[rr] = x;
+            vH = H[rr];
+            F[rr] = f;
+            int a = x - gO;
+            a = a > 0 ? a : 0;
+            const int f2 = f - gE;
+            f = f2 > a ? f2 : a;
+        }
+        // F entering this thread's block: max-plus scan over the lane's threads
+        int fin = 0;
+        if (S > 1) {
+            int D = nr * gE, V = f;
+#pragma unroll
+            for (int d = 1; d < S; d <<= 1) {
+                const int Dp = __shfl_up_sync(FULLM, D, d, S);
+                const int Vp = __shfl_up_sync(FULLM, V, d, S);
+                if (s >= d) {
+                    const int c = Vp - D;
+                    V = c > V ? c : V;
+                    D += Dp;
+                }
+            }
+            const int pv = __shfl_up_sync(FULLM, V, 1, S);
+            fin = s > 0 ? pv : 0;
+        }
+        // part 2: H, E with the F entering each row
+        int colmax = 0;
+        {
+            int fr = fin;
+#pragma unroll
+            for (int rr = 0; rr < RMAX; rr++) {
+                if (rr >= nr) break;
+                const int fv = fr > F[rr] ? fr : F[rr];
+                const int h = A[rr] > fv ? A[rr] : fv;
+                colmax = colmax > h ? colmax : h;
+                int hg = h - gO;
+                hg = hg > 0 ? hg : 0;
+                const int e2 = E[rr] - gE;
+                E[rr] = e2 > hg ? e2 : hg;
+                H[rr] = h;
+                fr -= gE;
+            }
+        }
+        // lazy-F (ext/ssw/ssw.c:285-299 / :491-502) in closed form: the loop carries
+        // the final F of each lane into the following lanes, decaying by gE per row,
+        // and raises H to it; its early exit drops only values that could no longer
+        // raise any H.  So H(l, j) = max(H, G(l) - j*gE) with G(l) the maximum over
+        // lanes l' < l of Ffinal(l') - (l - 1 - l') * segLen * gE.
+        {
+            int fout = fin - nr * gE;
+            fout = fout > f ? fout : f;  // F leaving this thread's block
+            int Y = __shfl_sync(FULLM, fout, l * S + s_last);
+#pragma unroll
+            for (int d = 1; d < NL; d <<= 1) {
+                const int Yp = __shfl_up_sync(FULLM, Y, d * S);
+                const int c = Yp - d * seg * gE;
+                if (l >= d) Y = Y > c ? Y : c;
+            }
+            const int Gp = __shfl_up_sync(FULLM, Y, S);
+            int g = l > 0 ? Gp - j0 * gE : 0;
+#pragma unroll
+            for (int rr = 0; rr < RMAX; rr++) {
+                if (rr >= nr) break;
+                if (g > H[rr]) {
+                    H[rr] = g;
+                    colmax = colmax > g ? colmax : g;
+                }
+                g -= gE;
+            }
+        }
+        if (__any_sync(FULLM, colmax > max)) {
+            max = warp_max32(colmax);
+            if (BYTE && max + bias >= 255) break;
+            end_ref = i;
+            int best = 0x7fffffff;
+#pragma unroll
+            for (int rr = 0; rr < RMAX; rr++) {
+                if (rr >= nr) break;
+                if (H[rr] == max) {
+                    const int pos = l * seg + j0 + rr;
+                    best = pos < best ? pos : best;
+                }
+            }
+            best = warp_min32(best);
+            end_read = best < qlen - 1 ? best : qlen - 1;
+        }
+        if (check_term && __any_sync(FULLM, colmax >= terminate) && warp_max32(colmax) == terminate) break;
+    }
+    EndPos res;
+    res.cols = cols;
+    res.score = !BYTE ? max : (max + bias >= 255 ? 255 : max);
+    res.ref = end_ref;
+    res.read = end_read;
+    return res;
+}
+
+// Tasks are taken in list order through a shared counter, so the longest windows
+// (put first by the caller) start first.
+template <int RMAX>
+__global__ void __launch_bounds__(128) k_ssw(SswTask* tasks, const uint32_t* order, uint32_t n_tasks,
+                                             const PrepRec* prep, const uint8_t* arena, AlignScores sc, int bias,
+                                             uint32_t* counters) {
+    constexpr int RW = (RMAX + 3) / 4;
+    extern __shared__ __align__(16) uint32_t ssw_smem[];
+    const int lane = threadIdx.x & 31;
+    uint32_t* prof = ssw_smem + (threadIdx.x / 32) * (5 * 32 * RW);
+    unsigned long long* cells = reinterpret_cast<unsigned long long*>(counters + 8);
+    for (;;) {
+        uint32_t li = 0;
+        if (lane == 0) li = atomicAdd(&counters[5], 1u);
+        li = __shfl_sync(FULLM, li, 0);
+        if (li >= n_tasks) break;
+        const uint32_t ti = order ? order[li] : li;
+        SswTask tk = tasks[ti];
+        const PrepRec p = prep[tk.job];
+        const uint8_t* q = arena + p.arena_off;
+        const uint8_t* r = q + p.qlen;
+        // forward: byte, word on overflow (ext/ssw/ssw.c:840-862)
+        EndPos e = ssw_warp_pass<16, RMAX>(q, (int)p.qlen, false, r, (int)p.wlen, false, false, 0, sc, bias, prof);
+        unsigned long long c_fb = (unsigned long long)p.qlen * e.cols, c_fw = 0, c_rb = 0, c_rw = 0;
+        bool word = false;
+        if (e.score == 255) {
+            __syncwarp();
+            e = ssw_warp_pass<8, RMAX>(q, (int)p.qlen, false, r, (int)p.wlen, false, false, 0, sc, bias, prof);
+            c_fw = (unsigned long long)p.qlen * e.cols;
+            word = true;
+        }
+        tk.score1 = e.score;
+        tk.ref_end1 = e.ref;
+        tk.read_end1 = e.read;
+        tk.word = word;
+        // reverse pass over read[0..=read_end1] and ref[0..=ref_end1] (ext/ssw/ssw.c:870-888)
+        EndPos b;
+        if (tk.ref_end1 < 0) {
+            b.score = 0;
+            b.ref = -1;
+            b.read = tk.read_end1;
+            b.cols = 0;
+        } else {
+            __syncwarp();
+            if (word)
+                b = ssw_warp_pass<8, RMAX>(q, tk.read_end1 + 1, true, r, tk.ref_end1 + 1, true, true, tk.score1, sc,
+                                           bias, prof);
+            else
+                b = ssw_warp_pass<16, RMAX>(q, tk.read_end1 + 1, true, r, tk.ref_end1 + 1, true, true, tk.score1, sc,
+                                            bias, prof);
+        }
+        (word ? c_rw : c_rb) = (unsigned long long)(tk.read_end1 + 1) * b.cols;
+        tk.ref_begin1 = b.ref;
+        tk.read_begin1 = tk.read_end1 - b.read;
+        tk.flag = tk.score1 > b.score ? 2 : 0;
+        if (lane == 0) {
+            tasks[ti] = tk;
+            atomicAdd(cells + 1, c_fb);
+            if (c_fw) atomicAdd(cells + 2, c_fw);
+            if (c_rb) atomicAdd(cells + 3, c_rb);
+            if (c_rw) atomicAdd(cells + 4, c_rw);
+        }
+        __syncwarp();
+    }
+}
+
+// window length of each task, for the longest-first order of k_ssw
+__global__ void k_task_keys(const SswTask* tasks, uint32_t n, const PrepRec* prep, uint32_t* key, uint32_t* idx) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const PrepRec p = prep[tasks[i].job];
+        const uint32_t cells = p.wlen * (p.qlen + 1) >> 7;  // < 2^16 for windows <= 2000, queries <= 2048
+        key[i] = 0xffffu - (cells < 0xffffu ? cells : 0xffffu);  // ascending: largest first
+        idx[i] = i;
     }
 }
 
@@ -510,6 +1083,207 @@ __device__ int band_pass(const uint8_t* ref, const uint8_t* read, int ref_len, i
     return max;
 }
 
+// banded_sw (ext/ssw/ssw.c:598-769), warp per task for bands of up to 31 cells
+// (band width <= 15): lane k holds cell x + k of row i (x = max(i - bw, 0)), the
+// previous row arrives by shuffles, and the row's F chain
+// F(j) = max(H(j-1) - gO, F(j-1) - gE) is a max-plus scan of max(E+, diag) - gO
+// over the lanes (exact when gap_open >= gap_extend, as H(j-1) = max(that, F+)).
+// Directions are kept as four ballots per row (E opened, F opened, H from the
+// diagonal, E over F) in the task's scratch, followed by the CIGAR; the traceback
+// reads them with the library's flat-array indexing, so an index that leaves a row
+// reads the neighbouring row's entries, or 0 where the pass wrote nothing.
+// Tasks whose band outgrows a warp keep raw_off == RAW_FALLBACK for k_band_width.
+__device__ int band_pass_warp(const uint8_t* ref, const uint8_t* read, int rl, int ql, int bw, const AlignScores& sc,
+                              uint32_t* rowbits) {
+    const int lane = threadIdx.x & 31;
+    const int gO = sc.gap_open, gE = sc.gap_extend;
+    const int width = 2 * bw + 3;
+    constexpr int NEG = -(1 << 28);
+    int prevH = 0, prevE = 0, mx = 0;
+    for (int i = 0; i < ql; i++) {
+        const int x = i - bw > 0 ? i - bw : 0, xe = i - 1 - bw > 0 ? i - 1 - bw : 0;
+        const int end = rl - 1 < i + bw ? rl - 1 : i + bw;
+        const int n = end - x + 1;
+        const int edge = end + 1 < width - 1 ? end + 1 : width - 1;
+        const int sh = x - xe;
+        const bool act = lane < n;
+        // previous row: H and E at column j (band index e = lane + sh + 1), H at j - 1
+        const int su = lane + sh < 31 ? lane + sh : 31;
+        const int sd = lane + sh - 1 > 0 ? lane + sh - 1 : 0;
+        int upH = __shfl_sync(FULLM, prevH, su), upE = __shfl_sync(FULLM, prevE, su);
+        int dg = __shfl_sync(FULLM, prevH, sd);
+        if (lane + sh + 1 == edge) {
+            upH = 0;
+            upE = 0;
+        }
+        if (lane + sh == 0) dg = 0;
+        const int t1 = i == 0 ? -gO : upH - gO;
+        const int t2 = i == 0 ? -gE : upE - gE;
+        const int E = t1 > t2 ? t1 : t2;
+        const bool dde3 = t1 > t2;
+        int D = 0;
+        if (act) D = dg + mat_score(c_ssw_code[ref[x + lane]], c_ssw_code[read[i]], sc);
+        const int e1 = E > 0 ? E : 0;
+        const int B = e1 > D ? e1 : D;
+        int T = act ? B - gO : NEG;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int Tp = __shfl_up_sync(FULLM, T, d);
+            const int c = Tp - d * gE;
+            if (lane >= d && c > T) T = c;
+        }
+        int Sx = __shfl_up_sync(FULLM, T, 1);
+        if (lane == 0) Sx = NEG;
+        const int f0 = -(lane + 1) * gE;
+        const int f = Sx > f0 ? Sx : f0;
+        const int f1 = f > 0 ? f : 0;
+        const int H = B > f1 ? B : f1;
+        int Hl = __shfl_up_sync(FULLM, H, 1), fl = __shfl_up_sync(FULLM, f, 1);
+        if (lane == 0) {
+            Hl = 0;
+            fl = 0;
+        }
+        const bool ddf5 = Hl - gO > fl - gE;
+        const int tm = e1 > f1 ? e1 : f1;
+        if (act && H > mx) mx = H;
+        if (rowbits) {
+            const unsigned b0 = __ballot_sync(FULLM, act && dde3);
+            const unsigned b1 = __ballot_sync(FULLM, act && ddf5);
+            const unsigned b2 = __ballot_sync(FULLM, act && tm <= D);
+            const unsigned b3 = __ballot_sync(FULLM, act && e1 > f1);
+            if (lane == 0) {
+                rowbits[4 * i] = b0;
+                rowbits[4 * i + 1] = b1;
+                rowbits[4 * i + 2] = b2;
+                rowbits[4 * i + 3] = b3;
+            }
+        }
+        prevH = act ? H : 0;
+        prevE = act ? E : 0;
+    }
+    for (int d = 16; d > 0; d >>= 1) {
+        const int o = __shfl_xor_sync(FULLM, mx, d);
+        mx = mx > o ? mx : o;
+    }
+    return mx;
+}
+
+__global__ void __launch_bounds__(128) k_band_warp(SswTask* tasks, uint32_t n_tasks, const PrepRec* prep,
+                                                   const uint8_t* arena, int32_t* hscratch, AlignScores sc,
+                                                   uint32_t* counters) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        uint32_t ti = 0;
+        if (lane == 0) ti = atomicAdd(&counters[6], 1u);
+        ti = __shfl_sync(FULLM, ti, 0);
+        if (ti >= n_tasks) break;
+        SswTask tk = tasks[ti];
+        if (tk.ref_begin1 < 0 || tk.read_begin1 < 0) continue;
+        const PrepRec p = prep[tk.job];
+        const uint8_t* q = arena + p.arena_off;
+        const uint8_t* r = q + p.qlen;
+        const int rl = tk.ref_end1 - tk.ref_begin1 + 1, ql = tk.read_end1 - tk.read_begin1 + 1;
+        const int len = rl > ql ? rl : ql;
+        int bw = (rl > ql ? rl - ql : ql - rl) + 1;
+        // band doubling (ext/ssw/ssw.c:626-660)
+        bool fallback = false;
+        int mx = 0;
+        do {
+            if (bw > 15) {
+                fallback = true;
+                break;
+            }
+            mx = band_pass_warp(r + tk.ref_begin1, q + tk.read_begin1, rl, ql, bw, sc, nullptr);
+            bw *= 2;
+        } while (mx < tk.score1 && bw <= len);
+        if (fallback) continue;  // raw_off stays RAW_FALLBACK
+        bw /= 2;
+        uint32_t* rowbits = reinterpret_cast<uint32_t*>(hscratch + p.h_off);
+        band_pass_warp(r + tk.ref_begin1, q + tk.read_begin1, rl, ql, bw, sc, rowbits);
+        __syncwarp();
+        if (lane == 0) {
+            // traceback (ext/ssw/ssw.c:680-753) over the flat direction array of
+            // (2bw+1) x 3 bytes per row
+            uint32_t* c = rowbits + 4 * (size_t)ql;
+            const int width_d = 2 * bw + 1;
+            const int64_t dsize = (int64_t)width_d * ql * 3;
+            auto dir_at = [&](int64_t at) -> int {
+                const int row = (int)(at / (3 * width_d));
+                const int rem = (int)(at % (3 * width_d));
+                const int k = rem / 3, w = rem % 3;
+                const int x = row - bw > 0 ? row - bw : 0;
+                const int end = rl - 1 < row + bw ? rl - 1 : row + bw;
+                if (k > end - x) return 0;  // not written by the pass
+                const uint32_t* rb = rowbits + 4 * (size_t)row;
+                const int dde = (rb[0] >> k) & 1 ? 3 : 2;
+                const int ddf = (rb[1] >> k) & 1 ? 5 : 4;
+                if (w == 0) return dde;
+                if (w == 1) return ddf;
+                return (rb[2] >> k) & 1 ? 1 : ((rb[3] >> k) & 1 ? dde : ddf);
+            };
+            int i = ql - 1, j = rl - 1, e = 0, which = 2;
+            int64_t line = (int64_t)width_d * i * 3;
+            char op = 'M', prev = 'M';
+            uint32_t nc = 0;
+            const uint32_t cap = (uint32_t)(rl + ql + 4);
+            bool fail = false;
+            auto enc = [](int l, char o) -> uint32_t {
+                return ((uint32_t)l << 4) | (o == 'M' ? 0u : o == 'I' ? 1u : 2u);
+            };
+            while (i >= 0 && j > 0) {
+                const int x = i - bw > 0 ? i - bw : 0;
+                const int64_t at = line + (int64_t)(j - x) * 3 + which;
+                if (at < 0 || at >= dsize) {
+                    fail = true;
+                    break;
+                }
+                switch (dir_at(at)) {
+                    case 1: --i; --j; which = 2; line -= width_d * 3; op = 'M'; break;
+                    case 2: --i; which = 0; line -= width_d * 3; op = 'I'; break;
+                    case 3: --i; which = 2; line -= width_d * 3; op = 'I'; break;
+                    case 4: --j; which = 1; op = 'D'; break;
+                    case 5: --j; which = 2; op = 'D'; break;
+                    default: fail = true;
+                }
+                if (fail) break;
+                if (op == prev) ++e;
+                else {
+                    if (nc >= cap) {
+                        fail = true;
+                        break;
+                    }
+                    c[nc++] = enc(e, prev);
+                    prev = op;
+                    e = 1;
+                }
+            }
+            if (!fail) {
+                if (nc + 2 > cap) fail = true;
+                else if (op == 'M') c[nc++] = enc(e + 1, op);
+                else {
+                    c[nc++] = enc(e, op);
+                    c[nc++] = enc(1, 'M');
+                }
+            }
+            tk.band_width = bw;
+            if (fail) {
+                tk.flag = 1;
+                tk.raw_len = 0;
+            } else {
+                for (uint32_t a = 0, b = nc - 1; a < b; a++, b--) {
+                    const uint32_t tmp = c[a];
+                    c[a] = c[b];
+                    c[b] = tmp;
+                }
+                tk.raw_len = nc;
+            }
+            tk.raw_off = (uint64_t)p.h_off + 4 * (uint64_t)ql;
+            tasks[ti] = tk;
+        }
+        __syncwarp();
+    }
+}
+
 __global__ void k_band_width(SswTask* tasks, const uint32_t* n_tasks_ptr, const PrepRec* prep, const uint8_t* arena,
                              int32_t* hscratch, AlignScores sc, uint64_t* dir_size, uint64_t* raw_size) {
     const uint32_t n = *n_tasks_ptr;
@@ -517,7 +1291,7 @@ __global__ void k_band_width(SswTask* tasks, const uint32_t* n_tasks_ptr, const 
         SswTask tk = tasks[ti];
         dir_size[ti] = 0;
         raw_size[ti] = 0;
-        if (tk.ref_begin1 < 0 || tk.read_begin1 < 0) continue;
+        if (tk.ref_begin1 < 0 || tk.read_begin1 < 0 || tk.raw_off != RAW_FALLBACK) continue;
         const PrepRec p = prep[tk.job];
         const uint8_t* q = arena + p.arena_off;
         const uint8_t* r = q + p.qlen;
@@ -548,7 +1322,7 @@ __global__ void k_band_trace(SswTask* tasks, const uint32_t* n_tasks_ptr, const 
     const uint32_t n = *n_tasks_ptr;
     for (uint32_t ti = blockIdx.x * blockDim.x + threadIdx.x; ti < n; ti += gridDim.x * blockDim.x) {
         SswTask tk = tasks[ti];
-        if (tk.ref_begin1 < 0 || tk.read_begin1 < 0 || tk.flag == 1) continue;
+        if (tk.ref_begin1 < 0 || tk.read_begin1 < 0 || tk.flag == 1 || tk.raw_off != RAW_FALLBACK) continue;
         const PrepRec p = prep[tk.job];
         const uint8_t* q = arena + p.arena_off;
         const uint8_t* r = q + p.qlen;
@@ -616,8 +1390,8 @@ __global__ void k_band_trace(SswTask* tasks, const uint32_t* n_tasks_ptr, const 
 
 // SswAligner::align (src/ssw.rs:156-188) + Aligner::align end bonus (src/aligner.rs:92-148)
 __global__ void k_finalize(const SswTask* tasks, const uint32_t* n_tasks_ptr, const PrepRec* prep, const uint8_t* arena,
-                           const uint64_t* raw_off, const uint32_t* raw, AlignScores sc, uint32_t* cigar,
-                           ExtResult* res) {
+                           const uint64_t* raw_off, const uint32_t* raw, const int32_t* hscratch, AlignScores sc,
+                           uint32_t* cigar, ExtResult* res) {
     const uint32_t n = *n_tasks_ptr;
     for (uint32_t ti = blockIdx.x * blockDim.x + threadIdx.x; ti < n; ti += gridDim.x * blockDim.x) {
         const SswTask tk = tasks[ti];
@@ -634,7 +1408,8 @@ __global__ void k_finalize(const SswTask* tasks, const uint32_t* n_tasks_ptr, co
         uint32_t qs = tk.read_begin1, qe = tk.read_end1 + 1, rs = tk.ref_begin1, re = tk.ref_end1 + 1;
         int32_t score = tk.score1;
         // M -> =/X over the aligned segments; reject walks past them (the reference panics there)
-        const uint32_t* rw = raw + raw_off[ti];
+        const uint32_t* rw = tk.raw_off == RAW_FALLBACK ? raw + raw_off[ti]
+                                                        : reinterpret_cast<const uint32_t*>(hscratch) + tk.raw_off;
         uint32_t ed = 0;
         bool bad = false;
         {
@@ -797,7 +1572,7 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
     ws.prep.reserve(n);
     ws.sizes.reserve(3 * ((size_t)n + 1));
     ws.offs.reserve(3 * ((size_t)n + 1));
-    ws.counters.reserve(16);
+    ws.counters.reserve(24);
     if (n == 0) {
         ws.h_results.clear();
         ws.h_cigar.clear();
@@ -805,12 +1580,26 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
     }
     uint64_t* sz[3] = {ws.sizes.p, ws.sizes.p + n + 1, ws.sizes.p + 2 * ((size_t)n + 1)};
     uint64_t* of[3] = {ws.offs.p, ws.offs.p + n + 1, ws.offs.p + 2 * ((size_t)n + 1)};
-    SA_CUDA(cudaMemsetAsync(ws.counters.p, 0, 16 * sizeof(uint32_t), st));
+    SA_CUDA(cudaMemsetAsync(ws.counters.p, 0, 24 * sizeof(uint32_t), st));
     kt->begin(KS_PREPARE, st);
+    ws.rescue_list.reserve(n);
     k_prepare<<<grid1(n), 256, 0, st>>>(ws.jobs.p, n, seq, off, refs, k, raw_refs, raw_off, ws.results.p, ws.prep.p,
-                                        sz[0], sz[1], sz[2]);
+                                        sz[0], sz[1], sz[2], ws.rescue_list.p, ws.counters.p + 4);
+    {
+        static bool attr = false;
+        const size_t smem = 2 * RESCUE_TAB_MAX * sizeof(unsigned long long);
+        if (!attr) {
+            SA_CUDA(cudaFuncSetAttribute(k_rescue_filter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            attr = true;
+        }
+        uint64_t blocks = ((uint64_t)n + 1) / 2;
+        if (blocks > 152ULL * 3) blocks = 152ULL * 3;
+        k_rescue_filter<<<(unsigned)(blocks ? blocks : 1), 64, smem, st>>>(ws.rescue_list.p, ws.counters.p + 4, seq,
+                                                                           off, refs, k, ws.prep.p, sz[0], sz[1],
+                                                                           sz[2]);
+    }
     kt->end(st);
-    launches++;
+    launches += 2;
     // exclusive scans of arena bytes, CIGAR capacity and banded-DP scratch per job
     uint64_t tot[3];
     for (int c = 0; c < 3; c++) {
@@ -853,30 +1642,90 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
             if (b > 152ULL * 16) b = 152ULL * 16;
             return (unsigned)(b ? b : 1);
         };
+        // register kernels while the profile fits in int8 and a lane's rows in SEG
+        const bool reg_ok = sc.match <= 127 && sc.mismatch <= 128;
+        const int segr_b = !reg_ok ? 0 : seg_b <= 8 ? 8 : seg_b <= 16 ? 16 : seg_b <= 32 ? 32 : 0;
+        const int segr_w = !reg_ok ? 0 : seg_w <= 8 ? 8 : seg_w <= 20 ? 20 : seg_w <= 32 ? 32 : 0;
+        // one striped pass over a task list: byte or word, forward (pass 0) or reverse (pass 1)
+        auto sw_launch = [&](bool word, const uint32_t* list, const uint32_t* n_ptr, uint32_t n_host, int pass) {
+            const int G = word ? 8 : 16;
+            const unsigned grid = blocks_for(n_tasks, tpb / G);
+            const int segr = word ? segr_w : segr_b;
+            const size_t smem_r = (size_t)(tpb / G) * 5 * G * ((segr + 3) / 4) * 4;
+#define SA_SWR(W, S)                                                                                              \
+    k_swr<W, S><<<grid, tpb, smem_r, st>>>(ws.tasks.p, list, n_ptr, n_host, ws.prep.p, ws.arena.p, sc, bias, pass, \
+                                           ws.counters.p, ws.list_word.p, ws.list_rev_byte.p, ws.list_rev_word.p)
+            if (!word && segr == 8) SA_SWR(false, 8);
+            else if (!word && segr == 16) SA_SWR(false, 16);
+            else if (!word && segr == 32) SA_SWR(false, 32);
+            else if (word && segr == 8) SA_SWR(true, 8);
+            else if (word && segr == 20) SA_SWR(true, 20);
+            else if (word && segr == 32) SA_SWR(true, 32);
+            else if (!word)
+                k_sw<false><<<grid, tpb, smem_b, st>>>(ws.tasks.p, list, n_ptr, n_host, ws.prep.p, ws.arena.p, sc,
+                                                       bias, pass, seg_b, ws.counters.p, ws.list_word.p,
+                                                       ws.list_rev_byte.p, ws.list_rev_word.p);
+            else
+                k_sw<true><<<grid, tpb, smem_w, st>>>(ws.tasks.p, list, n_ptr, n_host, ws.prep.p, ws.arena.p, sc,
+                                                      bias, pass, seg_w, ws.counters.p, ws.list_word.p,
+                                                      ws.list_rev_byte.p, ws.list_rev_word.p);
+#undef SA_SWR
+        };
+        // rows per thread of the warp-per-task kernel: ceil(segLen / S) in both modes
+        const int rows = std::max((seg_b + 1) / 2, (seg_w + 3) / 4);
+        const int rmax = rows <= 4 ? 4 : rows <= 8 ? 8 : rows <= 16 ? 16 : 0;
+        const bool fused = reg_ok && sc.gap_open >= sc.gap_extend && rmax;
+        if (fused) {
+            // one launch for every pass, longest windows first
+            ws.order.reserve(n_tasks);
+            kt->begin(KS_SW_BYTE, st);
+            k_task_keys<<<grid1(n_tasks), 256, 0, st>>>(ws.tasks.p, n_tasks, ws.prep.p, ws.list_word.p,
+                                                        ws.list_rev_word.p);
+            size_t tmp = 0;
+            cub::DeviceRadixSort::SortPairs(nullptr, tmp, ws.list_word.p, ws.list_rev_byte.p, ws.list_rev_word.p,
+                                            ws.order.p, (int)n_tasks, 0, 16, st);
+            ws.cub_tmp.reserve(tmp);
+            cub::DeviceRadixSort::SortPairs(ws.cub_tmp.p, tmp, ws.list_word.p, ws.list_rev_byte.p,
+                                            ws.list_rev_word.p, ws.order.p, (int)n_tasks, 0, 16, st);
+            const int wpb = tpb / 32;
+            uint64_t blocks = ((uint64_t)n_tasks + wpb - 1) / wpb;
+            if (blocks > 152ULL * 16) blocks = 152ULL * 16;
+#define SA_SSW(RM)                                                                                              \
+    k_ssw<RM><<<(unsigned)blocks, tpb, (size_t)wpb * 5 * 32 * ((RM + 3) / 4) * 4, st>>>(                       \
+        ws.tasks.p, ws.order.p, n_tasks, ws.prep.p, ws.arena.p, sc, bias, ws.counters.p)
+            if (rmax == 4) SA_SSW(4);
+            else if (rmax == 8) SA_SSW(8);
+            else SA_SSW(16);
+#undef SA_SSW
+            kt->end(st);
+            launches += 3;
+        } else {
         // forward byte pass over all tasks
         kt->begin(KS_SW_BYTE, st);
-        k_sw<false><<<blocks_for(n_tasks, tpb / 16), tpb, smem_b, st>>>(
-            ws.tasks.p, nullptr, nullptr, n_tasks, ws.prep.p, ws.arena.p, sc, bias, 0, seg_b, ws.counters.p,
-            ws.list_word.p, ws.list_rev_byte.p, ws.list_rev_word.p);
+        sw_launch(false, nullptr, nullptr, n_tasks, 0);
         kt->end(st);
         // forward word pass over the overflowed tasks
         kt->begin(KS_SW_WORD, st);
-        k_sw<true><<<blocks_for(n_tasks, tpb / 8), tpb, smem_w, st>>>(
-            ws.tasks.p, ws.list_word.p, ws.counters.p + 1, 0, ws.prep.p, ws.arena.p, sc, bias, 0, seg_w,
-            ws.counters.p, ws.list_word.p, ws.list_rev_byte.p, ws.list_rev_word.p);
+        sw_launch(true, ws.list_word.p, ws.counters.p + 1, 0, 0);
         kt->end(st);
         // reverse passes
         kt->begin(KS_SW_BYTE, st);
-        k_sw<false><<<blocks_for(n_tasks, tpb / 16), tpb, smem_b, st>>>(
-            ws.tasks.p, ws.list_rev_byte.p, ws.counters.p + 2, 0, ws.prep.p, ws.arena.p, sc, bias, 1, seg_b,
-            ws.counters.p, ws.list_word.p, ws.list_rev_byte.p, ws.list_rev_word.p);
+        sw_launch(false, ws.list_rev_byte.p, ws.counters.p + 2, 0, 1);
         kt->end(st);
         kt->begin(KS_SW_WORD, st);
-        k_sw<true><<<blocks_for(n_tasks, tpb / 8), tpb, smem_w, st>>>(
-            ws.tasks.p, ws.list_rev_word.p, ws.counters.p + 3, 0, ws.prep.p, ws.arena.p, sc, bias, 1, seg_w,
-            ws.counters.p, ws.list_word.p, ws.list_rev_byte.p, ws.list_rev_word.p);
+        sw_launch(true, ws.list_rev_word.p, ws.counters.p + 3, 0, 1);
         kt->end(st);
         launches += 4;
+        }
+        if (sc.gap_open >= sc.gap_extend) {
+            kt->begin(KS_BAND, st);
+            uint64_t blocks = ((uint64_t)n_tasks + 3) / 4;
+            if (blocks > 152ULL * 16) blocks = 152ULL * 16;
+            k_band_warp<<<(unsigned)blocks, 128, 0, st>>>(ws.tasks.p, n_tasks, ws.prep.p, ws.arena.p, ws.hscratch.p,
+                                                          sc, ws.counters.p);
+            kt->end(st);
+            launches++;
+        }
         ws.dir_size.reserve((size_t)n_tasks + 1);
         ws.dir_off.reserve((size_t)n_tasks + 1);
         ws.raw_size.reserve((size_t)n_tasks + 1);
@@ -905,7 +1754,8 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
         kt->end(st);
         kt->begin(KS_FINALIZE, st);
         k_finalize<<<grid1(n_tasks, 128), 128, 0, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p,
-                                                        ws.raw_off.p, ws.raw.p, sc, ws.cigar.p, ws.results.p);
+                                                        ws.raw_off.p, ws.raw.p, ws.hscratch.p, sc, ws.cigar.p,
+                                                        ws.results.p);
         kt->end(st);
         launches += 2;
     }
@@ -925,7 +1775,7 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
     SA_CUDA(cudaMemcpyAsync(ws.h_results.data(), ws.results.p, (size_t)n * sizeof(ExtResult), cudaMemcpyDeviceToHost,
                             st));
     if (used) SA_CUDA(cudaMemcpyAsync(ws.h_cigar.data(), ws.raw.p, used * 4, cudaMemcpyDeviceToHost, st));
-    SA_CUDA(cudaMemcpyAsync(ws.cells, ws.counters.p + 8, 4 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    SA_CUDA(cudaMemcpyAsync(ws.cells, ws.counters.p + 8, 5 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
     SA_CUDA(cudaStreamSynchronize(st));
     tot[1] = used;
     ws.total_cigar = tot[1];

@@ -49,8 +49,10 @@ struct ExtWorkspace {
     DevBuf<uint32_t> cigar;
     DevBuf<int32_t> hscratch;
     DevBuf<SswTask> tasks;
-    DevBuf<uint32_t> counters;  // [0] n_tasks [1] n_word [2] n_rev_byte [3] n_rev_word
+    DevBuf<uint32_t> counters;  // [0] n_tasks [1] n_word [2] n_rev_byte [3] n_rev_word [4] n_rescue, u64 cells at [8]
+    DevBuf<uint32_t> rescue_list;
     DevBuf<uint32_t> list_word, list_rev_byte, list_rev_word;
+    DevBuf<uint32_t> order;  // task order of the fused SSW kernel
     DevBuf<uint64_t> dir_size, dir_off;
     DevBuf<uint8_t> dir;
     DevBuf<uint64_t> raw_size, raw_off;
@@ -60,7 +62,7 @@ struct ExtWorkspace {
     std::vector<ExtResult> h_results;
     std::vector<uint32_t> h_cigar;
     uint64_t total_cigar = 0;
-    uint64_t cells[4] = {0, 0, 0, 0};  // SW cells: forward byte, forward word, reverse byte, reverse word
+    uint64_t cells[5] = {0, 0, 0, 0, 0};  // SW cells: canonical, then computed forward byte / word, reverse byte / word
 };
 
 // Runs jobs (already in ws.jobs, n of them) against the reads in nws.seq/nws.off.
@@ -68,5 +70,10 @@ struct ExtWorkspace {
 // number of kernel launches.
 uint32_t run_extension(const DevRefs& refs, const NamWorkspace& nws, uint32_t k, const AlignScores& sc, uint32_t n,
                        ExtWorkspace& ws, uint32_t max_qlen, cudaStream_t st, KernelTimers* kt = nullptr);
+// The same for reads at seq + off[read] (off holds n_reads + 1 absolute offsets);
+// raw_refs / raw_off give the reference bytes of JOB_ALIGN jobs (may be null).
+uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64_t* off, const uint8_t* raw_refs,
+                           const uint64_t* raw_off, uint32_t k, const AlignScores& sc, uint32_t n, ExtWorkspace& ws,
+                           uint32_t max_qlen, cudaStream_t st, KernelTimers* kt = nullptr);
 
 }  // namespace sa

@@ -7,6 +7,8 @@
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <exception>
@@ -20,6 +22,9 @@ namespace sa {
 Mapper::Mapper(const sa_index* idx, const sa_refs* refs, const sa_chaining_params& cp, const sa_mapping_params& mp)
     : idx_(idx), refs_(refs), cp_(cp), mp_(mp) {
     if (mp.rg_id) rg_id_ = mp.rg_id;
+    // SA_TRACE_WAVES=1: one line per extension wave on stderr
+    const char* tr = std::getenv("SA_TRACE_WAVES");
+    trace_ = tr && *tr && *tr != '0';
     SA_CUDA(cudaSetDevice(idx->device));
     SA_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
     const auto& cs = refs->contigs;
@@ -114,9 +119,9 @@ uint32_t Mapper::run_wave(ResultStore& store, const std::vector<ExtJob>& jobs, u
     AlignScores sc{mp_.match, mp_.mismatch, mp_.gap_open, mp_.gap_extend, mp_.end_bonus};
     uint32_t launches = run_extension(refs_view_, nws_, idx_->sp.k, sc, nj, ews_, max_qlen, st_, &kt_);
     d2h_bytes_ += (size_t)nj * sizeof(ExtResult) + ews_.total_cigar * 4;
-    for (int c = 0; c < 4; c++) sw_cells_[c] += ews_.cells[c];
-    store.cigars.emplace_back(ews_.h_cigar.begin(), ews_.h_cigar.end());
-    const uint32_t* cig = store.cigars.back().data();
+    for (int c = 0; c < 5; c++) sw_cells_[c] += ews_.cells[c];
+    store.cigars.push_back(std::make_shared<const std::vector<uint32_t>>(ews_.h_cigar.begin(), ews_.h_cigar.end()));
+    const uint32_t* cig = store.cigars.back()->data();
     for (uint32_t j = 0; j < nj; j++) {
         StoredResult r;
         static_cast<ExtResult&>(r) = ews_.h_results[j];
@@ -261,6 +266,7 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, ResultStore& store, u
     uint32_t waves = 0;
     std::vector<ExtJob> jobs;
     std::vector<size_t> batch;
+    const auto t_sched0 = std::chrono::steady_clock::now();
     try {
         std::unique_lock<std::mutex> lk(mu);
         for (;;) {
@@ -286,7 +292,18 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, ResultStore& store, u
             if (waves > 1000000) throw Error(SA_ERR_INVALID, "internal: extension waves do not converge");
             auto tw = std::chrono::steady_clock::now();
             launches += run_wave(store, jobs, max_qlen_);
-            t_ext_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - tw).count();
+            const auto tw2 = std::chrono::steady_clock::now();
+            t_ext_ += std::chrono::duration<double>(tw2 - tw).count();
+            if (trace_) {
+                uint64_t kinds[4] = {0, 0, 0, 0};
+                for (auto& j : jobs) kinds[j.kind & 3]++;
+                std::fprintf(stderr,
+                             "sa_wave %u t=%.4f dur=%.4f chunks=%zu jobs=%zu fast=%llu full=%llu rescue=%llu align=%llu\n",
+                             waves, std::chrono::duration<double>(tw - t_sched0).count(),
+                             std::chrono::duration<double>(tw2 - tw).count(), batch.size(), jobs.size(),
+                             (unsigned long long)kinds[0], (unsigned long long)kinds[1],
+                             (unsigned long long)kinds[2], (unsigned long long)kinds[3]);
+            }
             waves++;
             lk.lock();
             for (size_t c : batch) ready.push_back(c);
@@ -316,7 +333,7 @@ void Mapper::map_uploaded(sa_output* out) {
     jobs_run_ = 0;
     t_ext_ = 0;
     kt_.reset();
-    for (int c = 0; c < 4; c++) sw_cells_[c] = 0;
+    for (int c = 0; c < 5; c++) sw_cells_[c] = 0;
     nams_for_reads(launches);
     auto t1 = std::chrono::steady_clock::now();
     bv.nams = h_nams_.data();
@@ -377,7 +394,7 @@ void Mapper::map_uploaded(sa_output* out) {
     stats_.n_nams = h_nams_.size();
     stats_.n_anchors = 0;
     kt_.collect();
-    for (int c = 0; c < 4; c++) stats_.sw_cells[c] = sw_cells_[c];
+    for (int c = 0; c < 5; c++) stats_.sw_cells[c] = sw_cells_[c];
     for (int i = 0; i < 16; i++) {
         stats_.kernel_ms[i] = i < KS_COUNT ? kt_.ms[i] : 0.0;
         stats_.kernel_launches[i] = i < KS_COUNT ? kt_.launches[i] : 0;

@@ -49,9 +49,10 @@ class Mapper {
     sa_mapper_stats stats_{};
     double t_ext_ = 0;
     KernelTimers kt_;
-    uint64_t sw_cells_[4] = {0, 0, 0, 0};
+    uint64_t sw_cells_[5] = {0, 0, 0, 0, 0};
     unsigned policy_threads_ = std::max(1u, std::thread::hardware_concurrency());
     uint64_t wave_min_jobs_ = 32768;
+    bool trace_ = false;
 
     const sa_index* idx_;
     const sa_refs* refs_;

@@ -5,6 +5,7 @@
 #pragma once
 #include <cstdint>
 #include <deque>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -70,7 +71,7 @@ struct ResultStore {
     };
     std::vector<std::vector<Entry>> per_read;
     std::deque<StoredResult> results;
-    std::deque<std::vector<uint32_t>> cigars;  // one per wave
+    std::vector<std::shared_ptr<const std::vector<uint32_t>>> cigars;  // the waves' CIGAR copies referenced here
 };
 
 struct ReadView {

@@ -1,0 +1,511 @@
+// Serving engine: continuous batching of mapping requests on one GPU.
+//
+// One engine thread owns the device work: it admits queued requests into the
+// read arena (upload, NAM pipeline, NAMs copied back) and runs extension waves
+// over the requests of every chunk that stopped on a miss, whichever request it
+// belongs to.  Policy threads run the chunks whose results are in.  A wave starts
+// once enough jobs wait or when the policy threads have nothing left to run; a
+// request is admitted when its reads fit in the arena.
+#include <algorithm>
+#include <cstring>
+
+#include "session.h"
+
+namespace sa {
+
+bool RangeAllocator::alloc(uint64_t n, uint64_t& at) {
+    if (n == 0) n = 1;
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+        if (it->second >= n) {
+            at = it->first;
+            const uint64_t rest = it->second - n;
+            const uint64_t start = it->first + n;
+            free_.erase(it);
+            if (rest) free_[start] = rest;
+            return true;
+        }
+    }
+    return false;
+}
+
+void RangeAllocator::release(uint64_t at, uint64_t n) {
+    if (n == 0) n = 1;
+    auto it = free_.emplace(at, n).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+        it->second += nx->second;
+        free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+        auto pv = std::prev(it);
+        if (pv->first + pv->second == it->first) {
+            pv->second += it->second;
+            free_.erase(it);
+        }
+    }
+}
+
+uint64_t RangeAllocator::largest_free() const {
+    uint64_t m = 0;
+    for (auto& f : free_) m = std::max(m, f.second);
+    return m;
+}
+
+Session::Session(const sa_index* idx, const sa_refs* refs, const sa_chaining_params& cp, const sa_mapping_params& mp,
+                 const SessionConfig& sc)
+    : idx_(idx), refs_(refs), cp_(cp), mp_(mp), cfg_(sc) {
+    if (mp.rg_id) rg_id_ = mp.rg_id;
+    mp_.rg_id = nullptr;
+    SA_CUDA(cudaSetDevice(idx->device));
+    SA_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    const auto& cs = refs->contigs;
+    const uint32_t nc = (uint32_t)cs.size();
+    std::vector<uint64_t> woff(nc);
+    std::vector<uint32_t> clen(nc);
+    uint64_t nw = 0;
+    for (uint32_t c = 0; c < nc; c++) {
+        woff[c] = nw;
+        nw += cs[c].words.size() + 1;
+        clen[c] = (uint32_t)cs[c].len;
+        max_contig_len_ = std::max<uint32_t>(max_contig_len_, clen[c]);
+        contigs_.push_back(ContigInfo{&cs[c].name, cs[c].len});
+    }
+    std::vector<uint64_t> hw(nw, 0);
+    for (uint32_t c = 0; c < nc; c++) std::copy(cs[c].words.begin(), cs[c].words.end(), hw.begin() + woff[c]);
+    d_words_.reserve(std::max<uint64_t>(nw, 1));
+    d_woff_.reserve(std::max<uint32_t>(nc, 1));
+    d_clen_.reserve(std::max<uint32_t>(nc, 1));
+    if (nw) SA_CUDA(cudaMemcpy(d_words_.p, hw.data(), nw * 8, cudaMemcpyHostToDevice));
+    if (nc) {
+        SA_CUDA(cudaMemcpy(d_woff_.p, woff.data(), nc * 8, cudaMemcpyHostToDevice));
+        SA_CUDA(cudaMemcpy(d_clen_.p, clen.data(), nc * 4, cudaMemcpyHostToDevice));
+    }
+    refs_view_ = DevRefs{d_words_.p, d_woff_.p, d_clen_.p, nc};
+    pcfg_.mp = mp_;
+    pcfg_.rg_id = rg_id_;
+    pcfg_.has_rg = mp.rg_id != nullptr;
+    pcfg_.k = idx->sp.k;
+    if (cfg_.max_inflight_bases == 0) cfg_.max_inflight_bases = 1ull << 30;
+    const uint64_t slots = cfg_.max_inflight_bases / 32 + 65536;
+    arena_seq_.reserve(cfg_.max_inflight_bases + 16);
+    arena_off_.reserve(slots);
+    seq_alloc_.reset(cfg_.max_inflight_bases);
+    off_alloc_.reset(slots);
+    unsigned nt = cfg_.policy_threads ? cfg_.policy_threads : std::max(1u, std::thread::hardware_concurrency());
+    engine_ = std::thread([this] { engine(); });
+    for (unsigned t = 0; t < nt; t++) workers_.emplace_back([this] { worker(); });
+}
+
+Session::~Session() {
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        stop_ = true;
+        for (auto& q : queue_) {
+            q->state = 3;
+            q->error = "session destroyed before the request was admitted";
+            q->error_code = SA_ERR_CANCELLED;
+        }
+        queue_.clear();
+    }
+    cv_engine_.notify_all();
+    cv_done_.notify_all();
+    if (engine_.joinable()) engine_.join();
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        workers_stop_ = true;
+    }
+    cv_work_.notify_all();
+    for (auto& t : workers_) t.join();
+    if (st_) cudaStreamDestroy(st_);
+}
+
+uint64_t Session::submit(const sa_read_batch* r1, const sa_read_batch* r2) {
+    if (!r1) throw Error(SA_ERR_INVALID, "null read batch");
+    const bool paired = r2 != nullptr;
+    if (paired && r2->n != r1->n) throw Error(SA_ERR_INVALID, "r1 and r2 batches differ in size");
+    if (!paired && mp_.mode == SA_MODE_SAM && !mp_.use_ssw)
+        throw Error(SA_ERR_INVALID,
+                    "single-end SAM output needs use_ssw=1: the piecewise (block-aligner) extension is not "
+                    "implemented on the GPU");
+    auto r = std::make_unique<Request>();
+    r->paired = paired;
+    r->nrec = r1->n;
+    r->n_reads = paired ? 2 * r1->n : r1->n;
+    r->has_qual = r1->qual != nullptr && (!paired || r2->qual != nullptr);
+    r->has_comments = r1->comments && r1->comment_offsets;
+    r->seq_off.assign(1, 0);
+    r->name_off.assign(1, 0);
+    r->comment_off.assign(1, 0);
+    r->seq_off.reserve(r->n_reads + 1);
+    auto add = [&](const sa_read_batch* b, uint64_t i) {
+        const uint64_t s0 = b->seq_offsets[i], s1 = b->seq_offsets[i + 1];
+        if (s1 - s0 > MAX_READ_LEN)
+            throw Error(SA_ERR_INVALID, "read longer than " + std::to_string(MAX_READ_LEN) + " nt");
+        r->seq.insert(r->seq.end(), b->seq + s0, b->seq + s1);
+        if (r->has_qual) r->qual.insert(r->qual.end(), b->qual + s0, b->qual + s1);
+        r->seq_off.push_back(r->seq.size());
+        const uint64_t n0 = b->name_offsets[i], n1 = b->name_offsets[i + 1];
+        r->names.insert(r->names.end(), b->names + n0, b->names + n1);
+        r->name_off.push_back(r->names.size());
+        if (b->comments && b->comment_offsets) {
+            const uint64_t c0 = b->comment_offsets[i], c1 = b->comment_offsets[i + 1];
+            r->comments.insert(r->comments.end(), b->comments + c0, b->comments + c1);
+        }
+        r->comment_off.push_back(r->comments.size());
+    };
+    for (uint64_t i = 0; i < r1->n; i++) {
+        add(r1, i);
+        if (paired) add(r2, i);
+    }
+    r->total_bases = r->seq.size();
+    if (r->total_bases > seq_alloc_.capacity() || r->n_reads + 1 > off_alloc_.capacity())
+        throw Error(SA_ERR_INVALID, "request larger than the session's in-flight capacity (" +
+                                        std::to_string(seq_alloc_.capacity()) + " bases)");
+    r->bv.paired = paired;
+    r->bv.reads.resize(r->n_reads);
+    for (uint64_t i = 0; i < r->n_reads; i++) {
+        ReadView& v = r->bv.reads[i];
+        v.seq = r->seq.data() + r->seq_off[i];
+        v.len = (uint32_t)(r->seq_off[i + 1] - r->seq_off[i]);
+        v.qual = r->has_qual ? r->qual.data() + r->seq_off[i] : nullptr;
+        v.name = r->names.data() + r->name_off[i];
+        v.name_len = (uint32_t)(r->name_off[i + 1] - r->name_off[i]);
+        const uint64_t cl = r->comment_off[i + 1] - r->comment_off[i];
+        v.comment = cl ? r->comments.data() + r->comment_off[i] : nullptr;
+        v.comment_len = (uint32_t)cl;
+        r->max_qlen = std::max(r->max_qlen, v.len);
+    }
+    r->t_submit = std::chrono::steady_clock::now();
+    uint64_t id;
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        if (stop_) throw Error(SA_ERR_CANCELLED, "session is shutting down");
+        if (broken_) throw Error(SA_ERR_CUDA, "session failed: " + broken_msg_);
+        id = next_id_++;
+        r->id = id;
+        queue_.push_back(std::move(r));
+    }
+    cv_engine_.notify_one();
+    return id;
+}
+
+int Session::poll(uint64_t ticket) {
+    std::lock_guard<std::mutex> g(mu_);
+    auto it = live_.find(ticket);
+    if (it != live_.end()) return it->second->state >= 2 ? 1 : 0;
+    for (auto& q : queue_)
+        if (q->id == ticket) return 0;
+    throw Error(SA_ERR_INVALID, "unknown ticket");
+}
+
+bool Session::wait(uint64_t ticket, int64_t timeout_ms, std::unique_ptr<Request>& out) {
+    std::unique_lock<std::mutex> lk(mu_);
+    auto known = [&]() {
+        if (live_.count(ticket)) return true;
+        for (auto& q : queue_)
+            if (q->id == ticket) return true;
+        return false;
+    };
+    if (!known()) throw Error(SA_ERR_INVALID, "unknown ticket");
+    auto done = [&]() {
+        auto it = live_.find(ticket);
+        return it != live_.end() && it->second->state >= 2;
+    };
+    if (timeout_ms < 0) cv_done_.wait(lk, [&] { return done() || !known(); });
+    else if (!cv_done_.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return done() || !known(); }))
+        return false;
+    auto it = live_.find(ticket);
+    if (it == live_.end()) throw Error(SA_ERR_CANCELLED, "request was cancelled");
+    if (it->second->state == 3) {
+        const std::string msg = it->second->error;
+        const int32_t code = it->second->error_code ? it->second->error_code : SA_ERR_INVALID;
+        graveyard_.push_back(std::move(it->second));
+        live_.erase(it);
+        throw Error(code, msg);
+    }
+    out = std::move(it->second);
+    live_.erase(it);
+    return true;
+}
+
+uint64_t Session::in_flight() const {
+    std::lock_guard<std::mutex> g(mu_);
+    return inflight_ + queue_.size();
+}
+
+void Session::engine() {
+    std::vector<std::pair<Request*, size_t>> batch;
+    std::unique_lock<std::mutex> lk(mu_);
+    for (;;) {
+        auto can_admit = [&]() {
+            if (queue_.empty()) return false;
+            if (cfg_.max_inflight_requests && inflight_ >= cfg_.max_inflight_requests) return false;
+            const Request& q = *queue_.front();
+            return seq_alloc_.largest_free() >= std::max<uint64_t>(q.total_bases, 1) &&
+                   off_alloc_.largest_free() >= q.n_reads + 1;
+        };
+        auto idle = [&]() { return running_ == 0 && ready_.empty(); };
+        auto wave_ok = [&]() { return !waiting_.empty() && (waiting_jobs_ >= wave_min_jobs_ || idle()); };
+        cv_engine_.wait(lk, [&] { return (stop_ && inflight_ == 0) || wave_ok() || can_admit(); });
+        if (stop_ && inflight_ == 0) break;
+        const bool big = !waiting_.empty() && waiting_jobs_ >= wave_min_jobs_;
+        if (wave_ok() && (big || !can_admit())) {
+            batch.swap(waiting_);
+            waiting_.clear();
+            waiting_jobs_ = 0;
+            lk.unlock();
+            try {
+                run_wave(batch);
+            } catch (const std::exception& e) {
+                lk.lock();
+                fail_all(e.what(), dynamic_cast<const Error*>(&e) ? static_cast<const Error&>(e).code : SA_ERR_CUDA);
+                return;
+            }
+            lk.lock();
+            for (auto& b : batch) ready_.push_back(b);
+            batch.clear();
+            cv_work_.notify_all();
+            continue;
+        }
+        // admission
+        std::unique_ptr<Request> rq = std::move(queue_.front());
+        queue_.pop_front();
+        Request* r = rq.get();
+        seq_alloc_.alloc(std::max<uint64_t>(r->total_bases, 1), r->seq_base);
+        off_alloc_.alloc(r->n_reads + 1, r->read_base);
+        inflight_++;
+        r->state = 1;
+        r->t_admit = std::chrono::steady_clock::now();
+        live_[r->id] = std::move(rq);
+        lk.unlock();
+        try {
+            admit(*r);
+        } catch (const std::exception& e) {
+            lk.lock();
+            fail_all(e.what(), dynamic_cast<const Error*>(&e) ? static_cast<const Error&>(e).code : SA_ERR_CUDA);
+            return;
+        }
+        lk.lock();
+        if (r->chunks.empty()) {
+            lk.unlock();
+            complete(*r);
+            lk.lock();
+            continue;
+        }
+        for (size_t c = 0; c < r->chunks.size(); c++) ready_.emplace_back(r, c);
+        cv_work_.notify_all();
+    }
+}
+
+void Session::admit(Request& r) {
+    const uint32_t n = (uint32_t)r.n_reads;
+    if (n == 0) return;
+    // reads: pinned staging, local offsets for the NAM pipeline, arena copy for the extension
+    h_seq_.reserve(r.total_bases + 16);
+    h_off_.reserve((size_t)n + 1);
+    std::memcpy(h_seq_.p, r.seq.data(), r.total_bases);
+    std::memcpy(h_off_.p, r.seq_off.data(), ((size_t)n + 1) * 8);
+    nws_.seq.reserve(r.total_bases + 16);
+    nws_.off.reserve((size_t)n + 1);
+    SA_CUDA(cudaMemcpyAsync(nws_.seq.p, h_seq_.p, r.total_bases, cudaMemcpyHostToDevice, st_));
+    SA_CUDA(cudaMemcpyAsync(nws_.off.p, h_off_.p, ((size_t)n + 1) * 8, cudaMemcpyHostToDevice, st_));
+    SA_CUDA(cudaMemcpyAsync(arena_seq_.p + r.seq_base, nws_.seq.p, r.total_bases, cudaMemcpyDeviceToDevice, st_));
+    h_goff_.resize((size_t)n + 1);
+    for (uint32_t i = 0; i <= n; i++) h_goff_[i] = r.seq_base + r.seq_off[i];
+    SA_CUDA(cudaMemcpyAsync(arena_off_.p + r.read_base, h_goff_.data(), ((size_t)n + 1) * 8,
+                            cudaMemcpyHostToDevice, st_));
+    NamConfig cfg;
+    cfg.cp = ChainParams{cp_.max_lookback, cp_.diag_diff_penalty, cp_.gap_length_penalty, cp_.valid_score_threshold,
+                         cp_.max_ref_gap, cp_.matches_weight, cp_.max_diagonal_ratio};
+    cfg.mcs = mp_.mcs_strategy;
+    cfg.rescue_distance = mp_.rescue_distance;
+    run_nam_pipeline(idx_->view(), refs_view_, cfg, n, r.total_bases, max_contig_len_,
+                     (uint32_t)refs_->contigs.size(), nws_, st_);
+    const uint64_t tn = nws_.last_total_nams;
+    r.nam_off.resize((size_t)n + 1);
+    r.nams.resize(tn);
+    r.details.resize(n);
+    SA_CUDA(cudaMemcpyAsync(r.nam_off.data(), nws_.nam_off.p, ((size_t)n + 1) * 8, cudaMemcpyDeviceToHost, st_));
+    if (tn) SA_CUDA(cudaMemcpyAsync(r.nams.data(), nws_.nams.p, tn * sizeof(NamRec), cudaMemcpyDeviceToHost, st_));
+    SA_CUDA(cudaMemcpyAsync(r.details.data(), nws_.details.p, (size_t)n * sizeof(NamDetailsRec),
+                            cudaMemcpyDeviceToHost, st_));
+    SA_CUDA(cudaStreamSynchronize(st_));
+    r.bv.nams = r.nams.data();
+    r.bv.nam_off = r.nam_off.data();
+    r.bv.details = r.details.data();
+    // chunks (src/main.rs:591-604)
+    const bool paired = r.paired;
+    for (uint64_t i = 0; i < r.nrec;) {
+        uint64_t nt = 0, j = i;
+        while (j < r.nrec) {
+            nt += r.bv.reads[paired ? 2 * j : j].len + (paired ? r.bv.reads[2 * j + 1].len : 0);
+            j++;
+            if (nt > mp_.chunk_size) break;
+        }
+        ChunkState cs;
+        cs.first = cs.next = i;
+        cs.end = j;
+        r.chunks.push_back(std::move(cs));
+        i = j;
+    }
+    r.seeded.assign(r.chunks.size(), 0);
+    r.store.per_read.resize(n);
+}
+
+void Session::run_wave(std::vector<std::pair<Request*, size_t>>& batch) {
+    std::sort(batch.begin(), batch.end(), [](const std::pair<Request*, size_t>& a, const std::pair<Request*, size_t>& b) {
+        return a.first->id != b.first->id ? a.first->id < b.first->id : a.second < b.second;
+    });
+    std::vector<ExtJob> jobs;
+    std::vector<Request*> owner;
+    uint32_t max_qlen = 1;
+    for (auto& b : batch) {
+        Request* r = b.first;
+        auto& pend = r->chunks[b.second].pending;
+        for (ExtJob j : pend) {
+            j.read += (uint32_t)r->read_base;
+            jobs.push_back(j);
+            owner.push_back(r);
+        }
+        pend.clear();
+        max_qlen = std::max(max_qlen, r->max_qlen);
+    }
+    const uint32_t nj = (uint32_t)jobs.size();
+    if (!nj) return;
+    ews_.jobs.reserve(nj);
+    SA_CUDA(cudaMemcpyAsync(ews_.jobs.p, jobs.data(), (size_t)nj * sizeof(ExtJob), cudaMemcpyHostToDevice, st_));
+    AlignScores sc{mp_.match, mp_.mismatch, mp_.gap_open, mp_.gap_extend, mp_.end_bonus};
+    run_extension_raw(refs_view_, arena_seq_.p, arena_off_.p, nullptr, nullptr, idx_->sp.k, sc, nj, ews_, max_qlen,
+                      st_);
+    auto cig = std::make_shared<const std::vector<uint32_t>>(ews_.h_cigar.begin(), ews_.h_cigar.end());
+    Request* last = nullptr;
+    for (uint32_t j = 0; j < nj; j++) {
+        Request* r = owner[j];
+        if (r != last) {
+            r->store.cigars.push_back(cig);
+            r->waves++;
+            last = r;
+        }
+        StoredResult sr;
+        static_cast<ExtResult&>(sr) = ews_.h_results[j];
+        sr.cigar = cig->data() + sr.cigar_offset;
+        r->store.results.push_back(sr);
+        const uint64_t local = jobs[j].read - r->read_base;
+        r->store.per_read[local][jobs[j].tag].result = &r->store.results.back();
+    }
+}
+
+void Session::worker() {
+    std::unique_lock<std::mutex> lk(mu_);
+    for (;;) {
+        cv_work_.wait(lk, [&] { return workers_stop_ || !ready_.empty(); });
+        if (ready_.empty()) return;
+        auto item = ready_.front();
+        ready_.pop_front();
+        Request* r = item.first;
+        if (r->state == 3) continue;
+        ChunkState& cs = r->chunks[item.second];
+        const bool first = !r->seeded[item.second];
+        r->seeded[item.second] = 1;
+        running_++;
+        lk.unlock();
+        std::string err;
+        try {
+            Policy policy(pcfg_, contigs_, r->bv, r->store);
+            if (first) policy.seed_requests(cs);
+            else policy.run_chunk(cs);
+        } catch (const std::exception& e) {
+            err = e.what();
+        }
+        lk.lock();
+        running_--;
+        if (r->state == 3) continue;  // failed meanwhile
+        if (!err.empty()) {
+            fail_all("internal: " + err, SA_ERR_INVALID);
+            cv_engine_.notify_all();
+            continue;
+        }
+        bool finished = false;
+        if (!first && cs.done) {
+            finished = ++r->n_done == r->chunks.size();
+        } else if (cs.pending.empty()) {
+            if (!first) {
+                fail_all("internal: chunk stalled without a pending request", SA_ERR_INVALID);
+                cv_engine_.notify_all();
+                continue;
+            }
+            ready_.push_back(item);
+            cv_work_.notify_one();
+        } else {
+            waiting_.push_back(item);
+            waiting_jobs_ += cs.pending.size();
+        }
+        cv_engine_.notify_one();
+        if (finished) {
+            lk.unlock();
+            complete(*r);
+            lk.lock();
+        }
+    }
+}
+
+void Session::complete(Request& r) {
+    size_t total = 0;
+    for (auto& c : r.chunks) {
+        total += c.out.size();
+        r.mapped += c.mapped;
+    }
+    r.out.reserve(total);
+    for (auto& c : r.chunks) r.out += c.out;
+    if (mp_.mode == SA_MODE_ABUNDANCE) {
+        r.abundance.assign(contigs_.size(), 0.0);
+        for (auto& c : r.chunks)
+            for (auto& a : c.abundance) r.abundance[a.first] += a.second;
+    }
+    // release what the finished request no longer needs
+    r.chunks.clear();
+    r.chunks.shrink_to_fit();
+    r.store = ResultStore();
+    r.nams = std::vector<NamRec>();
+    r.nam_off = std::vector<uint64_t>();
+    r.details = std::vector<NamDetailsRec>();
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        seq_alloc_.release(r.seq_base, std::max<uint64_t>(r.total_bases, 1));
+        off_alloc_.release(r.read_base, r.n_reads + 1);
+        inflight_--;
+        r.state = 2;
+        r.t_done = std::chrono::steady_clock::now();
+    }
+    cv_done_.notify_all();
+    cv_engine_.notify_one();
+}
+
+// called with mu_ held
+void Session::fail_all(const std::string& msg, int32_t code) {
+    broken_ = true;
+    broken_msg_ = msg;
+    for (auto& kv : live_) {
+        Request& r = *kv.second;
+        if (r.state < 2) {
+            r.state = 3;
+            r.error = msg;
+            r.error_code = code;
+        }
+    }
+    for (auto& q : queue_) {
+        q->state = 3;
+        q->error = msg;
+        q->error_code = code;
+        live_[q->id] = std::move(q);
+    }
+    queue_.clear();
+    ready_.clear();
+    waiting_.clear();
+    waiting_jobs_ = 0;
+    inflight_ = 0;
+    cv_done_.notify_all();
+    cv_work_.notify_all();
+}
+
+}  // namespace sa

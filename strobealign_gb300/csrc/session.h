@@ -1,0 +1,149 @@
+// Serving engine behind sa_session: requests (read batches) are admitted into a
+// device read arena as memory frees up, get their NAMs from one pass of the device
+// pipeline, and then share the chunk scheduler and the extension waves with every
+// other request in flight.  Each request is its own chunk stream (chunks cut from
+// the request's records, fresh RNG and insert-size state per chunk,
+// src/main.rs:591-604,873-880), so its output does not depend on what else is in
+// flight.
+#pragma once
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+
+#include "policy.h"
+
+namespace sa {
+
+// First-fit allocator of [0, capacity) ranges with coalescing on free.
+class RangeAllocator {
+  public:
+    explicit RangeAllocator(uint64_t capacity = 0) { reset(capacity); }
+    void reset(uint64_t capacity) {
+        free_.clear();
+        if (capacity) free_[0] = capacity;
+        capacity_ = capacity;
+    }
+    bool alloc(uint64_t n, uint64_t& at);
+    void release(uint64_t at, uint64_t n);
+    uint64_t capacity() const { return capacity_; }
+    uint64_t largest_free() const;
+
+  private:
+    std::map<uint64_t, uint64_t> free_;  // start -> length
+    uint64_t capacity_ = 0;
+};
+
+struct Request {
+    uint64_t id = 0;
+    bool paired = false;
+    // owned copies of the records
+    std::vector<char> seq, qual, names, comments;
+    std::vector<uint64_t> seq_off, name_off, comment_off;  // per device read
+    bool has_qual = false, has_comments = false;
+    BatchView bv;
+    uint64_t nrec = 0, n_reads = 0, total_bases = 0;
+    uint32_t max_qlen = 1;
+    // device placement (arena units: bases, offset slots)
+    uint64_t seq_base = 0, read_base = 0;
+    // NAMs copied back from the device
+    std::vector<NamRec> nams;
+    std::vector<uint64_t> nam_off;
+    std::vector<NamDetailsRec> details;
+    ResultStore store;
+    std::vector<ChunkState> chunks;
+    std::vector<uint8_t> seeded;
+    size_t n_done = 0;
+    // result
+    std::string out;
+    uint64_t mapped = 0;
+    std::vector<double> abundance;
+    uint32_t waves = 0;
+    int state = 0;  // 0 queued, 1 admitted, 2 done, 3 failed
+    std::string error;
+    int32_t error_code = 0;
+    std::chrono::steady_clock::time_point t_submit, t_admit, t_done;
+};
+
+struct SessionConfig {
+    uint64_t max_inflight_bases = 1ull << 30;
+    uint32_t max_inflight_requests = 0;  // 0 = no limit
+    uint32_t policy_threads = 0;         // 0 = all host threads
+};
+
+class Session {
+  public:
+    Session(const sa_index* idx, const sa_refs* refs, const sa_chaining_params& cp, const sa_mapping_params& mp,
+            const SessionConfig& sc);
+    ~Session();
+    uint64_t submit(const sa_read_batch* r1, const sa_read_batch* r2);
+    // 1 done, 0 not yet; throws for an unknown ticket
+    int poll(uint64_t ticket);
+    // Waits up to timeout_ms (< 0: no limit).  Returns false on timeout.  On
+    // success the request is released and its output moved out.
+    bool wait(uint64_t ticket, int64_t timeout_ms, std::unique_ptr<Request>& out);
+    uint64_t in_flight() const;
+    const std::vector<ContigInfo>& contigs() const { return contigs_; }
+
+  private:
+    void engine();
+    void worker();
+    void admit(Request& r);
+    void run_wave(std::vector<std::pair<Request*, size_t>>& batch);
+    void complete(Request& r);
+    void fail_all(const std::string& msg, int32_t code);
+
+    const sa_index* idx_;
+    const sa_refs* refs_;
+    sa_chaining_params cp_;
+    sa_mapping_params mp_;
+    std::string rg_id_;
+    PolicyConfig pcfg_;
+    SessionConfig cfg_;
+    std::vector<ContigInfo> contigs_;
+    uint32_t max_contig_len_ = 0;
+    cudaStream_t st_ = nullptr;
+    DevBuf<uint64_t> d_words_, d_woff_;
+    DevBuf<uint32_t> d_clen_;
+    DevRefs refs_view_{};
+    NamWorkspace nws_;
+    ExtWorkspace ews_;
+    PinnedBuf<uint8_t> h_seq_;
+    PinnedBuf<uint64_t> h_off_;
+    // read arena
+    DevBuf<uint8_t> arena_seq_;
+    DevBuf<uint64_t> arena_off_;
+    RangeAllocator seq_alloc_, off_alloc_;
+    std::vector<uint64_t> h_goff_;
+
+    mutable std::mutex mu_;
+    std::condition_variable cv_engine_, cv_work_, cv_done_;
+    std::deque<std::unique_ptr<Request>> queue_;                    // submitted, not admitted
+    std::unordered_map<uint64_t, std::unique_ptr<Request>> live_;  // admitted or done
+    std::deque<std::pair<Request*, size_t>> ready_;
+    std::vector<std::pair<Request*, size_t>> waiting_;
+    uint64_t waiting_jobs_ = 0;
+    unsigned running_ = 0;
+    uint64_t next_id_ = 1;
+    uint32_t inflight_ = 0;
+    bool stop_ = false;
+    bool workers_stop_ = false;
+    bool broken_ = false;  // a device or internal error failed every request
+    std::string broken_msg_;
+    // failed requests stay allocated until the session is destroyed: queued work
+    // items may still point at them
+    std::vector<std::unique_ptr<Request>> graveyard_;
+    uint64_t wave_min_jobs_ = 32768;
+    std::thread engine_;
+    std::vector<std::thread> workers_;
+};
+
+}  // namespace sa
+
+struct sa_session {
+    sa::Session* s;
+};
