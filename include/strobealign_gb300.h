@@ -303,6 +303,7 @@ typedef struct {
     double seconds_total;   /* submit -> done */
     uint64_t n_reads;
     uint32_t n_waves; /* extension waves the request took part in */
+    uint64_t h2d_bytes, d2h_bytes; /* host<->device bytes moved for this request */
 } sa_request_stats;
 void sa_session_params_default(sa_session_params* p);
 int32_t sa_session_create(const sa_index* idx, const sa_refs* refs, const sa_chaining_params* cp,

@@ -78,7 +78,7 @@ class SessionParams(C.Structure):
 
 class RequestStats(C.Structure):
     _fields_ = [("seconds_queued", f64), ("seconds_service", f64), ("seconds_total", f64), ("n_reads", u64),
-                ("n_waves", u32)]
+                ("n_waves", u32), ("h2d_bytes", u64), ("d2h_bytes", u64)]
 
 
 class MapperStats(C.Structure):

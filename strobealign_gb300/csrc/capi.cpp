@@ -696,6 +696,8 @@ int32_t sa_session_wait(sa_session* s, uint64_t ticket, int64_t timeout_ms, sa_o
         stats->seconds_total = sec(r->t_submit, r->t_done);
         stats->n_reads = r->n_reads;
         stats->n_waves = r->waves;
+        stats->h2d_bytes = r->h2d_bytes;
+        stats->d2h_bytes = r->d2h_bytes;
     }
     if (abundances) {
         const auto& cs = s->s->contigs();

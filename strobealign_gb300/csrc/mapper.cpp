@@ -53,6 +53,7 @@ Mapper::Mapper(const sa_index* idx, const sa_refs* refs, const sa_chaining_param
     pcfg_.rg_id = rg_id_;
     pcfg_.has_rg = mp.rg_id != nullptr;
     pcfg_.k = idx->sp.k;
+    pcfg_.timing = trace_;
     if (!mp_.use_ssw && mp_.mode == SA_MODE_SAM) {
         // single-end piecewise extension (block-aligner) has no device implementation; paired-end
         // extension always uses SSW in the reference (src/mapper.rs:860-870)
@@ -110,28 +111,21 @@ void Mapper::nams_for_reads(uint32_t& launches) {
     d2h_bytes_ += ((size_t)n_reads_ + 1) * 8 + tn * sizeof(NamRec) + (size_t)n_reads_ * sizeof(NamDetailsRec);
 }
 
-uint32_t Mapper::run_wave(ResultStore& store, const std::vector<ExtJob>& jobs, uint32_t max_qlen) {
-    const uint32_t nj = (uint32_t)jobs.size();
-    if (!nj) return 0;
+std::shared_ptr<const WaveResults> Mapper::run_wave(const ExtJob* jobs, uint32_t nj, uint32_t max_qlen,
+                                                    uint32_t& launches) {
+    auto w = std::make_shared<WaveResults>();
+    if (!nj) return w;
     ews_.jobs.reserve(nj);
-    SA_CUDA(cudaMemcpyAsync(ews_.jobs.p, jobs.data(), (size_t)nj * sizeof(ExtJob), cudaMemcpyHostToDevice, st_));
+    SA_CUDA(cudaMemcpyAsync(ews_.jobs.p, jobs, (size_t)nj * sizeof(ExtJob), cudaMemcpyHostToDevice, st_));
     h2d_bytes_ += (size_t)nj * sizeof(ExtJob);
     AlignScores sc{mp_.match, mp_.mismatch, mp_.gap_open, mp_.gap_extend, mp_.end_bonus};
-    uint32_t launches = run_extension(refs_view_, nws_, idx_->sp.k, sc, nj, ews_, max_qlen, st_, &kt_);
+    launches += run_extension(refs_view_, nws_, idx_->sp.k, sc, nj, ews_, max_qlen, st_, &kt_);
     d2h_bytes_ += (size_t)nj * sizeof(ExtResult) + ews_.total_cigar * 4;
     for (int c = 0; c < 5; c++) sw_cells_[c] += ews_.cells[c];
-    store.cigars.push_back(std::make_shared<const std::vector<uint32_t>>(ews_.h_cigar.begin(), ews_.h_cigar.end()));
-    const uint32_t* cig = store.cigars.back()->data();
-    for (uint32_t j = 0; j < nj; j++) {
-        StoredResult r;
-        static_cast<ExtResult&>(r) = ews_.h_results[j];
-        r.cigar = cig + r.cigar_offset;
-        store.results.push_back(r);
-        const ExtJob& jb = jobs[j];
-        store.per_read[jb.read][jb.tag].result = &store.results.back();
-    }
+    w->results.swap(ews_.h_results);
+    w->cigar.swap(ews_.h_cigar);
     jobs_run_ += nj;
-    return launches;
+    return w;
 }
 
 void Mapper::upload(const sa_read_batch* r1, const sa_read_batch* r2) {
@@ -264,7 +258,6 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, ResultStore& store, u
     for (unsigned t = 0; t < nthreads; t++) th.emplace_back(worker);
 
     uint32_t waves = 0;
-    std::vector<ExtJob> jobs;
     std::vector<size_t> batch;
     const auto t_sched0 = std::chrono::steady_clock::now();
     try {
@@ -284,23 +277,28 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, ResultStore& store, u
             lk.unlock();
             // chunk order inside a wave keeps waves reproducible for a given grouping
             std::sort(batch.begin(), batch.end());
-            jobs.clear();
+            size_t nj = 0;
+            for (size_t c : batch) nj += chunks[c].pending.size();
+            h_jobs_.reserve(std::max<size_t>(nj, 1));
+            nj = 0;
             for (size_t c : batch) {
-                jobs.insert(jobs.end(), chunks[c].pending.begin(), chunks[c].pending.end());
-                chunks[c].pending.clear();
+                chunks[c].wave_first = nj;
+                std::memcpy(h_jobs_.p + nj, chunks[c].pending.data(), chunks[c].pending.size() * sizeof(ExtJob));
+                nj += chunks[c].pending.size();
             }
             if (waves > 1000000) throw Error(SA_ERR_INVALID, "internal: extension waves do not converge");
             auto tw = std::chrono::steady_clock::now();
-            launches += run_wave(store, jobs, max_qlen_);
+            auto wres = run_wave(h_jobs_.p, (uint32_t)nj, max_qlen_, launches);
+            for (size_t c : batch) chunks[c].wave = wres;
             const auto tw2 = std::chrono::steady_clock::now();
             t_ext_ += std::chrono::duration<double>(tw2 - tw).count();
             if (trace_) {
                 uint64_t kinds[4] = {0, 0, 0, 0};
-                for (auto& j : jobs) kinds[j.kind & 3]++;
+                for (size_t j = 0; j < nj; j++) kinds[h_jobs_.p[j].kind & 3]++;
                 std::fprintf(stderr,
                              "sa_wave %u t=%.4f dur=%.4f chunks=%zu jobs=%zu fast=%llu full=%llu rescue=%llu align=%llu\n",
                              waves, std::chrono::duration<double>(tw - t_sched0).count(),
-                             std::chrono::duration<double>(tw2 - tw).count(), batch.size(), jobs.size(),
+                             std::chrono::duration<double>(tw2 - tw).count(), batch.size(), nj,
                              (unsigned long long)kinds[0], (unsigned long long)kinds[1],
                              (unsigned long long)kinds[2], (unsigned long long)kinds[3]);
             }
@@ -357,6 +355,22 @@ void Mapper::map_uploaded(sa_output* out) {
     ResultStore store;
     store.per_read.resize(bv.reads.size());
     const uint32_t waves = schedule(chunks, store, launches);
+    if (trace_) {
+        double sr = 0, ss = 0, sd = 0;
+        uint64_t er = 0, es = 0, runs = 0;
+        for (auto& c : chunks) {
+            sr += c.seconds_real;
+            ss += c.seconds_spec;
+            sd += c.seconds_seed;
+            er += c.evals_real;
+            es += c.evals_spec;
+            runs += c.runs;
+        }
+        std::fprintf(stderr, "sa_policy chunks=%zu runs=%llu cpu_real=%.3f cpu_spec=%.3f cpu_seed=%.3f evals_real=%llu "
+                             "evals_spec=%llu\n",
+                     chunks.size(), (unsigned long long)runs, sr, ss, sd, (unsigned long long)er,
+                     (unsigned long long)es);
+    }
     for (auto& c : chunks)
         for (auto& a : c.abundance) abundances_[a.first] += a.second;
     size_t total_len = 0;

@@ -41,7 +41,8 @@ class Mapper {
     void set_wave_min_jobs(uint64_t n) { wave_min_jobs_ = n; }
 
   private:
-    uint32_t run_wave(ResultStore& store, const std::vector<ExtJob>& jobs, uint32_t max_qlen);
+    std::shared_ptr<const WaveResults> run_wave(const ExtJob* jobs, uint32_t nj, uint32_t max_qlen,
+                                                uint32_t& launches);
     uint32_t schedule(std::vector<ChunkState>& chunks, ResultStore& store, uint32_t& launches);
     BatchView bv_;
     bool have_batch_ = false;
@@ -72,6 +73,7 @@ class Mapper {
     ExtWorkspace ews_;
     PinnedBuf<uint8_t> h_seq_;
     PinnedBuf<uint64_t> h_off_;
+    PinnedBuf<ExtJob> h_jobs_;
     std::vector<uint64_t> h_nam_off_;
     std::vector<NamRec> h_nams_;
     std::vector<NamDetailsRec> h_details_;

@@ -1,6 +1,8 @@
 // Host-side mapping policy (see policy.h).  Follows src/mapper.rs and
 // src/maponly.rs decision by decision; every base-level alignment comes from the
 // GPU extension jobs.
+#include <chrono>
+
 #include "policy.h"
 
 #include <algorithm>
@@ -51,6 +53,7 @@ uint64_t Rng::gen_mod_u64(uint64_t n) {
 
 void InsertSize::update(uint64_t insert_size) {
     if (insert_size >= 2000) return;
+    last = insert_size;
     if (sample_size > 0) {
         float x = (float)insert_size;
         float e = x - mu;
@@ -433,22 +436,22 @@ void add_details(Details& a, const Details& b) {
 }  // namespace
 
 // ------------------------------------------------------------------ result access
-const StoredResult* Policy::lookup(uint32_t read, const JobKey& key) const {
+const ResultStore::Entry* Policy::lookup(uint32_t read, const JobKey& key) const {
     const auto& v = store_.per_read[read];
-    auto find = [&](const JobKey& k) -> const StoredResult* {
+    auto find = [&](const JobKey& k) -> const ResultStore::Entry* {
         for (auto& e : v)
-            if (e.key == k && e.result) return e.result;
+            if (e.key == k && e.result) return &e;
         return nullptr;
     };
-    if (const StoredResult* r = find(key)) return r;
+    if (const ResultStore::Entry* r = find(key)) return r;
     // extend_seed after is_consistent and after reverse_nam_if_needed coincide whenever
     // the latter does not flip the NAM
     if (key.kind == JOB_EXTEND_FULL) {
-        const StoredResult* f = find(JobKey{JOB_EXTEND_FAST, key.a, 0, 0, 0});
-        if (f && f->consistent) return f;
+        const ResultStore::Entry* f = find(JobKey{JOB_EXTEND_FAST, key.a, 0, 0, 0});
+        if (f && f->result->consistent) return f;
     } else if (key.kind == JOB_EXTEND_FAST) {
-        const StoredResult* f = find(JobKey{JOB_EXTEND_FULL, key.a, 0, 0, 0});
-        if (f && !f->flipped) return f;
+        const ResultStore::Entry* f = find(JobKey{JOB_EXTEND_FULL, key.a, 0, 0, 0});
+        if (f && !f->result->flipped) return f;
     }
     return nullptr;
 }
@@ -458,16 +461,36 @@ void Policy::want(uint32_t read, const ExtJob& job, const JobKey& key) {
     auto& v = store_.per_read[read];
     for (auto& e : v)
         if (e.key == key) return;  // pending
-    v.push_back(ResultStore::Entry{key, nullptr});
+    v.push_back(ResultStore::Entry{key, nullptr, nullptr});
     ExtJob j = job;
     j.tag = (uint32_t)(v.size() - 1);
     cur_->pending.push_back(j);
 }
 
-const StoredResult& Policy::get(uint32_t read, const ExtJob& job, const JobKey& key) {
-    if (const StoredResult* r = lookup(read, key)) return *r;
+StoredResult Policy::get(uint32_t read, const ExtJob& job, const JobKey& key) {
+    if (const ResultStore::Entry* e = lookup(read, key)) {
+        StoredResult r;
+        static_cast<ExtResult&>(r) = *e->result;
+        r.cigar = e->cigar + e->result->cigar_offset;
+        return r;
+    }
     want(read, job, key);
     throw Miss{};
+}
+
+void Policy::resolve(ChunkState& cs) {
+    if (!cs.wave) return;
+    const WaveResults& w = *cs.wave;
+    for (size_t j = 0; j < cs.pending.size(); j++) {
+        const ExtJob& jb = cs.pending[j];
+        auto& e = store_.per_read[jb.read][jb.tag];
+        e.result = &w.results[cs.wave_first + j];
+        e.cigar = w.cigar.data();
+        cs.result_bytes += sizeof(ExtResult) + (e.result->valid ? 4ull * e.result->cigar_len : 0);
+    }
+    cs.pending.clear();
+    cs.waves.push_back(std::move(cs.wave));
+    cs.wave.reset();
 }
 
 ExtJob Policy::nam_job(uint32_t read, const NamRec& cur, uint32_t kind) const {
@@ -1173,6 +1196,15 @@ void Policy::aemb_pe(uint64_t rec, Rng& rng, InsertSize& isd) {
 void Policy::seed_requests(ChunkState& cs) {
     if (cfg_.mp.mode != SA_MODE_SAM) return;
     cur_ = &cs;
+    const auto t0 = cfg_.timing ? std::chrono::steady_clock::now() : std::chrono::steady_clock::time_point();
+    struct Acc {
+        const PolicyConfig& c;
+        ChunkState& cs;
+        std::chrono::steady_clock::time_point t0;
+        ~Acc() {
+            if (c.timing) cs.seconds_seed += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        }
+    } acc{cfg_, cs, t0};
     const bool paired = bv_.paired;
     for (uint64_t rec = cs.first; rec < cs.end; rec++) {
         for (int m = 0; m < (paired ? 2 : 1); m++) {
@@ -1192,6 +1224,14 @@ void Policy::seed_requests(ChunkState& cs) {
 
 void Policy::run_chunk(ChunkState& cs) {
     cur_ = &cs;
+    resolve(cs);
+    const bool timing = cfg_.timing;
+    auto now = [] { return std::chrono::steady_clock::now(); };
+    auto since = [&](std::chrono::steady_clock::time_point t) {
+        return std::chrono::duration<double>(now() - t).count();
+    };
+    const auto t_run = timing ? now() : std::chrono::steady_clock::time_point();
+    cs.runs++;
     auto one = [&](uint64_t rec, Rng& rng, InsertSize& isd, std::string& out, uint64_t& mapped) {
         switch (cfg_.mp.mode) {
             case SA_MODE_SAM:
@@ -1218,32 +1258,60 @@ void Policy::run_chunk(ChunkState& cs) {
         } catch (const Miss&) {
             cs.out.resize(out_len);
             cs.abundance.resize(ab_len);
-            // look ahead: later reads of the chunk with the best-known state; after the
-            // first lookahead only the reads that missed in the previous one are revisited
+            // look ahead: later reads of the chunk with the best-known state, so that
+            // their requests join the next wave; after the first lookahead only the
+            // reads that missed are evaluated again, the others' effect on the state
+            // is replayed
             speculative_ = true;
-            Rng srng = cs.rng;
-            InsertSize sisd = cs.isd;
+            // the state as the real run will have it once the missing results are in:
+            // the draws made before the miss, no insert-size update (only the fast
+            // path updates it, and that path does not miss)
+            Rng srng = rng;
+            InsertSize sisd = isd;
             std::string scratch;
             std::vector<uint64_t> todo;
+            if (cs.effects.empty()) cs.effects.resize(cs.end - cs.first);
             auto visit = [&](uint64_t rec) {
+                cs.evals_spec++;
                 Rng r2 = srng;
                 InsertSize i2 = sisd;
                 uint64_t m2 = 0;
+                auto& ef = cs.effects[rec - cs.first];
                 try {
                     one(rec, r2, i2, scratch, m2);
-                    srng = r2;
-                    sisd = i2;
+                    ef.known = true;
+                    ef.rng_delta = r2.state - srng.state;
+                    ef.isd_update = i2.sample_size != sisd.sample_size;
+                    ef.isd_value = i2.last;
                 } catch (const Miss&) {
+                    // keep the draws made before the miss; see above for the estimate
+                    ef.known = false;
                     todo.push_back(rec);
                 }
+                srng = r2;
+                sisd = i2;
             };
+            const auto t_spec = timing ? now() : std::chrono::steady_clock::time_point();
+            if (timing) cs.seconds_real += std::chrono::duration<double>(t_spec - t_run).count();
             if (!cs.lookahead_started) {
                 for (uint64_t rec = cs.next + 1; rec < cs.end; rec++) visit(rec);
                 cs.lookahead_started = true;
             } else {
-                for (uint64_t rec : cs.lookahead_todo)
-                    if (rec > cs.next) visit(rec);
+                // evaluate the reads that missed last time; replay what the others did
+                size_t ti = 0;
+                const auto& old = cs.lookahead_todo;
+                for (uint64_t rec = cs.next + 1; rec < cs.end; rec++) {
+                    while (ti < old.size() && old[ti] < rec) ti++;
+                    const auto& ef = cs.effects[rec - cs.first];
+                    if ((ti < old.size() && old[ti] == rec) || !ef.known) {
+                        visit(rec);
+                    } else {
+                        srng.state += ef.rng_delta;
+                        if (ef.isd_update) sisd.update(ef.isd_value);
+                    }
+                }
             }
+            if (timing) cs.seconds_spec += since(t_spec);
             cs.lookahead_todo.swap(todo);
             speculative_ = false;
             return;
@@ -1252,7 +1320,9 @@ void Policy::run_chunk(ChunkState& cs) {
         cs.isd = isd;
         cs.mapped += mapped;
         cs.next++;
+        cs.evals_real++;
     }
+    if (timing) cs.seconds_real += since(t_run);
     cs.done = true;
 }
 

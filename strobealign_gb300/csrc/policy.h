@@ -27,6 +27,7 @@ struct Rng {
 struct InsertSize {
     uint64_t sample_size = 0;
     float mu = 300.0f, sigma = 100.0f, variance = 10000.0f, sse = 10000.0f;
+    uint64_t last = 0;  // value of the last accepted update (replayed by the lookahead)
     void update(uint64_t insert_size);
 };
 
@@ -53,25 +54,29 @@ struct JobKey {
 
 struct Miss {};
 
-// One extension result as the host keeps it: the device record plus the address
-// of its CIGAR in the wave's host copy.
+// Results of one extension wave copied back from the device: one ExtResult per
+// job, and the CIGAR ops they point into (ExtResult::cigar_offset).
+struct WaveResults {
+    std::vector<ExtResult> results;
+    std::vector<uint32_t> cigar;
+};
+
+// One extension result as the policy reads it: the device record plus the address
+// of its CIGAR.
 struct StoredResult : ExtResult {
     const uint32_t* cigar = nullptr;
 };
 
-// Extension results of one batch, accumulated over waves.  Storage is stable:
-// waves append (deque elements never move), so policy threads keep reading the
-// results they hold while the extension thread appends the next wave.  An entry of
-// per_read[r] is written only by the thread that runs the chunk owning read r, or
-// by the extension thread while that chunk waits for the wave.
+// Requests and results of one batch, per device read.  An entry is written only by
+// the thread that runs the chunk owning the read (chunks run on one thread at a
+// time), so no locking is needed.
 struct ResultStore {
     struct Entry {
         JobKey key;
-        const StoredResult* result;  // nullptr while pending
+        const ExtResult* result;  // nullptr while pending
+        const uint32_t* cigar;    // CIGAR base of the wave that produced the result
     };
     std::vector<std::vector<Entry>> per_read;
-    std::deque<StoredResult> results;
-    std::vector<std::shared_ptr<const std::vector<uint32_t>>> cigars;  // the waves' CIGAR copies referenced here
 };
 
 struct ReadView {
@@ -89,6 +94,7 @@ struct PolicyConfig {
     std::string rg_id;
     bool has_rg = false;
     uint32_t k = 0;
+    bool timing = false;  // accumulate ChunkState::seconds_* (diagnostics)
 };
 
 struct ContigInfo {
@@ -113,9 +119,26 @@ struct ChunkState {
     uint64_t mapped = 0;
     bool done = false;
     std::vector<ExtJob> pending;                          // requests raised by this chunk
+    // the wave that ran `pending`: its results start at wave_first, in pending's
+    // order; the thread that resumes the chunk points the entries at them
+    std::shared_ptr<const WaveResults> wave;
+    uint64_t wave_first = 0;
+    std::vector<std::shared_ptr<const WaveResults>> waves;  // keeps the results the entries use
+    uint64_t result_bytes = 0;  // device->host bytes of this chunk's results and CIGARs
     std::vector<std::pair<uint32_t, double>> abundance;   // (contig, weight) in read order
     bool lookahead_started = false;
     std::vector<uint64_t> lookahead_todo;                 // reads that missed in the last lookahead
+    // what each record did to the RNG and the insert-size estimate when the last
+    // lookahead evaluated it; later lookaheads replay it instead of evaluating again
+    struct Effect {
+        uint64_t rng_delta = 0;
+        uint64_t isd_value = 0;
+        bool known = false, isd_update = false;
+    };
+    std::vector<Effect> effects;
+    // host time by phase when PolicyConfig::timing is set
+    double seconds_real = 0, seconds_spec = 0, seconds_seed = 0;
+    uint64_t evals_real = 0, evals_spec = 0, runs = 0;
 };
 
 class Policy {
@@ -141,8 +164,9 @@ class Policy {
     }
 
     void want(uint32_t read, const ExtJob& job, const JobKey& key);
-    const StoredResult* lookup(uint32_t read, const JobKey& key) const;
-    const StoredResult& get(uint32_t read, const ExtJob& job, const JobKey& key);
+    const ResultStore::Entry* lookup(uint32_t read, const JobKey& key) const;
+    StoredResult get(uint32_t read, const ExtJob& job, const JobKey& key);
+    void resolve(ChunkState& cs);
 
     void se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mapped);
     void pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out, uint64_t& mapped);

@@ -7,6 +7,8 @@
 // once enough jobs wait or when the policy threads have nothing left to run; a
 // request is admitted when its reads fit in the arena.
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "session.h"
@@ -56,8 +58,13 @@ Session::Session(const sa_index* idx, const sa_refs* refs, const sa_chaining_par
     : idx_(idx), refs_(refs), cp_(cp), mp_(mp), cfg_(sc) {
     if (mp.rg_id) rg_id_ = mp.rg_id;
     mp_.rg_id = nullptr;
+    // SA_TRACE_WAVES=1: admissions and extension waves on stderr
+    const char* tr = std::getenv("SA_TRACE_WAVES");
+    trace_ = tr && *tr && *tr != '0';
+    t0_ = std::chrono::steady_clock::now();
     SA_CUDA(cudaSetDevice(idx->device));
     SA_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    SA_CUDA(cudaStreamCreateWithFlags(&sta_, cudaStreamNonBlocking));
     const auto& cs = refs->contigs;
     const uint32_t nc = (uint32_t)cs.size();
     std::vector<uint64_t> woff(nc);
@@ -93,6 +100,7 @@ Session::Session(const sa_index* idx, const sa_refs* refs, const sa_chaining_par
     off_alloc_.reset(slots);
     unsigned nt = cfg_.policy_threads ? cfg_.policy_threads : std::max(1u, std::thread::hardware_concurrency());
     engine_ = std::thread([this] { engine(); });
+    admitter_ = std::thread([this] { admitter(); });
     for (unsigned t = 0; t < nt; t++) workers_.emplace_back([this] { worker(); });
 }
 
@@ -108,7 +116,9 @@ Session::~Session() {
         queue_.clear();
     }
     cv_engine_.notify_all();
+    cv_admit_.notify_all();
     cv_done_.notify_all();
+    if (admitter_.joinable()) admitter_.join();
     if (engine_.joinable()) engine_.join();
     {
         std::lock_guard<std::mutex> g(mu_);
@@ -117,6 +127,7 @@ Session::~Session() {
     cv_work_.notify_all();
     for (auto& t : workers_) t.join();
     if (st_) cudaStreamDestroy(st_);
+    if (sta_) cudaStreamDestroy(sta_);
 }
 
 uint64_t Session::submit(const sa_read_batch* r1, const sa_read_batch* r2) {
@@ -179,13 +190,13 @@ uint64_t Session::submit(const sa_read_batch* r1, const sa_read_batch* r2) {
     uint64_t id;
     {
         std::lock_guard<std::mutex> g(mu_);
-        if (stop_) throw Error(SA_ERR_CANCELLED, "session is shutting down");
         if (broken_) throw Error(SA_ERR_CUDA, "session failed: " + broken_msg_);
+        if (stop_) throw Error(SA_ERR_CANCELLED, "session is shutting down");
         id = next_id_++;
         r->id = id;
         queue_.push_back(std::move(r));
     }
-    cv_engine_.notify_one();
+    cv_admit_.notify_one();
     return id;
 }
 
@@ -233,8 +244,43 @@ uint64_t Session::in_flight() const {
     return inflight_ + queue_.size();
 }
 
+// Extension waves, on the session's main stream.
 void Session::engine() {
     std::vector<std::pair<Request*, size_t>> batch;
+    std::unique_lock<std::mutex> lk(mu_);
+    for (;;) {
+        auto idle = [&]() { return running_ == 0 && ready_.empty(); };
+        auto wave_ok = [&]() { return !waiting_.empty() && (waiting_jobs_ >= wave_min_jobs_ || idle()); };
+        cv_engine_.wait(lk, [&] { return broken_ || (stop_ && inflight_ == 0 && !admitting_) || wave_ok(); });
+        if (broken_ || (stop_ && inflight_ == 0 && !admitting_)) break;
+        batch.swap(waiting_);
+        waiting_.clear();
+        waiting_jobs_ = 0;
+        lk.unlock();
+        try {
+            const auto tw = std::chrono::steady_clock::now();
+            run_wave(batch);
+            if (trace_) {
+                std::fprintf(stderr, "sa_swave t=%.4f dur=%.4f chunks=%zu\n",
+                             std::chrono::duration<double>(tw - t0_).count(),
+                             std::chrono::duration<double>(std::chrono::steady_clock::now() - tw).count(),
+                             batch.size());
+            }
+        } catch (const std::exception& e) {
+            lk.lock();
+            fail_all(e.what(), dynamic_cast<const Error*>(&e) ? static_cast<const Error&>(e).code : SA_ERR_CUDA);
+            return;
+        }
+        lk.lock();
+        for (auto& b : batch) ready_.push_back(b);
+        batch.clear();
+        cv_work_.notify_all();
+    }
+}
+
+// Admission: reads into the arena and the NAM pipeline, on a second stream so that
+// it overlaps the waves of the requests already in flight.
+void Session::admitter() {
     std::unique_lock<std::mutex> lk(mu_);
     for (;;) {
         auto can_admit = [&]() {
@@ -244,48 +290,35 @@ void Session::engine() {
             return seq_alloc_.largest_free() >= std::max<uint64_t>(q.total_bases, 1) &&
                    off_alloc_.largest_free() >= q.n_reads + 1;
         };
-        auto idle = [&]() { return running_ == 0 && ready_.empty(); };
-        auto wave_ok = [&]() { return !waiting_.empty() && (waiting_jobs_ >= wave_min_jobs_ || idle()); };
-        cv_engine_.wait(lk, [&] { return (stop_ && inflight_ == 0) || wave_ok() || can_admit(); });
-        if (stop_ && inflight_ == 0) break;
-        const bool big = !waiting_.empty() && waiting_jobs_ >= wave_min_jobs_;
-        if (wave_ok() && (big || !can_admit())) {
-            batch.swap(waiting_);
-            waiting_.clear();
-            waiting_jobs_ = 0;
-            lk.unlock();
-            try {
-                run_wave(batch);
-            } catch (const std::exception& e) {
-                lk.lock();
-                fail_all(e.what(), dynamic_cast<const Error*>(&e) ? static_cast<const Error&>(e).code : SA_ERR_CUDA);
-                return;
-            }
-            lk.lock();
-            for (auto& b : batch) ready_.push_back(b);
-            batch.clear();
-            cv_work_.notify_all();
-            continue;
-        }
-        // admission
+        cv_admit_.wait(lk, [&] { return broken_ || stop_ || can_admit(); });
+        if (broken_ || stop_) break;
         std::unique_ptr<Request> rq = std::move(queue_.front());
         queue_.pop_front();
         Request* r = rq.get();
         seq_alloc_.alloc(std::max<uint64_t>(r->total_bases, 1), r->seq_base);
         off_alloc_.alloc(r->n_reads + 1, r->read_base);
         inflight_++;
+        admitting_ = true;
         r->state = 1;
         r->t_admit = std::chrono::steady_clock::now();
         live_[r->id] = std::move(rq);
         lk.unlock();
         try {
+            const auto ta = std::chrono::steady_clock::now();
             admit(*r);
+            if (trace_)
+                std::fprintf(stderr, "sa_admit t=%.4f dur=%.4f id=%llu reads=%llu chunks=%zu\n",
+                             std::chrono::duration<double>(ta - t0_).count(),
+                             std::chrono::duration<double>(std::chrono::steady_clock::now() - ta).count(),
+                             (unsigned long long)r->id, (unsigned long long)r->n_reads, r->chunks.size());
         } catch (const std::exception& e) {
             lk.lock();
+            admitting_ = false;
             fail_all(e.what(), dynamic_cast<const Error*>(&e) ? static_cast<const Error&>(e).code : SA_ERR_CUDA);
             return;
         }
         lk.lock();
+        admitting_ = false;
         if (r->chunks.empty()) {
             lk.unlock();
             complete(*r);
@@ -294,7 +327,9 @@ void Session::engine() {
         }
         for (size_t c = 0; c < r->chunks.size(); c++) ready_.emplace_back(r, c);
         cv_work_.notify_all();
+        cv_engine_.notify_one();
     }
+    cv_engine_.notify_all();
 }
 
 void Session::admit(Request& r) {
@@ -307,29 +342,31 @@ void Session::admit(Request& r) {
     std::memcpy(h_off_.p, r.seq_off.data(), ((size_t)n + 1) * 8);
     nws_.seq.reserve(r.total_bases + 16);
     nws_.off.reserve((size_t)n + 1);
-    SA_CUDA(cudaMemcpyAsync(nws_.seq.p, h_seq_.p, r.total_bases, cudaMemcpyHostToDevice, st_));
-    SA_CUDA(cudaMemcpyAsync(nws_.off.p, h_off_.p, ((size_t)n + 1) * 8, cudaMemcpyHostToDevice, st_));
-    SA_CUDA(cudaMemcpyAsync(arena_seq_.p + r.seq_base, nws_.seq.p, r.total_bases, cudaMemcpyDeviceToDevice, st_));
+    SA_CUDA(cudaMemcpyAsync(nws_.seq.p, h_seq_.p, r.total_bases, cudaMemcpyHostToDevice, sta_));
+    SA_CUDA(cudaMemcpyAsync(nws_.off.p, h_off_.p, ((size_t)n + 1) * 8, cudaMemcpyHostToDevice, sta_));
+    SA_CUDA(cudaMemcpyAsync(arena_seq_.p + r.seq_base, nws_.seq.p, r.total_bases, cudaMemcpyDeviceToDevice, sta_));
     h_goff_.resize((size_t)n + 1);
     for (uint32_t i = 0; i <= n; i++) h_goff_[i] = r.seq_base + r.seq_off[i];
     SA_CUDA(cudaMemcpyAsync(arena_off_.p + r.read_base, h_goff_.data(), ((size_t)n + 1) * 8,
-                            cudaMemcpyHostToDevice, st_));
+                            cudaMemcpyHostToDevice, sta_));
     NamConfig cfg;
     cfg.cp = ChainParams{cp_.max_lookback, cp_.diag_diff_penalty, cp_.gap_length_penalty, cp_.valid_score_threshold,
                          cp_.max_ref_gap, cp_.matches_weight, cp_.max_diagonal_ratio};
     cfg.mcs = mp_.mcs_strategy;
     cfg.rescue_distance = mp_.rescue_distance;
     run_nam_pipeline(idx_->view(), refs_view_, cfg, n, r.total_bases, max_contig_len_,
-                     (uint32_t)refs_->contigs.size(), nws_, st_);
+                     (uint32_t)refs_->contigs.size(), nws_, sta_);
     const uint64_t tn = nws_.last_total_nams;
     r.nam_off.resize((size_t)n + 1);
     r.nams.resize(tn);
     r.details.resize(n);
-    SA_CUDA(cudaMemcpyAsync(r.nam_off.data(), nws_.nam_off.p, ((size_t)n + 1) * 8, cudaMemcpyDeviceToHost, st_));
-    if (tn) SA_CUDA(cudaMemcpyAsync(r.nams.data(), nws_.nams.p, tn * sizeof(NamRec), cudaMemcpyDeviceToHost, st_));
+    SA_CUDA(cudaMemcpyAsync(r.nam_off.data(), nws_.nam_off.p, ((size_t)n + 1) * 8, cudaMemcpyDeviceToHost, sta_));
+    if (tn) SA_CUDA(cudaMemcpyAsync(r.nams.data(), nws_.nams.p, tn * sizeof(NamRec), cudaMemcpyDeviceToHost, sta_));
     SA_CUDA(cudaMemcpyAsync(r.details.data(), nws_.details.p, (size_t)n * sizeof(NamDetailsRec),
-                            cudaMemcpyDeviceToHost, st_));
-    SA_CUDA(cudaStreamSynchronize(st_));
+                            cudaMemcpyDeviceToHost, sta_));
+    SA_CUDA(cudaStreamSynchronize(sta_));
+    r.h2d_bytes += r.total_bases + 2 * ((uint64_t)n + 1) * 8;
+    r.d2h_bytes += ((uint64_t)n + 1) * 8 + tn * sizeof(NamRec) + (uint64_t)n * sizeof(NamDetailsRec);
     r.bv.nams = r.nams.data();
     r.bv.nam_off = r.nam_off.data();
     r.bv.details = r.details.data();
@@ -356,43 +393,42 @@ void Session::run_wave(std::vector<std::pair<Request*, size_t>>& batch) {
     std::sort(batch.begin(), batch.end(), [](const std::pair<Request*, size_t>& a, const std::pair<Request*, size_t>& b) {
         return a.first->id != b.first->id ? a.first->id < b.first->id : a.second < b.second;
     });
-    std::vector<ExtJob> jobs;
-    std::vector<Request*> owner;
+    size_t nj = 0;
     uint32_t max_qlen = 1;
     for (auto& b : batch) {
-        Request* r = b.first;
-        auto& pend = r->chunks[b.second].pending;
-        for (ExtJob j : pend) {
-            j.read += (uint32_t)r->read_base;
-            jobs.push_back(j);
-            owner.push_back(r);
-        }
-        pend.clear();
-        max_qlen = std::max(max_qlen, r->max_qlen);
+        nj += b.first->chunks[b.second].pending.size();
+        max_qlen = std::max(max_qlen, b.first->max_qlen);
     }
-    const uint32_t nj = (uint32_t)jobs.size();
     if (!nj) return;
-    ews_.jobs.reserve(nj);
-    SA_CUDA(cudaMemcpyAsync(ews_.jobs.p, jobs.data(), (size_t)nj * sizeof(ExtJob), cudaMemcpyHostToDevice, st_));
-    AlignScores sc{mp_.match, mp_.mismatch, mp_.gap_open, mp_.gap_extend, mp_.end_bonus};
-    run_extension_raw(refs_view_, arena_seq_.p, arena_off_.p, nullptr, nullptr, idx_->sp.k, sc, nj, ews_, max_qlen,
-                      st_);
-    auto cig = std::make_shared<const std::vector<uint32_t>>(ews_.h_cigar.begin(), ews_.h_cigar.end());
+    // jobs in pinned staging with batch-global read indices; chunks keep theirs local
+    h_jobs_.reserve(nj);
+    size_t o = 0;
     Request* last = nullptr;
-    for (uint32_t j = 0; j < nj; j++) {
-        Request* r = owner[j];
+    for (auto& b : batch) {
+        Request* r = b.first;
+        ChunkState& cs = r->chunks[b.second];
+        cs.wave_first = o;
+        const uint32_t base = (uint32_t)r->read_base;
+        for (const ExtJob& j : cs.pending) {
+            ExtJob g = j;
+            g.read += base;
+            h_jobs_.p[o++] = g;
+        }
+        r->h2d_bytes += cs.pending.size() * sizeof(ExtJob);
         if (r != last) {
-            r->store.cigars.push_back(cig);
             r->waves++;
             last = r;
         }
-        StoredResult sr;
-        static_cast<ExtResult&>(sr) = ews_.h_results[j];
-        sr.cigar = cig->data() + sr.cigar_offset;
-        r->store.results.push_back(sr);
-        const uint64_t local = jobs[j].read - r->read_base;
-        r->store.per_read[local][jobs[j].tag].result = &r->store.results.back();
     }
+    ews_.jobs.reserve(nj);
+    SA_CUDA(cudaMemcpyAsync(ews_.jobs.p, h_jobs_.p, nj * sizeof(ExtJob), cudaMemcpyHostToDevice, st_));
+    AlignScores sc{mp_.match, mp_.mismatch, mp_.gap_open, mp_.gap_extend, mp_.end_bonus};
+    run_extension_raw(refs_view_, arena_seq_.p, arena_off_.p, nullptr, nullptr, idx_->sp.k, sc, (uint32_t)nj, ews_,
+                      max_qlen, st_);
+    auto w = std::make_shared<WaveResults>();
+    w->results.swap(ews_.h_results);
+    w->cigar.swap(ews_.h_cigar);
+    for (auto& b : batch) b.first->chunks[b.second].wave = w;
 }
 
 void Session::worker() {
@@ -454,6 +490,7 @@ void Session::complete(Request& r) {
     for (auto& c : r.chunks) {
         total += c.out.size();
         r.mapped += c.mapped;
+        r.d2h_bytes += c.result_bytes;
     }
     r.out.reserve(total);
     for (auto& c : r.chunks) r.out += c.out;
@@ -479,6 +516,7 @@ void Session::complete(Request& r) {
     }
     cv_done_.notify_all();
     cv_engine_.notify_one();
+    cv_admit_.notify_one();
 }
 
 // called with mu_ held
@@ -506,6 +544,8 @@ void Session::fail_all(const std::string& msg, int32_t code) {
     inflight_ = 0;
     cv_done_.notify_all();
     cv_work_.notify_all();
+    cv_engine_.notify_all();
+    cv_admit_.notify_all();
 }
 
 }  // namespace sa

@@ -63,6 +63,7 @@ struct Request {
     uint64_t mapped = 0;
     std::vector<double> abundance;
     uint32_t waves = 0;
+    uint64_t h2d_bytes = 0, d2h_bytes = 0;  // this request's share of the transfers
     int state = 0;  // 0 queued, 1 admitted, 2 done, 3 failed
     std::string error;
     int32_t error_code = 0;
@@ -91,6 +92,7 @@ class Session {
 
   private:
     void engine();
+    void admitter();
     void worker();
     void admit(Request& r);
     void run_wave(std::vector<std::pair<Request*, size_t>>& batch);
@@ -106,7 +108,8 @@ class Session {
     SessionConfig cfg_;
     std::vector<ContigInfo> contigs_;
     uint32_t max_contig_len_ = 0;
-    cudaStream_t st_ = nullptr;
+    cudaStream_t st_ = nullptr;   // extension waves
+    cudaStream_t sta_ = nullptr;  // admissions
     DevBuf<uint64_t> d_words_, d_woff_;
     DevBuf<uint32_t> d_clen_;
     DevRefs refs_view_{};
@@ -114,6 +117,7 @@ class Session {
     ExtWorkspace ews_;
     PinnedBuf<uint8_t> h_seq_;
     PinnedBuf<uint64_t> h_off_;
+    PinnedBuf<ExtJob> h_jobs_;
     // read arena
     DevBuf<uint8_t> arena_seq_;
     DevBuf<uint64_t> arena_off_;
@@ -121,7 +125,7 @@ class Session {
     std::vector<uint64_t> h_goff_;
 
     mutable std::mutex mu_;
-    std::condition_variable cv_engine_, cv_work_, cv_done_;
+    std::condition_variable cv_engine_, cv_admit_, cv_work_, cv_done_;
     std::deque<std::unique_ptr<Request>> queue_;                    // submitted, not admitted
     std::unordered_map<uint64_t, std::unique_ptr<Request>> live_;  // admitted or done
     std::deque<std::pair<Request*, size_t>> ready_;
@@ -132,13 +136,16 @@ class Session {
     uint32_t inflight_ = 0;
     bool stop_ = false;
     bool workers_stop_ = false;
+    bool admitting_ = false;
     bool broken_ = false;  // a device or internal error failed every request
     std::string broken_msg_;
     // failed requests stay allocated until the session is destroyed: queued work
     // items may still point at them
     std::vector<std::unique_ptr<Request>> graveyard_;
     uint64_t wave_min_jobs_ = 32768;
-    std::thread engine_;
+    bool trace_ = false;
+    std::chrono::steady_clock::time_point t0_;
+    std::thread engine_, admitter_;
     std::vector<std::thread> workers_;
 };
 
