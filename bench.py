@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload (1.0 = full)")
     ap.add_argument("--cpu-sample-pairs", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-served", action="store_true", help="skip the served and latency passes (profiling runs)")
     return ap.parse_args()
 
 
@@ -313,31 +314,35 @@ def main():
     plain_h2d, plain_d2h = h2d, d2h
     # served: the same pairs as a stream of requests (log-uniform 1..100k pairs), each
     # its own chunk stream, through one session with continuous batching
-    sizes = request_sizes(len(R1))
-    reqs, a = [], 0
-    for n in sizes:
-        reqs.append((slice_reads(sa, r1, a, a + n), slice_reads(sa, r2, a, a + n)))
-        a += n
-    session = sa.Session(index, refs)
-    served_pass(session, reqs)  # warm-up: arena, workspaces
-    barrier()
-    t0 = time.perf_counter()
-    s_h2d = s_d2h = 0
-    for _ in range(args.steps):
-        _, sst = served_pass(session, reqs)
-        s_h2d = sum(int(x["h2d_bytes"]) for x in sst)
-        s_d2h = sum(int(x["d2h_bytes"]) for x in sst)
-    barrier()
-    served_s = time.perf_counter() - t0
-    if pg:
-        tt = torch.tensor([served_s], device="cuda")
-        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
-        served_s = float(tt.item())
-    served = ws * n_reads * args.steps / served_s
-    cap_rps = len(reqs) * args.steps / served_s
-    lat = latency_pass(session, reqs, 0.7 * cap_rps, max(60, min(400, int(3 * 0.7 * cap_rps))))
-    session.close()
-    e2e = served
+    reqs, lat = [], None
+    served = s_h2d = s_d2h = None
+    if not args.no_served:
+        sizes = request_sizes(len(R1))
+        a = 0
+        for n in sizes:
+            reqs.append((slice_reads(sa, r1, a, a + n), slice_reads(sa, r2, a, a + n)))
+            a += n
+        session = sa.Session(index, refs)
+        served_pass(session, reqs)  # warm-up: arena, workspaces
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            _, sst = served_pass(session, reqs)
+            s_h2d = sum(int(x["h2d_bytes"]) for x in sst)
+            s_d2h = sum(int(x["d2h_bytes"]) for x in sst)
+        barrier()
+        served_s = time.perf_counter() - t0
+        if pg:
+            tt = torch.tensor([served_s], device="cuda")
+            pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+            served_s = float(tt.item())
+        served = ws * n_reads * args.steps / served_s
+        cap_rps = len(reqs) * args.steps / served_s
+        lat = latency_pass(session, reqs, 0.7 * cap_rps, max(60, min(400, int(3 * 0.7 * cap_rps))))
+        session.close()
+    e2e = served if served is not None else plain_e2e
+    if served is None:
+        s_h2d, s_d2h = plain_h2d, plain_d2h
     if rank != 0:
         pg.destroy_process_group()
         return
@@ -367,8 +372,8 @@ def main():
         "e2e": {"value": e2e, "unit": "reads/s", "h2d_bytes_per_step": s_h2d, "d2h_bytes_per_step": s_d2h},
         "plain": {"value_resident": value, "e2e": plain_e2e, "unit": "reads/s", "h2d_bytes_per_step": plain_h2d,
                   "d2h_bytes_per_step": plain_d2h},
-        "served": {"value": served, "unit": "reads/s", "vs_plain_e2e": served / plain_e2e,
-                   "latency_open_loop": lat},
+        "served": None if served is None else {"value": served, "unit": "reads/s",
+                                               "vs_plain_e2e": served / plain_e2e, "latency_open_loop": lat},
         "gpu_launches": launches,
         "stage_share": shares,
         "roofline": roofline,

@@ -1284,6 +1284,261 @@ __global__ void __launch_bounds__(128) k_band_warp(SswTask* tasks, uint32_t n_ta
     }
 }
 
+// The same band pass for any band width: the row's cells in chunks of 32 lanes,
+// the previous and current rows in shared memory (two buffers each for H and E),
+// and the F scan carried from chunk to chunk.  Directions: four ballots per chunk
+// and row, in the task's slice of the direction arena.
+__device__ int band_pass_wide(const uint8_t* ref, const uint8_t* read, int rl, int ql, int bw, const AlignScores& sc,
+                              int* buf, int maxc, uint32_t* rowbits, int nch) {
+    const int lane = threadIdx.x & 31;
+    const int gO = sc.gap_open, gE = sc.gap_extend;
+    const int width = 2 * bw + 3;
+    constexpr int NEG = -(1 << 28);
+    int* Hp = buf;
+    int* Ep = buf + maxc;
+    int* Hc = buf + 2 * maxc;
+    int* Ec = buf + 3 * maxc;
+    for (int t = lane; t <= width && t < maxc; t += 32) {
+        Hp[t] = 0;
+        Ep[t] = 0;
+    }
+    __syncwarp();
+    int mx = 0;
+    for (int i = 0; i < ql; i++) {
+        const int x = i - bw > 0 ? i - bw : 0, xe = i - 1 - bw > 0 ? i - 1 - bw : 0;
+        const int end = rl - 1 < i + bw ? rl - 1 : i + bw;
+        const int n = end - x + 1;
+        const int edge = end + 1 < width - 1 ? end + 1 : width - 1;
+        const int sh = x - xe;
+        const int rcode = c_ssw_code[read[i]];
+        int carryT = NEG, prevH = 0, prevF = 0;
+        for (int c = 0; c * 32 < n; c++) {
+            const int k = 32 * c + lane;
+            const bool act = k < n;
+            int upH = 0, upE = 0, dg = 0, D = 0;
+            if (act) {
+                if (k + sh + 1 != edge) {
+                    upH = Hp[k + sh];
+                    upE = Ep[k + sh];
+                }
+                dg = k + sh == 0 ? 0 : Hp[k + sh - 1];
+                D = dg + mat_score(c_ssw_code[ref[x + k]], rcode, sc);
+            }
+            const int t1 = i == 0 ? -gO : upH - gO;
+            const int t2 = i == 0 ? -gE : upE - gE;
+            const int E = t1 > t2 ? t1 : t2;
+            const bool dde3 = t1 > t2;
+            const int e1 = E > 0 ? E : 0;
+            const int B = e1 > D ? e1 : D;
+            int T = act ? B - gO : NEG;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int Tp = __shfl_up_sync(FULLM, T, d);
+                const int cc = Tp - d * gE;
+                if (lane >= d && cc > T) T = cc;
+            }
+            {
+                const int cc = carryT - (lane + 1) * gE;
+                if (cc > T) T = cc;
+            }
+            int Sx = __shfl_up_sync(FULLM, T, 1);
+            if (lane == 0) Sx = carryT;
+            const int f0 = -(k + 1) * gE;
+            const int f = Sx > f0 ? Sx : f0;
+            const int f1 = f > 0 ? f : 0;
+            const int H = B > f1 ? B : f1;
+            int Hl = __shfl_up_sync(FULLM, H, 1), fl = __shfl_up_sync(FULLM, f, 1);
+            if (lane == 0) {
+                Hl = prevH;
+                fl = prevF;
+            }
+            const bool ddf5 = Hl - gO > fl - gE;
+            const int tm = e1 > f1 ? e1 : f1;
+            if (act && H > mx) mx = H;
+            if (rowbits) {
+                const unsigned b0 = __ballot_sync(FULLM, act && dde3);
+                const unsigned b1 = __ballot_sync(FULLM, act && ddf5);
+                const unsigned b2 = __ballot_sync(FULLM, act && tm <= D);
+                const unsigned b3 = __ballot_sync(FULLM, act && e1 > f1);
+                if (lane == 0) {
+                    uint32_t* w = rowbits + ((size_t)i * nch + c) * 4;
+                    w[0] = b0;
+                    w[1] = b1;
+                    w[2] = b2;
+                    w[3] = b3;
+                }
+            }
+            if (act) {
+                Hc[k] = H;
+                Ec[k] = E;
+            }
+            carryT = __shfl_sync(FULLM, T, 31);
+            prevH = __shfl_sync(FULLM, H, 31);
+            prevF = __shfl_sync(FULLM, f, 31);
+        }
+        __syncwarp();
+        int* t = Hp;
+        Hp = Hc;
+        Hc = t;
+        t = Ep;
+        Ep = Ec;
+        Ec = t;
+    }
+    for (int d = 16; d > 0; d >>= 1) {
+        const int o = __shfl_xor_sync(FULLM, mx, d);
+        mx = mx > o ? mx : o;
+    }
+    return mx;
+}
+
+// traceback (ext/ssw/ssw.c:680-753) over the flat direction array of (2bw+1) x 3
+// bytes per row, decoded from the per-chunk ballots; one thread.
+__device__ bool band_traceback(const uint32_t* rowbits, int nch, int rl, int ql, int bw, uint32_t* c, uint32_t cap,
+                               uint32_t& nc_out) {
+    const int width_d = 2 * bw + 1;
+    const int64_t dsize = (int64_t)width_d * ql * 3;
+    auto dir_at = [&](int64_t at) -> int {
+        const int row = (int)(at / (3 * width_d));
+        const int rem = (int)(at % (3 * width_d));
+        const int k = rem / 3, w = rem % 3;
+        const int x = row - bw > 0 ? row - bw : 0;
+        const int end = rl - 1 < row + bw ? rl - 1 : row + bw;
+        if (k > end - x) return 0;  // not written by the pass
+        const uint32_t* rb = rowbits + ((size_t)row * nch + (k >> 5)) * 4;
+        const int bit = k & 31;
+        const int dde = (rb[0] >> bit) & 1 ? 3 : 2;
+        const int ddf = (rb[1] >> bit) & 1 ? 5 : 4;
+        if (w == 0) return dde;
+        if (w == 1) return ddf;
+        return (rb[2] >> bit) & 1 ? 1 : ((rb[3] >> bit) & 1 ? dde : ddf);
+    };
+    int i = ql - 1, j = rl - 1, e = 0, which = 2;
+    int64_t line = (int64_t)width_d * i * 3;
+    char op = 'M', prev = 'M';
+    uint32_t nc = 0;
+    auto enc = [](int l, char o) -> uint32_t { return ((uint32_t)l << 4) | (o == 'M' ? 0u : o == 'I' ? 1u : 2u); };
+    while (i >= 0 && j > 0) {
+        const int x = i - bw > 0 ? i - bw : 0;
+        const int64_t at = line + (int64_t)(j - x) * 3 + which;
+        if (at < 0 || at >= dsize) return false;
+        switch (dir_at(at)) {
+            case 1: --i; --j; which = 2; line -= width_d * 3; op = 'M'; break;
+            case 2: --i; which = 0; line -= width_d * 3; op = 'I'; break;
+            case 3: --i; which = 2; line -= width_d * 3; op = 'I'; break;
+            case 4: --j; which = 1; op = 'D'; break;
+            case 5: --j; which = 2; op = 'D'; break;
+            default: return false;
+        }
+        if (op == prev) ++e;
+        else {
+            if (nc >= cap) return false;
+            c[nc++] = enc(e, prev);
+            prev = op;
+            e = 1;
+        }
+    }
+    if (nc + 2 > cap) return false;
+    if (op == 'M') c[nc++] = enc(e + 1, op);
+    else {
+        c[nc++] = enc(e, op);
+        c[nc++] = enc(1, 'M');
+    }
+    for (uint32_t a = 0, b = nc - 1; a < b; a++, b--) {
+        const uint32_t tmp = c[a];
+        c[a] = c[b];
+        c[b] = tmp;
+    }
+    nc_out = nc;
+    return true;
+}
+
+// Band width search of the tasks k_band_warp left (raw_off == RAW_FALLBACK), warp
+// per task; sizes their direction (ballot words) and CIGAR slices.
+__global__ void __launch_bounds__(32) k_band_width_wide(SswTask* tasks, const uint32_t* n_tasks_ptr, const PrepRec* prep,
+                                                        const uint8_t* arena, AlignScores sc, int maxc,
+                                                        uint64_t* dir_size, uint64_t* raw_size, uint32_t* counters) {
+    extern __shared__ int band_smem[];
+    const int lane = threadIdx.x & 31;
+    const uint32_t n = *n_tasks_ptr;
+    for (;;) {
+        uint32_t ti = 0;
+        if (lane == 0) ti = atomicAdd(&counters[7], 1u);
+        ti = __shfl_sync(FULLM, ti, 0);
+        if (ti >= n) break;
+        SswTask tk = tasks[ti];
+        if (tk.ref_begin1 < 0 || tk.read_begin1 < 0 || tk.raw_off != RAW_FALLBACK) {
+            if (lane == 0) {
+                dir_size[ti] = 0;
+                raw_size[ti] = 0;
+            }
+            continue;
+        }
+        const PrepRec p = prep[tk.job];
+        const uint8_t* q = arena + p.arena_off;
+        const uint8_t* r = q + p.qlen;
+        const int rl = tk.ref_end1 - tk.ref_begin1 + 1, ql = tk.read_end1 - tk.read_begin1 + 1;
+        const int len = rl > ql ? rl : ql;
+        int bw = (rl > ql ? rl - ql : ql - rl) + 1;
+        int mx = 0;
+        bool fail = false;
+        do {
+            if (2 * bw + 4 > maxc) {
+                fail = true;
+                break;
+            }
+            mx = band_pass_wide(r + tk.ref_begin1, q + tk.read_begin1, rl, ql, bw, sc, band_smem, maxc, nullptr, 0);
+            bw *= 2;
+        } while (mx < tk.score1 && bw <= len);
+        bw /= 2;
+        if (lane == 0) {
+            tk.band_width = bw;
+            if (fail) tk.flag = 1;
+            tasks[ti] = tk;
+            const uint64_t nch = (uint64_t)(2 * bw + 1 + 31) / 32;
+            dir_size[ti] = fail ? 0 : (uint64_t)ql * nch * 16;
+            raw_size[ti] = fail ? 0 : (uint64_t)rl + ql + 4;
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(32) k_band_trace_wide(SswTask* tasks, const uint32_t* n_tasks_ptr, const PrepRec* prep,
+                                                        const uint8_t* arena, AlignScores sc, int maxc,
+                                                        const uint64_t* dir_off, uint8_t* dir,
+                                                        const uint64_t* raw_off, uint32_t* raw, uint32_t* counters) {
+    extern __shared__ int band_smem[];
+    const int lane = threadIdx.x & 31;
+    const uint32_t n = *n_tasks_ptr;
+    for (;;) {
+        uint32_t ti = 0;
+        if (lane == 0) ti = atomicAdd(&counters[18], 1u);
+        ti = __shfl_sync(FULLM, ti, 0);
+        if (ti >= n) break;
+        SswTask tk = tasks[ti];
+        if (tk.ref_begin1 < 0 || tk.read_begin1 < 0 || tk.raw_off != RAW_FALLBACK || tk.flag == 1) continue;
+        const PrepRec p = prep[tk.job];
+        const uint8_t* q = arena + p.arena_off;
+        const uint8_t* r = q + p.qlen;
+        const int rl = tk.ref_end1 - tk.ref_begin1 + 1, ql = tk.read_end1 - tk.read_begin1 + 1;
+        const int bw = tk.band_width;
+        const int nch = (2 * bw + 1 + 31) / 32;
+        uint32_t* rowbits = reinterpret_cast<uint32_t*>(dir + dir_off[ti]);
+        band_pass_wide(r + tk.ref_begin1, q + tk.read_begin1, rl, ql, bw, sc, band_smem, maxc, rowbits, nch);
+        __syncwarp();
+        if (lane == 0) {
+            uint32_t nc = 0;
+            if (band_traceback(rowbits, nch, rl, ql, bw, raw + raw_off[ti], (uint32_t)(rl + ql + 4), nc)) {
+                tk.raw_len = nc;
+            } else {
+                tk.flag = 1;
+                tk.raw_len = 0;
+            }
+            tasks[ti] = tk;
+        }
+        __syncwarp();
+    }
+}
+
 __global__ void k_band_width(SswTask* tasks, const uint32_t* n_tasks_ptr, const PrepRec* prep, const uint8_t* arena,
                              int32_t* hscratch, AlignScores sc, uint64_t* dir_size, uint64_t* raw_size) {
     const uint32_t n = *n_tasks_ptr;
@@ -1730,9 +1985,27 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
         ws.dir_off.reserve((size_t)n_tasks + 1);
         ws.raw_size.reserve((size_t)n_tasks + 1);
         ws.raw_off.reserve((size_t)n_tasks + 1);
+        const bool wide = sc.gap_open >= sc.gap_extend;
+        const int maxc = 2 * (int)std::max<uint32_t>(2048, max_qlen) + 8;
+        const size_t band_smem = (size_t)4 * maxc * sizeof(int);
+        unsigned band_blocks = (unsigned)std::min<uint64_t>(n_tasks, 152ULL * 3);
+        if (!band_blocks) band_blocks = 1;
         kt->begin(KS_BAND, st);
-        k_band_width<<<grid1(n_tasks, 128), 128, 0, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p,
-                                                          ws.hscratch.p, sc, ws.dir_size.p, ws.raw_size.p);
+        if (wide) {
+            static int attr_smem = 0;
+            if ((int)band_smem > attr_smem) {
+                SA_CUDA(cudaFuncSetAttribute(k_band_width_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)band_smem));
+                SA_CUDA(cudaFuncSetAttribute(k_band_trace_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)band_smem));
+                attr_smem = (int)band_smem;
+            }
+            k_band_width_wide<<<band_blocks, 32, band_smem, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p, sc,
+                                                                 maxc, ws.dir_size.p, ws.raw_size.p, ws.counters.p);
+        } else {
+            k_band_width<<<grid1(n_tasks, 128), 128, 0, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p,
+                                                              ws.hscratch.p, sc, ws.dir_size.p, ws.raw_size.p);
+        }
         kt->end(st);
         launches++;
         SA_CUDA(cudaMemsetAsync(ws.dir_size.p + n_tasks, 0, 8, st));
@@ -1748,9 +2021,14 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
         ws.raw.reserve(rtot + 1);
         SA_CUDA(cudaMemsetAsync(ws.dir.p, 0, dtot + 16, st));
         kt->begin(KS_BAND, st);
-        k_band_trace<<<grid1(n_tasks, 128), 128, 0, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p,
-                                                          ws.hscratch.p, sc, ws.dir_off.p, ws.dir.p, ws.raw_off.p,
-                                                          ws.raw.p);
+        if (wide)
+            k_band_trace_wide<<<band_blocks, 32, band_smem, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p, sc,
+                                                                 maxc, ws.dir_off.p, ws.dir.p, ws.raw_off.p, ws.raw.p,
+                                                                 ws.counters.p);
+        else
+            k_band_trace<<<grid1(n_tasks, 128), 128, 0, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p,
+                                                              ws.hscratch.p, sc, ws.dir_off.p, ws.dir.p, ws.raw_off.p,
+                                                              ws.raw.p);
         kt->end(st);
         kt->begin(KS_FINALIZE, st);
         k_finalize<<<grid1(n_tasks, 128), 128, 0, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p,
