@@ -167,6 +167,16 @@ def run_reference(args, ws, rank):
     print(json.dumps(out), flush=True)
 
 
+def slowest_rank(pg, seconds: float, device: str = "cpu") -> float:
+    """Max over ranks of a rank's wall time (the job's time); identity without a process group."""
+    if pg is None:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
 def request_sizes(n_pairs: int, seed: int = 105, lo: int = 1, hi: int = 100_000) -> list[int]:
     """Request sizes in pairs, log-uniform in [lo, hi], covering the workload's pairs in order."""
     import numpy as np
@@ -290,10 +300,7 @@ def main():
     mapper.set_profiling(False)
     ev_ms = ev0.elapsed_time(ev1)
     elapsed = max(wall, ev_ms / 1000.0)
-    if pg:
-        tt = torch.tensor([elapsed], device="cuda")
-        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
-        elapsed = float(tt.item())
+    elapsed = slowest_rank(pg, elapsed, "cuda")
     value = ws * n_reads * args.steps / elapsed
     sam_bytes = len(out)
     # end to end: host buffers in, SAM bytes out, every step
@@ -306,10 +313,7 @@ def main():
         h2d, d2h = int(st["h2d_bytes"]), int(st["d2h_bytes"])
     barrier()
     e2e_s = time.perf_counter() - t0
-    if pg:
-        tt = torch.tensor([e2e_s], device="cuda")
-        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = slowest_rank(pg, e2e_s, "cuda")
     plain_e2e = ws * n_reads * args.steps / e2e_s
     plain_h2d, plain_d2h = h2d, d2h
     # served: the same pairs as a stream of requests (log-uniform 1..100k pairs), each
@@ -332,10 +336,7 @@ def main():
             s_d2h = sum(int(x["d2h_bytes"]) for x in sst)
         barrier()
         served_s = time.perf_counter() - t0
-        if pg:
-            tt = torch.tensor([served_s], device="cuda")
-            pg.all_reduce(tt, op=pg.ReduceOp.MAX)
-            served_s = float(tt.item())
+        served_s = slowest_rank(pg, served_s, "cuda")
         served = ws * n_reads * args.steps / served_s
         cap_rps = len(reqs) * args.steps / served_s
         lat = latency_pass(session, reqs, 0.7 * cap_rps, max(60, min(400, int(3 * 0.7 * cap_rps))))

@@ -243,8 +243,9 @@ int32_t sa_index_read_sti(const char* path, const sa_seeding_params* p, int32_t 
     rd(&reserved, 8);
     std::vector<char> skip(reserved);
     if (reserved) rd(skip.data(), reserved);
-    uint32_t v[10];
-    rd(v, 4 * 10);
+    // filter_cutoff, bits, profile, k, s, w_min, w_max, q, max_dist (src/index.rs:384-402)
+    uint32_t v[9];
+    rd(v, 4 * 9);
     uint64_t main_mask;
     rd(&main_mask, 8);
     const uint32_t cutoff = v[0], sbits = v[1];
