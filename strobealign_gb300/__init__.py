@@ -350,13 +350,15 @@ class Mapper:
         self.h = h
         self.last = None
 
-    def map(self, r1: Reads, r2: Reads | None = None) -> bytes:
+    def map(self, r1: Reads, r2: Reads | None = None, copy: bool = True):
+        """Output bytes; with copy=False only their length (the bytes stay in the
+        library's buffer, which is freed: for timing runs)."""
         o = L.Output()
         b1 = r1.c()
         b2 = r2.c() if r2 is not None else None
         L.check(lib().sa_map_batch(self.h, C.byref(b1), C.byref(b2) if b2 is not None else None, C.byref(o)))
         try:
-            data = C.string_at(o.data, o.len) if o.len else b""
+            data = (C.string_at(o.data, o.len) if o.len else b"") if copy else o.len
             self.last = dict(n_reads=o.n_reads, n_mapped=o.n_mapped, n_waves=o.n_waves,
                              n_gpu_launches=o.n_gpu_launches)
             return data
@@ -371,12 +373,14 @@ class Mapper:
         L.check(lib().sa_mapper_upload(self.h, C.byref(self._b1),
                                        C.byref(self._b2) if self._b2 is not None else None))
 
-    def map_uploaded(self) -> bytes:
+    def map_uploaded(self, copy: bool = True):
         o = L.Output()
         L.check(lib().sa_map_uploaded(self.h, C.byref(o)))
         try:
             self.last = dict(n_reads=o.n_reads, n_mapped=o.n_mapped, n_waves=o.n_waves,
                              n_gpu_launches=o.n_gpu_launches)
+            if not copy:
+                return o.len
             return C.string_at(o.data, o.len) if o.len else b""
         finally:
             lib().sa_output_free(C.byref(o))
@@ -441,15 +445,15 @@ class Session:
         L.check(lib().sa_session_poll(self.h, ticket, C.byref(d)))
         return bool(d.value)
 
-    def wait(self, ticket: int, timeout_ms: int = -1, abundances: bool = False):
-        """(output bytes, stats dict[, abundances])"""
+    def wait(self, ticket: int, timeout_ms: int = -1, abundances: bool = False, copy: bool = True):
+        """(output bytes, stats dict[, abundances]); copy=False gives the output length instead."""
         o = L.Output()
         st = L.RequestStats()
         ab = np.zeros(len(self.refs), dtype=np.float64) if abundances else None
         L.check(lib().sa_session_wait(self.h, ticket, timeout_ms, C.byref(o), C.byref(st),
                                       _p(ab, C.c_double) if ab is not None else None, len(ab) if ab is not None else 0))
         try:
-            data = C.string_at(o.data, o.len) if o.len else b""
+            data = (C.string_at(o.data, o.len) if o.len else b"") if copy else o.len
         finally:
             lib().sa_output_free(C.byref(o))
         stats = {f: getattr(st, f) for f, _ in L.RequestStats._fields_}

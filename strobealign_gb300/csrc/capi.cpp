@@ -679,11 +679,10 @@ int32_t sa_session_wait(sa_session* s, uint64_t ticket, int64_t timeout_ms, sa_o
     require(s && out, "null argument");
     std::unique_ptr<Request> r;
     if (!s->s->wait(ticket, timeout_ms, r)) throw Error(SA_ERR_TIMEOUT, "request not finished within the timeout");
-    out->data = (char*)std::malloc(r->out.size() + 1);
-    if (!out->data) throw Error(SA_ERR_OOM, "output allocation failed");
-    std::memcpy(out->data, r->out.data(), r->out.size());
-    out->data[r->out.size()] = 0;
-    out->len = r->out.size();
+    if (!r->out) throw Error(r->error_code ? r->error_code : SA_ERR_OOM, r->error);
+    out->data = r->out;  // ownership passes to the caller (sa_output_free)
+    out->len = r->out_len;
+    r->out = nullptr;
     out->n_reads = r->n_reads;
     out->n_mapped = r->mapped;
     out->n_waves = r->waves;

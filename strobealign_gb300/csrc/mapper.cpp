@@ -15,6 +15,7 @@
 #include <mutex>
 #include <thread>
 
+#include "host_util.h"
 #include "mapper.h"
 
 namespace sa {
@@ -357,8 +358,9 @@ void Mapper::map_uploaded(sa_output* out) {
     const uint32_t waves = schedule(chunks, store, launches);
     if (trace_) {
         double sr = 0, ss = 0, sd = 0;
-        uint64_t er = 0, es = 0, runs = 0;
+        uint64_t er = 0, es = 0, runs = 0, eu = 0;
         for (auto& c : chunks) {
+            eu += c.evals_reused;
             sr += c.seconds_real;
             ss += c.seconds_spec;
             sd += c.seconds_seed;
@@ -367,9 +369,9 @@ void Mapper::map_uploaded(sa_output* out) {
             runs += c.runs;
         }
         std::fprintf(stderr, "sa_policy chunks=%zu runs=%llu cpu_real=%.3f cpu_spec=%.3f cpu_seed=%.3f evals_real=%llu "
-                             "evals_spec=%llu\n",
+                             "evals_spec=%llu reused=%llu\n",
                      chunks.size(), (unsigned long long)runs, sr, ss, sd, (unsigned long long)er,
-                     (unsigned long long)es);
+                     (unsigned long long)es, (unsigned long long)eu);
     }
     for (auto& c : chunks)
         for (auto& a : c.abundance) abundances_[a.first] += a.second;
@@ -381,10 +383,11 @@ void Mapper::map_uploaded(sa_output* out) {
     }
     out->data = (char*)std::malloc(total_len + 1);
     if (!out->data) throw Error(SA_ERR_OOM, "output allocation failed");
-    size_t o = 0;
-    for (auto& c : chunks) {
-        std::memcpy(out->data + o, c.out.data(), c.out.size());
-        o += c.out.size();
+    {
+        std::vector<const std::string*> parts;
+        parts.reserve(chunks.size());
+        for (auto& c : chunks) parts.push_back(&c.out);
+        parallel_concat(parts, out->data, policy_threads_);
     }
     out->data[total_len] = 0;
     out->len = total_len;

@@ -135,95 +135,147 @@ char comp_char(char c) {
     }
 }
 
-// CIGAR with soft clips, merged like Cigar::push (src/mapper.rs:173-182), in =/X or M form
-void put_cigar(std::string& o, const Alignment& a, bool eqx) {
+// CIGAR with soft clips, merged like Cigar::push (src/mapper.rs:173-182), in =/X or M form: w_cigar
+
+// Pointer writers for format_sam: the record is written into space reserved for
+// its largest possible size, then the string is cut to what was written.
+inline char* w_u64(char* p, uint64_t v) {
+    char b[24];
+    int n = 0;
+    do { b[n++] = (char)('0' + v % 10); v /= 10; } while (v);
+    while (n) *p++ = b[--n];
+    return p;
+}
+inline char* w_i64(char* p, int64_t v) {
+    if (v < 0) {
+        *p++ = '-';
+        return w_u64(p, (uint64_t)(-v));
+    }
+    return w_u64(p, (uint64_t)v);
+}
+inline char* w_str(char* p, const char* s, size_t n) {
+    std::memcpy(p, s, n);
+    return p + n;
+}
+inline char* w_lit(char* p, const char* s) { return w_str(p, s, std::strlen(s)); }
+
+struct CompTable {
+    char t[256];
+    CompTable() {
+        for (int i = 0; i < 256; i++) t[i] = comp_char((char)i);
+    }
+};
+const CompTable COMP;
+
+char* w_cigar(char* p, const Alignment& a, bool eqx) {
     static const char ch[] = "MIDNSHP=X";
     uint32_t pend_op = 99, pend_len = 0;
     auto push = [&](uint32_t op, uint32_t len) {
         if (len == 0) return;
         if (!eqx && (op == 7 || op == 8)) op = 0;
-        if (op == pend_op) { pend_len += len; return; }
-        if (pend_len) { put_u64(o, pend_len); o.push_back(ch[pend_op]); }
+        if (op == pend_op) {
+            pend_len += len;
+            return;
+        }
+        if (pend_len) {
+            p = w_u64(p, pend_len);
+            *p++ = ch[pend_op];
+        }
         pend_op = op;
         pend_len = len;
     };
     push(4, a.soft_clip_left);
     for (uint32_t i = 0; i < a.cigar_len; i++) push(a.cigar[i] & 15, a.cigar[i] >> 4);
     push(4, a.soft_clip_right);
-    if (pend_len) { put_u64(o, pend_len); o.push_back(ch[pend_op]); }
+    if (pend_len) {
+        p = w_u64(p, pend_len);
+        *p++ = ch[pend_op];
+    }
+    return p;
 }
 
 // src/io/sam.rs:53-138
 void format_sam(const Sam& r, const PolicyConfig& cfg, std::string& o) {
     const bool secondary = (r.flags & SECONDARY) != 0;
     const ReadView& rv = *r.rv;
-    o.append(rv.name, rv.name_len);
-    o.push_back('\t');
-    put_u64(o, r.flags);
-    o.push_back('\t');
-    if (r.rname) o += *r.rname;
-    else o.push_back('*');
-    o.push_back('\t');
-    put_u64(o, r.has_pos ? (uint64_t)r.pos + 1 : 0);
-    o.push_back('\t');
-    put_u64(o, r.mapq);
-    o.push_back('\t');
-    if (r.aln) put_cigar(o, *r.aln, cfg.mp.eqx != 0);
-    else o.push_back('*');
-    o.push_back('\t');
-    if (r.rnext) o += *r.rnext;
-    else o.push_back('*');
-    o.push_back('\t');
-    put_u64(o, r.has_pnext ? (uint64_t)r.pnext + 1 : 0);
-    o.push_back('\t');
-    put_i64(o, r.has_tlen ? r.tlen : 0);
-    o.push_back('\t');
+    size_t bound = rv.name_len + 2 * (size_t)rv.len + 160;
+    if (r.rname) bound += r.rname->size();
+    if (r.rnext) bound += r.rnext->size();
+    if (r.aln) bound += ((size_t)r.aln->cigar_len + 2) * 11;
+    if (cfg.has_rg) bound += 6 + cfg.rg_id.size();
+    if (cfg.mp.fastq_comments && rv.comment) bound += 1 + rv.comment_len;
+    const size_t start = o.size();
+    o.resize(start + bound);
+    char* const base = &o[start];
+    char* p = base;
+    p = w_str(p, rv.name, rv.name_len);
+    *p++ = '\t';
+    p = w_u64(p, r.flags);
+    *p++ = '\t';
+    if (r.rname) p = w_str(p, r.rname->data(), r.rname->size());
+    else *p++ = '*';
+    *p++ = '\t';
+    p = w_u64(p, r.has_pos ? (uint64_t)r.pos + 1 : 0);
+    *p++ = '\t';
+    p = w_u64(p, r.mapq);
+    *p++ = '\t';
+    if (r.aln) p = w_cigar(p, *r.aln, cfg.mp.eqx != 0);
+    else *p++ = '*';
+    *p++ = '\t';
+    if (r.rnext) p = w_str(p, r.rnext->data(), r.rnext->size());
+    else *p++ = '*';
+    *p++ = '\t';
+    p = w_u64(p, r.has_pnext ? (uint64_t)r.pnext + 1 : 0);
+    *p++ = '\t';
+    p = w_i64(p, r.has_tlen ? r.tlen : 0);
+    *p++ = '\t';
     if (!secondary && rv.len > 0) {
         if (r.seq_rc)
-            for (uint32_t i = rv.len; i-- > 0;) o.push_back(comp_char(rv.seq[i]));
+            for (uint32_t i = rv.len; i-- > 0;) *p++ = COMP.t[(uint8_t)rv.seq[i]];
         else
-            o.append(rv.seq, rv.len);
+            p = w_str(p, rv.seq, rv.len);
     } else {
-        o.push_back('*');
+        *p++ = '*';
     }
-    o.push_back('\t');
+    *p++ = '\t';
     if (rv.qual && !secondary && rv.len > 0) {
         if (r.seq_rc)
-            for (uint32_t i = rv.len; i-- > 0;) o.push_back(rv.qual[i]);
+            for (uint32_t i = rv.len; i-- > 0;) *p++ = rv.qual[i];
         else
-            o.append(rv.qual, rv.len);
+            p = w_str(p, rv.qual, rv.len);
     } else {
-        o.push_back('*');
+        *p++ = '*';
     }
     if (r.has_nm) {
-        o += "\tNM:i:";
-        put_u64(o, r.nm);
-        o += "\tAS:i:";
-        put_u64(o, r.as);
+        p = w_lit(p, "\tNM:i:");
+        p = w_u64(p, r.nm);
+        p = w_lit(p, "\tAS:i:");
+        p = w_u64(p, r.as);
     }
     if (cfg.mp.details && r.det) {
-        o += "\tna:i:";
-        put_u64(o, r.det->nam.n_nams);
-        o += "\tal:i:";
-        put_u64(o, r.det->tried_alignment);
-        o += "\tga:i:";
-        put_u64(o, r.det->gapped);
-        o += "\tX0:i:";
-        put_u64(o, r.det->best_alignments);
+        p = w_lit(p, "\tna:i:");
+        p = w_u64(p, r.det->nam.n_nams);
+        p = w_lit(p, "\tal:i:");
+        p = w_u64(p, r.det->tried_alignment);
+        p = w_lit(p, "\tga:i:");
+        p = w_u64(p, r.det->gapped);
+        p = w_lit(p, "\tX0:i:");
+        p = w_u64(p, r.det->best_alignments);
         if (r.flags & PAIRED) {
-            o += "\tmr:i:";
-            put_u64(o, r.det->mate_rescue);
+            p = w_lit(p, "\tmr:i:");
+            p = w_u64(p, r.det->mate_rescue);
         }
     }
     if (cfg.has_rg) {
-        o += "\tRG:Z:";
-        o += cfg.rg_id;
+        p = w_lit(p, "\tRG:Z:");
+        p = w_str(p, cfg.rg_id.data(), cfg.rg_id.size());
     }
     if (cfg.mp.fastq_comments && rv.comment) {
-        o.push_back('\t');
-        o.append(rv.comment, rv.comment_len);
+        *p++ = '\t';
+        p = w_str(p, rv.comment, rv.comment_len);
     }
-    o.push_back('\n');
+    *p++ = '\n';
+    o.resize(start + (size_t)(p - base));
 }
 
 Sam mapped_record(const Policy& P, const Alignment& a, const ReadView& rv, uint8_t mapq, bool secondary,
@@ -1248,7 +1300,20 @@ void Policy::run_chunk(ChunkState& cs) {
                 break;
         }
     };
+    const bool capture = cfg_.mp.mode == SA_MODE_SAM || cfg_.mp.mode == SA_MODE_PAF;
     while (cs.next < cs.end) {
+        if (capture && !cs.effects.empty()) {
+            const auto& ef = cs.effects[cs.next - cs.first];
+            if (ef.has_output && ef.pre_rng == cs.rng.state && ef.pre_isd.same_state(cs.isd)) {
+                cs.out.append(cs.spec_out, ef.out_off, ef.out_len);
+                cs.rng.state += ef.rng_delta;
+                cs.isd = ef.post_isd;
+                cs.mapped += ef.mapped;
+                cs.next++;
+                cs.evals_reused++;
+                continue;
+            }
+        }
         Rng rng = cs.rng;
         InsertSize isd = cs.isd;
         size_t out_len = cs.out.size(), ab_len = cs.abundance.size();
@@ -1277,17 +1342,31 @@ void Policy::run_chunk(ChunkState& cs) {
                 InsertSize i2 = sisd;
                 uint64_t m2 = 0;
                 auto& ef = cs.effects[rec - cs.first];
+                const size_t o0 = cs.spec_out.size();
+                speculative_ = !capture;  // when capturing, records are formatted into spec_out
                 try {
-                    one(rec, r2, i2, scratch, m2);
+                    one(rec, r2, i2, capture ? cs.spec_out : scratch, m2);
                     ef.known = true;
                     ef.rng_delta = r2.state - srng.state;
                     ef.isd_update = i2.sample_size != sisd.sample_size;
                     ef.isd_value = i2.last;
+                    if (capture) {
+                        ef.has_output = true;
+                        ef.pre_rng = srng.state;
+                        ef.pre_isd = sisd;
+                        ef.post_isd = i2;
+                        ef.out_off = o0;
+                        ef.out_len = cs.spec_out.size() - o0;
+                        ef.mapped = m2;
+                    }
                 } catch (const Miss&) {
                     // keep the draws made before the miss; see above for the estimate
                     ef.known = false;
+                    ef.has_output = false;
+                    if (capture) cs.spec_out.resize(o0);
                     todo.push_back(rec);
                 }
+                speculative_ = true;
                 srng = r2;
                 sisd = i2;
             };
@@ -1324,6 +1403,8 @@ void Policy::run_chunk(ChunkState& cs) {
     }
     if (timing) cs.seconds_real += since(t_run);
     cs.done = true;
+    std::string().swap(cs.spec_out);
+    std::vector<ChunkState::Effect>().swap(cs.effects);
 }
 
 }  // namespace sa

@@ -4,6 +4,7 @@
 // runs another extension wave and resumes the chunk at the read that missed.
 #pragma once
 #include <cstdint>
+#include <cstring>
 #include <deque>
 #include <memory>
 #include <string>
@@ -29,6 +30,15 @@ struct InsertSize {
     float mu = 300.0f, sigma = 100.0f, variance = 10000.0f, sse = 10000.0f;
     uint64_t last = 0;  // value of the last accepted update (replayed by the lookahead)
     void update(uint64_t insert_size);
+    bool same_state(const InsertSize& o) const {
+        auto bits = [](float f) {
+            uint32_t u;
+            std::memcpy(&u, &f, 4);
+            return u;
+        };
+        return sample_size == o.sample_size && bits(mu) == bits(o.mu) && bits(sigma) == bits(o.sigma) &&
+               bits(variance) == bits(o.variance) && bits(sse) == bits(o.sse);
+    }
 };
 
 struct Details {
@@ -134,8 +144,16 @@ struct ChunkState {
         uint64_t rng_delta = 0;
         uint64_t isd_value = 0;
         bool known = false, isd_update = false;
+        // SAM / PAF: the record's output from that evaluation and the state it started
+        // from; the real run reuses it when it reaches the record in the same state
+        bool has_output = false;
+        uint64_t pre_rng = 0;
+        InsertSize pre_isd, post_isd;
+        uint64_t out_off = 0, out_len = 0, mapped = 0;
     };
     std::vector<Effect> effects;
+    std::string spec_out;  // outputs captured by the lookahead
+    uint64_t evals_reused = 0;
     // host time by phase when PolicyConfig::timing is set
     double seconds_real = 0, seconds_spec = 0, seconds_seed = 0;
     uint64_t evals_real = 0, evals_spec = 0, runs = 0;

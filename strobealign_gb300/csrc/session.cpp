@@ -11,6 +11,7 @@
 #include <cstdlib>
 #include <cstring>
 
+#include "host_util.h"
 #include "session.h"
 
 namespace sa {
@@ -492,8 +493,17 @@ void Session::complete(Request& r) {
         r.mapped += c.mapped;
         r.d2h_bytes += c.result_bytes;
     }
-    r.out.reserve(total);
-    for (auto& c : r.chunks) r.out += c.out;
+    r.out = (char*)std::malloc(total + 1);
+    if (r.out) {
+        std::vector<const std::string*> parts;
+        for (auto& c : r.chunks) parts.push_back(&c.out);
+        parallel_concat(parts, r.out, total >= (64u << 20) ? 4 : 1);
+        r.out[total] = 0;
+        r.out_len = total;
+    } else {
+        r.error = "output allocation failed";
+        r.error_code = SA_ERR_OOM;
+    }
     if (mp_.mode == SA_MODE_ABUNDANCE) {
         r.abundance.assign(contigs_.size(), 0.0);
         for (auto& c : r.chunks)

@@ -7,6 +7,7 @@
 // flight.
 #pragma once
 #include <chrono>
+#include <cstdlib>
 #include <condition_variable>
 #include <deque>
 #include <map>
@@ -58,8 +59,9 @@ struct Request {
     std::vector<ChunkState> chunks;
     std::vector<uint8_t> seeded;
     size_t n_done = 0;
-    // result
-    std::string out;
+    // result: malloc'd, handed over to the caller by sa_session_wait
+    char* out = nullptr;
+    size_t out_len = 0;
     uint64_t mapped = 0;
     std::vector<double> abundance;
     uint32_t waves = 0;
@@ -68,6 +70,7 @@ struct Request {
     std::string error;
     int32_t error_code = 0;
     std::chrono::steady_clock::time_point t_submit, t_admit, t_done;
+    ~Request() { std::free(out); }
 };
 
 struct SessionConfig {
