@@ -143,7 +143,8 @@ __global__ void __launch_bounds__(64) k_rescue_filter(const uint32_t* __restrict
 __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict__ seq,
                           const uint64_t* __restrict__ off, DevRefs R, uint32_t k, const uint8_t* raw_refs,
                           const uint64_t* raw_off, ExtResult* res, PrepRec* prep, uint64_t* sz_arena,
-                          uint64_t* sz_cigar, uint64_t* sz_h, uint32_t* rescue_list, uint32_t* n_rescue) {
+                          uint64_t* sz_cigar, uint64_t* sz_h, uint32_t* rescue_list, uint32_t* n_rescue,
+                          uint32_t* max_pw_window) {
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         ExtJob jb = jobs[t];
         const uint8_t* s = seq + off[jb.read];
@@ -201,6 +202,19 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
                 p.wlen = (uint32_t)(we - ws);
                 // Aligner::align returns None for reference segments over 2000 (src/aligner.rs:83-86)
                 p.type = (jb.use_ssw && p.wlen <= 2000 && L > 0) ? 2 : 0;
+                if (!jb.use_ssw) {
+                    // extend_piecewise on the NAM's anchors over [ref_start - (L + pad),
+                    // ref_end + L + pad) (src/mapper.rs:588-610); single-end only, and only
+                    // for consistent NAMs (the policy drops the others)
+                    const uint64_t span = (uint64_t)L + pad;
+                    const uint32_t ds = jb.ref_start > span ? (uint32_t)(jb.ref_start - span) : 0;
+                    uint64_t de = (uint64_t)jb.ref_end + span;
+                    if (de > clen) de = clen;
+                    p.wstart = ds;
+                    p.wlen = de > ds ? (uint32_t)(de - ds) : 0;
+                    p.type = (cons && jb.anc_n > 0 && L > 0) ? 3 : 0;
+                    if (p.type == 3) atomicMax(max_pw_window, p.wlen);
+                }
             }
         } else if (jb.kind == JOB_RESCUE) {
             bool rc = jb.is_revcomp;
@@ -220,6 +234,10 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
         }
         uint64_t ab = 0, cap = 0, hs = 0;
         if (p.type == 1) cap = L + 1;
+        if (p.type == 3) {
+            ab = (uint64_t)L + p.wlen;
+            cap = (uint64_t)L + p.wlen + 8;  // every op consumes a query or reference base
+        }
         if (p.type == 2) {
             ab = (uint64_t)L + p.wlen;
             cap = 2ull * L + p.wlen + 4;
@@ -252,7 +270,7 @@ struct CigarWriter {
 __global__ void k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict__ seq, const uint64_t* __restrict__ off,
                        DevRefs R, const uint8_t* raw_refs, const uint64_t* raw_off, AlignScores sc, PrepRec* prep,
                        const uint64_t* off_arena, const uint64_t* off_cigar, const uint64_t* off_h, uint8_t* arena,
-                       uint32_t* cigar, ExtResult* res, SswTask* tasks, uint32_t* counters) {
+                       uint32_t* cigar, ExtResult* res, SswTask* tasks, uint32_t* counters, uint32_t* pw_list) {
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         PrepRec p = prep[t];
         p.arena_off = off_arena[t];
@@ -294,6 +312,12 @@ __global__ void k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict
             r.cigar_offset = (uint32_t)p.cigar_off;
             r.cigar_len = w.n;
             res[t] = r;
+        } else if (p.type == 3) {
+            uint8_t* q = arena + p.arena_off;
+            for (uint32_t i = 0; i < L; i++) q[i] = read_char(s, L, i, p.rc);
+            uint8_t* w = q + L;
+            for (uint32_t i = 0; i < p.wlen; i++) w[i] = ref_base(R, p.ref_id, p.wstart + i);
+            pw_list[atomicAdd(&counters[19], 1u)] = t;
         } else if (p.type == 2) {
             uint8_t* q = arena + p.arena_off;
             for (uint32_t i = 0; i < L; i++) q[i] = read_char(s, L, i, p.rc);
@@ -1761,6 +1785,386 @@ __global__ void k_finalize(const SswTask* tasks, const uint32_t* n_tasks_ptr, co
     }
 }
 
+// ------------------------------------------------------------------ piecewise (single end)
+// extend_piecewise (src/piecewisealigner.rs:396-510) with remove_spurious_anchors
+// (:596-719), warp per job.  The reference runs its DP pieces with the block-aligner
+// crate; they are computed here as full affine-gap DPs with the traceback tie rules of
+// the oracle's restatement (diagonal first, then the gap that produced H), which makes
+// this path parity-unpinned beyond the reference's golden cases.
+//
+// A piece's DP runs row by row on the warp, the columns in chunks of 32 lanes: F and
+// the diagonal come from the previous row (shared memory), and the row's E chain
+// E(j) = max(H(j-1) - gO, E(j-1) - gE) is a max-plus scan of max(diag, F) - gO over the
+// lanes (exact for gap_open >= gap_extend, since H(j-1) = max(that, E(j-1))).  Each cell
+// keeps four direction bits for the traceback.
+constexpr int PW_NEG = -(1 << 28);
+constexpr uint8_t PW_DIAG = 1, PW_FROM_E = 2, PW_EEXT = 4, PW_FEXT = 8;
+
+struct PwPiece {
+    int score;
+    int bi, bj;  // end cell
+    int nops;    // traceback ops, last op first (OP codes of src/cigar.rs)
+};
+
+// q: n query bytes, r: m reference bytes (REV: both read backwards).  LOCAL: best cell
+// (strict >, row-major, from 0) with the end bonus on the last query row; otherwise the
+// end is (n, m).  ops receives the traceback from the end cell back to (0, 0).
+template <bool LOCAL, bool REV>
+__device__ PwPiece pw_dp(const uint8_t* q, int n, const uint8_t* r, int m, const AlignScores& sc, int* rowbuf,
+                         uint8_t* dirs, uint8_t* ops) {
+    const int lane = threadIdx.x & 31;
+    const int go = sc.gap_open, ge = sc.gap_extend, match = sc.match, mism = sc.mismatch;
+    const int W = m + 1;
+    int* Hp = rowbuf;
+    int* Fp = rowbuf + W;
+    int* Hc = rowbuf + 2 * W;
+    int* Fc = rowbuf + 3 * W;
+    auto qv = [&](int i) { return REV ? q[n - 1 - i] : q[i]; };
+    auto rv = [&](int j) { return REV ? r[m - 1 - j] : r[j]; };
+    for (int j = lane; j <= m; j += 32) {
+        Hp[j] = j == 0 ? 0 : -go - (j - 1) * ge;
+        Fp[j] = PW_NEG;
+        uint8_t d = 0;
+        if (j >= 1) {
+            d |= PW_FROM_E;                        // H(0, j) = E(0, j)
+            if (j >= 2 && go != ge) d |= PW_EEXT;  // E(0, j) extends E(0, j-1), not opened from H
+        }
+        dirs[j] = d;
+    }
+    __syncwarp();
+    int best = 0, bi = 0, bj = 0;
+    for (int i = 1; i <= n; i++) {
+        const int hcol0 = -go - (i - 1) * ge;  // H(i, 0) = F(i, 0)
+        if (lane == 0) {
+            Hc[0] = hcol0;
+            Fc[0] = hcol0;
+            dirs[(size_t)i * W] = (i >= 2 && go != ge) ? PW_FEXT : 0;
+        }
+        const int qc = qv(i - 1);
+        const int bonus = (LOCAL && i == n) ? (int)sc.end_bonus : 0;
+        int carryT = hcol0 - go, carryE = PW_NEG, carryH = hcol0;
+        for (int c = 0; c * 32 < m; c++) {
+            const int j = 1 + 32 * c + lane;
+            const bool act = j <= m;
+            int F = PW_NEG, D = PW_NEG, B = PW_NEG;
+            bool fext = false;
+            if (act) {
+                const int hu = Hp[j], fu = Fp[j];
+                const int f1 = hu - go, f2 = fu - ge;
+                F = f1 > f2 ? f1 : f2;
+                fext = F == fu - ge && F != hu - go;
+                D = Hp[j - 1] + (qc == rv(j - 1) ? match : -mism) + bonus;
+                B = D > F ? D : F;
+            }
+            int T = act ? B - go : PW_NEG;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int Tp = __shfl_up_sync(FULLM, T, d);
+                const int cc = Tp - d * ge;
+                if (lane >= d && cc > T) T = cc;
+            }
+            {
+                const int cc = carryT - (lane + 1) * ge;
+                if (cc > T) T = cc;
+            }
+            int E = __shfl_up_sync(FULLM, T, 1);
+            if (lane == 0) E = carryT;
+            const int H = B > E ? B : E;
+            int El = __shfl_up_sync(FULLM, E, 1), Hl = __shfl_up_sync(FULLM, H, 1);
+            if (lane == 0) {
+                El = carryE;
+                Hl = carryH;
+            }
+            const bool eext = E == El - ge && E != Hl - go;
+            if (act) {
+                uint8_t d = 0;
+                if (H == D) d |= PW_DIAG;
+                if (H == E) d |= PW_FROM_E;
+                if (eext) d |= PW_EEXT;
+                if (fext) d |= PW_FEXT;
+                dirs[(size_t)i * W + j] = d;
+                Hc[j] = H;
+                Fc[j] = F;
+            }
+            if (LOCAL) {
+                int v = act ? H : PW_NEG;
+                for (int d = 16; d > 0; d >>= 1) {
+                    const int o = __shfl_xor_sync(FULLM, v, d);
+                    v = v > o ? v : o;
+                }
+                if (v > best) {
+                    const unsigned at = __ballot_sync(FULLM, act && H == v);
+                    best = v;
+                    bi = i;
+                    bj = 1 + 32 * c + (__ffs(at) - 1);
+                }
+            }
+            carryT = __shfl_sync(FULLM, T, 31);
+            carryE = __shfl_sync(FULLM, E, 31);
+            carryH = __shfl_sync(FULLM, H, 31);
+        }
+        __syncwarp();
+        int* t = Hp;
+        Hp = Hc;
+        Hc = t;
+        t = Fp;
+        Fp = Fc;
+        Fc = t;
+    }
+    if (!LOCAL) {
+        best = Hp[m];
+        bi = n;
+        bj = m;
+    }
+    __syncwarp();
+    PwPiece res;
+    res.score = best;
+    res.bi = bi;
+    res.bj = bj;
+    res.nops = 0;
+    if (lane == 0) {
+        int i = bi, j = bj, state = 0, nops = 0;
+        const int limit = 2 * (n + m) + 4;
+        for (int it = 0; (i > 0 || j > 0) && it < limit; it++) {
+            const uint8_t d = dirs[(size_t)i * W + j];
+            if (state == 0) {
+                if (i > 0 && j > 0 && (d & PW_DIAG)) {
+                    ops[nops++] = qv(i - 1) == rv(j - 1) ? 7 : 8;  // = / X
+                    i--;
+                    j--;
+                } else if (j > 0 && (d & PW_FROM_E)) {
+                    state = 1;
+                } else {
+                    state = 2;
+                }
+            } else if (state == 1) {
+                ops[nops++] = 2;  // D
+                const bool ext = j > 1 && (d & PW_EEXT);
+                j--;
+                state = ext ? 1 : 0;
+                if (i == 0 && j > 0) state = 1;
+            } else {
+                ops[nops++] = 1;  // I
+                const bool ext = i > 1 && (d & PW_FEXT);
+                i--;
+                state = ext ? 2 : 0;
+                if (j == 0 && i > 0) state = 2;
+            }
+        }
+        res.nops = nops;
+    }
+    res.nops = __shfl_sync(FULLM, res.nops, 0);
+    __syncwarp();
+    return res;
+}
+
+__global__ void __launch_bounds__(32) k_piecewise(const uint32_t* __restrict__ list, const uint32_t* n_list_ptr,
+                                                  const ExtJob* jobs, const PrepRec* prep, const uint8_t* arena,
+                                                  const uint32_t* __restrict__ anchors, AlignScores sc, uint32_t k,
+                                                  uint8_t* scratch, uint64_t cells_bytes, uint64_t ops_bytes,
+                                                  uint32_t* cigar, ExtResult* res, uint32_t* counters) {
+    extern __shared__ int pw_rows[];
+    const int lane = threadIdx.x & 31;
+    const uint32_t n_list = *n_list_ptr;
+    uint8_t* dirs = scratch + (size_t)blockIdx.x * (cells_bytes + ops_bytes);
+    uint8_t* ops = dirs + cells_bytes;
+    for (;;) {
+        uint32_t li = 0;
+        if (lane == 0) li = atomicAdd(&counters[22], 1u);
+        li = __shfl_sync(FULLM, li, 0);
+        if (li >= n_list) break;
+        const uint32_t t = list[li];
+        const ExtJob jb = jobs[t];
+        const PrepRec p = prep[t];
+        const uint8_t* q = arena + p.arena_off;
+        const uint8_t* dref = q + p.qlen;
+        const int L = (int)p.qlen, RL = (int)p.wlen;
+        const int padding = L / 10;
+        // anchors (last to first) as (query start, reference start in dref); the
+        // pruning below rewrites them in this task's slice of the ops scratch
+        int* anc = reinterpret_cast<int*>(ops + (((size_t)L + RL + 8 + 15) & ~(size_t)15));
+        const int na0 = (int)jb.anc_n;
+        for (int a = lane; a < na0; a += 32) {
+            anc[2 * a] = (int)anchors[2 * ((size_t)jb.anc_off + a)];
+            anc[2 * a + 1] = (int)anchors[2 * ((size_t)jb.anc_off + a) + 1] - (int)p.wstart;
+        }
+        __syncwarp();
+        int na = na0;
+        if (lane == 0) {
+            // remove_spurious_anchors (src/piecewisealigner.rs:596-719)
+            auto erase = [&](int from, int to) {  // [from, to)
+                for (int x = to; x < na; x++) {
+                    anc[2 * (x - (to - from))] = anc[2 * x];
+                    anc[2 * (x - (to - from)) + 1] = anc[2 * x + 1];
+                }
+                na -= to - from;
+            };
+            if (na >= 2) {
+                const long long tol = 5;
+                long long tracked = 0;
+                bool has_dev = false;
+                int dev = 0, i = 1;
+                while (i < na) {
+                    const long long qd = (long long)anc[2 * (i - 1)] - anc[2 * i];
+                    const long long rd = (long long)anc[2 * (i - 1) + 1] - anc[2 * i + 1];
+                    const long long indel = qd - rd;
+                    if ((indel < 0 ? -indel : indel) > tol) {
+                        const long long tt = tracked + indel;
+                        if (has_dev && (tt < 0 ? -tt : tt) <= tol) {
+                            erase(dev, i);
+                            i = dev;
+                            has_dev = false;
+                            tracked = 0;
+                            continue;
+                        }
+                        has_dev = true;
+                        dev = i;
+                        tracked = indel;
+                    }
+                    i++;
+                }
+                const int max_prune = (int)ceilf(__fmul_rn((float)na, 0.20f));
+                const int lim = na < max_prune ? na : max_prune;
+                for (int x = 1; x < lim; x++) {
+                    const long long qd = (long long)anc[2 * x] - anc[2 * (x - 1)];
+                    const long long rd = (long long)anc[2 * x + 1] - anc[2 * (x - 1) + 1];
+                    if (qd - rd != 0) {
+                        erase(0, x);
+                        break;
+                    }
+                }
+                const int lo = (na > max_prune ? na - max_prune : 0) + 1;
+                for (int x = na; x-- > lo;) {
+                    const long long qd = (long long)anc[2 * x] - anc[2 * (x - 1)];
+                    const long long rd = (long long)anc[2 * x + 1] - anc[2 * (x - 1) + 1];
+                    if (qd - rd != 0) {
+                        erase(x, na);
+                        break;
+                    }
+                }
+            }
+        }
+        na = __shfl_sync(FULLM, na, 0);
+        __syncwarp();
+        CigarWriter w{cigar + p.cigar_off, 0, p.cigar_cap, false};
+        auto push = [&](uint32_t op, int len) {
+            if (lane == 0 && len > 0) w.push(op, (uint32_t)len);
+        };
+        const int K = (int)k;
+        // before the first anchor
+        const int fqs = anc[2 * (na - 1)], frs = anc[2 * (na - 1) + 1];
+        int pre_qs, pre_rs, score;
+        if (fqs > 0 && frs > 0) {
+            const int rs = frs > fqs + padding ? frs - (fqs + padding) : 0;
+            const PwPiece pc = pw_dp<true, true>(q, fqs, dref + rs, frs - rs, sc, pw_rows, dirs, ops);
+            if (pc.score == 0) {
+                pre_qs = fqs;
+                pre_rs = frs;
+                score = 0;
+            } else {
+                pre_qs = fqs - pc.bi;
+                pre_rs = rs + (frs - rs) - pc.bj;
+                score = pc.score;
+                for (int x = 0; x < pc.nops; x++) push(ops[x], 1);
+            }
+        } else {
+            pre_qs = fqs;
+            pre_rs = frs;
+            score = fqs == 0 ? (int)sc.end_bonus : 0;
+        }
+        score += K * (int)sc.match;
+        push(7, K);
+        for (int i = na - 1; i >= 1; i--) {
+            const int cqs = anc[2 * (i - 1)], crs = anc[2 * (i - 1) + 1];
+            const int pqe = anc[2 * i] + K, prre = anc[2 * i + 1] + K;
+            const int qd = cqs - pqe, rd = crs - prre;
+            if (rd > 0 && qd > 0) {
+                if (rd == qd) {
+                    // hamming_align_global, taken if it scores above 85% of all matches
+                    int hs = 0;
+                    for (int x = 0; x < qd; x++) hs += q[pqe + x] == dref[prre + x] ? (int)sc.match : -(int)sc.mismatch;
+                    const int hsc = hs > 0 ? hs : 0;
+                    const uint32_t thr = (uint32_t)ceilf(__fmul_rn((float)qd, 0.85f));
+                    if (hsc > 0 && (uint32_t)hsc > (uint32_t)sc.match * thr) {
+                        score += hsc;
+                        for (int x = 0; x < qd; x++) push(q[pqe + x] == dref[prre + x] ? 7u : 8u, 1);
+                        score += K * (int)sc.match;
+                        push(7, K);
+                        continue;
+                    }
+                }
+                const PwPiece pc = pw_dp<false, false>(q + pqe, qd, dref + prre, rd, sc, pw_rows, dirs, ops);
+                score += pc.score;
+                for (int x = pc.nops; x-- > 0;) push(ops[x], 1);
+                score += K * (int)sc.match;
+                push(7, K);
+            } else if (rd < qd) {
+                const int ins = qd - rd;
+                score += -(int)sc.gap_open + (ins - 1) * -(int)sc.gap_extend;
+                push(1, ins);
+                const int mp = K + rd;
+                score += mp * (int)sc.match;
+                push(7, mp);
+            } else if (rd > qd) {
+                const int del = rd - qd;
+                score += -(int)sc.gap_open + (del - 1) * -(int)sc.gap_extend;
+                push(2, del);
+                const int mp = K + qd;
+                score += mp * (int)sc.match;
+                push(7, mp);
+            } else {
+                const int mp = K + qd;
+                score += mp * (int)sc.match;
+                push(7, mp);
+            }
+        }
+        // after the last anchor
+        const int lqe = anc[0] + K, lre = anc[1] + K;
+        int post_qe, post_re;
+        if (lqe < L && lre < RL) {
+            const int qlen2 = L - lqe;
+            const int re = lre + qlen2 + padding < RL ? lre + qlen2 + padding : RL;
+            const PwPiece pc = pw_dp<true, false>(q + lqe, qlen2, dref + lre, re - lre, sc, pw_rows, dirs, ops);
+            if (pc.score == 0) {
+                post_qe = lqe;
+                post_re = lre;
+            } else {
+                post_qe = lqe + pc.bi;
+                post_re = lre + pc.bj;
+                for (int x = pc.nops; x-- > 0;) push(ops[x], 1);
+            }
+            score += pc.score;
+        } else {
+            post_qe = lqe;
+            post_re = lre;
+            score += lqe == L ? (int)sc.end_bonus : 0;
+        }
+        if (lane == 0) {
+            ExtResult r = res[t];
+            r.valid = 0;
+            if (score > 0 && !w.overflow) {
+                uint32_t ed = 0;
+                for (uint32_t x = 0; x < w.n; x++) {
+                    const uint32_t op = w.out[x] & 15;
+                    if (op == 8 || op == 1 || op == 2) ed += w.out[x] >> 4;
+                }
+                r.valid = 1;
+                r.score = (uint32_t)score;
+                r.edit_distance = ed;
+                r.ref_start = p.wstart + (uint32_t)pre_rs;
+                r.length = (uint32_t)(post_re - pre_rs);
+                r.soft_clip_left = (uint32_t)pre_qs;
+                r.soft_clip_right = (uint32_t)(L - post_qe);
+                r.cigar_offset = (uint32_t)p.cigar_off;
+                r.cigar_len = w.n;
+                r.gapped = 1;
+            }
+            res[t] = r;
+        }
+        __syncwarp();
+    }
+}
+
 __global__ void k_cigar_used(const ExtResult* res, uint32_t n, uint64_t* used) {
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
         used[t] = res[t].valid ? res[t].cigar_len : 0;
@@ -1818,7 +2222,8 @@ void extension_init_tables() { init_tables(); }
 
 uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64_t* off, const uint8_t* raw_refs,
                            const uint64_t* raw_off, uint32_t k, const AlignScores& sc, uint32_t n, ExtWorkspace& ws,
-                           uint32_t max_qlen, cudaStream_t st, KernelTimers* kt) {
+                           uint32_t max_qlen, cudaStream_t st, KernelTimers* kt, const uint32_t* anchors,
+                           uint32_t max_anchors) {
     init_tables();
     KernelTimers none;
     if (!kt) kt = &none;
@@ -1839,7 +2244,8 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
     kt->begin(KS_PREPARE, st);
     ws.rescue_list.reserve(n);
     k_prepare<<<grid1(n), 256, 0, st>>>(ws.jobs.p, n, seq, off, refs, k, raw_refs, raw_off, ws.results.p, ws.prep.p,
-                                        sz[0], sz[1], sz[2], ws.rescue_list.p, ws.counters.p + 4);
+                                        sz[0], sz[1], sz[2], ws.rescue_list.p, ws.counters.p + 4,
+                                        ws.counters.p + 20);
     {
         static bool attr = false;
         const size_t smem = 2 * RESCUE_TAB_MAX * sizeof(unsigned long long);
@@ -1862,6 +2268,8 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
         excl_sum(ws, sz[c], of[c], (uint64_t)n + 1, st);
         SA_CUDA(cudaMemcpyAsync(&tot[c], of[c] + n, 8, cudaMemcpyDeviceToHost, st));
     }
+    uint32_t max_pw_window = 0;
+    SA_CUDA(cudaMemcpyAsync(&max_pw_window, ws.counters.p + 20, 4, cudaMemcpyDeviceToHost, st));
     launches += 3;
     SA_CUDA(cudaStreamSynchronize(st));
     ws.arena.reserve(tot[0] + 16);
@@ -1872,10 +2280,33 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
     ws.list_rev_byte.reserve(n);
     ws.list_rev_word.reserve(n);
     kt->begin(KS_FILL, st);
+    ws.pw_list.reserve(n);
     k_fill<<<grid1(n), 256, 0, st>>>(ws.jobs.p, n, seq, off, refs, raw_refs, raw_off, sc, ws.prep.p, of[0], of[1],
-                                     of[2], ws.arena.p, ws.cigar.p, ws.results.p, ws.tasks.p, ws.counters.p);
+                                     of[2], ws.arena.p, ws.cigar.p, ws.results.p, ws.tasks.p, ws.counters.p,
+                                     ws.pw_list.p);
     kt->end(st);
     launches++;
+    if (max_pw_window) {
+        // single-end piecewise jobs: a warp per job, each warp with its own DP scratch
+        if (!anchors) throw Error(SA_ERR_INVALID, "internal: piecewise jobs without anchors");
+        auto a16 = [](uint64_t x) { return (x + 15) & ~(uint64_t)15; };
+        const uint64_t cells = a16(((uint64_t)max_qlen + 1) * ((uint64_t)max_pw_window + 1));
+        const uint64_t opsb = a16((uint64_t)max_qlen + max_pw_window + 8) + a16(8ull * (max_anchors + 1));
+        const unsigned blocks = (unsigned)std::min<uint64_t>(n, 152ULL * 6);
+        ws.pw_scratch.reserve((cells + opsb) * blocks);
+        const size_t smem = 16 * ((size_t)max_pw_window + 2);
+        static size_t attr = 0;
+        if (smem > attr) {
+            SA_CUDA(cudaFuncSetAttribute(k_piecewise, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            attr = smem;
+        }
+        kt->begin(KS_EXT_OTHER, st);
+        k_piecewise<<<blocks, 32, smem, st>>>(ws.pw_list.p, ws.counters.p + 19, ws.jobs.p, ws.prep.p, ws.arena.p,
+                                              anchors, sc, k, ws.pw_scratch.p, cells, opsb, ws.cigar.p, ws.results.p,
+                                              ws.counters.p);
+        kt->end(st);
+        launches++;
+    }
     uint32_t cnt[4];
     SA_CUDA(cudaMemcpyAsync(cnt, ws.counters.p, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     SA_CUDA(cudaStreamSynchronize(st));
@@ -2061,8 +2492,10 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
 }
 
 uint32_t run_extension(const DevRefs& refs, const NamWorkspace& nws, uint32_t k, const AlignScores& sc, uint32_t n,
-                       ExtWorkspace& ws, uint32_t max_qlen, cudaStream_t st, KernelTimers* kt) {
-    return run_extension_raw(refs, nws.seq.p, nws.off.p, nullptr, nullptr, k, sc, n, ws, max_qlen, st, kt);
+                       ExtWorkspace& ws, uint32_t max_qlen, cudaStream_t st, KernelTimers* kt, const uint32_t* anchors,
+                       uint32_t max_anchors) {
+    return run_extension_raw(refs, nws.seq.p, nws.off.p, nullptr, nullptr, k, sc, n, ws, max_qlen, st, kt, anchors,
+                             max_anchors);
 }
 
 }  // namespace sa

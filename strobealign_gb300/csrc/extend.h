@@ -53,6 +53,9 @@ struct ExtWorkspace {
     DevBuf<uint32_t> rescue_list;
     DevBuf<uint32_t> list_word, list_rev_byte, list_rev_word;
     DevBuf<uint32_t> order;  // task order of the fused SSW kernel
+    DevBuf<uint32_t> pw_list;     // piecewise jobs
+    DevBuf<uint8_t> pw_scratch;   // per-warp DP directions, ops and anchors of k_piecewise
+    DevBuf<uint32_t> anchors;     // the wave's piecewise anchors (uploaded by the caller)
     DevBuf<uint64_t> dir_size, dir_off;
     DevBuf<uint8_t> dir;
     DevBuf<uint64_t> raw_size, raw_off;
@@ -68,12 +71,17 @@ struct ExtWorkspace {
 // Runs jobs (already in ws.jobs, n of them) against the reads in nws.seq/nws.off.
 // Results and CIGARs are copied back into ws.h_results / ws.h_cigar.  Returns the
 // number of kernel launches.
+// anchors: device (query start, reference start) pairs of the piecewise jobs
+// (ExtJob::anc_off / anc_n), max_anchors their largest count; null when no job has
+// use_ssw == 0.
 uint32_t run_extension(const DevRefs& refs, const NamWorkspace& nws, uint32_t k, const AlignScores& sc, uint32_t n,
-                       ExtWorkspace& ws, uint32_t max_qlen, cudaStream_t st, KernelTimers* kt = nullptr);
+                       ExtWorkspace& ws, uint32_t max_qlen, cudaStream_t st, KernelTimers* kt = nullptr,
+                       const uint32_t* anchors = nullptr, uint32_t max_anchors = 0);
 // The same for reads at seq + off[read] (off holds n_reads + 1 absolute offsets);
 // raw_refs / raw_off give the reference bytes of JOB_ALIGN jobs (may be null).
 uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64_t* off, const uint8_t* raw_refs,
                            const uint64_t* raw_off, uint32_t k, const AlignScores& sc, uint32_t n, ExtWorkspace& ws,
-                           uint32_t max_qlen, cudaStream_t st, KernelTimers* kt = nullptr);
+                           uint32_t max_qlen, cudaStream_t st, KernelTimers* kt = nullptr,
+                           const uint32_t* anchors = nullptr, uint32_t max_anchors = 0);
 
 }  // namespace sa

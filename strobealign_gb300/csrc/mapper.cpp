@@ -56,8 +56,8 @@ Mapper::Mapper(const sa_index* idx, const sa_refs* refs, const sa_chaining_param
     pcfg_.k = idx->sp.k;
     pcfg_.timing = trace_;
     if (!mp_.use_ssw && mp_.mode == SA_MODE_SAM) {
-        // single-end piecewise extension (block-aligner) has no device implementation; paired-end
-        // extension always uses SSW in the reference (src/mapper.rs:860-870)
+        // single-end extension without --ssw is piecewise on the NAM's anchors; paired-end
+        // extension always uses SSW (src/mapper.rs:860-870)
         single_end_piecewise_ = true;
     }
 }
@@ -98,9 +98,18 @@ void Mapper::nams_for_reads(uint32_t& launches) {
                          cp_.max_ref_gap, cp_.matches_weight, cp_.max_diagonal_ratio};
     cfg.mcs = mp_.mcs_strategy;
     cfg.rescue_distance = mp_.rescue_distance;
+    cfg.nam_anchors = single_end_piecewise_ && !bv_.paired;
     launches += run_nam_pipeline(idx_->view(), refs_view_, cfg, n_reads_, total_bases_, max_contig_len_,
                                  (uint32_t)refs_->contigs.size(), nws_, st_, &kt_);
     const uint64_t tn = nws_.last_total_nams;
+    if (cfg.nam_anchors) {
+        const uint64_t ta = nws_.last_total_nam_anchors;
+        h_nam_anc_off_.resize(tn + 1);
+        h_nam_anc_.resize(ta);
+        SA_CUDA(cudaMemcpyAsync(h_nam_anc_off_.data(), nws_.nam_anc_off.p, (tn + 1) * 8, cudaMemcpyDeviceToHost, st_));
+        if (ta) SA_CUDA(cudaMemcpyAsync(h_nam_anc_.data(), nws_.nam_anc.p, ta * 8, cudaMemcpyDeviceToHost, st_));
+        d2h_bytes_ += (tn + 1) * 8 + ta * 8;
+    }
     h_nam_off_.resize((size_t)n_reads_ + 1);
     h_nams_.resize(tn);
     h_details_.resize(n_reads_);
@@ -113,14 +122,21 @@ void Mapper::nams_for_reads(uint32_t& launches) {
 }
 
 std::shared_ptr<const WaveResults> Mapper::run_wave(const ExtJob* jobs, uint32_t nj, uint32_t max_qlen,
-                                                    uint32_t& launches) {
+                                                    uint32_t& launches, const std::vector<uint32_t>& anchors,
+                                                    uint32_t max_anchors) {
     auto w = std::make_shared<WaveResults>();
     if (!nj) return w;
     ews_.jobs.reserve(nj);
     SA_CUDA(cudaMemcpyAsync(ews_.jobs.p, jobs, (size_t)nj * sizeof(ExtJob), cudaMemcpyHostToDevice, st_));
     h2d_bytes_ += (size_t)nj * sizeof(ExtJob);
+    if (!anchors.empty()) {
+        ews_.anchors.reserve(anchors.size());
+        SA_CUDA(cudaMemcpyAsync(ews_.anchors.p, anchors.data(), anchors.size() * 4, cudaMemcpyHostToDevice, st_));
+        h2d_bytes_ += anchors.size() * 4;
+    }
     AlignScores sc{mp_.match, mp_.mismatch, mp_.gap_open, mp_.gap_extend, mp_.end_bonus};
-    launches += run_extension(refs_view_, nws_, idx_->sp.k, sc, nj, ews_, max_qlen, st_, &kt_);
+    launches += run_extension(refs_view_, nws_, idx_->sp.k, sc, nj, ews_, max_qlen, st_, &kt_,
+                              anchors.empty() ? nullptr : ews_.anchors.p, max_anchors);
     d2h_bytes_ += (size_t)nj * sizeof(ExtResult) + ews_.total_cigar * 4;
     for (int c = 0; c < 5; c++) sw_cells_[c] += ews_.cells[c];
     w->results.swap(ews_.h_results);
@@ -130,10 +146,6 @@ std::shared_ptr<const WaveResults> Mapper::run_wave(const ExtJob* jobs, uint32_t
 }
 
 void Mapper::upload(const sa_read_batch* r1, const sa_read_batch* r2) {
-    if (single_end_piecewise_ && !r2)
-        throw Error(SA_ERR_INVALID,
-                    "single-end SAM output needs use_ssw=1: the piecewise (block-aligner) extension is not "
-                    "implemented on the GPU");
     auto t0 = std::chrono::steady_clock::now();
     const bool paired = r2 != nullptr;
     if (paired && r2->n != r1->n) throw Error(SA_ERR_INVALID, "r1 and r2 batches differ in size");
@@ -287,9 +299,15 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, ResultStore& store, u
                 std::memcpy(h_jobs_.p + nj, chunks[c].pending.data(), chunks[c].pending.size() * sizeof(ExtJob));
                 nj += chunks[c].pending.size();
             }
+            wave_anchors_.clear();
+            uint32_t max_anchors = 0;
+            if (bv_.nam_anc) {
+                attach_piecewise_anchors(bv_, h_jobs_.p, nj, wave_anchors_);
+                for (size_t j = 0; j < nj; j++) max_anchors = std::max(max_anchors, h_jobs_.p[j].anc_n);
+            }
             if (waves > 1000000) throw Error(SA_ERR_INVALID, "internal: extension waves do not converge");
             auto tw = std::chrono::steady_clock::now();
-            auto wres = run_wave(h_jobs_.p, (uint32_t)nj, max_qlen_, launches);
+            auto wres = run_wave(h_jobs_.p, (uint32_t)nj, max_qlen_, launches, wave_anchors_, max_anchors);
             for (size_t c : batch) chunks[c].wave = wres;
             const auto tw2 = std::chrono::steady_clock::now();
             t_ext_ += std::chrono::duration<double>(tw2 - tw).count();
@@ -338,6 +356,11 @@ void Mapper::map_uploaded(sa_output* out) {
     bv.nams = h_nams_.data();
     bv.nam_off = h_nam_off_.data();
     bv.details = h_details_.data();
+    const bool piecewise = single_end_piecewise_ && !paired;
+    bv.nam_anc_off = piecewise ? h_nam_anc_off_.data() : nullptr;
+    bv.nam_anc = piecewise ? h_nam_anc_.data() : nullptr;
+    bv.anc_qbits = nws_.anchor_qbits;
+    bv.anc_pbits = nws_.anchor_pbits;
     // chunks (src/main.rs:591-604)
     std::vector<ChunkState> chunks;
     for (uint64_t i = 0; i < nrec;) {

@@ -42,7 +42,8 @@ class Mapper {
 
   private:
     std::shared_ptr<const WaveResults> run_wave(const ExtJob* jobs, uint32_t nj, uint32_t max_qlen,
-                                                uint32_t& launches);
+                                                uint32_t& launches, const std::vector<uint32_t>& anchors,
+                                                uint32_t max_anchors);
     uint32_t schedule(std::vector<ChunkState>& chunks, ResultStore& store, uint32_t& launches);
     BatchView bv_;
     bool have_batch_ = false;
@@ -77,6 +78,8 @@ class Mapper {
     std::vector<uint64_t> h_nam_off_;
     std::vector<NamRec> h_nams_;
     std::vector<NamDetailsRec> h_details_;
+    std::vector<uint64_t> h_nam_anc_off_, h_nam_anc_;  // single-end piecewise: NAM chain anchors
+    std::vector<uint32_t> wave_anchors_;
     uint32_t n_reads_ = 0;
     uint64_t total_bases_ = 0;
     uint64_t h2d_bytes_ = 0, d2h_bytes_ = 0;

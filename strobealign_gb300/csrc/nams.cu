@@ -527,7 +527,8 @@ __device__ __forceinline__ float chain_score(uint32_t dq, uint32_t dr, const Cha
 __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off, uint32_t n, const uint64_t* seg_off,
                                                const uint64_t* sorted, uint64_t* dedup, float* dp, uint32_t* pred,
                                                uint32_t* aux, uint64_t total_anchors, AnchorPack ap, ChainCtx cc,
-                                               NamRec* nam_out, uint32_t* nam_seg_count) {
+                                               NamRec* nam_out, uint32_t* nam_seg_count, uint64_t* anc_out,
+                                               uint64_t* anc_start) {
     const uint32_t lane = lane_id();
     const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
     const uint64_t qmask = (1ULL << ap.qbits) - 1, pmask = (1ULL << ap.pbits) - 1;
@@ -680,6 +681,11 @@ __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off,
         if (lane == 0) {
             uint32_t nn = 0;
             NamRec* outp = nam_out + b;
+            // a kept chain holds its end anchor (never marked used) and used
+            // predecessors, so kept chains list each anchor at most twice; a dropped
+            // chain's anchors are overwritten: 3 slots per anchor suffice
+            uint64_t* ao = anc_out ? anc_out + 3 * b : nullptr;
+            uint32_t acur = 0;
             for (uint32_t c = 0; c < M; c++) {
                 uint32_t i = sorted_c[c];
                 if (used[i]) continue;
@@ -687,11 +693,13 @@ __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off,
                 bool overlaps = false;
                 uint32_t nanch = 1;
                 const uint64_t ki = dedup[b + i];
+                if (ao) ao[acur] = ki;
                 uint32_t matching = cc.k;
                 uint32_t cov = (uint32_t)((ki >> ap.qbits) & pmask);
                 while (pred[b + j] != 0xffffffffu) {
                     j = pred[b + j];
                     if (used[j]) { overlaps = true; break; }
+                    if (ao) ao[acur + nanch] = dedup[b + j];
                     nanch++;
                     used[j] = 1;
                     uint32_t rsj = (uint32_t)((dedup[b + j] >> ap.qbits) & pmask);
@@ -712,6 +720,8 @@ __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off,
                 nr.score = __fadd_rn(dp[b + i], __fmul_rn(__uint2float_rn(nanch), cc.cp.matches_weight));
                 nr.is_revcomp = sg & 1;
                 nr.n_anchors = nanch;
+                if (anc_start) anc_start[b + nn] = 3 * b + acur;
+                acur += nanch;
                 outp[nn++] = nr;
             }
             nam_seg_count[sg] = nn;
@@ -724,7 +734,9 @@ __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off,
 // descending (src/nam.rs:168-170; the tie shuffle is applied by the host policy)
 __global__ void __launch_bounds__(256) k_nam_compact(uint32_t n, const uint64_t* seg_off, const NamRec* scratch,
                                                      const uint32_t* nam_seg_count, const uint64_t* nam_off,
-                                                     NamRec* out, NamDetailsRec* details) {
+                                                     NamRec* out, NamDetailsRec* details,
+                                                     const uint64_t* anc_start, uint64_t* anc_src,
+                                                     uint64_t* anc_count) {
     const uint32_t lane = lane_id();
     const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
     for (uint32_t r = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; r < n; r += nwarps) {
@@ -742,6 +754,10 @@ __global__ void __launch_bounds__(256) k_nam_compact(uint32_t n, const uint64_t*
             }
             nr.nam_id = t;
             out[ob + rank] = nr;
+            if (anc_src) {
+                anc_src[ob + rank] = t < c0 ? anc_start[seg_off[2 * r] + t] : anc_start[seg_off[2 * r + 1] + t - c0];
+                anc_count[ob + rank] = nr.n_anchors;
+            }
         }
         if (lane == 0) details[r].n_nams = c;
     }
@@ -750,6 +766,16 @@ __global__ void __launch_bounds__(256) k_nam_compact(uint32_t n, const uint64_t*
 __global__ void k_nam_counts(uint32_t n, const uint32_t* nam_seg_count, uint64_t* nam_count) {
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
         nam_count[r] = (uint64_t)nam_seg_count[2 * r] + nam_seg_count[2 * r + 1];
+}
+
+// each NAM's anchors, from the chaining scratch into one array in NAM output order
+__global__ void k_nam_anchor_gather(uint64_t total_nams, const uint64_t* src, const uint64_t* dst_off,
+                                    const uint64_t* sparse, uint64_t* dense) {
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total_nams;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t s = src[t], d = dst_off[t], c = dst_off[t + 1] - d;
+        for (uint64_t u = 0; u < c; u++) dense[d + u] = sparse[s + u];
+    }
 }
 
 inline unsigned warps_grid(uint64_t items) {
@@ -912,9 +938,14 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     ws.nam_seg_count.reserve(2 * (size_t)n);
     ChainCtx cc{cfg.cp, ix.p.k, ws.log2_lut.p};
     kt->begin(KS_CHAIN, st);
+    if (cfg.nam_anchors) {
+        ws.anc_sparse.reserve(3 * total_anchors + 1);
+        ws.anc_start.reserve(total_anchors + 1);
+    }
     k_chain<<<warps_grid(2 * (uint64_t)n), 32 * WARPS_PER_BLOCK, 0, st>>>(
         ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p, total_anchors, ap,
-        cc, ws.nam_scratch.p, ws.nam_seg_count.p);
+        cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
+        cfg.nam_anchors ? ws.anc_start.p : nullptr);
     kt->end(st);
     launches++;
     ws.nam_count.reserve((size_t)n + 1);
@@ -927,10 +958,34 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     SA_CUDA(cudaMemcpyAsync(&total_nams, ws.nam_off.p + n, 8, cudaMemcpyDeviceToHost, st));
     SA_CUDA(cudaStreamSynchronize(st));
     ws.nams.reserve(total_nams);
-    k_nam_compact<<<warps_grid(n), 32 * WARPS_PER_BLOCK, 0, st>>>(n, ws.seg_off.p, ws.nam_scratch.p,
-                                                                  ws.nam_seg_count.p, ws.nam_off.p, ws.nams.p,
-                                                                  ws.details.p);
+    if (cfg.nam_anchors) {
+        ws.nam_anc_src.reserve(total_nams + 1);
+        ws.nam_anc_off.reserve(total_nams + 1);
+    }
+    k_nam_compact<<<warps_grid(n), 32 * WARPS_PER_BLOCK, 0, st>>>(
+        n, ws.seg_off.p, ws.nam_scratch.p, ws.nam_seg_count.p, ws.nam_off.p, ws.nams.p, ws.details.p,
+        cfg.nam_anchors ? ws.anc_start.p : nullptr, cfg.nam_anchors ? ws.nam_anc_src.p : nullptr,
+        cfg.nam_anchors ? ws.nam_anc_off.p : nullptr);
     launches++;
+    ws.anchor_qbits = ap.qbits;
+    ws.anchor_pbits = ap.pbits;
+    ws.last_total_nam_anchors = 0;
+    if (cfg.nam_anchors) {
+        // counts -> offsets in place, then the gather
+        SA_CUDA(cudaMemsetAsync(ws.nam_anc_off.p + total_nams, 0, 8, st));
+        ws.nam_count.reserve(total_nams + 1);
+        SA_CUDA(cudaMemcpyAsync(ws.nam_count.p, ws.nam_anc_off.p, (total_nams + 1) * 8, cudaMemcpyDeviceToDevice, st));
+        cub_excl_sum(ws, ws.nam_count.p, ws.nam_anc_off.p, total_nams + 1, st);
+        uint64_t tot = 0;
+        SA_CUDA(cudaMemcpyAsync(&tot, ws.nam_anc_off.p + total_nams, 8, cudaMemcpyDeviceToHost, st));
+        SA_CUDA(cudaStreamSynchronize(st));
+        ws.nam_anc.reserve(tot + 1);
+        if (total_nams)
+            k_nam_anchor_gather<<<(unsigned)std::min<uint64_t>((total_nams + 255) / 256, 152 * 16), 256, 0, st>>>(
+                total_nams, ws.nam_anc_src.p, ws.nam_anc_off.p, ws.anc_sparse.p, ws.nam_anc.p);
+        launches += 3;
+        ws.last_total_nam_anchors = tot;
+    }
     SA_CUDA(cudaGetLastError());
     ws.last_total_nams = total_nams;
     return launches;

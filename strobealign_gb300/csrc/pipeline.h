@@ -42,6 +42,11 @@ struct NamWorkspace {
     DevBuf<uint64_t> nam_off;               // n + 1
     DevBuf<uint64_t> nam_count;             // n (u64 for the scan)
     DevBuf<NamRec> nams;
+    // with NamConfig::nam_anchors: the anchors of each NAM's chain, last to first
+    // (src/chainer.rs:420-440), as packed anchor keys; NAM t's are at
+    // nam_anc[nam_anc_off[t] .. nam_anc_off[t + 1])
+    DevBuf<uint64_t> anc_sparse, anc_start, nam_anc_src, nam_anc_off, nam_anc;
+    uint64_t last_total_nam_anchors = 0;
     DevBuf<uint8_t> cub_tmp;
     DevBuf<float> log2_lut;
     uint64_t last_total_nams = 0;
@@ -52,6 +57,7 @@ struct NamConfig {
     ChainParams cp;
     uint32_t mcs;
     uint32_t rescue_distance;
+    bool nam_anchors = false;  // also keep each NAM's chain anchors (single-end piecewise extension)
 };
 
 // Runs seeding -> hits -> rescue -> anchors -> sort -> chaining -> NAM compaction for

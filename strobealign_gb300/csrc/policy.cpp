@@ -560,8 +560,27 @@ ExtJob Policy::nam_job(uint32_t read, const NamRec& cur, uint32_t kind) const {
     j.query_start = n.query_start;
     j.query_end = n.query_end;
     j.is_revcomp = n.is_revcomp;
-    j.use_ssw = 1;
+    // paired-end extension always uses SSW (src/mapper.rs:860-870); single-end follows --ssw
+    j.use_ssw = (bv_.paired || cfg_.mp.use_ssw) ? 1 : 0;
+    j.nam = (uint32_t)(f != e ? f - b : 0);
     return j;
+}
+
+void attach_piecewise_anchors(const BatchView& bv, ExtJob* jobs, size_t n, std::vector<uint32_t>& anchors) {
+    const uint64_t qmask = (1ull << bv.anc_qbits) - 1, pmask = (1ull << bv.anc_pbits) - 1;
+    for (size_t i = 0; i < n; i++) {
+        ExtJob& j = jobs[i];
+        if (j.use_ssw || (j.kind != JOB_EXTEND_FAST && j.kind != JOB_EXTEND_FULL) || !bv.nam_anc) continue;
+        const uint64_t t = bv.nam_off[j.read] + j.nam;
+        const uint64_t a0 = bv.nam_anc_off[t], a1 = bv.nam_anc_off[t + 1];
+        j.anc_off = (uint32_t)(anchors.size() / 2);
+        j.anc_n = (uint32_t)(a1 - a0);
+        for (uint64_t a = a0; a < a1; a++) {
+            const uint64_t key = bv.nam_anc[a];
+            anchors.push_back((uint32_t)(key & qmask));
+            anchors.push_back((uint32_t)((key >> bv.anc_qbits) & pmask));
+        }
+    }
 }
 
 void Policy::want_nam(uint32_t read, const NamRec& n, uint32_t kind) { want(read, nam_job(read, n, kind), nam_key(n, kind)); }

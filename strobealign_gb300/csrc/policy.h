@@ -119,7 +119,16 @@ struct BatchView {
     const uint64_t* nam_off = nullptr;
     const NamDetailsRec* details = nullptr;
     bool paired = false;
+    // single-end piecewise extension: chain anchors of NAM t (index into nams) are the
+    // packed keys nam_anc[nam_anc_off[t] .. nam_anc_off[t + 1]), last to first
+    const uint64_t* nam_anc_off = nullptr;
+    const uint64_t* nam_anc = nullptr;
+    uint32_t anc_qbits = 0, anc_pbits = 0;
 };
+
+// Appends the anchors of piecewise jobs (use_ssw == 0) to `anchors` as (query
+// start, reference start) pairs and points the jobs at them; other jobs untouched.
+void attach_piecewise_anchors(const BatchView& bv, ExtJob* jobs, size_t n, std::vector<uint32_t>& anchors);
 
 struct ChunkState {
     uint64_t first = 0, next = 0, end = 0;  // record range [first, end), cursor next

@@ -118,6 +118,8 @@ struct ExtJob {
     uint32_t is_revcomp;  // NAM orientation; for rescue: 1 = align the read's reverse complement
     uint32_t use_ssw;     // extend_seed use_ssw (1 for all paired-end extension)
     uint32_t tag;         // caller bookkeeping
+    uint32_t nam;         // the NAM's index in its read's NAM list (piecewise anchors)
+    uint32_t anc_off, anc_n;  // piecewise: the NAM's anchors in the wave's anchor array
 };
 
 // Result of one job.  CIGAR (=/X/I/D, no soft clips) lives in the cigar arena.

@@ -135,10 +135,6 @@ uint64_t Session::submit(const sa_read_batch* r1, const sa_read_batch* r2) {
     if (!r1) throw Error(SA_ERR_INVALID, "null read batch");
     const bool paired = r2 != nullptr;
     if (paired && r2->n != r1->n) throw Error(SA_ERR_INVALID, "r1 and r2 batches differ in size");
-    if (!paired && mp_.mode == SA_MODE_SAM && !mp_.use_ssw)
-        throw Error(SA_ERR_INVALID,
-                    "single-end SAM output needs use_ssw=1: the piecewise (block-aligner) extension is not "
-                    "implemented on the GPU");
     auto r = std::make_unique<Request>();
     r->paired = paired;
     r->nrec = r1->n;
@@ -355,9 +351,18 @@ void Session::admit(Request& r) {
                          cp_.max_ref_gap, cp_.matches_weight, cp_.max_diagonal_ratio};
     cfg.mcs = mp_.mcs_strategy;
     cfg.rescue_distance = mp_.rescue_distance;
+    cfg.nam_anchors = !r.paired && mp_.mode == SA_MODE_SAM && !mp_.use_ssw;
     run_nam_pipeline(idx_->view(), refs_view_, cfg, n, r.total_bases, max_contig_len_,
                      (uint32_t)refs_->contigs.size(), nws_, sta_);
     const uint64_t tn = nws_.last_total_nams;
+    if (cfg.nam_anchors) {
+        const uint64_t ta = nws_.last_total_nam_anchors;
+        r.nam_anc_off.resize(tn + 1);
+        r.nam_anc.resize(ta);
+        SA_CUDA(cudaMemcpyAsync(r.nam_anc_off.data(), nws_.nam_anc_off.p, (tn + 1) * 8, cudaMemcpyDeviceToHost, sta_));
+        if (ta) SA_CUDA(cudaMemcpyAsync(r.nam_anc.data(), nws_.nam_anc.p, ta * 8, cudaMemcpyDeviceToHost, sta_));
+        r.d2h_bytes += (tn + 1) * 8 + ta * 8;
+    }
     r.nam_off.resize((size_t)n + 1);
     r.nams.resize(tn);
     r.details.resize(n);
@@ -371,6 +376,12 @@ void Session::admit(Request& r) {
     r.bv.nams = r.nams.data();
     r.bv.nam_off = r.nam_off.data();
     r.bv.details = r.details.data();
+    if (cfg.nam_anchors) {
+        r.bv.nam_anc_off = r.nam_anc_off.data();
+        r.bv.nam_anc = r.nam_anc.data();
+        r.bv.anc_qbits = nws_.anchor_qbits;
+        r.bv.anc_pbits = nws_.anchor_pbits;
+    }
     // chunks (src/main.rs:591-604)
     const bool paired = r.paired;
     for (uint64_t i = 0; i < r.nrec;) {
@@ -405,16 +416,21 @@ void Session::run_wave(std::vector<std::pair<Request*, size_t>>& batch) {
     h_jobs_.reserve(nj);
     size_t o = 0;
     Request* last = nullptr;
+    wave_anchors_.clear();
+    uint32_t max_anchors = 0;
     for (auto& b : batch) {
         Request* r = b.first;
         ChunkState& cs = r->chunks[b.second];
         cs.wave_first = o;
         const uint32_t base = (uint32_t)r->read_base;
-        for (const ExtJob& j : cs.pending) {
-            ExtJob g = j;
-            g.read += base;
-            h_jobs_.p[o++] = g;
+        const size_t o0 = o;
+        for (const ExtJob& j : cs.pending) h_jobs_.p[o++] = j;
+        if (r->bv.nam_anc) {
+            // anchors are looked up with the request's own read indices
+            attach_piecewise_anchors(r->bv, h_jobs_.p + o0, o - o0, wave_anchors_);
+            for (size_t x = o0; x < o; x++) max_anchors = std::max(max_anchors, h_jobs_.p[x].anc_n);
         }
+        for (size_t x = o0; x < o; x++) h_jobs_.p[x].read += base;
         r->h2d_bytes += cs.pending.size() * sizeof(ExtJob);
         if (r != last) {
             r->waves++;
@@ -423,9 +439,14 @@ void Session::run_wave(std::vector<std::pair<Request*, size_t>>& batch) {
     }
     ews_.jobs.reserve(nj);
     SA_CUDA(cudaMemcpyAsync(ews_.jobs.p, h_jobs_.p, nj * sizeof(ExtJob), cudaMemcpyHostToDevice, st_));
+    if (!wave_anchors_.empty()) {
+        ews_.anchors.reserve(wave_anchors_.size());
+        SA_CUDA(cudaMemcpyAsync(ews_.anchors.p, wave_anchors_.data(), wave_anchors_.size() * 4,
+                                cudaMemcpyHostToDevice, st_));
+    }
     AlignScores sc{mp_.match, mp_.mismatch, mp_.gap_open, mp_.gap_extend, mp_.end_bonus};
     run_extension_raw(refs_view_, arena_seq_.p, arena_off_.p, nullptr, nullptr, idx_->sp.k, sc, (uint32_t)nj, ews_,
-                      max_qlen, st_);
+                      max_qlen, st_, nullptr, wave_anchors_.empty() ? nullptr : ews_.anchors.p, max_anchors);
     auto w = std::make_shared<WaveResults>();
     w->results.swap(ews_.h_results);
     w->cigar.swap(ews_.h_cigar);
@@ -515,6 +536,8 @@ void Session::complete(Request& r) {
     r.store = ResultStore();
     r.nams = std::vector<NamRec>();
     r.nam_off = std::vector<uint64_t>();
+    r.nam_anc = std::vector<uint64_t>();
+    r.nam_anc_off = std::vector<uint64_t>();
     r.details = std::vector<NamDetailsRec>();
     {
         std::lock_guard<std::mutex> g(mu_);

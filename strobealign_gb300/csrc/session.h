@@ -55,6 +55,7 @@ struct Request {
     std::vector<NamRec> nams;
     std::vector<uint64_t> nam_off;
     std::vector<NamDetailsRec> details;
+    std::vector<uint64_t> nam_anc_off, nam_anc;  // single-end piecewise: NAM chain anchors
     ResultStore store;
     std::vector<ChunkState> chunks;
     std::vector<uint8_t> seeded;
@@ -121,6 +122,7 @@ class Session {
     PinnedBuf<uint8_t> h_seq_;
     PinnedBuf<uint64_t> h_off_;
     PinnedBuf<ExtJob> h_jobs_;
+    std::vector<uint32_t> wave_anchors_;
     // read arena
     DevBuf<uint8_t> arena_seq_;
     DevBuf<uint64_t> arena_off_;

@@ -223,6 +223,13 @@ def test_phix_single_end_ssw_matches_oracle(sa):
     assert got == want
 
 
+def test_phix_single_end_golden(sa):
+    # single-end without --ssw: piecewise extension on the NAM's anchors
+    got = _map_files(sa, str(GOLDEN / "phix.fasta"), [str(GOLDEN / "phix.1.fastq")], eqx=1, chunk_size=3, rg_id="1",
+                     rg=("1", ["SM:sample", "LB:library"]))
+    assert got == (GOLDEN / "phix.se.sam").read_bytes()
+
+
 def test_phix_paf_and_abundance_goldens(sa):
     got = _map_files(sa, str(GOLDEN / "phix.fasta"), [str(GOLDEN / "phix.1.fastq")], mode=sa.MODE_PAF)
     assert b"".join(got.splitlines(keepends=True)[-11:]) == (GOLDEN / "phix.se.paf").read_bytes()
@@ -260,6 +267,14 @@ def test_synthetic_paired_end_small_chunks_matches_oracle(sa, synth):
 def test_synthetic_single_end_ssw_matches_oracle(sa, synth):
     want = run_oracle_cli(["--no-PG", "--eqx", "--ssw", synth["fa"], synth["fse"]])
     got = _map_files(sa, synth["fa"], [synth["fse"]], eqx=1, use_ssw=1)
+    assert got == want, _first_diff(got, want)
+
+
+def test_synthetic_single_end_piecewise_matches_oracle(sa, synth):
+    # piecewise extension (block-aligner in the reference) restated as full affine DPs:
+    # parity with the oracle's restatement, unpinned beyond the reference's goldens
+    want = run_oracle_cli(["--no-PG", "--eqx", synth["fa"], synth["fse"]])
+    got = _map_files(sa, synth["fa"], [synth["fse"]], eqx=1)
     assert got == want, _first_diff(got, want)
 
 

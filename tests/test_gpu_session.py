@@ -47,7 +47,7 @@ def _alone(sa, refs, idx, reqs, **kw):
     return [m.map(x, y) for x, y in reqs]
 
 
-@pytest.mark.parametrize("kw", [dict(use_ssw=1, eqx=1), dict(use_ssw=1, chunk_size=60_000)])
+@pytest.mark.parametrize("kw", [dict(use_ssw=1, eqx=1), dict(use_ssw=1, chunk_size=60_000), dict(eqx=1)])
 def test_session_requests_identical_alone_and_in_the_mix(setup, kw):
     sa, refs, idx, r1, r2 = setup
     reqs = _requests(sa, r1, r2)
