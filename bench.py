@@ -1,19 +1,23 @@
 #!/usr/bin/env python3
-"""Aligned reads/s of strobealign's paired-end mapping path on GB300.
+"""Aligned reads/s of strobealign's mapping path on GB300.
 
-Workload: 50 Mbp synthetic reference in 20 contigs (GC 41%, 10% of it 2 kbp segmental
-copies at 2% divergence), 1M read pairs 2x150 bp, insert N(300, 30), 1% substitutions,
-0.1% indels, 2% of pairs with one mate too mutated to seed (mate rescue).  Seeded
-generators (strobealign_gb300.synthetic) stand in for the reference's read sets.
+Default workload (--workload pe50m): 50 Mbp synthetic reference in 20 contigs (GC 41%,
+10% of it 2 kbp segmental copies at 2% divergence), 1M read pairs 2x150 bp, insert
+N(300, 30), 1% substitutions, 0.1% indels, 2% of pairs with one mate too mutated to
+seed (mate rescue).  Other shapes: se5m (5 Mbp, 100k single-end), uneven200m (200 Mbp
+with repeat families, 2M single-end reads of 50-500 bp), human (3.1 Gbp with 50%
+repeats; --pairs sets the pair count).  Seeded generators (strobealign_gb300.synthetic)
+stand in for the reference's read sets.
 
-One step maps the whole batch: NAM finding, SSW-exact extension waves and SAM record
-formatting, chunked as the reference chunks its input.  `value` is measured with the
-reads already resident in device memory (sa_map_uploaded); `e2e` maps from host
-buffers through sa_map_batch (reads copied to the device, NAMs and alignments copied
-back, SAM bytes returned to the caller).  Index (160 MB) + reads (300 MB) exceed the
-129 MB L2, so no flush is done between steps.
+One step maps the whole batch: NAM finding, SSW-exact (paired-end / --ssw) or piecewise
+(single-end) extension waves and SAM record formatting, chunked as the reference chunks
+its input.  `value` is the plain form with the reads already resident in device memory
+(sa_map_uploaded); `plain.e2e` maps from host buffers through sa_map_batch; `e2e` is the
+served form: the same reads as a stream of requests (log-uniform 1..100k pairs) through
+sa_session submit/wait from host buffers, with continuous batching.  An open-loop pass
+at 70% of the served capacity gives p50/p99 request latency.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload W]
 
 Under torchrun each rank maps its own replica of the workload (no data exchange:
 chunks are independent), and rank 0 prints one JSON line with the aggregate rate
@@ -35,7 +39,19 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "aligned reads/s on 1 GB300 (bit-exact SAM), served vs plain; p50/p99 latency"
-WORKLOAD = "paired-end repetitive: 50 Mbp / 20 contigs, 1M pairs 2x150 bp, insert N(300,30), 1% sub, 0.1% indel"
+
+# Synthetic stand-ins for the reference's benchmark shapes (seeded generators in
+# strobealign_gb300/synthetic.py; genome seeds 1..4, read seeds 101..104).
+WORKLOADS = {
+    "pe50m": "paired-end repetitive: 50 Mbp / 20 contigs (GC 41%, 10% 2 kbp segmental copies at 2%), "
+             "1M pairs 2x150 bp, insert N(300,30), 1% sub, 0.1% indel, 2% of pairs need mate rescue",
+    "se5m": "plain small: 5 Mbp uniform / 1 contig, 100k single-end 150 bp, 1% sub, 0.1% indel",
+    "uneven200m": "uneven lengths: 200 Mbp / 8 contigs (GC 41%, 20% repeats from 300 bp-6 kbp families at "
+                  "10-20% divergence), 2M single-end reads U[50,500] bp, 1.5% sub, 0.2% indel",
+    "human": "human scale: 3.1 Gbp / 24 contigs (GC 41%, 50% interspersed repeats, 3% tandem), "
+             "pairs 2x150 bp, insert N(400,50), 1% sub, 0.1% indel",
+}
+WORKLOAD = WORKLOADS["pe50m"]
 
 
 def parse():
@@ -44,7 +60,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="pe50m", choices=sorted(WORKLOADS))
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload (1.0 = full)")
+    ap.add_argument("--pairs", type=int, default=0, help="override the read (pair) count")
     ap.add_argument("--cpu-sample-pairs", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-served", action="store_true", help="skip the served and latency passes (profiling runs)")
@@ -58,12 +76,29 @@ def dist_info():
     return ws, rank, local
 
 
-def workload(scale: float):
+def workload(scale: float, name: str = "pe50m", pairs: int = 0):
+    """(genome, reads 1, reads 2 or None, read length for the seeding preset)"""
     from strobealign_gb300 import synthetic as syn
+    if name == "se5m":
+        g = syn.make_genome(1, int(5_000_000 * scale), 1, gc=0.5)
+        r = syn.make_single_end(101, g, pairs or int(100_000 * scale), 150, 0.01, 0.001)
+        return g, r, None, 150
+    if name == "uneven200m":
+        g = syn.make_genome(3, int(200_000_000 * scale), 8, gc=0.41, repeat_fraction=0.20, family_len=(300, 6000),
+                            family_div=(0.10, 0.20))
+        r = syn.make_single_end(103, g, pairs or int(2_000_000 * scale), (50, 500), 0.015, 0.002)
+        n = min(500, len(r))
+        return g, r, None, int(r.offsets[n] // n) if n else 150  # read length estimated like the reference
+    if name == "human":
+        g = syn.make_genome(4, int(3_100_000_000 * scale), 24, gc=0.41, repeat_fraction=0.50, family_len=(300, 6000),
+                            family_div=(0.10, 0.20), tandem_fraction=0.03)
+        r1, r2 = syn.make_paired_end(104, g, pairs or int(10_000_000 * scale), 150, 400, 50, 0.01, 0.001)
+        return g, r1, r2, 150
     g = syn.make_genome(2, int(50_000_000 * scale), 20, gc=0.41, segdup_fraction=0.10, segdup_len=2000,
                         segdup_div=0.02)
-    r1, r2 = syn.make_paired_end(102, g, int(1_000_000 * scale), 150, 300, 30, 0.01, 0.001, rescue_fraction=0.02)
-    return g, r1, r2
+    r1, r2 = syn.make_paired_end(102, g, pairs or int(1_000_000 * scale), 150, 300, 30, 0.01, 0.001,
+                                 rescue_fraction=0.02)
+    return g, r1, r2, 150
 
 
 class ClockSampler:
@@ -126,27 +161,30 @@ def cpu_baseline(g, r1, r2, pairs: int, threads: int) -> dict:
     oracle_build.build()
     pairs = min(pairs, len(r1))
     with tempfile.TemporaryDirectory() as d:
-        fa, f1, f2 = os.path.join(d, "ref.fa"), os.path.join(d, "r1.fq"), os.path.join(d, "r2.fq")
+        fa = os.path.join(d, "ref.fa")
         g.write_fasta(fa)
-        for rs, f in ((r1, f1), (r2, f2)):
-            sub = syn.ReadSet(rs.seq[:int(rs.offsets[pairs])], rs.offsets[:pairs + 1], rs.names,
-                              rs.name_offsets[:pairs + 1], rs.qual)
-            sub.write_fastq(f)
+        files = []
+        for i, rs in enumerate(x for x in (r1, r2) if x is not None):
+            f = os.path.join(d, f"r{i + 1}.fq")
+            syn.ReadSet(rs.seq[:int(rs.offsets[pairs])], rs.offsets[:pairs + 1], rs.names,
+                        rs.name_offsets[:pairs + 1], rs.qual).write_fastq(f)
+            files.append(f)
         r = subprocess.run([str(oracle_build.cli_path()), "-t", str(threads), "--timing", "-o", os.path.join(d, "o.sam"),
-                            fa, f1, f2], capture_output=True, text=True, check=True)
+                            fa] + files, capture_output=True, text=True, check=True)
     line = [l for l in r.stderr.splitlines() if l.startswith("oracle_timing")][-1]
     kv = dict(x.split("=") for x in line.split()[1:])
     map_s = float(kv["map_s"])
-    return {"value": 2 * pairs / map_s, "unit": "reads/s", "cores": threads, "kind": "port",
-            "sample": f"{pairs} pairs of the same workload, index build excluded ({float(kv['index_s']):.1f} s)",
-            "seconds": map_s}
+    reads = pairs * len(files)
+    return {"value": reads / map_s, "unit": "reads/s", "cores": threads, "kind": "port",
+            "sample": f"{pairs} {'pairs' if len(files) == 2 else 'reads'} of the same workload, index build excluded "
+                      f"({float(kv['index_s']):.1f} s)", "seconds": map_s}
 
 
 def run_reference(args, ws, rank):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    g, r1, r2 = workload(args.scale)
+    g, r1, r2, _ = workload(args.scale, args.workload, args.pairs)
     for _ in range(args.warmup):
         cpu_baseline(g, r1, r2, min(2000, args.cpu_sample_pairs), threads)
     vals, secs = [], []
@@ -159,7 +197,8 @@ def run_reference(args, ws, rank):
            "warmup": args.warmup, "ms_per_step": 1000 * statistics.median(secs), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
            "impl": "reference",
-           "config": {"workload": WORKLOAD, "scale": args.scale, "sample_pairs": args.cpu_sample_pairs},
+           "config": {"workload": WORKLOADS[args.workload], "scale": args.scale,
+                      "sample_pairs": args.cpu_sample_pairs},
            "cpu_baseline": {"value": value, "unit": "reads/s", "cores": threads, "kind": "port",
                             "sample": f"{args.cpu_sample_pairs} pairs per step; the Rust reference cannot be built "
                                       "(no cargo); the oracle restates its CPU path"},
@@ -253,16 +292,16 @@ def main():
         pg = dist
     import strobealign_gb300 as sa
 
-    g, r1, r2 = workload(args.scale)
+    g, r1, r2, read_length = workload(args.scale, args.workload, args.pairs)
     refs = sa.References.from_sequences(g.names, [s.tobytes() for s in g.seqs])
-    params = sa.SeedingParameters.from_read_length(150)
+    params = sa.SeedingParameters.from_read_length(read_length)
     t = time.time()
     index = sa.StrobemerIndex.build(refs, params)
     torch.cuda.synchronize()
     index_s = time.time() - t
     R1 = sa.Reads.from_arrays(r1.seq, r1.offsets, r1.names, r1.name_offsets, r1.qual)
-    R2 = sa.Reads.from_arrays(r2.seq, r2.offsets, r2.names, r2.name_offsets, r2.qual)
-    n_reads = 2 * len(R1)
+    R2 = sa.Reads.from_arrays(r2.seq, r2.offsets, r2.names, r2.name_offsets, r2.qual) if r2 is not None else None
+    n_reads = (2 if r2 is not None else 1) * len(R1)
     mapper = sa.Mapper(index, refs)
     mapper.upload(R1, R2)
 
@@ -277,6 +316,7 @@ def main():
     mapper.set_profiling(True)
     kern = {}
     cells = {}
+    phases = {}
     launches = 0
     barrier()
     stream = torch.cuda.current_stream()
@@ -288,6 +328,8 @@ def main():
             out = mapper.map_uploaded(copy=False)
             st = mapper.stats()
             launches += int(st["n_launches"])
+            for k in ("seconds_nams", "seconds_extension", "seconds_policy"):
+                phases[k] = phases.get(k, 0.0) + st[k] / args.steps
             for k, v in st["sw_cells"].items():
                 cells[k] = cells.get(k, 0) + int(v)
             for k, v in st["kernel_ms"].items():
@@ -324,7 +366,7 @@ def main():
         sizes = request_sizes(len(R1))
         a = 0
         for n in sizes:
-            reqs.append((slice_reads(sa, r1, a, a + n), slice_reads(sa, r2, a, a + n)))
+            reqs.append((slice_reads(sa, r1, a, a + n), slice_reads(sa, r2, a, a + n) if r2 is not None else None))
             a += n
         session = sa.Session(index, refs)
         served_pass(session, reqs)  # warm-up: arena, workspaces
@@ -352,7 +394,8 @@ def main():
     total_ms = sum(v[0] for v in kern.values())
     dom = max(kern, key=lambda k: kern[k][0]) if kern else None
     shares = {k: round(v[0] / total_ms, 4) for k, v in kern.items() if total_ms and v[0] > 0}
-    roofline = roofline_for(dom, kern, cells, peaks, clk.summary()) if dom else None
+    counts = {k: int(st[k]) for k in ("n_bases", "n_randstrobes", "n_anchor_total")}
+    roofline, rooflines = roofline_for(dom, kern, cells, peaks, clk.summary(), counts, args.steps) if dom else (None, {})
     cpu = None
     if not args.no_cpu_baseline:
         try:
@@ -363,8 +406,10 @@ def main():
         "metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": ws, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": 1000 * elapsed / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "scale": args.scale, "reads_per_step": n_reads,
-                   "l2": "no flush: index 160 MB + reads 300 MB exceed the 129 MB L2",
+        "config": {"workload": WORKLOADS[args.workload], "scale": args.scale, "reads_per_step": n_reads,
+                   "l2": f"no flush: index {index.info.device_bytes / 1e6:.0f} MB + reads "
+                         f"{int(R1.seq_offsets[-1]) * (2 if R2 is not None else 1) / 1e6:.0f} MB "
+                         f"({'exceed' if index.info.device_bytes > 129e6 else 'with the reads exceed'} the 129 MB L2)",
                    "value_form": "plain: the whole batch through sa_map_uploaded, reads resident on the device",
                    "e2e_form": "served: the same pairs as requests of log-uniform 1..100k pairs through "
                                "sa_session submit/wait from host buffers, continuous batching",
@@ -377,7 +422,11 @@ def main():
                                                "vs_plain_e2e": served / plain_e2e, "latency_open_loop": lat},
         "gpu_launches": launches,
         "stage_share": shares,
+        # wall seconds per step: NAM pipeline (GPU), extension waves (GPU, incl. job
+        # upload and result download), host policy between and after waves
+        "phases_s": {k.replace("seconds_", ""): round(v, 4) for k, v in phases.items()},
         "roofline": roofline,
+        "rooflines": rooflines,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
     }
@@ -386,33 +435,62 @@ def main():
         pg.destroy_process_group()
 
 
-def roofline_for(dom, kern, cells, peaks, clocks) -> dict:
-    """achieved/peak of the dominant stage.
+# Algorithmic (compulsory) bytes per unit of the NAM stages: what the reference's
+# algorithm must read or write at least once, whatever the implementation.
+ALGO_BYTES = {
+    # read bases in; per randstrobe out: hash, reverse-complement hash, start, end
+    "seed": lambda c: c["n_bases"] + 24 * c["n_randstrobes"],
+    # per randstrobe probe: the bucket-directory pair (16 B) and one 32-byte table sector,
+    # and the hit record out (position, info, count: 16 B)
+    "hits": lambda c: 64 * c["n_randstrobes"],
+    # per anchor: the 16-byte table entry read and the 8-byte anchor key written
+    "anchors": lambda c: 24 * c["n_anchor_total"],
+    # per anchor key: read and write once
+    "sort": lambda c: 16 * c["n_anchor_total"],
+    # per anchor: key in, score and predecessor out
+    "chain": lambda c: 16 * c["n_anchor_total"],
+}
 
-    Extension (the striped SSW kernel k_sw: forward byte pass, word reruns of the
-    byte overflows, reverse passes) is integer-ALU bound.  Its algorithmic unit is
-    one SSW call with |query| x |reference window| cells (canonical cells, counted
-    once per call); achieved = canonical cells / device time of all k_sw launches,
-    against 152 SMs x 128 INT32 lanes x SM clock / 11 ops per cell.  The cells the
-    passes actually computed are reported beside it.  Other stages: HBM bound,
-    achieved not derived here."""
+
+def roofline_for(dom, kern, cells, peaks, clocks, counts, steps) -> dict:
+    """Roofline of every timed stage, and of the dominant one.
+
+    NAM stages are framed against HBM bandwidth with their algorithmic bytes per
+    launch (ALGO_BYTES, from the batch's counts).  Extension (the SSW kernel k_sw:
+    byte pass, word reruns of the byte overflows, reverse passes) is integer-ALU bound:
+    its unit is one SSW call of |query| x |reference window| canonical cells, against
+    152 SMs x 128 INT32 lanes x SM clock / 11 ops per cell; the cells the passes
+    actually computed are reported beside it."""
     hbm = peaks.get("hbm_gbs", 6800.0)
-    if dom in ("sw_byte", "sw_word"):
+    out = {}
+    for st, f in ALGO_BYTES.items():
+        if st not in kern or not kern[st][1]:
+            continue
+        ms, n = kern[st]
+        sec = ms / 1000.0
+        per_launch = f(counts) * steps / n
+        achieved = per_launch * n / sec / 1e9
+        out[st] = {"kernel": st, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                   "frac": achieved / hbm, "traffic": None, "avg_launch_ms": ms / n, "launches": n,
+                   "algorithmic_bytes_per_launch": per_launch}
+    if kern.get("sw_byte", [0, 0])[1]:
         ms = kern.get("sw_byte", [0.0, 0])[0] + kern.get("sw_word", [0.0, 0])[0]
         n = kern.get("sw_byte", [0.0, 0])[1] + kern.get("sw_word", [0.0, 0])[1]
         sec = ms / 1000.0
         clock = (clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)) * 1e6
         peak_gcups = 152 * 128 * clock / 11 / 1e9
-        achieved = cells.get("canonical", 0) / sec / 1e9
+        achieved = cells.get("canonical", 0) / sec / 1e9 if sec else 0.0
         computed = sum(v for k, v in cells.items() if k != "canonical")
-        return {"kernel": "k_sw (byte, word, reverse passes)", "bound": "int32", "achieved": achieved,
-                "peak": peak_gcups, "unit": "GCUPS", "frac": achieved / peak_gcups, "traffic": None,
-                "avg_launch_ms": ms / max(n, 1), "launches": n,
-                "computed_gcups": computed / sec / 1e9, "cells": cells,
-                "peak_source": "152 SMs x 128 INT32 lanes x median SM clock under load / 11 ops per cell"}
-    ms, n = kern[dom]
-    return {"kernel": dom, "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None,
-            "traffic": None, "avg_launch_ms": ms / max(n, 1)}
+        out["sw"] = {"kernel": "k_ssw (byte, word, reverse passes)", "bound": "int32", "achieved": achieved,
+                     "peak": peak_gcups, "unit": "GCUPS", "frac": achieved / peak_gcups, "traffic": None,
+                     "avg_launch_ms": ms / max(n, 1), "launches": n,
+                     "computed_gcups": computed / sec / 1e9 if sec else 0.0, "cells": cells,
+                     "peak_source": "152 SMs x 128 INT32 lanes x median SM clock under load / 11 ops per cell"}
+    key = "sw" if dom in ("sw_byte", "sw_word") else dom
+    head = dict(out.get(key) or {"kernel": dom, "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s",
+                                 "frac": None, "traffic": None})
+    head["stage"] = dom
+    return head, out
 
 
 if __name__ == "__main__":

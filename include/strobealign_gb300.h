@@ -346,6 +346,9 @@ typedef struct {
      * computed (up to an early stop): forward byte, forward word (byte overflow
      * reruns), reverse byte, reverse word */
     uint64_t sw_cells[5];
+    /* work counts of the NAM stages: read bases, randstrobes (both orientations; one
+     * index probe each), anchors */
+    uint64_t n_bases, n_randstrobes, n_anchor_total;
 } sa_mapper_stats;
 int32_t sa_mapper_get_stats(const sa_mapper* m, sa_mapper_stats* out);
 /* Record CUDA events around each stage's launches (off by default). */

@@ -114,4 +114,110 @@ __device__ __forceinline__ uint32_t idx_count_full(const DevIndex& ix, uint64_t 
     return r + idx_get_count(ix, pos, HASH_MASK);
 }
 
+// ------------------------------------------------------------------ latency-parallel probes
+// The same answers as idx_full_forward / idx_too_frequent above, with the dependent
+// memory rounds cut down: both orientations' lookups proceed side by side, a bucket of
+// up to 8 entries is scanned with independent loads instead of a binary search (the
+// lower bound is the number of smaller keys), larger buckets narrow 8-ary, and the
+// repeat test loads the entries at pos + cutoff and pos + 1 of both hits at once.
+
+// bucket range [ps, pe) of a full hash (same directory reads as idx_get_masked_from)
+__device__ __forceinline__ void idx_bucket(const DevIndex& ix, uint64_t hash, uint64_t& ps, uint64_t& pe) {
+    const uint64_t top = hash >> (64 - ix.bits);
+    if ((top & 1) == 0) {
+        ulonglong2 b = __ldg(reinterpret_cast<const ulonglong2*>(ix.buckets + top));
+        ps = b.x;
+        pe = b.y;
+    } else {
+        ps = __ldg(reinterpret_cast<const unsigned long long*>(ix.buckets) + top);
+        pe = __ldg(reinterpret_cast<const unsigned long long*>(ix.buckets) + top + 1);
+    }
+}
+
+// narrow [lo, hi) to at most 8 entries around the lower bound of key, 8-ary
+__device__ __forceinline__ void idx_narrow(const DevIndex& ix, uint64_t key, uint64_t& lo, uint64_t& hi) {
+    while (hi - lo > 8) {
+        const uint64_t len = hi - lo;
+        uint64_t piv[7];
+        uint64_t hv[7];
+#pragma unroll
+        for (int t = 0; t < 7; t++) {
+            piv[t] = lo + len * (uint64_t)(t + 1) / 8;
+            hv[t] = load_hash(ix.rs, piv[t]);
+        }
+        uint64_t nlo = lo, nhi = hi;
+#pragma unroll
+        for (int t = 0; t < 7; t++) {
+            if (hv[t] < key) nlo = piv[t] + 1;
+        }
+#pragma unroll
+        for (int t = 6; t >= 0; t--) {
+            if (hv[t] >= key) nhi = piv[t];
+        }
+        // the lower bound lies in [nlo, nhi]; keep one entry past the range so that an
+        // equal key at nhi is seen
+        lo = nlo;
+        hi = nhi < hi ? nhi + 1 : hi;
+    }
+}
+
+// lower bound of key in [lo, hi) (hi - lo <= 8) and whether the key is present
+__device__ __forceinline__ uint64_t idx_scan8(const DevIndex& ix, uint64_t key, uint64_t lo, uint64_t hi) {
+    const uint32_t len = (uint32_t)(hi - lo);
+    uint64_t hv[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) hv[t] = (uint32_t)t < len ? load_hash(ix.rs, lo + t) : UINT64_MAX;
+    uint32_t lt = 0;
+    bool eq = false;
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        lt += hv[t] < key;
+        eq |= (uint32_t)t < len && hv[t] == key;
+    }
+    return eq ? lo + lt : UINT64_MAX;
+}
+
+// count of the run of hash at pos (get_count with the full mask), given the bucket
+// end and the preloaded hash at pos + 1
+__device__ __forceinline__ uint32_t idx_count_at(const DevIndex& ix, uint64_t pos, uint64_t bucket_end,
+                                                 uint64_t h_pos, uint64_t h_next) {
+    if (pos + 1 >= bucket_end || h_next != h_pos) return 1;
+    return idx_get_count(ix, pos, HASH_MASK);
+}
+
+// full lookup of h (forward) with is_too_frequent (src/index.rs:309-323) using the
+// reverse-complement hash hrc; pos = UINT64_MAX when absent
+__device__ __forceinline__ void idx_full_probe(const DevIndex& ix, uint64_t h, uint64_t hrc, uint32_t cutoff,
+                                               uint64_t& pos, bool& filtered) {
+    const uint64_t ka = h & HASH_MASK, kb = hrc & HASH_MASK;
+    uint64_t sa, ea, sb, eb;
+    idx_bucket(ix, h, sa, ea);
+    idx_bucket(ix, hrc, sb, eb);
+    filtered = false;
+    uint64_t la = sa, ha = sa < ea ? ea : sa, lb = sb, hb = sb < eb ? eb : sb;
+    if (ha - la > 8) idx_narrow(ix, ka, la, ha);
+    if (hb - lb > 8) idx_narrow(ix, kb, lb, hb);
+    const uint64_t pa = idx_scan8(ix, ka, la, ha);
+    pos = pa;
+    if (pa == UINT64_MAX) return;
+    const uint64_t pb = idx_scan8(ix, kb, lb, hb);
+    // everything the repeat test can read, at once
+    const bool ga = pa + ix.filter_cutoff < ix.n, gb = pb != UINT64_MAX && pb + ix.filter_cutoff < ix.n;
+    const uint64_t a_cut = ga ? load_hash(ix.rs, pa + cutoff) : 0;
+    const uint64_t a_next = pa + 1 < ix.n ? load_hash(ix.rs, pa + 1) : 0;
+    const uint64_t b_cut = gb ? load_hash(ix.rs, pb + cutoff) : 0;
+    const uint64_t b_next = pb != UINT64_MAX && pb + 1 < ix.n ? load_hash(ix.rs, pb + 1) : 0;
+    if (ga && a_cut == ka) {
+        filtered = true;
+        return;
+    }
+    if (pb == UINT64_MAX) return;
+    if (gb && b_cut == kb) {
+        filtered = true;
+        return;
+    }
+    const uint64_t c = (uint64_t)idx_count_at(ix, pa, ea, ka, a_next) + idx_count_at(ix, pb, eb, kb, b_next);
+    filtered = c > cutoff;
+}
+
 }  // namespace sa

@@ -99,26 +99,34 @@ void Mapper::nams_for_reads(uint32_t& launches) {
     cfg.mcs = mp_.mcs_strategy;
     cfg.rescue_distance = mp_.rescue_distance;
     cfg.nam_anchors = single_end_piecewise_ && !bv_.paired;
+    const auto t0 = std::chrono::steady_clock::now();
     launches += run_nam_pipeline(idx_->view(), refs_view_, cfg, n_reads_, total_bases_, max_contig_len_,
                                  (uint32_t)refs_->contigs.size(), nws_, st_, &kt_);
+    const auto t1 = std::chrono::steady_clock::now();
     const uint64_t tn = nws_.last_total_nams;
     if (cfg.nam_anchors) {
         const uint64_t ta = nws_.last_total_nam_anchors;
-        h_nam_anc_off_.resize(tn + 1);
-        h_nam_anc_.resize(ta);
-        SA_CUDA(cudaMemcpyAsync(h_nam_anc_off_.data(), nws_.nam_anc_off.p, (tn + 1) * 8, cudaMemcpyDeviceToHost, st_));
-        if (ta) SA_CUDA(cudaMemcpyAsync(h_nam_anc_.data(), nws_.nam_anc.p, ta * 8, cudaMemcpyDeviceToHost, st_));
+        h_nam_anc_off_.reserve(tn + 1);
+        h_nam_anc_.reserve(ta);
+        SA_CUDA(cudaMemcpyAsync(h_nam_anc_off_.p, nws_.nam_anc_off.p, (tn + 1) * 8, cudaMemcpyDeviceToHost, st_));
+        if (ta) SA_CUDA(cudaMemcpyAsync(h_nam_anc_.p, nws_.nam_anc.p, ta * 8, cudaMemcpyDeviceToHost, st_));
         d2h_bytes_ += (tn + 1) * 8 + ta * 8;
     }
-    h_nam_off_.resize((size_t)n_reads_ + 1);
-    h_nams_.resize(tn);
-    h_details_.resize(n_reads_);
-    SA_CUDA(cudaMemcpyAsync(h_nam_off_.data(), nws_.nam_off.p, ((size_t)n_reads_ + 1) * 8, cudaMemcpyDeviceToHost, st_));
-    if (tn) SA_CUDA(cudaMemcpyAsync(h_nams_.data(), nws_.nams.p, tn * sizeof(NamRec), cudaMemcpyDeviceToHost, st_));
-    SA_CUDA(cudaMemcpyAsync(h_details_.data(), nws_.details.p, (size_t)n_reads_ * sizeof(NamDetailsRec),
+    h_nam_off_.reserve((size_t)n_reads_ + 1);
+    h_nams_.reserve(tn);
+    h_details_.reserve(n_reads_);
+    n_host_nams_ = tn;
+    SA_CUDA(cudaMemcpyAsync(h_nam_off_.p, nws_.nam_off.p, ((size_t)n_reads_ + 1) * 8, cudaMemcpyDeviceToHost, st_));
+    if (tn) SA_CUDA(cudaMemcpyAsync(h_nams_.p, nws_.nams.p, tn * sizeof(NamRec), cudaMemcpyDeviceToHost, st_));
+    SA_CUDA(cudaMemcpyAsync(h_details_.p, nws_.details.p, (size_t)n_reads_ * sizeof(NamDetailsRec),
                             cudaMemcpyDeviceToHost, st_));
     SA_CUDA(cudaStreamSynchronize(st_));
     d2h_bytes_ += ((size_t)n_reads_ + 1) * 8 + tn * sizeof(NamRec) + (size_t)n_reads_ * sizeof(NamDetailsRec);
+    if (trace_) {
+        const auto t2 = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "sa_nams reads=%u nams=%llu pipeline=%.4f copy=%.4f\n", n_reads_, (unsigned long long)tn,
+                     std::chrono::duration<double>(t1 - t0).count(), std::chrono::duration<double>(t2 - t1).count());
+    }
 }
 
 std::shared_ptr<const WaveResults> Mapper::run_wave(const ExtJob* jobs, uint32_t nj, uint32_t max_qlen,
@@ -353,12 +361,12 @@ void Mapper::map_uploaded(sa_output* out) {
     for (int c = 0; c < 5; c++) sw_cells_[c] = 0;
     nams_for_reads(launches);
     auto t1 = std::chrono::steady_clock::now();
-    bv.nams = h_nams_.data();
-    bv.nam_off = h_nam_off_.data();
-    bv.details = h_details_.data();
+    bv.nams = h_nams_.p;
+    bv.nam_off = h_nam_off_.p;
+    bv.details = h_details_.p;
     const bool piecewise = single_end_piecewise_ && !paired;
-    bv.nam_anc_off = piecewise ? h_nam_anc_off_.data() : nullptr;
-    bv.nam_anc = piecewise ? h_nam_anc_.data() : nullptr;
+    bv.nam_anc_off = piecewise ? h_nam_anc_off_.p : nullptr;
+    bv.nam_anc = piecewise ? h_nam_anc_.p : nullptr;
     bv.anc_qbits = nws_.anchor_qbits;
     bv.anc_pbits = nws_.anchor_pbits;
     // chunks (src/main.rs:591-604)
@@ -377,13 +385,16 @@ void Mapper::map_uploaded(sa_output* out) {
         i = j;
     }
     ResultStore store;
-    store.per_read.resize(bv.reads.size());
+    store.reset(bv.reads.size());
     const uint32_t waves = schedule(chunks, store, launches);
     if (trace_) {
-        double sr = 0, ss = 0, sd = 0;
-        uint64_t er = 0, es = 0, runs = 0, eu = 0;
+        double sr = 0, ss = 0, sd = 0, sf = 0;
+        uint64_t er = 0, es = 0, runs = 0, eu = 0, mm = 0, mk = 0;
         for (auto& c : chunks) {
             eu += c.evals_reused;
+            mm += c.miss_mispredicted;
+            mk += c.miss_unknown;
+            sf += c.seconds_format;
             sr += c.seconds_real;
             ss += c.seconds_spec;
             sd += c.seconds_seed;
@@ -391,10 +402,10 @@ void Mapper::map_uploaded(sa_output* out) {
             es += c.evals_spec;
             runs += c.runs;
         }
-        std::fprintf(stderr, "sa_policy chunks=%zu runs=%llu cpu_real=%.3f cpu_spec=%.3f cpu_seed=%.3f evals_real=%llu "
-                             "evals_spec=%llu reused=%llu\n",
-                     chunks.size(), (unsigned long long)runs, sr, ss, sd, (unsigned long long)er,
-                     (unsigned long long)es, (unsigned long long)eu);
+        std::fprintf(stderr, "sa_policy chunks=%zu runs=%llu cpu_real=%.3f cpu_spec=%.3f cpu_seed=%.3f cpu_format=%.3f "
+                             "evals_real=%llu evals_spec=%llu reused=%llu miss_mispredicted=%llu miss_unknown=%llu\n",
+                     chunks.size(), (unsigned long long)runs, sr, ss, sd, sf, (unsigned long long)er,
+                     (unsigned long long)es, (unsigned long long)eu, (unsigned long long)mm, (unsigned long long)mk);
     }
     for (auto& c : chunks)
         for (auto& a : c.abundance) abundances_[a.first] += a.second;
@@ -431,8 +442,18 @@ void Mapper::map_uploaded(sa_output* out) {
     stats_.n_launches = launches;
     stats_.h2d_bytes = h2d_bytes_;
     stats_.d2h_bytes = d2h_bytes_;
-    stats_.n_nams = h_nams_.size();
-    stats_.n_anchors = 0;
+    stats_.n_nams = n_host_nams_;
+    {
+        uint64_t rs = 0, an = 0;
+        for (uint32_t i = 0; i < n_reads_; i++) {
+            rs += h_details_.p[i].n_randstrobes;
+            an += h_details_.p[i].n_anchors;
+        }
+        stats_.n_anchors = an;
+        stats_.n_anchor_total = an;
+        stats_.n_randstrobes = rs;
+        stats_.n_bases = total_bases_;
+    }
     kt_.collect();
     for (int c = 0; c < 5; c++) stats_.sw_cells[c] = sw_cells_[c];
     for (int i = 0; i < 16; i++) {

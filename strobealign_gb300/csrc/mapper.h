@@ -28,9 +28,6 @@ class Mapper {
     void nams_for_reads(uint32_t& launches);
     uint32_t n_reads() const { return n_reads_; }
     uint64_t total_bases() const { return total_bases_; }
-    const std::vector<NamRec>& host_nams() const { return h_nams_; }
-    const std::vector<uint64_t>& host_nam_off() const { return h_nam_off_; }
-    const std::vector<NamDetailsRec>& host_details() const { return h_details_; }
     uint64_t h2d_bytes() const { return h2d_bytes_; }
     uint64_t d2h_bytes() const { return d2h_bytes_; }
     uint32_t last_launches() const { return last_launches_; }
@@ -75,10 +72,12 @@ class Mapper {
     PinnedBuf<uint8_t> h_seq_;
     PinnedBuf<uint64_t> h_off_;
     PinnedBuf<ExtJob> h_jobs_;
-    std::vector<uint64_t> h_nam_off_;
-    std::vector<NamRec> h_nams_;
-    std::vector<NamDetailsRec> h_details_;
-    std::vector<uint64_t> h_nam_anc_off_, h_nam_anc_;  // single-end piecewise: NAM chain anchors
+    // per-read NAMs and statistics of the current batch, pinned for the copy back
+    PinnedBuf<uint64_t> h_nam_off_;
+    PinnedBuf<NamRec> h_nams_;
+    PinnedBuf<NamDetailsRec> h_details_;
+    uint64_t n_host_nams_ = 0;
+    PinnedBuf<uint64_t> h_nam_anc_off_, h_nam_anc_;  // single-end piecewise: NAM chain anchors
     std::vector<uint32_t> wave_anchors_;
     uint32_t n_reads_ = 0;
     uint64_t total_bases_ = 0;

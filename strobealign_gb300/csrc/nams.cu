@@ -11,7 +11,8 @@
 //                   reference's early-break rules evaluated as a warp prefix-max, chain
 //                   extraction (src/chainer.rs:85-180, 386-449)
 //   k_nam_compact   warp per read: NAM ids in push order, stable sort by score
-//                   (src/nam.rs:168-170)
+//                   (src/nam.rs:168-170); reads with more than 32 NAMs through a
+//                   segmented stable sort and k_nam_gather
 //
 // Floating point follows the reference exactly: f32 with explicit round-to-nearest
 // intrinsics (no contraction) and log2(d + 1) from a table built with the host's
@@ -230,8 +231,47 @@ __device__ uint32_t warp_rescue_least_frequent(const DevIndex& ix, uint32_t s, u
     return __shfl_sync(FULL, rescued, 0);
 }
 
+// Per-randstrobe index probes of find_hits' first pass (src/hit.rs:143-187), ahead of
+// k_hits: lanes run over both orientations' randstrobes of a read together, each lane
+// one probe with the latency-parallel lookups.  Writes, per randstrobe slot, the table
+// position (UINT64_MAX if absent) and PROBE_* flags; k_hits compacts them in place.
+constexpr uint32_t PROBE_FULL = 1, PROBE_PARTIAL = 2, PROBE_FILTERED = 4;
+
+__global__ void __launch_bounds__(256) k_probe(DevIndex ix, const uint64_t* __restrict__ off, uint32_t n,
+                                               uint64_t total, uint32_t mcs, const uint64_t* __restrict__ qr_hash,
+                                               const uint64_t* __restrict__ qr_hash_rc,
+                                               const uint32_t* __restrict__ n_rs, uint64_t* __restrict__ hit_pos,
+                                               uint32_t* __restrict__ hit_info) {
+    const uint32_t lane = lane_id();
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
+    const uint32_t cutoff = ix.filter_cutoff;
+    for (uint32_t r = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; r < n; r += nwarps) {
+        const uint64_t o = off[r];
+        const uint32_t n0 = n_rs[2 * r], n1 = n_rs[2 * r + 1];
+        for (uint32_t j = lane; j < n0 + n1; j += 32) {
+            const uint32_t ori = j >= n0;
+            const uint64_t slot = ori * total + o + (j - ori * n0);
+            const uint64_t h = qr_hash[slot];
+            uint64_t pos;
+            bool filtered;
+            idx_full_probe(ix, h, qr_hash_rc[slot], cutoff, pos, filtered);
+            uint32_t flags = 0;
+            if (pos != UINT64_MAX) {
+                flags = PROBE_FULL | (filtered ? PROBE_FILTERED : 0u);
+            } else if (mcs == SA_MCS_ALWAYS) {
+                pos = idx_get_masked_from(ix, h, ix.p.main_mask, false, 0);
+                if (pos != UINT64_MAX)
+                    flags = PROBE_PARTIAL | (idx_too_frequent_partial(ix, pos, cutoff) ? PROBE_FILTERED : 0u);
+            }
+            hit_pos[slot] = pos;
+            hit_info[slot] = flags;
+        }
+    }
+}
+
 // find_hits (src/hit.rs:129-333) for both orientations of each read, then the
-// orientation heuristic (src/chainer.rs:205-216, src/hit.rs:76-81).
+// orientation heuristic (src/chainer.rs:205-216, src/hit.rs:76-81).  The first pass
+// reads k_probe's per-slot answers.
 __global__ void __launch_bounds__(256) k_hits(DevIndex ix, const uint64_t* __restrict__ off, uint32_t n,
                                               uint64_t total, uint32_t mcs, uint32_t rescue_distance,
                                               const uint64_t* qr_hash, const uint64_t* qr_hash_rc,
@@ -251,27 +291,27 @@ __global__ void __launch_bounds__(256) k_hits(DevIndex ix, const uint64_t* __res
             uint32_t nh = 0;
             uint32_t fnf = 0, ff = 0, ffound = 0, pnf = 0, pf = 0, pfound = 0;
             const bool do_full = mcs != SA_MCS_FIRST_STROBE;
-            // pass 1: full lookups (with partial fallback under MCS always)
+            // pass 1: full lookups (with partial fallback under MCS always), probed by
+            // k_probe; compacted in place (a slot is written only after every lane of
+            // the round has read its own)
             if (do_full) {
                 for (uint32_t c = 0; c < nr; c += 32) {
                     uint32_t i = c + lane;
                     bool is_hit = false, partial = false, filtered = false;
                     uint64_t pos = UINT64_MAX;
                     if (i < nr) {
-                        uint64_t h = qr_hash[b + i];
-                        pos = idx_full_forward(ix, h);
-                        if (pos != UINT64_MAX) {
+                        const uint32_t fl = hit_info[b + i];
+                        pos = hit_pos[b + i];
+                        filtered = fl & PROBE_FILTERED;
+                        if (fl & PROBE_FULL) {
                             is_hit = true;
-                            filtered = idx_too_frequent(ix, pos, cutoff, qr_hash_rc[b + i]);
                             if (filtered) ff++;
                             else ffound++;
                         } else {
                             fnf++;
                             if (mcs == SA_MCS_ALWAYS) {
-                                pos = idx_get_masked_from(ix, h, ix.p.main_mask, false, 0);
-                                if (pos != UINT64_MAX) {
+                                if (fl & PROBE_PARTIAL) {
                                     is_hit = partial = true;
-                                    filtered = idx_too_frequent_partial(ix, pos, cutoff);
                                     if (filtered) pf++;
                                     else pfound++;
                                 } else {
@@ -281,6 +321,7 @@ __global__ void __launch_bounds__(256) k_hits(DevIndex ix, const uint64_t* __res
                         }
                     }
                     uint32_t bal = __ballot_sync(FULL, is_hit);
+                    __syncwarp();
                     if (is_hit) {
                         uint32_t idx = nh + __popc(bal & lanemask_lt());
                         hit_pos[b + idx] = pos;
@@ -732,11 +773,29 @@ __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off,
 
 // NAM ids in push order (forward chains first), then a stable sort by score,
 // descending (src/nam.rs:168-170; the tie shuffle is applied by the host policy)
+// Order-preserving u32 key of a NAM score; -0 and +0 map to one key, as they compare
+// equal in the reference's sort.
+__device__ __forceinline__ uint32_t score_key(float s) {
+    const uint32_t b = __float_as_uint(s == 0.0f ? 0.0f : s);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+__device__ __forceinline__ uint64_t nam_anchor_src(const uint64_t* anc_start, const uint64_t* seg_off, uint32_t r,
+                                                   uint32_t c0, uint32_t t) {
+    return t < c0 ? anc_start[seg_off[2 * r] + t] : anc_start[seg_off[2 * r + 1] + t - c0];
+}
+
+// NAM ids in push order (forward chains, then reverse) and the stable sort by score,
+// descending (src/nam.rs:168-170), warp per read.  Up to 32 NAMs: ranks from the
+// warp's scores by shuffles.  More: the NAMs go to tmp in push order with sort keys,
+// and the read is listed for the segmented stable sort and k_nam_gather.
 __global__ void __launch_bounds__(256) k_nam_compact(uint32_t n, const uint64_t* seg_off, const NamRec* scratch,
                                                      const uint32_t* nam_seg_count, const uint64_t* nam_off,
                                                      NamRec* out, NamDetailsRec* details,
                                                      const uint64_t* anc_start, uint64_t* anc_src,
-                                                     uint64_t* anc_count) {
+                                                     uint64_t* anc_count, NamRec* tmp, uint32_t* keys,
+                                                     uint32_t* vals, uint32_t* long_reads, uint64_t* long_begin,
+                                                     uint64_t* long_end, uint32_t* n_long) {
     const uint32_t lane = lane_id();
     const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
     for (uint32_t r = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; r < n; r += nwarps) {
@@ -744,22 +803,66 @@ __global__ void __launch_bounds__(256) k_nam_compact(uint32_t n, const uint64_t*
         const NamRec* s0 = scratch + seg_off[2 * r];
         const NamRec* s1 = scratch + seg_off[2 * r + 1];
         const uint64_t ob = nam_off[r];
-        for (uint32_t t = lane; t < c; t += 32) {
-            NamRec nr = t < c0 ? s0[t] : s1[t - c0];
-            float s = nr.score;
+        if (lane == 0) details[r].n_nams = c;
+        if (c <= 32) {
+            NamRec nr{};
+            float s = 0.0f;
+            if (lane < c) {
+                nr = lane < c0 ? s0[lane] : s1[lane - c0];
+                s = nr.score;
+            }
             uint32_t rank = 0;
             for (uint32_t u = 0; u < c; u++) {
-                float su = u < c0 ? s0[u].score : s1[u - c0].score;
-                rank += (su > s) || (su == s && u < t);
+                const float su = __shfl_sync(FULL, s, u);
+                rank += (su > s) || (su == s && u < lane);
             }
-            nr.nam_id = t;
-            out[ob + rank] = nr;
-            if (anc_src) {
-                anc_src[ob + rank] = t < c0 ? anc_start[seg_off[2 * r] + t] : anc_start[seg_off[2 * r + 1] + t - c0];
-                anc_count[ob + rank] = nr.n_anchors;
+            if (lane < c) {
+                nr.nam_id = lane;
+                out[ob + rank] = nr;
+                if (anc_src) {
+                    anc_src[ob + rank] = nam_anchor_src(anc_start, seg_off, r, c0, lane);
+                    anc_count[ob + rank] = nr.n_anchors;
+                }
+            }
+        } else {
+            for (uint32_t t = lane; t < c; t += 32) {
+                NamRec nr = t < c0 ? s0[t] : s1[t - c0];
+                nr.nam_id = t;
+                tmp[ob + t] = nr;
+                keys[ob + t] = score_key(nr.score);
+                vals[ob + t] = t;
+            }
+            if (lane == 0) {
+                const uint32_t i = atomicAdd(n_long, 1u);
+                long_reads[i] = r;
+                long_begin[i] = ob;
+                long_end[i] = ob + c;
             }
         }
-        if (lane == 0) details[r].n_nams = c;
+    }
+}
+
+// the sorted order of each listed read applied: out[ob + rank] = tmp[ob + perm[rank]]
+__global__ void __launch_bounds__(256) k_nam_gather(uint32_t n_long, const uint32_t* long_reads,
+                                                    const uint64_t* seg_off, const uint32_t* nam_seg_count,
+                                                    const uint64_t* nam_off, const NamRec* tmp, const uint32_t* perm,
+                                                    NamRec* out, const uint64_t* anc_start, uint64_t* anc_src,
+                                                    uint64_t* anc_count) {
+    const uint32_t lane = lane_id();
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t i = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; i < n_long; i += nwarps) {
+        const uint32_t r = long_reads[i];
+        const uint32_t c0 = nam_seg_count[2 * r], c = c0 + nam_seg_count[2 * r + 1];
+        const uint64_t ob = nam_off[r];
+        for (uint32_t k = lane; k < c; k += 32) {
+            const uint32_t t = perm[ob + k];
+            const NamRec nr = tmp[ob + t];
+            out[ob + k] = nr;
+            if (anc_src) {
+                anc_src[ob + k] = nam_anchor_src(anc_start, seg_off, r, c0, t);
+                anc_count[ob + k] = nr.n_anchors;
+            }
+        }
     }
 }
 
@@ -890,6 +993,12 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     ws.orient.reserve(n);
     ws.details.reserve(n);
     kt->begin(KS_HITS, st);
+    if (cfg.mcs != SA_MCS_FIRST_STROBE) {
+        k_probe<<<warps_grid(n), 32 * WARPS_PER_BLOCK, 0, st>>>(ix, ws.off.p, n, total, cfg.mcs, ws.qr_hash.p,
+                                                                ws.qr_hash_rc.p, ws.n_rs.p, ws.hit_pos.p,
+                                                                ws.hit_info.p);
+        launches++;
+    }
     k_hits<<<warps_grid(n), 32 * WARPS_PER_BLOCK, 0, st>>>(
         ix, ws.off.p, n, total, cfg.mcs, cfg.rescue_distance, ws.qr_hash.p, ws.qr_hash_rc.p, ws.qr_start.p,
         ws.qr_end.p, ws.n_rs.p, ws.hit_pos.p, ws.hit_info.p, ws.hit_count_cache.p, ws.n_hits.p, ws.orient.p,
@@ -950,9 +1059,11 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     launches++;
     ws.nam_count.reserve((size_t)n + 1);
     ws.nam_off.reserve((size_t)n + 1);
+    kt->begin(KS_NAMS_OTHER, st);
     k_nam_counts<<<(n + 255) / 256 + 1, 256, 0, st>>>(n, ws.nam_seg_count.p, ws.nam_count.p);
     SA_CUDA(cudaMemsetAsync(ws.nam_count.p + n, 0, 8, st));
     cub_excl_sum(ws, ws.nam_count.p, ws.nam_off.p, (uint64_t)n + 1, st);
+    kt->end(st);
     launches += 2;
     uint64_t total_nams = 0;
     SA_CUDA(cudaMemcpyAsync(&total_nams, ws.nam_off.p + n, 8, cudaMemcpyDeviceToHost, st));
@@ -962,11 +1073,41 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
         ws.nam_anc_src.reserve(total_nams + 1);
         ws.nam_anc_off.reserve(total_nams + 1);
     }
+    ws.nam_tmp.reserve(total_nams);
+    ws.nam_keys.reserve(2 * total_nams);
+    ws.nam_vals.reserve(2 * total_nams);
+    ws.long_reads.reserve((size_t)n + 1);
+    ws.long_begin.reserve((size_t)n);
+    ws.long_end.reserve((size_t)n);
+    kt->begin(KS_NAMS_OTHER, st);
+    SA_CUDA(cudaMemsetAsync(ws.long_reads.p + n, 0, 4, st));
     k_nam_compact<<<warps_grid(n), 32 * WARPS_PER_BLOCK, 0, st>>>(
         n, ws.seg_off.p, ws.nam_scratch.p, ws.nam_seg_count.p, ws.nam_off.p, ws.nams.p, ws.details.p,
         cfg.nam_anchors ? ws.anc_start.p : nullptr, cfg.nam_anchors ? ws.nam_anc_src.p : nullptr,
-        cfg.nam_anchors ? ws.nam_anc_off.p : nullptr);
+        cfg.nam_anchors ? ws.nam_anc_off.p : nullptr, ws.nam_tmp.p, ws.nam_keys.p, ws.nam_vals.p,
+        ws.long_reads.p, ws.long_begin.p, ws.long_end.p, ws.long_reads.p + n);
     launches++;
+    uint32_t n_long = 0;
+    SA_CUDA(cudaMemcpyAsync(&n_long, ws.long_reads.p + n, 4, cudaMemcpyDeviceToHost, st));
+    SA_CUDA(cudaStreamSynchronize(st));
+    if (n_long) {
+        uint32_t* keys_out = ws.nam_keys.p + total_nams;
+        uint32_t* perm = ws.nam_vals.p + total_nams;
+        size_t tmp = 0;
+        cub::DeviceSegmentedSort::StableSortPairsDescending(nullptr, tmp, ws.nam_keys.p, keys_out, ws.nam_vals.p,
+                                                            perm, (int64_t)total_nams, (int64_t)n_long,
+                                                            ws.long_begin.p, ws.long_end.p, st);
+        ws.cub_tmp.reserve(tmp);
+        cub::DeviceSegmentedSort::StableSortPairsDescending(ws.cub_tmp.p, tmp, ws.nam_keys.p, keys_out,
+                                                            ws.nam_vals.p, perm, (int64_t)total_nams,
+                                                            (int64_t)n_long, ws.long_begin.p, ws.long_end.p, st);
+        k_nam_gather<<<warps_grid(n_long), 32 * WARPS_PER_BLOCK, 0, st>>>(
+            n_long, ws.long_reads.p, ws.seg_off.p, ws.nam_seg_count.p, ws.nam_off.p, ws.nam_tmp.p, perm, ws.nams.p,
+            cfg.nam_anchors ? ws.anc_start.p : nullptr, cfg.nam_anchors ? ws.nam_anc_src.p : nullptr,
+            cfg.nam_anchors ? ws.nam_anc_off.p : nullptr);
+        launches += 2;
+    }
+    kt->end(st);
     ws.anchor_qbits = ap.qbits;
     ws.anchor_pbits = ap.pbits;
     ws.last_total_nam_anchors = 0;

@@ -42,6 +42,12 @@ struct NamWorkspace {
     DevBuf<uint64_t> nam_off;               // n + 1
     DevBuf<uint64_t> nam_count;             // n (u64 for the scan)
     DevBuf<NamRec> nams;
+    // reads with more than 32 NAMs: push-order copy, sort keys / permutation (in, out),
+    // and the list of such reads with their output ranges; long_reads[n] counts them
+    DevBuf<NamRec> nam_tmp;
+    DevBuf<uint32_t> nam_keys, nam_vals;
+    DevBuf<uint32_t> long_reads;
+    DevBuf<uint64_t> long_begin, long_end;
     // with NamConfig::nam_anchors: the anchors of each NAM's chain, last to first
     // (src/chainer.rs:420-440), as packed anchor keys; NAM t's are at
     // nam_anc[nam_anc_off[t] .. nam_anc_off[t + 1])

@@ -428,11 +428,32 @@ struct NamPair {
 };
 
 // src/mapper.rs:1224-1299
-std::vector<NamPair> best_scoring_nam_pairs(const std::vector<NamRec>& n1, const std::vector<NamRec>& n2, float mu,
-                                            float sigma) {
-    std::vector<NamPair> pairs;
-    if (n1.empty() && n2.empty()) return pairs;
-    std::vector<uint32_t> added1, added2;
+// Stable sort for the short lists of one record: insertion sort (no allocation) up
+// to 32 elements, std::stable_sort beyond.  `before(a, b)`: a strictly precedes b.
+template <class T, class F>
+void stable_sort_small(std::vector<T>& v, F before) {
+    if (v.size() > 32) {
+        std::stable_sort(v.begin(), v.end(), before);
+        return;
+    }
+    for (size_t i = 1; i < v.size(); i++) {
+        T x = v[i];
+        size_t j = i;
+        while (j > 0 && before(x, v[j - 1])) {
+            v[j] = v[j - 1];
+            j--;
+        }
+        v[j] = x;
+    }
+}
+
+void best_scoring_nam_pairs(const std::vector<NamRec>& n1, const std::vector<NamRec>& n2, float mu, float sigma,
+                            std::vector<NamPair>& pairs, std::vector<uint32_t>& added1,
+                            std::vector<uint32_t>& added2) {
+    pairs.clear();
+    added1.clear();
+    added2.clear();
+    if (n1.empty() && n2.empty()) return;
     auto has = [](const std::vector<uint32_t>& v, uint32_t x) { return std::find(v.begin(), v.end(), x) != v.end(); };
     uint32_t best_joint = 0;
     for (size_t a = 0; a < n1.size() && a < 1000; a++) {
@@ -463,8 +484,7 @@ std::vector<NamPair> best_scoring_nam_pairs(const std::vector<NamRec>& n1, const
             pairs.push_back(NamPair{n.score, false, true, NamRec{}, n});
         }
     }
-    std::stable_sort(pairs.begin(), pairs.end(), [](const NamPair& a, const NamPair& b) { return a.score > b.score; });
-    return pairs;
+    stable_sort_small(pairs, [](const NamPair& a, const NamPair& b) { return a.score > b.score; });
 }
 
 void add_details(Details& a, const Details& b) {
@@ -487,12 +507,31 @@ void add_details(Details& a, const Details& b) {
 
 }  // namespace
 
+// Per-thread buffers of one record's evaluation, reused across records
+struct Policy::Scratch {
+    std::vector<NamRec> nams[2];
+    std::vector<Alignment> alignments, al1;
+    std::vector<std::pair<bool, Alignment>> al2;
+    std::vector<ScoredPair> pairs;
+    std::vector<std::pair<uint32_t, std::pair<bool, Alignment>>> cache[2];
+    std::vector<NamPair> np;
+    std::vector<uint32_t> added1, added2;
+    std::vector<Sam> recs;
+};
+
+Policy::Policy(const PolicyConfig& cfg, const std::vector<ContigInfo>& contigs, const BatchView& bv,
+               ResultStore& store)
+    : cfg_(cfg), contigs_(contigs), bv_(bv), store_(store), sc_(new Scratch) {}
+
+Policy::~Policy() = default;
+
 // ------------------------------------------------------------------ result access
 const ResultStore::Entry* Policy::lookup(uint32_t read, const JobKey& key) const {
-    const auto& v = store_.per_read[read];
+    const uint32_t h = store_.head[read];
+    const ResultStore::Entry* pool = cur_->entries.data();
     auto find = [&](const JobKey& k) -> const ResultStore::Entry* {
-        for (auto& e : v)
-            if (e.key == k && e.result) return &e;
+        for (uint32_t i = h; i != ResultStore::NONE; i = pool[i].next)
+            if (pool[i].key == k && pool[i].result) return &pool[i];
         return nullptr;
     };
     if (const ResultStore::Entry* r = find(key)) return r;
@@ -510,12 +549,14 @@ const ResultStore::Entry* Policy::lookup(uint32_t read, const JobKey& key) const
 
 void Policy::want(uint32_t read, const ExtJob& job, const JobKey& key) {
     if (lookup(read, key)) return;
-    auto& v = store_.per_read[read];
-    for (auto& e : v)
-        if (e.key == key) return;  // pending
-    v.push_back(ResultStore::Entry{key, nullptr, nullptr});
+    auto& pool = cur_->entries;
+    uint32_t& h = store_.head[read];
+    for (uint32_t i = h; i != ResultStore::NONE; i = pool[i].next)
+        if (pool[i].key == key) return;  // pending
+    pool.push_back(ResultStore::Entry{key, h, nullptr, nullptr});
+    h = (uint32_t)(pool.size() - 1);
     ExtJob j = job;
-    j.tag = (uint32_t)(v.size() - 1);
+    j.tag = h;
     cur_->pending.push_back(j);
 }
 
@@ -535,7 +576,7 @@ void Policy::resolve(ChunkState& cs) {
     const WaveResults& w = *cs.wave;
     for (size_t j = 0; j < cs.pending.size(); j++) {
         const ExtJob& jb = cs.pending[j];
-        auto& e = store_.per_read[jb.read][jb.tag];
+        auto& e = cs.entries[jb.tag];
         e.result = &w.results[cs.wave_first + j];
         e.cigar = w.cigar.data();
         cs.result_bytes += sizeof(ExtResult) + (e.result->valid ? 4ull * e.result->cigar_len : 0);
@@ -616,7 +657,7 @@ bool Policy::extend(uint32_t read, NamRec& nam, uint32_t kind, Alignment& out, b
 
 // rescue_align (src/mapper.rs:1094-1153): the window is fixed here, the
 // has_shared_substring filter and the alignment run on the GPU
-bool Policy::rescue(uint32_t read, const NamRec& mate, float mu, float sigma, Alignment& out) {
+bool Policy::rescue_job(uint32_t read, const NamRec& mate, float mu, float sigma, ExtJob& j, JobKey& key) const {
     const uint64_t rl = bv_.reads[read].len;
     const uint64_t w = sat_usize(mu + 5.0f * sigma);
     uint64_t rs, re;
@@ -636,7 +677,7 @@ bool Policy::rescue(uint32_t read, const NamRec& mate, float mu, float sigma, Al
     rs = std::min(rs, clen);
     re = std::min(re, clen);
     if (re < rs + cfg_.k) return false;
-    ExtJob j{};
+    j = ExtJob{};
     j.kind = JOB_RESCUE;
     j.read = read;
     j.ref_id = mate.ref_id;
@@ -644,21 +685,55 @@ bool Policy::rescue(uint32_t read, const NamRec& mate, float mu, float sigma, Al
     j.ref_end = (uint32_t)re;
     j.is_revcomp = rc;
     j.use_ssw = 1;
-    const StoredResult& r = get(read, j, JobKey{JOB_RESCUE, mate.ref_id, (uint32_t)rs, (uint32_t)re, rc ? 1u : 0u});
+    key = JobKey{JOB_RESCUE, mate.ref_id, (uint32_t)rs, (uint32_t)re, rc ? 1u : 0u};
+    return true;
+}
+
+bool Policy::rescue(uint32_t read, const NamRec& mate, float mu, float sigma, Alignment& out) {
+    ExtJob j;
+    JobKey key;
+    if (!rescue_job(read, mate, mu, sigma, j, key)) return false;
+    const StoredResult& r = get(read, j, key);
     if (!r.valid) return false;
     out = to_alignment(r, mate.ref_id);
     return true;
 }
 
+// Requests made on a miss for work a record will need once the missing results are
+// in: the NAM's full extension if it is unknown, else (need_valid: only when that
+// extension aligned) the rescue of the mate from the NAM as the extension flipped it.
+// Requests change no result, only which wave computes it.
+void Policy::want_rescue_chain(uint32_t read, const NamRec& nam, uint32_t mate, float mu, float sigma,
+                               bool need_valid) {
+    const ResultStore::Entry* e = lookup(read, nam_key(nam, JOB_EXTEND_FULL));
+    if (!e) {
+        want_nam(read, nam, JOB_EXTEND_FULL);
+        return;
+    }
+    if (need_valid && !e->result->valid) return;
+    NamRec m = nam;
+    m.is_revcomp = e->result->nam_is_revcomp;
+    m.query_start = e->result->nam_query_start;
+    m.query_end = e->result->nam_query_end;
+    ExtJob j;
+    JobKey key;
+    if (rescue_job(mate, m, mu, sigma, j, key)) want(mate, j, key);
+}
+
 // sort_nams (src/nam.rs:168-188): the GPU already applied the stable sort
-std::vector<NamRec> Policy::sorted_nams(uint32_t read, Rng& rng) const {
-    std::vector<NamRec> v(bv_.nams + bv_.nam_off[read], bv_.nams + bv_.nam_off[read + 1]);
+void Policy::sorted_nams(uint32_t read, Rng& rng, std::vector<NamRec>& v) const {
+    v.assign(bv_.nams + bv_.nam_off[read], bv_.nams + bv_.nam_off[read + 1]);
     if (!v.empty()) {
         size_t nb = 0;
         while (nb < v.size() && v[nb].score == v[0].score) nb++;
         if (nb > 1)
             for (size_t i = 1; i < nb; i++) std::swap(v[i], v[(size_t)rng.gen_mod_u64(i + 1)]);
     }
+}
+
+std::vector<NamRec> Policy::sorted_nams(uint32_t read, Rng& rng) const {
+    std::vector<NamRec> v;
+    sorted_nams(read, rng, v);
     return v;
 }
 
@@ -667,7 +742,8 @@ std::vector<NamRec> Policy::sorted_nams(uint32_t read, Rng& rng) const {
 void Policy::se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mapped) {
     const uint32_t read = (uint32_t)rec;
     const ReadView& rv = bv_.reads[read];
-    std::vector<NamRec> nams = sorted_nams(read, rng);
+    std::vector<NamRec>& nams = sc_->nams[0];
+    sorted_nams(read, rng, nams);
     Details details;
     details.nam = bv_.details[read];
     if (nams.empty()) {
@@ -681,7 +757,8 @@ void Policy::se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mappe
     size_t best_index = 0;
     bool have_best = false;
     Alignment best;
-    std::vector<Alignment> alignments;
+    std::vector<Alignment>& alignments = sc_->alignments;
+    alignments.clear();
     for (size_t tries = 0; tries < nams.size() && tries < max_tries; tries++) {
         NamRec& nam = nams[tries];
         float dropoff = nam.score / nam_max;
@@ -754,16 +831,17 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
     const uint32_t rd[2] = {(uint32_t)(2 * rec), (uint32_t)(2 * rec + 1)};
     const ReadView* rv[2] = {&bv_.reads[rd[0]], &bv_.reads[rd[1]]};
     Details det[2];
-    std::vector<NamRec> nams[2];
+    std::vector<NamRec>(&nams)[2] = sc_->nams;
     for (int i = 0; i < 2; i++) {
-        nams[i] = sorted_nams(rd[i], rng);
+        sorted_nams(rd[i], rng, nams[i]);
         det[i].nam = bv_.details[rd[i]];
     }
     for (int i = 0; i < 2; i++)
         if (!nams[i].empty()) want_nam(rd[i], nams[i][0], JOB_EXTEND_FAST);
     const float mu = isd.mu, sigma = isd.sigma, dropoff = cfg_.mp.dropoff_threshold;
     const size_t max_tries = cfg_.mp.max_tries;
-    std::vector<ScoredPair> pairs;
+    std::vector<ScoredPair>& pairs = sc_->pairs;
+    pairs.clear();
     bool fast = false;
     Alignment proper[2];
 
@@ -771,8 +849,10 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
         // src/mapper.rs:1018-1091; det[has] / det[other] as the reference passes them
         std::vector<NamRec>& n1 = nams[has];
         float max1 = n1[0].score;
-        std::vector<Alignment> al1;
-        std::vector<std::pair<bool, Alignment>> al2;
+        std::vector<Alignment>& al1 = sc_->al1;
+        std::vector<std::pair<bool, Alignment>>& al2 = sc_->al2;
+        al1.clear();
+        al2.clear();
         for (size_t t = 0; t < n1.size() && t < max_tries; t++) {
             NamRec& nam = n1[t];
             if (nam.score / max1 < dropoff) break;
@@ -781,20 +861,21 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
             bool ok;
             try {
                 ok = extend(rd[has], nam, JOB_EXTEND_FULL, a, consistent);
+                det[has].inconsistent_nams += !consistent;
+                if (ok) {
+                    det[has].gapped += a.gapped;
+                    al1.push_back(a);
+                    det[has].tried_alignment++;
+                    Alignment b;
+                    bool okb = rescue(rd[other], nam, mu, sigma, b);
+                    if (okb) det[other].mate_rescue++;
+                    al2.emplace_back(okb, b);
+                }
             } catch (const Miss&) {
+                // every later try is an extension and, when it aligns, a rescue
                 for (size_t u = t + 1; u < n1.size() && u < max_tries; u++)
-                    if (n1[u].score / max1 >= dropoff) want_nam(rd[has], n1[u], JOB_EXTEND_FULL);
+                    if (n1[u].score / max1 >= dropoff) want_rescue_chain(rd[has], n1[u], rd[other], mu, sigma, true);
                 throw;
-            }
-            det[has].inconsistent_nams += !consistent;
-            if (ok) {
-                det[has].gapped += a.gapped;
-                al1.push_back(a);
-                det[has].tried_alignment++;
-                Alignment b;
-                bool okb = rescue(rd[other], nam, mu, sigma, b);
-                if (okb) det[other].mate_rescue++;
-                al2.emplace_back(okb, b);
             }
         }
         for (auto& a1 : al1) {
@@ -857,7 +938,9 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
         if (!took_fast) {
             // full search (src/mapper.rs:882-1013)
             for (int i = 0; i < 2; i++) want_nam(rd[i], nams[i][0], JOB_EXTEND_FULL);
-            std::vector<std::pair<uint32_t, std::pair<bool, Alignment>>> cache[2];
+            std::vector<std::pair<uint32_t, std::pair<bool, Alignment>>>(&cache)[2] = sc_->cache;
+            cache[0].clear();
+            cache[1].clear();
             bool have_indv[2] = {false, false};
             Alignment indv[2];
             for (int i = 0; i < 2; i++) {
@@ -871,18 +954,31 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
                 det[i].gapped += ok ? a.gapped : 0;
                 cache[i].push_back({nams[i][0].nam_id, {ok, a}});
             }
-            std::vector<NamPair> np = best_scoring_nam_pairs(nams[0], nams[1], mu, sigma);
+            std::vector<NamPair>& np = sc_->np;
+            best_scoring_nam_pairs(nams[0], nams[1], mu, sigma, np, sc_->added1, sc_->added2);
             float max_score = np[0].score;
             size_t n_out = 0;
+            size_t cur = 0;  // the pair being evaluated
             auto prefetch = [&]() {
-                // on a miss, also request the NAM extensions the first pairs can need
-                for (size_t t = 0; t < np.size() && t < max_tries; t++) {
-                    if (np[t].h1) want_nam(rd[0], np[t].n1, JOB_EXTEND_FULL);
-                    if (np[t].h2) want_nam(rd[1], np[t].n2, JOB_EXTEND_FULL);
+                // on a miss, also request what the next pairs can need: their NAM
+                // extensions, and for a one-sided pair the rescue from its partner
+                // (pairs whose alignments fail do not count towards max_tries, so
+                // the loop can run through many pairs)
+                for (size_t t = cur; t < np.size() && t < cur + max_tries; t++) {
+                    if (np[t].score / max_score < dropoff) break;
+                    if (np[t].h1 && np[t].h2) {
+                        want_nam(rd[0], np[t].n1, JOB_EXTEND_FULL);
+                        want_nam(rd[1], np[t].n2, JOB_EXTEND_FULL);
+                    } else if (np[t].h1) {
+                        want_rescue_chain(rd[0], np[t].n1, rd[1], mu, sigma, false);
+                    } else if (np[t].h2) {
+                        want_rescue_chain(rd[1], np[t].n2, rd[0], mu, sigma, false);
+                    }
                 }
             };
             try {
-            for (auto& pr : np) {
+            for (; cur < np.size(); cur++) {
+                auto& pr = np[cur];
                 float sd = pr.score / max_score;
                 if (n_out >= max_tries || sd < dropoff) break;
                 bool hv[2] = {pr.h1, pr.h2};
@@ -968,7 +1064,8 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
             }
         }
     }
-    std::vector<Sam> recs;
+    std::vector<Sam>& recs = sc_->recs;
+    recs.clear();
     if (fast) {
         bool ps = proper_pair(proper[0], proper[1], isd.mu, isd.sigma);
         if (ps && isd.sample_size < 400 && proper[0].edit_distance + proper[1].edit_distance < 3)
@@ -979,7 +1076,7 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
         const Alignment* al[2] = {&proper[0], &proper[1]};
         paired_records(*this, al, rv, mq, det, false, ps, recs);
     } else {
-        std::stable_sort(pairs.begin(), pairs.end(), [](const ScoredPair& a, const ScoredPair& b) { return a.score > b.score; });
+        stable_sort_small(pairs, [](const ScoredPair& a, const ScoredPair& b) { return a.score > b.score; });
         // deduplicate_scored_pairs (src/mapper.rs:1322-1352)
         if (pairs.size() >= 2) {
             auto same = [](bool ha, const Alignment& a, bool hb, const Alignment& b) {
@@ -1040,10 +1137,13 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
         }
     }
     if (!cfg_.mp.output_unmapped && recs.size() >= 2 && !recs[0].is_mapped() && !recs[1].is_mapped()) recs.clear();
+    const auto tf = cfg_.timing ? std::chrono::steady_clock::now() : std::chrono::steady_clock::time_point();
     for (auto& r : recs) {
         if (!speculative_) format_sam(r, cfg_, out);
         mapped += r.is_mapped();
     }
+    if (cfg_.timing)
+        cur_->seconds_format += std::chrono::duration<double>(std::chrono::steady_clock::now() - tf).count();
 }
 
 // ------------------------------------------------------------------ map-only / aemb
@@ -1342,6 +1442,10 @@ void Policy::run_chunk(ChunkState& cs) {
         } catch (const Miss&) {
             cs.out.resize(out_len);
             cs.abundance.resize(ab_len);
+            if (!cs.effects.empty()) {
+                if (cs.effects[cs.next - cs.first].known) cs.miss_mispredicted++;
+                else cs.miss_unknown++;
+            }
             // look ahead: later reads of the chunk with the best-known state, so that
             // their requests join the next wave; after the first lookahead only the
             // reads that missed are evaluated again, the others' effect on the state
@@ -1424,6 +1528,7 @@ void Policy::run_chunk(ChunkState& cs) {
     cs.done = true;
     std::string().swap(cs.spec_out);
     std::vector<ChunkState::Effect>().swap(cs.effects);
+    std::vector<ResultStore::Entry>().swap(cs.entries);
 }
 
 }  // namespace sa

@@ -81,12 +81,16 @@ struct StoredResult : ExtResult {
 // the thread that runs the chunk owning the read (chunks run on one thread at a
 // time), so no locking is needed.
 struct ResultStore {
+    static constexpr uint32_t NONE = 0xffffffffu;
     struct Entry {
         JobKey key;
+        uint32_t next;            // the read's next entry in its chunk's pool, or NONE
         const ExtResult* result;  // nullptr while pending
         const uint32_t* cigar;    // CIGAR base of the wave that produced the result
     };
-    std::vector<std::vector<Entry>> per_read;
+    // per read: its first entry in the owning chunk's pool (ChunkState::entries)
+    std::vector<uint32_t> head;
+    void reset(size_t n_reads) { head.assign(n_reads, NONE); }
 };
 
 struct ReadView {
@@ -137,7 +141,8 @@ struct ChunkState {
     std::string out;
     uint64_t mapped = 0;
     bool done = false;
-    std::vector<ExtJob> pending;                          // requests raised by this chunk
+    std::vector<ResultStore::Entry> entries;              // requests and results of this chunk's reads
+    std::vector<ExtJob> pending;                          // requests raised by this chunk (tag: entry)
     // the wave that ran `pending`: its results start at wave_first, in pending's
     // order; the thread that resumes the chunk points the entries at them
     std::shared_ptr<const WaveResults> wave;
@@ -163,15 +168,20 @@ struct ChunkState {
     std::vector<Effect> effects;
     std::string spec_out;  // outputs captured by the lookahead
     uint64_t evals_reused = 0;
+    // real-run misses on a record the lookahead had evaluated to the end under another
+    // state (mispredicted), and on one it had not (unknown)
+    uint64_t miss_mispredicted = 0, miss_unknown = 0;
     // host time by phase when PolicyConfig::timing is set
-    double seconds_real = 0, seconds_spec = 0, seconds_seed = 0;
+    double seconds_real = 0, seconds_spec = 0, seconds_seed = 0, seconds_format = 0;
     uint64_t evals_real = 0, evals_spec = 0, runs = 0;
 };
 
 class Policy {
   public:
-    Policy(const PolicyConfig& cfg, const std::vector<ContigInfo>& contigs, const BatchView& bv, ResultStore& store)
-        : cfg_(cfg), contigs_(contigs), bv_(bv), store_(store) {}
+    Policy(const PolicyConfig& cfg, const std::vector<ContigInfo>& contigs, const BatchView& bv, ResultStore& store);
+    ~Policy();
+    Policy(const Policy&) = delete;
+    Policy& operator=(const Policy&) = delete;
     // Advance one chunk as far as the available results allow.  On a miss, the
     // rest of the chunk is evaluated speculatively (state copies, output dropped)
     // so that the jobs of later reads join the next wave.
@@ -186,6 +196,8 @@ class Policy {
     ResultStore& store_;
     ChunkState* cur_ = nullptr;
     bool speculative_ = false;
+    struct Scratch;
+    std::unique_ptr<Scratch> sc_;
     void add_abundance(uint32_t ref_id, double w) {
         if (!speculative_) cur_->abundance.emplace_back(ref_id, w);
     }
@@ -205,6 +217,7 @@ class Policy {
   public:
     // helpers used by the implementation file
     std::vector<NamRec> sorted_nams(uint32_t read, Rng& rng) const;
+    void sorted_nams(uint32_t read, Rng& rng, std::vector<NamRec>& out) const;
     ExtJob nam_job(uint32_t read, const NamRec& n, uint32_t kind) const;
     static JobKey nam_key(const NamRec& n, uint32_t kind) { return JobKey{kind, n.nam_id, 0, 0, 0}; }
     Alignment to_alignment(const StoredResult& r, uint32_t ref_id) const;
@@ -214,6 +227,8 @@ class Policy {
     // extend_seed with the given consistency semantics; applies the flip to nam
     bool extend(uint32_t read, NamRec& nam, uint32_t kind, Alignment& out, bool& consistent);
     bool rescue(uint32_t read, const NamRec& mate, float mu, float sigma, Alignment& out);
+    bool rescue_job(uint32_t read, const NamRec& mate, float mu, float sigma, ExtJob& j, JobKey& key) const;
+    void want_rescue_chain(uint32_t read, const NamRec& nam, uint32_t mate, float mu, float sigma, bool need_valid);
     void want_nam(uint32_t read, const NamRec& n, uint32_t kind);
 };
 

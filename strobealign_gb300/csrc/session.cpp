@@ -332,6 +332,7 @@ void Session::admitter() {
 void Session::admit(Request& r) {
     const uint32_t n = (uint32_t)r.n_reads;
     if (n == 0) return;
+    const auto ta = std::chrono::steady_clock::now();
     // reads: pinned staging, local offsets for the NAM pipeline, arena copy for the extension
     h_seq_.reserve(r.total_bases + 16);
     h_off_.reserve((size_t)n + 1);
@@ -352,8 +353,23 @@ void Session::admit(Request& r) {
     cfg.mcs = mp_.mcs_strategy;
     cfg.rescue_distance = mp_.rescue_distance;
     cfg.nam_anchors = !r.paired && mp_.mode == SA_MODE_SAM && !mp_.use_ssw;
+    if (trace_) {
+        // the staging copies above complete first, so that the pipeline's time is its own
+        SA_CUDA(cudaStreamSynchronize(sta_));
+    }
+    const auto tp1 = std::chrono::steady_clock::now();
+    KernelTimers kt;
+    kt.enabled = trace_;
     run_nam_pipeline(idx_->view(), refs_view_, cfg, n, r.total_bases, max_contig_len_,
-                     (uint32_t)refs_->contigs.size(), nws_, sta_);
+                     (uint32_t)refs_->contigs.size(), nws_, sta_, &kt);
+    if (trace_) {
+        SA_CUDA(cudaStreamSynchronize(sta_));
+        kt.collect();
+        std::fprintf(stderr, "sa_admit_kernels id=%llu seed=%.3f hits=%.3f anchors=%.3f sort=%.3f chain=%.3f other=%.3f\n",
+                     (unsigned long long)r.id, kt.ms[KS_SEED], kt.ms[KS_HITS], kt.ms[KS_ANCHORS], kt.ms[KS_SORT],
+                     kt.ms[KS_CHAIN], kt.ms[KS_NAMS_OTHER]);
+    }
+    const auto tp2 = std::chrono::steady_clock::now();
     const uint64_t tn = nws_.last_total_nams;
     if (cfg.nam_anchors) {
         const uint64_t ta = nws_.last_total_nam_anchors;
@@ -398,7 +414,14 @@ void Session::admit(Request& r) {
         i = j;
     }
     r.seeded.assign(r.chunks.size(), 0);
-    r.store.per_read.resize(n);
+    r.store.reset(n);
+    if (trace_) {
+        auto d = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+            return std::chrono::duration<double>(b - a).count();
+        };
+        std::fprintf(stderr, "sa_admit_parts id=%llu upload=%.4f pipeline=%.4f rest=%.4f\n",
+                     (unsigned long long)r.id, d(ta, tp1), d(tp1, tp2), d(tp2, std::chrono::steady_clock::now()));
+    }
 }
 
 void Session::run_wave(std::vector<std::pair<Request*, size_t>>& batch) {

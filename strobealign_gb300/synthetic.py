@@ -192,10 +192,38 @@ def _finish(rng, mat: np.ndarray, lens: np.ndarray, sub: float, indel: float, he
     return reads
 
 
+def _blocks(n: int, block: int):
+    return [(a, min(n, a + block)) for a in range(0, n, block)] or [(0, 0)]
+
+
+def _join(sets: list[ReadSet]) -> ReadSet:
+    if len(sets) == 1:
+        return sets[0]
+    seq = np.concatenate([x.seq for x in sets])
+    off = np.zeros(sum(len(x) for x in sets) + 1, dtype=np.uint64)
+    no = np.zeros_like(off)
+    i, so, nb = 0, 0, 0
+    for x in sets:
+        k = len(x)
+        off[i + 1:i + k + 1] = x.offsets[1:] + so
+        no[i + 1:i + k + 1] = x.name_offsets[1:] + nb
+        i += k
+        so += int(x.offsets[-1])
+        nb += int(x.name_offsets[-1])
+    return ReadSet(seq, off, b"".join(x.names for x in sets), no, b"".join(x.qual for x in sets))
+
+
 def make_single_end(seed: int, genome: Genome, n: int, length: int | tuple[int, int] = 150, sub: float = 0.01,
-                    indel: float = 0.001) -> ReadSet:
+                    indel: float = 0.001, block: int = 1_000_000) -> ReadSet:
+    """Reads from uniform positions on both strands; generated in blocks of `block`
+    reads (one RNG stream) to bound memory."""
     rng = np.random.Generator(np.random.PCG64(seed))
     g, lens, starts = _concat(genome)
+    return _join([_single_block(rng, g, lens, starts, a, b, length, sub, indel) for a, b in _blocks(n, block)])
+
+
+def _single_block(rng, g, lens, starts, first, last, length, sub, indel) -> ReadSet:
+    n = last - first
     if isinstance(length, int):
         L = np.full(n, length, dtype=np.int64)
     else:
@@ -208,16 +236,24 @@ def make_single_end(seed: int, genome: Genome, n: int, length: int | tuple[int, 
     rev_idx = pos[:, None] + np.maximum(L[:, None] - 1 - j[None, :], 0)
     mat = np.where(flip[:, None], COMP[g[rev_idx]], g[fwd_idx])
     reads = _finish(rng, mat, L, sub, indel)
-    return _pack(reads, [f"r{i}" for i in range(n)])
+    return _pack(reads, [f"r{i}" for i in range(first, last)])
 
 
 def make_paired_end(seed: int, genome: Genome, n: int, length: int = 150, insert_mean: float = 300,
                     insert_sd: float = 30, sub: float = 0.01, indel: float = 0.001,
-                    rescue_fraction: float = 0.0) -> tuple[ReadSet, ReadSet]:
+                    rescue_fraction: float = 0.0, block: int = 1_000_000) -> tuple[ReadSet, ReadSet]:
     """Pairs in FR orientation; `rescue_fraction` of pairs get one mate mutated
-    heavily so that it finds few or no seeds and has to be rescued from its mate."""
+    heavily so that it finds few or no seeds and has to be rescued from its mate.
+    Generated in blocks of `block` pairs (one RNG stream) to bound memory."""
     rng = np.random.Generator(np.random.PCG64(seed))
     g, lens, starts = _concat(genome)
+    parts = [_paired_block(rng, g, lens, starts, a, b, length, insert_mean, insert_sd, sub, indel, rescue_fraction)
+             for a, b in _blocks(n, block)]
+    return _join([p[0] for p in parts]), _join([p[1] for p in parts])
+
+
+def _paired_block(rng, g, lens, starts, first, last, length, insert_mean, insert_sd, sub, indel, rescue_fraction):
+    n = last - first
     ins = np.maximum(np.rint(rng.normal(insert_mean, insert_sd, size=n)).astype(np.int64), length)
     pos, ins = _positions(rng, lens, starts, ins)
     flip = rng.random(n) < 0.5
@@ -231,7 +267,7 @@ def make_paired_end(seed: int, genome: Genome, n: int, length: int = 150, insert
     which = rng.random(n) < 0.5
     ha = None if heavy is None else (heavy & which)
     hb = None if heavy is None else (heavy & ~which)
-    names = [f"p{i}" for i in range(n)]
+    names = [f"p{i}" for i in range(first, last)]
     return _pack(_finish(rng, a, L, sub, indel, ha), names), _pack(_finish(rng, b, L, sub, indel, hb), names)
 
 

@@ -168,10 +168,15 @@ class OracleIndex:
 
     def nams(self, seq: bytes, mcs: int = 0, rescue_distance: int = 100):
         cap = 4 * len(seq) + 16
-        out = (OraNam * cap)()
         n = C.c_size_t()
         det = OraNamDetails()
-        assert self.lib.ora_nams(self.h, seq, len(seq), mcs, rescue_distance, out, cap, C.byref(n), C.byref(det)) == 0
+        while True:
+            out = (OraNam * cap)()
+            rc = self.lib.ora_nams(self.h, seq, len(seq), mcs, rescue_distance, out, cap, C.byref(n), C.byref(det))
+            if rc == 0:
+                break
+            assert n.value > cap  # the only failure: more NAMs than room; n holds the count
+            cap = n.value
         rows = [tuple(getattr(out[i], f) for f, _ in OraNam._fields_) for i in range(n.value)]
         return rows, {f: getattr(det, f) for f, _ in OraNamDetails._fields_}
 

@@ -38,6 +38,23 @@ def synth(tmp_path_factory):
     return dict(dir=d, fa=fa, f1=f1, f2=f2, fse=fse, genome=g)
 
 
+@pytest.fixture(scope="module")
+def repeats(tmp_path_factory):
+    # many-copy families and tandem arrays: hashes above the repeat cutoff, buckets of
+    # hundreds of entries, local and global seed rescue, long rescue chains
+    from strobealign_gb300 import synthetic as syn
+    d = tmp_path_factory.mktemp("repeats")
+    g = syn.make_genome(31, 300_000, 2, gc=0.41, repeat_fraction=0.5, family_len=(300, 500),
+                        family_div=(0.0, 0.02), tandem_fraction=0.05)
+    fa = str(d / "ref.fa")
+    g.write_fasta(fa)
+    r1, r2 = syn.make_paired_end(32, g, 3000, 150, 300, 30, 0.01, 0.002, rescue_fraction=0.05)
+    f1, f2 = str(d / "r1.fq"), str(d / "r2.fq")
+    r1.write_fastq(f1)
+    r2.write_fastq(f2)
+    return dict(dir=d, fa=fa, f1=f1, f2=f2, genome=g)
+
+
 def _index(sa, fa, read_length=150):
     refs = sa.References.from_fasta(fa)
     p = sa.SeedingParameters.from_read_length(read_length)
@@ -120,15 +137,17 @@ def _nam_rows(arr):
              np.float32(x["score"]).view(np.uint32), int(x["is_revcomp"])) for x in arr]
 
 
+@pytest.mark.parametrize("genome", ["synth", "repeats"])
 @pytest.mark.parametrize("mcs", ["always", "rescue", "off", "first-strobe"])
-def test_nams_identical_to_oracle(sa, synth, mcs):
-    refs, idx = _index(sa, synth["fa"])
-    reads = sa.Reads.from_file(synth["f1"])
-    names, seqs = _reads_with_edge_cases(synth)
+def test_nams_identical_to_oracle(sa, synth, repeats, mcs, genome):
+    src = synth if genome == "synth" else repeats
+    refs, idx = _index(sa, src["fa"])
+    reads = sa.Reads.from_file(src["f1"])
+    names, seqs = _reads_with_edge_cases(src)
     batch_seqs = [reads.seq[reads.seq_offsets[i]:reads.seq_offsets[i + 1]] for i in range(600)] + seqs
     rb = sa.Reads.from_lists([f"n{i}" for i in range(len(batch_seqs))], batch_seqs)
     nams, det = sa.nams_batch(idx, rb, mapping=sa.mapping_defaults(mcs_strategy=mcs))
-    o = OracleIndex(synth["fa"], 150)
+    o = OracleIndex(src["fa"], 150)
     mcs_i = sa.MCS[mcs]
     for i, s in enumerate(batch_seqs):
         rows, od = o.nams(bytes(s), mcs_i)
@@ -254,6 +273,12 @@ def _first_diff(a: bytes, b: bytes) -> str:
 def test_synthetic_paired_end_sam_matches_oracle(sa, synth):
     want = run_oracle_cli(["--no-PG", "--eqx", synth["fa"], synth["f1"], synth["f2"]])
     got = _map_files(sa, synth["fa"], [synth["f1"], synth["f2"]], eqx=1)
+    assert got == want, _first_diff(got, want)
+
+
+def test_repetitive_paired_end_sam_matches_oracle(sa, repeats):
+    want = run_oracle_cli(["--no-PG", "--eqx", repeats["fa"], repeats["f1"], repeats["f2"]])
+    got = _map_files(sa, repeats["fa"], [repeats["f1"], repeats["f2"]], eqx=1)
     assert got == want, _first_diff(got, want)
 
 
