@@ -296,6 +296,7 @@ typedef struct {
     uint64_t max_inflight_bases;    /* device read arena in bases; 0 = 2^30 */
     uint32_t max_inflight_requests; /* 0 = no limit */
     uint32_t policy_threads;        /* host threads for the mapping policy; 0 = all */
+    uint32_t admission_streams;     /* requests whose NAM pipelines run at once; 0 = 2 */
 } sa_session_params;
 typedef struct {
     double seconds_queued;  /* submit -> admitted */

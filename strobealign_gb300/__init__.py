@@ -418,7 +418,7 @@ class Session:
 
     def __init__(self, index: StrobemerIndex, refs: References, chaining: L.ChainingParams | None = None,
                  mapping: L.MappingParams | None = None, max_inflight_bases: int = 0, max_inflight_requests: int = 0,
-                 policy_threads: int = 0, **kw):
+                 policy_threads: int = 0, admission_streams: int = 0, **kw):
         self.index, self.refs = index, refs
         self.cp = chaining or chaining_defaults()
         self.mp = mapping or mapping_defaults(**kw)
@@ -428,6 +428,8 @@ class Session:
             sp.max_inflight_bases = max_inflight_bases
         sp.max_inflight_requests = max_inflight_requests
         sp.policy_threads = policy_threads
+        if admission_streams:
+            sp.admission_streams = admission_streams
         h = C.c_void_p()
         L.check(lib().sa_session_create(index.h, refs.h, C.byref(self.cp), C.byref(self.mp), C.byref(sp),
                                         C.byref(h)))

@@ -625,6 +625,7 @@ void sa_session_params_default(sa_session_params* p) {
     p->max_inflight_bases = 1ull << 30;
     p->max_inflight_requests = 0;
     p->policy_threads = 0;
+    p->admission_streams = 2;
 }
 
 int32_t sa_session_create(const sa_index* idx, const sa_refs* refs, const sa_chaining_params* cp,
@@ -644,6 +645,7 @@ int32_t sa_session_create(const sa_index* idx, const sa_refs* refs, const sa_cha
         sc.max_inflight_bases = sp->max_inflight_bases;
         sc.max_inflight_requests = sp->max_inflight_requests;
         sc.policy_threads = sp->policy_threads;
+        sc.admission_streams = sp->admission_streams ? sp->admission_streams : 2;
     }
     auto* s = new sa_session{nullptr};
     try {

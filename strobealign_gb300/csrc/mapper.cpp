@@ -26,6 +26,8 @@ Mapper::Mapper(const sa_index* idx, const sa_refs* refs, const sa_chaining_param
     // SA_TRACE_WAVES=1: one line per extension wave on stderr
     const char* tr = std::getenv("SA_TRACE_WAVES");
     trace_ = tr && *tr && *tr != '0';
+    // SA_MAX_WAVE_JOBS: extension jobs per wave at most (tuning)
+    if (const char* mw = std::getenv("SA_MAX_WAVE_JOBS")) set_max_wave_jobs(std::strtoull(mw, nullptr, 10));
     SA_CUDA(cudaSetDevice(idx->device));
     SA_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
     const auto& cs = refs->contigs;
@@ -292,9 +294,17 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, ResultStore& store, u
                 return idle || waiting_jobs >= wave_min_jobs_;
             });
             if (stop || n_done == nchunks) break;
-            batch.swap(waiting);
-            waiting.clear();
-            waiting_jobs = 0;
+            // at most max_wave_jobs_ per wave (at least one chunk): the policy threads
+            // resume the chunks of one wave while the next runs on the device
+            batch.clear();
+            size_t k = 0, taken = 0;
+            while (k < waiting.size() &&
+                   (batch.empty() || taken + chunks[waiting[k]].pending.size() <= max_wave_jobs_)) {
+                taken += chunks[waiting[k]].pending.size();
+                batch.push_back(waiting[k++]);
+            }
+            waiting.erase(waiting.begin(), waiting.begin() + (ptrdiff_t)k);
+            waiting_jobs -= taken;
             lk.unlock();
             // chunk order inside a wave keeps waves reproducible for a given grouping
             std::sort(batch.begin(), batch.end());

@@ -36,6 +36,7 @@ class Mapper {
     void set_policy_threads(unsigned n) { policy_threads_ = n ? n : 1; }
     void set_profiling(bool on) { kt_.enabled = on; }
     void set_wave_min_jobs(uint64_t n) { wave_min_jobs_ = n; }
+    void set_max_wave_jobs(uint64_t n) { max_wave_jobs_ = n ? n : 1; }
 
   private:
     std::shared_ptr<const WaveResults> run_wave(const ExtJob* jobs, uint32_t nj, uint32_t max_qlen,
@@ -51,6 +52,7 @@ class Mapper {
     uint64_t sw_cells_[5] = {0, 0, 0, 0, 0};
     unsigned policy_threads_ = std::max(1u, std::thread::hardware_concurrency());
     uint64_t wave_min_jobs_ = 32768;
+    uint64_t max_wave_jobs_ = 262144;
     bool trace_ = false;
 
     const sa_index* idx_;

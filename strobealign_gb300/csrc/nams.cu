@@ -482,6 +482,75 @@ __device__ __forceinline__ uint32_t hit_anchors(const DevIndex& ix, uint64_t pos
     return cnt;
 }
 
+// A hit's run of equal-hash table entries: its first entry and hash (full hits:
+// the entry found; partial hits: get_masked_from with the forward main mask).  False
+// when a partial hit has no entry under that mask.
+__device__ __forceinline__ bool hit_run(const DevIndex& ix, uint64_t pos, uint32_t info, uint64_t hash,
+                                        uint64_t& start, uint64_t& fh) {
+    if (info & 2) {
+        start = idx_get_masked_from(ix, hash, ix.p.fwd_main_mask, true, pos);
+        if (start == UINT64_MAX) return false;
+        fh = load_rs(ix.rs, start).hash_offset & ix.p.fwd_main_mask;
+    } else {
+        start = pos;
+        fh = load_hash(ix.rs, pos);
+    }
+    return true;
+}
+
+// more than 32 entries in the run: the warp enumerates it together
+__device__ __forceinline__ bool run_is_long(const DevIndex& ix, uint64_t start, uint64_t fh, bool partial) {
+    const uint64_t i = start + 32;
+    if (i >= ix.n) return false;
+    const uint64_t h = partial ? (load_rs(ix.rs, i).hash_offset & ix.p.fwd_main_mask) : load_hash(ix.rs, i);
+    return h == fh;
+}
+
+// hit_anchors for one run by the whole warp (arguments uniform across the warp): lanes
+// take consecutive entries; the running-minimum length filter of full hits becomes a
+// prefix minimum over the lanes carried between 32-entry slices.
+__device__ uint32_t warp_run_anchors(const DevIndex& ix, uint64_t start, uint64_t fh, bool partial, uint32_t qs,
+                                     uint32_t qe, AnchorPack ap, uint64_t* out) {
+    const uint32_t lane = lane_id(), k = ix.p.k, ql = qe - qs;
+    uint32_t cnt = 0, carry = 0xffffffffu;
+    for (uint64_t c = start;; c += 32) {
+        const uint64_t i = c + lane;
+        bool valid = false;
+        RefRandstrobe rr{};
+        if (i < ix.n) {
+            rr = load_rs(ix.rs, i);
+            valid = partial ? (rr.hash_offset & ix.p.fwd_main_mask) == fh : rs_hash(rr) == fh;
+        }
+        // the table is sorted: the run's entries are a prefix of the lanes
+        const uint32_t vb = __ballot_sync(FULL, valid);
+        if (partial) {
+            if (valid && out) out[cnt + lane] = ap.key(rr.ref_index, rr.position, qs);
+            cnt += __popc(vb);
+        } else {
+            const uint32_t rl = valid ? (uint32_t)(rr.hash_offset & 0xff) + k : 0;
+            const uint32_t ld = valid ? (ql > rl ? ql - rl : rl - ql) : 0xffffffffu;
+            uint32_t incl = ld;
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t y = __shfl_up_sync(FULL, incl, d);
+                if (lane >= (uint32_t)d) incl = min(incl, y);
+            }
+            uint32_t excl = __shfl_up_sync(FULL, incl, 1);
+            if (lane == 0) excl = 0xffffffffu;
+            const bool o = valid && ld <= min(carry, excl);
+            const uint32_t ob = __ballot_sync(FULL, o);
+            if (o && out) {
+                const uint32_t p = cnt + 2 * __popc(ob & lanemask_lt());
+                out[p] = ap.key(rr.ref_index, rr.position, qs);
+                out[p + 1] = ap.key(rr.ref_index, rr.position + rl - k, qe - k);
+            }
+            cnt += 2 * __popc(ob);
+            carry = min(carry, __shfl_sync(FULL, incl, 31));
+        }
+        if (vb != FULL) break;
+    }
+    return cnt;
+}
+
 __device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, uint32_t& total) {
     uint32_t x = v;
     for (int d = 1; d < 32; d <<= 1) {
@@ -514,27 +583,44 @@ __global__ void __launch_bounds__(256) k_anchors(DevIndex ix, const uint64_t* __
             for (uint32_t c = 0; c < nh; c += 32) {
                 uint32_t h = c + lane;
                 uint32_t cnt = 0;
-                uint32_t info = 0;
+                uint32_t info = 0, qs = 0, qe = 0;
+                uint64_t start = 0, fh = 0;
+                bool has_run = false, is_long = false;
                 if (h < nh) {
                     info = hit_info[b + h];
                     if (!(info & 4)) {
+                        const uint32_t ri = info >> 3;
+                        qs = qr_start[b + ri];
+                        qe = (info & 2) ? qs + ix.p.k : qr_end[b + ri];
+                        has_run = hit_run(ix, hit_pos[b + h], info, qr_hash[b + ri], start, fh);
+                        is_long = has_run && run_is_long(ix, start, fh, info & 2);
                         if (FILL) cnt = hit_anchors_n[b + h];
-                        else {
-                            uint32_t ri = info >> 3;
-                            uint32_t qs = qr_start[b + ri];
-                            uint32_t qe = (info & 2) ? qs + ix.p.k : qr_end[b + ri];
-                            cnt = hit_anchors(ix, hit_pos[b + h], info, qr_hash[b + ri], qs, qe, ap, nullptr);
-                            hit_anchors_n[b + h] = cnt;
-                        }
+                        else if (has_run && !is_long) cnt = hit_anchors(ix, hit_pos[b + h], info, qr_hash[b + ri], qs, qe, ap, nullptr);
                     }
+                }
+                // long runs: counted by the whole warp, one hit at a time
+                const uint32_t lm = __ballot_sync(FULL, is_long);
+                if (!FILL) {
+                    for (uint32_t m = lm; m; m &= m - 1) {
+                        const int L = __ffs(m) - 1;
+                        const uint32_t c2 = warp_run_anchors(ix, __shfl_sync(FULL, start, L), __shfl_sync(FULL, fh, L),
+                                                             __shfl_sync(FULL, info, L) & 2, __shfl_sync(FULL, qs, L),
+                                                             __shfl_sync(FULL, qe, L), ap, nullptr);
+                        if (lane == (uint32_t)L) cnt = c2;
+                    }
+                    if (h < nh && !(info & 4)) hit_anchors_n[b + h] = cnt;
                 }
                 uint32_t tot;
                 uint32_t ex = warp_excl_scan(cnt, tot);
-                if (FILL && cnt) {
-                    uint32_t ri = info >> 3;
-                    uint32_t qs = qr_start[b + ri];
-                    uint32_t qe = (info & 2) ? qs + ix.p.k : qr_end[b + ri];
-                    hit_anchors(ix, hit_pos[b + h], info, qr_hash[b + ri], qs, qe, ap, anchors + acc + ex);
+                if (FILL) {
+                    if (cnt && !is_long)
+                        hit_anchors(ix, hit_pos[b + h], info, qr_hash[b + (info >> 3)], qs, qe, ap, anchors + acc + ex);
+                    for (uint32_t m = lm; m; m &= m - 1) {
+                        const int L = __ffs(m) - 1;
+                        warp_run_anchors(ix, __shfl_sync(FULL, start, L), __shfl_sync(FULL, fh, L),
+                                         __shfl_sync(FULL, info, L) & 2, __shfl_sync(FULL, qs, L),
+                                         __shfl_sync(FULL, qe, L), ap, anchors + acc + __shfl_sync(FULL, ex, L));
+                    }
                 }
                 acc += tot;
                 sum += tot;
@@ -565,11 +651,82 @@ __device__ __forceinline__ float chain_score(uint32_t dq, uint32_t dr, const Cha
     return __fsub_rn(score, __fadd_rn(lin, __fmul_rn(0.5f, lg)));
 }
 
+// Stable LSD radix sort of anchor indices idx[0..m) by score (dp[idx]) descending, by
+// one warp: four 8-bit passes over an order-preserving key, each a warp-ordered stable
+// counting scatter (rank among equal digits of a 32-slice from __match_any_sync).
+// idx and tmp are ping-pong buffers; the sorted order ends in tmp.
+__device__ __forceinline__ uint32_t desc_key(float s) {
+    const uint32_t b = __float_as_uint(s == 0.0f ? 0.0f : s);
+    return ~((b & 0x80000000u) ? ~b : (b | 0x80000000u));  // ascending key = descending score
+}
+
+__device__ void warp_radix_sort_desc(uint32_t* idx, uint32_t* tmp, uint32_t m, const float* dp, uint32_t* hist) {
+    const uint32_t lane = lane_id();
+    uint32_t* src = idx;
+    uint32_t* dst = tmp;
+    for (int pass = 0; pass < 4; pass++) {
+        const int sh = 8 * pass;
+        for (uint32_t t = lane; t < 256; t += 32) hist[t] = 0;
+        __syncwarp();
+        for (uint32_t c = lane; c < m; c += 32) atomicAdd(&hist[(desc_key(dp[src[c]]) >> sh) & 255], 1u);
+        __syncwarp();
+        // exclusive scan of the 256 counters, 8 per lane
+        uint32_t v[8], sum = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            v[k] = hist[lane * 8 + k];
+            sum += v[k];
+        }
+        uint32_t incl = sum;
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, d);
+            if (lane >= (uint32_t)d) incl += y;
+        }
+        uint32_t run = incl - sum;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            hist[lane * 8 + k] = run;
+            run += v[k];
+        }
+        __syncwarp();
+        for (uint32_t c0 = 0; c0 < m; c0 += 32) {
+            const uint32_t c = c0 + lane;
+            const bool in = c < m;
+            const uint32_t x = in ? src[c] : 0;
+            const uint32_t dg = in ? (desc_key(dp[x]) >> sh) & 255 : 256 + lane;
+            const uint32_t peers = __match_any_sync(FULL, dg);
+            const uint32_t base = in ? hist[dg] : 0;
+            __syncwarp();
+            if (in) {
+                dst[base + __popc(peers & lanemask_lt())] = x;
+                // the highest lane of each digit group advances the digit's offset
+                if ((peers >> lane) == 1u) hist[dg] = base + __popc(peers);
+            }
+            __syncwarp();
+        }
+        uint32_t* t = src;
+        src = dst;
+        dst = t;
+    }
+    // four passes: the result is back in idx; copy it to tmp for the caller
+    for (uint32_t c = lane; c < m; c += 32) tmp[c] = idx[c];
+}
+
+// RING: max_lookback < 64, so the predecessors of anchor i (and their scores) come
+// from a 64-entry ring in shared memory written as anchors are scored, instead of
+// global memory (the loop over a read orientation's anchors is serial; this takes
+// the store-to-load round trip out of each step).
+template <bool RING>
 __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off, uint32_t n, const uint64_t* seg_off,
                                                const uint64_t* sorted, uint64_t* dedup, float* dp, uint32_t* pred,
                                                uint32_t* aux, uint64_t total_anchors, AnchorPack ap, ChainCtx cc,
                                                NamRec* nam_out, uint32_t* nam_seg_count, uint64_t* anc_out,
                                                uint64_t* anc_start) {
+    __shared__ uint32_t hist[WARPS_PER_BLOCK * 256];
+    __shared__ uint64_t ring_key_s[RING ? WARPS_PER_BLOCK * 64 : 1];
+    __shared__ float ring_dp_s[RING ? WARPS_PER_BLOCK * 64 : 1];
+    uint64_t* ring_key = ring_key_s + (RING ? (threadIdx.x / 32) * 64 : 0);
+    float* ring_dp = ring_dp_s + (RING ? (threadIdx.x / 32) * 64 : 0);
     const uint32_t lane = lane_id();
     const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
     const uint64_t qmask = (1ULL << ap.qbits) - 1, pmask = (1ULL << ap.pbits) - 1;
@@ -600,8 +757,11 @@ __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off,
         const float kf = __uint2float_rn(cc.k);
         float best_score = 0.0f;
         uint32_t best_index = 0xffffffffu;
+        uint64_t best_key = 0;  // key and score of the anchor at best_index
+        uint64_t next_key = dedup[b];
         for (uint32_t i = 0; i < N; i++) {
-            const uint64_t ki = dedup[b + i];
+            const uint64_t ki = next_key;
+            if (i + 1 < N) next_key = dedup[b + i + 1];
             const uint32_t ri = (uint32_t)(ki >> (ap.pbits + ap.qbits)), rsi = (uint32_t)((ki >> ap.qbits) & pmask),
                            qi = (uint32_t)(ki & qmask);
             const uint32_t lookup_end = i > cc.cp.max_lookback ? i - cc.cp.max_lookback : 0;
@@ -616,7 +776,7 @@ __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off,
                 bool hard = false, valid = false, diag = false;
                 float val = 0.0f;
                 if (in) {
-                    const uint64_t kj = dedup[b + j];
+                    const uint64_t kj = RING ? ring_key[j & 63] : dedup[b + j];
                     const uint32_t rj = (uint32_t)(kj >> (ap.pbits + ap.qbits)),
                                    rsj = (uint32_t)((kj >> ap.qbits) & pmask), qj = (uint32_t)(kj & qmask);
                     if (rj != ri) hard = true;
@@ -629,7 +789,7 @@ __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off,
                             if (!(ratio > cc.cp.max_diagonal_ratio)) {
                                 valid = true;
                                 diag = dq == dr;
-                                val = __fadd_rn(dp[b + j], chain_score(dq, dr, cc));
+                                val = __fadd_rn(RING ? ring_dp[j & 63] : dp[b + j], chain_score(dq, dr, cc));
                             }
                         }
                     }
@@ -667,7 +827,7 @@ __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off,
             }
             // re-check of the best chain end (src/chainer.rs:150-165)
             if (best_index != 0xffffffffu) {
-                const uint64_t kb = dedup[b + best_index];
+                const uint64_t kb = best_key;
                 const uint32_t rb = (uint32_t)(kb >> (ap.pbits + ap.qbits)), rsb = (uint32_t)((kb >> ap.qbits) & pmask),
                                qb = (uint32_t)(kb & qmask);
                 if (rb == ri && qi > qb) {
@@ -675,7 +835,7 @@ __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off,
                     uint32_t mx = dq > dr ? dq : dr, mn = dq < dr ? dq : dr;
                     float ratio = __fdiv_rn(__uint2float_rn(mx), __uint2float_rn(mn));
                     if (dr < max_ref_gap && dr > 0 && ratio <= cc.cp.max_diagonal_ratio) {
-                        float ns = __fadd_rn(dp[b + best_index], chain_score(dq, dr, cc));
+                        float ns = __fadd_rn(best_score, chain_score(dq, dr, cc));
                         if (ns > cur) {
                             cur = ns;
                             cur_pred = best_index;
@@ -686,10 +846,15 @@ __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off,
             if (lane == 0) {
                 dp[b + i] = cur;
                 pred[b + i] = cur_pred;
+                if (RING) {
+                    ring_key[i & 63] = ki;
+                    ring_dp[i & 63] = cur;
+                }
             }
             if (cur > best_score) {
                 best_score = cur;
                 best_index = i;
+                best_key = ki;
             }
             __syncwarp();
         }
@@ -708,15 +873,18 @@ __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off,
             M += __popc(bal);
         }
         __syncwarp();
-        for (uint32_t c = lane; c < M; c += 32) {
-            uint32_t ci = cand[c];
-            float s = dp[b + ci];
+        // candidates by score, descending, ties in anchor order (a stable sort)
+        if (M <= 32) {
+            const uint32_t ci = lane < M ? cand[lane] : 0;
+            const float s = lane < M ? dp[b + ci] : 0.0f;
             uint32_t rank = 0;
             for (uint32_t u = 0; u < M; u++) {
-                float su = dp[b + cand[u]];
-                rank += (su > s) || (su == s && u < c);
+                const float su = __shfl_sync(FULL, s, u);
+                rank += (su > s) || (su == s && u < lane);
             }
-            sorted_c[rank] = ci;
+            if (lane < M) sorted_c[rank] = ci;
+        } else {
+            warp_radix_sort_desc(cand, sorted_c, M, dp + b, hist + (threadIdx.x / 32) * 256);
         }
         __syncwarp();
         if (lane == 0) {
@@ -1051,10 +1219,16 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
         ws.anc_sparse.reserve(3 * total_anchors + 1);
         ws.anc_start.reserve(total_anchors + 1);
     }
-    k_chain<<<warps_grid(2 * (uint64_t)n), 32 * WARPS_PER_BLOCK, 0, st>>>(
-        ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p, total_anchors, ap,
-        cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
-        cfg.nam_anchors ? ws.anc_start.p : nullptr);
+    if (cfg.cp.max_lookback < 64)
+        k_chain<true><<<warps_grid(2 * (uint64_t)n), 32 * WARPS_PER_BLOCK, 0, st>>>(
+            ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p,
+            total_anchors, ap, cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
+            cfg.nam_anchors ? ws.anc_start.p : nullptr);
+    else
+        k_chain<false><<<warps_grid(2 * (uint64_t)n), 32 * WARPS_PER_BLOCK, 0, st>>>(
+            ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p,
+            total_anchors, ap, cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
+            cfg.nam_anchors ? ws.anc_start.p : nullptr);
     kt->end(st);
     launches++;
     ws.nam_count.reserve((size_t)n + 1);

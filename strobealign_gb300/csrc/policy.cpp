@@ -521,13 +521,13 @@ struct Policy::Scratch {
 
 Policy::Policy(const PolicyConfig& cfg, const std::vector<ContigInfo>& contigs, const BatchView& bv,
                ResultStore& store)
-    : cfg_(cfg), contigs_(contigs), bv_(bv), store_(store), sc_(new Scratch) {}
+    : cfg_(cfg), contigs_(contigs), bv_(&bv), store_(&store), sc_(new Scratch) {}
 
 Policy::~Policy() = default;
 
 // ------------------------------------------------------------------ result access
 const ResultStore::Entry* Policy::lookup(uint32_t read, const JobKey& key) const {
-    const uint32_t h = store_.head[read];
+    const uint32_t h = store_->head[read];
     const ResultStore::Entry* pool = cur_->entries.data();
     auto find = [&](const JobKey& k) -> const ResultStore::Entry* {
         for (uint32_t i = h; i != ResultStore::NONE; i = pool[i].next)
@@ -550,7 +550,7 @@ const ResultStore::Entry* Policy::lookup(uint32_t read, const JobKey& key) const
 void Policy::want(uint32_t read, const ExtJob& job, const JobKey& key) {
     if (lookup(read, key)) return;
     auto& pool = cur_->entries;
-    uint32_t& h = store_.head[read];
+    uint32_t& h = store_->head[read];
     for (uint32_t i = h; i != ResultStore::NONE; i = pool[i].next)
         if (pool[i].key == key) return;  // pending
     pool.push_back(ResultStore::Entry{key, h, nullptr, nullptr});
@@ -560,15 +560,14 @@ void Policy::want(uint32_t read, const ExtJob& job, const JobKey& key) {
     cur_->pending.push_back(j);
 }
 
-StoredResult Policy::get(uint32_t read, const ExtJob& job, const JobKey& key) {
+bool Policy::get(uint32_t read, const ExtJob& job, const JobKey& key, StoredResult& r) {
     if (const ResultStore::Entry* e = lookup(read, key)) {
-        StoredResult r;
         static_cast<ExtResult&>(r) = *e->result;
         r.cigar = e->cigar + e->result->cigar_offset;
-        return r;
+        return true;
     }
     want(read, job, key);
-    throw Miss{};
+    return false;
 }
 
 void Policy::resolve(ChunkState& cs) {
@@ -588,8 +587,8 @@ void Policy::resolve(ChunkState& cs) {
 
 ExtJob Policy::nam_job(uint32_t read, const NamRec& cur, uint32_t kind) const {
     // jobs always carry the NAM as the GPU produced it (before any host-side flip)
-    const NamRec* b = bv_.nams + bv_.nam_off[read];
-    const NamRec* e = bv_.nams + bv_.nam_off[read + 1];
+    const NamRec* b = bv_->nams + bv_->nam_off[read];
+    const NamRec* e = bv_->nams + bv_->nam_off[read + 1];
     const NamRec* f = std::find_if(b, e, [&](const NamRec& x) { return x.nam_id == cur.nam_id; });
     const NamRec& n = f != e ? *f : cur;
     ExtJob j{};
@@ -602,7 +601,7 @@ ExtJob Policy::nam_job(uint32_t read, const NamRec& cur, uint32_t kind) const {
     j.query_end = n.query_end;
     j.is_revcomp = n.is_revcomp;
     // paired-end extension always uses SSW (src/mapper.rs:860-870); single-end follows --ssw
-    j.use_ssw = (bv_.paired || cfg_.mp.use_ssw) ? 1 : 0;
+    j.use_ssw = (bv_->paired || cfg_.mp.use_ssw) ? 1 : 0;
     j.nam = (uint32_t)(f != e ? f - b : 0);
     return j;
 }
@@ -642,23 +641,24 @@ Alignment Policy::to_alignment(const StoredResult& r, uint32_t ref_id) const {
     return a;
 }
 
-bool Policy::extend(uint32_t read, NamRec& nam, uint32_t kind, Alignment& out, bool& consistent) {
-    const StoredResult& r = get(read, nam_job(read, nam, kind), nam_key(nam, kind));
+int Policy::extend(uint32_t read, NamRec& nam, uint32_t kind, Alignment& out, bool& consistent) {
+    StoredResult r;
+    if (!get(read, nam_job(read, nam, kind), nam_key(nam, kind), r)) return MISSING;
     consistent = r.consistent != 0;
     if (kind == JOB_EXTEND_FULL) {
         nam.is_revcomp = r.nam_is_revcomp;
         nam.query_start = r.nam_query_start;
         nam.query_end = r.nam_query_end;
     }
-    if (!r.valid) return false;
+    if (!r.valid) return UNALIGNED;
     out = to_alignment(r, nam.ref_id);
-    return true;
+    return ALIGNED;
 }
 
 // rescue_align (src/mapper.rs:1094-1153): the window is fixed here, the
 // has_shared_substring filter and the alignment run on the GPU
 bool Policy::rescue_job(uint32_t read, const NamRec& mate, float mu, float sigma, ExtJob& j, JobKey& key) const {
-    const uint64_t rl = bv_.reads[read].len;
+    const uint64_t rl = bv_->reads[read].len;
     const uint64_t w = sat_usize(mu + 5.0f * sigma);
     uint64_t rs, re;
     bool rc;
@@ -689,14 +689,15 @@ bool Policy::rescue_job(uint32_t read, const NamRec& mate, float mu, float sigma
     return true;
 }
 
-bool Policy::rescue(uint32_t read, const NamRec& mate, float mu, float sigma, Alignment& out) {
+int Policy::rescue(uint32_t read, const NamRec& mate, float mu, float sigma, Alignment& out) {
     ExtJob j;
     JobKey key;
-    if (!rescue_job(read, mate, mu, sigma, j, key)) return false;
-    const StoredResult& r = get(read, j, key);
-    if (!r.valid) return false;
+    if (!rescue_job(read, mate, mu, sigma, j, key)) return UNALIGNED;
+    StoredResult r;
+    if (!get(read, j, key, r)) return MISSING;
+    if (!r.valid) return UNALIGNED;
     out = to_alignment(r, mate.ref_id);
-    return true;
+    return ALIGNED;
 }
 
 // Requests made on a miss for work a record will need once the missing results are
@@ -722,7 +723,7 @@ void Policy::want_rescue_chain(uint32_t read, const NamRec& nam, uint32_t mate, 
 
 // sort_nams (src/nam.rs:168-188): the GPU already applied the stable sort
 void Policy::sorted_nams(uint32_t read, Rng& rng, std::vector<NamRec>& v) const {
-    v.assign(bv_.nams + bv_.nam_off[read], bv_.nams + bv_.nam_off[read + 1]);
+    v.assign(bv_->nams + bv_->nam_off[read], bv_->nams + bv_->nam_off[read + 1]);
     if (!v.empty()) {
         size_t nb = 0;
         while (nb < v.size() && v[nb].score == v[0].score) nb++;
@@ -739,16 +740,16 @@ std::vector<NamRec> Policy::sorted_nams(uint32_t read, Rng& rng) const {
 
 // ------------------------------------------------------------------ single end
 // src/mapper.rs:349-528
-void Policy::se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mapped) {
+bool Policy::se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mapped) {
     const uint32_t read = (uint32_t)rec;
-    const ReadView& rv = bv_.reads[read];
+    const ReadView& rv = bv_->reads[read];
     std::vector<NamRec>& nams = sc_->nams[0];
     sorted_nams(read, rng, nams);
     Details details;
-    details.nam = bv_.details[read];
+    details.nam = bv_->details[read];
     if (nams.empty()) {
         if (cfg_.mp.output_unmapped && !speculative_) format_sam(unmapped_record(rv, details), cfg_, out);
-        return;
+        return true;
     }
     const float nam_max = nams[0].score;
     const size_t max_tries = cfg_.mp.max_tries;
@@ -765,15 +766,14 @@ void Policy::se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mappe
         if ((tries > 1 && best_edit == 0) || dropoff < cfg_.mp.dropoff_threshold) break;
         Alignment a;
         bool consistent;
-        bool ok;
-        try {
-            ok = extend(read, nam, JOB_EXTEND_FAST, a, consistent);
-        } catch (const Miss&) {
+        const int er = extend(read, nam, JOB_EXTEND_FAST, a, consistent);
+        if (er == MISSING) {
             // also request the next candidates this read may try
             for (size_t t = tries + 1; t < nams.size() && t < max_tries && t < tries + 4; t++)
                 if (nams[t].score / nam_max >= cfg_.mp.dropoff_threshold) want_nam(read, nams[t], JOB_EXTEND_FAST);
-            throw;
+            return false;
         }
+        const bool ok = er == ALIGNED;
         if (!consistent) {
             details.inconsistent_nams++;
             continue;
@@ -805,7 +805,7 @@ void Policy::se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mappe
     }
     if (!have_best) {
         if (cfg_.mp.output_unmapped && !speculative_) format_sam(unmapped_record(rv, details), cfg_, out);
-        return;
+        return true;
     }
     uint8_t mapq = (uint8_t)((60 * (best_score - second) + best_score - 1) / best_score);
     if (!speculative_) format_sam(mapped_record(*this, best, rv, mapq, false, details), cfg_, out);
@@ -823,18 +823,19 @@ void Policy::se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mappe
             if (!speculative_) format_sam(mapped_record(*this, a, rv, mapq, true, details), cfg_, out);
         }
     }
+    return true;
 }
 
 // ------------------------------------------------------------------ paired end
 // src/mapper.rs:624-1091
-void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out, uint64_t& mapped) {
+bool Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out, uint64_t& mapped) {
     const uint32_t rd[2] = {(uint32_t)(2 * rec), (uint32_t)(2 * rec + 1)};
-    const ReadView* rv[2] = {&bv_.reads[rd[0]], &bv_.reads[rd[1]]};
+    const ReadView* rv[2] = {&bv_->reads[rd[0]], &bv_->reads[rd[1]]};
     Details det[2];
     std::vector<NamRec>(&nams)[2] = sc_->nams;
     for (int i = 0; i < 2; i++) {
         sorted_nams(rd[i], rng, nams[i]);
-        det[i].nam = bv_.details[rd[i]];
+        det[i].nam = bv_->details[rd[i]];
     }
     for (int i = 0; i < 2; i++)
         if (!nams[i].empty()) want_nam(rd[i], nams[i][0], JOB_EXTEND_FAST);
@@ -845,7 +846,7 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
     bool fast = false;
     Alignment proper[2];
 
-    auto rescue_read = [&](int has, int other) {
+    auto rescue_read = [&](int has, int other) -> bool {
         // src/mapper.rs:1018-1091; det[has] / det[other] as the reference passes them
         std::vector<NamRec>& n1 = nams[has];
         float max1 = n1[0].score;
@@ -857,25 +858,30 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
             NamRec& nam = n1[t];
             if (nam.score / max1 < dropoff) break;
             Alignment a;
-            bool consistent;
-            bool ok;
-            try {
-                ok = extend(rd[has], nam, JOB_EXTEND_FULL, a, consistent);
-                det[has].inconsistent_nams += !consistent;
-                if (ok) {
-                    det[has].gapped += a.gapped;
-                    al1.push_back(a);
-                    det[has].tried_alignment++;
-                    Alignment b;
-                    bool okb = rescue(rd[other], nam, mu, sigma, b);
-                    if (okb) det[other].mate_rescue++;
-                    al2.emplace_back(okb, b);
-                }
-            } catch (const Miss&) {
-                // every later try is an extension and, when it aligns, a rescue
+            bool consistent = false;
+            // on a miss: every later try is an extension and, when it aligns, a rescue
+            auto prefetch_after = [&]() {
                 for (size_t u = t + 1; u < n1.size() && u < max_tries; u++)
                     if (n1[u].score / max1 >= dropoff) want_rescue_chain(rd[has], n1[u], rd[other], mu, sigma, true);
-                throw;
+            };
+            const int er = extend(rd[has], nam, JOB_EXTEND_FULL, a, consistent);
+            if (er == MISSING) {
+                prefetch_after();
+                return false;
+            }
+            det[has].inconsistent_nams += !consistent;
+            if (er == ALIGNED) {
+                det[has].gapped += a.gapped;
+                al1.push_back(a);
+                det[has].tried_alignment++;
+                Alignment b;
+                const int rr = rescue(rd[other], nam, mu, sigma, b);
+                if (rr == MISSING) {
+                    prefetch_after();
+                    return false;
+                }
+                if (rr == ALIGNED) det[other].mate_rescue++;
+                al2.emplace_back(rr == ALIGNED, b);
             }
         }
         for (auto& a1 : al1) {
@@ -906,13 +912,14 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
                 pairs.push_back(sp);
             }
         }
+        return true;
     };
 
     if (nams[0].empty() && nams[1].empty()) {
     } else if (!nams[0].empty() && nams[1].empty()) {
-        rescue_read(0, 1);
+        if (!rescue_read(0, 1)) return false;
     } else if (nams[0].empty() && !nams[1].empty()) {
-        rescue_read(1, 0);
+        if (!rescue_read(1, 0)) return false;
     } else {
         bool took_fast = false;
         if (top_dropoff(nams[0]) < dropoff && top_dropoff(nams[1]) < dropoff &&
@@ -921,8 +928,11 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
             Alignment a1, a2;
             bool c1, c2;
             want_nam(rd[1], m2, JOB_EXTEND_FAST);
-            bool ok1 = extend(rd[0], m1, JOB_EXTEND_FAST, a1, c1);
-            bool ok2 = extend(rd[1], m2, JOB_EXTEND_FAST, a2, c2);
+            const int e1 = extend(rd[0], m1, JOB_EXTEND_FAST, a1, c1);
+            if (e1 == MISSING) return false;
+            const int e2 = extend(rd[1], m2, JOB_EXTEND_FAST, a2, c2);
+            if (e2 == MISSING) return false;
+            const bool ok1 = e1 == ALIGNED, ok2 = e2 == ALIGNED;
             det[0].inconsistent_nams += !c1;
             det[1].inconsistent_nams += !c2;
             if (ok1 && ok2) {
@@ -946,7 +956,9 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
             for (int i = 0; i < 2; i++) {
                 Alignment a;
                 bool c;
-                bool ok = extend(rd[i], nams[i][0], JOB_EXTEND_FULL, a, c);
+                const int e = extend(rd[i], nams[i][0], JOB_EXTEND_FULL, a, c);
+                if (e == MISSING) return false;
+                const bool ok = e == ALIGNED;
                 det[i].inconsistent_nams += !c;
                 have_indv[i] = ok;
                 if (ok) indv[i] = a;
@@ -976,7 +988,6 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
                     }
                 }
             };
-            try {
             for (; cur < np.size(); cur++) {
                 auto& pr = np[cur];
                 float sd = pr.score / max_score;
@@ -993,8 +1004,13 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
                         auto it = std::find_if(cache[i].begin(), cache[i].end(),
                                                [&](auto& e) { return e.first == this_nam.nam_id; });
                         if (it == cache[i].end()) {
-                            bool c;
-                            ok = extend(rd[i], this_nam, JOB_EXTEND_FULL, a, c);
+                            bool c = false;
+                            const int e = extend(rd[i], this_nam, JOB_EXTEND_FULL, a, c);
+                            if (e == MISSING) {
+                                prefetch();
+                                return false;
+                            }
+                            ok = e == ALIGNED;
                             det[i].inconsistent_nams += !c;
                             det[i].tried_alignment++;
                             det[i].gapped += ok ? a.gapped : 0;
@@ -1006,13 +1022,22 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
                     } else {
                         NamRec other = *nm[1 - i];
                         // reverse_nam_if_needed on the partner, then rescue from it
-                        const StoredResult& fr = get(rd[1 - i], nam_job(rd[1 - i], other, JOB_EXTEND_FULL),
-                                                  nam_key(other, JOB_EXTEND_FULL));
+                        StoredResult fr;
+                        if (!get(rd[1 - i], nam_job(rd[1 - i], other, JOB_EXTEND_FULL),
+                                 nam_key(other, JOB_EXTEND_FULL), fr)) {
+                            prefetch();
+                            return false;
+                        }
                         det[1 - i].inconsistent_nams += !fr.consistent;
                         other.is_revcomp = fr.nam_is_revcomp;
                         other.query_start = fr.nam_query_start;
                         other.query_end = fr.nam_query_end;
-                        ok = rescue(rd[i], other, mu, sigma, a);
+                        const int rr = rescue(rd[i], other, mu, sigma, a);
+                        if (rr == MISSING) {
+                            prefetch();
+                            return false;
+                        }
+                        ok = rr == ALIGNED;
                         if (ok) {
                             det[i].mate_rescue++;
                             det[i].tried_alignment++;
@@ -1049,10 +1074,6 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
                 sp.a2 = a2;
                 pairs.push_back(sp);
                 n_out++;
-            }
-            } catch (const Miss&) {
-                prefetch();
-                throw;
             }
             if (have_indv[0] && have_indv[1]) {
                 ScoredPair sp;
@@ -1144,6 +1165,7 @@ void Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
     }
     if (cfg_.timing)
         cur_->seconds_format += std::chrono::duration<double>(std::chrono::steady_clock::now() - tf).count();
+    return true;
 }
 
 // ------------------------------------------------------------------ map-only / aemb
@@ -1302,24 +1324,24 @@ int best_paired_location(const std::vector<NamPairM>& pairs, const std::vector<N
 // src/maponly.rs:18-52
 void Policy::paf_se(uint64_t rec, Rng& rng, std::string& out) {
     std::vector<NamRec> nams = sorted_nams((uint32_t)rec, rng);
-    if (!nams.empty()) paf_line(*this, nams[0], bv_.reads[rec], 0, mapping_quality(nams), out);
+    if (!nams.empty()) paf_line(*this, nams[0], bv_->reads[rec], 0, mapping_quality(nams), out);
 }
 
 // src/maponly.rs:114-195
 void Policy::paf_pe(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out) {
     uint32_t a = (uint32_t)(2 * rec), b = a + 1;
-    std::vector<NamRec> n1 = unsorted_nams(bv_, a), n2 = unsorted_nams(bv_, b);
+    std::vector<NamRec> n1 = unsorted_nams(*bv_, a), n2 = unsorted_nams(*bv_, b);
     if (n1.empty() && n2.empty()) return;
-    std::vector<NamPairM> pairs = nam_pairs_maponly(n1, n2, isd.mu, isd.sigma, bv_.details[a].both_orientations,
-                                                    bv_.details[b].both_orientations);
+    std::vector<NamPairM> pairs = nam_pairs_maponly(n1, n2, isd.mu, isd.sigma, bv_->details[a].both_orientations,
+                                                    bv_->details[b].both_orientations);
     sort_nams_host(n1, rng);
     sort_nams_host(n2, rng);
     if (best_paired_location(pairs, n1, n2, isd)) {
-        paf_line(*this, pairs[0].n1, bv_.reads[a], 1, -1, out);
-        paf_line(*this, pairs[0].n2, bv_.reads[b], 2, -1, out);
+        paf_line(*this, pairs[0].n1, bv_->reads[a], 1, -1, out);
+        paf_line(*this, pairs[0].n2, bv_->reads[b], 2, -1, out);
     } else {
-        if (!n1.empty()) paf_line(*this, n1[0], bv_.reads[a], 1, -1, out);
-        if (!n2.empty()) paf_line(*this, n2[0], bv_.reads[b], 2, -1, out);
+        if (!n1.empty()) paf_line(*this, n1[0], bv_->reads[a], 1, -1, out);
+        if (!n2.empty()) paf_line(*this, n2[0], bv_->reads[b], 2, -1, out);
     }
 }
 
@@ -1328,31 +1350,31 @@ void Policy::aemb_se(uint64_t rec, Rng& rng) {
     std::vector<NamRec> nams = sorted_nams((uint32_t)rec, rng);
     size_t nb = 0;
     while (nb < nams.size() && nams[nb].score == nams[0].score) nb++;
-    double w = (double)bv_.reads[rec].len / (double)nb;
+    double w = (double)bv_->reads[rec].len / (double)nb;
     for (size_t i = 0; i < nb; i++) add_abundance(nams[i].ref_id, w);
 }
 
 // src/maponly.rs:198-261
 void Policy::aemb_pe(uint64_t rec, Rng& rng, InsertSize& isd) {
     uint32_t a = (uint32_t)(2 * rec), b = a + 1;
-    std::vector<NamRec> n1 = unsorted_nams(bv_, a), n2 = unsorted_nams(bv_, b);
+    std::vector<NamRec> n1 = unsorted_nams(*bv_, a), n2 = unsorted_nams(*bv_, b);
     if (n1.empty() && n2.empty()) return;
-    std::vector<NamPairM> pairs = nam_pairs_maponly(n1, n2, isd.mu, isd.sigma, bv_.details[a].both_orientations,
-                                                    bv_.details[b].both_orientations);
+    std::vector<NamPairM> pairs = nam_pairs_maponly(n1, n2, isd.mu, isd.sigma, bv_->details[a].both_orientations,
+                                                    bv_->details[b].both_orientations);
     sort_nams_host(n1, rng);
     sort_nams_host(n2, rng);
     if (best_paired_location(pairs, n1, n2, isd)) {
         double js = pairs[0].score;
         size_t nb = 0;
         while (nb < pairs.size() && pairs[nb].score == js) nb++;
-        double w1 = (double)bv_.reads[a].len / (double)nb, w2 = (double)bv_.reads[b].len / (double)nb;
+        double w1 = (double)bv_->reads[a].len / (double)nb, w2 = (double)bv_->reads[b].len / (double)nb;
         for (size_t i = 0; i < nb; i++) {
             add_abundance(pairs[i].n1.ref_id, w1);
             add_abundance(pairs[i].n2.ref_id, w2);
         }
     } else {
         const std::vector<NamRec>* lists[2] = {&n1, &n2};
-        uint32_t lens[2] = {bv_.reads[a].len, bv_.reads[b].len};
+        uint32_t lens[2] = {bv_->reads[a].len, bv_->reads[b].len};
         for (int t = 0; t < 2; t++) {
             const std::vector<NamRec>& n = *lists[t];
             size_t nb = 0;
@@ -1376,12 +1398,12 @@ void Policy::seed_requests(ChunkState& cs) {
             if (c.timing) cs.seconds_seed += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         }
     } acc{cfg_, cs, t0};
-    const bool paired = bv_.paired;
+    const bool paired = bv_->paired;
     for (uint64_t rec = cs.first; rec < cs.end; rec++) {
         for (int m = 0; m < (paired ? 2 : 1); m++) {
             uint32_t read = paired ? (uint32_t)(2 * rec + m) : (uint32_t)rec;
-            const NamRec* n = bv_.nams + bv_.nam_off[read];
-            size_t c = bv_.nam_off[read + 1] - bv_.nam_off[read];
+            const NamRec* n = bv_->nams + bv_->nam_off[read];
+            size_t c = bv_->nam_off[read + 1] - bv_->nam_off[read];
             if (!c) continue;
             size_t nb = 0;
             while (nb < c && n[nb].score == n[0].score) nb++;
@@ -1403,20 +1425,19 @@ void Policy::run_chunk(ChunkState& cs) {
     };
     const auto t_run = timing ? now() : std::chrono::steady_clock::time_point();
     cs.runs++;
-    auto one = [&](uint64_t rec, Rng& rng, InsertSize& isd, std::string& out, uint64_t& mapped) {
+    // false: the record stopped on a missing result
+    auto one = [&](uint64_t rec, Rng& rng, InsertSize& isd, std::string& out, uint64_t& mapped) -> bool {
         switch (cfg_.mp.mode) {
             case SA_MODE_SAM:
-                if (bv_.paired) pe_record(rec, rng, isd, out, mapped);
-                else se_record(rec, rng, out, mapped);
-                break;
+                return bv_->paired ? pe_record(rec, rng, isd, out, mapped) : se_record(rec, rng, out, mapped);
             case SA_MODE_PAF:
-                if (bv_.paired) paf_pe(rec, rng, isd, out);
+                if (bv_->paired) paf_pe(rec, rng, isd, out);
                 else paf_se(rec, rng, out);
-                break;
+                return true;
             default:
-                if (bv_.paired) aemb_pe(rec, rng, isd);
+                if (bv_->paired) aemb_pe(rec, rng, isd);
                 else aemb_se(rec, rng);
-                break;
+                return true;
         }
     };
     const bool capture = cfg_.mp.mode == SA_MODE_SAM || cfg_.mp.mode == SA_MODE_PAF;
@@ -1437,9 +1458,7 @@ void Policy::run_chunk(ChunkState& cs) {
         InsertSize isd = cs.isd;
         size_t out_len = cs.out.size(), ab_len = cs.abundance.size();
         uint64_t mapped = 0;
-        try {
-            one(cs.next, rng, isd, cs.out, mapped);
-        } catch (const Miss&) {
+        if (!one(cs.next, rng, isd, cs.out, mapped)) {
             cs.out.resize(out_len);
             cs.abundance.resize(ab_len);
             if (!cs.effects.empty()) {
@@ -1467,8 +1486,7 @@ void Policy::run_chunk(ChunkState& cs) {
                 auto& ef = cs.effects[rec - cs.first];
                 const size_t o0 = cs.spec_out.size();
                 speculative_ = !capture;  // when capturing, records are formatted into spec_out
-                try {
-                    one(rec, r2, i2, capture ? cs.spec_out : scratch, m2);
+                if (one(rec, r2, i2, capture ? cs.spec_out : scratch, m2)) {
                     ef.known = true;
                     ef.rng_delta = r2.state - srng.state;
                     ef.isd_update = i2.sample_size != sisd.sample_size;
@@ -1482,7 +1500,7 @@ void Policy::run_chunk(ChunkState& cs) {
                         ef.out_len = cs.spec_out.size() - o0;
                         ef.mapped = m2;
                     }
-                } catch (const Miss&) {
+                } else {
                     // keep the draws made before the miss; see above for the estimate
                     ef.known = false;
                     ef.has_output = false;

@@ -1,7 +1,8 @@
 // Host-side mapping policy: the sequential, per-chunk part of the reference's
 // mapping (src/mapper.rs, src/maponly.rs) that consumes GPU NAMs and GPU
-// extension results.  Missing extension results raise Miss; the batch driver then
-// runs another extension wave and resumes the chunk at the read that missed.
+// extension results.  A record whose extension result is missing requests it and
+// stops (the functions return MISSING / false up to the chunk loop); the batch driver
+// then runs another extension wave and resumes the chunk at the read that missed.
 #pragma once
 #include <cstdint>
 #include <cstring>
@@ -62,7 +63,6 @@ struct JobKey {
     }
 };
 
-struct Miss {};
 
 // Results of one extension wave copied back from the device: one ExtResult per
 // job, and the CIGAR ops they point into (ExtResult::cigar_offset).
@@ -192,8 +192,8 @@ class Policy {
   private:
     const PolicyConfig& cfg_;
     const std::vector<ContigInfo>& contigs_;
-    const BatchView& bv_;
-    ResultStore& store_;
+    const BatchView* bv_;
+    ResultStore* store_;
     ChunkState* cur_ = nullptr;
     bool speculative_ = false;
     struct Scratch;
@@ -204,11 +204,13 @@ class Policy {
 
     void want(uint32_t read, const ExtJob& job, const JobKey& key);
     const ResultStore::Entry* lookup(uint32_t read, const JobKey& key) const;
-    StoredResult get(uint32_t read, const ExtJob& job, const JobKey& key);
+    // the result of a job, or false after requesting it
+    bool get(uint32_t read, const ExtJob& job, const JobKey& key, StoredResult& out);
     void resolve(ChunkState& cs);
 
-    void se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mapped);
-    void pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out, uint64_t& mapped);
+    // false: stopped on a missing result (the record is evaluated again later)
+    bool se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mapped);
+    bool pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out, uint64_t& mapped);
     void paf_se(uint64_t rec, Rng& rng, std::string& out);
     void paf_pe(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out);
     void aemb_se(uint64_t rec, Rng& rng);
@@ -223,10 +225,18 @@ class Policy {
     Alignment to_alignment(const StoredResult& r, uint32_t ref_id) const;
     const PolicyConfig& cfg() const { return cfg_; }
     const std::vector<ContigInfo>& contigs() const { return contigs_; }
-    const BatchView& bv() const { return bv_; }
+    const BatchView& bv() const { return *bv_; }
+    // point the policy at another batch (a session's request) between chunk runs
+    void bind(const BatchView& bv, ResultStore& store) {
+        bv_ = &bv;
+        store_ = &store;
+    }
+    // results of extend / rescue: aligned, not aligned, or the job's result is missing
+    // (it has been requested)
+    enum { MISSING = -1, UNALIGNED = 0, ALIGNED = 1 };
     // extend_seed with the given consistency semantics; applies the flip to nam
-    bool extend(uint32_t read, NamRec& nam, uint32_t kind, Alignment& out, bool& consistent);
-    bool rescue(uint32_t read, const NamRec& mate, float mu, float sigma, Alignment& out);
+    int extend(uint32_t read, NamRec& nam, uint32_t kind, Alignment& out, bool& consistent);
+    int rescue(uint32_t read, const NamRec& mate, float mu, float sigma, Alignment& out);
     bool rescue_job(uint32_t read, const NamRec& mate, float mu, float sigma, ExtJob& j, JobKey& key) const;
     void want_rescue_chain(uint32_t read, const NamRec& nam, uint32_t mate, float mu, float sigma, bool need_valid);
     void want_nam(uint32_t read, const NamRec& n, uint32_t kind);

@@ -62,10 +62,20 @@ Session::Session(const sa_index* idx, const sa_refs* refs, const sa_chaining_par
     // SA_TRACE_WAVES=1: admissions and extension waves on stderr
     const char* tr = std::getenv("SA_TRACE_WAVES");
     trace_ = tr && *tr && *tr != '0';
+    // SA_MAX_WAVE_JOBS: extension jobs per wave at most (tuning)
+    if (const char* mw = std::getenv("SA_MAX_WAVE_JOBS")) max_wave_jobs_ = std::max<uint64_t>(1, std::strtoull(mw, nullptr, 10));
     t0_ = std::chrono::steady_clock::now();
     SA_CUDA(cudaSetDevice(idx->device));
     SA_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
-    SA_CUDA(cudaStreamCreateWithFlags(&sta_, cudaStreamNonBlocking));
+    // admissions at the highest stream priority: their blocks are dispatched ahead of
+    // queued wave blocks, so a new request's NAM pipeline does not wait behind a wave
+    int prio_least = 0, prio_greatest = 0;
+    SA_CUDA(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
+    const uint32_t n_lanes = std::max<uint32_t>(1, cfg_.admission_streams);
+    for (uint32_t l = 0; l < n_lanes; l++) {
+        lanes_.push_back(std::make_unique<AdmitLane>());
+        SA_CUDA(cudaStreamCreateWithPriority(&lanes_.back()->st, cudaStreamNonBlocking, prio_greatest));
+    }
     const auto& cs = refs->contigs;
     const uint32_t nc = (uint32_t)cs.size();
     std::vector<uint64_t> woff(nc);
@@ -101,7 +111,10 @@ Session::Session(const sa_index* idx, const sa_refs* refs, const sa_chaining_par
     off_alloc_.reset(slots);
     unsigned nt = cfg_.policy_threads ? cfg_.policy_threads : std::max(1u, std::thread::hardware_concurrency());
     engine_ = std::thread([this] { engine(); });
-    admitter_ = std::thread([this] { admitter(); });
+    for (auto& l : lanes_) {
+        AdmitLane* lp = l.get();
+        l->th = std::thread([this, lp] { admitter(*lp); });
+    }
     for (unsigned t = 0; t < nt; t++) workers_.emplace_back([this] { worker(); });
 }
 
@@ -119,7 +132,8 @@ Session::~Session() {
     cv_engine_.notify_all();
     cv_admit_.notify_all();
     cv_done_.notify_all();
-    if (admitter_.joinable()) admitter_.join();
+    for (auto& l : lanes_)
+        if (l->th.joinable()) l->th.join();
     if (engine_.joinable()) engine_.join();
     {
         std::lock_guard<std::mutex> g(mu_);
@@ -128,7 +142,8 @@ Session::~Session() {
     cv_work_.notify_all();
     for (auto& t : workers_) t.join();
     if (st_) cudaStreamDestroy(st_);
-    if (sta_) cudaStreamDestroy(sta_);
+    for (auto& l : lanes_)
+        if (l->st) cudaStreamDestroy(l->st);
 }
 
 uint64_t Session::submit(const sa_read_batch* r1, const sa_read_batch* r2) {
@@ -250,9 +265,18 @@ void Session::engine() {
         auto wave_ok = [&]() { return !waiting_.empty() && (waiting_jobs_ >= wave_min_jobs_ || idle()); };
         cv_engine_.wait(lk, [&] { return broken_ || (stop_ && inflight_ == 0 && !admitting_) || wave_ok(); });
         if (broken_ || (stop_ && inflight_ == 0 && !admitting_)) break;
-        batch.swap(waiting_);
-        waiting_.clear();
-        waiting_jobs_ = 0;
+        // at most max_wave_jobs_ per wave (at least one chunk), as in Mapper::schedule
+        batch.clear();
+        size_t k = 0;
+        uint64_t taken = 0;
+        while (k < waiting_.size()) {
+            const uint64_t nj = waiting_[k].first->chunks[waiting_[k].second].pending.size();
+            if (!batch.empty() && taken + nj > max_wave_jobs_) break;
+            taken += nj;
+            batch.push_back(waiting_[k++]);
+        }
+        waiting_.erase(waiting_.begin(), waiting_.begin() + (ptrdiff_t)k);
+        waiting_jobs_ -= taken;
         lk.unlock();
         try {
             const auto tw = std::chrono::steady_clock::now();
@@ -277,7 +301,7 @@ void Session::engine() {
 
 // Admission: reads into the arena and the NAM pipeline, on a second stream so that
 // it overlaps the waves of the requests already in flight.
-void Session::admitter() {
+void Session::admitter(AdmitLane& lane) {
     std::unique_lock<std::mutex> lk(mu_);
     for (;;) {
         auto can_admit = [&]() {
@@ -295,14 +319,14 @@ void Session::admitter() {
         seq_alloc_.alloc(std::max<uint64_t>(r->total_bases, 1), r->seq_base);
         off_alloc_.alloc(r->n_reads + 1, r->read_base);
         inflight_++;
-        admitting_ = true;
+        admitting_++;
         r->state = 1;
         r->t_admit = std::chrono::steady_clock::now();
         live_[r->id] = std::move(rq);
         lk.unlock();
         try {
             const auto ta = std::chrono::steady_clock::now();
-            admit(*r);
+            admit(*r, lane);
             if (trace_)
                 std::fprintf(stderr, "sa_admit t=%.4f dur=%.4f id=%llu reads=%llu chunks=%zu\n",
                              std::chrono::duration<double>(ta - t0_).count(),
@@ -310,12 +334,12 @@ void Session::admitter() {
                              (unsigned long long)r->id, (unsigned long long)r->n_reads, r->chunks.size());
         } catch (const std::exception& e) {
             lk.lock();
-            admitting_ = false;
+            admitting_--;
             fail_all(e.what(), dynamic_cast<const Error*>(&e) ? static_cast<const Error&>(e).code : SA_ERR_CUDA);
             return;
         }
         lk.lock();
-        admitting_ = false;
+        admitting_--;
         if (r->chunks.empty()) {
             lk.unlock();
             complete(*r);
@@ -329,24 +353,24 @@ void Session::admitter() {
     cv_engine_.notify_all();
 }
 
-void Session::admit(Request& r) {
+void Session::admit(Request& r, AdmitLane& lane) {
     const uint32_t n = (uint32_t)r.n_reads;
     if (n == 0) return;
     const auto ta = std::chrono::steady_clock::now();
     // reads: pinned staging, local offsets for the NAM pipeline, arena copy for the extension
-    h_seq_.reserve(r.total_bases + 16);
-    h_off_.reserve((size_t)n + 1);
-    std::memcpy(h_seq_.p, r.seq.data(), r.total_bases);
-    std::memcpy(h_off_.p, r.seq_off.data(), ((size_t)n + 1) * 8);
-    nws_.seq.reserve(r.total_bases + 16);
-    nws_.off.reserve((size_t)n + 1);
-    SA_CUDA(cudaMemcpyAsync(nws_.seq.p, h_seq_.p, r.total_bases, cudaMemcpyHostToDevice, sta_));
-    SA_CUDA(cudaMemcpyAsync(nws_.off.p, h_off_.p, ((size_t)n + 1) * 8, cudaMemcpyHostToDevice, sta_));
-    SA_CUDA(cudaMemcpyAsync(arena_seq_.p + r.seq_base, nws_.seq.p, r.total_bases, cudaMemcpyDeviceToDevice, sta_));
-    h_goff_.resize((size_t)n + 1);
-    for (uint32_t i = 0; i <= n; i++) h_goff_[i] = r.seq_base + r.seq_off[i];
-    SA_CUDA(cudaMemcpyAsync(arena_off_.p + r.read_base, h_goff_.data(), ((size_t)n + 1) * 8,
-                            cudaMemcpyHostToDevice, sta_));
+    lane.h_seq.reserve(r.total_bases + 16);
+    lane.h_off.reserve((size_t)n + 1);
+    std::memcpy(lane.h_seq.p, r.seq.data(), r.total_bases);
+    std::memcpy(lane.h_off.p, r.seq_off.data(), ((size_t)n + 1) * 8);
+    lane.nws.seq.reserve(r.total_bases + 16);
+    lane.nws.off.reserve((size_t)n + 1);
+    SA_CUDA(cudaMemcpyAsync(lane.nws.seq.p, lane.h_seq.p, r.total_bases, cudaMemcpyHostToDevice, lane.st));
+    SA_CUDA(cudaMemcpyAsync(lane.nws.off.p, lane.h_off.p, ((size_t)n + 1) * 8, cudaMemcpyHostToDevice, lane.st));
+    SA_CUDA(cudaMemcpyAsync(arena_seq_.p + r.seq_base, lane.nws.seq.p, r.total_bases, cudaMemcpyDeviceToDevice, lane.st));
+    lane.h_goff.resize((size_t)n + 1);
+    for (uint32_t i = 0; i <= n; i++) lane.h_goff[i] = r.seq_base + r.seq_off[i];
+    SA_CUDA(cudaMemcpyAsync(arena_off_.p + r.read_base, lane.h_goff.data(), ((size_t)n + 1) * 8,
+                            cudaMemcpyHostToDevice, lane.st));
     NamConfig cfg;
     cfg.cp = ChainParams{cp_.max_lookback, cp_.diag_diff_penalty, cp_.gap_length_penalty, cp_.valid_score_threshold,
                          cp_.max_ref_gap, cp_.matches_weight, cp_.max_diagonal_ratio};
@@ -355,38 +379,38 @@ void Session::admit(Request& r) {
     cfg.nam_anchors = !r.paired && mp_.mode == SA_MODE_SAM && !mp_.use_ssw;
     if (trace_) {
         // the staging copies above complete first, so that the pipeline's time is its own
-        SA_CUDA(cudaStreamSynchronize(sta_));
+        SA_CUDA(cudaStreamSynchronize(lane.st));
     }
     const auto tp1 = std::chrono::steady_clock::now();
     KernelTimers kt;
     kt.enabled = trace_;
     run_nam_pipeline(idx_->view(), refs_view_, cfg, n, r.total_bases, max_contig_len_,
-                     (uint32_t)refs_->contigs.size(), nws_, sta_, &kt);
+                     (uint32_t)refs_->contigs.size(), lane.nws, lane.st, &kt);
     if (trace_) {
-        SA_CUDA(cudaStreamSynchronize(sta_));
+        SA_CUDA(cudaStreamSynchronize(lane.st));
         kt.collect();
         std::fprintf(stderr, "sa_admit_kernels id=%llu seed=%.3f hits=%.3f anchors=%.3f sort=%.3f chain=%.3f other=%.3f\n",
                      (unsigned long long)r.id, kt.ms[KS_SEED], kt.ms[KS_HITS], kt.ms[KS_ANCHORS], kt.ms[KS_SORT],
                      kt.ms[KS_CHAIN], kt.ms[KS_NAMS_OTHER]);
     }
     const auto tp2 = std::chrono::steady_clock::now();
-    const uint64_t tn = nws_.last_total_nams;
+    const uint64_t tn = lane.nws.last_total_nams;
     if (cfg.nam_anchors) {
-        const uint64_t ta = nws_.last_total_nam_anchors;
+        const uint64_t ta = lane.nws.last_total_nam_anchors;
         r.nam_anc_off.resize(tn + 1);
         r.nam_anc.resize(ta);
-        SA_CUDA(cudaMemcpyAsync(r.nam_anc_off.data(), nws_.nam_anc_off.p, (tn + 1) * 8, cudaMemcpyDeviceToHost, sta_));
-        if (ta) SA_CUDA(cudaMemcpyAsync(r.nam_anc.data(), nws_.nam_anc.p, ta * 8, cudaMemcpyDeviceToHost, sta_));
+        SA_CUDA(cudaMemcpyAsync(r.nam_anc_off.data(), lane.nws.nam_anc_off.p, (tn + 1) * 8, cudaMemcpyDeviceToHost, lane.st));
+        if (ta) SA_CUDA(cudaMemcpyAsync(r.nam_anc.data(), lane.nws.nam_anc.p, ta * 8, cudaMemcpyDeviceToHost, lane.st));
         r.d2h_bytes += (tn + 1) * 8 + ta * 8;
     }
     r.nam_off.resize((size_t)n + 1);
     r.nams.resize(tn);
     r.details.resize(n);
-    SA_CUDA(cudaMemcpyAsync(r.nam_off.data(), nws_.nam_off.p, ((size_t)n + 1) * 8, cudaMemcpyDeviceToHost, sta_));
-    if (tn) SA_CUDA(cudaMemcpyAsync(r.nams.data(), nws_.nams.p, tn * sizeof(NamRec), cudaMemcpyDeviceToHost, sta_));
-    SA_CUDA(cudaMemcpyAsync(r.details.data(), nws_.details.p, (size_t)n * sizeof(NamDetailsRec),
-                            cudaMemcpyDeviceToHost, sta_));
-    SA_CUDA(cudaStreamSynchronize(sta_));
+    SA_CUDA(cudaMemcpyAsync(r.nam_off.data(), lane.nws.nam_off.p, ((size_t)n + 1) * 8, cudaMemcpyDeviceToHost, lane.st));
+    if (tn) SA_CUDA(cudaMemcpyAsync(r.nams.data(), lane.nws.nams.p, tn * sizeof(NamRec), cudaMemcpyDeviceToHost, lane.st));
+    SA_CUDA(cudaMemcpyAsync(r.details.data(), lane.nws.details.p, (size_t)n * sizeof(NamDetailsRec),
+                            cudaMemcpyDeviceToHost, lane.st));
+    SA_CUDA(cudaStreamSynchronize(lane.st));
     r.h2d_bytes += r.total_bases + 2 * ((uint64_t)n + 1) * 8;
     r.d2h_bytes += ((uint64_t)n + 1) * 8 + tn * sizeof(NamRec) + (uint64_t)n * sizeof(NamDetailsRec);
     r.bv.nams = r.nams.data();
@@ -395,8 +419,8 @@ void Session::admit(Request& r) {
     if (cfg.nam_anchors) {
         r.bv.nam_anc_off = r.nam_anc_off.data();
         r.bv.nam_anc = r.nam_anc.data();
-        r.bv.anc_qbits = nws_.anchor_qbits;
-        r.bv.anc_pbits = nws_.anchor_pbits;
+        r.bv.anc_qbits = lane.nws.anchor_qbits;
+        r.bv.anc_pbits = lane.nws.anchor_pbits;
     }
     // chunks (src/main.rs:591-604)
     const bool paired = r.paired;
@@ -477,6 +501,11 @@ void Session::run_wave(std::vector<std::pair<Request*, size_t>>& batch) {
 }
 
 void Session::worker() {
+    // one policy per thread, bound to each chunk's request in turn (its buffers are
+    // reused across records and requests)
+    BatchView none;
+    ResultStore none_store;
+    Policy policy(pcfg_, contigs_, none, none_store);
     std::unique_lock<std::mutex> lk(mu_);
     for (;;) {
         cv_work_.wait(lk, [&] { return workers_stop_ || !ready_.empty(); });
@@ -492,7 +521,7 @@ void Session::worker() {
         lk.unlock();
         std::string err;
         try {
-            Policy policy(pcfg_, contigs_, r->bv, r->store);
+            policy.bind(r->bv, r->store);
             if (first) policy.seed_requests(cs);
             else policy.run_chunk(cs);
         } catch (const std::exception& e) {

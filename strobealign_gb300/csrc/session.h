@@ -78,6 +78,19 @@ struct SessionConfig {
     uint64_t max_inflight_bases = 1ull << 30;
     uint32_t max_inflight_requests = 0;  // 0 = no limit
     uint32_t policy_threads = 0;         // 0 = all host threads
+    uint32_t admission_streams = 2;      // requests admitted concurrently (NAM pipelines in flight)
+};
+
+// One admission lane: a thread with its own stream, NAM workspace and staging, so that
+// the NAM pipelines of several requests run at once (a request's pipeline ends with its
+// slowest read orientation; concurrent lanes fill the GPU meanwhile).
+struct AdmitLane {
+    cudaStream_t st = nullptr;
+    NamWorkspace nws;
+    PinnedBuf<uint8_t> h_seq;
+    PinnedBuf<uint64_t> h_off;
+    std::vector<uint64_t> h_goff;
+    std::thread th;
 };
 
 class Session {
@@ -96,9 +109,9 @@ class Session {
 
   private:
     void engine();
-    void admitter();
+    void admitter(AdmitLane& lane);
     void worker();
-    void admit(Request& r);
+    void admit(Request& r, AdmitLane& lane);
     void run_wave(std::vector<std::pair<Request*, size_t>>& batch);
     void complete(Request& r);
     void fail_all(const std::string& msg, int32_t code);
@@ -113,21 +126,17 @@ class Session {
     std::vector<ContigInfo> contigs_;
     uint32_t max_contig_len_ = 0;
     cudaStream_t st_ = nullptr;   // extension waves
-    cudaStream_t sta_ = nullptr;  // admissions
+    std::vector<std::unique_ptr<AdmitLane>> lanes_;
     DevBuf<uint64_t> d_words_, d_woff_;
     DevBuf<uint32_t> d_clen_;
     DevRefs refs_view_{};
-    NamWorkspace nws_;
     ExtWorkspace ews_;
-    PinnedBuf<uint8_t> h_seq_;
-    PinnedBuf<uint64_t> h_off_;
     PinnedBuf<ExtJob> h_jobs_;
     std::vector<uint32_t> wave_anchors_;
     // read arena
     DevBuf<uint8_t> arena_seq_;
     DevBuf<uint64_t> arena_off_;
     RangeAllocator seq_alloc_, off_alloc_;
-    std::vector<uint64_t> h_goff_;
 
     mutable std::mutex mu_;
     std::condition_variable cv_engine_, cv_admit_, cv_work_, cv_done_;
@@ -141,16 +150,17 @@ class Session {
     uint32_t inflight_ = 0;
     bool stop_ = false;
     bool workers_stop_ = false;
-    bool admitting_ = false;
+    unsigned admitting_ = 0;  // admissions in progress
     bool broken_ = false;  // a device or internal error failed every request
     std::string broken_msg_;
     // failed requests stay allocated until the session is destroyed: queued work
     // items may still point at them
     std::vector<std::unique_ptr<Request>> graveyard_;
     uint64_t wave_min_jobs_ = 32768;
+    uint64_t max_wave_jobs_ = 262144;
     bool trace_ = false;
     std::chrono::steady_clock::time_point t0_;
-    std::thread engine_, admitter_;
+    std::thread engine_;
     std::vector<std::thread> workers_;
 };
 

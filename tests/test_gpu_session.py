@@ -72,7 +72,8 @@ def test_session_admission_limits(setup):
     reqs = _requests(sa, r1, r2)
     want = _alone(sa, refs, idx, reqs, use_ssw=1)
     # an arena of 4 Mbases admits only a few requests at a time; one request in flight at most
-    for kw in (dict(max_inflight_bases=4_000_000), dict(max_inflight_requests=1, policy_threads=3)):
+    for kw in (dict(max_inflight_bases=4_000_000), dict(max_inflight_requests=1, policy_threads=3),
+               dict(admission_streams=1), dict(admission_streams=4, max_inflight_bases=8_000_000)):
         s = sa.Session(idx, refs, use_ssw=1, **kw)
         tickets = [s.submit(x, y) for x, y in reqs]
         for i, t in enumerate(tickets):
