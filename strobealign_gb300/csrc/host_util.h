@@ -8,31 +8,34 @@
 
 namespace sa {
 
-// Concatenates parts into dst with up to `threads` threads, each copying a run of
-// consecutive parts of about equal total size.
-inline void parallel_concat(const std::vector<const std::string*>& parts, char* dst, unsigned threads) {
-    size_t total = 0;
-    for (auto* p : parts) total += p->size();
-    threads = std::max(1u, std::min<unsigned>(threads, (unsigned)parts.size()));
+// One copy of every chunk's output pieces into dst with up to `threads` threads,
+// each copying a run of consecutive pieces of about equal total size.
+template <class Chunk>
+inline void gather_chunk_outputs(const std::vector<Chunk>& chunks, char* dst, unsigned threads) {
+    struct Seg {
+        const char* src;
+        size_t len;
+    };
+    std::vector<Seg> segs;
+    for (const auto& c : chunks)
+        for (const auto& p : c.pieces) segs.push_back(Seg{(p.spec ? c.spec_out.data() : c.out.data()) + p.off, p.len});
+    std::vector<size_t> start(segs.size() + 1, 0);
+    for (size_t i = 0; i < segs.size(); i++) start[i + 1] = start[i] + segs[i].len;
+    const size_t total = start.back();
+    threads = std::max(1u, std::min<unsigned>(threads, (unsigned)std::max<size_t>(segs.size(), 1)));
     if (threads == 1 || total < (8u << 20)) {
-        size_t o = 0;
-        for (auto* p : parts) {
-            std::memcpy(dst + o, p->data(), p->size());
-            o += p->size();
-        }
+        for (size_t i = 0; i < segs.size(); i++) std::memcpy(dst + start[i], segs[i].src, segs[i].len);
         return;
     }
-    std::vector<size_t> start(parts.size() + 1, 0);
-    for (size_t i = 0; i < parts.size(); i++) start[i + 1] = start[i] + parts[i]->size();
     std::vector<std::thread> th;
     size_t first = 0;
-    for (unsigned t = 0; t < threads && first < parts.size(); t++) {
+    for (unsigned t = 0; t < threads && first < segs.size(); t++) {
         const size_t goal = total * (t + 1) / threads;
         size_t last = first;
-        while (last < parts.size() && (start[last + 1] <= goal || last == first)) last++;
-        if (t + 1 == threads) last = parts.size();
+        while (last < segs.size() && (start[last + 1] <= goal || last == first)) last++;
+        if (t + 1 == threads) last = segs.size();
         th.emplace_back([&, first, last] {
-            for (size_t i = first; i < last; i++) std::memcpy(dst + start[i], parts[i]->data(), parts[i]->size());
+            for (size_t i = first; i < last; i++) std::memcpy(dst + start[i], segs[i].src, segs[i].len);
         });
         first = last;
     }

@@ -422,17 +422,12 @@ void Mapper::map_uploaded(sa_output* out) {
     size_t total_len = 0;
     uint64_t mapped = 0;
     for (auto& c : chunks) {
-        total_len += c.out.size();
+        total_len += c.out_bytes;
         mapped += c.mapped;
     }
     out->data = (char*)std::malloc(total_len + 1);
     if (!out->data) throw Error(SA_ERR_OOM, "output allocation failed");
-    {
-        std::vector<const std::string*> parts;
-        parts.reserve(chunks.size());
-        for (auto& c : chunks) parts.push_back(&c.out);
-        parallel_concat(parts, out->data, policy_threads_);
-    }
+    gather_chunk_outputs(chunks, out->data, policy_threads_);
     out->data[total_len] = 0;
     out->len = total_len;
     out->n_reads = bv.reads.size();

@@ -444,44 +444,9 @@ struct AnchorPack {
     }
 };
 
-// add_to_anchors_full / add_to_anchors_partial (src/chainer.rs:304-366): counts when
-// out == nullptr, otherwise writes the anchors
-__device__ __forceinline__ uint32_t hit_anchors(const DevIndex& ix, uint64_t pos, uint32_t info, uint64_t hash,
-                                                uint32_t qs, uint32_t qe, AnchorPack ap, uint64_t* out) {
-    const uint32_t k = ix.p.k;
-    uint32_t cnt = 0;
-    if (info & 2) {
-        uint64_t e = idx_get_masked_from(ix, hash, ix.p.fwd_main_mask, true, pos);
-        if (e == UINT64_MAX) return 0;
-        uint64_t fh = load_rs(ix.rs, e).hash_offset & ix.p.fwd_main_mask;
-        for (uint64_t i = e; i < ix.n; i++) {
-            RefRandstrobe rr = load_rs(ix.rs, i);
-            if ((rr.hash_offset & ix.p.fwd_main_mask) != fh) break;
-            if (out) out[cnt] = ap.key(rr.ref_index, rr.position, qs);
-            cnt++;
-        }
-    } else {
-        uint64_t fh = load_hash(ix.rs, pos);
-        uint32_t minld = 0xffffffffu;
-        const uint32_t ql = qe - qs;
-        for (uint64_t i = pos; i < ix.n; i++) {
-            RefRandstrobe rr = load_rs(ix.rs, i);
-            if (rs_hash(rr) != fh) break;
-            uint32_t rl = (uint32_t)(rr.hash_offset & 0xff) + k;
-            uint32_t ld = ql > rl ? ql - rl : rl - ql;
-            if (ld <= minld) {
-                if (out) {
-                    out[cnt] = ap.key(rr.ref_index, rr.position, qs);
-                    out[cnt + 1] = ap.key(rr.ref_index, rr.position + rl - k, qe - k);
-                }
-                cnt += 2;
-                minld = ld;
-            }
-        }
-    }
-    return cnt;
-}
-
+// add_to_anchors_full / add_to_anchors_partial (src/chainer.rs:304-366) are split into
+// run_head (one lane, the first 32 entries of a run) and warp_run_anchors (the rest).
+//
 // A hit's run of equal-hash table entries: its first entry and hash (full hits:
 // the entry found; partial hits: get_masked_from with the forward main mask).  False
 // when a partial hit has no entry under that mask.
@@ -498,21 +463,45 @@ __device__ __forceinline__ bool hit_run(const DevIndex& ix, uint64_t pos, uint32
     return true;
 }
 
-// more than 32 entries in the run: the warp enumerates it together
-__device__ __forceinline__ bool run_is_long(const DevIndex& ix, uint64_t start, uint64_t fh, bool partial) {
-    const uint64_t i = start + 32;
-    if (i >= ix.n) return false;
-    const uint64_t h = partial ? (load_rs(ix.rs, i).hash_offset & ix.p.fwd_main_mask) : load_hash(ix.rs, i);
-    return h == fh;
+// The first 32 entries of a run by one lane (hit_anchors' loop): anchors to out (if
+// not null), their count, the running minimum length difference (full hits).  True
+// when the run ended within them; otherwise the warp continues from start + 32.
+__device__ __forceinline__ bool run_head(const DevIndex& ix, uint64_t start, uint64_t fh, bool partial, uint32_t qs,
+                                         uint32_t qe, AnchorPack ap, uint64_t* out, uint32_t& cnt, uint32_t& minld) {
+    const uint32_t k = ix.p.k, ql = qe - qs;
+    cnt = 0;
+    minld = 0xffffffffu;
+    const uint64_t end = start + 32 < ix.n ? start + 32 : ix.n;
+    for (uint64_t i = start; i < end; i++) {
+        const RefRandstrobe rr = load_rs(ix.rs, i);
+        if (partial) {
+            if ((rr.hash_offset & ix.p.fwd_main_mask) != fh) return true;
+            if (out) out[cnt] = ap.key(rr.ref_index, rr.position, qs);
+            cnt++;
+        } else {
+            if (rs_hash(rr) != fh) return true;
+            const uint32_t rl = (uint32_t)(rr.hash_offset & 0xff) + k;
+            const uint32_t ld = ql > rl ? ql - rl : rl - ql;
+            if (ld <= minld) {
+                if (out) {
+                    out[cnt] = ap.key(rr.ref_index, rr.position, qs);
+                    out[cnt + 1] = ap.key(rr.ref_index, rr.position + rl - k, qe - k);
+                }
+                cnt += 2;
+                minld = ld;
+            }
+        }
+    }
+    return end == ix.n;
 }
 
 // hit_anchors for one run by the whole warp (arguments uniform across the warp): lanes
 // take consecutive entries; the running-minimum length filter of full hits becomes a
 // prefix minimum over the lanes carried between 32-entry slices.
 __device__ uint32_t warp_run_anchors(const DevIndex& ix, uint64_t start, uint64_t fh, bool partial, uint32_t qs,
-                                     uint32_t qe, AnchorPack ap, uint64_t* out) {
+                                     uint32_t qe, AnchorPack ap, uint64_t* out, uint32_t carry) {
     const uint32_t lane = lane_id(), k = ix.p.k, ql = qe - qs;
-    uint32_t cnt = 0, carry = 0xffffffffu;
+    uint32_t cnt = 0;
     for (uint64_t c = start;; c += 32) {
         const uint64_t i = c + lane;
         bool valid = false;
@@ -582,7 +571,7 @@ __global__ void __launch_bounds__(256) k_anchors(DevIndex ix, const uint64_t* __
             uint32_t sum = 0;
             for (uint32_t c = 0; c < nh; c += 32) {
                 uint32_t h = c + lane;
-                uint32_t cnt = 0;
+                uint32_t cnt = 0, head = 0, minld = 0xffffffffu;
                 uint32_t info = 0, qs = 0, qe = 0;
                 uint64_t start = 0, fh = 0;
                 bool has_run = false, is_long = false;
@@ -593,34 +582,30 @@ __global__ void __launch_bounds__(256) k_anchors(DevIndex ix, const uint64_t* __
                         qs = qr_start[b + ri];
                         qe = (info & 2) ? qs + ix.p.k : qr_end[b + ri];
                         has_run = hit_run(ix, hit_pos[b + h], info, qr_hash[b + ri], start, fh);
-                        is_long = has_run && run_is_long(ix, start, fh, info & 2);
                         if (FILL) cnt = hit_anchors_n[b + h];
-                        else if (has_run && !is_long) cnt = hit_anchors(ix, hit_pos[b + h], info, qr_hash[b + ri], qs, qe, ap, nullptr);
                     }
                 }
-                // long runs: counted by the whole warp, one hit at a time
+                uint32_t tot = 0, ex = 0;
+                if (FILL) ex = warp_excl_scan(cnt, tot);
+                // each lane its run's first 32 entries; longer runs continue with the
+                // whole warp, one hit at a time
+                if (has_run)
+                    is_long = !run_head(ix, start, fh, info & 2, qs, qe, ap, FILL ? anchors + acc + ex : nullptr, head,
+                                        minld);
                 const uint32_t lm = __ballot_sync(FULL, is_long);
-                if (!FILL) {
-                    for (uint32_t m = lm; m; m &= m - 1) {
-                        const int L = __ffs(m) - 1;
-                        const uint32_t c2 = warp_run_anchors(ix, __shfl_sync(FULL, start, L), __shfl_sync(FULL, fh, L),
-                                                             __shfl_sync(FULL, info, L) & 2, __shfl_sync(FULL, qs, L),
-                                                             __shfl_sync(FULL, qe, L), ap, nullptr);
-                        if (lane == (uint32_t)L) cnt = c2;
-                    }
-                    if (h < nh && !(info & 4)) hit_anchors_n[b + h] = cnt;
+                for (uint32_t m = lm; m; m &= m - 1) {
+                    const int L = __ffs(m) - 1;
+                    const uint32_t hL = __shfl_sync(FULL, head, L);
+                    const uint32_t rest = warp_run_anchors(
+                        ix, __shfl_sync(FULL, start, L) + 32, __shfl_sync(FULL, fh, L), __shfl_sync(FULL, info, L) & 2,
+                        __shfl_sync(FULL, qs, L), __shfl_sync(FULL, qe, L), ap,
+                        FILL ? anchors + acc + __shfl_sync(FULL, ex, L) + hL : nullptr, __shfl_sync(FULL, minld, L));
+                    if (lane == (uint32_t)L) head += rest;
                 }
-                uint32_t tot;
-                uint32_t ex = warp_excl_scan(cnt, tot);
-                if (FILL) {
-                    if (cnt && !is_long)
-                        hit_anchors(ix, hit_pos[b + h], info, qr_hash[b + (info >> 3)], qs, qe, ap, anchors + acc + ex);
-                    for (uint32_t m = lm; m; m &= m - 1) {
-                        const int L = __ffs(m) - 1;
-                        warp_run_anchors(ix, __shfl_sync(FULL, start, L), __shfl_sync(FULL, fh, L),
-                                         __shfl_sync(FULL, info, L) & 2, __shfl_sync(FULL, qs, L),
-                                         __shfl_sync(FULL, qe, L), ap, anchors + acc + __shfl_sync(FULL, ex, L));
-                    }
+                if (!FILL) {
+                    cnt = head;
+                    if (h < nh && !(info & 4)) hit_anchors_n[b + h] = cnt;
+                    ex = warp_excl_scan(cnt, tot);
                 }
                 acc += tot;
                 sum += tot;

@@ -1445,7 +1445,7 @@ void Policy::run_chunk(ChunkState& cs) {
         if (capture && !cs.effects.empty()) {
             const auto& ef = cs.effects[cs.next - cs.first];
             if (ef.has_output && ef.pre_rng == cs.rng.state && ef.pre_isd.same_state(cs.isd)) {
-                cs.out.append(cs.spec_out, ef.out_off, ef.out_len);
+                cs.add_piece(true, ef.out_off, ef.out_len);
                 cs.rng.state += ef.rng_delta;
                 cs.isd = ef.post_isd;
                 cs.mapped += ef.mapped;
@@ -1458,7 +1458,9 @@ void Policy::run_chunk(ChunkState& cs) {
         InsertSize isd = cs.isd;
         size_t out_len = cs.out.size(), ab_len = cs.abundance.size();
         uint64_t mapped = 0;
-        if (!one(cs.next, rng, isd, cs.out, mapped)) {
+        const bool done_rec = one(cs.next, rng, isd, cs.out, mapped);
+        if (done_rec) cs.add_piece(false, out_len, cs.out.size() - out_len);
+        if (!done_rec) {
             cs.out.resize(out_len);
             cs.abundance.resize(ab_len);
             if (!cs.effects.empty()) {
@@ -1477,7 +1479,18 @@ void Policy::run_chunk(ChunkState& cs) {
             InsertSize sisd = isd;
             std::string scratch;
             std::vector<uint64_t> todo;
-            if (cs.effects.empty()) cs.effects.resize(cs.end - cs.first);
+            if (cs.effects.empty()) {
+                cs.effects.resize(cs.end - cs.first);
+                if (capture) {
+                    // room for the captured records (SEQ and QUAL plus the fixed fields)
+                    uint64_t est = 0;
+                    for (uint64_t rec = cs.next + 1; rec < cs.end; rec++) {
+                        if (bv_->paired) est += 2ull * (bv_->reads[2 * rec].len + bv_->reads[2 * rec + 1].len) + 320;
+                        else est += 2ull * bv_->reads[rec].len + 160;
+                    }
+                    cs.spec_out.reserve(est);
+                }
+            }
             auto visit = [&](uint64_t rec) {
                 cs.evals_spec++;
                 Rng r2 = srng;
@@ -1544,7 +1557,6 @@ void Policy::run_chunk(ChunkState& cs) {
     }
     if (timing) cs.seconds_real += since(t_run);
     cs.done = true;
-    std::string().swap(cs.spec_out);
     std::vector<ChunkState::Effect>().swap(cs.effects);
     std::vector<ResultStore::Entry>().swap(cs.entries);
 }

@@ -167,6 +167,23 @@ struct ChunkState {
     };
     std::vector<Effect> effects;
     std::string spec_out;  // outputs captured by the lookahead
+    // the chunk's output in record order: ranges of `out` (records the real run
+    // formatted) and of `spec_out` (captured records it reused), copied once into the
+    // final buffer
+    struct Piece {
+        bool spec;
+        uint64_t off, len;
+    };
+    std::vector<Piece> pieces;
+    uint64_t out_bytes = 0;
+    void add_piece(bool spec, uint64_t off, uint64_t len) {
+        if (!len) return;
+        if (!pieces.empty() && pieces.back().spec == spec && pieces.back().off + pieces.back().len == off)
+            pieces.back().len += len;
+        else
+            pieces.push_back(Piece{spec, off, len});
+        out_bytes += len;
+    }
     uint64_t evals_reused = 0;
     // real-run misses on a record the lookahead had evaluated to the end under another
     // state (mispredicted), and on one it had not (unknown)

@@ -562,15 +562,13 @@ void Session::worker() {
 void Session::complete(Request& r) {
     size_t total = 0;
     for (auto& c : r.chunks) {
-        total += c.out.size();
+        total += c.out_bytes;
         r.mapped += c.mapped;
         r.d2h_bytes += c.result_bytes;
     }
     r.out = (char*)std::malloc(total + 1);
     if (r.out) {
-        std::vector<const std::string*> parts;
-        for (auto& c : r.chunks) parts.push_back(&c.out);
-        parallel_concat(parts, r.out, total >= (64u << 20) ? 4 : 1);
+        gather_chunk_outputs(r.chunks, r.out, total >= (64u << 20) ? 4 : 1);
         r.out[total] = 0;
         r.out_len = total;
     } else {
