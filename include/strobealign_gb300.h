@@ -331,7 +331,11 @@ void sa_session_free(sa_session* s);
 int32_t sa_mapper_upload(sa_mapper* m, const sa_read_batch* r1, const sa_read_batch* r2);
 int32_t sa_map_uploaded(sa_mapper* m, sa_output* out);
 
-/* Stage timings and counters of the last mapped batch. */
+/* Stage timings and counters of the last mapped batch.  A large batch is cut into
+ * parts whose NAM pipelines overlap the extension waves and the policy:
+ * seconds_nams sums the parts' pipelines, seconds_extension the waves, and
+ * seconds_policy is the rest of seconds_total after the waves and the first part's
+ * pipeline. */
 typedef struct {
     double seconds_upload, seconds_nams, seconds_extension, seconds_policy, seconds_total;
     uint64_t n_jobs, n_waves, n_launches;
@@ -354,6 +358,10 @@ typedef struct {
 int32_t sa_mapper_get_stats(const sa_mapper* m, sa_mapper_stats* out);
 /* Record CUDA events around each stage's launches (off by default). */
 int32_t sa_mapper_set_profiling(sa_mapper* m, int32_t enable);
+/* Parts a large batch is cut into (runs of whole chunks, at least 4 chunks each): the
+ * NAM pipeline of one part runs while the earlier parts are extended and written.
+ * Output bytes do not depend on it.  Default 4; 1 = the whole batch at once. */
+int32_t sa_mapper_set_parts(sa_mapper* m, uint32_t parts);
 
 /* SAM header (src/io/sam.rs:176-200); cmd_line NULL omits the @PG line. */
 int32_t sa_sam_header(const sa_refs* refs, const char* cmd_line, const char* rg_id, const char* const* rg_fields,

@@ -398,6 +398,10 @@ class Mapper:
     def set_profiling(self, on: bool = True) -> None:
         L.check(lib().sa_mapper_set_profiling(self.h, 1 if on else 0))
 
+    def set_parts(self, parts: int) -> None:
+        """NAM-pipeline parts a large batch is cut into (output does not depend on it)."""
+        L.check(lib().sa_mapper_set_parts(self.h, parts))
+
     def abundances(self) -> np.ndarray:
         n = len(self.refs)
         out = np.zeros(n, dtype=np.float64)

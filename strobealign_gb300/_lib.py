@@ -138,6 +138,7 @@ SIGNATURES = {
     "sa_map_uploaded": (i32, [vp, P(Output)]),
     "sa_mapper_get_stats": (i32, [vp, P(MapperStats)]),
     "sa_mapper_set_profiling": (i32, [vp, i32]),
+    "sa_mapper_set_parts": (i32, [vp, u32]),
 }
 
 _lib = None

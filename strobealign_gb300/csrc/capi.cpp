@@ -419,6 +419,14 @@ int32_t sa_mapper_set_profiling(sa_mapper* m, int32_t enable) {
     SA_CATCH
 }
 
+int32_t sa_mapper_set_parts(sa_mapper* m, uint32_t parts) {
+    SA_TRY
+    require(m, "null argument");
+    m->m->set_parts(parts);
+    return SA_OK;
+    SA_CATCH
+}
+
 int32_t sa_mapper_get_stats(const sa_mapper* m, sa_mapper_stats* out) {
     SA_TRY
     require(m && out, "null argument");

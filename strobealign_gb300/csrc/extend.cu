@@ -877,23 +877,18 @@ __device__ __noinline__ EndPos ssw_warp_pass(const uint8_t* q, int qlen, bool q_
         int vH = __shfl_sync(FULLM, lastH, pred);
         if (tau == 0) vH = 0;
         // main pass, part 1: diagonal + E candidates and the local F scan (F entering
-        // this thread's first row taken as 0)
+        // this thread's first row taken as 0).  max/add pairs are single DPX ops.
         int A[RMAX], F[RMAX];
         int f = 0;
 #pragma unroll
         for (int rr = 0; rr < RMAX; rr++) {
             if (rr >= nr) break;
             const int m = (int)(int8_t)(uint8_t)(P[rr >> 2] >> (8 * (rr & 3)));
-            const int e = E[rr];
-            int x = vH + m;
-            x = x > e ? x : e;
+            const int x = __viaddmax_s32(vH, m, E[rr]);  // max(vH + m, E)
             A[rr] = x;
             vH = H[rr];
             F[rr] = f;
-            int a = x - gO;
-            a = a > 0 ? a : 0;
-            const int f2 = f - gE;
-            f = f2 > a ? f2 : a;
+            f = __viaddmax_s32(f, -gE, __viaddmax_s32(x, -gO, 0));  // max(f - gE, max(x - gO, 0))
         }
         // F entering this thread's block: max-plus scan over the lane's threads
         int fin = 0;
@@ -912,29 +907,14 @@ __device__ __noinline__ EndPos ssw_warp_pass(const uint8_t* q, int qlen, bool q_
             const int pv = __shfl_up_sync(FULLM, V, 1, S);
             fin = s > 0 ? pv : 0;
         }
-        // part 2: H, E with the F entering each row
-        int colmax = 0;
-        {
-            int fr = fin;
-#pragma unroll
-            for (int rr = 0; rr < RMAX; rr++) {
-                if (rr >= nr) break;
-                const int fv = fr > F[rr] ? fr : F[rr];
-                const int h = A[rr] > fv ? A[rr] : fv;
-                colmax = colmax > h ? colmax : h;
-                int hg = h - gO;
-                hg = hg > 0 ? hg : 0;
-                const int e2 = E[rr] - gE;
-                E[rr] = e2 > hg ? e2 : hg;
-                H[rr] = h;
-                fr -= gE;
-            }
-        }
         // lazy-F (ext/ssw/ssw.c:285-299 / :491-502) in closed form: the loop carries
         // the final F of each lane into the following lanes, decaying by gE per row,
         // and raises H to it; its early exit drops only values that could no longer
         // raise any H.  So H(l, j) = max(H, G(l) - j*gE) with G(l) the maximum over
-        // lanes l' < l of Ffinal(l') - (l - 1 - l') * segLen * gE.
+        // lanes l' < l of Ffinal(l') - (l - 1 - l') * segLen * gE.  G depends only on
+        // part 1 and the scan, so the raise joins part 2; E is computed from H before
+        // the raise, as in the library (its lazy-F loop leaves E alone).
+        int g;
         {
             int fout = fin - nr * gE;
             fout = fout > f ? fout : f;  // F leaving this thread's block
@@ -946,14 +926,20 @@ __device__ __noinline__ EndPos ssw_warp_pass(const uint8_t* q, int qlen, bool q_
                 if (l >= d) Y = Y > c ? Y : c;
             }
             const int Gp = __shfl_up_sync(FULLM, Y, S);
-            int g = l > 0 ? Gp - j0 * gE : 0;
+            g = l > 0 ? Gp - j0 * gE : 0;
+        }
+        // part 2: H, E with the F entering each row, then the lazy-F raise
+        int colmax = 0;
+        {
+            int fr = fin;
 #pragma unroll
             for (int rr = 0; rr < RMAX; rr++) {
                 if (rr >= nr) break;
-                if (g > H[rr]) {
-                    H[rr] = g;
-                    colmax = colmax > g ? colmax : g;
-                }
+                const int h = __vimax3_s32(A[rr], fr, F[rr]);
+                E[rr] = __viaddmax_s32(E[rr], -gE, __viaddmax_s32(h, -gO, 0));  // max(E - gE, max(h - gO, 0))
+                H[rr] = h > g ? h : g;
+                colmax = __vimax3_s32(colmax, h, g);
+                fr -= gE;
                 g -= gE;
             }
         }

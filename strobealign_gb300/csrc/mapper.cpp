@@ -28,8 +28,13 @@ Mapper::Mapper(const sa_index* idx, const sa_refs* refs, const sa_chaining_param
     trace_ = tr && *tr && *tr != '0';
     // SA_MAX_WAVE_JOBS: extension jobs per wave at most (tuning)
     if (const char* mw = std::getenv("SA_MAX_WAVE_JOBS")) set_max_wave_jobs(std::strtoull(mw, nullptr, 10));
+    // SA_PARTS: NAM-pipeline parts a large batch is cut into (tuning)
+    if (const char* np = std::getenv("SA_PARTS")) set_parts((uint32_t)std::strtoul(np, nullptr, 10));
     SA_CUDA(cudaSetDevice(idx->device));
     SA_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    int prio_least = 0, prio_greatest = 0;
+    SA_CUDA(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
+    SA_CUDA(cudaStreamCreateWithPriority(&stn_, cudaStreamNonBlocking, prio_greatest));
     const auto& cs = refs->contigs;
     const uint32_t nc = (uint32_t)cs.size();
     std::vector<uint64_t> woff(nc);
@@ -66,6 +71,7 @@ Mapper::Mapper(const sa_index* idx, const sa_refs* refs, const sa_chaining_param
 
 Mapper::~Mapper() {
     if (st_) cudaStreamDestroy(st_);
+    if (stn_) cudaStreamDestroy(stn_);
 }
 
 void Mapper::upload_reads(const std::vector<ReadView>& reads) {
@@ -94,41 +100,59 @@ void Mapper::upload_reads(const std::vector<ReadView>& reads) {
     h2d_bytes_ += total + ((size_t)n + 1) * 8;
 }
 
-void Mapper::nams_for_reads(uint32_t& launches) {
+// The NAM pipeline for one part, on stn_: the part's bases are copied out of the
+// uploaded batch with local offsets, and its NAMs, statistics (and for single-end
+// piecewise extension the NAMs' chain anchors) come back into the part's pinned buffers.
+void Mapper::part_nams(Part& p, uint32_t& launches) {
+    const auto t0 = std::chrono::steady_clock::now();
+    const uint32_t n = p.read_hi - p.read_lo;
+    const uint64_t base = h_off_.p[p.read_lo], total = h_off_.p[p.read_hi] - base;
     NamConfig cfg;
     cfg.cp = ChainParams{cp_.max_lookback, cp_.diag_diff_penalty, cp_.gap_length_penalty, cp_.valid_score_threshold,
                          cp_.max_ref_gap, cp_.matches_weight, cp_.max_diagonal_ratio};
     cfg.mcs = mp_.mcs_strategy;
     cfg.rescue_distance = mp_.rescue_distance;
     cfg.nam_anchors = single_end_piecewise_ && !bv_.paired;
-    const auto t0 = std::chrono::steady_clock::now();
-    launches += run_nam_pipeline(idx_->view(), refs_view_, cfg, n_reads_, total_bases_, max_contig_len_,
-                                 (uint32_t)refs_->contigs.size(), nws_, st_, &kt_);
-    const auto t1 = std::chrono::steady_clock::now();
-    const uint64_t tn = nws_.last_total_nams;
+    pws_.seq.reserve(total + 16);
+    pws_.off.reserve((size_t)n + 1);
+    h_poff_.reserve((size_t)n + 1);
+    for (uint32_t i = 0; i <= n; i++) h_poff_.p[i] = h_off_.p[p.read_lo + i] - base;
+    if (total) SA_CUDA(cudaMemcpyAsync(pws_.seq.p, nws_.seq.p + base, total, cudaMemcpyDeviceToDevice, stn_));
+    SA_CUDA(cudaMemcpyAsync(pws_.off.p, h_poff_.p, ((size_t)n + 1) * 8, cudaMemcpyHostToDevice, stn_));
+    launches += run_nam_pipeline(idx_->view(), refs_view_, cfg, n, total, max_contig_len_,
+                                 (uint32_t)refs_->contigs.size(), pws_, stn_, &kt_nam_);
+    const uint64_t tn = pws_.last_total_nams;
+    p.n_nams = tn;
+    uint64_t d2h = 0;
     if (cfg.nam_anchors) {
-        const uint64_t ta = nws_.last_total_nam_anchors;
-        h_nam_anc_off_.reserve(tn + 1);
-        h_nam_anc_.reserve(ta);
-        SA_CUDA(cudaMemcpyAsync(h_nam_anc_off_.p, nws_.nam_anc_off.p, (tn + 1) * 8, cudaMemcpyDeviceToHost, st_));
-        if (ta) SA_CUDA(cudaMemcpyAsync(h_nam_anc_.p, nws_.nam_anc.p, ta * 8, cudaMemcpyDeviceToHost, st_));
-        d2h_bytes_ += (tn + 1) * 8 + ta * 8;
+        const uint64_t ta = pws_.last_total_nam_anchors;
+        p.anc_off.reserve(tn + 1);
+        p.anc.reserve(ta);
+        SA_CUDA(cudaMemcpyAsync(p.anc_off.p, pws_.nam_anc_off.p, (tn + 1) * 8, cudaMemcpyDeviceToHost, stn_));
+        if (ta) SA_CUDA(cudaMemcpyAsync(p.anc.p, pws_.nam_anc.p, ta * 8, cudaMemcpyDeviceToHost, stn_));
+        d2h += (tn + 1) * 8 + ta * 8;
     }
-    h_nam_off_.reserve((size_t)n_reads_ + 1);
-    h_nams_.reserve(tn);
-    h_details_.reserve(n_reads_);
-    n_host_nams_ = tn;
-    SA_CUDA(cudaMemcpyAsync(h_nam_off_.p, nws_.nam_off.p, ((size_t)n_reads_ + 1) * 8, cudaMemcpyDeviceToHost, st_));
-    if (tn) SA_CUDA(cudaMemcpyAsync(h_nams_.p, nws_.nams.p, tn * sizeof(NamRec), cudaMemcpyDeviceToHost, st_));
-    SA_CUDA(cudaMemcpyAsync(h_details_.p, nws_.details.p, (size_t)n_reads_ * sizeof(NamDetailsRec),
-                            cudaMemcpyDeviceToHost, st_));
-    SA_CUDA(cudaStreamSynchronize(st_));
-    d2h_bytes_ += ((size_t)n_reads_ + 1) * 8 + tn * sizeof(NamRec) + (size_t)n_reads_ * sizeof(NamDetailsRec);
-    if (trace_) {
-        const auto t2 = std::chrono::steady_clock::now();
-        std::fprintf(stderr, "sa_nams reads=%u nams=%llu pipeline=%.4f copy=%.4f\n", n_reads_, (unsigned long long)tn,
-                     std::chrono::duration<double>(t1 - t0).count(), std::chrono::duration<double>(t2 - t1).count());
-    }
+    p.nam_off.reserve((size_t)n + 1);
+    p.nams.reserve(tn);
+    p.details.reserve(n);
+    SA_CUDA(cudaMemcpyAsync(p.nam_off.p, pws_.nam_off.p, ((size_t)n + 1) * 8, cudaMemcpyDeviceToHost, stn_));
+    if (tn) SA_CUDA(cudaMemcpyAsync(p.nams.p, pws_.nams.p, tn * sizeof(NamRec), cudaMemcpyDeviceToHost, stn_));
+    SA_CUDA(cudaMemcpyAsync(p.details.p, pws_.details.p, (size_t)n * sizeof(NamDetailsRec), cudaMemcpyDeviceToHost,
+                            stn_));
+    SA_CUDA(cudaStreamSynchronize(stn_));
+    d2h += ((size_t)n + 1) * 8 + tn * sizeof(NamRec) + (size_t)n * sizeof(NamDetailsRec);
+    p.bv.nams = p.nams.p;
+    p.bv.nam_off = p.nam_off.p;
+    p.bv.details = p.details.p;
+    p.bv.nam_anc_off = cfg.nam_anchors ? p.anc_off.p : nullptr;
+    p.bv.nam_anc = cfg.nam_anchors ? p.anc.p : nullptr;
+    p.bv.anc_qbits = pws_.anchor_qbits;
+    p.bv.anc_pbits = pws_.anchor_pbits;
+    p.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    d2h_bytes_ += d2h;  // atomic: the wave thread adds its transfers meanwhile
+    h2d_bytes_ += ((size_t)n + 1) * 8;
+    if (trace_)
+        std::fprintf(stderr, "sa_nams part reads=%u nams=%llu seconds=%.4f\n", n, (unsigned long long)tn, p.seconds);
 }
 
 std::shared_ptr<const WaveResults> Mapper::run_wave(const ExtJob* jobs, uint32_t nj, uint32_t max_qlen,
@@ -213,7 +237,7 @@ void Mapper::map(const sa_read_batch* r1, const sa_read_batch* r2, sa_output* ou
 // are waiting, or as soon as no policy thread could add more.  Which jobs share a
 // wave depends on timing; results do not (each job is a pure function of its
 // inputs, and the output of every chunk depends only on the results it reads).
-uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, ResultStore& store, uint32_t& launches) {
+uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, uint32_t& launches, uint32_t& nam_launches) {
     const size_t nchunks = chunks.size();
     const unsigned nthreads = std::max(1u, std::min<unsigned>(policy_threads_, (unsigned)nchunks));
     std::mutex mu;
@@ -224,11 +248,35 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, ResultStore& store, u
     unsigned running = 0;
     std::exception_ptr err;
     bool stop = false;
-    for (size_t c = 0; c < nchunks; c++) ready.push_back(c);
     std::vector<bool> is_seeded(nchunks, false);
 
+    // NAM pipelines part by part; a part's chunks become ready once its NAMs are in
+    std::thread nam_thread([&]() {
+        try {
+            for (size_t pi = 0; pi < n_parts_; pi++) {
+                {
+                    std::lock_guard<std::mutex> g(mu);
+                    if (stop) return;
+                }
+                Part& p = *parts_[pi];
+                part_nams(p, nam_launches);
+                std::lock_guard<std::mutex> g(mu);
+                for (size_t c = p.chunk_lo; c < p.chunk_hi; c++) ready.push_back(c);
+                cv_work.notify_all();
+                cv_ext.notify_one();
+            }
+        } catch (...) {
+            std::lock_guard<std::mutex> g(mu);
+            if (!err) err = std::current_exception();
+            stop = true;
+            cv_work.notify_all();
+            cv_ext.notify_all();
+        }
+    });
+
     auto worker = [&]() {
-        Policy policy(pcfg_, contigs_, bv_, store);
+        // one policy per thread, bound to each chunk's part in turn
+        Policy policy(pcfg_, contigs_, parts_[0]->bv, parts_[0]->store);
         std::unique_lock<std::mutex> lk(mu);
         for (;;) {
             cv_work.wait(lk, [&] { return stop || !ready.empty(); });
@@ -241,6 +289,7 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, ResultStore& store, u
             lk.unlock();
             ChunkState& cs = chunks[c];
             try {
+                policy.bind(parts_[cs.part]->bv, parts_[cs.part]->store);
                 if (first)
                     policy.seed_requests(cs);
                 else
@@ -312,16 +361,21 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, ResultStore& store, u
             for (size_t c : batch) nj += chunks[c].pending.size();
             h_jobs_.reserve(std::max<size_t>(nj, 1));
             nj = 0;
-            for (size_t c : batch) {
-                chunks[c].wave_first = nj;
-                std::memcpy(h_jobs_.p + nj, chunks[c].pending.data(), chunks[c].pending.size() * sizeof(ExtJob));
-                nj += chunks[c].pending.size();
-            }
             wave_anchors_.clear();
             uint32_t max_anchors = 0;
-            if (bv_.nam_anc) {
-                attach_piecewise_anchors(bv_, h_jobs_.p, nj, wave_anchors_);
-                for (size_t j = 0; j < nj; j++) max_anchors = std::max(max_anchors, h_jobs_.p[j].anc_n);
+            for (size_t c : batch) {
+                const Part& p = *parts_[chunks[c].part];
+                const size_t j0 = nj, cnt = chunks[c].pending.size();
+                chunks[c].wave_first = nj;
+                std::memcpy(h_jobs_.p + nj, chunks[c].pending.data(), cnt * sizeof(ExtJob));
+                nj += cnt;
+                // anchors are looked up with the part's read indices; the device reads
+                // of the whole batch are indexed from the part's first read
+                if (p.bv.nam_anc) {
+                    attach_piecewise_anchors(p.bv, h_jobs_.p + j0, cnt, wave_anchors_);
+                    for (size_t j = j0; j < nj; j++) max_anchors = std::max(max_anchors, h_jobs_.p[j].anc_n);
+                }
+                for (size_t j = j0; j < nj; j++) h_jobs_.p[j].read += p.read_lo;
             }
             if (waves > 1000000) throw Error(SA_ERR_INVALID, "internal: extension waves do not converge");
             auto tw = std::chrono::steady_clock::now();
@@ -353,6 +407,7 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, ResultStore& store, u
         cv_work.notify_all();
     }
     for (auto& t : th) t.join();
+    nam_thread.join();
     if (err) std::rethrow_exception(err);
     return waves;
 }
@@ -364,21 +419,13 @@ void Mapper::map_uploaded(sa_output* out) {
     const bool paired = bv.paired;
     const uint64_t nrec = paired ? bv.reads.size() / 2 : bv.reads.size();
     uint32_t launches = 0;
-    h2d_bytes_ = d2h_bytes_ = 0;
+    h2d_bytes_ = 0;
+    d2h_bytes_ = 0;
     jobs_run_ = 0;
     t_ext_ = 0;
     kt_.reset();
+    kt_nam_.reset();
     for (int c = 0; c < 5; c++) sw_cells_[c] = 0;
-    nams_for_reads(launches);
-    auto t1 = std::chrono::steady_clock::now();
-    bv.nams = h_nams_.p;
-    bv.nam_off = h_nam_off_.p;
-    bv.details = h_details_.p;
-    const bool piecewise = single_end_piecewise_ && !paired;
-    bv.nam_anc_off = piecewise ? h_nam_anc_off_.p : nullptr;
-    bv.nam_anc = piecewise ? h_nam_anc_.p : nullptr;
-    bv.anc_qbits = nws_.anchor_qbits;
-    bv.anc_pbits = nws_.anchor_pbits;
     // chunks (src/main.rs:591-604)
     std::vector<ChunkState> chunks;
     for (uint64_t i = 0; i < nrec;) {
@@ -394,13 +441,48 @@ void Mapper::map_uploaded(sa_output* out) {
         chunks.push_back(std::move(cs));
         i = j;
     }
-    ResultStore store;
-    store.reset(bv.reads.size());
-    const uint32_t waves = schedule(chunks, store, launches);
+    // parts: runs of whole chunks (at least 4 chunks each), so that chunk semantics and
+    // output order are those of the whole batch; read and record indices inside a part
+    // are local to it
+    const uint32_t rpr = paired ? 2 : 1;
+    const size_t nchunks = chunks.size();
+    n_parts_ = std::max<size_t>(1, std::min<size_t>(parts_target_, nchunks / 4));
+    while (parts_.size() < n_parts_) parts_.push_back(std::make_unique<Part>());
+    for (size_t pi = 0, c0 = 0; pi < n_parts_; pi++) {
+        const size_t c1 = pi + 1 == n_parts_ ? nchunks : nchunks * (pi + 1) / n_parts_;
+        Part& p = *parts_[pi];
+        p.chunk_lo = c0;
+        p.chunk_hi = c1;
+        p.rec_lo = c0 < nchunks ? chunks[c0].first : nrec;
+        p.rec_hi = c1 > 0 && c1 <= nchunks ? chunks[c1 - 1].end : p.rec_lo;
+        p.read_lo = (uint32_t)(rpr * p.rec_lo);
+        p.read_hi = (uint32_t)(rpr * p.rec_hi);
+        p.bv = BatchView();
+        p.bv.paired = paired;
+        p.bv.reads.assign(bv.reads.begin() + p.read_lo, bv.reads.begin() + p.read_hi);
+        p.store.reset(p.read_hi - p.read_lo);
+        p.n_nams = 0;
+        for (size_t c = c0; c < c1; c++) {
+            chunks[c].part = (uint32_t)pi;
+            chunks[c].first -= p.rec_lo;
+            chunks[c].next -= p.rec_lo;
+            chunks[c].end -= p.rec_lo;
+        }
+        c0 = c1;
+    }
+    uint32_t nam_launches = 0;
+    const auto t_sched = std::chrono::steady_clock::now();
+    const uint32_t waves = schedule(chunks, launches, nam_launches);
+    const auto t_sched_end = std::chrono::steady_clock::now();
+    launches += nam_launches;
+    double t_nams = 0;
+    for (size_t pi = 0; pi < n_parts_; pi++) t_nams += parts_[pi]->seconds;
     if (trace_) {
         double sr = 0, ss = 0, sd = 0, sf = 0;
-        uint64_t er = 0, es = 0, runs = 0, eu = 0, mm = 0, mk = 0;
+        uint64_t er = 0, es = 0, runs = 0, eu = 0, mm = 0, mk = 0, sr2 = 0, si = 0;
         for (auto& c : chunks) {
+            sr2 += c.stale_rng;
+            si += c.stale_isd;
             eu += c.evals_reused;
             mm += c.miss_mispredicted;
             mk += c.miss_unknown;
@@ -413,9 +495,11 @@ void Mapper::map_uploaded(sa_output* out) {
             runs += c.runs;
         }
         std::fprintf(stderr, "sa_policy chunks=%zu runs=%llu cpu_real=%.3f cpu_spec=%.3f cpu_seed=%.3f cpu_format=%.3f "
-                             "evals_real=%llu evals_spec=%llu reused=%llu miss_mispredicted=%llu miss_unknown=%llu\n",
+                             "evals_real=%llu evals_spec=%llu reused=%llu miss_mispredicted=%llu miss_unknown=%llu "
+                             "stale_rng=%llu stale_isd=%llu\n",
                      chunks.size(), (unsigned long long)runs, sr, ss, sd, sf, (unsigned long long)er,
-                     (unsigned long long)es, (unsigned long long)eu, (unsigned long long)mm, (unsigned long long)mk);
+                     (unsigned long long)es, (unsigned long long)eu, (unsigned long long)mm, (unsigned long long)mk,
+                     (unsigned long long)sr2, (unsigned long long)si);
     }
     for (auto& c : chunks)
         for (auto& a : c.abundance) abundances_[a.first] += a.second;
@@ -428,6 +512,13 @@ void Mapper::map_uploaded(sa_output* out) {
     out->data = (char*)std::malloc(total_len + 1);
     if (!out->data) throw Error(SA_ERR_OOM, "output allocation failed");
     gather_chunk_outputs(chunks, out->data, policy_threads_);
+    if (trace_) {
+        auto d = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+            return std::chrono::duration<double>(b - a).count();
+        };
+        std::fprintf(stderr, "sa_map setup=%.4f schedule=%.4f output=%.4f bytes=%zu\n", d(t0, t_sched),
+                     d(t_sched, t_sched_end), d(t_sched_end, std::chrono::steady_clock::now()), total_len);
+    }
     out->data[total_len] = 0;
     out->len = total_len;
     out->n_reads = bv.reads.size();
@@ -438,32 +529,39 @@ void Mapper::map_uploaded(sa_output* out) {
     last_waves_ = waves;
     auto t2 = std::chrono::steady_clock::now();
     last_seconds_ = std::chrono::duration<double>(t2 - t0).count();
-    stats_.seconds_nams = std::chrono::duration<double>(t1 - t0).count();
+    // the parts' NAM pipelines overlap the waves and the policy; the policy's share is
+    // what neither the waves nor the first part's pipeline cover
+    stats_.seconds_nams = t_nams;
     stats_.seconds_extension = t_ext_;
-    stats_.seconds_policy = std::max(0.0, std::chrono::duration<double>(t2 - t1).count() - t_ext_);
+    stats_.seconds_policy = std::max(0.0, last_seconds_ - t_ext_ - parts_[0]->seconds);
     stats_.seconds_total = last_seconds_;
     stats_.n_jobs = jobs_run_;
     stats_.n_waves = waves;
     stats_.n_launches = launches;
     stats_.h2d_bytes = h2d_bytes_;
     stats_.d2h_bytes = d2h_bytes_;
-    stats_.n_nams = n_host_nams_;
     {
-        uint64_t rs = 0, an = 0;
-        for (uint32_t i = 0; i < n_reads_; i++) {
-            rs += h_details_.p[i].n_randstrobes;
-            an += h_details_.p[i].n_anchors;
+        uint64_t rs = 0, an = 0, nn = 0;
+        for (size_t pi = 0; pi < n_parts_; pi++) {
+            const Part& p = *parts_[pi];
+            nn += p.n_nams;
+            for (uint32_t i = 0; i < p.read_hi - p.read_lo; i++) {
+                rs += p.details.p[i].n_randstrobes;
+                an += p.details.p[i].n_anchors;
+            }
         }
+        stats_.n_nams = nn;
         stats_.n_anchors = an;
         stats_.n_anchor_total = an;
         stats_.n_randstrobes = rs;
         stats_.n_bases = total_bases_;
     }
     kt_.collect();
+    kt_nam_.collect();
     for (int c = 0; c < 5; c++) stats_.sw_cells[c] = sw_cells_[c];
     for (int i = 0; i < 16; i++) {
-        stats_.kernel_ms[i] = i < KS_COUNT ? kt_.ms[i] : 0.0;
-        stats_.kernel_launches[i] = i < KS_COUNT ? kt_.launches[i] : 0;
+        stats_.kernel_ms[i] = i < KS_COUNT ? kt_.ms[i] + kt_nam_.ms[i] : 0.0;
+        stats_.kernel_launches[i] = i < KS_COUNT ? kt_.launches[i] + kt_nam_.launches[i] : 0;
     }
 }
 

@@ -1,5 +1,6 @@
 // Batch driver state behind sa_mapper.
 #pragma once
+#include <atomic>
 #include <thread>
 
 #include "policy.h"
@@ -25,7 +26,6 @@ class Mapper {
     ExtWorkspace& ext_ws() { return ews_; }
     cudaStream_t stream() const { return st_; }
     void upload_reads(const std::vector<ReadView>& reads);
-    void nams_for_reads(uint32_t& launches);
     uint32_t n_reads() const { return n_reads_; }
     uint64_t total_bases() const { return total_bases_; }
     uint64_t h2d_bytes() const { return h2d_bytes_; }
@@ -34,21 +34,40 @@ class Mapper {
     uint32_t last_waves() const { return last_waves_; }
     uint64_t jobs_run() const { return jobs_run_; }
     void set_policy_threads(unsigned n) { policy_threads_ = n ? n : 1; }
-    void set_profiling(bool on) { kt_.enabled = on; }
+    void set_profiling(bool on) { kt_.enabled = kt_nam_.enabled = on; }
+    void set_parts(uint32_t n) { parts_target_ = n ? n : 1; }
     void set_wave_min_jobs(uint64_t n) { wave_min_jobs_ = n; }
     void set_max_wave_jobs(uint64_t n) { max_wave_jobs_ = n ? n : 1; }
 
   private:
+    // One NAM-pipeline part of a batch: a run of whole chunks with their reads' NAMs on
+    // the host, and the part's own read view and result store (read and record indices
+    // local to the part).  The NAM pipeline of part p + 1 runs while the chunks of
+    // parts <= p are in the policy and extension waves.
+    struct Part {
+        uint64_t rec_lo = 0, rec_hi = 0;
+        uint32_t read_lo = 0, read_hi = 0;
+        size_t chunk_lo = 0, chunk_hi = 0;
+        BatchView bv;
+        ResultStore store;
+        PinnedBuf<uint64_t> nam_off;
+        PinnedBuf<NamRec> nams;
+        PinnedBuf<NamDetailsRec> details;
+        PinnedBuf<uint64_t> anc_off, anc;  // single-end piecewise: NAM chain anchors
+        uint64_t n_nams = 0;
+        double seconds = 0;
+    };
+    void part_nams(Part& p, uint32_t& launches);
     std::shared_ptr<const WaveResults> run_wave(const ExtJob* jobs, uint32_t nj, uint32_t max_qlen,
                                                 uint32_t& launches, const std::vector<uint32_t>& anchors,
                                                 uint32_t max_anchors);
-    uint32_t schedule(std::vector<ChunkState>& chunks, ResultStore& store, uint32_t& launches);
+    uint32_t schedule(std::vector<ChunkState>& chunks, uint32_t& launches, uint32_t& nam_launches);
     BatchView bv_;
     bool have_batch_ = false;
     uint32_t max_qlen_ = 1;
     sa_mapper_stats stats_{};
     double t_ext_ = 0;
-    KernelTimers kt_;
+    KernelTimers kt_, kt_nam_;
     uint64_t sw_cells_[5] = {0, 0, 0, 0, 0};
     unsigned policy_threads_ = std::max(1u, std::thread::hardware_concurrency());
     uint64_t wave_min_jobs_ = 32768;
@@ -61,7 +80,8 @@ class Mapper {
     sa_mapping_params mp_;
     std::string rg_id_;
     PolicyConfig pcfg_;
-    cudaStream_t st_ = nullptr;
+    cudaStream_t st_ = nullptr;   // uploads and extension waves
+    cudaStream_t stn_ = nullptr;  // NAM pipelines of the parts (highest priority)
     DevBuf<uint64_t> d_words_, d_woff_;
     DevBuf<uint32_t> d_clen_;
     DevRefs refs_view_{};
@@ -74,16 +94,16 @@ class Mapper {
     PinnedBuf<uint8_t> h_seq_;
     PinnedBuf<uint64_t> h_off_;
     PinnedBuf<ExtJob> h_jobs_;
-    // per-read NAMs and statistics of the current batch, pinned for the copy back
-    PinnedBuf<uint64_t> h_nam_off_;
-    PinnedBuf<NamRec> h_nams_;
-    PinnedBuf<NamDetailsRec> h_details_;
-    uint64_t n_host_nams_ = 0;
-    PinnedBuf<uint64_t> h_nam_anc_off_, h_nam_anc_;  // single-end piecewise: NAM chain anchors
+    std::vector<std::unique_ptr<Part>> parts_;  // grow-only; pinned buffers reused across batches
+    size_t n_parts_ = 0;
+    uint32_t parts_target_ = 4;
+    NamWorkspace pws_;            // NAM pipeline buffers of one part
+    PinnedBuf<uint64_t> h_poff_;  // a part's local read offsets
+    double t_nams_ = 0;
     std::vector<uint32_t> wave_anchors_;
     uint32_t n_reads_ = 0;
     uint64_t total_bases_ = 0;
-    uint64_t h2d_bytes_ = 0, d2h_bytes_ = 0;
+    std::atomic<uint64_t> h2d_bytes_{0}, d2h_bytes_{0};
     uint32_t last_launches_ = 0, last_waves_ = 0;
     uint64_t jobs_run_ = 0;
     double last_seconds_ = 0;

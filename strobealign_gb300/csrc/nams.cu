@@ -47,6 +47,38 @@ __device__ __forceinline__ uint8_t nt_code(uint8_t c) {
 }
 
 // ------------------------------------------------------------------ seeding
+// A read packed 2 bits per base (base i at bits 2(i % 32) of word i / 32) with one
+// N flag bit per base, so that any window of up to 32 bases comes out in O(1).
+__device__ __forceinline__ uint64_t spread_bits(uint32_t v) {
+    uint64_t x = v;
+    x = (x | (x << 16)) & 0x0000FFFF0000FFFFULL;
+    x = (x | (x << 8)) & 0x00FF00FF00FF00FFULL;
+    x = (x | (x << 4)) & 0x0F0F0F0F0F0F0F0FULL;
+    x = (x | (x << 2)) & 0x3333333333333333ULL;
+    x = (x | (x << 1)) & 0x5555555555555555ULL;
+    return x;
+}
+__device__ __forceinline__ uint64_t window_bits(const uint64_t* packed, uint32_t q) {
+    const uint32_t w = q >> 5, sh = 2 * (q & 31);
+    const uint64_t lo = packed[w] >> sh;
+    return sh ? lo | (packed[w + 1] << (64 - sh)) : lo;
+}
+__device__ __forceinline__ uint32_t window_n(const uint32_t* nflags, uint32_t q) {
+    const uint32_t w = q >> 5;
+    return (uint32_t)((((uint64_t)nflags[w + 1] << 32) | nflags[w]) >> (q & 31));
+}
+__device__ __forceinline__ uint64_t low_mask(uint32_t bits) { return bits >= 64 ? ~0ULL : (1ULL << bits) - 1; }
+// the n-base window w (base 0 in the low bits) as the reference encodes it: forward
+// with the first base most significant, reverse complement with the first base least
+__device__ __forceinline__ void kmer_codes(uint64_t w, uint32_t n, uint64_t& fw, uint64_t& rc) {
+    const uint64_t m = low_mask(2 * n);
+    w &= m;
+    rc = ~w & m;
+    uint64_t r = __brevll(w);
+    r = ((r >> 1) & 0x5555555555555555ULL) | ((r & 0x5555555555555555ULL) << 1);
+    fw = r >> (64 - 2 * n);
+}
+
 // src/seeding/syncmers.rs:171-237: a syncmer at p requires an N-free k-mer window
 // and the (t-1)-th of its k-s+1 s-mer hashes to equal their minimum.
 // CHECKED (offsets supplied by a caller, not built here): a read whose offsets are
@@ -58,7 +90,9 @@ __global__ void __launch_bounds__(256) k_seed(const uint8_t* __restrict__ seq, c
                                               uint64_t* qr_hash, uint64_t* qr_hash_rc, uint32_t* qr_start,
                                               uint32_t* qr_end, uint64_t total, uint32_t* n_rs) {
     extern __shared__ uint8_t smem[];
-    uint8_t* codes = smem + (threadIdx.x / 32) * MAX_READ_LEN;
+    // per warp: packed bases (MAX_READ_LEN / 32 + 2 words) then N flags
+    uint64_t* packed = reinterpret_cast<uint64_t*>(smem + (threadIdx.x / 32) * MAX_READ_LEN);
+    uint32_t* nflags = reinterpret_cast<uint32_t*>(packed + MAX_READ_LEN / 32 + 2);
     const uint32_t lane = lane_id();
     const uint32_t span = p.k - p.s, step = 32 - span;
     const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
@@ -75,7 +109,17 @@ __global__ void __launch_bounds__(256) k_seed(const uint8_t* __restrict__ seq, c
             }
         }
         const uint32_t L = (uint32_t)(off[r + 1] - o);
-        for (uint32_t i = lane; i < L; i += 32) codes[i] = nt_code(seq[o + i]);
+        const uint32_t nwords = (L + 31) / 32;
+        for (uint32_t w = 0; w <= nwords; w++) {
+            const uint32_t i = w * 32 + lane;
+            const uint32_t cc = i < L ? nt_code(seq[o + i]) : 0;
+            const uint32_t b0 = __ballot_sync(FULL, cc & 1), b1 = __ballot_sync(FULL, (cc >> 1) & 1);
+            const uint32_t bn = __ballot_sync(FULL, cc > 3);
+            if (lane == 0) {
+                packed[w] = spread_bits(b0) | (spread_bits(b1) << 1);
+                nflags[w] = bn;
+            }
+        }
         __syncwarp();
         uint32_t nsyn = 0;
         for (uint32_t c = 0; L >= p.k && c + p.k <= L; c += step) {
@@ -83,12 +127,8 @@ __global__ void __launch_bounds__(256) k_seed(const uint8_t* __restrict__ seq, c
             bool v = q + p.s <= L;
             uint64_t fw = 0, rc = 0;
             if (v) {
-                for (uint32_t b = 0; b < p.s; b++) {
-                    uint32_t cc = codes[q + b];
-                    if (cc > 3) { v = false; break; }
-                    fw = (fw << 2) | cc;
-                    rc |= (uint64_t)(3 - cc) << (2 * b);
-                }
+                v = (window_n(nflags, q) & (uint32_t)low_mask(p.s)) == 0;
+                kmer_codes(window_bits(packed, q), p.s, fw, rc);
             }
             uint64_t hs = v ? xxh64_u64(fw < rc ? fw : rc) : 0;
             bool ok = true;
@@ -105,12 +145,8 @@ __global__ void __launch_bounds__(256) k_seed(const uint8_t* __restrict__ seq, c
             uint64_t kh = 0;
             uint32_t fwd = 0;
             if (is_syn) {
-                uint64_t kf = 0, kr = 0;
-                for (uint32_t b = 0; b < p.k; b++) {
-                    uint32_t cc = codes[pos + b];
-                    kf = (kf << 2) | cc;
-                    kr |= (uint64_t)(3 - cc) << (2 * b);
-                }
+                uint64_t kf, kr;
+                kmer_codes(window_bits(packed, pos), p.k, kf, kr);
                 kh = xxh64_u64(kf < kr ? kf : kr);
                 fwd = kf <= kr;
             }
@@ -622,7 +658,26 @@ struct ChainCtx {
     ChainParams cp;
     uint32_t k;
     const float* lut;
+    // fl(mx / mn) > max_diagonal_ratio without the division, for integers below 2^24
+    // (whose float conversions are exact): with R = M * 2^e (M the 24-bit significand),
+    // the quotient rounds above R exactly when mx / mn exceeds the midpoint
+    // (2M + 1) * 2^(e - 1), or reaches it when M is odd (ties go to even).  That is
+    // mx * 2^(1 - e) > mn * (2M + 1) in 64-bit integers.  ratio_exact is false when R
+    // does not fit this form; the division is used then.
+    bool ratio_exact;
+    bool ratio_strict;
+    uint32_t ratio_shift;
+    uint64_t ratio_num;
 };
+
+// fl(mx / mn) > R, as the reference computes it in f32 (0 / 0 is NaN: false)
+__device__ __forceinline__ bool ratio_above(uint32_t mx, uint32_t mn, const ChainCtx& c) {
+    if (c.ratio_exact) {
+        const uint64_t lhs = (uint64_t)mx << c.ratio_shift, rhs = (uint64_t)mn * c.ratio_num;
+        return mx != 0 && (c.ratio_strict ? lhs > rhs : lhs >= rhs);
+    }
+    return __fdiv_rn(__uint2float_rn(mx), __uint2float_rn(mn)) > c.cp.max_diagonal_ratio;
+}
 
 // compute_score (src/chainer.rs:286-302)
 __device__ __forceinline__ float chain_score(uint32_t dq, uint32_t dr, const ChainCtx& c) {
@@ -770,8 +825,7 @@ __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off,
                         if (dr >= max_ref_gap) hard = true;
                         else {
                             uint32_t mx = dq > dr ? dq : dr, mn = dq < dr ? dq : dr;
-                            float ratio = __fdiv_rn(__uint2float_rn(mx), __uint2float_rn(mn));
-                            if (!(ratio > cc.cp.max_diagonal_ratio)) {
+                            if (!ratio_above(mx, mn, cc)) {
                                 valid = true;
                                 diag = dq == dr;
                                 val = __fadd_rn(RING ? ring_dp[j & 63] : dp[b + j], chain_score(dq, dr, cc));
@@ -818,8 +872,7 @@ __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off,
                 if (rb == ri && qi > qb) {
                     uint32_t dq = qi - qb, dr = rsi - rsb;
                     uint32_t mx = dq > dr ? dq : dr, mn = dq < dr ? dq : dr;
-                    float ratio = __fdiv_rn(__uint2float_rn(mx), __uint2float_rn(mn));
-                    if (dr < max_ref_gap && dr > 0 && ratio <= cc.cp.max_diagonal_ratio) {
+                    if (dr < max_ref_gap && dr > 0 && !ratio_above(mx, mn, cc)) {
                         float ns = __fadd_rn(best_score, chain_score(dq, dr, cc));
                         if (ns > cur) {
                             cur = ns;
@@ -1198,7 +1251,24 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     ws.aux.reserve(3 * total_anchors);
     ws.nam_scratch.reserve(total_anchors);
     ws.nam_seg_count.reserve(2 * (size_t)n);
-    ChainCtx cc{cfg.cp, ix.p.k, ws.log2_lut.p};
+    ChainCtx cc{cfg.cp, ix.p.k, ws.log2_lut.p, false, true, 0, 0};
+    {
+        // R = M * 2^e with M the 24-bit significand of a normal positive float
+        const float R = cfg.cp.max_diagonal_ratio;
+        int ex = 0;
+        const float fr = std::frexp(R, &ex);  // R = fr * 2^ex, fr in [0.5, 1)
+        if (std::isfinite(R) && R > 0.0f && fr != 0.0f) {
+            const uint64_t M = (uint64_t)std::ldexp((double)fr, 24);  // exact: 24 significant bits
+            const int e = ex - 24;
+            const int shift = 1 - e;
+            if (M >= (1u << 23) && M < (1u << 24) && shift >= 0 && shift <= 30) {
+                cc.ratio_exact = true;
+                cc.ratio_strict = (M & 1) == 0;
+                cc.ratio_shift = (uint32_t)shift;
+                cc.ratio_num = 2 * M + 1;
+            }
+        }
+    }
     kt->begin(KS_CHAIN, st);
     if (cfg.nam_anchors) {
         ws.anc_sparse.reserve(3 * total_anchors + 1);

@@ -1444,7 +1444,16 @@ void Policy::run_chunk(ChunkState& cs) {
     while (cs.next < cs.end) {
         if (capture && !cs.effects.empty()) {
             const auto& ef = cs.effects[cs.next - cs.first];
-            if (ef.has_output && ef.pre_rng == cs.rng.state && ef.pre_isd.same_state(cs.isd)) {
+            // A record that drew nothing from the RNG took no path that depends on its
+            // state (the path up to a first draw is the same under any state), so its
+            // output holds under any RNG state; one that drew needs the same state.
+            const bool rng_ok = ef.rng_delta == 0 || ef.pre_rng == cs.rng.state;
+            const bool isd_ok = ef.pre_isd.same_state(cs.isd);
+            if (ef.has_output) {
+                cs.stale_rng += !rng_ok;
+                cs.stale_isd += !isd_ok;
+            }
+            if (ef.has_output && rng_ok && isd_ok) {
                 cs.add_piece(true, ef.out_off, ef.out_len);
                 cs.rng.state += ef.rng_delta;
                 cs.isd = ef.post_isd;

@@ -136,6 +136,7 @@ void attach_piecewise_anchors(const BatchView& bv, ExtJob* jobs, size_t n, std::
 
 struct ChunkState {
     uint64_t first = 0, next = 0, end = 0;  // record range [first, end), cursor next
+    uint32_t part = 0;                      // the batch part whose reads these are (Mapper)
     Rng rng;
     InsertSize isd;
     std::string out;
@@ -188,6 +189,8 @@ struct ChunkState {
     // real-run misses on a record the lookahead had evaluated to the end under another
     // state (mispredicted), and on one it had not (unknown)
     uint64_t miss_mispredicted = 0, miss_unknown = 0;
+    // captured outputs not reused: the RNG state, the insert-size state differed
+    uint64_t stale_rng = 0, stale_isd = 0;
     // host time by phase when PolicyConfig::timing is set
     double seconds_real = 0, seconds_spec = 0, seconds_seed = 0, seconds_format = 0;
     uint64_t evals_real = 0, evals_spec = 0, runs = 0;

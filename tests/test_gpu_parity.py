@@ -282,6 +282,22 @@ def test_repetitive_paired_end_sam_matches_oracle(sa, repeats):
     assert got == want, _first_diff(got, want)
 
 
+def test_mapping_is_independent_of_parts(sa, synth):
+    # a batch cut into NAM-pipeline parts (runs of whole chunks) maps to the same bytes
+    # as the whole batch in one part, and an empty batch maps to nothing
+    refs, idx = _index(sa, synth["fa"])
+    r1 = sa.Reads.from_file(synth["f1"])
+    r2 = sa.Reads.from_file(synth["f2"])
+    outs = []
+    for parts in (1, 2, 5):
+        m = sa.Mapper(idx, refs, chunk_size=20000, eqx=1)
+        m.set_parts(parts)
+        outs.append(m.map(r1, r2))
+    assert outs[0] == outs[1] == outs[2] and len(outs[0]) > 0
+    empty = sa.Reads.from_lists([], [])
+    assert sa.Mapper(idx, refs).map(empty, empty) == b""
+
+
 def test_synthetic_paired_end_small_chunks_matches_oracle(sa, synth):
     # many chunks: the per-chunk RNG and insert-size restarts are exercised
     want = run_oracle_cli(["--no-PG", "--chunk-size=20000", synth["fa"], synth["f1"], synth["f2"]])
