@@ -254,88 +254,124 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
 }
 
 // run-merging CIGAR writer (Cigar::push, src/cigar.rs:100-110)
+// Appends CIGAR ops, merging runs of one op.  The open run stays in a register and is
+// stored when the op changes or at finish() (a store and reload per base otherwise).
 struct CigarWriter {
     uint32_t* out;
     uint32_t n;
     uint32_t cap;
     bool overflow;
+    uint32_t open = 0;  // (len << 4) | op of the run being extended, 0 if none
     __device__ void push(uint32_t op, uint32_t len) {
         if (len == 0) return;
-        if (n > 0 && (out[n - 1] & 15) == op) out[n - 1] += len << 4;
-        else if (n < cap) out[n++] = (len << 4) | op;
-        else overflow = true;
+        if (open && (open & 15) == op) {
+            open += len << 4;
+            return;
+        }
+        close_run();
+        open = (len << 4) | op;
     }
+    __device__ void close_run() {
+        if (!open) return;
+        if (n < cap) out[n++] = open;
+        else overflow = true;
+        open = 0;
+    }
+    __device__ void finish() { close_run(); }
 };
 
-__global__ void k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict__ seq, const uint64_t* __restrict__ off,
-                       DevRefs R, const uint8_t* raw_refs, const uint64_t* raw_off, AlignScores sc, PrepRec* prep,
-                       const uint64_t* off_arena, const uint64_t* off_cigar, const uint64_t* off_h, uint8_t* arena,
-                       uint32_t* cigar, ExtResult* res, SswTask* tasks, uint32_t* counters, uint32_t* pw_list) {
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+// Warp per job: the Hamming path (hamming_align, src/aligner.rs:181-259) from
+// 32-position match masks, or the SSW / piecewise job's query and reference window
+// bytes copied into the arena with the lanes on consecutive positions.
+constexpr int FILL_WARPS = 8;
+__global__ void __launch_bounds__(32 * FILL_WARPS) k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict__ seq,
+                                                          const uint64_t* __restrict__ off, DevRefs R,
+                                                          const uint8_t* raw_refs, const uint64_t* raw_off,
+                                                          AlignScores sc, PrepRec* prep, const uint64_t* off_arena,
+                                                          const uint64_t* off_cigar, const uint64_t* off_h,
+                                                          uint8_t* arena, uint32_t* cigar, ExtResult* res,
+                                                          SswTask* tasks, uint32_t* counters, uint32_t* pw_list) {
+    __shared__ uint32_t eq_masks[FILL_WARPS][MAX_READ_LEN / 32];
+    uint32_t* masks = eq_masks[threadIdx.x / 32];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nwarps = gridDim.x * FILL_WARPS;
+    for (uint32_t t = blockIdx.x * FILL_WARPS + threadIdx.x / 32; t < n; t += nwarps) {
         PrepRec p = prep[t];
         p.arena_off = off_arena[t];
         p.cigar_off = off_cigar[t];
         p.h_off = off_h[t];
-        prep[t] = p;
+        __syncwarp();
+        if (lane == 0) prep[t] = p;
         const uint8_t* s = seq + off[p.read];
         const uint32_t L = p.qlen;
         if (p.type == 1) {
-            // hamming_align (src/aligner.rs:181-259)
-            int32_t score = (int32_t)sc.end_bonus, best = 0;
-            uint32_t start = 0, bs = 0, be = 0;
-            for (uint32_t i = 0; i < L; i++) {
-                bool eq = read_char(s, L, i, p.rc) == ref_base(R, p.ref_id, p.wstart + i);
-                score += eq ? (int32_t)sc.match : -(int32_t)sc.mismatch;
-                if (score < 0) { start = i + 1; score = 0; }
-                if (score > best) { bs = start; best = score; be = i + 1; }
+            // hamming_align (src/aligner.rs:181-259): match masks, then the scan
+            for (uint32_t c = 0; c < L; c += 32) {
+                const uint32_t i = c + lane;
+                const bool eq = i < L && read_char(s, L, i, p.rc) == ref_base(R, p.ref_id, p.wstart + i);
+                const uint32_t m = __ballot_sync(FULLM, eq);
+                if (lane == 0) masks[c / 32] = m;
             }
-            if (score + (int32_t)sc.end_bonus > best) {
-                best = score + (int32_t)sc.end_bonus;
-                be = L;
-                bs = start;
+            __syncwarp();
+            if (lane == 0) {
+                int32_t score = (int32_t)sc.end_bonus, best = 0;
+                uint32_t start = 0, bs = 0, be = 0;
+                for (uint32_t i = 0; i < L; i++) {
+                    const bool eq = (masks[i >> 5] >> (i & 31)) & 1;
+                    score += eq ? (int32_t)sc.match : -(int32_t)sc.mismatch;
+                    if (score < 0) { start = i + 1; score = 0; }
+                    if (score > best) { bs = start; best = score; be = i + 1; }
+                }
+                if (score + (int32_t)sc.end_bonus > best) {
+                    best = score + (int32_t)sc.end_bonus;
+                    be = L;
+                    bs = start;
+                }
+                CigarWriter w{cigar + p.cigar_off, 0, p.cigar_cap, false};
+                uint32_t mm = 0;
+                for (uint32_t i = bs; i < be; i++) {
+                    const bool eq = (masks[i >> 5] >> (i & 31)) & 1;
+                    mm += !eq;
+                    w.push(eq ? 7u : 8u, 1);
+                }
+                w.finish();
+                ExtResult r = res[t];
+                r.valid = w.overflow ? 0 : 1;
+                r.score = (uint32_t)best;
+                r.edit_distance = mm;
+                r.ref_start = p.wstart + bs;
+                r.length = be - bs;
+                r.soft_clip_left = bs;
+                r.soft_clip_right = L - be;
+                r.cigar_offset = (uint32_t)p.cigar_off;
+                r.cigar_len = w.n;
+                res[t] = r;
             }
-            CigarWriter w{cigar + p.cigar_off, 0, p.cigar_cap, false};
-            uint32_t mm = 0;
-            for (uint32_t i = bs; i < be; i++) {
-                bool eq = read_char(s, L, i, p.rc) == ref_base(R, p.ref_id, p.wstart + i);
-                mm += !eq;
-                w.push(eq ? 7u : 8u, 1);
-            }
-            ExtResult r = res[t];
-            r.valid = w.overflow ? 0 : 1;
-            r.score = (uint32_t)best;
-            r.edit_distance = mm;
-            r.ref_start = p.wstart + bs;
-            r.length = be - bs;
-            r.soft_clip_left = bs;
-            r.soft_clip_right = L - be;
-            r.cigar_offset = (uint32_t)p.cigar_off;
-            r.cigar_len = w.n;
-            res[t] = r;
-        } else if (p.type == 3) {
+            __syncwarp();
+        } else if (p.type == 2 || p.type == 3) {
             uint8_t* q = arena + p.arena_off;
-            for (uint32_t i = 0; i < L; i++) q[i] = read_char(s, L, i, p.rc);
+            for (uint32_t i = lane; i < L; i += 32) q[i] = read_char(s, L, i, p.rc);
             uint8_t* w = q + L;
-            for (uint32_t i = 0; i < p.wlen; i++) w[i] = ref_base(R, p.ref_id, p.wstart + i);
-            pw_list[atomicAdd(&counters[19], 1u)] = t;
-        } else if (p.type == 2) {
-            uint8_t* q = arena + p.arena_off;
-            for (uint32_t i = 0; i < L; i++) q[i] = read_char(s, L, i, p.rc);
-            uint8_t* w = q + L;
-            if (jobs[t].kind == JOB_ALIGN) {
+            if (p.type == 2 && jobs[t].kind == JOB_ALIGN) {
                 const uint8_t* rr = raw_refs + raw_off[p.ref_id];
-                for (uint32_t i = 0; i < p.wlen; i++) w[i] = rr[i];
+                for (uint32_t i = lane; i < p.wlen; i += 32) w[i] = rr[i];
             } else {
-                for (uint32_t i = 0; i < p.wlen; i++) w[i] = ref_base(R, p.ref_id, p.wstart + i);
+                for (uint32_t i = lane; i < p.wlen; i += 32) w[i] = ref_base(R, p.ref_id, p.wstart + i);
             }
-            uint32_t ti = atomicAdd(&counters[0], 1u);
-            atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8), (unsigned long long)L * p.wlen);
-            SswTask tk{};
-            tk.job = t;
-            tk.raw_off = RAW_FALLBACK;
-            tk.ref_begin1 = -1;
-            tk.read_begin1 = -1;
-            tasks[ti] = tk;
+            if (lane == 0) {
+                if (p.type == 3) {
+                    pw_list[atomicAdd(&counters[19], 1u)] = t;
+                } else {
+                    const uint32_t ti = atomicAdd(&counters[0], 1u);
+                    atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8), (unsigned long long)L * p.wlen);
+                    SswTask tk{};
+                    tk.job = t;
+                    tk.raw_off = RAW_FALLBACK;
+                    tk.ref_begin1 = -1;
+                    tk.read_begin1 = -1;
+                    tasks[ti] = tk;
+                }
+            }
         }
     }
 }
@@ -834,7 +870,6 @@ __device__ __noinline__ EndPos ssw_warp_pass(const uint8_t* q, int qlen, bool q_
     const int s_last = (seg - 1) / R;
     // owner of the row before this thread's first row (row l*seg + j0 - 1)
     const int pred = s > 0 ? tau - 1 : (l > 0 ? (l - 1) * S + s_last : 0);
-    const int src_last = l > 0 ? (l - 1) * S + s_last : 0;
     const int gO = sc.gap_open, gE = sc.gap_extend;
     const int match = sc.match, mism = -(int)sc.mismatch;
     // prof[(b * 32 + tau) * RW + w]: this thread's rows j0 + 4w .. 4w+3 against reference code b (4 = N)
@@ -1758,6 +1793,7 @@ __global__ void k_finalize(const SswTask* tasks, const uint32_t* n_tasks_ptr, co
             score = bscore + (int32_t)sc.end_bonus;
             edits = bed;
         }
+        w.finish();
         r.valid = w.overflow ? 0 : 1;
         r.score = (uint32_t)score;
         r.edit_distance = edits;
@@ -2125,6 +2161,7 @@ __global__ void __launch_bounds__(32) k_piecewise(const uint32_t* __restrict__ l
             post_re = lre;
             score += lqe == L ? (int)sc.end_bonus : 0;
         }
+        if (lane == 0) w.finish();
         if (lane == 0) {
             ExtResult r = res[t];
             r.valid = 0;
@@ -2267,9 +2304,9 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
     ws.list_rev_word.reserve(n);
     kt->begin(KS_FILL, st);
     ws.pw_list.reserve(n);
-    k_fill<<<grid1(n), 256, 0, st>>>(ws.jobs.p, n, seq, off, refs, raw_refs, raw_off, sc, ws.prep.p, of[0], of[1],
-                                     of[2], ws.arena.p, ws.cigar.p, ws.results.p, ws.tasks.p, ws.counters.p,
-                                     ws.pw_list.p);
+    k_fill<<<grid1((n + FILL_WARPS - 1) / FILL_WARPS, 1), 32 * FILL_WARPS, 0, st>>>(
+        ws.jobs.p, n, seq, off, refs, raw_refs, raw_off, sc, ws.prep.p, of[0], of[1], of[2], ws.arena.p, ws.cigar.p,
+        ws.results.p, ws.tasks.p, ws.counters.p, ws.pw_list.p);
     kt->end(st);
     launches++;
     if (max_pw_window) {
@@ -2448,7 +2485,8 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
                                                               ws.raw.p);
         kt->end(st);
         kt->begin(KS_FINALIZE, st);
-        k_finalize<<<grid1(n_tasks, 128), 128, 0, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p,
+        // one warp per block: a wave's few thousand SSW tasks spread over all SMs
+        k_finalize<<<grid1(n_tasks, 32), 32, 0, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p,
                                                         ws.raw_off.p, ws.raw.p, ws.hscratch.p, sc, ws.cigar.p,
                                                         ws.results.p);
         kt->end(st);
