@@ -280,98 +280,78 @@ struct CigarWriter {
     __device__ void finish() { close_run(); }
 };
 
-// Warp per job: the Hamming path (hamming_align, src/aligner.rs:181-259) from
-// 32-position match masks, or the SSW / piecewise job's query and reference window
-// bytes copied into the arena with the lanes on consecutive positions.
-constexpr int FILL_WARPS = 8;
-__global__ void __launch_bounds__(32 * FILL_WARPS) k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict__ seq,
-                                                          const uint64_t* __restrict__ off, DevRefs R,
-                                                          const uint8_t* raw_refs, const uint64_t* raw_off,
-                                                          AlignScores sc, PrepRec* prep, const uint64_t* off_arena,
-                                                          const uint64_t* off_cigar, const uint64_t* off_h,
-                                                          uint8_t* arena, uint32_t* cigar, ExtResult* res,
-                                                          SswTask* tasks, uint32_t* counters, uint32_t* pw_list) {
-    __shared__ uint32_t eq_masks[FILL_WARPS][MAX_READ_LEN / 32];
-    uint32_t* masks = eq_masks[threadIdx.x / 32];
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t nwarps = gridDim.x * FILL_WARPS;
-    for (uint32_t t = blockIdx.x * FILL_WARPS + threadIdx.x / 32; t < n; t += nwarps) {
+// Thread per job: the Hamming path (hamming_align, src/aligner.rs:181-259), or the
+// SSW / piecewise job's query and reference window bytes copied into the arena.
+__global__ void k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict__ seq, const uint64_t* __restrict__ off,
+                       DevRefs R, const uint8_t* raw_refs, const uint64_t* raw_off, AlignScores sc, PrepRec* prep,
+                       const uint64_t* off_arena, const uint64_t* off_cigar, const uint64_t* off_h, uint8_t* arena,
+                       uint32_t* cigar, ExtResult* res, SswTask* tasks, uint32_t* counters, uint32_t* pw_list) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         PrepRec p = prep[t];
         p.arena_off = off_arena[t];
         p.cigar_off = off_cigar[t];
         p.h_off = off_h[t];
-        __syncwarp();
-        if (lane == 0) prep[t] = p;
+        prep[t] = p;
         const uint8_t* s = seq + off[p.read];
         const uint32_t L = p.qlen;
         if (p.type == 1) {
-            // hamming_align (src/aligner.rs:181-259): match masks, then the scan
-            for (uint32_t c = 0; c < L; c += 32) {
-                const uint32_t i = c + lane;
-                const bool eq = i < L && read_char(s, L, i, p.rc) == ref_base(R, p.ref_id, p.wstart + i);
-                const uint32_t m = __ballot_sync(FULLM, eq);
-                if (lane == 0) masks[c / 32] = m;
+            // hamming_align (src/aligner.rs:181-259)
+            int32_t score = (int32_t)sc.end_bonus, best = 0;
+            uint32_t start = 0, bs = 0, be = 0;
+            for (uint32_t i = 0; i < L; i++) {
+                bool eq = read_char(s, L, i, p.rc) == ref_base(R, p.ref_id, p.wstart + i);
+                score += eq ? (int32_t)sc.match : -(int32_t)sc.mismatch;
+                if (score < 0) { start = i + 1; score = 0; }
+                if (score > best) { bs = start; best = score; be = i + 1; }
             }
-            __syncwarp();
-            if (lane == 0) {
-                int32_t score = (int32_t)sc.end_bonus, best = 0;
-                uint32_t start = 0, bs = 0, be = 0;
-                for (uint32_t i = 0; i < L; i++) {
-                    const bool eq = (masks[i >> 5] >> (i & 31)) & 1;
-                    score += eq ? (int32_t)sc.match : -(int32_t)sc.mismatch;
-                    if (score < 0) { start = i + 1; score = 0; }
-                    if (score > best) { bs = start; best = score; be = i + 1; }
-                }
-                if (score + (int32_t)sc.end_bonus > best) {
-                    best = score + (int32_t)sc.end_bonus;
-                    be = L;
-                    bs = start;
-                }
-                CigarWriter w{cigar + p.cigar_off, 0, p.cigar_cap, false};
-                uint32_t mm = 0;
-                for (uint32_t i = bs; i < be; i++) {
-                    const bool eq = (masks[i >> 5] >> (i & 31)) & 1;
-                    mm += !eq;
-                    w.push(eq ? 7u : 8u, 1);
-                }
-                w.finish();
-                ExtResult r = res[t];
-                r.valid = w.overflow ? 0 : 1;
-                r.score = (uint32_t)best;
-                r.edit_distance = mm;
-                r.ref_start = p.wstart + bs;
-                r.length = be - bs;
-                r.soft_clip_left = bs;
-                r.soft_clip_right = L - be;
-                r.cigar_offset = (uint32_t)p.cigar_off;
-                r.cigar_len = w.n;
-                res[t] = r;
+            if (score + (int32_t)sc.end_bonus > best) {
+                best = score + (int32_t)sc.end_bonus;
+                be = L;
+                bs = start;
             }
-            __syncwarp();
-        } else if (p.type == 2 || p.type == 3) {
+            CigarWriter w{cigar + p.cigar_off, 0, p.cigar_cap, false};
+            uint32_t mm = 0;
+            for (uint32_t i = bs; i < be; i++) {
+                bool eq = read_char(s, L, i, p.rc) == ref_base(R, p.ref_id, p.wstart + i);
+                mm += !eq;
+                w.push(eq ? 7u : 8u, 1);
+            }
+            w.finish();
+            ExtResult r = res[t];
+            r.valid = w.overflow ? 0 : 1;
+            r.score = (uint32_t)best;
+            r.edit_distance = mm;
+            r.ref_start = p.wstart + bs;
+            r.length = be - bs;
+            r.soft_clip_left = bs;
+            r.soft_clip_right = L - be;
+            r.cigar_offset = (uint32_t)p.cigar_off;
+            r.cigar_len = w.n;
+            res[t] = r;
+        } else if (p.type == 3) {
             uint8_t* q = arena + p.arena_off;
-            for (uint32_t i = lane; i < L; i += 32) q[i] = read_char(s, L, i, p.rc);
+            for (uint32_t i = 0; i < L; i++) q[i] = read_char(s, L, i, p.rc);
             uint8_t* w = q + L;
-            if (p.type == 2 && jobs[t].kind == JOB_ALIGN) {
+            for (uint32_t i = 0; i < p.wlen; i++) w[i] = ref_base(R, p.ref_id, p.wstart + i);
+            pw_list[atomicAdd(&counters[19], 1u)] = t;
+        } else if (p.type == 2) {
+            uint8_t* q = arena + p.arena_off;
+            for (uint32_t i = 0; i < L; i++) q[i] = read_char(s, L, i, p.rc);
+            uint8_t* w = q + L;
+            if (jobs[t].kind == JOB_ALIGN) {
                 const uint8_t* rr = raw_refs + raw_off[p.ref_id];
-                for (uint32_t i = lane; i < p.wlen; i += 32) w[i] = rr[i];
+                for (uint32_t i = 0; i < p.wlen; i++) w[i] = rr[i];
             } else {
-                for (uint32_t i = lane; i < p.wlen; i += 32) w[i] = ref_base(R, p.ref_id, p.wstart + i);
+                for (uint32_t i = 0; i < p.wlen; i++) w[i] = ref_base(R, p.ref_id, p.wstart + i);
             }
-            if (lane == 0) {
-                if (p.type == 3) {
-                    pw_list[atomicAdd(&counters[19], 1u)] = t;
-                } else {
-                    const uint32_t ti = atomicAdd(&counters[0], 1u);
-                    atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8), (unsigned long long)L * p.wlen);
-                    SswTask tk{};
-                    tk.job = t;
-                    tk.raw_off = RAW_FALLBACK;
-                    tk.ref_begin1 = -1;
-                    tk.read_begin1 = -1;
-                    tasks[ti] = tk;
-                }
-            }
+            uint32_t ti = atomicAdd(&counters[0], 1u);
+            atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8), (unsigned long long)L * p.wlen);
+            SswTask tk{};
+            tk.job = t;
+            tk.raw_off = RAW_FALLBACK;
+            tk.ref_begin1 = -1;
+            tk.read_begin1 = -1;
+            tasks[ti] = tk;
         }
     }
 }
@@ -1006,8 +986,9 @@ __device__ __noinline__ EndPos ssw_warp_pass(const uint8_t* q, int qlen, bool q_
 
 // Tasks are taken in list order through a shared counter, so the longest windows
 // (put first by the caller) start first.
+// the shortest-read variant fits 5 blocks per SM without spills (96 registers)
 template <int RMAX>
-__global__ void __launch_bounds__(128) k_ssw(SswTask* tasks, const uint32_t* order, uint32_t n_tasks,
+__global__ void __launch_bounds__(128, RMAX <= 4 ? 5 : 1) k_ssw(SswTask* tasks, const uint32_t* order, uint32_t n_tasks,
                                              const PrepRec* prep, const uint8_t* arena, AlignScores sc, int bias,
                                              uint32_t* counters) {
     constexpr int RW = (RMAX + 3) / 4;
@@ -2304,9 +2285,9 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
     ws.list_rev_word.reserve(n);
     kt->begin(KS_FILL, st);
     ws.pw_list.reserve(n);
-    k_fill<<<grid1((n + FILL_WARPS - 1) / FILL_WARPS, 1), 32 * FILL_WARPS, 0, st>>>(
-        ws.jobs.p, n, seq, off, refs, raw_refs, raw_off, sc, ws.prep.p, of[0], of[1], of[2], ws.arena.p, ws.cigar.p,
-        ws.results.p, ws.tasks.p, ws.counters.p, ws.pw_list.p);
+    k_fill<<<grid1(n), 256, 0, st>>>(ws.jobs.p, n, seq, off, refs, raw_refs, raw_off, sc, ws.prep.p, of[0], of[1],
+                                     of[2], ws.arena.p, ws.cigar.p, ws.results.p, ws.tasks.p, ws.counters.p,
+                                     ws.pw_list.p);
     kt->end(st);
     launches++;
     if (max_pw_window) {

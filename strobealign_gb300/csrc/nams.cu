@@ -475,8 +475,13 @@ __global__ void __launch_bounds__(256) k_hits(DevIndex ix, const uint64_t* __res
 // ------------------------------------------------------------------ anchors
 struct AnchorPack {
     uint32_t qbits, pbits;
+    // When seg_shift is set, the read orientation's index sits above the anchor key
+    // (hi = segment << seg_shift), so that one radix sort of the whole batch orders
+    // anchors by segment, then (ref_id, ref_start, query_start); k_chain masks it off.
+    uint32_t seg_shift = 0;
+    uint64_t hi = 0;
     __device__ __forceinline__ uint64_t key(uint32_t ref_id, uint32_t ref_start, uint32_t qs) const {
-        return ((uint64_t)ref_id << (pbits + qbits)) | ((uint64_t)ref_start << qbits) | qs;
+        return hi | ((uint64_t)ref_id << (pbits + qbits)) | ((uint64_t)ref_start << qbits) | qs;
     }
 };
 
@@ -604,6 +609,8 @@ __global__ void __launch_bounds__(256) k_anchors(DevIndex ix, const uint64_t* __
             const uint64_t b = ori * total + o;
             const uint32_t nh = (m >> ori) & 1 ? n_hits[2 * r + ori] : 0;
             uint64_t acc = FILL ? seg_off[2 * r + ori] : 0;
+            AnchorPack aps = ap;
+            if (ap.seg_shift) aps.hi = (uint64_t)(2 * r + ori) << ap.seg_shift;
             uint32_t sum = 0;
             for (uint32_t c = 0; c < nh; c += 32) {
                 uint32_t h = c + lane;
@@ -626,7 +633,7 @@ __global__ void __launch_bounds__(256) k_anchors(DevIndex ix, const uint64_t* __
                 // each lane its run's first 32 entries; longer runs continue with the
                 // whole warp, one hit at a time
                 if (has_run)
-                    is_long = !run_head(ix, start, fh, info & 2, qs, qe, ap, FILL ? anchors + acc + ex : nullptr, head,
+                    is_long = !run_head(ix, start, fh, info & 2, qs, qe, aps, FILL ? anchors + acc + ex : nullptr, head,
                                         minld);
                 const uint32_t lm = __ballot_sync(FULL, is_long);
                 for (uint32_t m = lm; m; m &= m - 1) {
@@ -634,7 +641,7 @@ __global__ void __launch_bounds__(256) k_anchors(DevIndex ix, const uint64_t* __
                     const uint32_t hL = __shfl_sync(FULL, head, L);
                     const uint32_t rest = warp_run_anchors(
                         ix, __shfl_sync(FULL, start, L) + 32, __shfl_sync(FULL, fh, L), __shfl_sync(FULL, info, L) & 2,
-                        __shfl_sync(FULL, qs, L), __shfl_sync(FULL, qe, L), ap,
+                        __shfl_sync(FULL, qs, L), __shfl_sync(FULL, qe, L), aps,
                         FILL ? anchors + acc + __shfl_sync(FULL, ex, L) + hL : nullptr, __shfl_sync(FULL, minld, L));
                     if (lane == (uint32_t)L) head += rest;
                 }
@@ -757,7 +764,7 @@ __device__ void warp_radix_sort_desc(uint32_t* idx, uint32_t* tmp, uint32_t m, c
 // global memory (the loop over a read orientation's anchors is serial; this takes
 // the store-to-load round trip out of each step).
 template <bool RING>
-__global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off, uint32_t n, const uint64_t* seg_off,
+__global__ void __launch_bounds__(256, 5) k_chain(const uint64_t* __restrict__ off, uint32_t n, const uint64_t* seg_off,
                                                const uint64_t* sorted, uint64_t* dedup, float* dp, uint32_t* pred,
                                                uint32_t* aux, uint64_t total_anchors, AnchorPack ap, ChainCtx cc,
                                                NamRec* nam_out, uint32_t* nam_seg_count, uint64_t* anc_out,
@@ -776,6 +783,7 @@ __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off,
         const uint32_t read_len = (uint32_t)(off[r + 1] - off[r]);
         // dedup (src/chainer.rs:228-229)
         uint32_t N = 0;
+        const uint64_t kmask = ap.seg_shift ? (1ULL << ap.seg_shift) - 1 : ~0ULL;  // drop the segment prefix
         for (uint64_t c = b; c < e; c += 32) {
             uint64_t i = c + lane;
             bool keep = false;
@@ -785,7 +793,7 @@ __global__ void __launch_bounds__(256) k_chain(const uint64_t* __restrict__ off,
                 keep = i == b || sorted[i - 1] != key;
             }
             uint32_t bal = __ballot_sync(FULL, keep);
-            if (keep) dedup[b + N + __popc(bal & lanemask_lt())] = key;
+            if (keep) dedup[b + N + __popc(bal & lanemask_lt())] = key & kmask;
             N += __popc(bal);
         }
         __syncwarp();
@@ -1191,6 +1199,11 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     ap.pbits = ceil_log2((uint64_t)max_contig_len + 1);
     uint32_t rbits = ceil_log2((uint64_t)n_contigs);
     if (ap.qbits + ap.pbits + rbits > 64) throw Error(SA_ERR_INVALID, "contig count/length too large for anchor keys");
+    // one radix sort over (read orientation, anchor key) when both fit in 64 bits, else a
+    // segmented sort per read orientation
+    const uint32_t abits = ap.qbits + ap.pbits + rbits, sbits = ceil_log2(2 * (uint64_t)n);
+    const bool radix = abits + sbits <= 64 && abits < 64;
+    if (radix) ap.seg_shift = abits;
     launches += run_seeding(ix.p, n, total, ws, st, kt);
     ws.hit_pos.reserve(2 * total);
     ws.hit_info.reserve(2 * total);
@@ -1237,12 +1250,22 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     if (total_anchors) {
         size_t tmp = 0;
         kt->begin(KS_SORT, st);
-        cub::DeviceSegmentedSort::SortKeys(nullptr, tmp, ws.anchors.p, ws.anchors_sorted.p, (int64_t)total_anchors,
-                                           (int64_t)(2 * (uint64_t)n), ws.seg_off.p, ws.seg_off.p + 1, st);
-        ws.cub_tmp.reserve(tmp);
-        cub::DeviceSegmentedSort::SortKeys(ws.cub_tmp.p, tmp, ws.anchors.p, ws.anchors_sorted.p,
-                                           (int64_t)total_anchors, (int64_t)(2 * (uint64_t)n), ws.seg_off.p,
-                                           ws.seg_off.p + 1, st);
+        if (radix) {
+            const int end_bit = (int)(abits + sbits);
+            cub::DeviceRadixSort::SortKeys(nullptr, tmp, ws.anchors.p, ws.anchors_sorted.p, (int64_t)total_anchors, 0,
+                                           end_bit, st);
+            ws.cub_tmp.reserve(tmp);
+            cub::DeviceRadixSort::SortKeys(ws.cub_tmp.p, tmp, ws.anchors.p, ws.anchors_sorted.p,
+                                           (int64_t)total_anchors, 0, end_bit, st);
+        } else {
+            cub::DeviceSegmentedSort::SortKeys(nullptr, tmp, ws.anchors.p, ws.anchors_sorted.p,
+                                               (int64_t)total_anchors, (int64_t)(2 * (uint64_t)n), ws.seg_off.p,
+                                               ws.seg_off.p + 1, st);
+            ws.cub_tmp.reserve(tmp);
+            cub::DeviceSegmentedSort::SortKeys(ws.cub_tmp.p, tmp, ws.anchors.p, ws.anchors_sorted.p,
+                                               (int64_t)total_anchors, (int64_t)(2 * (uint64_t)n), ws.seg_off.p,
+                                               ws.seg_off.p + 1, st);
+        }
         kt->end(st);
         launches++;
     }

@@ -167,6 +167,45 @@ struct CompTable {
 };
 const CompTable COMP;
 
+// Reversed copies 16 bytes at a time with GCC vector extensions (portable: TBL on Arm,
+// scalar elsewhere).  Reverse complement: the complement of an upper-cased A, C, G, T
+// or U is looked up by its low 4 bits; any other byte becomes N, as in comp_char.
+typedef unsigned char v16u8 __attribute__((vector_size(16)));
+const v16u8 REV16 = {15, 14, 13, 12, 11, 10, 9, 8, 7, 6, 5, 4, 3, 2, 1, 0};
+
+inline char* w_revcomp(char* p, const char* s, uint32_t len) {
+    const v16u8 tab = {'N', 'T', 'N', 'G', 'A', 'A', 'N', 'C', 'N', 'N', 'N', 'N', 'N', 'N', 'N', 'N'};
+    uint32_t i = len;
+    while (i >= 16) {
+        v16u8 x;
+        std::memcpy(&x, s + i - 16, 16);
+        x = __builtin_shuffle(x, REV16);
+        const v16u8 up = x & (unsigned char)0xDF;
+        const v16u8 ok = (up == 'A') | (up == 'C') | (up == 'G') | (up == 'T') | (up == 'U');
+        const v16u8 c = __builtin_shuffle(tab, (v16u8)(x & (unsigned char)15));
+        const v16u8 y = (c & ok) | ((unsigned char)'N' & ~ok);
+        std::memcpy(p, &y, 16);
+        p += 16;
+        i -= 16;
+    }
+    while (i > 0) *p++ = COMP.t[(uint8_t)s[--i]];
+    return p;
+}
+
+inline char* w_reversed(char* p, const char* s, uint32_t len) {
+    uint32_t i = len;
+    while (i >= 16) {
+        v16u8 x;
+        std::memcpy(&x, s + i - 16, 16);
+        x = __builtin_shuffle(x, REV16);
+        std::memcpy(p, &x, 16);
+        p += 16;
+        i -= 16;
+    }
+    while (i > 0) *p++ = s[--i];
+    return p;
+}
+
 char* w_cigar(char* p, const Alignment& a, bool eqx) {
     static const char ch[] = "MIDNSHP=X";
     uint32_t pend_op = 99, pend_len = 0;
@@ -204,9 +243,10 @@ void format_sam(const Sam& r, const PolicyConfig& cfg, std::string& o) {
     if (r.aln) bound += ((size_t)r.aln->cigar_len + 2) * 11;
     if (cfg.has_rg) bound += 6 + cfg.rg_id.size();
     if (cfg.mp.fastq_comments && rv.comment) bound += 1 + rv.comment_len;
-    const size_t start = o.size();
-    o.resize(start + bound);
-    char* const base = &o[start];
+    // written into per-thread scratch, then appended (no zero fill of the bound)
+    thread_local std::vector<char> scratch;
+    if (scratch.size() < bound) scratch.resize(2 * bound);
+    char* const base = scratch.data();
     char* p = base;
     p = w_str(p, rv.name, rv.name_len);
     *p++ = '\t';
@@ -231,7 +271,7 @@ void format_sam(const Sam& r, const PolicyConfig& cfg, std::string& o) {
     *p++ = '\t';
     if (!secondary && rv.len > 0) {
         if (r.seq_rc)
-            for (uint32_t i = rv.len; i-- > 0;) *p++ = COMP.t[(uint8_t)rv.seq[i]];
+            p = w_revcomp(p, rv.seq, rv.len);
         else
             p = w_str(p, rv.seq, rv.len);
     } else {
@@ -240,7 +280,7 @@ void format_sam(const Sam& r, const PolicyConfig& cfg, std::string& o) {
     *p++ = '\t';
     if (rv.qual && !secondary && rv.len > 0) {
         if (r.seq_rc)
-            for (uint32_t i = rv.len; i-- > 0;) *p++ = rv.qual[i];
+            p = w_reversed(p, rv.qual, rv.len);
         else
             p = w_str(p, rv.qual, rv.len);
     } else {
@@ -275,7 +315,7 @@ void format_sam(const Sam& r, const PolicyConfig& cfg, std::string& o) {
         p = w_str(p, rv.comment, rv.comment_len);
     }
     *p++ = '\n';
-    o.resize(start + (size_t)(p - base));
+    o.append(base, (size_t)(p - base));
 }
 
 Sam mapped_record(const Policy& P, const Alignment& a, const ReadView& rv, uint8_t mapq, bool secondary,
