@@ -152,7 +152,8 @@ void Mapper::part_nams(Part& p, uint32_t& launches) {
     d2h_bytes_ += d2h;  // atomic: the wave thread adds its transfers meanwhile
     h2d_bytes_ += ((size_t)n + 1) * 8;
     if (trace_)
-        std::fprintf(stderr, "sa_nams part reads=%u nams=%llu seconds=%.4f\n", n, (unsigned long long)tn, p.seconds);
+        std::fprintf(stderr, "sa_nams part t=%.4f reads=%u nams=%llu seconds=%.4f\n",
+                     std::chrono::duration<double>(t0 - t_map0_).count(), n, (unsigned long long)tn, p.seconds);
 }
 
 std::shared_ptr<const WaveResults> Mapper::run_wave(const ExtJob* jobs, uint32_t nj, uint32_t max_qlen,
@@ -331,7 +332,7 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, uint32_t& launches, u
 
     uint32_t waves = 0;
     std::vector<size_t> batch;
-    const auto t_sched0 = std::chrono::steady_clock::now();
+    const auto t_sched0 = t_map0_;
     try {
         std::unique_lock<std::mutex> lk(mu);
         for (;;) {
@@ -415,6 +416,7 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, uint32_t& launches, u
 void Mapper::map_uploaded(sa_output* out) {
     if (!have_batch_) throw Error(SA_ERR_INVALID, "no uploaded batch");
     auto t0 = std::chrono::steady_clock::now();
+    t_map0_ = t0;
     BatchView& bv = bv_;
     const bool paired = bv.paired;
     const uint64_t nrec = paired ? bv.reads.size() / 2 : bv.reads.size();

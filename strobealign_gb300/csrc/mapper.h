@@ -1,6 +1,7 @@
 // Batch driver state behind sa_mapper.
 #pragma once
 #include <atomic>
+#include <chrono>
 #include <thread>
 
 #include "policy.h"
@@ -100,6 +101,7 @@ class Mapper {
     NamWorkspace pws_;            // NAM pipeline buffers of one part
     PinnedBuf<uint64_t> h_poff_;  // a part's local read offsets
     double t_nams_ = 0;
+    std::chrono::steady_clock::time_point t_map0_;  // start of the current map (trace times)
     std::vector<uint32_t> wave_anchors_;
     uint32_t n_reads_ = 0;
     uint64_t total_bases_ = 0;

@@ -303,35 +303,45 @@ void Session::engine() {
 // it overlaps the waves of the requests already in flight.
 void Session::admitter(AdmitLane& lane) {
     std::unique_lock<std::mutex> lk(mu_);
+    std::vector<Request*> group;
     for (;;) {
-        auto can_admit = [&]() {
-            if (queue_.empty()) return false;
+        auto fits = [&](const Request& q) {
             if (cfg_.max_inflight_requests && inflight_ >= cfg_.max_inflight_requests) return false;
-            const Request& q = *queue_.front();
             return seq_alloc_.largest_free() >= std::max<uint64_t>(q.total_bases, 1) &&
                    off_alloc_.largest_free() >= q.n_reads + 1;
         };
-        cv_admit_.wait(lk, [&] { return broken_ || stop_ || can_admit(); });
+        cv_admit_.wait(lk, [&] { return broken_ || stop_ || (!queue_.empty() && fits(*queue_.front())); });
         if (broken_ || stop_) break;
-        std::unique_ptr<Request> rq = std::move(queue_.front());
-        queue_.pop_front();
-        Request* r = rq.get();
-        seq_alloc_.alloc(std::max<uint64_t>(r->total_bases, 1), r->seq_base);
-        off_alloc_.alloc(r->n_reads + 1, r->read_base);
-        inflight_++;
+        // one NAM pipeline for the queued requests at the front, up to a read budget (the
+        // fixed cost of a pipeline run is paid once), all single-end or all paired-end
+        group.clear();
+        uint64_t group_reads = 0;
+        const bool paired = queue_.front()->paired;
+        while (!queue_.empty() && (group.empty() || (queue_.front()->paired == paired &&
+                                                     group_reads + queue_.front()->n_reads <= admit_group_reads_ &&
+                                                     fits(*queue_.front())))) {
+            std::unique_ptr<Request> rq = std::move(queue_.front());
+            queue_.pop_front();
+            Request* r = rq.get();
+            seq_alloc_.alloc(std::max<uint64_t>(r->total_bases, 1), r->seq_base);
+            off_alloc_.alloc(r->n_reads + 1, r->read_base);
+            inflight_++;
+            r->state = 1;
+            r->t_admit = std::chrono::steady_clock::now();
+            live_[r->id] = std::move(rq);
+            group.push_back(r);
+            group_reads += r->n_reads;
+        }
         admitting_++;
-        r->state = 1;
-        r->t_admit = std::chrono::steady_clock::now();
-        live_[r->id] = std::move(rq);
         lk.unlock();
         try {
             const auto ta = std::chrono::steady_clock::now();
-            admit(*r, lane);
+            admit_group(group, lane);
             if (trace_)
-                std::fprintf(stderr, "sa_admit t=%.4f dur=%.4f id=%llu reads=%llu chunks=%zu\n",
+                std::fprintf(stderr, "sa_admit t=%.4f dur=%.4f id=%llu reads=%llu requests=%zu\n",
                              std::chrono::duration<double>(ta - t0_).count(),
                              std::chrono::duration<double>(std::chrono::steady_clock::now() - ta).count(),
-                             (unsigned long long)r->id, (unsigned long long)r->n_reads, r->chunks.size());
+                             (unsigned long long)group[0]->id, (unsigned long long)group_reads, group.size());
         } catch (const std::exception& e) {
             lk.lock();
             admitting_--;
@@ -340,111 +350,161 @@ void Session::admitter(AdmitLane& lane) {
         }
         lk.lock();
         admitting_--;
-        if (r->chunks.empty()) {
-            lk.unlock();
-            complete(*r);
-            lk.lock();
-            continue;
+        for (Request* r : group) {
+            if (r->chunks.empty()) {
+                lk.unlock();
+                complete(*r);
+                lk.lock();
+                continue;
+            }
+            for (size_t c = 0; c < r->chunks.size(); c++) ready_.emplace_back(r, c);
         }
-        for (size_t c = 0; c < r->chunks.size(); c++) ready_.emplace_back(r, c);
         cv_work_.notify_all();
         cv_engine_.notify_one();
     }
     cv_engine_.notify_all();
 }
 
-void Session::admit(Request& r, AdmitLane& lane) {
-    const uint32_t n = (uint32_t)r.n_reads;
-    if (n == 0) return;
+// Admission of a group of requests: their reads go to the lane's staging back to back
+// and to each request's arena range; one NAM pipeline runs over all of them; the NAMs,
+// statistics (and chain anchors) come back once and are split per request, with the
+// request's own read indices.
+void Session::admit_group(const std::vector<Request*>& group, AdmitLane& lane) {
     const auto ta = std::chrono::steady_clock::now();
-    // reads: pinned staging, local offsets for the NAM pipeline, arena copy for the extension
-    lane.h_seq.reserve(r.total_bases + 16);
-    lane.h_off.reserve((size_t)n + 1);
-    std::memcpy(lane.h_seq.p, r.seq.data(), r.total_bases);
-    std::memcpy(lane.h_off.p, r.seq_off.data(), ((size_t)n + 1) * 8);
-    lane.nws.seq.reserve(r.total_bases + 16);
-    lane.nws.off.reserve((size_t)n + 1);
-    SA_CUDA(cudaMemcpyAsync(lane.nws.seq.p, lane.h_seq.p, r.total_bases, cudaMemcpyHostToDevice, lane.st));
-    SA_CUDA(cudaMemcpyAsync(lane.nws.off.p, lane.h_off.p, ((size_t)n + 1) * 8, cudaMemcpyHostToDevice, lane.st));
-    SA_CUDA(cudaMemcpyAsync(arena_seq_.p + r.seq_base, lane.nws.seq.p, r.total_bases, cudaMemcpyDeviceToDevice, lane.st));
-    lane.h_goff.resize((size_t)n + 1);
-    for (uint32_t i = 0; i <= n; i++) lane.h_goff[i] = r.seq_base + r.seq_off[i];
-    SA_CUDA(cudaMemcpyAsync(arena_off_.p + r.read_base, lane.h_goff.data(), ((size_t)n + 1) * 8,
-                            cudaMemcpyHostToDevice, lane.st));
+    uint64_t n64 = 0, bases = 0;
+    for (const Request* r : group) {
+        n64 += r->n_reads;
+        bases += r->total_bases;
+    }
+    const uint32_t n = (uint32_t)n64;
+    const bool paired = group[0]->paired;
+    const bool nam_anchors = !paired && mp_.mode == SA_MODE_SAM && !mp_.use_ssw;
+    if (n > 0) {
+        lane.h_seq.reserve(bases + 16);
+        lane.h_off.reserve((size_t)n + 1);
+        lane.nws.seq.reserve(bases + 16);
+        lane.nws.off.reserve((size_t)n + 1);
+        uint64_t b0 = 0, i0 = 0;
+        for (const Request* r : group) {
+            std::memcpy(lane.h_seq.p + b0, r->seq.data(), r->total_bases);
+            for (uint64_t i = 0; i < r->n_reads; i++) lane.h_off.p[i0 + i] = b0 + r->seq_off[i];
+            b0 += r->total_bases;
+            i0 += r->n_reads;
+        }
+        lane.h_off.p[n] = bases;
+        SA_CUDA(cudaMemcpyAsync(lane.nws.seq.p, lane.h_seq.p, bases, cudaMemcpyHostToDevice, lane.st));
+        SA_CUDA(cudaMemcpyAsync(lane.nws.off.p, lane.h_off.p, ((size_t)n + 1) * 8, cudaMemcpyHostToDevice, lane.st));
+        // each request's bases and global offsets into its arena range
+        b0 = 0;
+        for (const Request* r : group) {
+            if (r->n_reads == 0) continue;
+            SA_CUDA(cudaMemcpyAsync(arena_seq_.p + r->seq_base, lane.nws.seq.p + b0, r->total_bases,
+                                    cudaMemcpyDeviceToDevice, lane.st));
+            lane.h_goff.resize(r->n_reads + 1);
+            for (uint64_t i = 0; i <= r->n_reads; i++) lane.h_goff[i] = r->seq_base + r->seq_off[i];
+            SA_CUDA(cudaMemcpyAsync(arena_off_.p + r->read_base, lane.h_goff.data(), (r->n_reads + 1) * 8,
+                                    cudaMemcpyHostToDevice, lane.st));
+            b0 += r->total_bases;
+        }
+    }
     NamConfig cfg;
     cfg.cp = ChainParams{cp_.max_lookback, cp_.diag_diff_penalty, cp_.gap_length_penalty, cp_.valid_score_threshold,
                          cp_.max_ref_gap, cp_.matches_weight, cp_.max_diagonal_ratio};
     cfg.mcs = mp_.mcs_strategy;
     cfg.rescue_distance = mp_.rescue_distance;
-    cfg.nam_anchors = !r.paired && mp_.mode == SA_MODE_SAM && !mp_.use_ssw;
-    if (trace_) {
-        // the staging copies above complete first, so that the pipeline's time is its own
-        SA_CUDA(cudaStreamSynchronize(lane.st));
-    }
+    cfg.nam_anchors = nam_anchors;
+    if (trace_) SA_CUDA(cudaStreamSynchronize(lane.st));  // the pipeline's time is its own
     const auto tp1 = std::chrono::steady_clock::now();
-    KernelTimers kt;
-    kt.enabled = trace_;
-    run_nam_pipeline(idx_->view(), refs_view_, cfg, n, r.total_bases, max_contig_len_,
-                     (uint32_t)refs_->contigs.size(), lane.nws, lane.st, &kt);
-    if (trace_) {
+    uint64_t tn = 0, ta_total = 0;
+    if (n > 0) {
+        KernelTimers kt;
+        kt.enabled = trace_;
+        run_nam_pipeline(idx_->view(), refs_view_, cfg, n, bases, max_contig_len_, (uint32_t)refs_->contigs.size(),
+                         lane.nws, lane.st, &kt);
+        if (trace_) {
+            SA_CUDA(cudaStreamSynchronize(lane.st));
+            kt.collect();
+            std::fprintf(stderr,
+                         "sa_admit_kernels id=%llu seed=%.3f hits=%.3f anchors=%.3f sort=%.3f chain=%.3f other=%.3f\n",
+                         (unsigned long long)group[0]->id, kt.ms[KS_SEED], kt.ms[KS_HITS], kt.ms[KS_ANCHORS],
+                         kt.ms[KS_SORT], kt.ms[KS_CHAIN], kt.ms[KS_NAMS_OTHER]);
+        }
+        tn = lane.nws.last_total_nams;
+        lane.h_nam_off.reserve((size_t)n + 1);
+        lane.h_nams.reserve(tn);
+        lane.h_details.reserve(n);
+        SA_CUDA(cudaMemcpyAsync(lane.h_nam_off.p, lane.nws.nam_off.p, ((size_t)n + 1) * 8, cudaMemcpyDeviceToHost,
+                                lane.st));
+        if (tn)
+            SA_CUDA(cudaMemcpyAsync(lane.h_nams.p, lane.nws.nams.p, tn * sizeof(NamRec), cudaMemcpyDeviceToHost,
+                                    lane.st));
+        SA_CUDA(cudaMemcpyAsync(lane.h_details.p, lane.nws.details.p, (size_t)n * sizeof(NamDetailsRec),
+                                cudaMemcpyDeviceToHost, lane.st));
+        if (nam_anchors) {
+            ta_total = lane.nws.last_total_nam_anchors;
+            lane.h_anc_off.reserve(tn + 1);
+            lane.h_anc.reserve(ta_total + 1);
+            SA_CUDA(cudaMemcpyAsync(lane.h_anc_off.p, lane.nws.nam_anc_off.p, (tn + 1) * 8, cudaMemcpyDeviceToHost,
+                                    lane.st));
+            if (ta_total)
+                SA_CUDA(cudaMemcpyAsync(lane.h_anc.p, lane.nws.nam_anc.p, ta_total * 8, cudaMemcpyDeviceToHost,
+                                        lane.st));
+        }
         SA_CUDA(cudaStreamSynchronize(lane.st));
-        kt.collect();
-        std::fprintf(stderr, "sa_admit_kernels id=%llu seed=%.3f hits=%.3f anchors=%.3f sort=%.3f chain=%.3f other=%.3f\n",
-                     (unsigned long long)r.id, kt.ms[KS_SEED], kt.ms[KS_HITS], kt.ms[KS_ANCHORS], kt.ms[KS_SORT],
-                     kt.ms[KS_CHAIN], kt.ms[KS_NAMS_OTHER]);
     }
     const auto tp2 = std::chrono::steady_clock::now();
-    const uint64_t tn = lane.nws.last_total_nams;
-    if (cfg.nam_anchors) {
-        const uint64_t ta = lane.nws.last_total_nam_anchors;
-        r.nam_anc_off.resize(tn + 1);
-        r.nam_anc.resize(ta);
-        SA_CUDA(cudaMemcpyAsync(r.nam_anc_off.data(), lane.nws.nam_anc_off.p, (tn + 1) * 8, cudaMemcpyDeviceToHost, lane.st));
-        if (ta) SA_CUDA(cudaMemcpyAsync(r.nam_anc.data(), lane.nws.nam_anc.p, ta * 8, cudaMemcpyDeviceToHost, lane.st));
-        r.d2h_bytes += (tn + 1) * 8 + ta * 8;
-    }
-    r.nam_off.resize((size_t)n + 1);
-    r.nams.resize(tn);
-    r.details.resize(n);
-    SA_CUDA(cudaMemcpyAsync(r.nam_off.data(), lane.nws.nam_off.p, ((size_t)n + 1) * 8, cudaMemcpyDeviceToHost, lane.st));
-    if (tn) SA_CUDA(cudaMemcpyAsync(r.nams.data(), lane.nws.nams.p, tn * sizeof(NamRec), cudaMemcpyDeviceToHost, lane.st));
-    SA_CUDA(cudaMemcpyAsync(r.details.data(), lane.nws.details.p, (size_t)n * sizeof(NamDetailsRec),
-                            cudaMemcpyDeviceToHost, lane.st));
-    SA_CUDA(cudaStreamSynchronize(lane.st));
-    r.h2d_bytes += r.total_bases + 2 * ((uint64_t)n + 1) * 8;
-    r.d2h_bytes += ((uint64_t)n + 1) * 8 + tn * sizeof(NamRec) + (uint64_t)n * sizeof(NamDetailsRec);
-    r.bv.nams = r.nams.data();
-    r.bv.nam_off = r.nam_off.data();
-    r.bv.details = r.details.data();
-    if (cfg.nam_anchors) {
-        r.bv.nam_anc_off = r.nam_anc_off.data();
-        r.bv.nam_anc = r.nam_anc.data();
-        r.bv.anc_qbits = lane.nws.anchor_qbits;
-        r.bv.anc_pbits = lane.nws.anchor_pbits;
-    }
-    // chunks (src/main.rs:591-604)
-    const bool paired = r.paired;
-    for (uint64_t i = 0; i < r.nrec;) {
-        uint64_t nt = 0, j = i;
-        while (j < r.nrec) {
-            nt += r.bv.reads[paired ? 2 * j : j].len + (paired ? r.bv.reads[2 * j + 1].len : 0);
-            j++;
-            if (nt > mp_.chunk_size) break;
+    // split per request
+    uint64_t i0 = 0;
+    for (Request* rp : group) {
+        Request& r = *rp;
+        const uint64_t rn = r.n_reads;
+        const uint64_t t0 = rn ? lane.h_nam_off.p[i0] : 0, t1 = rn ? lane.h_nam_off.p[i0 + rn] : 0;
+        r.nam_off.resize(rn + 1);
+        for (uint64_t i = 0; i <= rn; i++) r.nam_off[i] = rn ? lane.h_nam_off.p[i0 + i] - t0 : 0;
+        r.nams.assign(lane.h_nams.p + t0, lane.h_nams.p + t1);
+        r.details.assign(lane.h_details.p + i0, lane.h_details.p + i0 + rn);
+        r.h2d_bytes += r.total_bases + 2 * (rn + 1) * 8;
+        r.d2h_bytes += (rn + 1) * 8 + (t1 - t0) * sizeof(NamRec) + rn * sizeof(NamDetailsRec);
+        r.bv.nams = r.nams.data();
+        r.bv.nam_off = r.nam_off.data();
+        r.bv.details = r.details.data();
+        if (nam_anchors && rn) {
+            const uint64_t a0 = lane.h_anc_off.p[t0], a1 = lane.h_anc_off.p[t1];
+            r.nam_anc_off.resize(t1 - t0 + 1);
+            for (uint64_t t = t0; t <= t1; t++) r.nam_anc_off[t - t0] = lane.h_anc_off.p[t] - a0;
+            r.nam_anc.assign(lane.h_anc.p + a0, lane.h_anc.p + a1);
+            r.d2h_bytes += (t1 - t0 + 1) * 8 + (a1 - a0) * 8;
+            r.bv.nam_anc_off = r.nam_anc_off.data();
+            r.bv.nam_anc = r.nam_anc.data();
+            r.bv.anc_qbits = lane.nws.anchor_qbits;
+            r.bv.anc_pbits = lane.nws.anchor_pbits;
         }
-        ChunkState cs;
-        cs.first = cs.next = i;
-        cs.end = j;
-        r.chunks.push_back(std::move(cs));
-        i = j;
+        i0 += rn;
+        if (rn == 0) continue;
+        // chunks (src/main.rs:591-604)
+        for (uint64_t i = 0; i < r.nrec;) {
+            uint64_t nt = 0, j = i;
+            while (j < r.nrec) {
+                nt += r.bv.reads[paired ? 2 * j : j].len + (paired ? r.bv.reads[2 * j + 1].len : 0);
+                j++;
+                if (nt > mp_.chunk_size) break;
+            }
+            ChunkState cs;
+            cs.first = cs.next = i;
+            cs.end = j;
+            r.chunks.push_back(std::move(cs));
+            i = j;
+        }
+        r.seeded.assign(r.chunks.size(), 0);
+        r.store.reset(rn);
     }
-    r.seeded.assign(r.chunks.size(), 0);
-    r.store.reset(n);
     if (trace_) {
         auto d = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
             return std::chrono::duration<double>(b - a).count();
         };
         std::fprintf(stderr, "sa_admit_parts id=%llu upload=%.4f pipeline=%.4f rest=%.4f\n",
-                     (unsigned long long)r.id, d(ta, tp1), d(tp1, tp2), d(tp2, std::chrono::steady_clock::now()));
+                     (unsigned long long)group[0]->id, d(ta, tp1), d(tp1, tp2),
+                     d(tp2, std::chrono::steady_clock::now()));
     }
 }
 

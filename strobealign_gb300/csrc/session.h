@@ -90,6 +90,10 @@ struct AdmitLane {
     PinnedBuf<uint8_t> h_seq;
     PinnedBuf<uint64_t> h_off;
     std::vector<uint64_t> h_goff;
+    // a group's NAMs, statistics and chain anchors as copied back, before the split
+    PinnedBuf<uint64_t> h_nam_off, h_anc_off, h_anc;
+    PinnedBuf<NamRec> h_nams;
+    PinnedBuf<NamDetailsRec> h_details;
     std::thread th;
 };
 
@@ -111,7 +115,7 @@ class Session {
     void engine();
     void admitter(AdmitLane& lane);
     void worker();
-    void admit(Request& r, AdmitLane& lane);
+    void admit_group(const std::vector<Request*>& group, AdmitLane& lane);
     void run_wave(std::vector<std::pair<Request*, size_t>>& batch);
     void complete(Request& r);
     void fail_all(const std::string& msg, int32_t code);
@@ -157,6 +161,7 @@ class Session {
     // items may still point at them
     std::vector<std::unique_ptr<Request>> graveyard_;
     uint64_t wave_min_jobs_ = 32768;
+    uint64_t admit_group_reads_ = 262144;  // reads one admission's NAM pipeline takes at most
     uint64_t max_wave_jobs_ = 262144;
     bool trace_ = false;
     std::chrono::steady_clock::time_point t0_;
