@@ -1,12 +1,28 @@
 // Small host-side helpers shared by the batch driver and the session engine.
 #pragma once
+#include <sys/mman.h>
+
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <thread>
 #include <vector>
 
 namespace sa {
+
+// Output buffer for the caller (released with free()): large ones 2 MiB aligned and
+// advised to use huge pages, so that the first touch of hundreds of MB faults in few
+// pages.
+inline char* alloc_output(size_t bytes) {
+    if (bytes < (64u << 20)) return (char*)std::malloc(bytes);
+    void* p = nullptr;
+    if (posix_memalign(&p, 2u << 20, bytes) != 0) return nullptr;
+#ifdef MADV_HUGEPAGE
+    madvise(p, bytes, MADV_HUGEPAGE);
+#endif
+    return (char*)p;
+}
 
 // One copy of every chunk's output pieces into dst with up to `threads` threads,
 // each copying a run of consecutive pieces of about equal total size.

@@ -28,6 +28,8 @@ Mapper::Mapper(const sa_index* idx, const sa_refs* refs, const sa_chaining_param
     trace_ = tr && *tr && *tr != '0';
     // SA_MAX_WAVE_JOBS: extension jobs per wave at most (tuning)
     if (const char* mw = std::getenv("SA_MAX_WAVE_JOBS")) set_max_wave_jobs(std::strtoull(mw, nullptr, 10));
+    // SA_WAVE_MIN_JOBS: jobs that start a wave while policy threads are still busy (tuning)
+    if (const char* mj = std::getenv("SA_WAVE_MIN_JOBS")) set_wave_min_jobs(std::max<uint64_t>(1, std::strtoull(mj, nullptr, 10)));
     // SA_PARTS: NAM-pipeline parts a large batch is cut into (tuning)
     if (const char* np = std::getenv("SA_PARTS")) set_parts((uint32_t)std::strtoul(np, nullptr, 10));
     SA_CUDA(cudaSetDevice(idx->device));
@@ -187,7 +189,7 @@ void Mapper::upload(const sa_read_batch* r1, const sa_read_batch* r2) {
     const uint64_t nrec = r1->n;
     bv_ = BatchView();
     bv_.paired = paired;
-    bv_.reads.resize(paired ? 2 * nrec : nrec);
+    reads_.resize(paired ? 2 * nrec : nrec);
     auto view = [](const sa_read_batch* b, uint64_t i) {
         ReadView v;
         v.seq = b->seq + b->seq_offsets[i];
@@ -205,16 +207,17 @@ void Mapper::upload(const sa_read_batch* r1, const sa_read_batch* r2) {
     };
     for (uint64_t i = 0; i < nrec; i++) {
         if (paired) {
-            bv_.reads[2 * i] = view(r1, i);
-            bv_.reads[2 * i + 1] = view(r2, i);
+            reads_[2 * i] = view(r1, i);
+            reads_[2 * i + 1] = view(r2, i);
         } else {
-            bv_.reads[i] = view(r1, i);
+            reads_[i] = view(r1, i);
         }
     }
     max_qlen_ = 1;
-    for (auto& r : bv_.reads) max_qlen_ = std::max(max_qlen_, r.len);
+    bv_.reads = ReadSpan{reads_.data(), reads_.size()};
+    for (auto& r : reads_) max_qlen_ = std::max(max_qlen_, r.len);
     h2d_bytes_ = 0;
-    upload_reads(bv_.reads);
+    upload_reads(reads_);
     SA_CUDA(cudaStreamSynchronize(st_));
     have_batch_ = true;
     stats_.seconds_upload = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -461,7 +464,7 @@ void Mapper::map_uploaded(sa_output* out) {
         p.read_hi = (uint32_t)(rpr * p.rec_hi);
         p.bv = BatchView();
         p.bv.paired = paired;
-        p.bv.reads.assign(bv.reads.begin() + p.read_lo, bv.reads.begin() + p.read_hi);
+        p.bv.reads = ReadSpan{reads_.data() + p.read_lo, (size_t)(p.read_hi - p.read_lo)};
         p.store.reset(p.read_hi - p.read_lo);
         p.n_nams = 0;
         for (size_t c = c0; c < c1; c++) {
@@ -511,7 +514,7 @@ void Mapper::map_uploaded(sa_output* out) {
         total_len += c.out_bytes;
         mapped += c.mapped;
     }
-    out->data = (char*)std::malloc(total_len + 1);
+    out->data = alloc_output(total_len + 1);
     if (!out->data) throw Error(SA_ERR_OOM, "output allocation failed");
     gather_chunk_outputs(chunks, out->data, policy_threads_);
     if (trace_) {

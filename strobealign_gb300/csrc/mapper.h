@@ -63,6 +63,7 @@ class Mapper {
                                                 uint32_t& launches, const std::vector<uint32_t>& anchors,
                                                 uint32_t max_anchors);
     uint32_t schedule(std::vector<ChunkState>& chunks, uint32_t& launches, uint32_t& nam_launches);
+    std::vector<ReadView> reads_;  // the uploaded batch's read views (device read order)
     BatchView bv_;
     bool have_batch_ = false;
     uint32_t max_qlen_ = 1;

@@ -117,8 +117,17 @@ struct ContigInfo {
 };
 
 // Per-read inputs the policy reads
+// A batch's read views: a view into an array its owner keeps (the mapper, a session
+// request), so that batch parts share it without copies
+struct ReadSpan {
+    const ReadView* p = nullptr;
+    size_t n = 0;
+    const ReadView& operator[](size_t i) const { return p[i]; }
+    size_t size() const { return n; }
+};
+
 struct BatchView {
-    std::vector<ReadView> reads;         // device read order (pairs interleaved)
+    ReadSpan reads;                      // device read order (pairs interleaved)
     const NamRec* nams = nullptr;
     const uint64_t* nam_off = nullptr;
     const NamDetailsRec* details = nullptr;

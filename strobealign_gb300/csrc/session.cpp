@@ -64,6 +64,11 @@ Session::Session(const sa_index* idx, const sa_refs* refs, const sa_chaining_par
     trace_ = tr && *tr && *tr != '0';
     // SA_MAX_WAVE_JOBS: extension jobs per wave at most (tuning)
     if (const char* mw = std::getenv("SA_MAX_WAVE_JOBS")) max_wave_jobs_ = std::max<uint64_t>(1, std::strtoull(mw, nullptr, 10));
+    // SA_WAVE_MIN_JOBS: jobs that start a wave while policy threads are still busy;
+    // SA_ADMIT_GROUP_READS: reads one admission takes at most (tuning)
+    if (const char* mj = std::getenv("SA_WAVE_MIN_JOBS")) wave_min_jobs_ = std::max<uint64_t>(1, std::strtoull(mj, nullptr, 10));
+    if (const char* ag = std::getenv("SA_ADMIT_GROUP_READS"))
+        admit_group_reads_ = std::max<uint64_t>(1, std::strtoull(ag, nullptr, 10));
     t0_ = std::chrono::steady_clock::now();
     SA_CUDA(cudaSetDevice(idx->device));
     SA_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
@@ -156,48 +161,80 @@ uint64_t Session::submit(const sa_read_batch* r1, const sa_read_batch* r2) {
     r->n_reads = paired ? 2 * r1->n : r1->n;
     r->has_qual = r1->qual != nullptr && (!paired || r2->qual != nullptr);
     r->has_comments = r1->comments && r1->comment_offsets;
-    r->seq_off.assign(1, 0);
-    r->name_off.assign(1, 0);
-    r->comment_off.assign(1, 0);
-    r->seq_off.reserve(r->n_reads + 1);
-    auto add = [&](const sa_read_batch* b, uint64_t i) {
-        const uint64_t s0 = b->seq_offsets[i], s1 = b->seq_offsets[i + 1];
-        if (s1 - s0 > MAX_READ_LEN)
-            throw Error(SA_ERR_INVALID, "read longer than " + std::to_string(MAX_READ_LEN) + " nt");
-        r->seq.insert(r->seq.end(), b->seq + s0, b->seq + s1);
-        if (r->has_qual) r->qual.insert(r->qual.end(), b->qual + s0, b->qual + s1);
-        r->seq_off.push_back(r->seq.size());
-        const uint64_t n0 = b->name_offsets[i], n1 = b->name_offsets[i + 1];
-        r->names.insert(r->names.end(), b->names + n0, b->names + n1);
-        r->name_off.push_back(r->names.size());
-        if (b->comments && b->comment_offsets) {
-            const uint64_t c0 = b->comment_offsets[i], c1 = b->comment_offsets[i + 1];
-            r->comments.insert(r->comments.end(), b->comments + c0, b->comments + c1);
-        }
-        r->comment_off.push_back(r->comments.size());
-    };
-    for (uint64_t i = 0; i < r1->n; i++) {
-        add(r1, i);
-        if (paired) add(r2, i);
+    const sa_read_batch* mates[2] = {r1, r2};
+    const int nm = paired ? 2 : 1;
+    // qualities, names and comments: one block per mate, copied whole; sequences in
+    // device read order (mates interleaved), as the arena and the NAM pipeline take them
+    uint64_t seq_total = 0, qual_base[2] = {0, 0}, name_base[2] = {0, 0}, com_base[2] = {0, 0};
+    uint64_t qual_total = 0, name_total = 0, com_total = 0;
+    for (int m = 0; m < nm; m++) {
+        const sa_read_batch* b = mates[m];
+        const uint64_t n = b->n;
+        const uint64_t sb = n ? b->seq_offsets[n] - b->seq_offsets[0] : 0;
+        seq_total += sb;
+        qual_base[m] = qual_total;
+        if (r->has_qual) qual_total += sb;
+        name_base[m] = name_total;
+        name_total += n ? b->name_offsets[n] - b->name_offsets[0] : 0;
+        com_base[m] = com_total;
+        if (b->comments && b->comment_offsets)
+            com_total += n ? b->comment_offsets[n] - b->comment_offsets[0] : 0;
     }
-    r->total_bases = r->seq.size();
+    r->qual.resize(qual_total);
+    r->names.resize(name_total);
+    r->comments.resize(com_total);
+    for (int m = 0; m < nm; m++) {
+        const sa_read_batch* b = mates[m];
+        const uint64_t n = b->n;
+        if (!n) continue;
+        if (r->has_qual)
+            std::memcpy(r->qual.data() + qual_base[m], b->qual + b->seq_offsets[0], b->seq_offsets[n] - b->seq_offsets[0]);
+        std::memcpy(r->names.data() + name_base[m], b->names + b->name_offsets[0],
+                    b->name_offsets[n] - b->name_offsets[0]);
+        if (b->comments && b->comment_offsets)
+            std::memcpy(r->comments.data() + com_base[m], b->comments + b->comment_offsets[0],
+                        b->comment_offsets[n] - b->comment_offsets[0]);
+    }
+    r->seq.resize(seq_total);
+    r->seq_off.resize(r->n_reads + 1);
+    r->read_views.resize(r->n_reads);
+    r->bv.paired = paired;
+    uint64_t so = 0;
+    for (uint64_t i = 0; i < r1->n; i++) {
+        for (int m = 0; m < nm; m++) {
+            const sa_read_batch* b = mates[m];
+            const uint64_t s0 = b->seq_offsets[i], s1 = b->seq_offsets[i + 1];
+            if (s1 - s0 > MAX_READ_LEN)
+                throw Error(SA_ERR_INVALID, "read longer than " + std::to_string(MAX_READ_LEN) + " nt");
+            const uint64_t d = paired ? 2 * i + m : i;
+            std::memcpy(r->seq.data() + so, b->seq + s0, s1 - s0);
+            r->seq_off[d] = so;
+            ReadView& v = r->read_views[d];
+            v.seq = r->seq.data() + so;
+            v.len = (uint32_t)(s1 - s0);
+            v.qual = r->has_qual ? r->qual.data() + qual_base[m] + (s0 - b->seq_offsets[0]) : nullptr;
+            const uint64_t n0 = b->name_offsets[i], n1 = b->name_offsets[i + 1];
+            v.name = r->names.data() + name_base[m] + (n0 - b->name_offsets[0]);
+            v.name_len = (uint32_t)(n1 - n0);
+            v.comment = nullptr;
+            v.comment_len = 0;
+            if (b->comments && b->comment_offsets) {
+                const uint64_t c0 = b->comment_offsets[i], c1 = b->comment_offsets[i + 1];
+                if (c1 > c0) {
+                    v.comment = r->comments.data() + com_base[m] + (c0 - b->comment_offsets[0]);
+                    v.comment_len = (uint32_t)(c1 - c0);
+                }
+            }
+            r->max_qlen = std::max(r->max_qlen, v.len);
+            so += s1 - s0;
+        }
+    }
+    r->seq_off[r->n_reads] = so;
+    r->total_bases = so;
     if (r->total_bases > seq_alloc_.capacity() || r->n_reads + 1 > off_alloc_.capacity())
         throw Error(SA_ERR_INVALID, "request larger than the session's in-flight capacity (" +
                                         std::to_string(seq_alloc_.capacity()) + " bases)");
-    r->bv.paired = paired;
-    r->bv.reads.resize(r->n_reads);
-    for (uint64_t i = 0; i < r->n_reads; i++) {
-        ReadView& v = r->bv.reads[i];
-        v.seq = r->seq.data() + r->seq_off[i];
-        v.len = (uint32_t)(r->seq_off[i + 1] - r->seq_off[i]);
-        v.qual = r->has_qual ? r->qual.data() + r->seq_off[i] : nullptr;
-        v.name = r->names.data() + r->name_off[i];
-        v.name_len = (uint32_t)(r->name_off[i + 1] - r->name_off[i]);
-        const uint64_t cl = r->comment_off[i + 1] - r->comment_off[i];
-        v.comment = cl ? r->comments.data() + r->comment_off[i] : nullptr;
-        v.comment_len = (uint32_t)cl;
-        r->max_qlen = std::max(r->max_qlen, v.len);
-    }
+    r->bv.reads = ReadSpan{r->read_views.data(), r->read_views.size()};
     r->t_submit = std::chrono::steady_clock::now();
     uint64_t id;
     {
@@ -626,7 +663,7 @@ void Session::complete(Request& r) {
         r.mapped += c.mapped;
         r.d2h_bytes += c.result_bytes;
     }
-    r.out = (char*)std::malloc(total + 1);
+    r.out = alloc_output(total + 1);
     if (r.out) {
         gather_chunk_outputs(r.chunks, r.out, total >= (64u << 20) ? 4 : 1);
         r.out[total] = 0;

@@ -44,8 +44,11 @@ struct Request {
     bool paired = false;
     // owned copies of the records
     std::vector<char> seq, qual, names, comments;
-    std::vector<uint64_t> seq_off, name_off, comment_off;  // per device read
+    // sequences in device read order (mates interleaved) with per-read offsets;
+    // qualities, names and comments one block per mate (read views point into them)
+    std::vector<uint64_t> seq_off;
     bool has_qual = false, has_comments = false;
+    std::vector<ReadView> read_views;  // device read order; bv.reads views them
     BatchView bv;
     uint64_t nrec = 0, n_reads = 0, total_bases = 0;
     uint32_t max_qlen = 1;

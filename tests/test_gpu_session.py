@@ -114,3 +114,24 @@ def test_session_abundance_mode_matches_mapper(setup):
         m.map(x, y)
     np.testing.assert_allclose(total, m.abundances(), rtol=1e-12, atol=0)
     s.close()
+
+
+def test_session_comments_and_missing_qualities(setup):
+    # FASTQ comments (--fastq-comments) and reads without qualities go through a
+    # session's record copies as through the mapper
+    sa, refs, idx, r1, r2 = setup
+    n = 500
+    seqs1 = [bytes(r1.seq[r1.offsets[i]:r1.offsets[i + 1]]) for i in range(n)]
+    seqs2 = [bytes(r2.seq[r2.offsets[i]:r2.offsets[i + 1]]) for i in range(n)]
+    names = [f"q{i}" for i in range(n)]
+    comments = [f"BX:Z:{i % 7}" if i % 3 else "" for i in range(n)]
+    a1 = sa.Reads.from_lists(names, seqs1, comments=comments)
+    a2 = sa.Reads.from_lists(names, seqs2, comments=comments)
+    for kw in (dict(fastq_comments=1), dict()):
+        want = sa.Mapper(idx, refs, **kw).map(a1, a2)
+        s = sa.Session(idx, refs, **kw)
+        t = [s.submit(a1, a2), s.submit(a1, None)]
+        got = [s.wait(x)[0] for x in t]
+        assert got[0] == want
+        assert got[1] == sa.Mapper(idx, refs, **kw).map(a1, None)
+        s.close()
