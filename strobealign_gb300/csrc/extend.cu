@@ -2296,7 +2296,9 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
         auto a16 = [](uint64_t x) { return (x + 15) & ~(uint64_t)15; };
         const uint64_t cells = a16(((uint64_t)max_qlen + 1) * ((uint64_t)max_pw_window + 1));
         const uint64_t opsb = a16((uint64_t)max_qlen + max_pw_window + 8) + a16(8ull * (max_anchors + 1));
-        const unsigned blocks = (unsigned)std::min<uint64_t>(n, 152ULL * 6);
+        // single-warp blocks, up to 16 per SM: the per-job work is mostly serial (anchor
+        // pruning, gap checks, traceback pushes), so more resident warps hide its latency
+        const unsigned blocks = (unsigned)std::min<uint64_t>(n, 152ULL * 16);
         ws.pw_scratch.reserve((cells + opsb) * blocks);
         const size_t smem = 16 * ((size_t)max_pw_window + 2);
         static size_t attr = 0;

@@ -4,12 +4,37 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <memory>
 #include <cstring>
 #include <string>
 #include <thread>
 #include <vector>
 
 namespace sa {
+
+// Array of trivially constructible elements allocated without initialisation (a
+// vector resize value-initialises what is then overwritten anyway); resize drops the
+// contents
+template <class T>
+struct PodArray {
+    std::unique_ptr<T[]> p;
+    size_t n = 0, cap = 0;
+    void resize(size_t k) {
+        if (k > cap) {
+            p.reset(new T[k]);
+            cap = k;
+        }
+        n = k;
+    }
+    T* data() { return p.get(); }
+    const T* data() const { return p.get(); }
+    size_t size() const { return n; }
+    T& operator[](size_t i) { return p[i]; }
+    const T& operator[](size_t i) const { return p[i]; }
+    T* begin() { return p.get(); }
+    T* end() { return p.get() + n; }
+};
+using RawBytes = PodArray<char>;
 
 // Output buffer for the caller (released with free()): large ones 2 MiB aligned and
 // advised to use huge pages, so that the first touch of hundreds of MB faults in few
@@ -22,6 +47,35 @@ inline char* alloc_output(size_t bytes) {
     madvise(p, bytes, MADV_HUGEPAGE);
 #endif
     return (char*)p;
+}
+
+// fn(begin, end) over [0, n) split into `threads` contiguous ranges on their own threads
+template <class F>
+inline void parallel_ranges(uint64_t n, unsigned threads, F fn) {
+    threads = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(threads, n / 4096 + 1));
+    if (threads == 1) {
+        fn((uint64_t)0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < threads; t++) th.emplace_back(fn, n * t / threads, n * (t + 1) / threads);
+    for (auto& x : th) x.join();
+}
+
+// memcpy split over threads for large copies
+inline void parallel_memcpy(void* dst, const void* src, size_t bytes, unsigned threads) {
+    const size_t per = (size_t)4 << 20;
+    threads = (unsigned)std::max<size_t>(1, std::min<size_t>(threads, bytes / per + 1));
+    if (threads == 1) {
+        if (bytes) std::memcpy(dst, src, bytes);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < threads; t++) {
+        const size_t a = bytes * t / threads, b = bytes * (t + 1) / threads;
+        th.emplace_back([=] { std::memcpy((char*)dst + a, (const char*)src + a, b - a); });
+    }
+    for (auto& x : th) x.join();
 }
 
 // One copy of every chunk's output pieces into dst with up to `threads` threads,

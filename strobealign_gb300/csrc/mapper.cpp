@@ -76,12 +76,12 @@ Mapper::~Mapper() {
     if (stn_) cudaStreamDestroy(stn_);
 }
 
-void Mapper::upload_reads(const std::vector<ReadView>& reads) {
+void Mapper::upload_reads(const ReadSpan& reads) {
     uint64_t total = 0;
-    for (auto& r : reads) {
-        if (r.len > MAX_READ_LEN)
+    for (size_t i = 0; i < reads.size(); i++) {
+        if (reads[i].len > MAX_READ_LEN)
             throw Error(SA_ERR_INVALID, "read longer than " + std::to_string(MAX_READ_LEN) + " nt");
-        total += r.len;
+        total += reads[i].len;
     }
     const uint32_t n = (uint32_t)reads.size();
     h_seq_.reserve(total + 16);
@@ -89,10 +89,13 @@ void Mapper::upload_reads(const std::vector<ReadView>& reads) {
     uint64_t o = 0;
     for (uint32_t i = 0; i < n; i++) {
         h_off_.p[i] = o;
-        std::memcpy(h_seq_.p + o, reads[i].seq, reads[i].len);
         o += reads[i].len;
     }
     h_off_.p[n] = o;
+    // the bases into pinned staging, in parallel
+    parallel_ranges(n, policy_threads_, [&](uint64_t a, uint64_t b) {
+        for (uint64_t i = a; i < b; i++) std::memcpy(h_seq_.p + h_off_.p[i], reads[i].seq, reads[i].len);
+    });
     nws_.seq.reserve(total + 16);
     nws_.off.reserve((size_t)n + 1);
     SA_CUDA(cudaMemcpyAsync(nws_.seq.p, h_seq_.p, total, cudaMemcpyHostToDevice, st_));
@@ -205,19 +208,21 @@ void Mapper::upload(const sa_read_batch* r1, const sa_read_batch* r2) {
         }
         return v;
     };
-    for (uint64_t i = 0; i < nrec; i++) {
-        if (paired) {
-            reads_[2 * i] = view(r1, i);
-            reads_[2 * i + 1] = view(r2, i);
-        } else {
-            reads_[i] = view(r1, i);
+    parallel_ranges(nrec, policy_threads_, [&](uint64_t a, uint64_t b) {
+        for (uint64_t i = a; i < b; i++) {
+            if (paired) {
+                reads_[2 * i] = view(r1, i);
+                reads_[2 * i + 1] = view(r2, i);
+            } else {
+                reads_[i] = view(r1, i);
+            }
         }
-    }
+    });
     max_qlen_ = 1;
     bv_.reads = ReadSpan{reads_.data(), reads_.size()};
     for (auto& r : reads_) max_qlen_ = std::max(max_qlen_, r.len);
     h2d_bytes_ = 0;
-    upload_reads(reads_);
+    upload_reads(bv_.reads);
     SA_CUDA(cudaStreamSynchronize(st_));
     have_batch_ = true;
     stats_.seconds_upload = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

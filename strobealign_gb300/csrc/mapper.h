@@ -4,6 +4,7 @@
 #include <chrono>
 #include <thread>
 
+#include "host_util.h"
 #include "policy.h"
 
 namespace sa {
@@ -26,7 +27,7 @@ class Mapper {
     NamWorkspace& nam_ws() { return nws_; }
     ExtWorkspace& ext_ws() { return ews_; }
     cudaStream_t stream() const { return st_; }
-    void upload_reads(const std::vector<ReadView>& reads);
+    void upload_reads(const ReadSpan& reads);
     uint32_t n_reads() const { return n_reads_; }
     uint64_t total_bases() const { return total_bases_; }
     uint64_t h2d_bytes() const { return h2d_bytes_; }
@@ -63,7 +64,7 @@ class Mapper {
                                                 uint32_t& launches, const std::vector<uint32_t>& anchors,
                                                 uint32_t max_anchors);
     uint32_t schedule(std::vector<ChunkState>& chunks, uint32_t& launches, uint32_t& nam_launches);
-    std::vector<ReadView> reads_;  // the uploaded batch's read views (device read order)
+    PodArray<ReadView> reads_;  // the uploaded batch's read views (device read order)
     BatchView bv_;
     bool have_batch_ = false;
     uint32_t max_qlen_ = 1;

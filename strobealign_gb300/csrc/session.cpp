@@ -188,7 +188,8 @@ uint64_t Session::submit(const sa_read_batch* r1, const sa_read_batch* r2) {
         const uint64_t n = b->n;
         if (!n) continue;
         if (r->has_qual)
-            std::memcpy(r->qual.data() + qual_base[m], b->qual + b->seq_offsets[0], b->seq_offsets[n] - b->seq_offsets[0]);
+            parallel_memcpy(r->qual.data() + qual_base[m], b->qual + b->seq_offsets[0],
+                            b->seq_offsets[n] - b->seq_offsets[0], 8);
         std::memcpy(r->names.data() + name_base[m], b->names + b->name_offsets[0],
                     b->name_offsets[n] - b->name_offsets[0]);
         if (b->comments && b->comment_offsets)
@@ -199,36 +200,50 @@ uint64_t Session::submit(const sa_read_batch* r1, const sa_read_batch* r2) {
     r->seq_off.resize(r->n_reads + 1);
     r->read_views.resize(r->n_reads);
     r->bv.paired = paired;
+    // offsets first (a prefix sum), then the copies and views in parallel
     uint64_t so = 0;
     for (uint64_t i = 0; i < r1->n; i++) {
         for (int m = 0; m < nm; m++) {
             const sa_read_batch* b = mates[m];
-            const uint64_t s0 = b->seq_offsets[i], s1 = b->seq_offsets[i + 1];
-            if (s1 - s0 > MAX_READ_LEN)
+            const uint64_t len = b->seq_offsets[i + 1] - b->seq_offsets[i];
+            if (len > MAX_READ_LEN)
                 throw Error(SA_ERR_INVALID, "read longer than " + std::to_string(MAX_READ_LEN) + " nt");
-            const uint64_t d = paired ? 2 * i + m : i;
-            std::memcpy(r->seq.data() + so, b->seq + s0, s1 - s0);
-            r->seq_off[d] = so;
-            ReadView& v = r->read_views[d];
-            v.seq = r->seq.data() + so;
-            v.len = (uint32_t)(s1 - s0);
-            v.qual = r->has_qual ? r->qual.data() + qual_base[m] + (s0 - b->seq_offsets[0]) : nullptr;
-            const uint64_t n0 = b->name_offsets[i], n1 = b->name_offsets[i + 1];
-            v.name = r->names.data() + name_base[m] + (n0 - b->name_offsets[0]);
-            v.name_len = (uint32_t)(n1 - n0);
-            v.comment = nullptr;
-            v.comment_len = 0;
-            if (b->comments && b->comment_offsets) {
-                const uint64_t c0 = b->comment_offsets[i], c1 = b->comment_offsets[i + 1];
-                if (c1 > c0) {
-                    v.comment = r->comments.data() + com_base[m] + (c0 - b->comment_offsets[0]);
-                    v.comment_len = (uint32_t)(c1 - c0);
-                }
-            }
-            r->max_qlen = std::max(r->max_qlen, v.len);
-            so += s1 - s0;
+            r->seq_off[paired ? 2 * i + m : i] = so;
+            so += len;
         }
     }
+    const unsigned copy_threads = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+    parallel_ranges(r1->n, copy_threads, [&](uint64_t ia, uint64_t ib) {
+        uint32_t mq = 1;
+        for (uint64_t i = ia; i < ib; i++) {
+            for (int m = 0; m < nm; m++) {
+                const sa_read_batch* b = mates[m];
+                const uint64_t s0 = b->seq_offsets[i], s1 = b->seq_offsets[i + 1];
+                const uint64_t d = paired ? 2 * i + m : i;
+                const uint64_t at = r->seq_off[d];
+                std::memcpy(r->seq.data() + at, b->seq + s0, s1 - s0);
+                ReadView& v = r->read_views[d];
+                v.seq = r->seq.data() + at;
+                v.len = (uint32_t)(s1 - s0);
+                v.qual = r->has_qual ? r->qual.data() + qual_base[m] + (s0 - b->seq_offsets[0]) : nullptr;
+                const uint64_t n0 = b->name_offsets[i], n1 = b->name_offsets[i + 1];
+                v.name = r->names.data() + name_base[m] + (n0 - b->name_offsets[0]);
+                v.name_len = (uint32_t)(n1 - n0);
+                v.comment = nullptr;
+                v.comment_len = 0;
+                if (b->comments && b->comment_offsets) {
+                    const uint64_t c0 = b->comment_offsets[i], c1 = b->comment_offsets[i + 1];
+                    if (c1 > c0) {
+                        v.comment = r->comments.data() + com_base[m] + (c0 - b->comment_offsets[0]);
+                        v.comment_len = (uint32_t)(c1 - c0);
+                    }
+                }
+                mq = std::max(mq, v.len);
+            }
+        }
+        std::lock_guard<std::mutex> g(r->max_qlen_mu);
+        r->max_qlen = std::max(r->max_qlen, mq);
+    });
     r->seq_off[r->n_reads] = so;
     r->total_bases = so;
     if (r->total_bases > seq_alloc_.capacity() || r->n_reads + 1 > off_alloc_.capacity())

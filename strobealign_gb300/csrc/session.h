@@ -16,6 +16,7 @@
 #include <thread>
 #include <unordered_map>
 
+#include "host_util.h"
 #include "policy.h"
 
 namespace sa {
@@ -43,15 +44,16 @@ struct Request {
     uint64_t id = 0;
     bool paired = false;
     // owned copies of the records
-    std::vector<char> seq, qual, names, comments;
+    RawBytes seq, qual, names, comments;
     // sequences in device read order (mates interleaved) with per-read offsets;
     // qualities, names and comments one block per mate (read views point into them)
     std::vector<uint64_t> seq_off;
     bool has_qual = false, has_comments = false;
-    std::vector<ReadView> read_views;  // device read order; bv.reads views them
+    PodArray<ReadView> read_views;  // device read order; bv.reads views them
     BatchView bv;
     uint64_t nrec = 0, n_reads = 0, total_bases = 0;
     uint32_t max_qlen = 1;
+    std::mutex max_qlen_mu;  // guards max_qlen while submit's copy threads run
     // device placement (arena units: bases, offset slots)
     uint64_t seq_base = 0, read_base = 0;
     // NAMs copied back from the device
