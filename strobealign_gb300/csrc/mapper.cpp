@@ -162,21 +162,21 @@ void Mapper::part_nams(Part& p, uint32_t& launches) {
 }
 
 std::shared_ptr<const WaveResults> Mapper::run_wave(const ExtJob* jobs, uint32_t nj, uint32_t max_qlen,
-                                                    uint32_t& launches, const std::vector<uint32_t>& anchors,
-                                                    uint32_t max_anchors) {
+                                                    uint32_t& launches, const uint32_t* anchors,
+                                                    size_t anchor_words, uint32_t max_anchors) {
     auto w = std::make_shared<WaveResults>();
     if (!nj) return w;
     ews_.jobs.reserve(nj);
     SA_CUDA(cudaMemcpyAsync(ews_.jobs.p, jobs, (size_t)nj * sizeof(ExtJob), cudaMemcpyHostToDevice, st_));
     h2d_bytes_ += (size_t)nj * sizeof(ExtJob);
-    if (!anchors.empty()) {
-        ews_.anchors.reserve(anchors.size());
-        SA_CUDA(cudaMemcpyAsync(ews_.anchors.p, anchors.data(), anchors.size() * 4, cudaMemcpyHostToDevice, st_));
-        h2d_bytes_ += anchors.size() * 4;
+    if (anchor_words) {
+        ews_.anchors.reserve(anchor_words);
+        SA_CUDA(cudaMemcpyAsync(ews_.anchors.p, anchors, anchor_words * 4, cudaMemcpyHostToDevice, st_));
+        h2d_bytes_ += anchor_words * 4;
     }
     AlignScores sc{mp_.match, mp_.mismatch, mp_.gap_open, mp_.gap_extend, mp_.end_bonus};
     launches += run_extension(refs_view_, nws_, idx_->sp.k, sc, nj, ews_, max_qlen, st_, &kt_,
-                              anchors.empty() ? nullptr : ews_.anchors.p, max_anchors);
+                              anchor_words ? ews_.anchors.p : nullptr, max_anchors);
     d2h_bytes_ += (size_t)nj * sizeof(ExtResult) + ews_.total_cigar * 4;
     for (int c = 0; c < 5; c++) sw_cells_[c] += ews_.cells[c];
     w->results.swap(ews_.h_results);
@@ -370,25 +370,38 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, uint32_t& launches, u
             for (size_t c : batch) nj += chunks[c].pending.size();
             h_jobs_.reserve(std::max<size_t>(nj, 1));
             nj = 0;
-            wave_anchors_.clear();
             uint32_t max_anchors = 0;
+            uint64_t n_anc = 0;
             for (size_t c : batch) {
                 const Part& p = *parts_[chunks[c].part];
                 const size_t j0 = nj, cnt = chunks[c].pending.size();
                 chunks[c].wave_first = nj;
                 std::memcpy(h_jobs_.p + nj, chunks[c].pending.data(), cnt * sizeof(ExtJob));
                 nj += cnt;
-                // anchors are looked up with the part's read indices; the device reads
-                // of the whole batch are indexed from the part's first read
-                if (p.bv.nam_anc) {
-                    attach_piecewise_anchors(p.bv, h_jobs_.p + j0, cnt, wave_anchors_);
-                    for (size_t j = j0; j < nj; j++) max_anchors = std::max(max_anchors, h_jobs_.p[j].anc_n);
-                }
-                for (size_t j = j0; j < nj; j++) h_jobs_.p[j].read += p.read_lo;
+                // anchors are looked up with the part's read indices
+                if (p.bv.nam_anc) n_anc += piecewise_anchor_offsets(p.bv, h_jobs_.p + j0, cnt, n_anc, max_anchors);
+            }
+            wave_anchors_.resize(2 * n_anc);
+            if (n_anc)
+                parallel_ranges(batch.size(), policy_threads_, [&](uint64_t a, uint64_t b) {
+                    for (uint64_t k = a; k < b; k++) {
+                        const ChunkState& cs = chunks[batch[k]];
+                        const Part& p = *parts_[cs.part];
+                        if (p.bv.nam_anc)
+                            piecewise_anchor_fill(p.bv, h_jobs_.p + cs.wave_first, cs.pending.size(),
+                                                  wave_anchors_.data());
+                    }
+                });
+            // the device reads of the whole batch are indexed from the part's first read
+            for (size_t c : batch) {
+                const uint32_t lo = parts_[chunks[c].part]->read_lo;
+                ExtJob* j = h_jobs_.p + chunks[c].wave_first;
+                for (size_t x = 0; x < chunks[c].pending.size(); x++) j[x].read += lo;
             }
             if (waves > 1000000) throw Error(SA_ERR_INVALID, "internal: extension waves do not converge");
             auto tw = std::chrono::steady_clock::now();
-            auto wres = run_wave(h_jobs_.p, (uint32_t)nj, max_qlen_, launches, wave_anchors_, max_anchors);
+            auto wres = run_wave(h_jobs_.p, (uint32_t)nj, max_qlen_, launches, wave_anchors_.data(),
+                                 wave_anchors_.size(), max_anchors);
             for (size_t c : batch) chunks[c].wave = wres;
             const auto tw2 = std::chrono::steady_clock::now();
             t_ext_ += std::chrono::duration<double>(tw2 - tw).count();

@@ -61,7 +61,7 @@ class Mapper {
     };
     void part_nams(Part& p, uint32_t& launches);
     std::shared_ptr<const WaveResults> run_wave(const ExtJob* jobs, uint32_t nj, uint32_t max_qlen,
-                                                uint32_t& launches, const std::vector<uint32_t>& anchors,
+                                                uint32_t& launches, const uint32_t* anchors, size_t anchor_words,
                                                 uint32_t max_anchors);
     uint32_t schedule(std::vector<ChunkState>& chunks, uint32_t& launches, uint32_t& nam_launches);
     PodArray<ReadView> reads_;  // the uploaded batch's read views (device read order)
@@ -104,7 +104,7 @@ class Mapper {
     PinnedBuf<uint64_t> h_poff_;  // a part's local read offsets
     double t_nams_ = 0;
     std::chrono::steady_clock::time_point t_map0_;  // start of the current map (trace times)
-    std::vector<uint32_t> wave_anchors_;
+    PodArray<uint32_t> wave_anchors_;  // a wave's piecewise anchors (query, reference start pairs)
     uint32_t n_reads_ = 0;
     uint64_t total_bases_ = 0;
     std::atomic<uint64_t> h2d_bytes_{0}, d2h_bytes_{0};

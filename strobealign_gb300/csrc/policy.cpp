@@ -646,19 +646,35 @@ ExtJob Policy::nam_job(uint32_t read, const NamRec& cur, uint32_t kind) const {
     return j;
 }
 
-void attach_piecewise_anchors(const BatchView& bv, ExtJob* jobs, size_t n, std::vector<uint32_t>& anchors) {
-    const uint64_t qmask = (1ull << bv.anc_qbits) - 1, pmask = (1ull << bv.anc_pbits) - 1;
+static bool is_piecewise(const BatchView& bv, const ExtJob& j) {
+    return !j.use_ssw && (j.kind == JOB_EXTEND_FAST || j.kind == JOB_EXTEND_FULL) && bv.nam_anc;
+}
+
+uint64_t piecewise_anchor_offsets(const BatchView& bv, ExtJob* jobs, size_t n, uint64_t first, uint32_t& max_n) {
+    uint64_t at = first;
     for (size_t i = 0; i < n; i++) {
         ExtJob& j = jobs[i];
-        if (j.use_ssw || (j.kind != JOB_EXTEND_FAST && j.kind != JOB_EXTEND_FULL) || !bv.nam_anc) continue;
+        if (!is_piecewise(bv, j)) continue;
         const uint64_t t = bv.nam_off[j.read] + j.nam;
-        const uint64_t a0 = bv.nam_anc_off[t], a1 = bv.nam_anc_off[t + 1];
-        j.anc_off = (uint32_t)(anchors.size() / 2);
-        j.anc_n = (uint32_t)(a1 - a0);
-        for (uint64_t a = a0; a < a1; a++) {
-            const uint64_t key = bv.nam_anc[a];
-            anchors.push_back((uint32_t)(key & qmask));
-            anchors.push_back((uint32_t)((key >> bv.anc_qbits) & pmask));
+        j.anc_off = (uint32_t)at;
+        j.anc_n = (uint32_t)(bv.nam_anc_off[t + 1] - bv.nam_anc_off[t]);
+        max_n = std::max(max_n, j.anc_n);
+        at += j.anc_n;
+    }
+    return at - first;
+}
+
+void piecewise_anchor_fill(const BatchView& bv, const ExtJob* jobs, size_t n, uint32_t* anchors) {
+    const uint64_t qmask = (1ull << bv.anc_qbits) - 1, pmask = (1ull << bv.anc_pbits) - 1;
+    for (size_t i = 0; i < n; i++) {
+        const ExtJob& j = jobs[i];
+        if (!is_piecewise(bv, j)) continue;
+        const uint64_t a0 = bv.nam_anc_off[bv.nam_off[j.read] + j.nam];
+        uint32_t* o = anchors + 2 * (uint64_t)j.anc_off;
+        for (uint32_t a = 0; a < j.anc_n; a++) {
+            const uint64_t key = bv.nam_anc[a0 + a];
+            o[2 * a] = (uint32_t)(key & qmask);
+            o[2 * a + 1] = (uint32_t)((key >> bv.anc_qbits) & pmask);
         }
     }
 }

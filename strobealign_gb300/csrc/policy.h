@@ -139,9 +139,13 @@ struct BatchView {
     uint32_t anc_qbits = 0, anc_pbits = 0;
 };
 
-// Appends the anchors of piecewise jobs (use_ssw == 0) to `anchors` as (query
-// start, reference start) pairs and points the jobs at them; other jobs untouched.
-void attach_piecewise_anchors(const BatchView& bv, ExtJob* jobs, size_t n, std::vector<uint32_t>& anchors);
+// The anchors of piecewise jobs (use_ssw == 0) as (query start, reference start)
+// pairs of a wave's anchor array, in two passes: offsets points the jobs at
+// consecutive ranges from anchor `first` on (returns how many anchors they take and
+// raises max_n to the largest count); fill writes them (independent per job, so
+// callers may split it over threads).  Other jobs are untouched.
+uint64_t piecewise_anchor_offsets(const BatchView& bv, ExtJob* jobs, size_t n, uint64_t first, uint32_t& max_n);
+void piecewise_anchor_fill(const BatchView& bv, const ExtJob* jobs, size_t n, uint32_t* anchors);
 
 struct ChunkState {
     uint64_t first = 0, next = 0, end = 0;  // record range [first, end), cursor next

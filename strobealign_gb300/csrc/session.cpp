@@ -575,37 +575,47 @@ void Session::run_wave(std::vector<std::pair<Request*, size_t>>& batch) {
     h_jobs_.reserve(nj);
     size_t o = 0;
     Request* last = nullptr;
-    wave_anchors_.clear();
     uint32_t max_anchors = 0;
+    uint64_t n_anc = 0;
     for (auto& b : batch) {
         Request* r = b.first;
         ChunkState& cs = r->chunks[b.second];
         cs.wave_first = o;
-        const uint32_t base = (uint32_t)r->read_base;
         const size_t o0 = o;
         for (const ExtJob& j : cs.pending) h_jobs_.p[o++] = j;
-        if (r->bv.nam_anc) {
-            // anchors are looked up with the request's own read indices
-            attach_piecewise_anchors(r->bv, h_jobs_.p + o0, o - o0, wave_anchors_);
-            for (size_t x = o0; x < o; x++) max_anchors = std::max(max_anchors, h_jobs_.p[x].anc_n);
-        }
-        for (size_t x = o0; x < o; x++) h_jobs_.p[x].read += base;
+        // anchors are looked up with the request's own read indices
+        if (r->bv.nam_anc) n_anc += piecewise_anchor_offsets(r->bv, h_jobs_.p + o0, o - o0, n_anc, max_anchors);
         r->h2d_bytes += cs.pending.size() * sizeof(ExtJob);
         if (r != last) {
             r->waves++;
             last = r;
         }
     }
+    wave_anchors_.resize(2 * n_anc);
+    if (n_anc)
+        parallel_ranges(batch.size(), 8, [&](uint64_t a, uint64_t b) {
+            for (uint64_t k = a; k < b; k++) {
+                const Request* r = batch[k].first;
+                const ChunkState& cs = r->chunks[batch[k].second];
+                if (r->bv.nam_anc)
+                    piecewise_anchor_fill(r->bv, h_jobs_.p + cs.wave_first, cs.pending.size(), wave_anchors_.data());
+            }
+        });
+    for (auto& b : batch) {
+        const ChunkState& cs = b.first->chunks[b.second];
+        const uint32_t base = (uint32_t)b.first->read_base;
+        for (size_t x = 0; x < cs.pending.size(); x++) h_jobs_.p[cs.wave_first + x].read += base;
+    }
     ews_.jobs.reserve(nj);
     SA_CUDA(cudaMemcpyAsync(ews_.jobs.p, h_jobs_.p, nj * sizeof(ExtJob), cudaMemcpyHostToDevice, st_));
-    if (!wave_anchors_.empty()) {
+    if (wave_anchors_.size()) {
         ews_.anchors.reserve(wave_anchors_.size());
         SA_CUDA(cudaMemcpyAsync(ews_.anchors.p, wave_anchors_.data(), wave_anchors_.size() * 4,
                                 cudaMemcpyHostToDevice, st_));
     }
     AlignScores sc{mp_.match, mp_.mismatch, mp_.gap_open, mp_.gap_extend, mp_.end_bonus};
     run_extension_raw(refs_view_, arena_seq_.p, arena_off_.p, nullptr, nullptr, idx_->sp.k, sc, (uint32_t)nj, ews_,
-                      max_qlen, st_, nullptr, wave_anchors_.empty() ? nullptr : ews_.anchors.p, max_anchors);
+                      max_qlen, st_, nullptr, wave_anchors_.size() ? ews_.anchors.p : nullptr, max_anchors);
     auto w = std::make_shared<WaveResults>();
     w->results.swap(ews_.h_results);
     w->cigar.swap(ews_.h_cigar);

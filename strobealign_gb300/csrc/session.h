@@ -141,7 +141,7 @@ class Session {
     DevRefs refs_view_{};
     ExtWorkspace ews_;
     PinnedBuf<ExtJob> h_jobs_;
-    std::vector<uint32_t> wave_anchors_;
+    PodArray<uint32_t> wave_anchors_;  // a wave's piecewise anchors (query, reference start pairs)
     // read arena
     DevBuf<uint8_t> arena_seq_;
     DevBuf<uint64_t> arena_off_;
