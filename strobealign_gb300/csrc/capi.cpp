@@ -378,7 +378,7 @@ int32_t sa_map_batch(sa_mapper* m, const sa_read_batch* r1, const sa_read_batch*
 
 void sa_output_free(sa_output* out) {
     if (!out) return;
-    std::free(out->data);
+    release_output(out->data);
     out->data = nullptr;
     out->len = 0;
 }

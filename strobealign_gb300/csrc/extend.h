@@ -1,6 +1,7 @@
 // Extension pipeline (extend.cu): extend_seed / rescue_align / Aligner::align for a
 // list of jobs.
 #pragma once
+#include "host_util.h"
 #include "pipeline.h"
 
 namespace sa {
@@ -61,9 +62,10 @@ struct ExtWorkspace {
     DevBuf<uint64_t> raw_size, raw_off;
     DevBuf<uint32_t> raw;
     DevBuf<uint8_t> cub_tmp;
-    // host mirrors
-    std::vector<ExtResult> h_results;
-    std::vector<uint32_t> h_cigar;
+    // host mirrors (capacity kept across waves; the callers swap them with pooled
+    // wave buffers)
+    PodArray<ExtResult> h_results;
+    PodArray<uint32_t> h_cigar;
     uint64_t total_cigar = 0;
     uint64_t cells[5] = {0, 0, 0, 0, 0};  // SW cells: canonical, then computed forward byte / word, reverse byte / word
 };

@@ -5,6 +5,8 @@
 #include <algorithm>
 #include <cstdlib>
 #include <memory>
+#include <mutex>
+#include <unordered_map>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -29,6 +31,7 @@ struct PodArray {
     T* data() { return p.get(); }
     const T* data() const { return p.get(); }
     size_t size() const { return n; }
+    void clear() { n = 0; }
     T& operator[](size_t i) { return p[i]; }
     const T& operator[](size_t i) const { return p[i]; }
     T* begin() { return p.get(); }
@@ -36,18 +39,65 @@ struct PodArray {
 };
 using RawBytes = PodArray<char>;
 
-// Output buffer for the caller (released with free()): large ones 2 MiB aligned and
-// advised to use huge pages, so that the first touch of hundreds of MB faults in few
-// pages.
-inline char* alloc_output(size_t bytes) {
-    if (bytes < (64u << 20)) return (char*)std::malloc(bytes);
-    void* p = nullptr;
-    if (posix_memalign(&p, 2u << 20, bytes) != 0) return nullptr;
+// Output buffers handed to the caller (released with release_output, which
+// sa_output_free calls).  Large ones are 2 MiB aligned and advised to use huge pages,
+// and a few released ones are kept for reuse: a stream of batches then writes its SAM
+// into memory that is already paged in instead of faulting in hundreds of MB each time.
+class OutputPool {
+  public:
+    static constexpr size_t LARGE = (size_t)64 << 20;
+    char* alloc(size_t bytes) {
+        if (bytes < LARGE) return (char*)std::malloc(bytes);
+        std::lock_guard<std::mutex> g(mu_);
+        size_t best = free_.size();
+        for (size_t i = 0; i < free_.size(); i++)
+            if (free_[i].second >= bytes && (best == free_.size() || free_[i].second < free_[best].second)) best = i;
+        if (best < free_.size()) {
+            const auto it = free_[best];
+            free_.erase(free_.begin() + (ptrdiff_t)best);
+            kept_ -= it.second;
+            caps_[it.first] = it.second;
+            return it.first;
+        }
+        void* p = nullptr;
+        if (posix_memalign(&p, (size_t)2 << 20, bytes) != 0) return nullptr;
 #ifdef MADV_HUGEPAGE
-    madvise(p, bytes, MADV_HUGEPAGE);
+        madvise(p, bytes, MADV_HUGEPAGE);
 #endif
-    return (char*)p;
+        caps_[(char*)p] = bytes;
+        return (char*)p;
+    }
+    void release(char* p) {
+        if (!p) return;
+        std::lock_guard<std::mutex> g(mu_);
+        const auto it = caps_.find(p);
+        if (it == caps_.end()) {
+            std::free(p);
+            return;
+        }
+        const size_t cap = it->second;
+        caps_.erase(it);
+        if (free_.size() < 4 && kept_ + cap <= ((size_t)8 << 30)) {
+            free_.emplace_back(p, cap);
+            kept_ += cap;
+        } else {
+            std::free(p);
+        }
+    }
+
+  private:
+    std::mutex mu_;
+    std::unordered_map<char*, size_t> caps_;        // large buffers handed out
+    std::vector<std::pair<char*, size_t>> free_;    // released, kept for reuse
+    size_t kept_ = 0;
+};
+
+inline OutputPool& output_pool() {
+    static OutputPool pool;
+    return pool;
 }
+inline char* alloc_output(size_t bytes) { return output_pool().alloc(bytes); }
+inline void release_output(char* p) { output_pool().release(p); }
 
 // fn(begin, end) over [0, n) split into `threads` contiguous ranges on their own threads
 template <class F>

@@ -164,8 +164,13 @@ void Mapper::part_nams(Part& p, uint32_t& launches) {
 std::shared_ptr<const WaveResults> Mapper::run_wave(const ExtJob* jobs, uint32_t nj, uint32_t max_qlen,
                                                     uint32_t& launches, const uint32_t* anchors,
                                                     size_t anchor_words, uint32_t max_anchors) {
-    auto w = std::make_shared<WaveResults>();
+    std::shared_ptr<WaveResults> w = wave_pool_.take();
+    w->results.clear();
+    w->cigar.clear();
     if (!nj) return w;
+    // the pooled buffers (with their capacity) take the copy back
+    std::swap(w->results, ews_.h_results);
+    std::swap(w->cigar, ews_.h_cigar);
     ews_.jobs.reserve(nj);
     SA_CUDA(cudaMemcpyAsync(ews_.jobs.p, jobs, (size_t)nj * sizeof(ExtJob), cudaMemcpyHostToDevice, st_));
     h2d_bytes_ += (size_t)nj * sizeof(ExtJob);
@@ -179,8 +184,8 @@ std::shared_ptr<const WaveResults> Mapper::run_wave(const ExtJob* jobs, uint32_t
                               anchor_words ? ews_.anchors.p : nullptr, max_anchors);
     d2h_bytes_ += (size_t)nj * sizeof(ExtResult) + ews_.total_cigar * 4;
     for (int c = 0; c < 5; c++) sw_cells_[c] += ews_.cells[c];
-    w->results.swap(ews_.h_results);
-    w->cigar.swap(ews_.h_cigar);
+    std::swap(w->results, ews_.h_results);
+    std::swap(w->cigar, ews_.h_cigar);
     jobs_run_ += nj;
     return w;
 }
@@ -461,6 +466,17 @@ void Mapper::map_uploaded(sa_output* out) {
         ChunkState cs;
         cs.first = cs.next = i;
         cs.end = j;
+        // buffers of an earlier batch's chunk: their memory is paged in already
+        const size_t c = chunks.size();
+        if (c < chunk_pool_.size()) {
+            ChunkBuffers& b = chunk_pool_[c];
+            std::swap(cs.out, b.out);
+            std::swap(cs.spec_out, b.spec_out);
+            std::swap(cs.effects, b.effects);
+            std::swap(cs.entries, b.entries);
+            std::swap(cs.pieces, b.pieces);
+        }
+        cs.keep_buffers = true;
         chunks.push_back(std::move(cs));
         i = j;
     }
@@ -535,6 +551,22 @@ void Mapper::map_uploaded(sa_output* out) {
     out->data = alloc_output(total_len + 1);
     if (!out->data) throw Error(SA_ERR_OOM, "output allocation failed");
     gather_chunk_outputs(chunks, out->data, policy_threads_);
+    // keep the chunks' buffers (emptied) for the next batch
+    if (chunk_pool_.size() < chunks.size()) chunk_pool_.resize(chunks.size());
+    for (size_t c = 0; c < chunks.size(); c++) {
+        ChunkBuffers& b = chunk_pool_[c];
+        ChunkState& cs = chunks[c];
+        cs.out.clear();
+        cs.spec_out.clear();
+        cs.effects.clear();
+        cs.entries.clear();
+        cs.pieces.clear();
+        std::swap(cs.out, b.out);
+        std::swap(cs.spec_out, b.spec_out);
+        std::swap(cs.effects, b.effects);
+        std::swap(cs.entries, b.entries);
+        std::swap(cs.pieces, b.pieces);
+    }
     if (trace_) {
         auto d = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
             return std::chrono::duration<double>(b - a).count();

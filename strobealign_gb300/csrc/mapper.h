@@ -105,6 +105,15 @@ class Mapper {
     double t_nams_ = 0;
     std::chrono::steady_clock::time_point t_map0_;  // start of the current map (trace times)
     PodArray<uint32_t> wave_anchors_;  // a wave's piecewise anchors (query, reference start pairs)
+    WavePool wave_pool_;
+    // output and bookkeeping buffers of the last batch's chunks, reused by the next
+    struct ChunkBuffers {
+        std::string out, spec_out;
+        std::vector<ChunkState::Effect> effects;
+        std::vector<ResultStore::Entry> entries;
+        std::vector<ChunkState::Piece> pieces;
+    };
+    std::vector<ChunkBuffers> chunk_pool_;
     uint32_t n_reads_ = 0;
     uint64_t total_bases_ = 0;
     std::atomic<uint64_t> h2d_bytes_{0}, d2h_bytes_{0};

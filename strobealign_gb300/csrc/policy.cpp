@@ -1622,8 +1622,13 @@ void Policy::run_chunk(ChunkState& cs) {
     }
     if (timing) cs.seconds_real += since(t_run);
     cs.done = true;
-    std::vector<ChunkState::Effect>().swap(cs.effects);
-    std::vector<ResultStore::Entry>().swap(cs.entries);
+    if (cs.keep_buffers) {
+        cs.effects.clear();
+        cs.entries.clear();
+    } else {
+        std::vector<ChunkState::Effect>().swap(cs.effects);
+        std::vector<ResultStore::Entry>().swap(cs.entries);
+    }
 }
 
 }  // namespace sa

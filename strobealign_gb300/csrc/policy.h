@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "extend.h"
+#include "host_util.h"
 
 namespace sa {
 
@@ -67,8 +68,21 @@ struct JobKey {
 // Results of one extension wave copied back from the device: one ExtResult per
 // job, and the CIGAR ops they point into (ExtResult::cigar_offset).
 struct WaveResults {
-    std::vector<ExtResult> results;
-    std::vector<uint32_t> cigar;
+    PodArray<ExtResult> results;
+    PodArray<uint32_t> cigar;
+};
+
+// Wave result buffers reused once no chunk refers to them any more (the pool holds
+// the only reference), so that a wave's copy back lands in memory already paged in.
+struct WavePool {
+    std::vector<std::shared_ptr<WaveResults>> items;
+    std::shared_ptr<WaveResults> take() {
+        for (auto& w : items)
+            if (w.use_count() == 1) return w;
+        auto w = std::make_shared<WaveResults>();
+        if (items.size() < 64) items.push_back(w);
+        return w;
+    }
 };
 
 // One extension result as the policy reads it: the device record plus the address
@@ -150,6 +164,7 @@ void piecewise_anchor_fill(const BatchView& bv, const ExtJob* jobs, size_t n, ui
 struct ChunkState {
     uint64_t first = 0, next = 0, end = 0;  // record range [first, end), cursor next
     uint32_t part = 0;                      // the batch part whose reads these are (Mapper)
+    bool keep_buffers = false;              // done: clear the buffers but keep their memory (pooled)
     Rng rng;
     InsertSize isd;
     std::string out;

@@ -614,11 +614,14 @@ void Session::run_wave(std::vector<std::pair<Request*, size_t>>& batch) {
                                 cudaMemcpyHostToDevice, st_));
     }
     AlignScores sc{mp_.match, mp_.mismatch, mp_.gap_open, mp_.gap_extend, mp_.end_bonus};
+    // the pooled buffers (with their capacity) take the copy back
+    std::shared_ptr<WaveResults> w = wave_pool_.take();
+    std::swap(w->results, ews_.h_results);
+    std::swap(w->cigar, ews_.h_cigar);
     run_extension_raw(refs_view_, arena_seq_.p, arena_off_.p, nullptr, nullptr, idx_->sp.k, sc, (uint32_t)nj, ews_,
                       max_qlen, st_, nullptr, wave_anchors_.size() ? ews_.anchors.p : nullptr, max_anchors);
-    auto w = std::make_shared<WaveResults>();
-    w->results.swap(ews_.h_results);
-    w->cigar.swap(ews_.h_cigar);
+    std::swap(w->results, ews_.h_results);
+    std::swap(w->cigar, ews_.h_cigar);
     for (auto& b : batch) b.first->chunks[b.second].wave = w;
 }
 

@@ -76,7 +76,7 @@ struct Request {
     std::string error;
     int32_t error_code = 0;
     std::chrono::steady_clock::time_point t_submit, t_admit, t_done;
-    ~Request() { std::free(out); }
+    ~Request() { release_output(out); }
 };
 
 struct SessionConfig {
@@ -142,6 +142,7 @@ class Session {
     ExtWorkspace ews_;
     PinnedBuf<ExtJob> h_jobs_;
     PodArray<uint32_t> wave_anchors_;  // a wave's piecewise anchors (query, reference start pairs)
+    WavePool wave_pool_;
     // read arena
     DevBuf<uint8_t> arena_seq_;
     DevBuf<uint64_t> arena_off_;
