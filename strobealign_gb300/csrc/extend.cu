@@ -10,6 +10,8 @@
 //               one lane per SSE lane, 16 lanes per task in byte mode and 8 in word
 //               mode, so 2 resp. 4 tasks per warp; the lazy-F pass leaves E alone
 //               and byte mode reruns in word mode once max + bias >= 255
+//   k_ssw_wave  the same passes for reads up to 192 nt: eight threads per task, one
+//               or two SSE lanes per thread, a wavefront over the reference columns
 //   k_band_*    banded_sw (ext/ssw/ssw.c:598-769): band doubling, then the final
 //               pass with directions and the traceback, one thread per task
 //   k_finalize  M -> =/X (src/cigar.rs:149-187), edit distance and the end-bonus
@@ -1042,6 +1044,284 @@ __global__ void __launch_bounds__(128, RMAX <= 4 ? 5 : 1) k_ssw(SswTask* tasks, 
         tk.flag = tk.score1 > b.score ? 2 : 0;
         if (lane == 0) {
             tasks[ti] = tk;
+            atomicAdd(cells + 1, c_fb);
+            if (c_fw) atomicAdd(cells + 2, c_fw);
+            if (c_rb) atomicAdd(cells + 3, c_rb);
+            if (c_rw) atomicAdd(cells + 4, c_rw);
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------ SSW, lane wavefront
+// ssw_align's passes (ext/ssw/ssw.c:818-888) with eight threads per task, four tasks
+// per warp.  Thread t holds the query rows t*N .. t*N + N - 1 in registers: one SSE
+// lane of segLen = N rows in word mode (8 lanes), two consecutive lanes of N/2 rows
+// in byte mode (16 lanes); rows past the read are the library's padding (score 0).
+// Every thread starts at a lane boundary, so its F chain starts at 0 as in the
+// library's main loop (ext/ssw/ssw.c:256-283), and the lazy-F pass reduces to a raise
+// G that enters each lane: G(l + 1) = max(G(l) - segLen * gE, Ffinal(l)), applied as
+// H = max(H, G - j * gE) at row j (E keeps the value before the raise).
+//
+// The threads form a wavefront over the reference columns: thread t works on column
+// s - t at step s and passes to thread t + 1 its last row's H, its final F, its G and
+// the column's best (score, row) so far, so the last thread holds each column's
+// maximum and the row of its first occurrence, and keeps the running maximum, the
+// end positions and the stop conditions (byte overflow, the reverse pass's
+// terminate score) in the library's column order.
+//
+// Scores are ints scaled by 256: the low byte of a packed key holds 255 - row, so a
+// single max per cell tracks both the column maximum and its smallest row.  The
+// query profile (rows x 5 reference codes) is int16 in shared memory, 8 rows per
+// 16-byte word, laid out [code][word][lane] per warp.
+constexpr int WV_T = 8;      // threads per task
+constexpr int WAVE_NMAX = 24;  // rows per thread: reads up to 8 * 24 = 192 nt
+constexpr int WV_SCALE = 8;  // log2 of the score scale (rows < 256)
+
+struct WaveScores {
+    int gO, gE;  // scaled
+};
+
+template <int N, bool BYTE>
+__device__ __forceinline__ EndPos wave_loop(const uint8_t* r, int rlen, bool r_rev, int qlen, bool check_term,
+                                            int terminate, int bias, WaveScores ws, const uint4* prof, int gl,
+                                            unsigned m, bool run) {
+    constexpr int NW = (N + 7) / 8;
+    int H[N], E[N];
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+        H[j] = 0;
+        E[j] = 0;
+    }
+    const int gO = ws.gO, gE = ws.gE;
+    const int tb = 255 - gl * N - (N - 1);  // key low byte: 255 - row
+    const int gbit = (threadIdx.x & 31) | (WV_T - 1);  // this group's last thread
+    int max = 0, end_ref = BYTE ? -1 : 0, end_read = qlen - 1, cols = 0;
+    int h_out = 0, f_out = 0, g_out = 0, k_out = -1, b_out = 0, hdiag = 0;
+    int rb_next = (run && gl == 0 && rlen > 0) ? c_ssw_code[r[r_rev ? rlen - 1 : 0]] : 0;
+    const int steps = run ? rlen + WV_T - 1 : 0;
+    bool done = false;
+    for (int s = 0;; s++) {
+        const bool act = s < steps && !done;
+        if (!__any_sync(m, act)) break;
+        const int hin = __shfl_up_sync(m, h_out, 1, WV_T);
+        const int fin0 = __shfl_up_sync(m, f_out, 1, WV_T);
+        const int gin0 = __shfl_up_sync(m, g_out, 1, WV_T);
+        const int kin0 = __shfl_up_sync(m, k_out, 1, WV_T);
+        int rb = __shfl_up_sync(m, b_out, 1, WV_T);
+        const int c = s - gl;
+        bool stop = false;
+        if (act && gl == 0) {
+            rb = rb_next;
+            if (s + 1 < rlen) rb_next = c_ssw_code[r[r_rev ? rlen - 2 - s : s + 1]];
+        }
+        if (act && c >= 0 && c < rlen) {
+            const int fin = gl == 0 ? 0 : fin0, gin = gl == 0 ? 0 : gin0, kin = gl == 0 ? -1 : kin0;
+            int diag = gl == 0 ? 0 : hdiag;
+            // every thread starts a lane: F restarts at 0 and G takes the F leaving the
+            // lane above (ext/ssw/ssw.c:285-299); row j of a lane is raised to G - j * gE
+            int gb = fin > gin ? fin : gin;
+            int F = 0;
+            int k0 = -1, k1 = -1;
+            uint4 P[NW];
+#pragma unroll
+            for (int w = 0; w < NW; w++) P[w] = prof[(rb * NW + w) * 32];
+#pragma unroll
+            for (int j = 0; j < N; j++) {
+                constexpr int H2 = BYTE ? N / 2 : N;
+                const int jl = BYTE && j >= H2 ? j - H2 : j;  // row within its lane
+                const uint32_t pw = (&P[j >> 3].x)[(j >> 1) & 3];
+                const int sc = (j & 1) ? ((int)pw >> 16) : (int)(int16_t)(pw & 0xffffu);
+                const int A = __viaddmax_s32(diag, sc, E[j]);  // max(H(diag) + score, E)
+                const int u = __viaddmax_s32(A, -gO, 0);
+                const int Hp = A > F ? A : F;                   // H before the lazy-F raise
+                const int t = __viaddmax_s32(F, -gO, u);        // max(Hp - gO, 0)
+                E[j] = __viaddmax_s32(E[j], -gE, t);
+                // the library's max(F - gE, max(Hp - gO, 0)); F - gO <= F - gE drops out, so
+                // the F chain carries one max per row
+                F = __viaddmax_s32(F, -gE, u);
+                const int gj = gb - jl * gE;
+                const int Hr = Hp > gj ? Hp : gj;
+                if (j & 1) k1 = __viaddmax_s32(Hr, N - 1 - j, k1);
+                else k0 = __viaddmax_s32(Hr, N - 1 - j, k0);
+                diag = H[j];
+                H[j] = Hr;
+                if (BYTE && j == H2 - 1) {
+                    // the second lane of this thread starts
+                    const int ge = gb - H2 * gE;
+                    gb = F > ge ? F : ge;
+                    F = 0;
+                }
+            }
+            const int g = gb - (BYTE ? N / 2 : N) * gE;  // G entering the next thread's first row
+            int key = k0 > k1 ? k0 : k1;
+            key += tb;
+            k_out = key > kin ? key : kin;
+            h_out = H[N - 1];
+            f_out = F;
+            g_out = g;
+            b_out = rb;
+            if (gl == WV_T - 1) {
+                // column c complete: the library's per-column bookkeeping
+                const int i = r_rev ? rlen - 1 - c : c;
+                const int cm = k_out >> WV_SCALE;
+                cols = c + 1;
+                if (cm > max) {
+                    max = cm;
+                    if (BYTE && max + bias >= 255) {
+                        stop = true;
+                    } else {
+                        end_ref = i;
+                        const int row = 255 - (k_out & 255);
+                        end_read = row < qlen - 1 ? row : qlen - 1;
+                    }
+                }
+                if (check_term && cm == terminate) stop = true;
+            }
+        }
+        hdiag = hin;
+        if ((__ballot_sync(m, stop) >> gbit) & 1u) done = true;
+    }
+    EndPos res;
+    const int src = WV_T - 1;
+    res.cols = __shfl_sync(m, cols, src, WV_T);
+    const int mx = __shfl_sync(m, max, src, WV_T);
+    res.score = !BYTE ? mx : (mx + bias >= 255 ? 255 : mx);
+    res.ref = __shfl_sync(m, end_ref, src, WV_T);
+    // the library scans the stored column for the maximum: all rows when it stayed 0
+    const int rd = __shfl_sync(m, end_read, src, WV_T);
+    res.read = mx == 0 ? 0 : rd;
+    return res;
+}
+
+// One pass of every group of the warp that runs it (run): this thread's rows of the
+// striped profile, then the wavefront with N = 2 * segLen (byte) or segLen (word) rows
+// per thread.  All 32 threads enter together.  When the running groups share N, the
+// warp runs them in lockstep (full-warp shuffles and votes); otherwise each group runs
+// on its own with its own mask.
+template <int NMAX, bool BYTE>
+__device__ __forceinline__ EndPos wave_pass(bool run, const uint8_t* q, int qlen, bool q_rev, const uint8_t* r, int rlen,
+                            bool r_rev, bool check_term, int terminate, const AlignScores& sc, int bias, uint4* prof,
+                            int gl, unsigned gm) {
+    EndPos z;
+    z.score = 0;
+    z.ref = BYTE ? -1 : 0;
+    z.read = qlen - 1;
+    z.cols = 0;
+    if (run && qlen <= 0) run = false;
+    const int N = !run ? 0 : BYTE ? 2 * ((qlen + 15) / 16) : (qlen + 7) / 8;
+    const int nmax = __reduce_max_sync(FULLM, N);
+    const int nmin = __reduce_min_sync(FULLM, run ? N : 0x7fffffff);
+    if (nmax == 0) return z;  // no group of this warp runs this pass
+    const bool uni = nmin == nmax;
+    if (!uni && !run) return z;
+    const unsigned m = uni ? FULLM : gm;
+    const int NN = uni ? nmax : N;
+    if (run) {
+        const int nw = (NN + 7) / 8;
+        const int match = sc.match << WV_SCALE, mism = -((int)sc.mismatch << WV_SCALE);
+        for (int b = 0; b < 5; b++)
+            for (int w = 0; w < nw; w++) {
+                uint32_t v[4];
+                for (int x = 0; x < 4; x++) {
+                    uint32_t pair = 0;
+                    for (int y = 0; y < 2; y++) {
+                        const int j = 8 * w + 2 * x + y, pos = gl * NN + j;
+                        int sv = 0;
+                        if (j < NN && pos < qlen) {
+                            const int code = c_ssw_code[q_rev ? q[qlen - 1 - pos] : q[pos]];
+                            sv = (code == b && b < 4) ? match : mism;
+                        }
+                        pair |= (uint32_t)(uint16_t)(int16_t)sv << (16 * y);
+                    }
+                    v[x] = pair;
+                }
+                prof[(b * nw + w) * 32] = make_uint4(v[0], v[1], v[2], v[3]);
+            }
+    }
+    const WaveScores ws{(int)sc.gap_open << WV_SCALE, (int)sc.gap_extend << WV_SCALE};
+    EndPos res = z;
+    // byte mode: N is even, so the odd cases are never taken there
+#define SA_WV(K)                                                                                                 \
+    case K:                                                                                                      \
+        if constexpr (K <= NMAX && (!BYTE || K % 2 == 0))                                                        \
+            res = wave_loop<K, BYTE>(r, rlen, r_rev, qlen, check_term, terminate, bias, ws, prof, gl, m, run);   \
+        break;
+    switch (NN) {
+        SA_WV(1) SA_WV(2) SA_WV(3) SA_WV(4) SA_WV(5) SA_WV(6) SA_WV(7) SA_WV(8)
+        SA_WV(9) SA_WV(10) SA_WV(11) SA_WV(12) SA_WV(13) SA_WV(14) SA_WV(15) SA_WV(16)
+        SA_WV(17) SA_WV(18) SA_WV(19) SA_WV(20) SA_WV(21) SA_WV(22) SA_WV(23) SA_WV(24)
+        default: break;
+    }
+#undef SA_WV
+    return run ? res : z;
+}
+
+// ssw_align's end searches with wave_pass for tasks of reads up to 8 * NMAX nt, in
+// the longest-first order of k_ssw: each warp takes four consecutive tasks (one per
+// group of eight threads) and runs the forward byte pass, the forward word pass of the
+// tasks that overflowed, then the reverse passes in each task's mode.
+template <int NMAX>
+__global__ void __launch_bounds__(128, 4) k_ssw_wave(SswTask* tasks, const uint32_t* order, uint32_t n_tasks,
+                                                      const PrepRec* prep, const uint8_t* arena, AlignScores sc,
+                                                      int bias, uint32_t* counters) {
+    constexpr int NW = (NMAX + 7) / 8;
+    extern __shared__ __align__(16) uint4 wv_smem[];
+    const int lane = threadIdx.x & 31, gi = lane / WV_T, gl = lane % WV_T;
+    const unsigned gm = 0xffu << (WV_T * gi);
+    uint4* prof = wv_smem + (threadIdx.x / 32) * (5 * NW * 32) + lane;
+    unsigned long long* cells = reinterpret_cast<unsigned long long*>(counters + 8);
+    constexpr uint32_t G = 32 / WV_T;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&counters[5], G);
+        base = __shfl_sync(FULLM, base, 0);
+        if (base >= n_tasks) break;
+        const uint32_t li = base + gi;
+        const bool have = li < n_tasks;
+        const uint32_t ti = have ? (order ? order[li] : li) : 0;
+        int qlen = 0, wlen = 0;
+        const uint8_t* q = arena;
+        if (have) {
+            const PrepRec& pr = prep[tasks[ti].job];
+            qlen = (int)pr.qlen;
+            wlen = (int)pr.wlen;
+            q = arena + pr.arena_off;
+        }
+        const uint8_t* r = q + qlen;
+        // forward: byte, word on overflow (ext/ssw/ssw.c:840-862)
+        EndPos e = wave_pass<NMAX, true>(have, q, qlen, false, r, wlen, false, false, 0, sc, bias, prof, gl, gm);
+        const bool word = have && e.score == 255;
+        const EndPos ew = wave_pass<NMAX, false>(word, q, qlen, false, r, wlen, false, false, 0, sc, bias, prof, gl,
+                                                 gm);
+        unsigned long long c_fb = (unsigned long long)qlen * e.cols, c_fw = 0, c_rb = 0, c_rw = 0;
+        if (word) {
+            e = ew;
+            c_fw = (unsigned long long)qlen * e.cols;
+        }
+        // reverse pass over read[0..=read_end1] and ref[0..=ref_end1] (ext/ssw/ssw.c:870-888)
+        const bool rev = have && e.ref >= 0;
+        const EndPos bb = wave_pass<NMAX, true>(rev && !word, q, e.read + 1, true, r, e.ref + 1, true, true, e.score,
+                                                sc, bias, prof, gl, gm);
+        const EndPos bw = wave_pass<NMAX, false>(rev && word, q, e.read + 1, true, r, e.ref + 1, true, true, e.score,
+                                                 sc, bias, prof, gl, gm);
+        EndPos b = word ? bw : bb;
+        if (!rev) {
+            b.score = 0;
+            b.ref = -1;
+            b.read = e.read;
+            b.cols = 0;
+        }
+        (word ? c_rw : c_rb) = (unsigned long long)(e.read + 1) * b.cols;
+        if (have && gl == 0) {
+            SswTask& tk = tasks[ti];
+            tk.score1 = e.score;
+            tk.ref_end1 = e.ref;
+            tk.read_end1 = e.read;
+            tk.word = word;
+            tk.ref_begin1 = b.ref;
+            tk.read_begin1 = e.read - b.read;
+            tk.flag = e.score > b.score ? 2 : 0;
             atomicAdd(cells + 1, c_fb);
             if (c_fw) atomicAdd(cells + 2, c_fw);
             if (c_rb) atomicAdd(cells + 3, c_rb);
@@ -2366,7 +2646,9 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
         // rows per thread of the warp-per-task kernel: ceil(segLen / S) in both modes
         const int rows = std::max((seg_b + 1) / 2, (seg_w + 3) / 4);
         const int rmax = rows <= 4 ? 4 : rows <= 8 ? 8 : rows <= 16 ? 16 : 0;
-        const bool fused = reg_ok && sc.gap_open >= sc.gap_extend && rmax;
+        // the closed-form lazy-F pass needs gap_open > gap_extend: with equal penalties the
+        // library's lazy-F loop stops after the first row of each lane
+        const bool fused = reg_ok && sc.gap_open > sc.gap_extend && rmax;
         if (fused) {
             // one launch for every pass, longest windows first
             ws.order.reserve(n_tasks);
@@ -2385,7 +2667,15 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
 #define SA_SSW(RM)                                                                                              \
     k_ssw<RM><<<(unsigned)blocks, tpb, (size_t)wpb * 5 * 32 * ((RM + 3) / 4) * 4, st>>>(                       \
         ws.tasks.p, ws.order.p, n_tasks, ws.prep.p, ws.arena.p, sc, bias, ws.counters.p)
-            if (rmax == 4) SA_SSW(4);
+            if (max_qlen <= 8 * WAVE_NMAX) {
+                // eight threads per task (reads up to 192 nt)
+                const uint64_t per_block = (uint64_t)wpb * (32 / WV_T);  // tasks per block and round
+                uint64_t wblocks = ((uint64_t)n_tasks + per_block - 1) / per_block;
+                if (wblocks > 152ULL * 16) wblocks = 152ULL * 16;
+                const size_t smem = (size_t)wpb * 5 * ((WAVE_NMAX + 7) / 8) * 32 * sizeof(uint4);
+                k_ssw_wave<WAVE_NMAX><<<(unsigned)wblocks, tpb, smem, st>>>(ws.tasks.p, ws.order.p, n_tasks, ws.prep.p,
+                                                                           ws.arena.p, sc, bias, ws.counters.p);
+            } else if (rmax == 4) SA_SSW(4);
             else if (rmax == 8) SA_SSW(8);
             else SA_SSW(16);
 #undef SA_SSW

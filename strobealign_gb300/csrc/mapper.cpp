@@ -454,14 +454,18 @@ void Mapper::map_uploaded(sa_output* out) {
     kt_.reset();
     kt_nam_.reset();
     for (int c = 0; c < 5; c++) sw_cells_[c] = 0;
-    // chunks (src/main.rs:591-604)
+    // chunks (src/main.rs:591-604), cut on the uploaded read offsets (record j's bases
+    // are off[rpr * (j + 1)] - off[rpr * j])
     std::vector<ChunkState> chunks;
+    chunks.reserve(total_bases_ / (mp_.chunk_size + 1) + 2);
+    const uint64_t* off = h_off_.p;
+    const uint64_t step = paired ? 2 : 1;
     for (uint64_t i = 0; i < nrec;) {
-        uint64_t nt = 0, j = i;
+        uint64_t j = i;
+        const uint64_t base = off[step * i];
         while (j < nrec) {
-            nt += bv.reads[paired ? 2 * j : j].len + (paired ? bv.reads[2 * j + 1].len : 0);
             j++;
-            if (nt > mp_.chunk_size) break;
+            if (off[step * j] - base > mp_.chunk_size) break;
         }
         ChunkState cs;
         cs.first = cs.next = i;

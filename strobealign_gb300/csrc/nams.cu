@@ -7,9 +7,10 @@
 //                   local rescue, orientation choice (src/hit.rs, src/chainer.rs:205-216)
 //   k_anchors       warp per read: anchor count, then fill (src/chainer.rs:304-384)
 //   segmented sort  (ref_id, ref_start, query_start) packed in a u64 key
-//   k_chain         warp per read-orientation: dedup, collinear chaining DP with the
-//                   reference's early-break rules evaluated as a warp prefix-max, chain
-//                   extraction (src/chainer.rs:85-180, 386-449)
+//   k_chain4        warp per four read-orientations: dedup, collinear chaining DP with
+//                   the reference's early-break rules evaluated as a prefix max over
+//                   the candidates (eight lanes per orientation), chain extraction
+//                   (src/chainer.rs:85-180, 386-449)
 //   k_nam_compact   warp per read: NAM ids in push order, stable sort by score
 //                   (src/nam.rs:168-170); reads with more than 32 NAMs through a
 //                   segmented stable sort and k_nam_gather
@@ -477,7 +478,7 @@ struct AnchorPack {
     uint32_t qbits, pbits;
     // When seg_shift is set, the read orientation's index sits above the anchor key
     // (hi = segment << seg_shift), so that one radix sort of the whole batch orders
-    // anchors by segment, then (ref_id, ref_start, query_start); k_chain masks it off.
+    // anchors by segment, then (ref_id, ref_start, query_start); k_chain4 masks it off.
     uint32_t seg_shift = 0;
     uint64_t hi = 0;
     __device__ __forceinline__ uint64_t key(uint32_t ref_id, uint32_t ref_start, uint32_t qs) const {
@@ -759,229 +760,386 @@ __device__ void warp_radix_sort_desc(uint32_t* idx, uint32_t* tmp, uint32_t m, c
     for (uint32_t c = lane; c < m; c += 32) tmp[c] = idx[c];
 }
 
-// RING: max_lookback < 64, so the predecessors of anchor i (and their scores) come
-// from a 64-entry ring in shared memory written as anchors are scored, instead of
-// global memory (the loop over a read orientation's anchors is serial; this takes
-// the store-to-load round trip out of each step).
-template <bool RING>
-__global__ void __launch_bounds__(256, 5) k_chain(const uint64_t* __restrict__ off, uint32_t n, const uint64_t* seg_off,
-                                               const uint64_t* sorted, uint64_t* dedup, float* dp, uint32_t* pred,
-                                               uint32_t* aux, uint64_t total_anchors, AnchorPack ap, ChainCtx cc,
-                                               NamRec* nam_out, uint32_t* nam_seg_count, uint64_t* anc_out,
-                                               uint64_t* anc_start) {
-    __shared__ uint32_t hist[WARPS_PER_BLOCK * 256];
-    __shared__ uint64_t ring_key_s[RING ? WARPS_PER_BLOCK * 64 : 1];
-    __shared__ float ring_dp_s[RING ? WARPS_PER_BLOCK * 64 : 1];
-    uint64_t* ring_key = ring_key_s + (RING ? (threadIdx.x / 32) * 64 : 0);
-    float* ring_dp = ring_dp_s + (RING ? (threadIdx.x / 32) * 64 : 0);
+// extract_chains (src/chainer.rs:386-449) for one read orientation (segment sg, anchors
+// b .. b + N of the deduplicated list) by the whole warp; best_score is the segment's
+// best chain score.  hist: this warp's 256 shared counters.
+__device__ void chain_extract(const uint64_t* dedup, const float* dp, const uint32_t* pred, uint32_t* aux,
+                              uint64_t total_anchors, uint64_t b, uint32_t N, uint32_t sg, float best_score,
+                              const AnchorPack& ap, const ChainCtx& cc, NamRec* nam_out, uint32_t* nam_seg_count,
+                              uint64_t* anc_out, uint64_t* anc_start, uint32_t* hist) {
     const uint32_t lane = lane_id();
+    const uint64_t qmask = (1ULL << ap.qbits) - 1, pmask = (1ULL << ap.pbits) - 1;
+    const float valid_score = __fmul_rn(best_score, cc.cp.valid_score_threshold);
+    uint32_t* cand = aux + b;
+    uint32_t* sorted_c = aux + total_anchors + b;
+    uint32_t* used = aux + 2 * total_anchors + b;
+    uint32_t M = 0;
+    for (uint32_t c = 0; c < N; c += 32) {
+        uint32_t i = c + lane;
+        bool take = i < N && dp[b + i] >= valid_score;
+        uint32_t bal = __ballot_sync(FULL, take);
+        if (take) cand[M + __popc(bal & lanemask_lt())] = i;
+        if (i < N) used[i] = 0;
+        M += __popc(bal);
+    }
+    __syncwarp();
+    // candidates by score, descending, ties in anchor order (a stable sort)
+    if (M <= 32) {
+        const uint32_t ci = lane < M ? cand[lane] : 0;
+        const float s = lane < M ? dp[b + ci] : 0.0f;
+        uint32_t rank = 0;
+        for (uint32_t u = 0; u < M; u++) {
+            const float su = __shfl_sync(FULL, s, u);
+            rank += (su > s) || (su == s && u < lane);
+        }
+        if (lane < M) sorted_c[rank] = ci;
+    } else {
+        warp_radix_sort_desc(cand, sorted_c, M, dp + b, hist);
+    }
+    __syncwarp();
+    if (lane == 0) {
+        uint32_t nn = 0;
+        NamRec* outp = nam_out + b;
+        // a kept chain holds its end anchor (never marked used) and used
+        // predecessors, so kept chains list each anchor at most twice; a dropped
+        // chain's anchors are overwritten: 3 slots per anchor suffice
+        uint64_t* ao = anc_out ? anc_out + 3 * b : nullptr;
+        uint32_t acur = 0;
+        for (uint32_t c = 0; c < M; c++) {
+            uint32_t i = sorted_c[c];
+            if (used[i]) continue;
+            uint32_t j = i;
+            bool overlaps = false;
+            uint32_t nanch = 1;
+            const uint64_t ki = dedup[b + i];
+            if (ao) ao[acur] = ki;
+            uint32_t matching = cc.k;
+            uint32_t cov = (uint32_t)((ki >> ap.qbits) & pmask);
+            while (pred[b + j] != 0xffffffffu) {
+                j = pred[b + j];
+                if (used[j]) { overlaps = true; break; }
+                if (ao) ao[acur + nanch] = dedup[b + j];
+                nanch++;
+                used[j] = 1;
+                uint32_t rsj = (uint32_t)((dedup[b + j] >> ap.qbits) & pmask);
+                uint32_t d = cov > rsj ? cov - rsj : 0;
+                matching += d < cc.k ? d : cc.k;
+                cov = rsj;
+            }
+            if (overlaps) continue;
+            const uint64_t kf2 = dedup[b + j];
+            NamRec nr;
+            nr.nam_id = nn;
+            nr.query_start = (uint32_t)(kf2 & qmask);
+            nr.query_end = (uint32_t)(ki & qmask) + cc.k;
+            nr.ref_start = (uint32_t)((kf2 >> ap.qbits) & pmask);
+            nr.ref_end = (uint32_t)((ki >> ap.qbits) & pmask) + cc.k;
+            nr.matching_bases = matching;
+            nr.ref_id = (uint32_t)(ki >> (ap.pbits + ap.qbits));
+            nr.score = __fadd_rn(dp[b + i], __fmul_rn(__uint2float_rn(nanch), cc.cp.matches_weight));
+            nr.is_revcomp = sg & 1;
+            nr.n_anchors = nanch;
+            if (anc_start) anc_start[b + nn] = 3 * b + acur;
+            acur += nanch;
+            outp[nn++] = nr;
+        }
+        nam_seg_count[sg] = nn;
+    }
+    __syncwarp();
+}
+
+// Chaining (src/chainer.rs:128-176 and 386-449) for four read orientations per warp
+// (2 reads).  The deduplication and the extraction run over the whole warp, one
+// orientation after the other.  The DP is serial over a read orientation's anchors;
+// the candidates j of anchor i (back to max_lookback) are scored in parallel and an
+// exclusive prefix max over them reproduces the reference's downward scan with its
+// ">=" updates and its stops (a different reference or a gap >= max_ref_gap ends the
+// scan; an update on the same diagonal ends it after that candidate).  The DP runs for
+// the four orientations at once, one group of eight lanes each, eight candidates at a
+// time (most anchors stop at the first candidate: the one before on the same
+// diagonal).  Warps whose orientations have more than CHAIN_GROUP_MAX anchors run the
+// DP with the whole warp per orientation, 32 candidates at a time.
+//
+// RING: max_lookback < 64, so the predecessors of anchor i (and their scores) come
+// from a 64-entry ring in shared memory per orientation, written as anchors are
+// scored, instead of global memory (this takes the store-to-load round trip out of
+// each serial step).
+constexpr uint32_t CHAIN_GROUP_MAX = 96;
+constexpr uint32_t CG = 8;  // lanes per orientation in the grouped DP
+
+template <bool RING>
+__device__ __forceinline__ void chain_candidates(uint32_t j, bool in, const uint64_t* dedup, const float* dp,
+                                                 uint64_t b, const uint64_t* ring_key, const float* ring_dp,
+                                                 uint32_t ri, uint32_t rsi, uint32_t qi, uint32_t max_ref_gap,
+                                                 const ChainCtx& cc, const AnchorPack& ap, bool& hard, bool& valid,
+                                                 bool& diag, float& val) {
+    const uint64_t qmask = (1ULL << ap.qbits) - 1, pmask = (1ULL << ap.pbits) - 1;
+    hard = valid = diag = false;
+    val = 0.0f;
+    if (!in) return;
+    const uint64_t kj = RING ? ring_key[j & 63] : dedup[b + j];
+    const uint32_t rj = (uint32_t)(kj >> (ap.pbits + ap.qbits)), rsj = (uint32_t)((kj >> ap.qbits) & pmask),
+                   qj = (uint32_t)(kj & qmask);
+    if (rj != ri) {
+        hard = true;
+    } else if (qi >= qj) {
+        const uint32_t dq = qi - qj, dr = rsi - rsj;
+        if (dr >= max_ref_gap) {
+            hard = true;
+        } else {
+            const uint32_t mx = dq > dr ? dq : dr, mn = dq < dr ? dq : dr;
+            if (!ratio_above(mx, mn, cc)) {
+                valid = true;
+                diag = dq == dr;
+                val = __fadd_rn(RING ? ring_dp[j & 63] : dp[b + j], chain_score(dq, dr, cc));
+            }
+        }
+    }
+}
+
+template <bool RING>
+__global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ off, uint32_t n, const uint64_t* seg_off,
+                                                const uint64_t* sorted, uint64_t* dedup, float* dp, uint32_t* pred,
+                                                uint32_t* aux, uint64_t total_anchors, AnchorPack ap, ChainCtx cc,
+                                                NamRec* nam_out, uint32_t* nam_seg_count, uint64_t* anc_out,
+                                                uint64_t* anc_start) {
+    __shared__ uint32_t hist[WARPS_PER_BLOCK * 256];
+    __shared__ uint64_t ring_key_s[RING ? WARPS_PER_BLOCK * 4 * 64 : 1];
+    __shared__ float ring_dp_s[RING ? WARPS_PER_BLOCK * 4 * 64 : 1];
+    const uint32_t lane = lane_id(), g = lane / CG, gl = lane % CG, gsh = CG * g;
+    const uint32_t wib = threadIdx.x / 32;
     const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
     const uint64_t qmask = (1ULL << ap.qbits) - 1, pmask = (1ULL << ap.pbits) - 1;
-    for (uint32_t sg = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; sg < 2 * n; sg += nwarps) {
-        const uint64_t b = seg_off[sg], e = seg_off[sg + 1];
-        const uint32_t r = sg >> 1;
-        const uint32_t read_len = (uint32_t)(off[r + 1] - off[r]);
-        // dedup (src/chainer.rs:228-229)
-        uint32_t N = 0;
-        const uint64_t kmask = ap.seg_shift ? (1ULL << ap.seg_shift) - 1 : ~0ULL;  // drop the segment prefix
-        for (uint64_t c = b; c < e; c += 32) {
-            uint64_t i = c + lane;
-            bool keep = false;
-            uint64_t key = 0;
-            if (i < e) {
-                key = sorted[i];
-                keep = i == b || sorted[i - 1] != key;
+    const uint64_t kmask = ap.seg_shift ? (1ULL << ap.seg_shift) - 1 : ~0ULL;  // drop the segment prefix
+    const float kf = __uint2float_rn(cc.k);
+    const uint32_t nseg = 2 * n;
+    for (uint32_t sg0 = 4 * (blockIdx.x * (blockDim.x / 32) + wib); sg0 < nseg; sg0 += 4 * nwarps) {
+        // dedup (src/chainer.rs:228-229), one orientation after the other
+        uint32_t Nq[4];
+        uint64_t bq[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const uint32_t sg = sg0 + q;
+            Nq[q] = 0;
+            bq[q] = 0;
+            if (sg >= nseg) continue;
+            const uint64_t b = seg_off[sg], e = seg_off[sg + 1];
+            bq[q] = b;
+            uint32_t N = 0;
+            for (uint64_t c = b; c < e; c += 32) {
+                const uint64_t i = c + lane;
+                bool keep = false;
+                uint64_t key = 0;
+                if (i < e) {
+                    key = sorted[i];
+                    keep = i == b || sorted[i - 1] != key;
+                }
+                const uint32_t bal = __ballot_sync(FULL, keep);
+                if (keep) dedup[b + N + __popc(bal & lanemask_lt())] = key & kmask;
+                N += __popc(bal);
             }
-            uint32_t bal = __ballot_sync(FULL, keep);
-            if (keep) dedup[b + N + __popc(bal & lanemask_lt())] = key & kmask;
-            N += __popc(bal);
+            Nq[q] = N;
         }
         __syncwarp();
-        if (N == 0) {
-            if (lane == 0) nam_seg_count[sg] = 0;
-            continue;
-        }
-        const uint32_t max_ref_gap = cc.cp.max_ref_gap ? cc.cp.max_ref_gap : read_len;
-        const float kf = __uint2float_rn(cc.k);
-        float best_score = 0.0f;
-        uint32_t best_index = 0xffffffffu;
-        uint64_t best_key = 0;  // key and score of the anchor at best_index
-        uint64_t next_key = dedup[b];
-        for (uint32_t i = 0; i < N; i++) {
-            const uint64_t ki = next_key;
-            if (i + 1 < N) next_key = dedup[b + i + 1];
-            const uint32_t ri = (uint32_t)(ki >> (ap.pbits + ap.qbits)), rsi = (uint32_t)((ki >> ap.qbits) & pmask),
-                           qi = (uint32_t)(ki & qmask);
-            const uint32_t lookup_end = i > cc.cp.max_lookback ? i - cc.cp.max_lookback : 0;
-            float cur = kf;  // dp[i] as the reference's downward scan leaves it
-            uint32_t cur_pred = 0xffffffffu;
-            bool stop = false;
-            // candidates j = i-1, i-2, ... in chunks of 32, lane t handles j = i-1-(base+t)
-            for (uint32_t base = 0; !stop && base < i - lookup_end; base += 32) {
-                const uint32_t t = base + lane;
-                bool in = t < i - lookup_end;
-                uint32_t j = i - 1 - t;
-                bool hard = false, valid = false, diag = false;
-                float val = 0.0f;
-                if (in) {
-                    const uint64_t kj = RING ? ring_key[j & 63] : dedup[b + j];
-                    const uint32_t rj = (uint32_t)(kj >> (ap.pbits + ap.qbits)),
-                                   rsj = (uint32_t)((kj >> ap.qbits) & pmask), qj = (uint32_t)(kj & qmask);
-                    if (rj != ri) hard = true;
-                    else if (qi >= qj) {
-                        uint32_t dq = qi - qj, dr = rsi - rsj;
-                        if (dr >= max_ref_gap) hard = true;
-                        else {
-                            uint32_t mx = dq > dr ? dq : dr, mn = dq < dr ? dq : dr;
-                            if (!ratio_above(mx, mn, cc)) {
-                                valid = true;
-                                diag = dq == dr;
-                                val = __fadd_rn(RING ? ring_dp[j & 63] : dp[b + j], chain_score(dq, dr, cc));
+        const uint32_t nmax = max(max(Nq[0], Nq[1]), max(Nq[2], Nq[3]));
+        float best_q[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (nmax <= CHAIN_GROUP_MAX) {
+            // grouped DP: group g scores orientation sg0 + g
+            const uint32_t sg = sg0 + g;
+            const uint32_t N = g == 0 ? Nq[0] : g == 1 ? Nq[1] : g == 2 ? Nq[2] : Nq[3];
+            const uint64_t b = g == 0 ? bq[0] : g == 1 ? bq[1] : g == 2 ? bq[2] : bq[3];
+            uint64_t* ring_key = ring_key_s + (RING ? (wib * 4 + g) * 64 : 0);
+            float* ring_dp = ring_dp_s + (RING ? (wib * 4 + g) * 64 : 0);
+            const uint32_t read_len = sg < nseg ? (uint32_t)(off[(sg >> 1) + 1] - off[sg >> 1]) : 0;
+            const uint32_t max_ref_gap = cc.cp.max_ref_gap ? cc.cp.max_ref_gap : read_len;
+            float best_score = 0.0f;
+            uint32_t best_index = 0xffffffffu;
+            uint64_t best_key = 0;
+            uint64_t next_key = N ? dedup[b] : 0;
+            for (uint32_t i = 0; i < nmax; i++) {
+                const bool act = i < N;
+                const uint64_t ki = next_key;
+                if (act && i + 1 < N) next_key = dedup[b + i + 1];
+                const uint32_t ri = (uint32_t)(ki >> (ap.pbits + ap.qbits)), rsi = (uint32_t)((ki >> ap.qbits) & pmask),
+                               qi = (uint32_t)(ki & qmask);
+                const uint32_t lookup_end = i > cc.cp.max_lookback ? i - cc.cp.max_lookback : 0;
+                const uint32_t span = act ? i - lookup_end : 0;  // candidates j = i-1 .. lookup_end
+                float cur = kf;
+                uint32_t cur_pred = 0xffffffffu;
+                bool more = span > 0;
+                for (uint32_t base = 0; __any_sync(FULL, more); base += CG) {
+                    const uint32_t t = base + gl;
+                    const bool in = more && t < span;
+                    const uint32_t j = i - 1 - t;
+                    bool hard, valid, diag;
+                    float val;
+                    chain_candidates<RING>(j, in, dedup, dp, b, ring_key, ring_dp, ri, rsi, qi, max_ref_gap, cc, ap,
+                                           hard, valid, diag, val);
+                    const uint32_t hb = (__ballot_sync(FULL, hard) >> gsh) & 0xffu;
+                    const uint32_t lim = hb ? (uint32_t)(__ffs(hb) - 1) : CG;  // lanes >= lim are not reached
+                    if (gl >= lim) valid = false;
+                    // exclusive prefix max of val over valid lanes in scan order
+                    float incl = valid ? val : -INFINITY;
+                    for (uint32_t d = 1; d < CG; d <<= 1) {
+                        const float y = __shfl_up_sync(FULL, incl, d, CG);
+                        if (gl >= d) incl = fmaxf(incl, y);
+                    }
+                    float excl = __shfl_up_sync(FULL, incl, 1, CG);
+                    if (gl == 0) excl = -INFINITY;
+                    const bool upd = valid && val >= fmaxf(cur, excl);
+                    const uint32_t ub = (__ballot_sync(FULL, upd) >> gsh) & 0xffu;
+                    const uint32_t sb = (__ballot_sync(FULL, upd && diag) >> gsh) & 0xffu;
+                    uint32_t reach = lim;
+                    bool stop = hb != 0;
+                    if (sb) {
+                        reach = (uint32_t)__ffs(sb);
+                        stop = true;
+                    }
+                    const uint32_t um = ub & (reach >= CG ? 0xffu : ((1u << reach) - 1));
+                    const uint32_t last = um ? 31 - __clz(um) : 0;
+                    const float lv = __shfl_sync(FULL, val, last, CG);
+                    if (more && um) {
+                        cur = lv;
+                        cur_pred = i - 1 - (base + last);
+                    }
+                    if (stop || base + CG >= span) more = false;
+                }
+                // re-check of the best chain end (src/chainer.rs:150-165)
+                if (act && best_index != 0xffffffffu) {
+                    const uint64_t kb = best_key;
+                    const uint32_t rb = (uint32_t)(kb >> (ap.pbits + ap.qbits)),
+                                   rsb = (uint32_t)((kb >> ap.qbits) & pmask), qb = (uint32_t)(kb & qmask);
+                    if (rb == ri && qi > qb) {
+                        const uint32_t dq = qi - qb, dr = rsi - rsb;
+                        const uint32_t mx = dq > dr ? dq : dr, mn = dq < dr ? dq : dr;
+                        if (dr < max_ref_gap && dr > 0 && !ratio_above(mx, mn, cc)) {
+                            const float ns = __fadd_rn(best_score, chain_score(dq, dr, cc));
+                            if (ns > cur) {
+                                cur = ns;
+                                cur_pred = best_index;
                             }
                         }
                     }
                 }
-                uint32_t hb = __ballot_sync(FULL, hard);
-                uint32_t lim = hb ? (uint32_t)(__ffs(hb) - 1) : 32;  // lanes >= lim are not reached
-                if (lane >= lim) valid = false;
-                // exclusive prefix max of val over valid lanes in scan order
-                float x = valid ? val : -INFINITY;
-                float incl = x;
-                for (int d = 1; d < 32; d <<= 1) {
-                    float y = __shfl_up_sync(FULL, incl, d);
-                    if (lane >= (uint32_t)d) incl = fmaxf(incl, y);
-                }
-                float excl = __shfl_up_sync(FULL, incl, 1);
-                if (lane == 0) excl = -INFINITY;
-                float before = fmaxf(cur, excl);
-                bool upd = valid && val >= before;
-                uint32_t ub = __ballot_sync(FULL, upd);
-                uint32_t sb = __ballot_sync(FULL, upd && diag);
-                uint32_t reach = lim;
-                if (sb) {
-                    uint32_t sl = (uint32_t)(__ffs(sb) - 1);
-                    reach = sl + 1;
-                    stop = true;
-                }
-                if (hb) stop = true;
-                uint32_t um = ub & (reach >= 32 ? FULL : ((1u << reach) - 1));
-                if (um) {
-                    uint32_t last = 31 - __clz(um);
-                    float lv = __shfl_sync(FULL, val, last);
-                    cur = lv;
-                    cur_pred = i - 1 - (base + last);
-                }
-            }
-            // re-check of the best chain end (src/chainer.rs:150-165)
-            if (best_index != 0xffffffffu) {
-                const uint64_t kb = best_key;
-                const uint32_t rb = (uint32_t)(kb >> (ap.pbits + ap.qbits)), rsb = (uint32_t)((kb >> ap.qbits) & pmask),
-                               qb = (uint32_t)(kb & qmask);
-                if (rb == ri && qi > qb) {
-                    uint32_t dq = qi - qb, dr = rsi - rsb;
-                    uint32_t mx = dq > dr ? dq : dr, mn = dq < dr ? dq : dr;
-                    if (dr < max_ref_gap && dr > 0 && !ratio_above(mx, mn, cc)) {
-                        float ns = __fadd_rn(best_score, chain_score(dq, dr, cc));
-                        if (ns > cur) {
-                            cur = ns;
-                            cur_pred = best_index;
-                        }
+                if (act && gl == 0) {
+                    dp[b + i] = cur;
+                    pred[b + i] = cur_pred;
+                    if (RING) {
+                        ring_key[i & 63] = ki;
+                        ring_dp[i & 63] = cur;
                     }
                 }
-            }
-            if (lane == 0) {
-                dp[b + i] = cur;
-                pred[b + i] = cur_pred;
-                if (RING) {
-                    ring_key[i & 63] = ki;
-                    ring_dp[i & 63] = cur;
+                if (act && cur > best_score) {
+                    best_score = cur;
+                    best_index = i;
+                    best_key = ki;
                 }
+                __syncwarp();
             }
-            if (cur > best_score) {
-                best_score = cur;
-                best_index = i;
-                best_key = ki;
-            }
-            __syncwarp();
-        }
-        // extract_chains (src/chainer.rs:386-449)
-        const float valid_score = __fmul_rn(best_score, cc.cp.valid_score_threshold);
-        uint32_t* cand = aux + b;
-        uint32_t* sorted_c = aux + total_anchors + b;
-        uint32_t* used = aux + 2 * total_anchors + b;
-        uint32_t M = 0;
-        for (uint32_t c = 0; c < N; c += 32) {
-            uint32_t i = c + lane;
-            bool take = i < N && dp[b + i] >= valid_score;
-            uint32_t bal = __ballot_sync(FULL, take);
-            if (take) cand[M + __popc(bal & lanemask_lt())] = i;
-            if (i < N) used[i] = 0;
-            M += __popc(bal);
-        }
-        __syncwarp();
-        // candidates by score, descending, ties in anchor order (a stable sort)
-        if (M <= 32) {
-            const uint32_t ci = lane < M ? cand[lane] : 0;
-            const float s = lane < M ? dp[b + ci] : 0.0f;
-            uint32_t rank = 0;
-            for (uint32_t u = 0; u < M; u++) {
-                const float su = __shfl_sync(FULL, s, u);
-                rank += (su > s) || (su == s && u < lane);
-            }
-            if (lane < M) sorted_c[rank] = ci;
+#pragma unroll
+            for (int q = 0; q < 4; q++) best_q[q] = __shfl_sync(FULL, best_score, q * CG);
         } else {
-            warp_radix_sort_desc(cand, sorted_c, M, dp + b, hist + (threadIdx.x / 32) * 256);
-        }
-        __syncwarp();
-        if (lane == 0) {
-            uint32_t nn = 0;
-            NamRec* outp = nam_out + b;
-            // a kept chain holds its end anchor (never marked used) and used
-            // predecessors, so kept chains list each anchor at most twice; a dropped
-            // chain's anchors are overwritten: 3 slots per anchor suffice
-            uint64_t* ao = anc_out ? anc_out + 3 * b : nullptr;
-            uint32_t acur = 0;
-            for (uint32_t c = 0; c < M; c++) {
-                uint32_t i = sorted_c[c];
-                if (used[i]) continue;
-                uint32_t j = i;
-                bool overlaps = false;
-                uint32_t nanch = 1;
-                const uint64_t ki = dedup[b + i];
-                if (ao) ao[acur] = ki;
-                uint32_t matching = cc.k;
-                uint32_t cov = (uint32_t)((ki >> ap.qbits) & pmask);
-                while (pred[b + j] != 0xffffffffu) {
-                    j = pred[b + j];
-                    if (used[j]) { overlaps = true; break; }
-                    if (ao) ao[acur + nanch] = dedup[b + j];
-                    nanch++;
-                    used[j] = 1;
-                    uint32_t rsj = (uint32_t)((dedup[b + j] >> ap.qbits) & pmask);
-                    uint32_t d = cov > rsj ? cov - rsj : 0;
-                    matching += d < cc.k ? d : cc.k;
-                    cov = rsj;
+            // the whole warp per orientation
+            uint64_t* ring_key = ring_key_s + (RING ? wib * 4 * 64 : 0);
+            float* ring_dp = ring_dp_s + (RING ? wib * 4 * 64 : 0);
+            for (int q = 0; q < 4; q++) {
+                const uint32_t sg = sg0 + q, N = Nq[q];
+                if (sg >= nseg || N == 0) continue;
+                const uint64_t b = bq[q];
+                const uint32_t read_len = (uint32_t)(off[(sg >> 1) + 1] - off[sg >> 1]);
+                const uint32_t max_ref_gap = cc.cp.max_ref_gap ? cc.cp.max_ref_gap : read_len;
+                float best_score = 0.0f;
+                uint32_t best_index = 0xffffffffu;
+                uint64_t best_key = 0;
+                uint64_t next_key = dedup[b];
+                for (uint32_t i = 0; i < N; i++) {
+                    const uint64_t ki = next_key;
+                    if (i + 1 < N) next_key = dedup[b + i + 1];
+                    const uint32_t ri = (uint32_t)(ki >> (ap.pbits + ap.qbits)),
+                                   rsi = (uint32_t)((ki >> ap.qbits) & pmask), qi = (uint32_t)(ki & qmask);
+                    const uint32_t lookup_end = i > cc.cp.max_lookback ? i - cc.cp.max_lookback : 0;
+                    float cur = kf;
+                    uint32_t cur_pred = 0xffffffffu;
+                    bool stop = false;
+                    for (uint32_t base = 0; !stop && base < i - lookup_end; base += 32) {
+                        const uint32_t t = base + lane;
+                        const bool in = t < i - lookup_end;
+                        const uint32_t j = i - 1 - t;
+                        bool hard, valid, diag;
+                        float val;
+                        chain_candidates<RING>(j, in, dedup, dp, b, ring_key, ring_dp, ri, rsi, qi, max_ref_gap, cc,
+                                               ap, hard, valid, diag, val);
+                        const uint32_t hb = __ballot_sync(FULL, hard);
+                        const uint32_t lim = hb ? (uint32_t)(__ffs(hb) - 1) : 32;
+                        if (lane >= lim) valid = false;
+                        float incl = valid ? val : -INFINITY;
+                        for (int d = 1; d < 32; d <<= 1) {
+                            const float y = __shfl_up_sync(FULL, incl, d);
+                            if (lane >= (uint32_t)d) incl = fmaxf(incl, y);
+                        }
+                        float excl = __shfl_up_sync(FULL, incl, 1);
+                        if (lane == 0) excl = -INFINITY;
+                        const bool upd = valid && val >= fmaxf(cur, excl);
+                        const uint32_t ub = __ballot_sync(FULL, upd);
+                        const uint32_t sb = __ballot_sync(FULL, upd && diag);
+                        uint32_t reach = lim;
+                        if (sb) {
+                            reach = (uint32_t)__ffs(sb);
+                            stop = true;
+                        }
+                        if (hb) stop = true;
+                        const uint32_t um = ub & (reach >= 32 ? FULL : ((1u << reach) - 1));
+                        if (um) {
+                            const uint32_t last = 31 - __clz(um);
+                            cur = __shfl_sync(FULL, val, last);
+                            cur_pred = i - 1 - (base + last);
+                        }
+                    }
+                    if (best_index != 0xffffffffu) {
+                        const uint64_t kb = best_key;
+                        const uint32_t rb = (uint32_t)(kb >> (ap.pbits + ap.qbits)),
+                                       rsb = (uint32_t)((kb >> ap.qbits) & pmask), qb = (uint32_t)(kb & qmask);
+                        if (rb == ri && qi > qb) {
+                            const uint32_t dq = qi - qb, dr = rsi - rsb;
+                            const uint32_t mx = dq > dr ? dq : dr, mn = dq < dr ? dq : dr;
+                            if (dr < max_ref_gap && dr > 0 && !ratio_above(mx, mn, cc)) {
+                                const float ns = __fadd_rn(best_score, chain_score(dq, dr, cc));
+                                if (ns > cur) {
+                                    cur = ns;
+                                    cur_pred = best_index;
+                                }
+                            }
+                        }
+                    }
+                    if (lane == 0) {
+                        dp[b + i] = cur;
+                        pred[b + i] = cur_pred;
+                        if (RING) {
+                            ring_key[i & 63] = ki;
+                            ring_dp[i & 63] = cur;
+                        }
+                    }
+                    if (cur > best_score) {
+                        best_score = cur;
+                        best_index = i;
+                        best_key = ki;
+                    }
+                    __syncwarp();
                 }
-                if (overlaps) continue;
-                const uint64_t kf2 = dedup[b + j];
-                NamRec nr;
-                nr.nam_id = nn;
-                nr.query_start = (uint32_t)(kf2 & qmask);
-                nr.query_end = (uint32_t)(ki & qmask) + cc.k;
-                nr.ref_start = (uint32_t)((kf2 >> ap.qbits) & pmask);
-                nr.ref_end = (uint32_t)((ki >> ap.qbits) & pmask) + cc.k;
-                nr.matching_bases = matching;
-                nr.ref_id = (uint32_t)(ki >> (ap.pbits + ap.qbits));
-                nr.score = __fadd_rn(dp[b + i], __fmul_rn(__uint2float_rn(nanch), cc.cp.matches_weight));
-                nr.is_revcomp = sg & 1;
-                nr.n_anchors = nanch;
-                if (anc_start) anc_start[b + nn] = 3 * b + acur;
-                acur += nanch;
-                outp[nn++] = nr;
+                best_q[q] = best_score;
             }
-            nam_seg_count[sg] = nn;
         }
         __syncwarp();
+        for (int q = 0; q < 4; q++) {
+            const uint32_t sg = sg0 + q;
+            if (sg >= nseg) break;
+            if (Nq[q] == 0) {
+                if (lane == 0) nam_seg_count[sg] = 0;
+                continue;
+            }
+            chain_extract(dedup, dp, pred, aux, total_anchors, bq[q], Nq[q], sg, best_q[q], ap, cc, nam_out,
+                          nam_seg_count, anc_out, anc_start, hist + wib * 256);
+        }
     }
 }
 
@@ -1298,12 +1456,12 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
         ws.anc_start.reserve(total_anchors + 1);
     }
     if (cfg.cp.max_lookback < 64)
-        k_chain<true><<<warps_grid(2 * (uint64_t)n), 32 * WARPS_PER_BLOCK, 0, st>>>(
+        k_chain4<true><<<warps_grid((2 * (uint64_t)n + 3) / 4), 32 * WARPS_PER_BLOCK, 0, st>>>(
             ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p,
             total_anchors, ap, cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
             cfg.nam_anchors ? ws.anc_start.p : nullptr);
     else
-        k_chain<false><<<warps_grid(2 * (uint64_t)n), 32 * WARPS_PER_BLOCK, 0, st>>>(
+        k_chain4<false><<<warps_grid((2 * (uint64_t)n + 3) / 4), 32 * WARPS_PER_BLOCK, 0, st>>>(
             ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p,
             total_anchors, ap, cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
             cfg.nam_anchors ? ws.anc_start.p : nullptr);

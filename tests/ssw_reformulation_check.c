@@ -1,4 +1,5 @@
-// The GPU striped Smith-Waterman (strobealign_gb300/csrc/extend.cu, k_ssw) computes
+// The GPU striped Smith-Waterman (strobealign_gb300/csrc/extend.cu, k_ssw and
+// k_ssw_wave) computes
 // two parts of ssw.c's striped passes (ext/ssw/ssw.c:163-596) in a different form:
 //   * the in-segment F recurrence as vF' = max(vF - gE, max(max(vH + m, E) - gO, 0)),
 //   * the lazy-F loop (ext/ssw/ssw.c:285-299) in closed form:
@@ -7,7 +8,8 @@
 // This program runs both the library's order of operations (mode 0) and the
 // rewritten form (mode 2) on random tasks with planted alignments and compares
 // every column's H and E and the reported maximum and end positions.  Valid for
-// gap_open >= gap_extend, the case the GPU kernel is used for.
+// gap_open > gap_extend, the case the GPU kernels are used for (with equal penalties
+// the library's lazy-F loop stops after the first row of each lane).
 // Usage: ssw_reformulation_check [trials]; exit status 1 on any difference.
 #include <stdio.h>
 #include <stdlib.h>
@@ -113,7 +115,7 @@ static long run(const int* q, int qlen, const int* r, int rlen, int NL, int gO, 
 int main(int argc, char** argv) {
     int trials = argc > 1 ? atoi(argv[1]) : 20000;
     int bad = 0; long cols = 0, lazylong = 0;
-    int pens[][4] = {{12, 1, 2, 8}, {12, 1, 2, 8}, {6, 1, 1, 4}, {5, 2, 2, 3}, {11, 1, 1, 1}, {4, 4, 2, 2}, {3, 1, 5, 1}};
+    int pens[][4] = {{12, 1, 2, 8}, {12, 1, 2, 8}, {6, 1, 1, 4}, {5, 2, 2, 3}, {11, 1, 1, 1}, {5, 4, 2, 2}, {3, 1, 5, 1}};
     for (int t = 0; t < trials; t++) {
         int* P = pens[rnd() % 7];
         int gO = P[0], gE = P[1], match = P[2], mism = P[3];

@@ -157,12 +157,15 @@ def test_nams_identical_to_oracle(sa, synth, repeats, mcs, genome):
             assert det[i][k] == v, (i, k)
 
 
-# the longest query of a batch picks the striped kernel variant (rows per lane)
-@pytest.mark.parametrize("max_len", [64, 160, 256, 500])
-def test_align_batch_identical_to_oracle(sa, max_len):
+# the longest query of a batch picks the striped kernel variant (rows per lane); the
+# scores cover the defaults, equal gap penalties (the library's lazy-F loop then stops
+# after each lane's first row) and a larger gap extension
+@pytest.mark.parametrize("max_len,scores", [(64, None), (160, None), (192, None), (256, None), (500, None),
+                                            (160, (2, 4, 2, 2)), (500, (2, 4, 2, 2)), (160, (3, 5, 6, 2))])
+def test_align_batch_identical_to_oracle(sa, max_len, scores):
     rnd = random.Random(11 + max_len)
     qs, rs = [], []
-    lengths = [x for x in (1, 10, 17, 50, 64, 100, 127, 150, 160, 200, 256, 300, 500) if x <= max_len]
+    lengths = [x for x in (1, 10, 17, 50, 64, 100, 127, 150, 160, 191, 192, 200, 256, 300, 500) if x <= max_len]
     for _ in range(1500):
         L = rnd.choice(lengths)
         q = bytes(rnd.choice(b"ACGT") for _ in range(L))
@@ -185,9 +188,15 @@ def test_align_batch_identical_to_oracle(sa, max_len):
             r = bytes(rnd.choice(b"ACGT") for _ in range(rnd.randint(1, 80)))
         qs.append(q)
         rs.append(r)
-    got = sa.align_batch(qs, rs)
+    mp = None
+    kw = {}
+    if scores is not None:
+        mp = sa.mapping_defaults()
+        mp.match, mp.mismatch, mp.gap_open, mp.gap_extend = scores
+        kw = dict(match=scores[0], mismatch=scores[1], go=scores[2], ge=scores[3])
+    got = sa.align_batch(qs, rs, mp)
     for q, r, g in zip(qs, rs, got):
-        assert g == aligner_oracle(q, r), (q, r)
+        assert g == aligner_oracle(q, r, **kw), (q, r)
 
 
 def _map_files(sa, fa, files, read_length=None, header=True, **kw):
