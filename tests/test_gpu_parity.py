@@ -182,8 +182,10 @@ def test_align_batch_identical_to_oracle(sa, max_len, scores):
                 core += bytes([c, rnd.choice(b"ACGT")])
             else:
                 core.append(c)
-        r = bytes(rnd.choice(b"ACGT") for _ in range(rnd.randint(0, 30))) + bytes(core) + \
-            bytes(rnd.choice(b"ACGT") for _ in range(rnd.randint(0, 30)))
+        # wide flanks make windows like mate rescue's (read + 450 nt)
+        fl = 300 if rnd.random() < 0.2 else 30
+        r = bytes(rnd.choice(b"ACGT") for _ in range(rnd.randint(0, fl))) + bytes(core) + \
+            bytes(rnd.choice(b"ACGT") for _ in range(rnd.randint(0, fl)))
         if rnd.random() < 0.05:
             r = bytes(rnd.choice(b"ACGT") for _ in range(rnd.randint(1, 80)))
         qs.append(q)
