@@ -848,6 +848,23 @@ __device__ void chain_extract(const uint64_t* dedup, const float* dp, const uint
     __syncwarp();
 }
 
+// The read orientations that have anchors, in increasing order within each warp's 32
+// (only the better orientation of a read gets anchors, src/chainer.rs:205-216, so about
+// half are empty); k_chain4 takes them four at a time.
+__global__ void k_seg_list(const uint64_t* seg_count, uint32_t nseg, uint32_t* list, uint32_t* n_list) {
+    const uint32_t lane = lane_id();
+    const uint32_t step = gridDim.x * blockDim.x;
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < nseg; base += step) {
+        const uint32_t sg = base + lane;
+        const bool ne = sg < nseg && seg_count[sg] > 0;
+        const uint32_t bal = __ballot_sync(FULL, ne);
+        uint32_t at = 0;
+        if (lane == 0 && bal) at = atomicAdd(n_list, (uint32_t)__popc(bal));
+        at = __shfl_sync(FULL, at, 0);
+        if (ne) list[at + __popc(bal & lanemask_lt())] = sg;
+    }
+}
+
 // Chaining (src/chainer.rs:128-176 and 386-449) for four read orientations per warp
 // (2 reads).  The deduplication and the extraction run over the whole warp, one
 // orientation after the other.  The DP is serial over a read orientation's anchors;
@@ -858,7 +875,9 @@ __device__ void chain_extract(const uint64_t* dedup, const float* dp, const uint
 // the four orientations at once, one group of eight lanes each, eight candidates at a
 // time (most anchors stop at the first candidate: the one before on the same
 // diagonal).  Warps whose orientations have more than CHAIN_GROUP_MAX anchors run the
-// DP with the whole warp per orientation, 32 candidates at a time.
+// DP with the whole warp per orientation, 32 candidates at a time.  The orientations
+// come from k_seg_list (those with anchors); nam_seg_count of the others is zeroed
+// before the launch.
 //
 // RING: max_lookback < 64, so the predecessors of anchor i (and their scores) come
 // from a 64-entry ring in shared memory per orientation, written as anchors are
@@ -902,7 +921,7 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
                                                 const uint64_t* sorted, uint64_t* dedup, float* dp, uint32_t* pred,
                                                 uint32_t* aux, uint64_t total_anchors, AnchorPack ap, ChainCtx cc,
                                                 NamRec* nam_out, uint32_t* nam_seg_count, uint64_t* anc_out,
-                                                uint64_t* anc_start) {
+                                                uint64_t* anc_start, const uint32_t* seg_list, uint32_t n_list) {
     __shared__ uint32_t hist[WARPS_PER_BLOCK * 256];
     __shared__ uint64_t ring_key_s[RING ? WARPS_PER_BLOCK * 4 * 64 : 1];
     __shared__ float ring_dp_s[RING ? WARPS_PER_BLOCK * 4 * 64 : 1];
@@ -912,17 +931,20 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
     const uint64_t qmask = (1ULL << ap.qbits) - 1, pmask = (1ULL << ap.pbits) - 1;
     const uint64_t kmask = ap.seg_shift ? (1ULL << ap.seg_shift) - 1 : ~0ULL;  // drop the segment prefix
     const float kf = __uint2float_rn(cc.k);
-    const uint32_t nseg = 2 * n;
-    for (uint32_t sg0 = 4 * (blockIdx.x * (blockDim.x / 32) + wib); sg0 < nseg; sg0 += 4 * nwarps) {
+    constexpr uint32_t NONE = 0xffffffffu;
+    for (uint32_t l0 = 4 * (blockIdx.x * (blockDim.x / 32) + wib); l0 < n_list; l0 += 4 * nwarps) {
+        uint32_t sgq[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) sgq[q] = l0 + q < n_list ? seg_list[l0 + q] : NONE;
         // dedup (src/chainer.rs:228-229), one orientation after the other
         uint32_t Nq[4];
         uint64_t bq[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            const uint32_t sg = sg0 + q;
+            const uint32_t sg = sgq[q];
             Nq[q] = 0;
             bq[q] = 0;
-            if (sg >= nseg) continue;
+            if (sg == NONE) continue;
             const uint64_t b = seg_off[sg], e = seg_off[sg + 1];
             bq[q] = b;
             uint32_t N = 0;
@@ -944,13 +966,13 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
         const uint32_t nmax = max(max(Nq[0], Nq[1]), max(Nq[2], Nq[3]));
         float best_q[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         if (nmax <= CHAIN_GROUP_MAX) {
-            // grouped DP: group g scores orientation sg0 + g
-            const uint32_t sg = sg0 + g;
+            // grouped DP: group g scores the g-th orientation
+            const uint32_t sg = g == 0 ? sgq[0] : g == 1 ? sgq[1] : g == 2 ? sgq[2] : sgq[3];
             const uint32_t N = g == 0 ? Nq[0] : g == 1 ? Nq[1] : g == 2 ? Nq[2] : Nq[3];
             const uint64_t b = g == 0 ? bq[0] : g == 1 ? bq[1] : g == 2 ? bq[2] : bq[3];
             uint64_t* ring_key = ring_key_s + (RING ? (wib * 4 + g) * 64 : 0);
             float* ring_dp = ring_dp_s + (RING ? (wib * 4 + g) * 64 : 0);
-            const uint32_t read_len = sg < nseg ? (uint32_t)(off[(sg >> 1) + 1] - off[sg >> 1]) : 0;
+            const uint32_t read_len = sg != NONE ? (uint32_t)(off[(sg >> 1) + 1] - off[sg >> 1]) : 0;
             const uint32_t max_ref_gap = cc.cp.max_ref_gap ? cc.cp.max_ref_gap : read_len;
             float best_score = 0.0f;
             uint32_t best_index = 0xffffffffu;
@@ -1043,8 +1065,8 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
             uint64_t* ring_key = ring_key_s + (RING ? wib * 4 * 64 : 0);
             float* ring_dp = ring_dp_s + (RING ? wib * 4 * 64 : 0);
             for (int q = 0; q < 4; q++) {
-                const uint32_t sg = sg0 + q, N = Nq[q];
-                if (sg >= nseg || N == 0) continue;
+                const uint32_t sg = sgq[q], N = Nq[q];
+                if (sg == NONE || N == 0) continue;
                 const uint64_t b = bq[q];
                 const uint32_t read_len = (uint32_t)(off[(sg >> 1) + 1] - off[sg >> 1]);
                 const uint32_t max_ref_gap = cc.cp.max_ref_gap ? cc.cp.max_ref_gap : read_len;
@@ -1131,8 +1153,8 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
         }
         __syncwarp();
         for (int q = 0; q < 4; q++) {
-            const uint32_t sg = sg0 + q;
-            if (sg >= nseg) break;
+            const uint32_t sg = sgq[q];
+            if (sg == NONE) break;
             if (Nq[q] == 0) {
                 if (lane == 0) nam_seg_count[sg] = 0;
                 continue;
@@ -1394,8 +1416,15 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     SA_CUDA(cudaMemsetAsync(ws.seg_count.p + 2 * (size_t)n, 0, 8, st));
     cub_excl_sum(ws, ws.seg_count.p, ws.seg_off.p, 2 * (uint64_t)n + 1, st);
     launches++;
+    ws.seg_list.reserve(2 * (size_t)n + 1);
+    SA_CUDA(cudaMemsetAsync(ws.seg_list.p + 2 * (size_t)n, 0, 4, st));
+    k_seg_list<<<warps_grid((2 * (uint64_t)n + 31) / 32), 32 * WARPS_PER_BLOCK, 0, st>>>(
+        ws.seg_count.p, 2 * n, ws.seg_list.p, ws.seg_list.p + 2 * (size_t)n);
+    launches++;
     uint64_t total_anchors = 0;
+    uint32_t n_list = 0;
     SA_CUDA(cudaMemcpyAsync(&total_anchors, ws.seg_off.p + 2 * (size_t)n, 8, cudaMemcpyDeviceToHost, st));
+    SA_CUDA(cudaMemcpyAsync(&n_list, ws.seg_list.p + 2 * (size_t)n, 4, cudaMemcpyDeviceToHost, st));
     SA_CUDA(cudaStreamSynchronize(st));
     ws.anchors.reserve(total_anchors);
     ws.anchors_sorted.reserve(total_anchors);
@@ -1451,20 +1480,21 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
         }
     }
     kt->begin(KS_CHAIN, st);
+    SA_CUDA(cudaMemsetAsync(ws.nam_seg_count.p, 0, 2 * (size_t)n * sizeof(uint32_t), st));
     if (cfg.nam_anchors) {
         ws.anc_sparse.reserve(3 * total_anchors + 1);
         ws.anc_start.reserve(total_anchors + 1);
     }
     if (cfg.cp.max_lookback < 64)
-        k_chain4<true><<<warps_grid((2 * (uint64_t)n + 3) / 4), 32 * WARPS_PER_BLOCK, 0, st>>>(
+        k_chain4<true><<<warps_grid(((uint64_t)n_list + 3) / 4), 32 * WARPS_PER_BLOCK, 0, st>>>(
             ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p,
             total_anchors, ap, cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
-            cfg.nam_anchors ? ws.anc_start.p : nullptr);
+            cfg.nam_anchors ? ws.anc_start.p : nullptr, ws.seg_list.p, n_list);
     else
-        k_chain4<false><<<warps_grid((2 * (uint64_t)n + 3) / 4), 32 * WARPS_PER_BLOCK, 0, st>>>(
+        k_chain4<false><<<warps_grid(((uint64_t)n_list + 3) / 4), 32 * WARPS_PER_BLOCK, 0, st>>>(
             ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p,
             total_anchors, ap, cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
-            cfg.nam_anchors ? ws.anc_start.p : nullptr);
+            cfg.nam_anchors ? ws.anc_start.p : nullptr, ws.seg_list.p, n_list);
     kt->end(st);
     launches++;
     ws.nam_count.reserve((size_t)n + 1);
