@@ -474,15 +474,12 @@ __global__ void __launch_bounds__(256) k_hits(DevIndex ix, const uint64_t* __res
 }
 
 // ------------------------------------------------------------------ anchors
+// Anchor keys: (ref_id, ref_start, query_start) packed so that integer order is the
+// reference's anchor order (src/chainer.rs:228).
 struct AnchorPack {
     uint32_t qbits, pbits;
-    // When seg_shift is set, the read orientation's index sits above the anchor key
-    // (hi = segment << seg_shift), so that one radix sort of the whole batch orders
-    // anchors by segment, then (ref_id, ref_start, query_start); k_chain4 masks it off.
-    uint32_t seg_shift = 0;
-    uint64_t hi = 0;
     __device__ __forceinline__ uint64_t key(uint32_t ref_id, uint32_t ref_start, uint32_t qs) const {
-        return hi | ((uint64_t)ref_id << (pbits + qbits)) | ((uint64_t)ref_start << qbits) | qs;
+        return ((uint64_t)ref_id << (pbits + qbits)) | ((uint64_t)ref_start << qbits) | qs;
     }
 };
 
@@ -611,7 +608,6 @@ __global__ void __launch_bounds__(256) k_anchors(DevIndex ix, const uint64_t* __
             const uint32_t nh = (m >> ori) & 1 ? n_hits[2 * r + ori] : 0;
             uint64_t acc = FILL ? seg_off[2 * r + ori] : 0;
             AnchorPack aps = ap;
-            if (ap.seg_shift) aps.hi = (uint64_t)(2 * r + ori) << ap.seg_shift;
             uint32_t sum = 0;
             for (uint32_t c = 0; c < nh; c += 32) {
                 uint32_t h = c + lane;
@@ -850,19 +846,98 @@ __device__ void chain_extract(const uint64_t* dedup, const float* dp, const uint
 
 // The read orientations that have anchors, in increasing order within each warp's 32
 // (only the better orientation of a read gets anchors, src/chainer.rs:205-216, so about
-// half are empty); k_chain4 takes them four at a time.
-__global__ void k_seg_list(const uint64_t* seg_count, uint32_t nseg, uint32_t* list, uint32_t* n_list) {
+// half are empty); k_chain4 takes them four at a time.  The ranges of those with more
+// than CHAIN_SORT_SMALL anchors go to sort_begin / sort_end for a segmented sort;
+// k_chain4 sorts the others itself.  n_list[0]: listed orientations, n_list[1]: ranges.
+constexpr uint32_t CHAIN_SORT_SMALL = 256;
+
+__global__ void k_seg_list(const uint64_t* seg_count, const uint64_t* seg_off, uint32_t nseg, uint32_t* list,
+                           uint32_t* n_list, uint64_t* sort_begin, uint64_t* sort_end) {
     const uint32_t lane = lane_id();
     const uint32_t step = gridDim.x * blockDim.x;
     for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < nseg; base += step) {
         const uint32_t sg = base + lane;
-        const bool ne = sg < nseg && seg_count[sg] > 0;
-        const uint32_t bal = __ballot_sync(FULL, ne);
-        uint32_t at = 0;
+        const uint64_t cnt = sg < nseg ? seg_count[sg] : 0;
+        const bool ne = cnt > 0, big = cnt > CHAIN_SORT_SMALL;
+        const uint32_t bal = __ballot_sync(FULL, ne), bb = __ballot_sync(FULL, big);
+        uint32_t at = 0, atb = 0;
         if (lane == 0 && bal) at = atomicAdd(n_list, (uint32_t)__popc(bal));
+        if (lane == 0 && bb) atb = atomicAdd(n_list + 1, (uint32_t)__popc(bb));
         at = __shfl_sync(FULL, at, 0);
+        atb = __shfl_sync(FULL, atb, 0);
         if (ne) list[at + __popc(bal & lanemask_lt())] = sg;
+        if (big) {
+            const uint32_t k = atb + __popc(bb & lanemask_lt());
+            const uint64_t o = seg_off[sg];
+            sort_begin[k] = o;
+            sort_end[k] = o + cnt;
+        }
     }
+}
+
+// Ascending bitonic sort of R * 32 keys held R per lane (element r * 32 + lane in v[r]).
+template <int R>
+__device__ __forceinline__ void warp_bitonic_sort(uint64_t (&v)[R]) {
+    const uint32_t lane = lane_id();
+#pragma unroll
+    for (uint32_t k = 2; k <= 32 * R; k <<= 1) {
+#pragma unroll
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+                // partners in two registers of one lane; the direction depends on r only
+                const int jr = (int)(j >> 5);
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    if (r & jr) continue;
+                    const int r2 = r | jr;
+                    const bool asc = ((32u * r) & k) == 0;
+                    const uint64_t lo = v[r] < v[r2] ? v[r] : v[r2], hi = v[r] < v[r2] ? v[r2] : v[r];
+                    v[r] = asc ? lo : hi;
+                    v[r2] = asc ? hi : lo;
+                }
+            } else {
+                const bool lower = (lane & j) == 0;
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    const uint64_t p = __shfl_xor_sync(FULL, v[r], j);
+                    const bool asc = ((32 * r + lane) & k) == 0;
+                    const bool take_min = lower == asc;
+                    v[r] = take_min ? (p < v[r] ? p : v[r]) : (p > v[r] ? p : v[r]);
+                }
+            }
+        }
+    }
+}
+
+// Sort the cnt <= 32 * R keys at keys[0..cnt) (one read orientation's anchors, in the
+// order k_anchors wrote them) and write the distinct ones back in order; returns their
+// number (src/chainer.rs:228-229).
+template <int R>
+__device__ __forceinline__ uint32_t warp_sort_dedup(uint64_t* keys, uint32_t cnt) {
+    const uint32_t lane = lane_id();
+    uint64_t v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = 32 * r + lane < cnt ? keys[32 * r + lane] : ~0ULL;
+    warp_bitonic_sort<R>(v);
+    uint32_t bal[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        uint64_t prev = __shfl_up_sync(FULL, v[r], 1);
+        if (r > 0) {
+            const uint64_t last = __shfl_sync(FULL, v[r > 0 ? r - 1 : 0], 31);
+            if (lane == 0) prev = last;
+        }
+        const uint32_t e = 32 * r + lane;
+        bal[r] = __ballot_sync(FULL, e < cnt && (e == 0 || prev != v[r]));
+    }
+    __syncwarp();
+    uint32_t n = 0;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        if ((bal[r] >> lane) & 1u) keys[n + __popc(bal[r] & lanemask_lt())] = v[r];
+        n += __popc(bal[r]);
+    }
+    return n;
 }
 
 // Chaining (src/chainer.rs:128-176 and 386-449) for four read orientations per warp
@@ -929,7 +1004,6 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
     const uint32_t wib = threadIdx.x / 32;
     const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
     const uint64_t qmask = (1ULL << ap.qbits) - 1, pmask = (1ULL << ap.pbits) - 1;
-    const uint64_t kmask = ap.seg_shift ? (1ULL << ap.seg_shift) - 1 : ~0ULL;  // drop the segment prefix
     const float kf = __uint2float_rn(cc.k);
     constexpr uint32_t NONE = 0xffffffffu;
     for (uint32_t l0 = 4 * (blockIdx.x * (blockDim.x / 32) + wib); l0 < n_list; l0 += 4 * nwarps) {
@@ -948,17 +1022,26 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
             const uint64_t b = seg_off[sg], e = seg_off[sg + 1];
             bq[q] = b;
             uint32_t N = 0;
-            for (uint64_t c = b; c < e; c += 32) {
-                const uint64_t i = c + lane;
-                bool keep = false;
-                uint64_t key = 0;
-                if (i < e) {
-                    key = sorted[i];
-                    keep = i == b || sorted[i - 1] != key;
+            const uint32_t cnt = (uint32_t)(e - b);
+            if (cnt <= CHAIN_SORT_SMALL) {
+                // the orientation's keys, still unsorted in the dedup buffer: sort them here
+                if (cnt <= 32) N = warp_sort_dedup<1>(dedup + b, cnt);
+                else if (cnt <= 64) N = warp_sort_dedup<2>(dedup + b, cnt);
+                else if (cnt <= 128) N = warp_sort_dedup<4>(dedup + b, cnt);
+                else N = warp_sort_dedup<8>(dedup + b, cnt);
+            } else {
+                for (uint64_t c = b; c < e; c += 32) {
+                    const uint64_t i = c + lane;
+                    bool keep = false;
+                    uint64_t key = 0;
+                    if (i < e) {
+                        key = sorted[i];
+                        keep = i == b || sorted[i - 1] != key;
+                    }
+                    const uint32_t bal = __ballot_sync(FULL, keep);
+                    if (keep) dedup[b + N + __popc(bal & lanemask_lt())] = key;
+                    N += __popc(bal);
                 }
-                const uint32_t bal = __ballot_sync(FULL, keep);
-                if (keep) dedup[b + N + __popc(bal & lanemask_lt())] = key & kmask;
-                N += __popc(bal);
             }
             Nq[q] = N;
         }
@@ -1379,11 +1462,6 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     ap.pbits = ceil_log2((uint64_t)max_contig_len + 1);
     uint32_t rbits = ceil_log2((uint64_t)n_contigs);
     if (ap.qbits + ap.pbits + rbits > 64) throw Error(SA_ERR_INVALID, "contig count/length too large for anchor keys");
-    // one radix sort over (read orientation, anchor key) when both fit in 64 bits, else a
-    // segmented sort per read orientation
-    const uint32_t abits = ap.qbits + ap.pbits + rbits, sbits = ceil_log2(2 * (uint64_t)n);
-    const bool radix = abits + sbits <= 64 && abits < 64;
-    if (radix) ap.seg_shift = abits;
     launches += run_seeding(ix.p, n, total, ws, st, kt);
     ws.hit_pos.reserve(2 * total);
     ws.hit_info.reserve(2 * total);
@@ -1416,15 +1494,18 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     SA_CUDA(cudaMemsetAsync(ws.seg_count.p + 2 * (size_t)n, 0, 8, st));
     cub_excl_sum(ws, ws.seg_count.p, ws.seg_off.p, 2 * (uint64_t)n + 1, st);
     launches++;
-    ws.seg_list.reserve(2 * (size_t)n + 1);
-    SA_CUDA(cudaMemsetAsync(ws.seg_list.p + 2 * (size_t)n, 0, 4, st));
+    ws.seg_list.reserve(2 * (size_t)n + 2);
+    ws.sort_begin.reserve(2 * (size_t)n);
+    ws.sort_end.reserve(2 * (size_t)n);
+    SA_CUDA(cudaMemsetAsync(ws.seg_list.p + 2 * (size_t)n, 0, 8, st));
     k_seg_list<<<warps_grid((2 * (uint64_t)n + 31) / 32), 32 * WARPS_PER_BLOCK, 0, st>>>(
-        ws.seg_count.p, 2 * n, ws.seg_list.p, ws.seg_list.p + 2 * (size_t)n);
+        ws.seg_count.p, ws.seg_off.p, 2 * n, ws.seg_list.p, ws.seg_list.p + 2 * (size_t)n, ws.sort_begin.p,
+        ws.sort_end.p);
     launches++;
     uint64_t total_anchors = 0;
-    uint32_t n_list = 0;
+    uint32_t n_list[2] = {0, 0};
     SA_CUDA(cudaMemcpyAsync(&total_anchors, ws.seg_off.p + 2 * (size_t)n, 8, cudaMemcpyDeviceToHost, st));
-    SA_CUDA(cudaMemcpyAsync(&n_list, ws.seg_list.p + 2 * (size_t)n, 4, cudaMemcpyDeviceToHost, st));
+    SA_CUDA(cudaMemcpyAsync(n_list, ws.seg_list.p + 2 * (size_t)n, 8, cudaMemcpyDeviceToHost, st));
     SA_CUDA(cudaStreamSynchronize(st));
     ws.anchors.reserve(total_anchors);
     ws.anchors_sorted.reserve(total_anchors);
@@ -1434,25 +1515,16 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
         ws.orient.p, ws.hit_anchors.p, nullptr, ws.seg_off.p, ws.anchors.p, ap, ws.details.p);
     kt->end(st);
     launches++;
-    if (total_anchors) {
+    if (n_list[1]) {
+        // orientations with more than CHAIN_SORT_SMALL anchors; k_chain4 sorts the rest
         size_t tmp = 0;
         kt->begin(KS_SORT, st);
-        if (radix) {
-            const int end_bit = (int)(abits + sbits);
-            cub::DeviceRadixSort::SortKeys(nullptr, tmp, ws.anchors.p, ws.anchors_sorted.p, (int64_t)total_anchors, 0,
-                                           end_bit, st);
-            ws.cub_tmp.reserve(tmp);
-            cub::DeviceRadixSort::SortKeys(ws.cub_tmp.p, tmp, ws.anchors.p, ws.anchors_sorted.p,
-                                           (int64_t)total_anchors, 0, end_bit, st);
-        } else {
-            cub::DeviceSegmentedSort::SortKeys(nullptr, tmp, ws.anchors.p, ws.anchors_sorted.p,
-                                               (int64_t)total_anchors, (int64_t)(2 * (uint64_t)n), ws.seg_off.p,
-                                               ws.seg_off.p + 1, st);
-            ws.cub_tmp.reserve(tmp);
-            cub::DeviceSegmentedSort::SortKeys(ws.cub_tmp.p, tmp, ws.anchors.p, ws.anchors_sorted.p,
-                                               (int64_t)total_anchors, (int64_t)(2 * (uint64_t)n), ws.seg_off.p,
-                                               ws.seg_off.p + 1, st);
-        }
+        cub::DeviceSegmentedSort::SortKeys(nullptr, tmp, ws.anchors.p, ws.anchors_sorted.p, (int64_t)total_anchors,
+                                           (int64_t)n_list[1], ws.sort_begin.p, ws.sort_end.p, st);
+        ws.cub_tmp.reserve(tmp);
+        cub::DeviceSegmentedSort::SortKeys(ws.cub_tmp.p, tmp, ws.anchors.p, ws.anchors_sorted.p,
+                                           (int64_t)total_anchors, (int64_t)n_list[1], ws.sort_begin.p, ws.sort_end.p,
+                                           st);
         kt->end(st);
         launches++;
     }
@@ -1486,15 +1558,15 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
         ws.anc_start.reserve(total_anchors + 1);
     }
     if (cfg.cp.max_lookback < 64)
-        k_chain4<true><<<warps_grid(((uint64_t)n_list + 3) / 4), 32 * WARPS_PER_BLOCK, 0, st>>>(
+        k_chain4<true><<<warps_grid(((uint64_t)n_list[0] + 3) / 4), 32 * WARPS_PER_BLOCK, 0, st>>>(
             ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p,
             total_anchors, ap, cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
-            cfg.nam_anchors ? ws.anc_start.p : nullptr, ws.seg_list.p, n_list);
+            cfg.nam_anchors ? ws.anc_start.p : nullptr, ws.seg_list.p, n_list[0]);
     else
-        k_chain4<false><<<warps_grid(((uint64_t)n_list + 3) / 4), 32 * WARPS_PER_BLOCK, 0, st>>>(
+        k_chain4<false><<<warps_grid(((uint64_t)n_list[0] + 3) / 4), 32 * WARPS_PER_BLOCK, 0, st>>>(
             ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p,
             total_anchors, ap, cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
-            cfg.nam_anchors ? ws.anc_start.p : nullptr, ws.seg_list.p, n_list);
+            cfg.nam_anchors ? ws.anc_start.p : nullptr, ws.seg_list.p, n_list[0]);
     kt->end(st);
     launches++;
     ws.nam_count.reserve((size_t)n + 1);

@@ -47,8 +47,10 @@ struct NamWorkspace {
     DevBuf<NamRec> nam_tmp;
     DevBuf<uint32_t> nam_keys, nam_vals;
     DevBuf<uint32_t> long_reads;
-    // read orientations with anchors (2n slots), their count in slot 2n
+    // read orientations with anchors (2n slots), their count in slot 2n and the count of
+    // those sorted by the segmented sort in slot 2n + 1; that sort's ranges
     DevBuf<uint32_t> seg_list;
+    DevBuf<uint64_t> sort_begin, sort_end;
     DevBuf<uint64_t> long_begin, long_end;
     // with NamConfig::nam_anchors: the anchors of each NAM's chain, last to first
     // (src/chainer.rs:420-440), as packed anchor keys; NAM t's are at
