@@ -39,6 +39,58 @@ struct PodArray {
 };
 using RawBytes = PodArray<char>;
 
+// Growable byte buffer for formatted output.  Unlike std::string it grows without
+// zero-filling: tail(bound) hands out room for a write of at most bound bytes and
+// commit(end) keeps what was written, so a record is formatted in place.
+class OutBuf {
+  public:
+    size_t size() const { return n_; }
+    bool empty() const { return n_ == 0; }
+    const char* data() const { return p_.get(); }
+    char* data() { return p_.get(); }
+    void clear() { n_ = 0; }
+    void reserve(size_t k) {
+        if (k > cap_) grow(k);
+    }
+    void resize(size_t k) {  // bytes past the old size are not initialised
+        if (k > cap_) grow(k);
+        n_ = k;
+    }
+    char* tail(size_t bound) {
+        if (n_ + bound > cap_) grow(n_ + bound);
+        return p_.get() + n_;
+    }
+    void commit(const char* end) { n_ = (size_t)(end - p_.get()); }
+    void append(const char* s, size_t k) {
+        if (k) std::memcpy(tail(k), s, k);
+        n_ += k;
+    }
+    void push_back(char c) {
+        *tail(1) = c;
+        n_++;
+    }
+    OutBuf& operator+=(const std::string& s) {
+        append(s.data(), s.size());
+        return *this;
+    }
+    OutBuf& operator+=(const char* s) {
+        append(s, std::strlen(s));
+        return *this;
+    }
+
+  private:
+    void grow(size_t need) {
+        size_t c = cap_ * 2 > need ? cap_ * 2 : need;
+        if (c < 4096) c = 4096;
+        std::unique_ptr<char[]> q(new char[c]);
+        if (n_) std::memcpy(q.get(), p_.get(), n_);
+        p_ = std::move(q);
+        cap_ = c;
+    }
+    std::unique_ptr<char[]> p_;
+    size_t n_ = 0, cap_ = 0;
+};
+
 // Output buffers handed to the caller (released with release_output, which
 // sa_output_free calls).  Large ones are 2 MiB aligned and advised to use huge pages,
 // and a few released ones are kept for reuse: a stream of batches then writes its SAM

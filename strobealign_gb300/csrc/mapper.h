@@ -108,7 +108,7 @@ class Mapper {
     WavePool wave_pool_;
     // output and bookkeeping buffers of the last batch's chunks, reused by the next
     struct ChunkBuffers {
-        std::string out, spec_out;
+        OutBuf out, spec_out;
         std::vector<ChunkState::Effect> effects;
         std::vector<ResultStore::Entry> entries;
         std::vector<ChunkState::Piece> pieces;

@@ -114,13 +114,13 @@ struct Sam {
 
 const std::string EQUALS = "=";
 
-inline void put_u64(std::string& o, uint64_t v) {
+inline void put_u64(OutBuf& o, uint64_t v) {
     char b[24];
     int n = 0;
     do { b[n++] = (char)('0' + v % 10); v /= 10; } while (v);
     while (n) o.push_back(b[--n]);
 }
-inline void put_i64(std::string& o, int64_t v) {
+inline void put_i64(OutBuf& o, int64_t v) {
     if (v < 0) { o.push_back('-'); put_u64(o, (uint64_t)(-v)); }
     else put_u64(o, (uint64_t)v);
 }
@@ -234,7 +234,7 @@ char* w_cigar(char* p, const Alignment& a, bool eqx) {
 }
 
 // src/io/sam.rs:53-138
-void format_sam(const Sam& r, const PolicyConfig& cfg, std::string& o) {
+void format_sam(const Sam& r, const PolicyConfig& cfg, OutBuf& o) {
     const bool secondary = (r.flags & SECONDARY) != 0;
     const ReadView& rv = *r.rv;
     size_t bound = rv.name_len + 2 * (size_t)rv.len + 160;
@@ -243,11 +243,8 @@ void format_sam(const Sam& r, const PolicyConfig& cfg, std::string& o) {
     if (r.aln) bound += ((size_t)r.aln->cigar_len + 2) * 11;
     if (cfg.has_rg) bound += 6 + cfg.rg_id.size();
     if (cfg.mp.fastq_comments && rv.comment) bound += 1 + rv.comment_len;
-    // written into per-thread scratch, then appended (no zero fill of the bound)
-    thread_local std::vector<char> scratch;
-    if (scratch.size() < bound) scratch.resize(2 * bound);
-    char* const base = scratch.data();
-    char* p = base;
+    // written in place at the end of the output (no zero fill of the bound)
+    char* p = o.tail(bound);
     p = w_str(p, rv.name, rv.name_len);
     *p++ = '\t';
     p = w_u64(p, r.flags);
@@ -315,7 +312,7 @@ void format_sam(const Sam& r, const PolicyConfig& cfg, std::string& o) {
         p = w_str(p, rv.comment, rv.comment_len);
     }
     *p++ = '\n';
-    o.append(base, (size_t)(p - base));
+    o.commit(p);
 }
 
 Sam mapped_record(const Policy& P, const Alignment& a, const ReadView& rv, uint8_t mapq, bool secondary,
@@ -796,7 +793,7 @@ std::vector<NamRec> Policy::sorted_nams(uint32_t read, Rng& rng) const {
 
 // ------------------------------------------------------------------ single end
 // src/mapper.rs:349-528
-bool Policy::se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mapped) {
+bool Policy::se_record(uint64_t rec, Rng& rng, OutBuf& out, uint64_t& mapped) {
     const uint32_t read = (uint32_t)rec;
     const ReadView& rv = bv_->reads[read];
     std::vector<NamRec>& nams = sc_->nams[0];
@@ -884,7 +881,7 @@ bool Policy::se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mappe
 
 // ------------------------------------------------------------------ paired end
 // src/mapper.rs:624-1091
-bool Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out, uint64_t& mapped) {
+bool Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, OutBuf& out, uint64_t& mapped) {
     const uint32_t rd[2] = {(uint32_t)(2 * rec), (uint32_t)(2 * rec + 1)};
     const ReadView* rv[2] = {&bv_->reads[rd[0]], &bv_->reads[rd[1]]};
     Details det[2];
@@ -1227,7 +1224,7 @@ bool Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out
 // ------------------------------------------------------------------ map-only / aemb
 namespace {
 
-void paf_line(const Policy& P, const NamRec& nam, const ReadView& rv, int end, int mapq, std::string& o) {
+void paf_line(const Policy& P, const NamRec& nam, const ReadView& rv, int end, int mapq, OutBuf& o) {
     o.append(rv.name, rv.name_len);
     if (end == 1) o += "/1";
     else if (end == 2) o += "/2";
@@ -1378,13 +1375,13 @@ int best_paired_location(const std::vector<NamPairM>& pairs, const std::vector<N
 }  // namespace
 
 // src/maponly.rs:18-52
-void Policy::paf_se(uint64_t rec, Rng& rng, std::string& out) {
+void Policy::paf_se(uint64_t rec, Rng& rng, OutBuf& out) {
     std::vector<NamRec> nams = sorted_nams((uint32_t)rec, rng);
     if (!nams.empty()) paf_line(*this, nams[0], bv_->reads[rec], 0, mapping_quality(nams), out);
 }
 
 // src/maponly.rs:114-195
-void Policy::paf_pe(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out) {
+void Policy::paf_pe(uint64_t rec, Rng& rng, InsertSize& isd, OutBuf& out) {
     uint32_t a = (uint32_t)(2 * rec), b = a + 1;
     std::vector<NamRec> n1 = unsorted_nams(*bv_, a), n2 = unsorted_nams(*bv_, b);
     if (n1.empty() && n2.empty()) return;
@@ -1482,7 +1479,7 @@ void Policy::run_chunk(ChunkState& cs) {
     const auto t_run = timing ? now() : std::chrono::steady_clock::time_point();
     cs.runs++;
     // false: the record stopped on a missing result
-    auto one = [&](uint64_t rec, Rng& rng, InsertSize& isd, std::string& out, uint64_t& mapped) -> bool {
+    auto one = [&](uint64_t rec, Rng& rng, InsertSize& isd, OutBuf& out, uint64_t& mapped) -> bool {
         switch (cfg_.mp.mode) {
             case SA_MODE_SAM:
                 return bv_->paired ? pe_record(rec, rng, isd, out, mapped) : se_record(rec, rng, out, mapped);
@@ -1542,7 +1539,7 @@ void Policy::run_chunk(ChunkState& cs) {
             // path updates it, and that path does not miss)
             Rng srng = rng;
             InsertSize sisd = isd;
-            std::string scratch;
+            OutBuf scratch;
             std::vector<uint64_t> todo;
             if (cs.effects.empty()) {
                 cs.effects.resize(cs.end - cs.first);

@@ -167,7 +167,7 @@ struct ChunkState {
     bool keep_buffers = false;              // done: clear the buffers but keep their memory (pooled)
     Rng rng;
     InsertSize isd;
-    std::string out;
+    OutBuf out;
     uint64_t mapped = 0;
     bool done = false;
     std::vector<ResultStore::Entry> entries;              // requests and results of this chunk's reads
@@ -195,7 +195,7 @@ struct ChunkState {
         uint64_t out_off = 0, out_len = 0, mapped = 0;
     };
     std::vector<Effect> effects;
-    std::string spec_out;  // outputs captured by the lookahead
+    OutBuf spec_out;  // outputs captured by the lookahead
     // the chunk's output in record order: ranges of `out` (records the real run
     // formatted) and of `spec_out` (captured records it reused), copied once into the
     // final buffer
@@ -257,10 +257,10 @@ class Policy {
     void resolve(ChunkState& cs);
 
     // false: stopped on a missing result (the record is evaluated again later)
-    bool se_record(uint64_t rec, Rng& rng, std::string& out, uint64_t& mapped);
-    bool pe_record(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out, uint64_t& mapped);
-    void paf_se(uint64_t rec, Rng& rng, std::string& out);
-    void paf_pe(uint64_t rec, Rng& rng, InsertSize& isd, std::string& out);
+    bool se_record(uint64_t rec, Rng& rng, OutBuf& out, uint64_t& mapped);
+    bool pe_record(uint64_t rec, Rng& rng, InsertSize& isd, OutBuf& out, uint64_t& mapped);
+    void paf_se(uint64_t rec, Rng& rng, OutBuf& out);
+    void paf_pe(uint64_t rec, Rng& rng, InsertSize& isd, OutBuf& out);
     void aemb_se(uint64_t rec, Rng& rng);
     void aemb_pe(uint64_t rec, Rng& rng, InsertSize& isd);
 
