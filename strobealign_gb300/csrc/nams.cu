@@ -844,30 +844,35 @@ __device__ void chain_extract(const uint64_t* dedup, const float* dp, const uint
     __syncwarp();
 }
 
-// The read orientations that have anchors, in increasing order within each warp's 32
-// (only the better orientation of a read gets anchors, src/chainer.rs:205-216, so about
-// half are empty); k_chain4 takes them four at a time.  The ranges of those with more
-// than CHAIN_SORT_SMALL anchors go to sort_begin / sort_end for a segmented sort;
-// k_chain4 sorts the others itself.  n_list[0]: listed orientations, n_list[1]: ranges.
+// The read orientations that have anchors (only the better orientation of a read gets
+// anchors, src/chainer.rs:205-216, so about half are empty), for k_chain4: those with
+// at most CHAIN_GROUP_MAX anchors in `list` (increasing within each warp's 32), taken
+// four per warp, the others in `long_list`, one per warp.  The ranges of those with
+// more than CHAIN_SORT_SMALL anchors go to sort_begin / sort_end for a segmented sort;
+// k_chain4 sorts the others itself.  n_list: [0] listed, [1] sort ranges, [2] long.
 constexpr uint32_t CHAIN_SORT_SMALL = 256;
+constexpr uint32_t CHAIN_GROUP_MAX = 96;
 
 __global__ void k_seg_list(const uint64_t* seg_count, const uint64_t* seg_off, uint32_t nseg, uint32_t* list,
-                           uint32_t* n_list, uint64_t* sort_begin, uint64_t* sort_end) {
+                           uint32_t* long_list, uint32_t* n_list, uint64_t* sort_begin, uint64_t* sort_end) {
     const uint32_t lane = lane_id();
     const uint32_t step = gridDim.x * blockDim.x;
     for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < nseg; base += step) {
         const uint32_t sg = base + lane;
         const uint64_t cnt = sg < nseg ? seg_count[sg] : 0;
-        const bool ne = cnt > 0, big = cnt > CHAIN_SORT_SMALL;
-        const uint32_t bal = __ballot_sync(FULL, ne), bb = __ballot_sync(FULL, big);
-        uint32_t at = 0, atb = 0;
-        if (lane == 0 && bal) at = atomicAdd(n_list, (uint32_t)__popc(bal));
-        if (lane == 0 && bb) atb = atomicAdd(n_list + 1, (uint32_t)__popc(bb));
-        at = __shfl_sync(FULL, at, 0);
-        atb = __shfl_sync(FULL, atb, 0);
-        if (ne) list[at + __popc(bal & lanemask_lt())] = sg;
+        const bool lng = cnt > CHAIN_GROUP_MAX, shrt = cnt > 0 && !lng, big = cnt > CHAIN_SORT_SMALL;
+        const uint32_t bs = __ballot_sync(FULL, shrt), bl = __ballot_sync(FULL, lng), bb = __ballot_sync(FULL, big);
+        uint32_t as = 0, al = 0, ab = 0;
+        if (lane == 0 && bs) as = atomicAdd(n_list, (uint32_t)__popc(bs));
+        if (lane == 0 && bb) ab = atomicAdd(n_list + 1, (uint32_t)__popc(bb));
+        if (lane == 0 && bl) al = atomicAdd(n_list + 2, (uint32_t)__popc(bl));
+        as = __shfl_sync(FULL, as, 0);
+        ab = __shfl_sync(FULL, ab, 0);
+        al = __shfl_sync(FULL, al, 0);
+        if (shrt) list[as + __popc(bs & lanemask_lt())] = sg;
+        if (lng) long_list[al + __popc(bl & lanemask_lt())] = sg;
         if (big) {
-            const uint32_t k = atb + __popc(bb & lanemask_lt());
+            const uint32_t k = ab + __popc(bb & lanemask_lt());
             const uint64_t o = seg_off[sg];
             sort_begin[k] = o;
             sort_end[k] = o + cnt;
@@ -958,7 +963,6 @@ __device__ __forceinline__ uint32_t warp_sort_dedup(uint64_t* keys, uint32_t cnt
 // from a 64-entry ring in shared memory per orientation, written as anchors are
 // scored, instead of global memory (this takes the store-to-load round trip out of
 // each serial step).
-constexpr uint32_t CHAIN_GROUP_MAX = 96;
 constexpr uint32_t CG = 8;  // lanes per orientation in the grouped DP
 
 template <bool RING>
@@ -996,7 +1000,8 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
                                                 const uint64_t* sorted, uint64_t* dedup, float* dp, uint32_t* pred,
                                                 uint32_t* aux, uint64_t total_anchors, AnchorPack ap, ChainCtx cc,
                                                 NamRec* nam_out, uint32_t* nam_seg_count, uint64_t* anc_out,
-                                                uint64_t* anc_start, const uint32_t* seg_list, uint32_t n_list) {
+                                                uint64_t* anc_start, const uint32_t* seg_list, uint32_t n_list,
+                                                const uint32_t* long_list, uint32_t n_long) {
     __shared__ uint32_t hist[WARPS_PER_BLOCK * 256];
     __shared__ uint64_t ring_key_s[RING ? WARPS_PER_BLOCK * 4 * 64 : 1];
     __shared__ float ring_dp_s[RING ? WARPS_PER_BLOCK * 4 * 64 : 1];
@@ -1006,10 +1011,18 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
     const uint64_t qmask = (1ULL << ap.qbits) - 1, pmask = (1ULL << ap.pbits) - 1;
     const float kf = __uint2float_rn(cc.k);
     constexpr uint32_t NONE = 0xffffffffu;
-    for (uint32_t l0 = 4 * (blockIdx.x * (blockDim.x / 32) + wib); l0 < n_list; l0 += 4 * nwarps) {
-        uint32_t sgq[4];
+    // units: the long orientations first (one per warp, so they start first), then the
+    // short ones four at a time
+    const uint32_t n_units = n_long + (n_list + 3) / 4;
+    for (uint32_t u = blockIdx.x * (blockDim.x / 32) + wib; u < n_units; u += nwarps) {
+        uint32_t sgq[4] = {NONE, NONE, NONE, NONE};
+        if (u < n_long) {
+            sgq[0] = long_list[u];
+        } else {
+            const uint32_t l0 = 4 * (u - n_long);
 #pragma unroll
-        for (int q = 0; q < 4; q++) sgq[q] = l0 + q < n_list ? seg_list[l0 + q] : NONE;
+            for (int q = 0; q < 4; q++) sgq[q] = l0 + q < n_list ? seg_list[l0 + q] : NONE;
+        }
         // dedup (src/chainer.rs:228-229), one orientation after the other
         uint32_t Nq[4];
         uint64_t bq[4];
@@ -1048,7 +1061,7 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
         __syncwarp();
         const uint32_t nmax = max(max(Nq[0], Nq[1]), max(Nq[2], Nq[3]));
         float best_q[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        if (nmax <= CHAIN_GROUP_MAX) {
+        if (u >= n_long && nmax <= CHAIN_GROUP_MAX) {
             // grouped DP: group g scores the g-th orientation
             const uint32_t sg = g == 0 ? sgq[0] : g == 1 ? sgq[1] : g == 2 ? sgq[2] : sgq[3];
             const uint32_t N = g == 0 ? Nq[0] : g == 1 ? Nq[1] : g == 2 ? Nq[2] : Nq[3];
@@ -1237,7 +1250,7 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
         __syncwarp();
         for (int q = 0; q < 4; q++) {
             const uint32_t sg = sgq[q];
-            if (sg == NONE) break;
+            if (sg == NONE) continue;
             if (Nq[q] == 0) {
                 if (lane == 0) nam_seg_count[sg] = 0;
                 continue;
@@ -1494,18 +1507,20 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     SA_CUDA(cudaMemsetAsync(ws.seg_count.p + 2 * (size_t)n, 0, 8, st));
     cub_excl_sum(ws, ws.seg_count.p, ws.seg_off.p, 2 * (uint64_t)n + 1, st);
     launches++;
-    ws.seg_list.reserve(2 * (size_t)n + 2);
+    // seg_list: short list [0, 2n), long list [2n, 4n), counts at 4n
+    ws.seg_list.reserve(4 * (size_t)n + 4);
     ws.sort_begin.reserve(2 * (size_t)n);
     ws.sort_end.reserve(2 * (size_t)n);
-    SA_CUDA(cudaMemsetAsync(ws.seg_list.p + 2 * (size_t)n, 0, 8, st));
+    uint32_t* const long_list = ws.seg_list.p + 2 * (size_t)n;
+    uint32_t* const list_counts = ws.seg_list.p + 4 * (size_t)n;
+    SA_CUDA(cudaMemsetAsync(list_counts, 0, 12, st));
     k_seg_list<<<warps_grid((2 * (uint64_t)n + 31) / 32), 32 * WARPS_PER_BLOCK, 0, st>>>(
-        ws.seg_count.p, ws.seg_off.p, 2 * n, ws.seg_list.p, ws.seg_list.p + 2 * (size_t)n, ws.sort_begin.p,
-        ws.sort_end.p);
+        ws.seg_count.p, ws.seg_off.p, 2 * n, ws.seg_list.p, long_list, list_counts, ws.sort_begin.p, ws.sort_end.p);
     launches++;
     uint64_t total_anchors = 0;
-    uint32_t n_list[2] = {0, 0};
+    uint32_t n_list[3] = {0, 0, 0};
     SA_CUDA(cudaMemcpyAsync(&total_anchors, ws.seg_off.p + 2 * (size_t)n, 8, cudaMemcpyDeviceToHost, st));
-    SA_CUDA(cudaMemcpyAsync(n_list, ws.seg_list.p + 2 * (size_t)n, 8, cudaMemcpyDeviceToHost, st));
+    SA_CUDA(cudaMemcpyAsync(n_list, list_counts, 12, cudaMemcpyDeviceToHost, st));
     SA_CUDA(cudaStreamSynchronize(st));
     ws.anchors.reserve(total_anchors);
     ws.anchors_sorted.reserve(total_anchors);
@@ -1558,15 +1573,15 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
         ws.anc_start.reserve(total_anchors + 1);
     }
     if (cfg.cp.max_lookback < 64)
-        k_chain4<true><<<warps_grid(((uint64_t)n_list[0] + 3) / 4), 32 * WARPS_PER_BLOCK, 0, st>>>(
+        k_chain4<true><<<warps_grid((uint64_t)n_list[2] + ((uint64_t)n_list[0] + 3) / 4), 32 * WARPS_PER_BLOCK, 0, st>>>(
             ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p,
             total_anchors, ap, cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
-            cfg.nam_anchors ? ws.anc_start.p : nullptr, ws.seg_list.p, n_list[0]);
+            cfg.nam_anchors ? ws.anc_start.p : nullptr, ws.seg_list.p, n_list[0], long_list, n_list[2]);
     else
-        k_chain4<false><<<warps_grid(((uint64_t)n_list[0] + 3) / 4), 32 * WARPS_PER_BLOCK, 0, st>>>(
+        k_chain4<false><<<warps_grid((uint64_t)n_list[2] + ((uint64_t)n_list[0] + 3) / 4), 32 * WARPS_PER_BLOCK, 0, st>>>(
             ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p,
             total_anchors, ap, cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
-            cfg.nam_anchors ? ws.anc_start.p : nullptr, ws.seg_list.p, n_list[0]);
+            cfg.nam_anchors ? ws.anc_start.p : nullptr, ws.seg_list.p, n_list[0], long_list, n_list[2]);
     kt->end(st);
     launches++;
     ws.nam_count.reserve((size_t)n + 1);
