@@ -491,8 +491,13 @@ void Mapper::map_uploaded(sa_output* out) {
     const size_t nchunks = chunks.size();
     n_parts_ = std::max<size_t>(1, std::min<size_t>(parts_target_, nchunks / 4));
     while (parts_.size() < n_parts_) parts_.push_back(std::make_unique<Part>());
+    // the first part is half the size of the others, so that the policy threads and the
+    // first extension wave start sooner
+    const size_t first = n_parts_ > 1 ? std::max<size_t>(1, nchunks / (2 * n_parts_ - 1)) : nchunks;
     for (size_t pi = 0, c0 = 0; pi < n_parts_; pi++) {
-        const size_t c1 = pi + 1 == n_parts_ ? nchunks : nchunks * (pi + 1) / n_parts_;
+        const size_t c1 = pi + 1 == n_parts_ ? nchunks
+                          : pi == 0       ? first
+                                          : first + (nchunks - first) * pi / (n_parts_ - 1);
         Part& p = *parts_[pi];
         p.chunk_lo = c0;
         p.chunk_hi = c1;
