@@ -180,17 +180,28 @@ inline void parallel_memcpy(void* dst, const void* src, size_t bytes, unsigned t
     for (auto& x : th) x.join();
 }
 
-// One copy of every chunk's output pieces into dst with up to `threads` threads,
-// each copying a run of consecutive pieces of about equal total size.
+// A chunk's output pieces, in order, into dst (one thread).
 template <class Chunk>
-inline void gather_chunk_outputs(const std::vector<Chunk>& chunks, char* dst, unsigned threads) {
+inline void copy_chunk_output(const Chunk& c, char* dst) {
+    for (const auto& p : c.pieces) {
+        std::memcpy(dst, (p.spec ? c.spec_out.data() : c.out.data()) + p.off, p.len);
+        dst += p.len;
+    }
+}
+
+// One copy of the output pieces of chunks [chunk0, end) into dst with up to `threads`
+// threads, each copying a run of consecutive pieces of about equal total size.
+template <class Chunk>
+inline void gather_chunk_outputs(const std::vector<Chunk>& chunks, char* dst, unsigned threads, size_t chunk0 = 0) {
     struct Seg {
         const char* src;
         size_t len;
     };
     std::vector<Seg> segs;
-    for (const auto& c : chunks)
+    for (size_t ci = chunk0; ci < chunks.size(); ci++) {
+        const auto& c = chunks[ci];
         for (const auto& p : c.pieces) segs.push_back(Seg{(p.spec ? c.spec_out.data() : c.out.data()) + p.off, p.len});
+    }
     std::vector<size_t> start(segs.size() + 1, 0);
     for (size_t i = 0; i < segs.size(); i++) start[i + 1] = start[i] + segs[i].len;
     const size_t total = start.back();

@@ -292,9 +292,19 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, uint32_t& launches, u
         // one policy per thread, bound to each chunk's part in turn
         Policy policy(pcfg_, contigs_, parts_[0]->bv, parts_[0]->store);
         std::unique_lock<std::mutex> lk(mu);
+        auto copy_ready = [&] { return so_.dst && !so_.overflow && so_.next_claim < so_.done_prefix; };
         for (;;) {
-            cv_work.wait(lk, [&] { return stop || !ready.empty(); });
+            cv_work.wait(lk, [&] { return stop || !ready.empty() || copy_ready(); });
             if (stop) return;
+            if (ready.empty()) {
+                // nothing to map: copy the next finished chunk's output into place
+                const size_t cc = so_.next_claim++;
+                char* d = so_.dst + so_.off[cc];
+                lk.unlock();
+                copy_chunk_output(chunks[cc], d);
+                lk.lock();
+                continue;
+            }
             const size_t c = ready.front();
             ready.pop_front();
             running++;
@@ -321,6 +331,16 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, uint32_t& launches, u
             running--;
             if (!first && cs.done) {
                 n_done++;
+                if (so_.dst) {
+                    so_.done[c] = 1;
+                    while (so_.done_prefix < nchunks && so_.done[so_.done_prefix]) {
+                        const size_t d = so_.done_prefix;
+                        so_.off[d + 1] = so_.off[d] + chunks[d].out_bytes;
+                        if (so_.off[d + 1] > so_.cap) so_.overflow = true;
+                        so_.done_prefix++;
+                    }
+                    if (copy_ready()) cv_work.notify_one();
+                }
             } else if (cs.pending.empty()) {
                 // nothing requested: a seeded chunk runs at once; a stalled one is a bug
                 if (!first) {
@@ -518,9 +538,25 @@ void Mapper::map_uploaded(sa_output* out) {
         }
         c0 = c1;
     }
+    // output buffer sized from the previous batch (large batches only)
+    so_ = StreamOut();
+    const size_t est = (size_t)(bytes_per_record_ * 1.15 * (double)nrec) + ((size_t)1 << 20);
+    if (bytes_per_record_ > 0 && est >= OutputPool::LARGE) {
+        so_.cap = (est + OutputPool::LARGE - 1) / OutputPool::LARGE * OutputPool::LARGE;
+        so_.dst = alloc_output(so_.cap + 1);
+        so_.off.assign(chunks.size() + 1, 0);
+        so_.done.assign(chunks.size(), 0);
+    }
     uint32_t nam_launches = 0;
     const auto t_sched = std::chrono::steady_clock::now();
-    const uint32_t waves = schedule(chunks, launches, nam_launches);
+    uint32_t waves = 0;
+    try {
+        waves = schedule(chunks, launches, nam_launches);
+    } catch (...) {
+        if (so_.dst) release_output(so_.dst);
+        so_ = StreamOut();
+        throw;
+    }
     const auto t_sched_end = std::chrono::steady_clock::now();
     launches += nam_launches;
     double t_nams = 0;
@@ -557,9 +593,19 @@ void Mapper::map_uploaded(sa_output* out) {
         total_len += c.out_bytes;
         mapped += c.mapped;
     }
-    out->data = alloc_output(total_len + 1);
-    if (!out->data) throw Error(SA_ERR_OOM, "output allocation failed");
-    gather_chunk_outputs(chunks, out->data, policy_threads_);
+    if (so_.dst && !so_.overflow && total_len <= so_.cap) {
+        // the chunks copied while mapping are in place; gather the rest behind them
+        out->data = so_.dst;
+        const size_t c0 = so_.next_claim;
+        gather_chunk_outputs(chunks, so_.dst + so_.off[c0], policy_threads_, c0);
+    } else {
+        if (so_.dst) release_output(so_.dst);
+        out->data = alloc_output(total_len + 1);
+        if (!out->data) throw Error(SA_ERR_OOM, "output allocation failed");
+        gather_chunk_outputs(chunks, out->data, policy_threads_);
+    }
+    so_ = StreamOut();
+    if (nrec) bytes_per_record_ = (double)total_len / (double)nrec;
     // keep the chunks' buffers (emptied) for the next batch
     if (chunk_pool_.size() < chunks.size()) chunk_pool_.resize(chunks.size());
     for (size_t c = 0; c < chunks.size(); c++) {

@@ -114,6 +114,20 @@ class Mapper {
         std::vector<ChunkState::Piece> pieces;
     };
     std::vector<ChunkBuffers> chunk_pool_;
+    // Output copied while the batch is mapped: idle policy threads copy each chunk whose
+    // predecessors are all done into `dst` (sized from the previous batch's bytes per
+    // record); the rest is gathered at the end.  Without room it falls back to one
+    // gather into an exact buffer.
+    struct StreamOut {
+        char* dst = nullptr;
+        size_t cap = 0;
+        bool overflow = false;
+        std::vector<size_t> off;       // chunk c's output offset, for c <= done_prefix
+        std::vector<char> done;        // chunk finished (set under the schedule lock)
+        size_t done_prefix = 0;        // chunks [0, done_prefix) are all done
+        size_t next_claim = 0;         // chunks [0, next_claim) copied or being copied
+    } so_;
+    double bytes_per_record_ = 0;  // previous batch, for the output estimate
     uint32_t n_reads_ = 0;
     uint64_t total_bases_ = 0;
     std::atomic<uint64_t> h2d_bytes_{0}, d2h_bytes_{0};
