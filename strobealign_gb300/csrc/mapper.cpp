@@ -492,14 +492,7 @@ void Mapper::map_uploaded(sa_output* out) {
         cs.end = j;
         // buffers of an earlier batch's chunk: their memory is paged in already
         const size_t c = chunks.size();
-        if (c < chunk_pool_.size()) {
-            ChunkBuffers& b = chunk_pool_[c];
-            std::swap(cs.out, b.out);
-            std::swap(cs.spec_out, b.spec_out);
-            std::swap(cs.effects, b.effects);
-            std::swap(cs.entries, b.entries);
-            std::swap(cs.pieces, b.pieces);
-        }
+        if (c < chunk_pool_.size()) chunk_pool_[c].lend(cs);
         cs.keep_buffers = true;
         chunks.push_back(std::move(cs));
         i = j;
@@ -608,20 +601,7 @@ void Mapper::map_uploaded(sa_output* out) {
     if (nrec) bytes_per_record_ = (double)total_len / (double)nrec;
     // keep the chunks' buffers (emptied) for the next batch
     if (chunk_pool_.size() < chunks.size()) chunk_pool_.resize(chunks.size());
-    for (size_t c = 0; c < chunks.size(); c++) {
-        ChunkBuffers& b = chunk_pool_[c];
-        ChunkState& cs = chunks[c];
-        cs.out.clear();
-        cs.spec_out.clear();
-        cs.effects.clear();
-        cs.entries.clear();
-        cs.pieces.clear();
-        std::swap(cs.out, b.out);
-        std::swap(cs.spec_out, b.spec_out);
-        std::swap(cs.effects, b.effects);
-        std::swap(cs.entries, b.entries);
-        std::swap(cs.pieces, b.pieces);
-    }
+    for (size_t c = 0; c < chunks.size(); c++) chunk_pool_[c].reclaim(chunks[c]);
     if (trace_) {
         auto d = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
             return std::chrono::duration<double>(b - a).count();

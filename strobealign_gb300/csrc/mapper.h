@@ -106,14 +106,7 @@ class Mapper {
     std::chrono::steady_clock::time_point t_map0_;  // start of the current map (trace times)
     PodArray<uint32_t> wave_anchors_;  // a wave's piecewise anchors (query, reference start pairs)
     WavePool wave_pool_;
-    // output and bookkeeping buffers of the last batch's chunks, reused by the next
-    struct ChunkBuffers {
-        OutBuf out, spec_out;
-        std::vector<ChunkState::Effect> effects;
-        std::vector<ResultStore::Entry> entries;
-        std::vector<ChunkState::Piece> pieces;
-    };
-    std::vector<ChunkBuffers> chunk_pool_;
+    std::vector<ChunkBuffers> chunk_pool_;  // the last batch's chunk buffers, lent to the next
     // Output copied while the batch is mapped: idle policy threads copy each chunk whose
     // predecessors are all done into `dst` (sized from the previous batch's bytes per
     // record); the rest is gathered at the end.  Without room it falls back to one

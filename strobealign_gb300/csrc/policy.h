@@ -224,6 +224,36 @@ struct ChunkState {
     uint64_t evals_real = 0, evals_spec = 0, runs = 0;
 };
 
+// Output and bookkeeping buffers of a finished chunk, kept for a later chunk (their
+// memory is paged in already): lend() moves them into a new chunk, reclaim() takes
+// them back, emptied, when a chunk's output has been gathered.
+struct ChunkBuffers {
+    OutBuf out, spec_out;
+    std::vector<ChunkState::Effect> effects;
+    std::vector<ResultStore::Entry> entries;
+    std::vector<ChunkState::Piece> pieces;
+    void lend(ChunkState& cs) {
+        std::swap(cs.out, out);
+        std::swap(cs.spec_out, spec_out);
+        std::swap(cs.effects, effects);
+        std::swap(cs.entries, entries);
+        std::swap(cs.pieces, pieces);
+        cs.keep_buffers = true;
+    }
+    void reclaim(ChunkState& cs) {
+        cs.out.clear();
+        cs.spec_out.clear();
+        cs.effects.clear();
+        cs.entries.clear();
+        cs.pieces.clear();
+        std::swap(cs.out, out);
+        std::swap(cs.spec_out, spec_out);
+        std::swap(cs.effects, effects);
+        std::swap(cs.entries, entries);
+        std::swap(cs.pieces, pieces);
+    }
+};
+
 class Policy {
   public:
     Policy(const PolicyConfig& cfg, const std::vector<ContigInfo>& contigs, const BatchView& bv, ResultStore& store);

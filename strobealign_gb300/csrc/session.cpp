@@ -533,7 +533,7 @@ void Session::admit_group(const std::vector<Request*>& group, AdmitLane& lane) {
         }
         i0 += rn;
         if (rn == 0) continue;
-        // chunks (src/main.rs:591-604)
+        // chunks (src/main.rs:591-604), with buffers of finished requests' chunks
         for (uint64_t i = 0; i < r.nrec;) {
             uint64_t nt = 0, j = i;
             while (j < r.nrec) {
@@ -544,6 +544,14 @@ void Session::admit_group(const std::vector<Request*>& group, AdmitLane& lane) {
             ChunkState cs;
             cs.first = cs.next = i;
             cs.end = j;
+            {
+                std::lock_guard<std::mutex> g(chunk_pool_mu_);
+                if (!chunk_pool_.empty()) {
+                    chunk_pool_.back().lend(cs);
+                    chunk_pool_.pop_back();
+                }
+            }
+            cs.keep_buffers = true;
             r.chunks.push_back(std::move(cs));
             i = j;
         }
@@ -705,7 +713,15 @@ void Session::complete(Request& r) {
         for (auto& c : r.chunks)
             for (auto& a : c.abundance) r.abundance[a.first] += a.second;
     }
-    // release what the finished request no longer needs
+    // release what the finished request no longer needs; its chunk buffers go to the pool
+    {
+        std::lock_guard<std::mutex> g(chunk_pool_mu_);
+        for (auto& c : r.chunks) {
+            if (chunk_pool_.size() >= 384) break;  // bounds the pooled memory (a few MB per chunk)
+            chunk_pool_.emplace_back();
+            chunk_pool_.back().reclaim(c);
+        }
+    }
     r.chunks.clear();
     r.chunks.shrink_to_fit();
     r.store = ResultStore();

@@ -143,6 +143,9 @@ class Session {
     PinnedBuf<ExtJob> h_jobs_;
     PodArray<uint32_t> wave_anchors_;  // a wave's piecewise anchors (query, reference start pairs)
     WavePool wave_pool_;
+    // buffers of finished requests' chunks, lent to the chunks of new requests
+    std::mutex chunk_pool_mu_;
+    std::vector<ChunkBuffers> chunk_pool_;
     // read arena
     DevBuf<uint8_t> arena_seq_;
     DevBuf<uint64_t> arena_off_;
