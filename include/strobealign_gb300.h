@@ -297,6 +297,11 @@ typedef struct {
     uint32_t max_inflight_requests; /* 0 = no limit */
     uint32_t policy_threads;        /* host threads for the mapping policy; 0 = all */
     uint32_t admission_streams;     /* requests whose NAM pipelines run at once; 0 = 2 */
+    uint32_t borrow_inputs;         /* 1: sa_session_submit keeps pointers to the batch's
+                                       sequences, qualities, names and comments instead of
+                                       copying them; the caller keeps them unchanged until
+                                       sa_session_wait returns for that request. 0 (default):
+                                       copied, the caller may free them after submit. */
 } sa_session_params;
 typedef struct {
     double seconds_queued;  /* submit -> admitted */
@@ -309,8 +314,8 @@ typedef struct {
 void sa_session_params_default(sa_session_params* p);
 int32_t sa_session_create(const sa_index* idx, const sa_refs* refs, const sa_chaining_params* cp,
                           const sa_mapping_params* mp, const sa_session_params* sp, sa_session** out);
-/* Copies the batch and queues it; r2 = NULL for single-end.  SA_ERR_INVALID if the
- * request can never fit in the arena. */
+/* Copies the batch (or, with borrow_inputs, refers to it) and queues it; r2 = NULL for
+ * single-end.  SA_ERR_INVALID if the request can never fit in the arena. */
 int32_t sa_session_submit(sa_session* s, const sa_read_batch* r1, const sa_read_batch* r2, uint64_t* ticket);
 /* *done = 1 once the request's output is ready. */
 int32_t sa_session_poll(sa_session* s, uint64_t ticket, int32_t* done);

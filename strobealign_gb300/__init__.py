@@ -422,8 +422,12 @@ class Session:
 
     def __init__(self, index: StrobemerIndex, refs: References, chaining: L.ChainingParams | None = None,
                  mapping: L.MappingParams | None = None, max_inflight_bases: int = 0, max_inflight_requests: int = 0,
-                 policy_threads: int = 0, admission_streams: int = 0, **kw):
+                 policy_threads: int = 0, admission_streams: int = 0, borrow_inputs: bool = False, **kw):
         self.index, self.refs = index, refs
+        # borrow_inputs: the session reads the submitted Reads in place; they are kept
+        # referenced here until wait() returns for their ticket
+        self.borrow = bool(borrow_inputs)
+        self._borrowed: dict[int, tuple] = {}
         self.cp = chaining or chaining_defaults()
         self.mp = mapping or mapping_defaults(**kw)
         sp = L.SessionParams()
@@ -434,6 +438,7 @@ class Session:
         sp.policy_threads = policy_threads
         if admission_streams:
             sp.admission_streams = admission_streams
+        sp.borrow_inputs = 1 if self.borrow else 0
         h = C.c_void_p()
         L.check(lib().sa_session_create(index.h, refs.h, C.byref(self.cp), C.byref(self.mp), C.byref(sp),
                                         C.byref(h)))
@@ -444,6 +449,8 @@ class Session:
         b2 = r2.c() if r2 is not None else None
         t = C.c_uint64()
         L.check(lib().sa_session_submit(self.h, C.byref(b1), C.byref(b2) if b2 is not None else None, C.byref(t)))
+        if self.borrow:
+            self._borrowed[t.value] = (r1, r2, b1, b2)
         return t.value
 
     def poll(self, ticket: int) -> bool:
@@ -458,6 +465,7 @@ class Session:
         ab = np.zeros(len(self.refs), dtype=np.float64) if abundances else None
         L.check(lib().sa_session_wait(self.h, ticket, timeout_ms, C.byref(o), C.byref(st),
                                       _p(ab, C.c_double) if ab is not None else None, len(ab) if ab is not None else 0))
+        self._borrowed.pop(ticket, None)
         try:
             data = (C.string_at(o.data, o.len) if o.len else b"") if copy else o.len
         finally:

@@ -74,7 +74,7 @@ class Output(C.Structure):
 
 class SessionParams(C.Structure):
     _fields_ = [("max_inflight_bases", u64), ("max_inflight_requests", u32), ("policy_threads", u32),
-                ("admission_streams", u32)]
+                ("admission_streams", u32), ("borrow_inputs", u32)]
 
 
 class RequestStats(C.Structure):

@@ -634,6 +634,7 @@ void sa_session_params_default(sa_session_params* p) {
     p->max_inflight_requests = 0;
     p->policy_threads = 0;
     p->admission_streams = 2;
+    p->borrow_inputs = 0;
 }
 
 int32_t sa_session_create(const sa_index* idx, const sa_refs* refs, const sa_chaining_params* cp,
@@ -654,6 +655,7 @@ int32_t sa_session_create(const sa_index* idx, const sa_refs* refs, const sa_cha
         sc.max_inflight_requests = sp->max_inflight_requests;
         sc.policy_threads = sp->policy_threads;
         sc.admission_streams = sp->admission_streams ? sp->admission_streams : 2;
+        sc.borrow_inputs = sp->borrow_inputs != 0;
     }
     auto* s = new sa_session{nullptr};
     try {

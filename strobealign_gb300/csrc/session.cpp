@@ -180,10 +180,13 @@ uint64_t Session::submit(const sa_read_batch* r1, const sa_read_batch* r2) {
         if (b->comments && b->comment_offsets)
             com_total += n ? b->comment_offsets[n] - b->comment_offsets[0] : 0;
     }
-    r->qual.resize(qual_total);
-    r->names.resize(name_total);
-    r->comments.resize(com_total);
-    for (int m = 0; m < nm; m++) {
+    const bool borrow = cfg_.borrow_inputs;
+    if (!borrow) {
+        r->qual.resize(qual_total);
+        r->names.resize(name_total);
+        r->comments.resize(com_total);
+    }
+    for (int m = 0; m < nm && !borrow; m++) {
         const sa_read_batch* b = mates[m];
         const uint64_t n = b->n;
         if (!n) continue;
@@ -196,7 +199,7 @@ uint64_t Session::submit(const sa_read_batch* r1, const sa_read_batch* r2) {
             std::memcpy(r->comments.data() + com_base[m], b->comments + b->comment_offsets[0],
                         b->comment_offsets[n] - b->comment_offsets[0]);
     }
-    r->seq.resize(seq_total);
+    if (!borrow) r->seq.resize(seq_total);
     r->seq_off.resize(r->n_reads + 1);
     r->read_views.resize(r->n_reads);
     r->bv.paired = paired;
@@ -221,19 +224,28 @@ uint64_t Session::submit(const sa_read_batch* r1, const sa_read_batch* r2) {
                 const uint64_t s0 = b->seq_offsets[i], s1 = b->seq_offsets[i + 1];
                 const uint64_t d = paired ? 2 * i + m : i;
                 const uint64_t at = r->seq_off[d];
-                std::memcpy(r->seq.data() + at, b->seq + s0, s1 - s0);
                 ReadView& v = r->read_views[d];
-                v.seq = r->seq.data() + at;
-                v.len = (uint32_t)(s1 - s0);
-                v.qual = r->has_qual ? r->qual.data() + qual_base[m] + (s0 - b->seq_offsets[0]) : nullptr;
                 const uint64_t n0 = b->name_offsets[i], n1 = b->name_offsets[i + 1];
-                v.name = r->names.data() + name_base[m] + (n0 - b->name_offsets[0]);
+                v.len = (uint32_t)(s1 - s0);
                 v.name_len = (uint32_t)(n1 - n0);
                 v.comment = nullptr;
                 v.comment_len = 0;
-                if (b->comments && b->comment_offsets) {
-                    const uint64_t c0 = b->comment_offsets[i], c1 = b->comment_offsets[i + 1];
-                    if (c1 > c0) {
+                const bool com = b->comments && b->comment_offsets && b->comment_offsets[i + 1] > b->comment_offsets[i];
+                if (borrow) {
+                    v.seq = b->seq + s0;
+                    v.qual = r->has_qual ? b->qual + s0 : nullptr;
+                    v.name = b->names + n0;
+                    if (com) {
+                        v.comment = b->comments + b->comment_offsets[i];
+                        v.comment_len = (uint32_t)(b->comment_offsets[i + 1] - b->comment_offsets[i]);
+                    }
+                } else {
+                    std::memcpy(r->seq.data() + at, b->seq + s0, s1 - s0);
+                    v.seq = r->seq.data() + at;
+                    v.qual = r->has_qual ? r->qual.data() + qual_base[m] + (s0 - b->seq_offsets[0]) : nullptr;
+                    v.name = r->names.data() + name_base[m] + (n0 - b->name_offsets[0]);
+                    if (com) {
+                        const uint64_t c0 = b->comment_offsets[i], c1 = b->comment_offsets[i + 1];
                         v.comment = r->comments.data() + com_base[m] + (c0 - b->comment_offsets[0]);
                         v.comment_len = (uint32_t)(c1 - c0);
                     }
@@ -438,7 +450,16 @@ void Session::admit_group(const std::vector<Request*>& group, AdmitLane& lane) {
         lane.nws.off.reserve((size_t)n + 1);
         uint64_t b0 = 0, i0 = 0;
         for (const Request* r : group) {
-            std::memcpy(lane.h_seq.p + b0, r->seq.data(), r->total_bases);
+            if (!r->seq.size() && r->total_bases) {
+                // borrowed batch: the bases from the caller's records, in device read order
+                char* dst = (char*)lane.h_seq.p + b0;
+                parallel_ranges(r->n_reads, 4, [&](uint64_t a, uint64_t e) {
+                    for (uint64_t i = a; i < e; i++)
+                        std::memcpy(dst + r->seq_off[i], r->read_views[i].seq, r->read_views[i].len);
+                });
+            } else {
+                std::memcpy(lane.h_seq.p + b0, r->seq.data(), r->total_bases);
+            }
             for (uint64_t i = 0; i < r->n_reads; i++) lane.h_off.p[i0 + i] = b0 + r->seq_off[i];
             b0 += r->total_bases;
             i0 += r->n_reads;

@@ -43,7 +43,7 @@ class RangeAllocator {
 struct Request {
     uint64_t id = 0;
     bool paired = false;
-    // owned copies of the records
+    // owned copies of the records (empty when the session borrows the caller's batch)
     RawBytes seq, qual, names, comments;
     // sequences in device read order (mates interleaved) with per-read offsets;
     // qualities, names and comments one block per mate (read views point into them)
@@ -84,6 +84,7 @@ struct SessionConfig {
     uint32_t max_inflight_requests = 0;  // 0 = no limit
     uint32_t policy_threads = 0;         // 0 = all host threads
     uint32_t admission_streams = 2;      // requests admitted concurrently (NAM pipelines in flight)
+    bool borrow_inputs = false;          // read views point into the caller's batch (no copies)
 };
 
 // One admission lane: a thread with its own stream, NAM workspace and staging, so that

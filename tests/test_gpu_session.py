@@ -73,7 +73,8 @@ def test_session_admission_limits(setup):
     want = _alone(sa, refs, idx, reqs, use_ssw=1)
     # an arena of 4 Mbases admits only a few requests at a time; one request in flight at most
     for kw in (dict(max_inflight_bases=4_000_000), dict(max_inflight_requests=1, policy_threads=3),
-               dict(admission_streams=1), dict(admission_streams=4, max_inflight_bases=8_000_000)):
+               dict(admission_streams=1), dict(admission_streams=4, max_inflight_bases=8_000_000),
+               dict(borrow_inputs=True), dict(borrow_inputs=True, max_inflight_bases=4_000_000)):
         s = sa.Session(idx, refs, use_ssw=1, **kw)
         tickets = [s.submit(x, y) for x, y in reqs]
         for i, t in enumerate(tickets):
@@ -127,9 +128,9 @@ def test_session_comments_and_missing_qualities(setup):
     comments = [f"BX:Z:{i % 7}" if i % 3 else "" for i in range(n)]
     a1 = sa.Reads.from_lists(names, seqs1, comments=comments)
     a2 = sa.Reads.from_lists(names, seqs2, comments=comments)
-    for kw in (dict(fastq_comments=1), dict()):
+    for kw, skw in ((dict(fastq_comments=1), {}), (dict(), {}), (dict(fastq_comments=1), dict(borrow_inputs=True))):
         want = sa.Mapper(idx, refs, **kw).map(a1, a2)
-        s = sa.Session(idx, refs, **kw)
+        s = sa.Session(idx, refs, **skw, **kw)
         t = [s.submit(a1, a2), s.submit(a1, None)]
         got = [s.wait(x)[0] for x in t]
         assert got[0] == want
