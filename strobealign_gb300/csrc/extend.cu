@@ -992,7 +992,7 @@ __device__ __noinline__ EndPos ssw_warp_pass(const uint8_t* q, int qlen, bool q_
 template <int RMAX>
 __global__ void __launch_bounds__(128, RMAX <= 4 ? 5 : 1) k_ssw(SswTask* tasks, const uint32_t* order, uint32_t n_tasks,
                                              const PrepRec* prep, const uint8_t* arena, AlignScores sc, int bias,
-                                             uint32_t* counters) {
+                                             uint32_t* counters, uint32_t* queue, uint32_t qmin) {
     constexpr int RW = (RMAX + 3) / 4;
     extern __shared__ __align__(16) uint32_t ssw_smem[];
     const int lane = threadIdx.x & 31;
@@ -1000,12 +1000,13 @@ __global__ void __launch_bounds__(128, RMAX <= 4 ? 5 : 1) k_ssw(SswTask* tasks, 
     unsigned long long* cells = reinterpret_cast<unsigned long long*>(counters + 8);
     for (;;) {
         uint32_t li = 0;
-        if (lane == 0) li = atomicAdd(&counters[5], 1u);
+        if (lane == 0) li = atomicAdd(queue, 1u);
         li = __shfl_sync(FULLM, li, 0);
         if (li >= n_tasks) break;
         const uint32_t ti = order ? order[li] : li;
         SswTask tk = tasks[ti];
         const PrepRec p = prep[tk.job];
+        if (p.qlen <= qmin) continue;  // k_ssw_wave's task
         const uint8_t* q = arena + p.arena_off;
         const uint8_t* r = q + p.qlen;
         // forward: byte, word on overflow (ext/ssw/ssw.c:840-862)
@@ -1264,7 +1265,7 @@ __device__ __forceinline__ EndPos wave_pass(bool run, const uint8_t* q, int qlen
 template <int NMAX>
 __global__ void __launch_bounds__(128, 4) k_ssw_wave(SswTask* tasks, const uint32_t* order, uint32_t n_tasks,
                                                       const PrepRec* prep, const uint8_t* arena, AlignScores sc,
-                                                      int bias, uint32_t* counters) {
+                                                      int bias, uint32_t* counters, uint32_t qmax) {
     constexpr int NW = (NMAX + 7) / 8;
     extern __shared__ __align__(16) uint4 wv_smem[];
     const int lane = threadIdx.x & 31, gi = lane / WV_T, gl = lane % WV_T;
@@ -1278,8 +1279,12 @@ __global__ void __launch_bounds__(128, 4) k_ssw_wave(SswTask* tasks, const uint3
         base = __shfl_sync(FULLM, base, 0);
         if (base >= n_tasks) break;
         const uint32_t li = base + gi;
-        const bool have = li < n_tasks;
-        const uint32_t ti = have ? (order ? order[li] : li) : 0;
+        uint32_t ti = 0;
+        bool have = li < n_tasks;
+        if (have) {
+            ti = order ? order[li] : li;
+            have = prep[tasks[ti].job].qlen <= qmax;  // longer reads: k_ssw's task
+        }
         int qlen = 0, wlen = 0;
         const uint8_t* q = arena;
         if (have) {
@@ -2666,18 +2671,25 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
             if (blocks > 152ULL * 16) blocks = 152ULL * 16;
 #define SA_SSW(RM)                                                                                              \
     k_ssw<RM><<<(unsigned)blocks, tpb, (size_t)wpb * 5 * 32 * ((RM + 3) / 4) * 4, st>>>(                       \
-        ws.tasks.p, ws.order.p, n_tasks, ws.prep.p, ws.arena.p, sc, bias, ws.counters.p)
-            if (max_qlen <= 8 * WAVE_NMAX) {
-                // eight threads per task (reads up to 192 nt)
+        ws.tasks.p, ws.order.p, n_tasks, ws.prep.p, ws.arena.p, sc, bias, ws.counters.p, ws.counters.p + 21, \
+        (uint32_t)(8 * WAVE_NMAX))
+            // tasks of reads up to 192 nt: eight threads per task; the longer ones of a batch
+            // of mixed lengths a warp per task, in a launch before
+            if (max_qlen > 8 * WAVE_NMAX) {
+                if (rmax == 4) SA_SSW(4);
+                else if (rmax == 8) SA_SSW(8);
+                else SA_SSW(16);
+                launches++;
+            }
+            {
                 const uint64_t per_block = (uint64_t)wpb * (32 / WV_T);  // tasks per block and round
                 uint64_t wblocks = ((uint64_t)n_tasks + per_block - 1) / per_block;
                 if (wblocks > 152ULL * 16) wblocks = 152ULL * 16;
                 const size_t smem = (size_t)wpb * 5 * ((WAVE_NMAX + 7) / 8) * 32 * sizeof(uint4);
-                k_ssw_wave<WAVE_NMAX><<<(unsigned)wblocks, tpb, smem, st>>>(ws.tasks.p, ws.order.p, n_tasks, ws.prep.p,
-                                                                           ws.arena.p, sc, bias, ws.counters.p);
-            } else if (rmax == 4) SA_SSW(4);
-            else if (rmax == 8) SA_SSW(8);
-            else SA_SSW(16);
+                k_ssw_wave<WAVE_NMAX><<<(unsigned)wblocks, tpb, smem, st>>>(
+                    ws.tasks.p, ws.order.p, n_tasks, ws.prep.p, ws.arena.p, sc, bias, ws.counters.p,
+                    (uint32_t)(8 * WAVE_NMAX));
+            }
 #undef SA_SSW
             kt->end(st);
             launches += 3;
