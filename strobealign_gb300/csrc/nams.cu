@@ -7,9 +7,10 @@
 //                   local rescue, orientation choice (src/hit.rs, src/chainer.rs:205-216)
 //   k_anchors       warp per read: anchor count, then fill (src/chainer.rs:304-384)
 //   segmented sort  (ref_id, ref_start, query_start) packed in a u64 key
-//   k_chain4        warp per four read-orientations: dedup, collinear chaining DP with
-//                   the reference's early-break rules evaluated as a prefix max over
-//                   the candidates (eight lanes per orientation), chain extraction
+//   k_chain4        warp per eight read orientations: anchor sort and dedup, collinear
+//                   chaining DP with the reference's early-break rules evaluated as a
+//                   prefix max over the candidates (four lanes per orientation), chain
+//                   extraction
 //                   (src/chainer.rs:85-180, 386-449)
 //   k_nam_compact   warp per read: NAM ids in push order, stable sort by score
 //                   (src/nam.rs:168-170); reads with more than 32 NAMs through a
@@ -945,25 +946,28 @@ __device__ __forceinline__ uint32_t warp_sort_dedup(uint64_t* keys, uint32_t cnt
     return n;
 }
 
-// Chaining (src/chainer.rs:128-176 and 386-449) for four read orientations per warp
-// (2 reads).  The deduplication and the extraction run over the whole warp, one
+// Chaining (src/chainer.rs:128-176 and 386-449) for NG = 8 read orientations per warp.
+// The anchor sort, the deduplication and the extraction run over the whole warp, one
 // orientation after the other.  The DP is serial over a read orientation's anchors;
 // the candidates j of anchor i (back to max_lookback) are scored in parallel and an
 // exclusive prefix max over them reproduces the reference's downward scan with its
 // ">=" updates and its stops (a different reference or a gap >= max_ref_gap ends the
 // scan; an update on the same diagonal ends it after that candidate).  The DP runs for
-// the four orientations at once, one group of eight lanes each, eight candidates at a
+// the NG orientations at once, one group of CG = 4 lanes each, four candidates at a
 // time (most anchors stop at the first candidate: the one before on the same
-// diagonal).  Warps whose orientations have more than CHAIN_GROUP_MAX anchors run the
-// DP with the whole warp per orientation, 32 candidates at a time.  The orientations
-// come from k_seg_list (those with anchors); nam_seg_count of the others is zeroed
-// before the launch.
+// diagonal).  Orientations with more than CHAIN_GROUP_MAX anchors get a warp each and
+// run the DP with all 32 lanes, 32 candidates at a time.  The orientations come from
+// k_seg_list (those with anchors); nam_seg_count of the others is zeroed before the
+// launch.
 //
 // RING: max_lookback < 64, so the predecessors of anchor i (and their scores) come
 // from a 64-entry ring in shared memory per orientation, written as anchors are
 // scored, instead of global memory (this takes the store-to-load round trip out of
 // each serial step).
-constexpr uint32_t CG = 8;  // lanes per orientation in the grouped DP
+constexpr uint32_t CG = 4;                   // lanes per orientation in the grouped DP
+constexpr uint32_t NG = 32 / CG;             // orientations per warp
+constexpr uint32_t GMASK = (1u << CG) - 1;  // one group's ballot bits
+constexpr uint32_t CHAIN_WARPS = 4;          // warps per block (shared rings: 28 KB per block)
 
 template <bool RING>
 __device__ __forceinline__ void chain_candidates(uint32_t j, bool in, const uint64_t* dedup, const float* dp,
@@ -996,15 +1000,15 @@ __device__ __forceinline__ void chain_candidates(uint32_t j, bool in, const uint
 }
 
 template <bool RING>
-__global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ off, uint32_t n, const uint64_t* seg_off,
+__global__ void __launch_bounds__(32 * CHAIN_WARPS, 8) k_chain4(const uint64_t* __restrict__ off, uint32_t n, const uint64_t* seg_off,
                                                 const uint64_t* sorted, uint64_t* dedup, float* dp, uint32_t* pred,
                                                 uint32_t* aux, uint64_t total_anchors, AnchorPack ap, ChainCtx cc,
                                                 NamRec* nam_out, uint32_t* nam_seg_count, uint64_t* anc_out,
                                                 uint64_t* anc_start, const uint32_t* seg_list, uint32_t n_list,
                                                 const uint32_t* long_list, uint32_t n_long) {
-    __shared__ uint32_t hist[WARPS_PER_BLOCK * 256];
-    __shared__ uint64_t ring_key_s[RING ? WARPS_PER_BLOCK * 4 * 64 : 1];
-    __shared__ float ring_dp_s[RING ? WARPS_PER_BLOCK * 4 * 64 : 1];
+    __shared__ uint32_t hist[CHAIN_WARPS * 256];
+    __shared__ uint64_t ring_key_s[RING ? CHAIN_WARPS * NG * 64 : 1];
+    __shared__ float ring_dp_s[RING ? CHAIN_WARPS * NG * 64 : 1];
     const uint32_t lane = lane_id(), g = lane / CG, gl = lane % CG, gsh = CG * g;
     const uint32_t wib = threadIdx.x / 32;
     const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
@@ -1012,28 +1016,24 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
     const float kf = __uint2float_rn(cc.k);
     constexpr uint32_t NONE = 0xffffffffu;
     // units: the long orientations first (one per warp, so they start first), then the
-    // short ones four at a time
-    const uint32_t n_units = n_long + (n_list + 3) / 4;
+    // short ones NG at a time.  Lane q holds the q-th orientation's segment, anchor count
+    // after dedup, first anchor and best score.
+    const uint32_t n_units = n_long + (n_list + NG - 1) / NG;
     for (uint32_t u = blockIdx.x * (blockDim.x / 32) + wib; u < n_units; u += nwarps) {
-        uint32_t sgq[4] = {NONE, NONE, NONE, NONE};
+        uint32_t my_sg = NONE;
         if (u < n_long) {
-            sgq[0] = long_list[u];
+            if (lane == 0) my_sg = long_list[u];
         } else {
-            const uint32_t l0 = 4 * (u - n_long);
-#pragma unroll
-            for (int q = 0; q < 4; q++) sgq[q] = l0 + q < n_list ? seg_list[l0 + q] : NONE;
+            const uint32_t l = NG * (u - n_long) + lane;
+            if (lane < NG && l < n_list) my_sg = seg_list[l];
         }
         // dedup (src/chainer.rs:228-229), one orientation after the other
-        uint32_t Nq[4];
-        uint64_t bq[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const uint32_t sg = sgq[q];
-            Nq[q] = 0;
-            bq[q] = 0;
+        uint32_t my_n = 0;
+        uint64_t my_b = 0;
+        for (uint32_t q = 0; q < NG; q++) {
+            const uint32_t sg = __shfl_sync(FULL, my_sg, q);
             if (sg == NONE) continue;
             const uint64_t b = seg_off[sg], e = seg_off[sg + 1];
-            bq[q] = b;
             uint32_t N = 0;
             const uint32_t cnt = (uint32_t)(e - b);
             if (cnt <= CHAIN_SORT_SMALL) {
@@ -1056,18 +1056,21 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
                     N += __popc(bal);
                 }
             }
-            Nq[q] = N;
+            if (lane == q) {
+                my_n = N;
+                my_b = b;
+            }
         }
         __syncwarp();
-        const uint32_t nmax = max(max(Nq[0], Nq[1]), max(Nq[2], Nq[3]));
-        float best_q[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        const uint32_t nmax = __reduce_max_sync(FULL, my_n);
+        float my_best = 0.0f;
         if (u >= n_long && nmax <= CHAIN_GROUP_MAX) {
             // grouped DP: group g scores the g-th orientation
-            const uint32_t sg = g == 0 ? sgq[0] : g == 1 ? sgq[1] : g == 2 ? sgq[2] : sgq[3];
-            const uint32_t N = g == 0 ? Nq[0] : g == 1 ? Nq[1] : g == 2 ? Nq[2] : Nq[3];
-            const uint64_t b = g == 0 ? bq[0] : g == 1 ? bq[1] : g == 2 ? bq[2] : bq[3];
-            uint64_t* ring_key = ring_key_s + (RING ? (wib * 4 + g) * 64 : 0);
-            float* ring_dp = ring_dp_s + (RING ? (wib * 4 + g) * 64 : 0);
+            const uint32_t sg = __shfl_sync(FULL, my_sg, g);
+            const uint32_t N = __shfl_sync(FULL, my_n, g);
+            const uint64_t b = __shfl_sync(FULL, my_b, g);
+            uint64_t* ring_key = ring_key_s + (RING ? (wib * NG + g) * 64 : 0);
+            float* ring_dp = ring_dp_s + (RING ? (wib * NG + g) * 64 : 0);
             const uint32_t read_len = sg != NONE ? (uint32_t)(off[(sg >> 1) + 1] - off[sg >> 1]) : 0;
             const uint32_t max_ref_gap = cc.cp.max_ref_gap ? cc.cp.max_ref_gap : read_len;
             float best_score = 0.0f;
@@ -1093,7 +1096,7 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
                     float val;
                     chain_candidates<RING>(j, in, dedup, dp, b, ring_key, ring_dp, ri, rsi, qi, max_ref_gap, cc, ap,
                                            hard, valid, diag, val);
-                    const uint32_t hb = (__ballot_sync(FULL, hard) >> gsh) & 0xffu;
+                    const uint32_t hb = (__ballot_sync(FULL, hard) >> gsh) & GMASK;
                     const uint32_t lim = hb ? (uint32_t)(__ffs(hb) - 1) : CG;  // lanes >= lim are not reached
                     if (gl >= lim) valid = false;
                     // exclusive prefix max of val over valid lanes in scan order
@@ -1105,15 +1108,15 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
                     float excl = __shfl_up_sync(FULL, incl, 1, CG);
                     if (gl == 0) excl = -INFINITY;
                     const bool upd = valid && val >= fmaxf(cur, excl);
-                    const uint32_t ub = (__ballot_sync(FULL, upd) >> gsh) & 0xffu;
-                    const uint32_t sb = (__ballot_sync(FULL, upd && diag) >> gsh) & 0xffu;
+                    const uint32_t ub = (__ballot_sync(FULL, upd) >> gsh) & GMASK;
+                    const uint32_t sb = (__ballot_sync(FULL, upd && diag) >> gsh) & GMASK;
                     uint32_t reach = lim;
                     bool stop = hb != 0;
                     if (sb) {
                         reach = (uint32_t)__ffs(sb);
                         stop = true;
                     }
-                    const uint32_t um = ub & (reach >= CG ? 0xffu : ((1u << reach) - 1));
+                    const uint32_t um = ub & (reach >= CG ? GMASK : ((1u << reach) - 1));
                     const uint32_t last = um ? 31 - __clz(um) : 0;
                     const float lv = __shfl_sync(FULL, val, last, CG);
                     if (more && um) {
@@ -1154,16 +1157,16 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
                 }
                 __syncwarp();
             }
-#pragma unroll
-            for (int q = 0; q < 4; q++) best_q[q] = __shfl_sync(FULL, best_score, q * CG);
+            const float bs = __shfl_sync(FULL, best_score, (lane % NG) * CG);
+            if (lane < NG) my_best = bs;
         } else {
             // the whole warp per orientation
-            uint64_t* ring_key = ring_key_s + (RING ? wib * 4 * 64 : 0);
-            float* ring_dp = ring_dp_s + (RING ? wib * 4 * 64 : 0);
-            for (int q = 0; q < 4; q++) {
-                const uint32_t sg = sgq[q], N = Nq[q];
+            uint64_t* ring_key = ring_key_s + (RING ? wib * NG * 64 : 0);
+            float* ring_dp = ring_dp_s + (RING ? wib * NG * 64 : 0);
+            for (uint32_t q = 0; q < NG; q++) {
+                const uint32_t sg = __shfl_sync(FULL, my_sg, q), N = __shfl_sync(FULL, my_n, q);
+                const uint64_t b = __shfl_sync(FULL, my_b, q);
                 if (sg == NONE || N == 0) continue;
-                const uint64_t b = bq[q];
                 const uint32_t read_len = (uint32_t)(off[(sg >> 1) + 1] - off[sg >> 1]);
                 const uint32_t max_ref_gap = cc.cp.max_ref_gap ? cc.cp.max_ref_gap : read_len;
                 float best_score = 0.0f;
@@ -1244,18 +1247,20 @@ __global__ void __launch_bounds__(256, 4) k_chain4(const uint64_t* __restrict__ 
                     }
                     __syncwarp();
                 }
-                best_q[q] = best_score;
+                if (lane == q) my_best = best_score;
             }
         }
         __syncwarp();
-        for (int q = 0; q < 4; q++) {
-            const uint32_t sg = sgq[q];
+        for (uint32_t q = 0; q < NG; q++) {
+            const uint32_t sg = __shfl_sync(FULL, my_sg, q), N = __shfl_sync(FULL, my_n, q);
+            const uint64_t b = __shfl_sync(FULL, my_b, q);
+            const float best = __shfl_sync(FULL, my_best, q);
             if (sg == NONE) continue;
-            if (Nq[q] == 0) {
+            if (N == 0) {
                 if (lane == 0) nam_seg_count[sg] = 0;
                 continue;
             }
-            chain_extract(dedup, dp, pred, aux, total_anchors, bq[q], Nq[q], sg, best_q[q], ap, cc, nam_out,
+            chain_extract(dedup, dp, pred, aux, total_anchors, b, N, sg, best, ap, cc, nam_out,
                           nam_seg_count, anc_out, anc_start, hist + wib * 256);
         }
     }
@@ -1568,17 +1573,20 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     }
     kt->begin(KS_CHAIN, st);
     SA_CUDA(cudaMemsetAsync(ws.nam_seg_count.p, 0, 2 * (size_t)n * sizeof(uint32_t), st));
+    const uint64_t chain_units = (uint64_t)n_list[2] + ((uint64_t)n_list[0] + NG - 1) / NG;
+    const unsigned chain_grid = (unsigned)std::max<uint64_t>(
+        1, std::min<uint64_t>((chain_units + CHAIN_WARPS - 1) / CHAIN_WARPS, 152ULL * 64));
     if (cfg.nam_anchors) {
         ws.anc_sparse.reserve(3 * total_anchors + 1);
         ws.anc_start.reserve(total_anchors + 1);
     }
     if (cfg.cp.max_lookback < 64)
-        k_chain4<true><<<warps_grid((uint64_t)n_list[2] + ((uint64_t)n_list[0] + 3) / 4), 32 * WARPS_PER_BLOCK, 0, st>>>(
+        k_chain4<true><<<chain_grid, 32 * CHAIN_WARPS, 0, st>>>(
             ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p,
             total_anchors, ap, cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
             cfg.nam_anchors ? ws.anc_start.p : nullptr, ws.seg_list.p, n_list[0], long_list, n_list[2]);
     else
-        k_chain4<false><<<warps_grid((uint64_t)n_list[2] + ((uint64_t)n_list[0] + 3) / 4), 32 * WARPS_PER_BLOCK, 0, st>>>(
+        k_chain4<false><<<chain_grid, 32 * CHAIN_WARPS, 0, st>>>(
             ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p,
             total_anchors, ap, cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
             cfg.nam_anchors ? ws.anc_start.p : nullptr, ws.seg_list.p, n_list[0], long_list, n_list[2]);
