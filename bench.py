@@ -1,21 +1,29 @@
 #!/usr/bin/env python3
-"""Aligned reads/s of strobealign's mapping path on GB300.
+"""Aligned reads/s of strobealign's mapping path on GB300, with bit-exact SAM.
 
-Default workload (--workload pe50m): 50 Mbp synthetic reference in 20 contigs (GC 41%,
-10% of it 2 kbp segmental copies at 2% divergence), 1M read pairs 2x150 bp, insert
-N(300, 30), 1% substitutions, 0.1% indels, 2% of pairs with one mate too mutated to
-seed (mate rescue).  Other shapes: se5m (5 Mbp, 100k single-end), uneven200m (200 Mbp
-with repeat families, 2M single-end reads of 50-500 bp), human (3.1 Gbp with 50%
-repeats; --pairs sets the pair count).  Seeded generators (strobealign_gb300.synthetic)
-stand in for the reference's read sets.
+Default workload (--workload human): a 3.1 Gbp synthetic genome in 24 contigs (GC 41%,
+50% interspersed repeats from 300 bp-6 kbp families at 10-20% divergence, 3% tandem
+repeats of period 2-50) and 10M read pairs of 2x150 bp, insert N(400, 50), 1%
+substitutions, 0.1% indels.  Other shapes: pe50m (50 Mbp, 10% segmental copies, 1M
+pairs with mate rescue), se5m (5 Mbp, 100k single-end 150 bp), uneven200m (200 Mbp,
+20% repeats, 2M single-end reads of 50-500 bp).  Seeded generators
+(strobealign_gb300.synthetic) stand in for the reference's read sets.
 
 One step maps the whole batch: NAM finding, SSW-exact (paired-end / --ssw) or piecewise
 (single-end) extension waves and SAM record formatting, chunked as the reference chunks
-its input.  `value` is the plain form with the reads already resident in device memory
-(sa_map_uploaded); `plain.e2e` maps from host buffers through sa_map_batch; `e2e` is the
-served form: the same reads as a stream of requests (log-uniform 1..100k pairs) through
-sa_session submit/wait from host buffers, with continuous batching.  An open-loop pass
-at 70% of the served capacity gives p50/p99 request latency.
+its input.
+  value   the batched engine (continuous batching, overlapped NAM parts) with the reads
+          resident in device memory (sa_map_uploaded)
+  e2e     the served form: the same reads as a stream of requests (log-uniform 1..100k
+          pairs) through sa_session submit/wait from host buffers
+  plain   the plain, stage-synchronous GPU form (sa_mapper_set_schedule overlap = 0)
+          from host buffers, beside the batched engine from host buffers
+An open-loop pass at 70% of the served capacity gives p50/p99 request latency.
+
+Parity leg (--parity full, the default): after the timed passes the batch is mapped once
+more and its SAM bytes are compared with the oracle's (the CPU restatement of the
+reference path) on the whole batch, and the GPU-built index with the oracle's; the
+oracle's run is also the CPU baseline (all host threads).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload W]
 
@@ -28,6 +36,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -43,30 +52,35 @@ METRIC = "aligned reads/s on 1 GB300 (bit-exact SAM), served vs plain; p50/p99 l
 # Synthetic stand-ins for the reference's benchmark shapes (seeded generators in
 # strobealign_gb300/synthetic.py; genome seeds 1..4, read seeds 101..104).
 WORKLOADS = {
+    "human": "human scale: 3.1 Gbp / 24 contigs (GC 41%, 50% interspersed repeats from 300 bp-6 kbp families at "
+             "10-20% divergence, 3% tandem repeats of period 2-50), 10M pairs 2x150 bp, insert N(400,50), 1% sub, "
+             "0.1% indel",
     "pe50m": "paired-end repetitive: 50 Mbp / 20 contigs (GC 41%, 10% 2 kbp segmental copies at 2%), "
              "1M pairs 2x150 bp, insert N(300,30), 1% sub, 0.1% indel, 2% of pairs need mate rescue",
     "se5m": "plain small: 5 Mbp uniform / 1 contig, 100k single-end 150 bp, 1% sub, 0.1% indel",
     "uneven200m": "uneven lengths: 200 Mbp / 8 contigs (GC 41%, 20% repeats from 300 bp-6 kbp families at "
                   "10-20% divergence), 2M single-end reads U[50,500] bp, 1.5% sub, 0.2% indel",
-    "human": "human scale: 3.1 Gbp / 24 contigs (GC 41%, 50% interspersed repeats, 3% tandem), "
-             "pairs 2x150 bp, insert N(400,50), 1% sub, 0.1% indel",
 }
-WORKLOAD = WORKLOADS["pe50m"]
+DEFAULT_WORKLOAD = "human"
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="pe50m", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload (1.0 = full)")
     ap.add_argument("--pairs", type=int, default=0, help="override the read (pair) count")
-    ap.add_argument("--cpu-sample-pairs", type=int, default=20000)
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ssw", action="store_true", help="single-end extension by SSW (--ssw) instead of piecewise")
+    ap.add_argument("--parity", default="full", choices=["full", "off"],
+                    help="compare the whole batch's SAM (and the index) with the oracle's")
+    ap.add_argument("--cpu-sample-pairs", type=int, default=0,
+                    help="reference arm: records per step (0 = four 1 Mnt chunks per host thread)")
+    ap.add_argument("--aux-steps", type=int, default=3, help="steps of the plain and batched host-buffer passes")
     ap.add_argument("--no-served", action="store_true", help="skip the served and latency passes (profiling runs)")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def dist_info():
@@ -76,7 +90,7 @@ def dist_info():
     return ws, rank, local
 
 
-def workload(scale: float, name: str = "pe50m", pairs: int = 0):
+def workload(scale: float, name: str = DEFAULT_WORKLOAD, pairs: int = 0):
     """(genome, reads 1, reads 2 or None, read length for the seeding preset)"""
     from strobealign_gb300 import synthetic as syn
     if name == "se5m":
@@ -99,6 +113,20 @@ def workload(scale: float, name: str = "pe50m", pairs: int = 0):
     r1, r2 = syn.make_paired_end(102, g, pairs or int(1_000_000 * scale), 150, 300, 30, 0.01, 0.001,
                                  rescue_fraction=0.02)
     return g, r1, r2, 150
+
+
+def host_cpu() -> dict:
+    """Host cores as nproc and lscpu report them."""
+    info = {"nproc": os.cpu_count(), "machine": platform.machine()}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            k, _, v = line.partition(":")
+            if k.strip() in ("Model name", "CPU(s)", "Thread(s) per core"):
+                info[k.strip()] = v.strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return info
 
 
 class ClockSampler:
@@ -153,57 +181,140 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(g, r1, r2, pairs: int, threads: int) -> dict:
-    """The oracle (C++ restatement of the reference's CPU path) on a bounded sample,
-    all host threads; index build excluded from the rate."""
-    from oracle import build as oracle_build
+def _prefix(rs, n: int):
+    """The first n records of a ReadSet (views, no copy of the bases)."""
     from strobealign_gb300 import synthetic as syn
-    oracle_build.build()
-    pairs = min(pairs, len(r1))
-    with tempfile.TemporaryDirectory() as d:
-        fa = os.path.join(d, "ref.fa")
-        g.write_fasta(fa)
-        files = []
-        for i, rs in enumerate(x for x in (r1, r2) if x is not None):
-            f = os.path.join(d, f"r{i + 1}.fq")
-            syn.ReadSet(rs.seq[:int(rs.offsets[pairs])], rs.offsets[:pairs + 1], rs.names,
-                        rs.name_offsets[:pairs + 1], rs.qual).write_fastq(f)
-            files.append(f)
-        r = subprocess.run([str(oracle_build.cli_path()), "-t", str(threads), "--timing", "-o", os.path.join(d, "o.sam"),
-                            fa] + files, capture_output=True, text=True, check=True)
-    line = [l for l in r.stderr.splitlines() if l.startswith("oracle_timing")][-1]
-    kv = dict(x.split("=") for x in line.split()[1:])
-    map_s = float(kv["map_s"])
-    reads = pairs * len(files)
-    return {"value": reads / map_s, "unit": "reads/s", "cores": threads, "kind": "port",
-            "sample": f"{pairs} {'pairs' if len(files) == 2 else 'reads'} of the same workload, index build excluded "
-                      f"({float(kv['index_s']):.1f} s)", "seconds": map_s}
+    o, no = rs.offsets, rs.name_offsets
+    return syn.ReadSet(rs.seq[:int(o[n])], o[:n + 1], rs.names[:int(no[n])], no[:n + 1],
+                       rs.qual[:int(o[n])] if rs.qual is not None else None)
+
+
+def _slice(rs, a: int, b: int):
+    """Records [a, b) of a ReadSet with offsets starting at 0."""
+    from strobealign_gb300 import synthetic as syn
+    o, no = rs.offsets, rs.name_offsets
+    return syn.ReadSet(rs.seq[int(o[a]):int(o[b])], o[a:b + 1] - o[a], rs.names[int(no[a]):int(no[b])],
+                       no[a:b + 1] - no[a], rs.qual[int(o[a]):int(o[b])] if rs.qual is not None else None)
+
+
+def oracle_index(g, read_length: int, threads: int):
+    """The oracle's make_index over the workload's genome (all host threads)."""
+    from oracle.binding import OracleIndex
+    return OracleIndex(g.names, g.seqs, read_length, threads=threads)
+
+
+def chunk_records(rs, rs2, chunks: int, chunk_size: int = 1_000_000) -> int:
+    """Records that make `chunks` of the reference's chunks (src/main.rs:591-604)."""
+    import numpy as np
+    lens = np.diff(rs.offsets).astype(np.int64)
+    if rs2 is not None:
+        lens = lens + np.diff(rs2.offsets).astype(np.int64)
+    n, i = len(lens), 0
+    c = np.cumsum(lens)
+    for _ in range(chunks):
+        if i >= n:
+            break
+        base = c[i - 1] if i else 0
+        j = int(np.searchsorted(c, base + chunk_size, side="right"))  # first record past the limit
+        i = min(n, j + 1)
+    return i
 
 
 def run_reference(args, ws, rank):
+    """The reference arm: the oracle (the CPU restatement of the reference's path; the
+    Rust crate cannot be built here) on the host cores, index built once, each step a
+    bounded sample of the same workload of at least four 1 Mnt chunks per thread."""
     if rank != 0:
-        return
+        return None
     threads = os.cpu_count() or 1
-    g, r1, r2, _ = workload(args.scale, args.workload, args.pairs)
-    for _ in range(args.warmup):
-        cpu_baseline(g, r1, r2, min(2000, args.cpu_sample_pairs), threads)
-    vals, secs = [], []
-    for _ in range(args.steps):
-        b = cpu_baseline(g, r1, r2, args.cpu_sample_pairs, threads)
-        vals.append(b["value"])
-        secs.append(b["seconds"])
-    value = statistics.median(vals)
+    g, r1, r2, rl = workload(args.scale, args.workload, args.pairs)
+    idx = oracle_index(g, rl, threads)
+    n = len(r1)
+    per = args.cpu_sample_pairs or chunk_records(r1, r2, 4 * threads)
+    per = max(1, min(per, n))
+    use_ssw = bool(args.ssw)
+
+    def step(i: int, m: int, th: int):
+        a = (i * m) % max(1, n - m + 1)
+        x1 = _slice(r1, a, a + m)
+        x2 = _slice(r2, a, a + m) if r2 is not None else None
+        _, sec = idx.map_batch(x1, x2, threads=th, use_ssw=use_ssw)
+        return sec
+
+    for w in range(args.warmup):
+        step(w, min(per, 2000), threads)
+    secs = [step(i, per, threads) for i in range(args.steps)]
+    reads = per * (2 if r2 is not None else 1)
+    value = reads / statistics.median(secs)
+    # one chunk's worth on a single thread (the per-core rate)
+    one = chunk_records(r1, r2, 1)
+    t1 = reads_1 = None
+    if one:
+        t1 = step(0, one, 1)
+        reads_1 = one * (2 if r2 is not None else 1)
+    cpu = host_cpu()
     out = {"metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1000 * statistics.median(secs), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
            "impl": "reference",
-           "config": {"workload": WORKLOADS[args.workload], "scale": args.scale,
-                      "sample_pairs": args.cpu_sample_pairs},
+           "config": {"workload": WORKLOADS[args.workload], "scale": args.scale, "pairs_per_step": per,
+                      "ssw": use_ssw},
            "cpu_baseline": {"value": value, "unit": "reads/s", "cores": threads, "kind": "port",
-                            "sample": f"{args.cpu_sample_pairs} pairs per step; the Rust reference cannot be built "
-                                      "(no cargo); the oracle restates its CPU path"},
+                            "sample": f"{per} {'pairs' if r2 is not None else 'reads'} per step (at least four "
+                                      f"1 Mnt chunks per thread), records rotating through the batch; index built "
+                                      f"once ({idx.build_seconds:.1f} s); the Rust reference cannot be built here "
+                                      f"(no cargo), the oracle restates its CPU path",
+                            "single_thread": None if t1 is None else
+                            {"value": reads_1 / t1, "unit": "reads/s", "cores": 1,
+                             "sample": f"one 1 Mnt chunk ({one} records)"},
+                            "host": cpu},
            "e2e": {"value": value, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
+    return out
+
+
+def parity_leg(g, r1, r2, rl, idx, gpu_sam: bytes, use_ssw: bool, threads: int) -> tuple[dict, dict]:
+    """The whole batch through the oracle: SAM bytes and the index compared with the
+    GPU's; the oracle's mapping time is the CPU baseline on all host threads."""
+    import numpy as np
+    t0 = time.perf_counter()
+    o = oracle_index(g, rl, threads)
+    n, bits, cutoff = o.info()
+    ot, od = o.arrays()
+    gt, gd = idx.to_host()
+    index_same = (bits == idx.bits and cutoff == idx.filter_cutoff and n == len(gt) and
+                  bool(np.array_equal(gd, od)) and bool(np.array_equal(gt.view(np.uint8), ot.view(np.uint8))))
+    del gt, gd
+    want, sec = o.map_batch(r1, r2, threads=threads, use_ssw=use_ssw, eqx=False)
+    same = want == gpu_sam
+    first = None
+    if not same:
+        a = np.frombuffer(gpu_sam, np.uint8)
+        b = np.frombuffer(want, np.uint8)
+        m = min(len(a), len(b))
+        k = int(np.argmax(a[:m] != b[:m])) if m and (a[:m] != b[:m]).any() else m
+        line = int(np.count_nonzero(a[:k] == 10))
+        lo = gpu_sam.rfind(b"\n", 0, k) + 1
+        first = {"byte": k, "line": line, "gpu": gpu_sam[lo:gpu_sam.find(b"\n", k)][:300].decode(errors="replace"),
+                 "oracle": want[lo:want.find(b"\n", k)][:300].decode(errors="replace")}
+    reads = len(r1) * (2 if r2 is not None else 1)
+    parity = {"reads": reads, "records": len(r1), "sam_bytes": len(gpu_sam), "identical": same, "first_diff": first,
+              "index_identical": index_same, "index": {"bits": bits, "filter_cutoff": cutoff, "randstrobes": n},
+              "oracle_index_s": round(o.build_seconds, 2), "oracle_map_s": round(sec, 2),
+              "leg_s": round(time.perf_counter() - t0, 1)}
+    cpu = {"value": reads / sec, "unit": "reads/s", "cores": threads, "kind": "port",
+           "sample": f"the whole batch ({len(r1)} {'pairs' if r2 is not None else 'reads'}), index build excluded "
+                     f"({o.build_seconds:.1f} s on {threads} threads); the oracle restates the reference's CPU path",
+           "seconds": sec, "host": host_cpu()}
+    # one chunk on one thread
+    one = chunk_records(r1, r2, 1)
+    if one:
+        x1 = _prefix(r1, one)
+        x2 = _prefix(r2, one) if r2 is not None else None
+        _, s1 = o.map_batch(x1, x2, threads=1, use_ssw=use_ssw)
+        cpu["single_thread"] = {"value": one * (2 if r2 is not None else 1) / s1, "unit": "reads/s", "cores": 1,
+                                "sample": f"one 1 Mnt chunk ({one} records)"}
+    return parity, cpu
 
 
 def slowest_rank(pg, seconds: float, device: str = "cpu") -> float:
@@ -292,7 +403,11 @@ def main():
         pg = dist
     import strobealign_gb300 as sa
 
+    t = time.time()
     g, r1, r2, read_length = workload(args.scale, args.workload, args.pairs)
+    gen_s = time.time() - t
+    single_end = r2 is None
+    use_ssw = bool(args.ssw) and single_end
     refs = sa.References.from_sequences(g.names, [s.tobytes() for s in g.seqs])
     params = sa.SeedingParameters.from_read_length(read_length)
     t = time.time()
@@ -302,7 +417,7 @@ def main():
     R1 = sa.Reads.from_arrays(r1.seq, r1.offsets, r1.names, r1.name_offsets, r1.qual)
     R2 = sa.Reads.from_arrays(r2.seq, r2.offsets, r2.names, r2.name_offsets, r2.qual) if r2 is not None else None
     n_reads = (2 if r2 is not None else 1) * len(R1)
-    mapper = sa.Mapper(index, refs)
+    mapper = sa.Mapper(index, refs, use_ssw=1 if use_ssw else 0)
     mapper.upload(R1, R2)
 
     def barrier():
@@ -312,12 +427,13 @@ def main():
 
     for _ in range(max(3, args.warmup)):
         mapper.map_uploaded(copy=False)
-    # timed region: reads resident in device memory
+    # timed region: the batched engine, reads resident in device memory
     mapper.set_profiling(True)
     kern = {}
     cells = {}
     phases = {}
     launches = 0
+    waves = []
     barrier()
     stream = torch.cuda.current_stream()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -328,6 +444,7 @@ def main():
             out = mapper.map_uploaded(copy=False)
             st = mapper.stats()
             launches += int(st["n_launches"])
+            waves.append(int(st["n_waves"]))
             for k in ("seconds_nams", "seconds_extension", "seconds_policy"):
                 phases[k] = phases.get(k, 0.0) + st[k] / args.steps
             for k, v in st["sw_cells"].items():
@@ -345,20 +462,28 @@ def main():
     elapsed = slowest_rank(pg, elapsed, "cuda")
     value = ws * n_reads * args.steps / elapsed
     sam_bytes = int(out)
-    # end to end: host buffers in, SAM bytes out, every step
-    h2d = d2h = 0
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        mapper.map(R1, R2, copy=False)
-        st = mapper.stats()
-        h2d, d2h = int(st["h2d_bytes"]), int(st["d2h_bytes"])
-    barrier()
-    e2e_s = time.perf_counter() - t0
-    e2e_s = slowest_rank(pg, e2e_s, "cuda")
-    plain_e2e = ws * n_reads * args.steps / e2e_s
-    plain_h2d, plain_d2h = h2d, d2h
-    # served: the same pairs as a stream of requests (log-uniform 1..100k pairs), each
+    aux = max(1, min(args.steps, args.aux_steps))
+
+    def host_pass(steps: int):
+        """Whole batch from host buffers through sa_map_batch: (rate, h2d, d2h)."""
+        h2d = d2h = 0
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            mapper.map(R1, R2, copy=False)
+            st = mapper.stats()
+            h2d, d2h = int(st["h2d_bytes"]), int(st["d2h_bytes"])
+        barrier()
+        sec = slowest_rank(pg, time.perf_counter() - t0, "cuda")
+        return ws * n_reads * steps / sec, h2d, d2h, int(st["n_waves"]), int(st["n_launches"])
+
+    # the batched engine from host buffers, then the plain stage-synchronous form
+    batched_e2e, b_h2d, b_d2h, _, _ = host_pass(aux)
+    mapper.set_schedule(overlap=False)
+    mapper.map(R1, R2, copy=False)  # warm-up of the plain form
+    plain_e2e, plain_h2d, plain_d2h, plain_waves, plain_launches = host_pass(aux)
+    mapper.set_schedule()
+    # served: the same records as a stream of requests (log-uniform 1..100k pairs), each
     # its own chunk stream, through one session with continuous batching
     reqs, lat = [], None
     served = s_h2d = s_d2h = None
@@ -368,7 +493,7 @@ def main():
         for n in sizes:
             reqs.append((slice_reads(sa, r1, a, a + n), slice_reads(sa, r2, a, a + n) if r2 is not None else None))
             a += n
-        session = sa.Session(index, refs)
+        session = sa.Session(index, refs, use_ssw=1 if use_ssw else 0)
         served_pass(session, reqs)  # warm-up: arena, workspaces
         barrier()
         t0 = time.perf_counter()
@@ -383,9 +508,18 @@ def main():
         cap_rps = len(reqs) * args.steps / served_s
         lat = latency_pass(session, reqs, 0.7 * cap_rps, max(60, min(400, int(3 * 0.7 * cap_rps))))
         session.close()
-    e2e = served if served is not None else plain_e2e
+    e2e = served if served is not None else batched_e2e
     if served is None:
-        s_h2d, s_d2h = plain_h2d, plain_d2h
+        s_h2d, s_d2h = b_h2d, b_d2h
+    # parity: the batch once more, its bytes against the oracle's (rank 0 only)
+    parity = cpu = None
+    if rank == 0 and args.parity == "full":
+        gpu_sam = mapper.map_uploaded(copy=True)
+        try:
+            parity, cpu = parity_leg(g, r1, r2, read_length, index, gpu_sam, use_ssw, os.cpu_count() or 1)
+        except Exception as e:  # reported, never fatal for the GPU line
+            parity = {"identical": None, "error": str(e)[:300]}
+        del gpu_sam
     if rank != 0:
         pg.destroy_process_group()
         return
@@ -400,30 +534,34 @@ def main():
     shares = {k: round(v[0] / total_ms, 4) for k, v in kern.items() if total_ms and v[0] > 0}
     counts = {k: int(st[k]) for k in ("n_bases", "n_randstrobes", "n_anchor_total")}
     roofline, rooflines = roofline_for(dom, kern, cells, peaks, clk.summary(), counts, args.steps) if dom else (None, {})
-    cpu = None
-    if not args.no_cpu_baseline:
-        try:
-            cpu = cpu_baseline(g, r1, r2, args.cpu_sample_pairs, os.cpu_count() or 1)
-        except Exception as e:  # reported, never fatal for the GPU line
-            cpu = {"value": None, "error": str(e)[:200]}
+    reads_gb = int(R1.seq_offsets[-1]) * (2 if R2 is not None else 1) / 1e9
     out = {
         "metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": ws, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": 1000 * elapsed / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
         "config": {"workload": WORKLOADS[args.workload], "scale": args.scale, "reads_per_step": n_reads,
-                   "l2": f"no flush: index {index.info.device_bytes / 1e6:.0f} MB + reads "
-                         f"{int(R1.seq_offsets[-1]) * (2 if R2 is not None else 1) / 1e6:.0f} MB "
-                         f"({'exceed' if index.info.device_bytes > 129e6 else 'with the reads exceed'} the 129 MB L2)",
-                   "value_form": "plain: the whole batch through sa_map_uploaded, reads resident on the device",
-                   "e2e_form": "served: the same pairs as requests of log-uniform 1..100k pairs through "
+                   "extension": "ssw" if (use_ssw or not single_end) else "piecewise",
+                   "l2": f"no flush: index {index.info.device_bytes / 1e6:.0f} MB + reads {reads_gb * 1e3:.0f} MB "
+                         f"exceed the 129 MB L2",
+                   "value_form": "batched engine: the whole batch through sa_map_uploaded, reads resident on the "
+                                 "device, NAM parts overlapped with the policy and extension waves",
+                   "e2e_form": "served: the same records as requests of log-uniform 1..100k pairs through "
                                "sa_session submit/wait from host buffers, continuous batching",
-                   "requests_per_step": len(reqs), "sam_bytes_per_step": sam_bytes,
-                   "index_build_s": round(index_s, 3)},
+                   "plain_form": "stage-synchronous: sa_map_batch from host buffers with overlap = 0 (NAM parts "
+                                 "one after another, then policy and extension waves taking turns)",
+                   "aux_steps": aux, "requests_per_step": len(reqs), "sam_bytes_per_step": sam_bytes,
+                   "index_build_s": round(index_s, 3), "generate_s": round(gen_s, 1),
+                   "waves_per_step": waves},
         "e2e": {"value": e2e, "unit": "reads/s", "h2d_bytes_per_step": s_h2d, "d2h_bytes_per_step": s_d2h},
-        "plain": {"value_resident": value, "e2e": plain_e2e, "unit": "reads/s", "h2d_bytes_per_step": plain_h2d,
-                  "d2h_bytes_per_step": plain_d2h},
+        "parity": parity,
+        "plain": {"e2e": plain_e2e, "unit": "reads/s", "h2d_bytes_per_step": plain_h2d,
+                  "d2h_bytes_per_step": plain_d2h, "waves": plain_waves, "launches": plain_launches},
+        "batched": {"value_resident": value, "e2e": batched_e2e, "unit": "reads/s", "h2d_bytes_per_step": b_h2d,
+                    "d2h_bytes_per_step": b_d2h},
         "served": None if served is None else {"value": served, "unit": "reads/s",
-                                               "vs_plain_e2e": served / plain_e2e, "latency_open_loop": lat},
+                                               "vs_plain_e2e": served / plain_e2e,
+                                               "vs_batched_e2e": served / batched_e2e,
+                                               "latency_open_loop": lat},
         "gpu_launches": launches,
         "stage_share": shares,
         # wall seconds per step: NAM pipeline (GPU), extension waves (GPU, incl. job

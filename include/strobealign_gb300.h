@@ -365,8 +365,34 @@ int32_t sa_mapper_get_stats(const sa_mapper* m, sa_mapper_stats* out);
 int32_t sa_mapper_set_profiling(sa_mapper* m, int32_t enable);
 /* Parts a large batch is cut into (runs of whole chunks, at least 4 chunks each): the
  * NAM pipeline of one part runs while the earlier parts are extended and written.
- * Output bytes do not depend on it.  Default 4; 1 = the whole batch at once. */
+ * Output bytes do not depend on it.  Default 4; batches of more than 2^27 bases get
+ * as many parts as hold at most 2^27 bases each. */
 int32_t sa_mapper_set_parts(sa_mapper* m, uint32_t parts);
+
+/* How a batch is scheduled on the device and the host.  No counterpart in the
+ * reference (it maps chunks on CPU threads); output bytes never depend on it.
+ *   parts          NAM-pipeline parts (runs of whole chunks, at least 4 chunks each);
+ *                  0 = 4.  Batches of more than 2^27 bases get more parts, so that a
+ *                  part holds at most 2^27 bases.  With overlap, part p + 1's pipeline
+ *                  runs while earlier parts are extended.
+ *   overlap        1 (default): continuous batching -- policy threads run the chunks
+ *                  whose results are in while the next extension wave runs, and the
+ *                  output is copied into place while mapping.  0: the plain,
+ *                  stage-synchronous form -- each stage is launched over everything
+ *                  waiting for it and the host and device take turns: a wave starts
+ *                  only when no chunk can proceed, and chunks resume only when every
+ *                  waiting request has run.
+ *   wave_min_jobs  waiting jobs that start a wave while policy threads are busy
+ *                  (overlap = 1); 0 = 32768.
+ *   max_wave_jobs  jobs per wave at most; 0 = 262144. */
+typedef struct {
+    uint32_t parts;
+    uint32_t overlap;
+    uint64_t wave_min_jobs;
+    uint64_t max_wave_jobs;
+} sa_schedule_params;
+void sa_schedule_params_default(sa_schedule_params* p);
+int32_t sa_mapper_set_schedule(sa_mapper* m, const sa_schedule_params* p);
 
 /* SAM header (src/io/sam.rs:176-200); cmd_line NULL omits the @PG line. */
 int32_t sa_sam_header(const sa_refs* refs, const char* cmd_line, const char* rg_id, const char* const* rg_fields,

@@ -19,7 +19,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
-SOURCES = ["seeding.cpp", "nams.cpp", "ssw.cpp", "mapper.cpp", "piecewise.cpp", "io.cpp"]
+SOURCES = ["seeding.cpp", "nams.cpp", "ssw.cpp", "mapper.cpp", "piecewise.cpp", "io.cpp", "driver.cpp"]
 FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-Wall"]
 REFERENCE_TREE = Path(os.environ.get("STROBEALIGN_REFERENCE", "/root/reference"))
 

@@ -2,7 +2,11 @@
 // ctypes to compare stage outputs (randstrobes, index arrays, NAMs, alignments)
 // with the GPU library.
 #include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cstdlib>
 #include <cstring>
+#include <thread>
 
 #include "oracle.hpp"
 
@@ -103,6 +107,126 @@ void* ora_index_from_fasta(const char* path, size_t read_length, int32_t bits, d
     return o;
 }
 
+// The same from contigs in memory (ASCII bases), built on `threads` threads;
+// *seconds = the index build time.
+void* ora_index_from_buffers(size_t n, const char* const* names, const char* const* seqs, const size_t* lens,
+                             size_t read_length, int32_t bits, double filter_fraction, uint32_t threads,
+                             double* seconds) {
+    auto* o = new OraIndex();
+    o->refs.resize(n);
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> th;
+    for (uint32_t t = 0; t < std::max<uint32_t>(threads, 1); t++)
+        th.emplace_back([&] {
+            for (size_t i; (i = next.fetch_add(1)) < n;) {
+                o->refs[i].name = names[i];
+                o->refs[i].seq.data.reserve(lens[i] / 32 + 1);
+                for (size_t j = 0; j < lens[i]; j++) o->refs[i].seq.push((uint8_t)seqs[i][j]);
+            }
+        });
+    for (auto& t : th) t.join();
+    SeedingParameters p = SeedingParameters::from_read_length(read_length);
+    uint8_t b = bits < 0 ? pick_bits(o->refs, p) : (uint8_t)bits;
+    auto t0 = std::chrono::steady_clock::now();
+    o->index = make_index(o->refs, p, b, filter_fraction, std::max<uint32_t>(threads, 1));
+    if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return o;
+}
+
+struct ora_read_batch {
+    size_t n;
+    const char* seq;
+    const uint64_t* seq_offsets;
+    const char* qual;  // NULL: no qualities
+    const char* names;
+    const uint64_t* name_offsets;
+};
+
+struct ora_map_opts {
+    uint32_t mode;  // 0 SAM, 1 PAF, 2 abundances
+    uint32_t max_secondary;
+    float dropoff;
+    uint32_t rescue_distance, max_tries, mcs, output_unmapped, use_ssw, eqx, details;
+    uint64_t chunk_size;
+    uint32_t threads;
+};
+
+static void records_from(const ora_read_batch* b, std::vector<SequenceRecord>& out, uint32_t threads) {
+    out.resize(b->n);
+    const size_t per = 1 << 14, nb = (b->n + per - 1) / per;
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> th;
+    for (uint32_t t = 0; t < std::max<uint32_t>(threads, 1); t++)
+        th.emplace_back([&] {
+            for (size_t k; (k = next.fetch_add(1)) < nb;)
+                for (size_t i = k * per; i < std::min(b->n, (k + 1) * per); i++) {
+                    SequenceRecord& r = out[i];
+                    r.name.assign(b->names + b->name_offsets[i], b->name_offsets[i + 1] - b->name_offsets[i]);
+                    r.seq.assign(b->seq + b->seq_offsets[i], b->seq_offsets[i + 1] - b->seq_offsets[i]);
+                    if (b->qual) {
+                        r.qual.assign(b->qual + b->seq_offsets[i], b->seq_offsets[i + 1] - b->seq_offsets[i]);
+                        r.has_qual = true;
+                    }
+                }
+        });
+    for (auto& t : th) t.join();
+}
+
+// The chunk driver (driver.cpp) over records in memory.  *out (malloc'ed, release with
+// ora_output_free) receives the records' SAM / PAF bytes without a header, or for mode
+// 2 the per-contig abundances (f64, divided by contig length) as raw bytes;
+// *seconds = the mapping time (record conversion excluded).
+int32_t ora_map_batch(void* h, const ora_read_batch* r1, const ora_read_batch* r2, const ora_map_opts* opt,
+                      char** out, size_t* out_len, double* seconds) {
+    auto* o = (OraIndex*)h;
+    std::vector<SequenceRecord> a, b;
+    records_from(r1, a, opt->threads);
+    if (r2) records_from(r2, b, opt->threads);
+    Context ctx;
+    ctx.refs = &o->refs;
+    ctx.index = &o->index;
+    ctx.mp.max_secondary = opt->max_secondary;
+    ctx.mp.dropoff_threshold = opt->dropoff;
+    ctx.mp.rescue_distance = opt->rescue_distance;
+    ctx.mp.max_tries = opt->max_tries;
+    ctx.mp.mcs = (Mcs)opt->mcs;
+    ctx.mp.output_unmapped = opt->output_unmapped != 0;
+    ctx.mp.use_ssw = opt->use_ssw != 0;
+    ctx.so.eqx = opt->eqx != 0;
+    ctx.so.details = opt->details != 0;
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<double> ab;
+    std::vector<std::string> outs = map_records(ctx, a, r2 ? &b : nullptr, (MapMode)opt->mode,
+                                                std::max<uint32_t>(opt->threads, 1), opt->chunk_size, &ab);
+    if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (opt->mode == 2) {
+        *out_len = ab.size() * sizeof(double);
+        *out = (char*)std::malloc(std::max<size_t>(*out_len, 1));
+        for (size_t i = 0; i < ab.size(); i++) ab[i] /= (double)o->refs[i].seq.len;
+        std::memcpy(*out, ab.data(), *out_len);
+        return 0;
+    }
+    size_t total = 0;
+    std::vector<size_t> at(outs.size() + 1, 0);
+    for (size_t i = 0; i < outs.size(); i++) at[i + 1] = at[i] + outs[i].size();
+    total = at.back();
+    *out = (char*)std::malloc(std::max<size_t>(total, 1));
+    *out_len = total;
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> th;
+    for (uint32_t t = 0; t < std::max<uint32_t>(opt->threads, 1); t++)
+        th.emplace_back([&] {
+            for (size_t i; (i = next.fetch_add(1)) < outs.size();) {
+                std::memcpy(*out + at[i], outs[i].data(), outs[i].size());
+                std::string().swap(outs[i]);
+            }
+        });
+    for (auto& t : th) t.join();
+    return 0;
+}
+
+void ora_output_free(char* p) { std::free(p); }
+
 void ora_index_free(void* h) { delete (OraIndex*)h; }
 
 // sizes: [n_randstrobes, bits, filter_cutoff]
@@ -111,6 +235,13 @@ void ora_index_info(void* h, uint64_t* out3) {
     out3[0] = o->index.randstrobes.size();
     out3[1] = o->index.bits;
     out3[2] = o->index.filter_cutoff;
+}
+
+// Pointers to the index arrays (valid until ora_index_free), for comparisons without a copy.
+void ora_index_view(void* h, const void** randstrobes, const uint64_t** buckets) {
+    auto* o = (OraIndex*)h;
+    *randstrobes = o->index.randstrobes.data();
+    *buckets = o->index.bucket_starts.data();
 }
 
 void ora_index_arrays(void* h, void* randstrobes, uint64_t* buckets) {

@@ -2,7 +2,8 @@
 // src/main.rs that fix output bytes: read-length estimation (:1003-1012), chunking
 // (:591-604, chunk = records until the nucleotide count exceeds chunk_size), a fresh
 // Rng::with_seed(0) and InsertSizeDistribution per chunk (:878-879), output in chunk
-// order (:653-667) and the abundance table (:990-1001).  Chunks run on -t threads.
+// order (:653-667) and the abundance table (:990-1001).  Chunks run on -t threads
+// (driver.cpp), and so does the index build.
 //
 //   sa_oracle [options] ref.fa reads1.fq [reads2.fq]
 #include "oracle.hpp"
@@ -116,7 +117,7 @@ int main(int argc, char** argv) {
     SeedingParameters sp = SeedingParameters::from_read_length(read_length);
     auto t0 = std::chrono::steady_clock::now();
     uint8_t bits = pick_bits(refs, sp);
-    Index index = make_index(refs, sp, bits, a.filter_fraction);
+    Index index = make_index(refs, sp, bits, a.filter_fraction, std::max<size_t>(a.threads, 1));
     auto t1 = std::chrono::steady_clock::now();
 
     Context ctx;
@@ -135,48 +136,11 @@ int main(int argc, char** argv) {
     if (a.has_rg_id) { ctx.so.rg_id = a.rg_id; ctx.so.has_rg = true; }
     else if (!a.rg.empty()) { ctx.so.rg_id = "1"; ctx.so.has_rg = true; }
 
-    // chunking (src/main.rs:591-604)
-    size_t n = paired ? std::min(r1.size(), r2.size()) : r1.size();
-    std::vector<std::pair<size_t, size_t>> chunks;
-    for (size_t i = 0; i < n;) {
-        size_t nt = 0, j = i;
-        while (j < n) {
-            nt += r1[j].seq.size() + (paired ? r2[j].seq.size() : 0);
-            j++;
-            if (nt > a.chunk_size) break;
-        }
-        chunks.emplace_back(i, j);
-        i = j;
-    }
-    std::vector<std::string> outs(chunks.size());
-    std::vector<std::vector<double>> ab(std::max<size_t>(a.threads, 1), std::vector<double>(refs.size(), 0.0));
-    std::atomic<size_t> next{0};
-    auto worker = [&](size_t tid) {
-        for (;;) {
-            size_t c = next.fetch_add(1);
-            if (c >= chunks.size()) break;
-            Rng rng(0);
-            InsertSizeDistribution isd;
-            std::string& out = outs[c];
-            for (size_t i = chunks[c].first; i < chunks[c].second; i++) {
-                Details d;
-                if (a.aemb) {
-                    if (paired) abundances_paired_end_read(r1[i], r2[i], ctx, ab[tid], isd, rng);
-                    else abundances_single_end_read(r1[i], ctx, ab[tid], rng);
-                } else if (a.map_only) {
-                    out += paired ? map_paired_end_read(r1[i], r2[i], ctx, isd, rng, d)
-                                  : map_single_end_read(r1[i], ctx, rng, d);
-                } else {
-                    out += paired ? align_paired_end_read(r1[i], r2[i], ctx, isd, rng, d)
-                                  : align_single_end_read(r1[i], ctx, rng, d);
-                }
-            }
-        }
-    };
-    std::vector<std::thread> th;
+    MapMode mode = a.aemb ? MapMode::Abundance : a.map_only ? MapMode::Paf : MapMode::Sam;
     size_t nt = std::max<size_t>(a.threads, 1);
-    for (size_t t = 0; t < nt; t++) th.emplace_back(worker, t);
-    for (auto& t : th) t.join();
+    size_t n = paired ? std::min(r1.size(), r2.size()) : r1.size();
+    std::vector<double> tot;
+    std::vector<std::string> outs = map_records(ctx, r1, paired ? &r2 : nullptr, mode, nt, a.chunk_size, &tot);
     auto t2 = std::chrono::steady_clock::now();
 
     FILE* fo = a.output.empty() ? stdout : std::fopen(a.output.c_str(), "wb");
@@ -190,9 +154,6 @@ int main(int argc, char** argv) {
     }
     for (auto& o : outs) std::fwrite(o.data(), 1, o.size(), fo);
     if (a.aemb) {
-        std::vector<double> tot(refs.size(), 0.0);
-        for (size_t t = 0; t < nt; t++)
-            for (size_t i = 0; i < refs.size(); i++) tot[i] += ab[t][i];
         for (size_t i = 0; i < refs.size(); i++)
             std::fprintf(fo, "%s\t%.6f\n", refs[i].name.c_str(), tot[i] / (double)refs[i].seq.len);
     }

@@ -111,7 +111,7 @@ struct Index {
 
 uint8_t pick_bits(const std::vector<RefSeq>& refs, const SeedingParameters& p);
 Index make_index(const std::vector<RefSeq>& refs, const SeedingParameters& p, uint8_t bits,
-                 double filter_fraction);
+                 double filter_fraction, size_t threads = 1);
 bool write_sti(const Index& idx, const std::string& path);
 int read_sti(const std::string& path, const SeedingParameters& p, uint8_t bits, Index& out);
 
@@ -304,6 +304,15 @@ std::string map_paired_end_read(const SequenceRecord& r1, const SequenceRecord& 
 void abundances_single_end_read(const SequenceRecord& r, const Context& ctx, std::vector<double>& ab, Rng& rng);
 void abundances_paired_end_read(const SequenceRecord& r1, const SequenceRecord& r2, const Context& ctx,
                                 std::vector<double>& ab, InsertSizeDistribution& isd, Rng& rng);
+
+// Chunk driver of src/main.rs:591-604,873-988 (driver.cpp): per-chunk output strings in
+// chunk order; abundances (if requested) summed over threads, not yet divided by length.
+enum class MapMode { Sam = 0, Paf = 1, Abundance = 2 };
+std::vector<std::pair<size_t, size_t>> chunk_ranges(const std::vector<SequenceRecord>& r1,
+                                                    const std::vector<SequenceRecord>* r2, size_t chunk_size);
+std::vector<std::string> map_records(const Context& ctx, const std::vector<SequenceRecord>& r1,
+                                     const std::vector<SequenceRecord>* r2, MapMode mode, size_t threads,
+                                     size_t chunk_size, std::vector<double>* abundances);
 
 // Piecewise single-end extension (src/piecewisealigner.rs); block-aligner restated.
 void remove_spurious_anchors(std::vector<Anchor>& anchors);

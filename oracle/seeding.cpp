@@ -4,6 +4,8 @@
 #include "oracle.hpp"
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <deque>
 #include <cmath>
 
@@ -245,29 +247,96 @@ uint8_t pick_bits(const std::vector<RefSeq>& refs, const SeedingParameters& p) {
     return (uint8_t)(lg - 1);
 }
 
-// src/indexer.rs:18-170 (make_index) and :222-253 (assign_randstrobes)
-Index make_index(const std::vector<RefSeq>& refs, const SeedingParameters& p, uint8_t bits, double filter_fraction) {
+// RefRandstrobe order (src/index.rs:15-25: derived Ord over hash_offset, position,
+// ref_index).  A total order on distinct records, so any correct sort gives the same
+// table.
+static inline bool rs_less(const RefRandstrobe& a, const RefRandstrobe& b) {
+    if (a.hash_offset != b.hash_offset) return a.hash_offset < b.hash_offset;
+    if (a.position != b.position) return a.position < b.position;
+    return a.ref_index < b.ref_index;
+}
+
+template <class F>
+static void parallel_for(size_t n, size_t threads, F f) {
+    if (threads <= 1 || n <= 1) {
+        for (size_t i = 0; i < n; i++) f(i);
+        return;
+    }
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < std::min(threads, n); t++)
+        th.emplace_back([&] {
+            for (size_t i; (i = next.fetch_add(1)) < n;) f(i);
+        });
+    for (auto& t : th) t.join();
+}
+
+// The sort of make_index on several threads: records scattered by the top 12 bits
+// of hash_offset (the leading key), then every range sorted on its own.
+static void sort_randstrobes(std::vector<RefRandstrobe>& rs, size_t threads) {
+    if (threads <= 1 || rs.size() < (1u << 20)) {
+        std::sort(rs.begin(), rs.end(), rs_less);
+        return;
+    }
+    const int B = 12;
+    const size_t NB = (size_t)1 << B, n = rs.size();
+    const size_t parts = threads * 4, per = (n + parts - 1) / parts;
+    std::vector<std::vector<size_t>> cnt(parts, std::vector<size_t>(NB, 0));
+    parallel_for(parts, threads, [&](size_t t) {
+        for (size_t i = t * per; i < std::min(n, (t + 1) * per); i++) cnt[t][rs[i].hash_offset >> (64 - B)]++;
+    });
+    std::vector<size_t> start(NB + 1, 0);
+    std::vector<std::vector<size_t>> pos(parts, std::vector<size_t>(NB, 0));
+    size_t acc = 0;
+    for (size_t b = 0; b < NB; b++) {
+        start[b] = acc;
+        for (size_t t = 0; t < parts; t++) {
+            pos[t][b] = acc;
+            acc += cnt[t][b];
+        }
+    }
+    start[NB] = acc;
+    std::vector<RefRandstrobe> out(n);
+    parallel_for(parts, threads, [&](size_t t) {
+        for (size_t i = t * per; i < std::min(n, (t + 1) * per); i++)
+            out[pos[t][rs[i].hash_offset >> (64 - B)]++] = rs[i];
+    });
+    parallel_for(NB, threads, [&](size_t b) { std::sort(out.begin() + start[b], out.begin() + start[b + 1], rs_less); });
+    rs.swap(out);
+}
+
+// src/indexer.rs:18-170 (make_index) and :222-253 (assign_randstrobes).  Contigs are
+// turned into randstrobes on `threads` threads and the records concatenated in
+// contig order; the sort is a total order, so the table does not depend on threads.
+Index make_index(const std::vector<RefSeq>& refs, const SeedingParameters& p, uint8_t bits, double filter_fraction,
+                 size_t threads) {
     Index idx;
     idx.params = p;
     idx.bits = bits;
     std::vector<RefRandstrobe>& rs = idx.randstrobes;
-    for (size_t ri = 0; ri < refs.size(); ri++) {
+    std::vector<std::vector<RefRandstrobe>> per(refs.size());
+    parallel_for(refs.size(), threads, [&](size_t ri) {
         const PackedSeq& seq = refs[ri].seq;
-        if (seq.len < p.w_max) continue;
+        if (seq.len < p.w_max) return;
         std::vector<Syncmer> sy = syncmers_of_ref(seq, p);
         std::vector<Randstrobe> out;
         randstrobes_from_syncmers(sy, p, out);
+        std::vector<Syncmer>().swap(sy);
+        per[ri].reserve(out.size());
         for (auto& r : out) {
             uint64_t off = (uint64_t)(uint8_t)(r.strobe2_pos - r.strobe1_pos);
-            rs.push_back(RefRandstrobe{(r.hash & REF_RANDSTROBE_HASH_MASK) | off, (uint32_t)r.strobe1_pos,
-                                       (uint32_t)ri});
+            per[ri].push_back(RefRandstrobe{(r.hash & REF_RANDSTROBE_HASH_MASK) | off, (uint32_t)r.strobe1_pos,
+                                            (uint32_t)ri});
         }
-    }
-    std::sort(rs.begin(), rs.end(), [](const RefRandstrobe& a, const RefRandstrobe& b) {
-        if (a.hash_offset != b.hash_offset) return a.hash_offset < b.hash_offset;
-        if (a.position != b.position) return a.position < b.position;
-        return a.ref_index < b.ref_index;
     });
+    size_t total = 0;
+    for (auto& v : per) total += v.size();
+    rs.reserve(total);
+    for (auto& v : per) {
+        rs.insert(rs.end(), v.begin(), v.end());
+        std::vector<RefRandstrobe>().swap(v);
+    }
+    sort_randstrobes(rs, threads);
     std::vector<uint64_t>& starts = idx.bucket_starts;
     starts.reserve(((size_t)1 << bits) + 1);
     std::vector<size_t> counts;
@@ -290,11 +359,18 @@ Index make_index(const std::vector<RefSeq>& refs, const SeedingParameters& p, ui
     }
     if (count != 1) counts.push_back(count);
     while (starts.size() < ((size_t)1 << bits) + 1) starts.push_back(rs.size());
-    std::sort(counts.begin(), counts.end(), std::greater<size_t>());
+    // counts sorted in descending order (src/indexer.rs:138-155); only the element at
+    // index_cutoff (or the last one) is read, so a selection gives the same value
     size_t index_cutoff = (size_t)((double)unique * filter_fraction);
     size_t cutoff;
-    if (index_cutoff < counts.size()) cutoff = counts[index_cutoff];
-    else cutoff = counts.empty() ? 30 : counts.back();
+    if (index_cutoff < counts.size()) {
+        std::nth_element(counts.begin(), counts.begin() + index_cutoff, counts.end(), std::greater<size_t>());
+        cutoff = counts[index_cutoff];
+    } else if (!counts.empty()) {
+        cutoff = *std::min_element(counts.begin(), counts.end());
+    } else {
+        cutoff = 30;
+    }
     idx.filter_cutoff = std::clamp<size_t>(cutoff, 30, 100);
     return idx;
 }

@@ -402,6 +402,20 @@ class Mapper:
         """NAM-pipeline parts a large batch is cut into (output does not depend on it)."""
         L.check(lib().sa_mapper_set_parts(self.h, parts))
 
+    def set_schedule(self, parts: int = 4, overlap: bool = True, wave_min_jobs: int = 0,
+                     max_wave_jobs: int = 0) -> None:
+        """Batch scheduling (sa_mapper_set_schedule); output bytes do not depend on it.
+        overlap=False with parts=1 is the plain, stage-synchronous form."""
+        sp = L.ScheduleParams()
+        lib().sa_schedule_params_default(C.byref(sp))
+        sp.parts = parts
+        sp.overlap = 1 if overlap else 0
+        if wave_min_jobs:
+            sp.wave_min_jobs = wave_min_jobs
+        if max_wave_jobs:
+            sp.max_wave_jobs = max_wave_jobs
+        L.check(lib().sa_mapper_set_schedule(self.h, C.byref(sp)))
+
     def abundances(self) -> np.ndarray:
         n = len(self.refs)
         out = np.zeros(n, dtype=np.float64)

@@ -77,6 +77,10 @@ class SessionParams(C.Structure):
                 ("admission_streams", u32), ("borrow_inputs", u32)]
 
 
+class ScheduleParams(C.Structure):
+    _fields_ = [("parts", u32), ("overlap", u32), ("wave_min_jobs", u64), ("max_wave_jobs", u64)]
+
+
 class RequestStats(C.Structure):
     _fields_ = [("seconds_queued", f64), ("seconds_service", f64), ("seconds_total", f64), ("n_reads", u64),
                 ("n_waves", u32), ("h2d_bytes", u64), ("d2h_bytes", u64)]
@@ -139,6 +143,8 @@ SIGNATURES = {
     "sa_mapper_get_stats": (i32, [vp, P(MapperStats)]),
     "sa_mapper_set_profiling": (i32, [vp, i32]),
     "sa_mapper_set_parts": (i32, [vp, u32]),
+    "sa_schedule_params_default": (None, [P(ScheduleParams)]),
+    "sa_mapper_set_schedule": (i32, [vp, P(ScheduleParams)]),
 }
 
 _lib = None

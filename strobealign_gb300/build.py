@@ -35,6 +35,24 @@ def library_path() -> Path:
     return LIBDIR / LIBNAME
 
 
+def synth_library_path() -> Path:
+    return LIBDIR / "libsa_synth.so"
+
+
+def build_synth(force: bool = False) -> Path:
+    """The workload generator (synth.cpp), a host-only library of its own."""
+    LIBDIR.mkdir(exist_ok=True)
+    src, lib = HERE / "synth.cpp", synth_library_path()
+    if force or _needs(lib, [src]):
+        tmp = lib.with_suffix(".so.tmp")
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", "-Wall", "-o", str(tmp), str(src)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, lib)
+    return lib
+
+
 def _needs(obj: Path, deps: list[Path]) -> bool:
     if not obj.exists():
         return True
@@ -82,6 +100,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, lib)
+    build_synth(force)
     return lib
 
 

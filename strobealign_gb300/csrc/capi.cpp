@@ -427,6 +427,26 @@ int32_t sa_mapper_set_parts(sa_mapper* m, uint32_t parts) {
     SA_CATCH
 }
 
+void sa_schedule_params_default(sa_schedule_params* p) {
+    if (!p) return;
+    p->parts = 4;
+    p->overlap = 1;
+    p->wave_min_jobs = 32768;
+    p->max_wave_jobs = 262144;
+}
+
+int32_t sa_mapper_set_schedule(sa_mapper* m, const sa_schedule_params* p) {
+    SA_TRY
+    require(m && p, "null argument");
+    require(p->overlap <= 1, "overlap must be 0 or 1");
+    m->m->set_parts(p->parts ? p->parts : 4);
+    m->m->set_overlap(p->overlap != 0);
+    m->m->set_wave_min_jobs(p->wave_min_jobs ? p->wave_min_jobs : 32768);
+    m->m->set_max_wave_jobs(p->max_wave_jobs ? p->max_wave_jobs : 262144);
+    return SA_OK;
+    SA_CATCH
+}
+
 int32_t sa_mapper_get_stats(const sa_mapper* m, sa_mapper_stats* out) {
     SA_TRY
     require(m && out, "null argument");

@@ -263,6 +263,7 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, uint32_t& launches, u
     std::exception_ptr err;
     bool stop = false;
     std::vector<bool> is_seeded(nchunks, false);
+    bool nam_done = false;  // every part's NAMs are in (the plain form waits for it)
 
     // NAM pipelines part by part; a part's chunks become ready once its NAMs are in
     std::thread nam_thread([&]() {
@@ -274,11 +275,18 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, uint32_t& launches, u
                 }
                 Part& p = *parts_[pi];
                 part_nams(p, nam_launches);
+                if (!overlap_) continue;  // the plain form starts the policy after the last part
                 std::lock_guard<std::mutex> g(mu);
                 for (size_t c = p.chunk_lo; c < p.chunk_hi; c++) ready.push_back(c);
                 cv_work.notify_all();
                 cv_ext.notify_one();
             }
+            std::lock_guard<std::mutex> g(mu);
+            if (!overlap_)
+                for (size_t c = 0; c < nchunks; c++) ready.push_back(c);
+            nam_done = true;
+            cv_work.notify_all();
+            cv_ext.notify_one();
         } catch (...) {
             std::lock_guard<std::mutex> g(mu);
             if (!err) err = std::current_exception();
@@ -364,7 +372,7 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, uint32_t& launches, u
     for (unsigned t = 0; t < nthreads; t++) th.emplace_back(worker);
 
     uint32_t waves = 0;
-    std::vector<size_t> batch;
+    std::vector<size_t> batch, held;
     const auto t_sched0 = t_map0_;
     try {
         std::unique_lock<std::mutex> lk(mu);
@@ -374,6 +382,7 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, uint32_t& launches, u
                 if (stop || n_done == nchunks) return true;
                 if (waiting.empty()) return false;
                 const bool idle = running == 0 && ready.empty();
+                if (!overlap_) return idle && nam_done;
                 return idle || waiting_jobs >= wave_min_jobs_;
             });
             if (stop || n_done == nchunks) break;
@@ -442,6 +451,13 @@ uint32_t Mapper::schedule(std::vector<ChunkState>& chunks, uint32_t& launches, u
             }
             waves++;
             lk.lock();
+            if (!overlap_) {
+                // plain form: the chunks resume together once every waiting request has run
+                held.insert(held.end(), batch.begin(), batch.end());
+                if (!waiting.empty()) continue;
+                batch.swap(held);
+                held.clear();
+            }
             for (size_t c : batch) ready.push_back(c);
             cv_work.notify_all();
         }
@@ -502,7 +518,10 @@ void Mapper::map_uploaded(sa_output* out) {
     // are local to it
     const uint32_t rpr = paired ? 2 : 1;
     const size_t nchunks = chunks.size();
-    n_parts_ = std::max<size_t>(1, std::min<size_t>(parts_target_, nchunks / 4));
+    // at least parts_target_ parts, and enough that a part holds at most
+    // MAX_PART_BASES bases (the NAM workspace takes about 100 bytes per base)
+    const size_t by_bases = (size_t)((total_bases_ + MAX_PART_BASES - 1) / MAX_PART_BASES);
+    n_parts_ = std::max<size_t>(1, std::min<size_t>(std::max<size_t>(parts_target_, by_bases), nchunks / 4));
     while (parts_.size() < n_parts_) parts_.push_back(std::make_unique<Part>());
     // the first part is half the size of the others, so that the policy threads and the
     // first extension wave start sooner
@@ -534,7 +553,7 @@ void Mapper::map_uploaded(sa_output* out) {
     // output buffer sized from the previous batch (large batches only)
     so_ = StreamOut();
     const size_t est = (size_t)(bytes_per_record_ * 1.15 * (double)nrec) + ((size_t)1 << 20);
-    if (bytes_per_record_ > 0 && est >= OutputPool::LARGE) {
+    if (overlap_ && bytes_per_record_ > 0 && est >= OutputPool::LARGE) {
         so_.cap = (est + OutputPool::LARGE - 1) / OutputPool::LARGE * OutputPool::LARGE;
         so_.dst = alloc_output(so_.cap + 1);
         so_.off.assign(chunks.size() + 1, 0);

@@ -11,6 +11,7 @@ namespace sa {
 
 class Mapper {
   public:
+    static constexpr uint64_t MAX_PART_BASES = 1ULL << 27;
     Mapper(const sa_index* idx, const sa_refs* refs, const sa_chaining_params& cp, const sa_mapping_params& mp);
     ~Mapper();
     void map(const sa_read_batch* r1, const sa_read_batch* r2, sa_output* out);
@@ -40,6 +41,10 @@ class Mapper {
     void set_parts(uint32_t n) { parts_target_ = n ? n : 1; }
     void set_wave_min_jobs(uint64_t n) { wave_min_jobs_ = n; }
     void set_max_wave_jobs(uint64_t n) { max_wave_jobs_ = n ? n : 1; }
+    // false: stage-synchronous (plain) form: the policy and the extension waves
+    // alternate, every waiting request goes into the waves before any chunk resumes,
+    // and the output is gathered after the last chunk
+    void set_overlap(bool on) { overlap_ = on; }
 
   private:
     // One NAM-pipeline part of a batch: a run of whole chunks with their reads' NAMs on
@@ -75,6 +80,7 @@ class Mapper {
     unsigned policy_threads_ = std::max(1u, std::thread::hardware_concurrency());
     uint64_t wave_min_jobs_ = 32768;
     uint64_t max_wave_jobs_ = 262144;
+    bool overlap_ = true;
     bool trace_ = false;
 
     const sa_index* idx_;

@@ -309,6 +309,28 @@ def test_mapping_is_independent_of_parts(sa, synth):
     assert sa.Mapper(idx, refs).map(empty, empty) == b""
 
 
+def test_plain_schedule_matches_batched_engine(sa, synth):
+    # the stage-synchronous form (overlap = 0: NAM parts one after another, then policy
+    # and waves taking turns, small waves) maps to the same bytes as the batched engine
+    # and the oracle, paired-end and single-end
+    refs, idx = _index(sa, synth["fa"])
+    r1 = sa.Reads.from_file(synth["f1"])
+    r2 = sa.Reads.from_file(synth["f2"])
+    se = sa.Reads.from_file(synth["fse"])
+    want = run_oracle_cli(["--no-PG", "--chunk-size=20000", synth["fa"], synth["f1"], synth["f2"]])
+    want = want[len(sa.sam_header(refs)):]
+    for r in ((r1, r2), (se, None)):
+        outs = []
+        for overlap, parts, max_wave in ((True, 4, 0), (False, 1, 0), (False, 3, 500)):
+            m = sa.Mapper(idx, refs, chunk_size=20000)
+            m.set_schedule(parts=parts, overlap=overlap, max_wave_jobs=max_wave)
+            outs.append(m.map(*r))
+            outs.append(m.map(*r))  # the same mapper again (pooled buffers)
+        assert all(o == outs[0] for o in outs) and outs[0]
+        if r[1] is not None:
+            assert outs[0] == want, _first_diff(outs[0], want)
+
+
 def test_synthetic_paired_end_small_chunks_matches_oracle(sa, synth):
     # many chunks: the per-chunk RNG and insert-size restarts are exercised
     want = run_oracle_cli(["--no-PG", "--chunk-size=20000", synth["fa"], synth["f1"], synth["f2"]])
