@@ -514,12 +514,12 @@ def main():
     # parity: the batch once more, its bytes against the oracle's (rank 0 only)
     parity = cpu = None
     if rank == 0 and args.parity == "full":
-        gpu_sam = mapper.map_uploaded(copy=True)
         try:
+            gpu_sam = mapper.map_uploaded(copy=True)
             parity, cpu = parity_leg(g, r1, r2, read_length, index, gpu_sam, use_ssw, os.cpu_count() or 1)
+            del gpu_sam
         except Exception as e:  # reported, never fatal for the GPU line
-            parity = {"identical": None, "error": str(e)[:300]}
-        del gpu_sam
+            parity = {"identical": None, "error": f"{type(e).__name__}: {str(e)[:300]}"}
     if rank != 0:
         pg.destroy_process_group()
         return

@@ -257,6 +257,52 @@ int32_t sa_align_batch(const sa_mapping_params* mp, size_t n, const char* querie
                        const char* refs, const uint64_t* ref_offsets, sa_alignment* out, uint32_t* cigar,
                        size_t cigar_capacity);
 
+/* Stage entry points on caller-given bytes, for parity tests against the reference's
+ * unit vectors.  They run the device functions of the mapping path's extension
+ * kernels on (query, reference) pairs given here instead of on a batch's reads and
+ * the index's reference.  Host buffers; synchronous; CIGAR ops in the reference
+ * encoding len << 4 | op (src/cigar.rs:5-16), =/X form, at
+ * cigar[cigar_offset .. + cigar_len).  score is signed: global pieces can score
+ * below zero.  SA_ERR_INVALID when cigar_capacity is too small (sum over items of
+ * |query| + |reference| + 4 always suffices). */
+typedef struct {
+    int32_t valid; /* 0 where the reference returns None */
+    int32_t score;
+    uint32_t query_start, query_end, ref_start, ref_end;
+    uint32_t edit_distance;
+    uint32_t cigar_offset, cigar_len;
+} sa_stage_alignment;
+/* kind 0: hamming_align (src/aligner.rs:218-259; its segment is
+ * highest_scoring_segment, :180-216), kind 1: hamming_align_global (:261-291).  Scores
+ * from mp (match, mismatch, end_bonus); NULL = defaults. */
+int32_t sa_hamming_batch(const sa_mapping_params* mp, size_t n, const uint32_t* kinds, const char* queries,
+                         const uint64_t* query_offsets, const char* refs, const uint64_t* ref_offsets,
+                         sa_stage_alignment* out, uint32_t* cigar, size_t cigar_capacity);
+/* One piece of single-end piecewise extension per item (src/piecewisealigner.rs):
+ * kind 0 global_alignment (:68-130), kind 1 xdrop_alignment GlobalStartLocalEnd (the
+ * piece after the last anchor), kind 2 xdrop_alignment LocalStartGlobalEnd (the piece
+ * before the first anchor) (:132-240).  The pieces are full affine DPs (the
+ * reference's block-aligner 0.5.1 runs them in adaptive blocks; x-drop does not
+ * trigger on reads of up to 2048 nt at the default x-drop of 500). */
+int32_t sa_piecewise_pieces(const sa_mapping_params* mp, size_t n, const uint32_t* kinds, const char* queries,
+                            const uint64_t* query_offsets, const char* refs, const uint64_t* ref_offsets,
+                            sa_stage_alignment* out, uint32_t* cigar, size_t cigar_capacity);
+/* remove_spurious_anchors (src/piecewisealigner.rs:596-719) on n chains in place.
+ * anchors: (query_start, ref_start) int32 pairs, chain t at pairs [offsets[t],
+ * offsets[t+1]); out_counts[t] = anchors kept (the first out_counts[t] pairs of the
+ * chain's range). */
+int32_t sa_remove_spurious_anchors(size_t n, int32_t* anchors, const uint64_t* offsets, uint32_t* out_counts);
+/* extend_piecewise (src/piecewisealigner.rs:396-510) per item, with
+ * remove_spurious_anchors first, as single-end mapping runs it: query against the
+ * reference window, anchors (query_start, ref_start in the window) u32 pairs listed
+ * last to first at pairs [anchor_offsets[i], anchor_offsets[i+1]) (at least one),
+ * k the seeding k-mer length, padding = |query| / 10 (src/mapper.rs:586-593).  Scores
+ * from mp. */
+int32_t sa_piecewise_batch(const sa_mapping_params* mp, uint32_t k, size_t n, const char* queries,
+                           const uint64_t* query_offsets, const char* refs, const uint64_t* ref_offsets,
+                           const uint32_t* anchors, const uint64_t* anchor_offsets, sa_stage_alignment* out,
+                           uint32_t* cigar, size_t cigar_capacity);
+
 /* ---------------------------------------------------------------- mapping */
 typedef struct sa_mapper sa_mapper;
 /* The mapper keeps the index and per-batch arenas resident on the device. */

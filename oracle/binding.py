@@ -105,7 +105,9 @@ class OracleIndex:
         if r != 0:
             raise RuntimeError(f"ora_map_batch failed ({r})")
         try:
-            data = C.string_at(out.value, n.value) if n.value else b""
+            m = n.value
+            data = (C.string_at(out.value, m) if m < (1 << 31) else
+                    np.ctypeslib.as_array((C.c_uint8 * m).from_address(out.value)).tobytes()) if m else b""
         finally:
             lib().ora_output_free(out)
         return data, sec.value

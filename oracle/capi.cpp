@@ -295,4 +295,131 @@ int32_t ora_nams(void* h, const char* seq, size_t len, int32_t mcs, uint32_t res
     return 0;
 }
 
+// ---- unit-vector entry points (the reference's own unit tests, tests/golden/unit_vectors.json)
+struct ora_stage {
+    int32_t valid, score;
+    uint32_t query_start, query_end, ref_start, ref_end, edit_distance, cigar_len;
+};
+
+static int32_t put_cigar(const Cigar& c, uint32_t* cigar, size_t cap, ora_stage* o) {
+    o->cigar_len = (uint32_t)c.ops.size();
+    if (c.ops.size() > cap) return -1;
+    for (size_t i = 0; i < c.ops.size(); i++) cigar[i] = c.ops[i];
+    return 0;
+}
+
+uint64_t ora_xxh64(uint64_t x) { return xxh64(x); }
+
+// SyncmerParameters::pick_bits (src/indexer.rs:294-300) for a FASTA's contigs
+uint32_t ora_pick_bits(const char* fasta, uint32_t k, uint32_t s) {
+    std::vector<RefSeq> refs;
+    std::string err;
+    if (!read_fasta(fasta, refs, err)) return 0;
+    SeedingParameters p;
+    p.k = k;
+    p.s = s;
+    return pick_bits(refs, p);
+}
+
+// kind 0 hamming_align, 1 hamming_align_global (src/aligner.rs:218-291)
+int32_t ora_hamming(int32_t kind, const char* q, size_t ql, const char* r, size_t rl, uint8_t match, uint8_t mismatch,
+                    uint32_t end_bonus, ora_stage* o, uint32_t* cigar, size_t cap) {
+    std::memset(o, 0, sizeof(*o));
+    std::string a(q, ql), b(r, rl);
+    AlignmentInfo h;
+    if (kind == 0) {
+        std::optional<AlignmentInfo> x = hamming_align(a, b, match, mismatch, end_bonus);
+        if (!x) return 0;
+        h = *x;
+    } else {
+        h = hamming_align_global(a, b, match, mismatch);
+    }
+    o->valid = 1;
+    o->score = (int32_t)h.score;
+    o->query_start = (uint32_t)h.query_start;
+    o->query_end = (uint32_t)h.query_end;
+    o->ref_start = (uint32_t)h.ref_start;
+    o->ref_end = (uint32_t)h.ref_end;
+    o->edit_distance = (uint32_t)h.edit_distance;
+    return put_cigar(h.cigar, cigar, cap, o);
+}
+
+// one piecewise DP piece: kind 0 global, 1 xdrop GlobalStartLocalEnd, 2 LocalStartGlobalEnd
+int32_t ora_piece(int32_t kind, const char* q, size_t ql, const char* r, size_t rl, uint8_t match, uint8_t mismatch,
+                  uint8_t gap_open, uint8_t gap_extend, uint32_t end_bonus, ora_stage* o, uint32_t* cigar,
+                  size_t cap) {
+    Scores sc;
+    sc.match = match;
+    sc.mismatch = mismatch;
+    sc.gap_open = gap_open;
+    sc.gap_extend = gap_extend;
+    sc.end_bonus = end_bonus;
+    PieceResult p = piecewise_piece(kind, std::string(q, ql), std::string(r, rl), sc);
+    std::memset(o, 0, sizeof(*o));
+    o->valid = 1;
+    o->score = p.score;
+    o->query_start = (uint32_t)p.query_start;
+    o->query_end = (uint32_t)p.query_end;
+    o->ref_start = (uint32_t)p.ref_start;
+    o->ref_end = (uint32_t)p.ref_end;
+    o->edit_distance = (uint32_t)p.cigar.edit_distance();
+    return put_cigar(p.cigar, cigar, cap, o);
+}
+
+// remove_spurious_anchors on (query_start, ref_start) pairs in place; returns the count kept
+uint32_t ora_remove_spurious_anchors(int32_t* pairs, uint32_t n) {
+    std::vector<Anchor> a(n);
+    for (uint32_t i = 0; i < n; i++) a[i] = Anchor{0, (size_t)pairs[2 * i + 1], (size_t)pairs[2 * i]};
+    remove_spurious_anchors(a);
+    for (size_t i = 0; i < a.size(); i++) {
+        pairs[2 * i] = (int32_t)a[i].query_start;
+        pairs[2 * i + 1] = (int32_t)a[i].ref_start;
+    }
+    return (uint32_t)a.size();
+}
+
+// extend_piecewise with remove_spurious_anchors first, as the mapper runs it
+// (src/mapper.rs:586-593); anchors (query_start, ref_start) pairs last to first
+int32_t ora_extend_piecewise(const char* q, size_t ql, const char* r, size_t rl, const uint32_t* pairs, uint32_t n,
+                             uint32_t k, uint32_t padding, uint8_t match, uint8_t mismatch, uint8_t gap_open,
+                             uint8_t gap_extend, uint32_t end_bonus, int32_t xdrop, int32_t prune, ora_stage* o,
+                             uint32_t* cigar, size_t cap) {
+    Scores sc;
+    sc.match = match;
+    sc.mismatch = mismatch;
+    sc.gap_open = gap_open;
+    sc.gap_extend = gap_extend;
+    sc.end_bonus = end_bonus;
+    std::vector<Anchor> a(n);
+    for (uint32_t i = 0; i < n; i++) a[i] = Anchor{0, pairs[2 * i + 1], pairs[2 * i]};
+    if (prune) remove_spurious_anchors(a);
+    std::memset(o, 0, sizeof(*o));
+    std::optional<AlignmentInfo> x = extend_piecewise(std::string(q, ql), std::string(r, rl), a, padding, k, sc, xdrop);
+    if (!x) return 0;
+    o->valid = 1;
+    o->score = (int32_t)x->score;
+    o->query_start = (uint32_t)x->query_start;
+    o->query_end = (uint32_t)x->query_end;
+    o->ref_start = (uint32_t)x->ref_start;
+    o->ref_end = (uint32_t)x->ref_end;
+    o->edit_distance = (uint32_t)x->edit_distance;
+    return put_cigar(x->cigar, cigar, cap, o);
+}
+
+// collinear_chaining's best score (src/chainer.rs:85-180) on (ref_id, ref_start,
+// query_start) triples with the default chaining parameters
+float ora_chain_best_score(const uint64_t* triples, size_t n, uint32_t k, uint64_t max_ref_gap) {
+    std::vector<Anchor> a(n);
+    for (size_t i = 0; i < n; i++) a[i] = Anchor{triples[3 * i], triples[3 * i + 1], triples[3 * i + 2]};
+    ChainingParameters cp;
+    std::vector<float> dp;
+    std::vector<size_t> pred;
+    size_t bi;
+    return collinear_chaining(a, k, max_ref_gap, cp, dp, pred, bi);
+}
+
+int32_t ora_has_shared_substring(const char* read, size_t rl, const char* ref, size_t fl, uint32_t k) {
+    return has_shared_substring(std::string(read, rl), std::string(ref, fl), k) ? 1 : 0;
+}
+
 }  // extern "C"

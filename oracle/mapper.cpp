@@ -512,7 +512,7 @@ static float top_dropoff(const std::vector<Nam>& nams) {
 }
 
 // src/mapper.rs:1157-1168
-static bool has_shared_substring(const std::string& read, const std::string& ref, size_t k) {
+bool has_shared_substring(const std::string& read, const std::string& ref, size_t k) {
     size_t sub = 2 * k / 3, step = k / 3;
     size_t lim = read.size() > sub ? read.size() - sub : 0;
     for (size_t i = 0; i < lim; i += step) {

@@ -255,16 +255,16 @@ std::vector<Anchor> hits_to_anchors(const std::vector<Hit>& hits, const Index& i
     return a;
 }
 
-// src/chainer.rs:85-180 (collinear_chaining) + :386-449 (extract_chains)
-static void chain_and_extract(std::vector<Anchor>& anchors, size_t read_len, size_t k, const ChainingParameters& cp,
-                              bool is_revcomp, std::vector<Nam>& chains) {
+// src/chainer.rs:85-180 (collinear_chaining): dp[i] the best chain score ending at
+// anchor i, pred[i] its predecessor; returns the best score (best_index its anchor).
+float collinear_chaining(const std::vector<Anchor>& anchors, size_t k, size_t max_ref_gap,
+                         const ChainingParameters& cp, std::vector<float>& dp, std::vector<size_t>& pred,
+                         size_t& best_index) {
     size_t n = anchors.size();
-    if (n == 0) return;
-    size_t max_ref_gap = cp.has_max_ref_gap ? cp.max_ref_gap : read_len;
-    std::vector<float> dp(n, (float)k);
-    std::vector<size_t> pred(n, SIZE_MAX);
+    dp.assign(n, (float)k);
+    pred.assign(n, SIZE_MAX);
     float best_score = 0.0f;
-    size_t best_index = SIZE_MAX;
+    best_index = SIZE_MAX;
     for (size_t i = 0; i < n; i++) {
         size_t lookup_end = i > cp.max_lookback ? i - cp.max_lookback : 0;
         const Anchor& ai = anchors[i];
@@ -305,6 +305,20 @@ static void chain_and_extract(std::vector<Anchor>& anchors, size_t read_len, siz
             best_index = i;
         }
     }
+    return best_score;
+}
+
+// src/chainer.rs:386-449 (extract_chains) after collinear_chaining
+static void chain_and_extract(std::vector<Anchor>& anchors, size_t read_len, size_t k, const ChainingParameters& cp,
+                              bool is_revcomp, std::vector<Nam>& chains) {
+    size_t n = anchors.size();
+    if (n == 0) return;
+    size_t max_ref_gap = cp.has_max_ref_gap ? cp.max_ref_gap : read_len;
+    std::vector<float> dp;
+    std::vector<size_t> pred;
+    size_t best_index;
+    float best_score = collinear_chaining(anchors, k, max_ref_gap, cp, dp, pred, best_index);
+    (void)best_index;
     float valid = best_score * cp.valid_score_threshold;
     std::vector<std::pair<size_t, float>> cand;
     for (size_t i = 0; i < n; i++)

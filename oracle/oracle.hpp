@@ -183,6 +183,9 @@ struct Details {
 };
 
 float chaining_score(size_t dq, size_t dr, size_t k, const ChainingParameters& cp);
+float collinear_chaining(const std::vector<Anchor>& anchors, size_t k, size_t max_ref_gap,
+                         const ChainingParameters& cp, std::vector<float>& dp, std::vector<size_t>& pred,
+                         size_t& best_index);
 
 void find_hits(const std::vector<QueryRandstrobe>& qr, const Index& idx, Mcs mcs, size_t filter_cutoff,
                size_t rescue_distance, HitsDetails& details, std::vector<Hit>& hits);
@@ -315,6 +318,15 @@ std::vector<std::string> map_records(const Context& ctx, const std::vector<Seque
                                      size_t chunk_size, std::vector<double>* abundances);
 
 // Piecewise single-end extension (src/piecewisealigner.rs); block-aligner restated.
+// One DP piece: kind 0 global_alignment, 1 xdrop GlobalStartLocalEnd, 2 xdrop
+// LocalStartGlobalEnd (signed score).
+struct PieceResult {
+    int32_t score = 0;
+    size_t query_start = 0, query_end = 0, ref_start = 0, ref_end = 0;
+    Cigar cigar;
+};
+PieceResult piecewise_piece(int kind, const std::string& q, const std::string& r, const Scores& sc);
+bool has_shared_substring(const std::string& read, const std::string& ref, size_t k);  // src/mapper.rs:1157-1168
 void remove_spurious_anchors(std::vector<Anchor>& anchors);
 std::optional<AlignmentInfo> extend_piecewise(const std::string& query, const std::string& ref,
                                               const std::vector<Anchor>& anchors, size_t padding, size_t k,

@@ -3,9 +3,11 @@
 // the block-aligner 0.5.1 crate (global alignment with a fixed block covering the
 // whole matrix, and an x-drop "global start / local end" alignment with a
 // position-specific end bonus).  The crate is not available here; both kernels are
-// restated as full affine-gap Gotoh DPs with a diagonal-first traceback.  Where the
-// crate's adaptive band or traceback tie rules differ, results can differ:
-// PARITY UNPINNED beyond the reference's golden cases.
+// restated as full affine-gap Gotoh DPs whose traceback takes a deletion, then an
+// insertion, before the diagonal on ties -- the order the reference's 30 piecewise unit
+// vectors (tests/golden/unit_vectors.json) agree with; the deletion-vs-insertion order
+// is not pinned by any vector.  Where the crate's adaptive blocks or tie rules differ
+// otherwise, results can differ: PARITY UNPINNED beyond those vectors and the goldens.
 #include "oracle.hpp"
 
 #include <algorithm>
@@ -70,13 +72,16 @@ static void affine_dp(size_t n, size_t m, Sub sub, int32_t go, int32_t ge, bool 
     ops_rev.clear();
     while (i > 0 || j > 0) {
         if (state == 0) {
-            if (i > 0 && j > 0 && H[at(i, j)] == H[at(i - 1, j - 1)] + sub(i - 1, j - 1)) {
+            // gaps before the diagonal, deletion first: a gap that ties with matches
+            // goes to the end of the run, as the reference's extend_piecewise_complex
+            // vector (src/piecewisealigner.rs:1672-1710) requires
+            if (j > 0 && H[at(i, j)] == E[at(i, j)]) {
+                state = 1;
+            } else if (i > 0 && (j == 0 || H[at(i, j)] == F[at(i, j)])) {
+                state = 2;
+            } else {
                 ops_rev.push_back(q[i - 1] == r[j - 1] ? OP_EQ : OP_X);
                 i--; j--;
-            } else if (j > 0 && H[at(i, j)] == E[at(i, j)]) {
-                state = 1;
-            } else {
-                state = 2;
             }
         } else if (state == 1) {
             ops_rev.push_back(OP_D);
@@ -147,6 +152,18 @@ static PwResult xdrop_alignment(const std::string& q0, const std::string& r0, bo
 }
 
 }  // namespace
+
+PieceResult piecewise_piece(int kind, const std::string& q, const std::string& r, const Scores& sc) {
+    PwResult p = kind == 0 ? global_alignment(q, r, sc) : xdrop_alignment(q, r, kind == 1, sc);
+    PieceResult o;
+    o.score = p.score;
+    o.query_start = p.query_start;
+    o.query_end = p.query_end;
+    o.ref_start = p.ref_start;
+    o.ref_end = p.ref_end;
+    o.cigar = p.cigar;
+    return o;
+}
 
 // src/piecewisealigner.rs:596-719
 void remove_spurious_anchors(std::vector<Anchor>& a) {

@@ -38,6 +38,16 @@ def _p(arr, ctype):
     return arr.ctypes.data_as(C.POINTER(ctype))
 
 
+def _bytes(ptr, n: int) -> bytes:
+    """n bytes at ptr (ctypes.string_at takes a C int size, so large buffers go
+    through numpy)."""
+    if not n:
+        return b""
+    if n < (1 << 31):
+        return C.string_at(ptr, n)
+    return np.ctypeslib.as_array((C.c_uint8 * n).from_address(ptr)).tobytes()
+
+
 class SeedingParameters:
     """SeedingParameters (src/seeding/parameters.rs:164-221)."""
 
@@ -211,10 +221,10 @@ class Reads:
             so = np.ctypeslib.as_array(v.seq_offsets, shape=(n + 1,)).copy()
             no = np.ctypeslib.as_array(v.name_offsets, shape=(n + 1,)).copy()
             co = np.ctypeslib.as_array(v.comment_offsets, shape=(n + 1,)).copy()
-            seq = C.string_at(v.seq, int(so[-1])) if so[-1] else b""
-            names = C.string_at(v.names, int(no[-1])) if no[-1] else b""
-            qual = C.string_at(v.qual, int(so[-1])) if v.qual else None
-            comments = C.string_at(v.comments, int(co[-1])) if co[-1] else b""
+            seq = _bytes(v.seq, int(so[-1]))
+            names = _bytes(v.names, int(no[-1]))
+            qual = _bytes(v.qual, int(so[-1])) if v.qual else None
+            comments = _bytes(v.comments, int(co[-1]))
             return cls(seq, so, names, no, qual, comments, co)
         finally:
             lib().sa_reads_free(h)
@@ -337,6 +347,89 @@ def align_batch(queries, refs, mapping: L.MappingParams | None = None):
     return res
 
 
+def _pairs(queries, refs):
+    bq = [q.encode() if isinstance(q, str) else bytes(q) for q in queries]
+    br = [r.encode() if isinstance(r, str) else bytes(r) for r in refs]
+    n = len(bq)
+    qo = np.zeros(n + 1, dtype=np.uint64)
+    qo[1:] = np.cumsum([len(x) for x in bq])
+    ro = np.zeros(n + 1, dtype=np.uint64)
+    ro[1:] = np.cumsum([len(x) for x in br])
+    return b"".join(bq), qo, b"".join(br), ro
+
+
+def _stage_results(out, cig, n) -> list:
+    res = []
+    for i in range(n):
+        a = out[i]
+        if not a.valid:
+            res.append(None)
+            continue
+        ops = cig[a.cigar_offset:a.cigar_offset + a.cigar_len]
+        res.append(dict(score=int(a.score), query_start=int(a.query_start), query_end=int(a.query_end),
+                        ref_start=int(a.ref_start), ref_end=int(a.ref_end), edit_distance=int(a.edit_distance),
+                        cigar=cigar_str(ops)))
+    return res
+
+
+def _stage(fn, kinds, queries, refs, mapping):
+    Q, qo, R, ro = _pairs(queries, refs)
+    n = len(qo) - 1
+    k = np.ascontiguousarray(kinds, dtype=np.uint32)
+    out = (L.StageAlignment * max(n, 1))()
+    cap = int(qo[-1] + ro[-1] + 4 * n + 8)
+    cig = np.zeros(cap, dtype=np.uint32)
+    m = mapping or mapping_defaults()
+    L.check(fn(C.byref(m), n, _p(k, C.c_uint32), C.c_char_p(Q), _p(qo, C.c_uint64), C.c_char_p(R),
+               _p(ro, C.c_uint64), out, _p(cig, C.c_uint32), cap))
+    return _stage_results(out, cig, n)
+
+
+def hamming_batch(queries, refs, kinds, mapping: L.MappingParams | None = None):
+    """hamming_align (kind 0) / hamming_align_global (kind 1) of (query, reference)
+    pairs on the GPU; dicts, or None where the reference returns None."""
+    return _stage(lib().sa_hamming_batch, kinds, queries, refs, mapping)
+
+
+PIECE_GLOBAL, PIECE_AFTER_LAST, PIECE_BEFORE_FIRST = 0, 1, 2
+
+
+def piecewise_pieces(queries, refs, kinds, mapping: L.MappingParams | None = None):
+    """One piecewise-extension piece per pair: global (0), x-drop GlobalStartLocalEnd
+    (1) or LocalStartGlobalEnd (2)."""
+    return _stage(lib().sa_piecewise_pieces, kinds, queries, refs, mapping)
+
+
+def remove_spurious_anchors(chains):
+    """remove_spurious_anchors on chains of (query_start, ref_start) pairs."""
+    off = np.zeros(len(chains) + 1, dtype=np.uint64)
+    off[1:] = np.cumsum([len(c) for c in chains])
+    anc = np.array([v for c in chains for a in c for v in a] or [0], dtype=np.int32)
+    cnt = np.zeros(max(1, len(chains)), dtype=np.uint32)
+    L.check(lib().sa_remove_spurious_anchors(len(chains), _p(anc, C.c_int32), _p(off, C.c_uint64),
+                                             _p(cnt, C.c_uint32)))
+    return [[(int(anc[2 * j]), int(anc[2 * j + 1])) for j in range(int(off[i]), int(off[i]) + int(cnt[i]))]
+            for i in range(len(chains))]
+
+
+def piecewise_batch(queries, refs, anchors, k: int, mapping: L.MappingParams | None = None):
+    """extend_piecewise (with remove_spurious_anchors) per (query, window, anchors last
+    to first as (query_start, ref_start) pairs)."""
+    Q, qo, R, ro = _pairs(queries, refs)
+    n = len(qo) - 1
+    aoff = np.zeros(n + 1, dtype=np.uint64)
+    aoff[1:] = np.cumsum([len(a) for a in anchors])
+    anc = np.array([v for a in anchors for x in a for v in x] or [0], dtype=np.uint32)
+    out = (L.StageAlignment * max(n, 1))()
+    cap = int(2 * qo[-1] + ro[-1] + 4 * n + 8)
+    cig = np.zeros(cap, dtype=np.uint32)
+    m = mapping or mapping_defaults()
+    L.check(lib().sa_piecewise_batch(C.byref(m), k, n, C.c_char_p(Q), _p(qo, C.c_uint64), C.c_char_p(R),
+                                     _p(ro, C.c_uint64), _p(anc, C.c_uint32), _p(aoff, C.c_uint64), out,
+                                     _p(cig, C.c_uint32), cap))
+    return _stage_results(out, cig, n)
+
+
 class Mapper:
     """Maps batches of reads; keeps the index and its device arenas resident."""
 
@@ -358,7 +451,7 @@ class Mapper:
         b2 = r2.c() if r2 is not None else None
         L.check(lib().sa_map_batch(self.h, C.byref(b1), C.byref(b2) if b2 is not None else None, C.byref(o)))
         try:
-            data = (C.string_at(o.data, o.len) if o.len else b"") if copy else o.len
+            data = _bytes(o.data, o.len) if copy else o.len
             self.last = dict(n_reads=o.n_reads, n_mapped=o.n_mapped, n_waves=o.n_waves,
                              n_gpu_launches=o.n_gpu_launches)
             return data
@@ -381,7 +474,7 @@ class Mapper:
                              n_gpu_launches=o.n_gpu_launches)
             if not copy:
                 return o.len
-            return C.string_at(o.data, o.len) if o.len else b""
+            return _bytes(o.data, o.len)
         finally:
             lib().sa_output_free(C.byref(o))
 
@@ -481,7 +574,7 @@ class Session:
                                       _p(ab, C.c_double) if ab is not None else None, len(ab) if ab is not None else 0))
         self._borrowed.pop(ticket, None)
         try:
-            data = (C.string_at(o.data, o.len) if o.len else b"") if copy else o.len
+            data = _bytes(o.data, o.len) if copy else o.len
         finally:
             lib().sa_output_free(C.byref(o))
         stats = {f: getattr(st, f) for f, _ in L.RequestStats._fields_}
@@ -505,6 +598,6 @@ def sam_header(refs: References, cmd_line: str | None = None, rg_id: str | None 
     L.check(lib().sa_sam_header(refs.h, cmd_line.encode() if cmd_line else None, rg_id.encode() if rg_id else None,
                                 arr, len(f), C.byref(o)))
     try:
-        return C.string_at(o.data, o.len)
+        return _bytes(o.data, o.len)
     finally:
         lib().sa_output_free(C.byref(o))

@@ -67,6 +67,11 @@ class AlignmentC(C.Structure):
                 ("ref_end", u32), ("edit_distance", u32), ("cigar_offset", u32), ("cigar_len", u32)]
 
 
+class StageAlignment(C.Structure):
+    _fields_ = [("valid", i32), ("score", i32), ("query_start", u32), ("query_end", u32), ("ref_start", u32),
+                ("ref_end", u32), ("edit_distance", u32), ("cigar_offset", u32), ("cigar_len", u32)]
+
+
 class Output(C.Structure):
     _fields_ = [("data", vp), ("len", sz), ("n_reads", u64), ("n_mapped", u64), ("n_waves", u32),
                 ("n_gpu_launches", u32)]
@@ -144,6 +149,12 @@ SIGNATURES = {
     "sa_mapper_set_profiling": (i32, [vp, i32]),
     "sa_mapper_set_parts": (i32, [vp, u32]),
     "sa_schedule_params_default": (None, [P(ScheduleParams)]),
+    "sa_hamming_batch": (i32, [P(MappingParams), sz, P(u32), vp, P(u64), vp, P(u64), P(StageAlignment), P(u32), sz]),
+    "sa_piecewise_pieces": (i32, [P(MappingParams), sz, P(u32), vp, P(u64), vp, P(u64), P(StageAlignment), P(u32),
+                                  sz]),
+    "sa_remove_spurious_anchors": (i32, [sz, P(i32), P(u64), P(u32)]),
+    "sa_piecewise_batch": (i32, [P(MappingParams), u32, sz, vp, P(u64), vp, P(u64), P(u32), P(u64),
+                                 P(StageAlignment), P(u32), sz]),
     "sa_mapper_set_schedule": (i32, [vp, P(ScheduleParams)]),
 }
 

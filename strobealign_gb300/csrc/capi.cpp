@@ -645,6 +645,105 @@ int32_t sa_align_batch(const sa_mapping_params* mp, size_t n, const char* querie
     SA_CATCH
 }
 
+namespace {
+
+void stage_common(const sa_mapping_params* mp, size_t n, const char* q, const uint64_t* qoff, const char* r,
+                  const uint64_t* roff, std::vector<uint64_t>& qo, std::vector<uint64_t>& ro, AlignScores& sc) {
+    require(n == 0 || (q && qoff && r && roff), "null argument");
+    require(n < (1ull << 31), "too many items");
+    sa_mapping_params m;
+    if (mp) m = *mp;
+    else sa_mapping_params_default(&m);
+    sc = AlignScores{m.match, m.mismatch, m.gap_open, m.gap_extend, m.end_bonus};
+    qo.assign(n + 1, 0);
+    ro.assign(n + 1, 0);
+    for (size_t i = 0; i <= n; i++) {
+        qo[i] = n ? qoff[i] - qoff[0] : 0;
+        ro[i] = n ? roff[i] - roff[0] : 0;
+        if (i && i <= n) require(qoff[i] >= qoff[i - 1] && roff[i] >= roff[i - 1], "offsets must not decrease");
+        if (i < n) require(qoff[i + 1] - qoff[i] <= MAX_READ_LEN, "query too long");
+    }
+}
+
+}  // namespace
+
+int32_t sa_hamming_batch(const sa_mapping_params* mp, size_t n, const uint32_t* kinds, const char* queries,
+                         const uint64_t* query_offsets, const char* refs, const uint64_t* ref_offsets,
+                         sa_stage_alignment* out, uint32_t* cigar, size_t cigar_capacity) {
+    SA_TRY
+    std::vector<uint64_t> qo, ro;
+    AlignScores sc;
+    stage_common(mp, n, queries, query_offsets, refs, ref_offsets, qo, ro, sc);
+    if (n == 0) return SA_OK;
+    require(kinds && out && cigar, "null argument");
+    for (size_t i = 0; i < n; i++) require(kinds[i] <= 1, "kind must be 0 or 1");
+    static_assert(sizeof(sa_stage_alignment) == sizeof(StageAlignment), "stage alignment layout");
+    stage_hamming((uint32_t)n, kinds, (const uint8_t*)queries + query_offsets[0], qo.data(),
+                  (const uint8_t*)refs + ref_offsets[0], ro.data(), sc, reinterpret_cast<StageAlignment*>(out), cigar,
+                  cigar_capacity, 0);
+    return SA_OK;
+    SA_CATCH
+}
+
+int32_t sa_piecewise_pieces(const sa_mapping_params* mp, size_t n, const uint32_t* kinds, const char* queries,
+                            const uint64_t* query_offsets, const char* refs, const uint64_t* ref_offsets,
+                            sa_stage_alignment* out, uint32_t* cigar, size_t cigar_capacity) {
+    SA_TRY
+    std::vector<uint64_t> qo, ro;
+    AlignScores sc;
+    stage_common(mp, n, queries, query_offsets, refs, ref_offsets, qo, ro, sc);
+    if (n == 0) return SA_OK;
+    require(kinds && out && cigar, "null argument");
+    require(sc.gap_open >= sc.gap_extend, "gap_open must be at least gap_extend");
+    for (size_t i = 0; i < n; i++) {
+        require(kinds[i] <= 2, "kind must be 0, 1 or 2");
+        require(ro[i + 1] - ro[i] <= 4 * MAX_READ_LEN, "reference piece too long");
+    }
+    stage_pieces((uint32_t)n, kinds, (const uint8_t*)queries + query_offsets[0], qo.data(),
+                 (const uint8_t*)refs + ref_offsets[0], ro.data(), sc, reinterpret_cast<StageAlignment*>(out), cigar,
+                 cigar_capacity, 0);
+    return SA_OK;
+    SA_CATCH
+}
+
+int32_t sa_remove_spurious_anchors(size_t n, int32_t* anchors, const uint64_t* offsets, uint32_t* out_counts) {
+    SA_TRY
+    if (n == 0) return SA_OK;
+    require(anchors && offsets && out_counts, "null argument");
+    require(offsets[0] == 0, "offsets must start at 0");
+    for (size_t i = 0; i < n; i++) require(offsets[i + 1] >= offsets[i], "offsets must not decrease");
+    stage_prune((uint32_t)n, anchors, offsets, out_counts, 0);
+    return SA_OK;
+    SA_CATCH
+}
+
+int32_t sa_piecewise_batch(const sa_mapping_params* mp, uint32_t k, size_t n, const char* queries,
+                           const uint64_t* query_offsets, const char* refs, const uint64_t* ref_offsets,
+                           const uint32_t* anchors, const uint64_t* anchor_offsets, sa_stage_alignment* out,
+                           uint32_t* cigar, size_t cigar_capacity) {
+    SA_TRY
+    std::vector<uint64_t> qo, ro;
+    AlignScores sc;
+    stage_common(mp, n, queries, query_offsets, refs, ref_offsets, qo, ro, sc);
+    if (n == 0) return SA_OK;
+    require(anchors && anchor_offsets && out && cigar, "null argument");
+    require(k >= 1 && k <= 32, "k out of range");
+    require(sc.gap_open >= sc.gap_extend, "gap_open must be at least gap_extend");
+    require(anchor_offsets[0] == 0, "anchor offsets must start at 0");
+    for (size_t i = 0; i < n; i++) {
+        const uint64_t L = qo[i + 1] - qo[i], W = ro[i + 1] - ro[i];
+        require(anchor_offsets[i + 1] > anchor_offsets[i], "every item needs at least one anchor");
+        require(W <= 4 * MAX_READ_LEN, "reference window too long");
+        for (uint64_t a = anchor_offsets[i]; a < anchor_offsets[i + 1]; a++)
+            require(anchors[2 * a] + k <= L && anchors[2 * a + 1] + k <= W, "anchor outside its query or window");
+    }
+    stage_piecewise((uint32_t)n, (const uint8_t*)queries + query_offsets[0], qo.data(),
+                    (const uint8_t*)refs + ref_offsets[0], ro.data(), anchors, anchor_offsets, k, sc,
+                    reinterpret_cast<StageAlignment*>(out), cigar, cigar_capacity, 0);
+    return SA_OK;
+    SA_CATCH
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------- serving

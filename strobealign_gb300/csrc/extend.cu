@@ -282,6 +282,42 @@ struct CigarWriter {
     __device__ void finish() { close_run(); }
 };
 
+// highest_scoring_segment (src/aligner.rs:180-216): the best-scoring ungapped segment
+// of a query against an equal-length reference (eq(i): base i matches), with the end
+// bonus once for each query end the segment reaches.  Returns the score; [bs, be) is
+// the segment.
+template <class EQ>
+__device__ __forceinline__ int32_t highest_scoring_segment(EQ eq, uint32_t L, const AlignScores& sc, uint32_t& bs,
+                                                           uint32_t& be) {
+    int32_t score = (int32_t)sc.end_bonus, best = 0;
+    uint32_t start = 0;
+    bs = be = 0;
+    for (uint32_t i = 0; i < L; i++) {
+        score += eq(i) ? (int32_t)sc.match : -(int32_t)sc.mismatch;
+        if (score < 0) { start = i + 1; score = 0; }
+        if (score > best) { bs = start; best = score; be = i + 1; }
+    }
+    if (score + (int32_t)sc.end_bonus > best) {
+        best = score + (int32_t)sc.end_bonus;
+        be = L;
+        bs = start;
+    }
+    return best;
+}
+
+// The =/X CIGAR of [bs, be) (hamming_align, src/aligner.rs:233-248); returns the mismatches.
+template <class EQ>
+__device__ __forceinline__ uint32_t hamming_cigar(EQ eq, uint32_t bs, uint32_t be, CigarWriter& w) {
+    uint32_t mm = 0;
+    for (uint32_t i = bs; i < be; i++) {
+        const bool e = eq(i);
+        mm += !e;
+        w.push(e ? 7u : 8u, 1);
+    }
+    w.finish();
+    return mm;
+}
+
 // Thread per job: the Hamming path (hamming_align, src/aligner.rs:181-259), or the
 // SSW / piecewise job's query and reference window bytes copied into the arena.
 __global__ void k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict__ seq, const uint64_t* __restrict__ off,
@@ -298,27 +334,11 @@ __global__ void k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict
         const uint32_t L = p.qlen;
         if (p.type == 1) {
             // hamming_align (src/aligner.rs:181-259)
-            int32_t score = (int32_t)sc.end_bonus, best = 0;
-            uint32_t start = 0, bs = 0, be = 0;
-            for (uint32_t i = 0; i < L; i++) {
-                bool eq = read_char(s, L, i, p.rc) == ref_base(R, p.ref_id, p.wstart + i);
-                score += eq ? (int32_t)sc.match : -(int32_t)sc.mismatch;
-                if (score < 0) { start = i + 1; score = 0; }
-                if (score > best) { bs = start; best = score; be = i + 1; }
-            }
-            if (score + (int32_t)sc.end_bonus > best) {
-                best = score + (int32_t)sc.end_bonus;
-                be = L;
-                bs = start;
-            }
+            auto eq = [&](uint32_t i) { return read_char(s, L, i, p.rc) == ref_base(R, p.ref_id, p.wstart + i); };
+            uint32_t bs, be;
+            const int32_t best = highest_scoring_segment(eq, L, sc, bs, be);
             CigarWriter w{cigar + p.cigar_off, 0, p.cigar_cap, false};
-            uint32_t mm = 0;
-            for (uint32_t i = bs; i < be; i++) {
-                bool eq = read_char(s, L, i, p.rc) == ref_base(R, p.ref_id, p.wstart + i);
-                mm += !eq;
-                w.push(eq ? 7u : 8u, 1);
-            }
-            w.finish();
+            const uint32_t mm = hamming_cigar(eq, bs, be, w);
             ExtResult r = res[t];
             r.valid = w.overflow ? 0 : 1;
             r.score = (uint32_t)best;
@@ -2076,9 +2096,10 @@ __global__ void k_finalize(const SswTask* tasks, const uint32_t* n_tasks_ptr, co
 // ------------------------------------------------------------------ piecewise (single end)
 // extend_piecewise (src/piecewisealigner.rs:396-510) with remove_spurious_anchors
 // (:596-719), warp per job.  The reference runs its DP pieces with the block-aligner
-// crate; they are computed here as full affine-gap DPs with the traceback tie rules of
-// the oracle's restatement (diagonal first, then the gap that produced H), which makes
-// this path parity-unpinned beyond the reference's golden cases.
+// crate; they are computed here as full affine-gap DPs whose traceback takes a
+// deletion, then an insertion, before the diagonal on ties -- the order the reference's
+// piecewise unit vectors agree with.  Beyond those vectors and the goldens this path is
+// parity-unpinned.
 //
 // A piece's DP runs row by row on the warp, the columns in chunks of 32 lanes: F and
 // the diagonal come from the previous row (shared memory), and the row's E chain
@@ -2086,7 +2107,7 @@ __global__ void k_finalize(const SswTask* tasks, const uint32_t* n_tasks_ptr, co
 // lanes (exact for gap_open >= gap_extend, since H(j-1) = max(that, E(j-1))).  Each cell
 // keeps four direction bits for the traceback.
 constexpr int PW_NEG = -(1 << 28);
-constexpr uint8_t PW_DIAG = 1, PW_FROM_E = 2, PW_EEXT = 4, PW_FEXT = 8;
+constexpr uint8_t PW_DIAG = 1, PW_FROM_E = 2, PW_EEXT = 4, PW_FEXT = 8, PW_FROM_F = 16;
 
 struct PwPiece {
     int score;
@@ -2168,6 +2189,7 @@ __device__ PwPiece pw_dp(const uint8_t* q, int n, const uint8_t* r, int m, const
                 uint8_t d = 0;
                 if (H == D) d |= PW_DIAG;
                 if (H == E) d |= PW_FROM_E;
+                if (H == F) d |= PW_FROM_F;
                 if (eext) d |= PW_EEXT;
                 if (fext) d |= PW_FEXT;
                 dirs[(size_t)i * W + j] = d;
@@ -2216,14 +2238,17 @@ __device__ PwPiece pw_dp(const uint8_t* q, int n, const uint8_t* r, int m, const
         for (int it = 0; (i > 0 || j > 0) && it < limit; it++) {
             const uint8_t d = dirs[(size_t)i * W + j];
             if (state == 0) {
-                if (i > 0 && j > 0 && (d & PW_DIAG)) {
+                // a deletion, then an insertion, before the diagonal on ties: a gap
+                // that ties with matches goes to the end of the run (the reference's
+                // extend_piecewise_complex vector, src/piecewisealigner.rs:1672-1710)
+                if (j > 0 && (d & PW_FROM_E)) {
+                    state = 1;
+                } else if (i > 0 && (j == 0 || (d & PW_FROM_F))) {
+                    state = 2;
+                } else {
                     ops[nops++] = qv(i - 1) == rv(j - 1) ? 7 : 8;  // = / X
                     i--;
                     j--;
-                } else if (j > 0 && (d & PW_FROM_E)) {
-                    state = 1;
-                } else {
-                    state = 2;
                 }
             } else if (state == 1) {
                 ops[nops++] = 2;  // D
@@ -2244,6 +2269,71 @@ __device__ PwPiece pw_dp(const uint8_t* q, int n, const uint8_t* r, int m, const
     res.nops = __shfl_sync(FULLM, res.nops, 0);
     __syncwarp();
     return res;
+}
+
+// remove_spurious_anchors (src/piecewisealigner.rs:596-719) on anchors held as
+// (query start, reference start) int pairs, in place; na is updated.  Serial (one
+// thread): the first pass erases the anchors between two cancelling indels, the second
+// the chain ends (up to ceil(20%) of the anchors on each side) up to an indel.
+__device__ void prune_spurious_anchors(int* anc, int& na) {
+    auto erase = [&](int from, int to) {  // [from, to)
+        for (int x = to; x < na; x++) {
+            anc[2 * (x - (to - from))] = anc[2 * x];
+            anc[2 * (x - (to - from)) + 1] = anc[2 * x + 1];
+        }
+        na -= to - from;
+    };
+    if (na < 2) return;
+    const long long tol = 5;
+    long long tracked = 0;
+    bool has_dev = false;
+    int dev = 0, i = 1;
+    while (i < na) {
+        const long long qd = (long long)anc[2 * (i - 1)] - anc[2 * i];
+        const long long rd = (long long)anc[2 * (i - 1) + 1] - anc[2 * i + 1];
+        const long long indel = qd - rd;
+        if ((indel < 0 ? -indel : indel) > tol) {
+            const long long tt = tracked + indel;
+            if (has_dev && (tt < 0 ? -tt : tt) <= tol) {
+                erase(dev, i);
+                i = dev;
+                has_dev = false;
+                tracked = 0;
+                continue;
+            }
+            has_dev = true;
+            dev = i;
+            tracked = indel;
+        }
+        i++;
+    }
+    const int max_prune = (int)ceilf(__fmul_rn((float)na, 0.20f));
+    const int lim = na < max_prune ? na : max_prune;
+    for (int x = 1; x < lim; x++) {
+        const long long qd = (long long)anc[2 * x] - anc[2 * (x - 1)];
+        const long long rd = (long long)anc[2 * x + 1] - anc[2 * (x - 1) + 1];
+        if (qd - rd != 0) {
+            erase(0, x);
+            break;
+        }
+    }
+    const int lo = (na > max_prune ? na - max_prune : 0) + 1;
+    for (int x = na; x-- > lo;) {
+        const long long qd = (long long)anc[2 * x] - anc[2 * (x - 1)];
+        const long long rd = (long long)anc[2 * x + 1] - anc[2 * (x - 1) + 1];
+        if (qd - rd != 0) {
+            erase(x, na);
+            break;
+        }
+    }
+}
+
+// hamming_align_global's score (src/aligner.rs:261-291): matches minus mismatches over
+// equal-length pieces, floored at 0.
+__device__ __forceinline__ int hamming_global_score(const uint8_t* q, const uint8_t* r, int n, const AlignScores& sc) {
+    int hs = 0;
+    for (int x = 0; x < n; x++) hs += q[x] == r[x] ? (int)sc.match : -(int)sc.mismatch;
+    return hs > 0 ? hs : 0;
 }
 
 __global__ void __launch_bounds__(32) k_piecewise(const uint32_t* __restrict__ list, const uint32_t* n_list_ptr,
@@ -2278,60 +2368,7 @@ __global__ void __launch_bounds__(32) k_piecewise(const uint32_t* __restrict__ l
         }
         __syncwarp();
         int na = na0;
-        if (lane == 0) {
-            // remove_spurious_anchors (src/piecewisealigner.rs:596-719)
-            auto erase = [&](int from, int to) {  // [from, to)
-                for (int x = to; x < na; x++) {
-                    anc[2 * (x - (to - from))] = anc[2 * x];
-                    anc[2 * (x - (to - from)) + 1] = anc[2 * x + 1];
-                }
-                na -= to - from;
-            };
-            if (na >= 2) {
-                const long long tol = 5;
-                long long tracked = 0;
-                bool has_dev = false;
-                int dev = 0, i = 1;
-                while (i < na) {
-                    const long long qd = (long long)anc[2 * (i - 1)] - anc[2 * i];
-                    const long long rd = (long long)anc[2 * (i - 1) + 1] - anc[2 * i + 1];
-                    const long long indel = qd - rd;
-                    if ((indel < 0 ? -indel : indel) > tol) {
-                        const long long tt = tracked + indel;
-                        if (has_dev && (tt < 0 ? -tt : tt) <= tol) {
-                            erase(dev, i);
-                            i = dev;
-                            has_dev = false;
-                            tracked = 0;
-                            continue;
-                        }
-                        has_dev = true;
-                        dev = i;
-                        tracked = indel;
-                    }
-                    i++;
-                }
-                const int max_prune = (int)ceilf(__fmul_rn((float)na, 0.20f));
-                const int lim = na < max_prune ? na : max_prune;
-                for (int x = 1; x < lim; x++) {
-                    const long long qd = (long long)anc[2 * x] - anc[2 * (x - 1)];
-                    const long long rd = (long long)anc[2 * x + 1] - anc[2 * (x - 1) + 1];
-                    if (qd - rd != 0) {
-                        erase(0, x);
-                        break;
-                    }
-                }
-                const int lo = (na > max_prune ? na - max_prune : 0) + 1;
-                for (int x = na; x-- > lo;) {
-                    const long long qd = (long long)anc[2 * x] - anc[2 * (x - 1)];
-                    const long long rd = (long long)anc[2 * x + 1] - anc[2 * (x - 1) + 1];
-                    if (qd - rd != 0) {
-                        erase(x, na);
-                        break;
-                    }
-                }
-            }
-        }
+        if (lane == 0) prune_spurious_anchors(anc, na);
         na = __shfl_sync(FULLM, na, 0);
         __syncwarp();
         CigarWriter w{cigar + p.cigar_off, 0, p.cigar_cap, false};
@@ -2369,9 +2406,7 @@ __global__ void __launch_bounds__(32) k_piecewise(const uint32_t* __restrict__ l
             if (rd > 0 && qd > 0) {
                 if (rd == qd) {
                     // hamming_align_global, taken if it scores above 85% of all matches
-                    int hs = 0;
-                    for (int x = 0; x < qd; x++) hs += q[pqe + x] == dref[prre + x] ? (int)sc.match : -(int)sc.mismatch;
-                    const int hsc = hs > 0 ? hs : 0;
+                    const int hsc = hamming_global_score(q + pqe, dref + prre, qd, sc);
                     const uint32_t thr = (uint32_t)ceilf(__fmul_rn((float)qd, 0.85f));
                     if (hsc > 0 && (uint32_t)hsc > (uint32_t)sc.match * thr) {
                         score += hsc;
@@ -2503,6 +2538,105 @@ void init_tables() {
     SA_CUDA(cudaMemcpyToSymbol(c_ssw_code, code, 256));
     SA_CUDA(cudaMemcpyToSymbol(c_comp, comp, 256));
     g_tables_ready = true;
+}
+
+// ------------------------------------------------------------------ stage entry points
+// Kernels behind sa_hamming_batch, sa_piecewise_pieces, sa_remove_spurious_anchors and
+// sa_piecewise_batch: the device functions of the extension path on caller-given
+// (query, reference) bytes, for parity tests against the reference's unit vectors.
+
+// Thread per pair: kind 0 hamming_align (src/aligner.rs:218-259; None unless the lengths
+// agree), kind 1 hamming_align_global (:261-291).
+__global__ void k_stage_hamming(uint32_t n, const uint32_t* kinds, const uint8_t* q, const uint64_t* qo,
+                                const uint8_t* r, const uint64_t* ro, AlignScores sc, StageAlignment* out,
+                                uint32_t* cigar, const uint64_t* cig_off) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const uint8_t* a = q + qo[t];
+        const uint8_t* b = r + ro[t];
+        const uint32_t L = (uint32_t)(qo[t + 1] - qo[t]), RL = (uint32_t)(ro[t + 1] - ro[t]);
+        StageAlignment o{};
+        CigarWriter w{cigar + cig_off[t], 0, (uint32_t)(cig_off[t + 1] - cig_off[t]), false};
+        auto eq = [&](uint32_t i) { return a[i] == b[i]; };
+        if (kinds[t] == 0) {
+            if (L == RL) {
+                uint32_t bs, be;
+                o.score = highest_scoring_segment(eq, L, sc, bs, be);
+                o.edit_distance = hamming_cigar(eq, bs, be, w);
+                o.query_start = o.ref_start = bs;
+                o.query_end = o.ref_end = be;
+                o.valid = !w.overflow;
+            }
+        } else {
+            const uint32_t m = L < RL ? L : RL;
+            o.score = hamming_global_score(a, b, (int)m, sc);
+            o.edit_distance = hamming_cigar(eq, 0, m, w);
+            o.query_end = o.ref_end = L;
+            o.valid = !w.overflow;
+        }
+        o.cigar_offset = (uint32_t)cig_off[t];
+        o.cigar_len = w.n;
+        out[t] = o;
+    }
+}
+
+// Warp per piece: kind 0 global_alignment (src/piecewisealigner.rs:68-130), 1 the
+// x-drop piece after the last anchor (GlobalStartLocalEnd), 2 the one before the first
+// anchor (LocalStartGlobalEnd) (:132-240), as k_piecewise runs them.
+__global__ void __launch_bounds__(32) k_stage_pieces(uint32_t n, const uint32_t* kinds, const uint8_t* q,
+                                                     const uint64_t* qo, const uint8_t* r, const uint64_t* ro,
+                                                     AlignScores sc, uint8_t* scratch, const uint64_t* scr_off,
+                                                     StageAlignment* out, uint32_t* cigar, const uint64_t* cig_off) {
+    extern __shared__ int pw_rows[];
+    const int lane = threadIdx.x & 31;
+    for (uint32_t t = blockIdx.x; t < n; t += gridDim.x) {
+        const uint8_t* a = q + qo[t];
+        const uint8_t* b = r + ro[t];
+        const int L = (int)(qo[t + 1] - qo[t]), RL = (int)(ro[t + 1] - ro[t]);
+        uint8_t* dirs = scratch + scr_off[t];
+        uint8_t* ops = dirs + (size_t)(L + 1) * (RL + 1);
+        PwPiece pc;
+        if (kinds[t] == 0) pc = pw_dp<false, false>(a, L, b, RL, sc, pw_rows, dirs, ops);
+        else if (kinds[t] == 1) pc = pw_dp<true, false>(a, L, b, RL, sc, pw_rows, dirs, ops);
+        else pc = pw_dp<true, true>(a, L, b, RL, sc, pw_rows, dirs, ops);
+        if (lane == 0) {
+            StageAlignment o{};
+            CigarWriter w{cigar + cig_off[t], 0, (uint32_t)(cig_off[t + 1] - cig_off[t]), false};
+            if (kinds[t] == 2) {
+                for (int x = 0; x < pc.nops; x++) w.push(ops[x], 1);
+                o.query_start = (uint32_t)(L - pc.bi);
+                o.ref_start = (uint32_t)(RL - pc.bj);
+                o.query_end = (uint32_t)L;
+                o.ref_end = (uint32_t)RL;
+            } else {
+                for (int x = pc.nops; x-- > 0;) w.push(ops[x], 1);
+                o.query_end = (uint32_t)pc.bi;
+                o.ref_end = (uint32_t)pc.bj;
+            }
+            w.finish();
+            uint32_t ed = 0;
+            for (uint32_t x = 0; x < w.n; x++) {
+                const uint32_t op = w.out[x] & 15;
+                if (op == 8 || op == 1 || op == 2) ed += w.out[x] >> 4;
+            }
+            o.valid = !w.overflow;
+            o.score = pc.score;
+            o.edit_distance = ed;
+            o.cigar_offset = (uint32_t)cig_off[t];
+            o.cigar_len = w.n;
+            out[t] = o;
+        }
+        __syncwarp();
+    }
+}
+
+// Thread per chain: remove_spurious_anchors in place on (query start, reference start)
+// pairs.
+__global__ void k_stage_prune(uint32_t n, int* anc, const uint64_t* off, uint32_t* counts) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        int na = (int)(off[t + 1] - off[t]);
+        prune_spurious_anchors(anc + 2 * off[t], na);
+        counts[t] = (uint32_t)na;
+    }
 }
 
 }  // namespace
@@ -2805,6 +2939,187 @@ uint32_t run_extension(const DevRefs& refs, const NamWorkspace& nws, uint32_t k,
                        uint32_t max_anchors) {
     return run_extension_raw(refs, nws.seq.p, nws.off.p, nullptr, nullptr, k, sc, n, ws, max_qlen, st, kt, anchors,
                              max_anchors);
+}
+
+// ------------------------------------------------------------------ stage entry points
+namespace {
+
+template <class T>
+void upload(DevBuf<T>& d, const T* h, size_t n, cudaStream_t st) {
+    d.reserve(std::max<size_t>(n, 1));
+    if (n) SA_CUDA(cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, st));
+}
+
+struct StageInputs {
+    DevBuf<uint32_t> kinds;
+    DevBuf<uint8_t> q, r;
+    DevBuf<uint64_t> qo, ro, co;
+    DevBuf<StageAlignment> out;
+    DevBuf<uint32_t> cigar;
+    std::vector<uint64_t> cig_off;
+    void load(uint32_t n, const uint32_t* k, const uint8_t* hq, const uint64_t* hqo, const uint8_t* hr,
+              const uint64_t* hro, cudaStream_t st) {
+        cig_off.assign((size_t)n + 1, 0);
+        for (uint32_t i = 0; i < n; i++) cig_off[i + 1] = cig_off[i] + (hqo[i + 1] - hqo[i]) + (hro[i + 1] - hro[i]) + 4;
+        upload(kinds, k, n, st);
+        upload(q, hq, hqo[n], st);
+        upload(r, hr, hro[n], st);
+        upload(qo, hqo, (size_t)n + 1, st);
+        upload(ro, hro, (size_t)n + 1, st);
+        upload(co, cig_off.data(), (size_t)n + 1, st);
+        out.reserve(std::max<uint32_t>(n, 1));
+        cigar.reserve(cig_off[n] + 1);
+    }
+    void fetch(uint32_t n, StageAlignment* hout, uint32_t* hcig, size_t cap, cudaStream_t st) {
+        if (cig_off[n] > cap) throw Error(SA_ERR_INVALID, "cigar capacity too small");
+        if (n) SA_CUDA(cudaMemcpyAsync(hout, out.p, (size_t)n * sizeof(StageAlignment), cudaMemcpyDeviceToHost, st));
+        if (cig_off[n]) SA_CUDA(cudaMemcpyAsync(hcig, cigar.p, cig_off[n] * 4, cudaMemcpyDeviceToHost, st));
+        SA_CUDA(cudaStreamSynchronize(st));
+    }
+};
+
+}  // namespace
+
+void stage_hamming(uint32_t n, const uint32_t* kinds, const uint8_t* q, const uint64_t* qo, const uint8_t* r,
+                   const uint64_t* ro, const AlignScores& sc, StageAlignment* out, uint32_t* cigar, size_t cap,
+                   cudaStream_t st) {
+    StageInputs in;
+    in.load(n, kinds, q, qo, r, ro, st);
+    if (n)
+        k_stage_hamming<<<grid1(n), 256, 0, st>>>(n, in.kinds.p, in.q.p, in.qo.p, in.r.p, in.ro.p, sc, in.out.p,
+                                                  in.cigar.p, in.co.p);
+    SA_CUDA(cudaGetLastError());
+    in.fetch(n, out, cigar, cap, st);
+}
+
+void stage_pieces(uint32_t n, const uint32_t* kinds, const uint8_t* q, const uint64_t* qo, const uint8_t* r,
+                  const uint64_t* ro, const AlignScores& sc, StageAlignment* out, uint32_t* cigar, size_t cap,
+                  cudaStream_t st) {
+    StageInputs in;
+    in.load(n, kinds, q, qo, r, ro, st);
+    std::vector<uint64_t> so((size_t)n + 1, 0);
+    uint64_t max_r = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const uint64_t L = qo[i + 1] - qo[i], R = ro[i + 1] - ro[i];
+        so[i + 1] = so[i] + (((L + 1) * (R + 1) + L + R + 8 + 15) & ~15ull);
+        max_r = std::max(max_r, R);
+    }
+    DevBuf<uint8_t> scratch;
+    DevBuf<uint64_t> d_so;
+    scratch.reserve(so[n] + 16);
+    upload(d_so, so.data(), so.size(), st);
+    const size_t smem = 16 * ((size_t)max_r + 2);
+    if (smem > 48 * 1024)
+        SA_CUDA(cudaFuncSetAttribute(k_stage_pieces, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (n)
+        k_stage_pieces<<<(unsigned)std::min<uint32_t>(n, 4096), 32, smem, st>>>(
+            n, in.kinds.p, in.q.p, in.qo.p, in.r.p, in.ro.p, sc, scratch.p, d_so.p, in.out.p, in.cigar.p, in.co.p);
+    SA_CUDA(cudaGetLastError());
+    in.fetch(n, out, cigar, cap, st);
+}
+
+void stage_prune(uint32_t n, int32_t* anchors, const uint64_t* off, uint32_t* counts, cudaStream_t st) {
+    DevBuf<int> d_anc;
+    DevBuf<uint64_t> d_off;
+    DevBuf<uint32_t> d_cnt;
+    upload(d_anc, anchors, 2 * off[n], st);
+    upload(d_off, off, (size_t)n + 1, st);
+    d_cnt.reserve(std::max<uint32_t>(n, 1));
+    if (n) k_stage_prune<<<grid1(n), 128, 0, st>>>(n, d_anc.p, d_off.p, d_cnt.p);
+    SA_CUDA(cudaGetLastError());
+    if (off[n]) SA_CUDA(cudaMemcpyAsync(anchors, d_anc.p, 2 * off[n] * sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (n) SA_CUDA(cudaMemcpyAsync(counts, d_cnt.p, (size_t)n * 4, cudaMemcpyDeviceToHost, st));
+    SA_CUDA(cudaStreamSynchronize(st));
+}
+
+void stage_piecewise(uint32_t n, const uint8_t* q, const uint64_t* qo, const uint8_t* r, const uint64_t* ro,
+                     const uint32_t* anchors, const uint64_t* anc_off, uint32_t k, const AlignScores& sc,
+                     StageAlignment* out, uint32_t* cigar, size_t cap, cudaStream_t st) {
+    init_tables();
+    // one job per (query, window): the arena holds the query then the window, the
+    // anchors their (query start, window start) pairs last to first, as a wave of
+    // piecewise jobs has them
+    std::vector<ExtJob> jobs(std::max<uint32_t>(n, 1));
+    std::vector<PrepRec> prep(std::max<uint32_t>(n, 1));
+    std::vector<uint8_t> arena;
+    std::vector<uint32_t> list(std::max<uint32_t>(n, 1));
+    uint64_t cig = 0, max_q = 0, max_w = 0, max_a = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const uint64_t L = qo[i + 1] - qo[i], W = ro[i + 1] - ro[i], A = anc_off[i + 1] - anc_off[i];
+        if (A == 0) throw Error(SA_ERR_INVALID, "piecewise job without anchors");
+        ExtJob j{};
+        j.anc_off = (uint32_t)anc_off[i];
+        j.anc_n = (uint32_t)A;
+        jobs[i] = j;
+        PrepRec p{};
+        p.type = 3;
+        p.qlen = (uint32_t)L;
+        p.wlen = (uint32_t)W;
+        p.arena_off = arena.size();
+        p.cigar_off = cig;
+        p.cigar_cap = (uint32_t)(2 * L + W + 4);
+        cig += p.cigar_cap;
+        arena.insert(arena.end(), q + qo[i], q + qo[i + 1]);
+        arena.insert(arena.end(), r + ro[i], r + ro[i + 1]);
+        prep[i] = p;
+        list[i] = i;
+        max_q = std::max(max_q, L);
+        max_w = std::max(max_w, W);
+        max_a = std::max(max_a, A);
+    }
+    DevBuf<ExtJob> d_jobs;
+    DevBuf<PrepRec> d_prep;
+    DevBuf<uint8_t> d_arena, d_scratch;
+    DevBuf<uint32_t> d_list, d_anc, d_cigar, d_counters;
+    DevBuf<ExtResult> d_res;
+    upload(d_jobs, jobs.data(), jobs.size(), st);
+    upload(d_prep, prep.data(), prep.size(), st);
+    upload(d_arena, arena.data(), arena.size(), st);
+    upload(d_list, list.data(), list.size(), st);
+    upload(d_anc, anchors, 2 * anc_off[n], st);
+    d_cigar.reserve(cig + 1);
+    d_res.reserve(std::max<uint32_t>(n, 1));
+    d_counters.reserve(24);
+    SA_CUDA(cudaMemsetAsync(d_counters.p, 0, 24 * 4, st));
+    SA_CUDA(cudaMemcpyAsync(d_counters.p + 19, &n, 4, cudaMemcpyHostToDevice, st));
+    SA_CUDA(cudaMemsetAsync(d_res.p, 0, std::max<uint32_t>(n, 1) * sizeof(ExtResult), st));
+    auto a16 = [](uint64_t x) { return (x + 15) & ~(uint64_t)15; };
+    const uint64_t cells = a16((max_q + 1) * (max_w + 1));
+    const uint64_t opsb = a16(max_q + max_w + 8) + a16(8ull * (max_a + 1));
+    const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(n, 1024));
+    d_scratch.reserve((cells + opsb) * blocks);
+    const size_t smem = 16 * ((size_t)max_w + 2);
+    if (smem > 48 * 1024)
+        SA_CUDA(cudaFuncSetAttribute(k_piecewise, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (n)
+        k_piecewise<<<blocks, 32, smem, st>>>(d_list.p, d_counters.p + 19, d_jobs.p, d_prep.p, d_arena.p, d_anc.p, sc,
+                                              k, d_scratch.p, cells, opsb, d_cigar.p, d_res.p, d_counters.p);
+    SA_CUDA(cudaGetLastError());
+    std::vector<ExtResult> res(std::max<uint32_t>(n, 1));
+    std::vector<uint32_t> hc(cig + 1);
+    SA_CUDA(cudaMemcpyAsync(res.data(), d_res.p, res.size() * sizeof(ExtResult), cudaMemcpyDeviceToHost, st));
+    SA_CUDA(cudaMemcpyAsync(hc.data(), d_cigar.p, hc.size() * 4, cudaMemcpyDeviceToHost, st));
+    SA_CUDA(cudaStreamSynchronize(st));
+    size_t w = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const ExtResult& x = res[i];
+        StageAlignment o{};
+        o.valid = x.valid;
+        if (x.valid) {
+            if (w + x.cigar_len > cap) throw Error(SA_ERR_INVALID, "cigar capacity too small");
+            o.score = (int32_t)x.score;
+            o.query_start = x.soft_clip_left;
+            o.query_end = prep[i].qlen - x.soft_clip_right;
+            o.ref_start = x.ref_start;
+            o.ref_end = x.ref_start + x.length;
+            o.edit_distance = x.edit_distance;
+            o.cigar_offset = (uint32_t)w;
+            o.cigar_len = x.cigar_len;
+            std::memcpy(cigar + w, hc.data() + x.cigar_offset, (size_t)x.cigar_len * 4);
+            w += x.cigar_len;
+        }
+        out[i] = o;
+    }
 }
 
 }  // namespace sa

@@ -86,4 +86,30 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
                            uint32_t max_qlen, cudaStream_t st, KernelTimers* kt = nullptr,
                            const uint32_t* anchors = nullptr, uint32_t max_anchors = 0);
 
+// Result of a stage entry point (sa_stage_alignment): signed score, since global
+// pieces can score below zero.
+struct StageAlignment {
+    int32_t valid;
+    int32_t score;
+    uint32_t query_start, query_end, ref_start, ref_end;
+    uint32_t edit_distance;
+    uint32_t cigar_offset, cigar_len;
+};
+
+// Stage entry points (extend.cu) on caller-given bytes; synchronous on st.
+// kinds: 0 hamming_align, 1 hamming_align_global.
+void stage_hamming(uint32_t n, const uint32_t* kinds, const uint8_t* q, const uint64_t* qo, const uint8_t* r,
+                   const uint64_t* ro, const AlignScores& sc, StageAlignment* out, uint32_t* cigar, size_t cap,
+                   cudaStream_t st);
+// kinds: 0 global piece, 1 x-drop piece after the last anchor, 2 before the first.
+void stage_pieces(uint32_t n, const uint32_t* kinds, const uint8_t* q, const uint64_t* qo, const uint8_t* r,
+                  const uint64_t* ro, const AlignScores& sc, StageAlignment* out, uint32_t* cigar, size_t cap,
+                  cudaStream_t st);
+// anchors: (query start, reference start) pairs, chain t at [off[t], off[t+1]); pruned in place.
+void stage_prune(uint32_t n, int32_t* anchors, const uint64_t* off, uint32_t* counts, cudaStream_t st);
+// extend_piecewise per (query, reference window, anchors last to first).
+void stage_piecewise(uint32_t n, const uint8_t* q, const uint64_t* qo, const uint8_t* r, const uint64_t* ro,
+                     const uint32_t* anchors, const uint64_t* anc_off, uint32_t k, const AlignScores& sc,
+                     StageAlignment* out, uint32_t* cigar, size_t cap, cudaStream_t st);
+
 }  // namespace sa
