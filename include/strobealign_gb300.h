@@ -199,7 +199,9 @@ int32_t sa_randstrobes_batch(const sa_index* idx, const sa_read_batch* reads, sa
  * The first call on each device looks up the scratch address
  * (cudaGetSymbolAddress; this may load the library's device code), so make that
  * call outside any stream capture; a call with n_reads = 0 does only this setup
- * and launches nothing.  Later calls only launch.
+ * and launches nothing.  Later calls only launch.  The address is kept per device
+ * and CUDA context: the first call in a context created anew (for instance after
+ * cudaDeviceReset) looks it up again.
  *
  * Runs on the calling thread's current device, asynchronously on `stream` (a
  * cudaStream_t; NULL = legacy default stream).  idx supplies only the seeding
@@ -211,7 +213,10 @@ int32_t sa_randstrobes_batch(const sa_index* idx, const sa_read_batch* reads, sa
  * [total_bases + d_seq_offsets[r], + d_counts[2r+1]), with the values of the
  * hash / hash_revcomp / start / end fields of sa_query_randstrobe.  A read whose
  * offsets decrease, end past total_bases or span more than 2048 bases gets
- * d_counts = UINT32_MAX in both orientations.  Only argument errors are reported
+ * d_counts = UINT32_MAX in both orientations.  d_seq_offsets must not decrease:
+ * each read is checked on its own, so in an array that decreases somewhere two
+ * reads that are each well-formed can overlap, and overlapping reads race on their
+ * output and scratch slots.  Only argument errors are reported
  * by the return value; kernel results are ready when the stream reaches them. */
 #define SA_RANDSTROBES_NOALLOC_MAX_BASES 1048576u
 int32_t sa_randstrobes_device_noalloc(const sa_index* idx, const uint8_t* d_seq, const uint64_t* d_seq_offsets,
@@ -339,15 +344,25 @@ int32_t sa_mapper_abundances(const sa_mapper* m, double* out, size_t n);
  * submit/poll/wait may be called from any thread. */
 typedef struct sa_session sa_session;
 typedef struct {
-    uint64_t max_inflight_bases;    /* device read arena in bases; 0 = 2^30 */
+    uint64_t max_inflight_bases;    /* device read arena in bases; 0 = an eighth of the free
+                                       device memory beyond the reserve (2^24..2^33) */
     uint32_t max_inflight_requests; /* 0 = no limit */
     uint32_t policy_threads;        /* host threads for the mapping policy; 0 = all */
     uint32_t admission_streams;     /* requests whose NAM pipelines run at once; 0 = 2 */
     uint32_t borrow_inputs;         /* 1: sa_session_submit keeps pointers to the batch's
                                        sequences, qualities, names and comments instead of
                                        copying them; the caller keeps them unchanged until
-                                       sa_session_wait returns for that request. 0 (default):
-                                       copied, the caller may free them after submit. */
+                                       sa_session_wait returns for that request (also when it
+                                       returns an error: by then no session thread reads
+                                       them). 0 (default): copied, the caller may free them
+                                       after submit. */
+    uint64_t device_reserve_bytes;  /* device memory admission leaves free for everything
+                                       else; 0 = max(2 GiB, 5% of the device).  A request is
+                                       admitted when its reads fit in the arena and the free
+                                       device memory beyond this reserve covers the NAM
+                                       workspace its admission group needs (160 bytes per
+                                       base); one that cannot fit while nothing else is in
+                                       flight fails with SA_ERR_BUSY. */
 } sa_session_params;
 typedef struct {
     double seconds_queued;  /* submit -> admitted */
@@ -372,6 +387,13 @@ int32_t sa_session_poll(sa_session* s, uint64_t ticket, int32_t* done);
  * otherwise.  The ticket is invalid afterwards. */
 int32_t sa_session_wait(sa_session* s, uint64_t ticket, int64_t timeout_ms, sa_output* out, sa_request_stats* stats,
                         double* abundances, size_t n_abundances);
+/* What the session chose at creation. */
+typedef struct {
+    uint64_t arena_bases;          /* device read arena (bases) */
+    uint64_t device_reserve_bytes; /* device memory admission leaves free */
+    uint64_t refused_requests;     /* requests refused for lack of device memory so far */
+} sa_session_info;
+int32_t sa_session_get_info(const sa_session* s, sa_session_info* out);
 /* Finishes the admitted requests, cancels the queued ones, frees the session. */
 void sa_session_free(sa_session* s);
 

@@ -529,7 +529,8 @@ class Session:
 
     def __init__(self, index: StrobemerIndex, refs: References, chaining: L.ChainingParams | None = None,
                  mapping: L.MappingParams | None = None, max_inflight_bases: int = 0, max_inflight_requests: int = 0,
-                 policy_threads: int = 0, admission_streams: int = 0, borrow_inputs: bool = False, **kw):
+                 policy_threads: int = 0, admission_streams: int = 0, borrow_inputs: bool = False,
+                 device_reserve_bytes: int = 0, **kw):
         self.index, self.refs = index, refs
         # borrow_inputs: the session reads the submitted Reads in place; they are kept
         # referenced here until wait() returns for their ticket
@@ -546,6 +547,7 @@ class Session:
         if admission_streams:
             sp.admission_streams = admission_streams
         sp.borrow_inputs = 1 if self.borrow else 0
+        sp.device_reserve_bytes = device_reserve_bytes
         h = C.c_void_p()
         L.check(lib().sa_session_create(index.h, refs.h, C.byref(self.cp), C.byref(self.mp), C.byref(sp),
                                         C.byref(h)))
@@ -559,6 +561,14 @@ class Session:
         if self.borrow:
             self._borrowed[t.value] = (r1, r2, b1, b2)
         return t.value
+
+    @property
+    def info(self) -> dict:
+        """The device read arena (bases) and memory reserve the session chose, and the
+        requests refused for lack of device memory."""
+        i = L.SessionInfo()
+        L.check(lib().sa_session_get_info(self.h, C.byref(i)))
+        return {f: int(getattr(i, f)) for f, _ in L.SessionInfo._fields_}
 
     def poll(self, ticket: int) -> bool:
         d = C.c_int32()

@@ -79,7 +79,11 @@ class Output(C.Structure):
 
 class SessionParams(C.Structure):
     _fields_ = [("max_inflight_bases", u64), ("max_inflight_requests", u32), ("policy_threads", u32),
-                ("admission_streams", u32), ("borrow_inputs", u32)]
+                ("admission_streams", u32), ("borrow_inputs", u32), ("device_reserve_bytes", u64)]
+
+
+class SessionInfo(C.Structure):
+    _fields_ = [("arena_bases", u64), ("device_reserve_bytes", u64), ("refused_requests", u64)]
 
 
 class ScheduleParams(C.Structure):
@@ -111,6 +115,7 @@ SIGNATURES = {
     "sa_session_poll": (i32, [vp, u64, P(i32)]),
     "sa_session_wait": (i32, [vp, u64, i64, P(Output), P(RequestStats), P(f64), sz]),
     "sa_session_free": (None, [vp]),
+    "sa_session_get_info": (i32, [vp, P(SessionInfo)]),
     "sa_last_error": (cp, []),
     "sa_version": (cp, []),
     "sa_seeding_params_from_read_length": (i32, [sz, P(SeedingParams)]),

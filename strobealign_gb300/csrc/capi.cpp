@@ -545,6 +545,10 @@ int32_t sa_nams_batch(const sa_index* idx, const sa_chaining_params* cp, const s
     else sa_chaining_params_default(&c);
     if (mp) m = *mp;
     else sa_mapping_params_default(&m);
+    // the same limits as sa_mapper_create: the chaining log2 table covers gaps below
+    // LOG2_LUT_SIZE, and the lookback ring holds 1024 predecessors
+    require(c.max_lookback <= 1024, "max_lookback above 1024 is not supported");
+    require(c.max_ref_gap < LOG2_LUT_SIZE, "max_ref_gap too large");
     NamWorkspace ws;
     const uint32_t n = (uint32_t)reads->n;
     uint64_t total = reads->seq_offsets[n] - reads->seq_offsets[0];
@@ -749,11 +753,22 @@ int32_t sa_piecewise_batch(const sa_mapping_params* mp, uint32_t k, size_t n, co
 // ---------------------------------------------------------------- serving
 void sa_session_params_default(sa_session_params* p) {
     if (!p) return;
-    p->max_inflight_bases = 1ull << 30;
+    p->max_inflight_bases = 0;
     p->max_inflight_requests = 0;
     p->policy_threads = 0;
     p->admission_streams = 2;
     p->borrow_inputs = 0;
+    p->device_reserve_bytes = 0;
+}
+
+int32_t sa_session_get_info(const sa_session* s, sa_session_info* out) {
+    SA_TRY
+    require(s && s->s && out, "null argument");
+    out->arena_bases = s->s->arena_bases();
+    out->device_reserve_bytes = s->s->reserve_bytes();
+    out->refused_requests = s->s->refused();
+    return SA_OK;
+    SA_CATCH
 }
 
 int32_t sa_session_create(const sa_index* idx, const sa_refs* refs, const sa_chaining_params* cp,
@@ -775,6 +790,7 @@ int32_t sa_session_create(const sa_index* idx, const sa_refs* refs, const sa_cha
         sc.policy_threads = sp->policy_threads;
         sc.admission_streams = sp->admission_streams ? sp->admission_streams : 2;
         sc.borrow_inputs = sp->borrow_inputs != 0;
+        sc.device_reserve_bytes = sp->device_reserve_bytes;
     }
     auto* s = new sa_session{nullptr};
     try {

@@ -2509,7 +2509,7 @@ __global__ void k_cigar_gather(ExtResult* res, uint32_t n, const uint32_t* cigar
 
 inline unsigned grid1(uint64_t n, unsigned block = 256) {
     uint64_t g = (n + block - 1) / block;
-    if (g > 152ULL * 16) g = 152ULL * 16;
+    if (g > sm_count() * 16) g = sm_count() * 16;
     return (unsigned)(g ? g : 1);
 }
 
@@ -2677,7 +2677,7 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
             attr = true;
         }
         uint64_t blocks = ((uint64_t)n + 1) / 2;
-        if (blocks > 152ULL * 3) blocks = 152ULL * 3;
+        if (blocks > sm_count() * 3) blocks = sm_count() * 3;
         k_rescue_filter<<<(unsigned)(blocks ? blocks : 1), 64, smem, st>>>(ws.rescue_list.p, ws.counters.p + 4, seq,
                                                                            off, refs, k, ws.prep.p, sz[0], sz[1],
                                                                            sz[2]);
@@ -2717,7 +2717,7 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
         const uint64_t opsb = a16((uint64_t)max_qlen + max_pw_window + 8) + a16(8ull * (max_anchors + 1));
         // single-warp blocks, up to 16 per SM: the per-job work is mostly serial (anchor
         // pruning, gap checks, traceback pushes), so more resident warps hide its latency
-        const unsigned blocks = (unsigned)std::min<uint64_t>(n, 152ULL * 16);
+        const unsigned blocks = (unsigned)std::min<uint64_t>(n, sm_count() * 16);
         ws.pw_scratch.reserve((cells + opsb) * blocks);
         const size_t smem = 16 * ((size_t)max_pw_window + 2);
         static size_t attr = 0;
@@ -2750,7 +2750,7 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
         }
         auto blocks_for = [](uint32_t items, int per_block) {
             uint64_t b = (items + per_block - 1) / per_block;
-            if (b > 152ULL * 16) b = 152ULL * 16;
+            if (b > sm_count() * 16) b = sm_count() * 16;
             return (unsigned)(b ? b : 1);
         };
         // register kernels while the profile fits in int8 and a lane's rows in SEG
@@ -2802,7 +2802,7 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
                                             ws.list_rev_word.p, ws.order.p, (int)n_tasks, 0, 16, st);
             const int wpb = tpb / 32;
             uint64_t blocks = ((uint64_t)n_tasks + wpb - 1) / wpb;
-            if (blocks > 152ULL * 16) blocks = 152ULL * 16;
+            if (blocks > sm_count() * 16) blocks = sm_count() * 16;
 #define SA_SSW(RM)                                                                                              \
     k_ssw<RM><<<(unsigned)blocks, tpb, (size_t)wpb * 5 * 32 * ((RM + 3) / 4) * 4, st>>>(                       \
         ws.tasks.p, ws.order.p, n_tasks, ws.prep.p, ws.arena.p, sc, bias, ws.counters.p, ws.counters.p + 21, \
@@ -2818,7 +2818,7 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
             {
                 const uint64_t per_block = (uint64_t)wpb * (32 / WV_T);  // tasks per block and round
                 uint64_t wblocks = ((uint64_t)n_tasks + per_block - 1) / per_block;
-                if (wblocks > 152ULL * 16) wblocks = 152ULL * 16;
+                if (wblocks > sm_count() * 16) wblocks = sm_count() * 16;
                 const size_t smem = (size_t)wpb * 5 * ((WAVE_NMAX + 7) / 8) * 32 * sizeof(uint4);
                 k_ssw_wave<WAVE_NMAX><<<(unsigned)wblocks, tpb, smem, st>>>(
                     ws.tasks.p, ws.order.p, n_tasks, ws.prep.p, ws.arena.p, sc, bias, ws.counters.p,
@@ -2848,7 +2848,7 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
         if (sc.gap_open >= sc.gap_extend) {
             kt->begin(KS_BAND, st);
             uint64_t blocks = ((uint64_t)n_tasks + 3) / 4;
-            if (blocks > 152ULL * 16) blocks = 152ULL * 16;
+            if (blocks > sm_count() * 16) blocks = sm_count() * 16;
             k_band_warp<<<(unsigned)blocks, 128, 0, st>>>(ws.tasks.p, n_tasks, ws.prep.p, ws.arena.p, ws.hscratch.p,
                                                           sc, ws.counters.p);
             kt->end(st);
@@ -2861,7 +2861,7 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
         const bool wide = sc.gap_open >= sc.gap_extend;
         const int maxc = 2 * (int)std::max<uint32_t>(2048, max_qlen) + 8;
         const size_t band_smem = (size_t)4 * maxc * sizeof(int);
-        unsigned band_blocks = (unsigned)std::min<uint64_t>(n_tasks, 152ULL * 3);
+        unsigned band_blocks = (unsigned)std::min<uint64_t>(n_tasks, sm_count() * 3);
         if (!band_blocks) band_blocks = 1;
         kt->begin(KS_BAND, st);
         if (wide) {

@@ -44,6 +44,21 @@ struct ReadStore {
 };
 void load_reads(const std::string& path, ReadStore& rs);
 
+// Streaming multiprocessors of the calling thread's current device; grid sizes are
+// capped at multiples of it (queried once per device and thread).
+inline uint64_t sm_count() {
+    static thread_local int cached_dev = -1;
+    static thread_local uint64_t cached = 1;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return cached;
+    if (dev != cached_dev) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0) cached = (uint64_t)v;
+        cached_dev = dev;
+    }
+    return cached;
+}
+
 // Device buffer with RAII release.
 template <class T>
 struct DevBuf {

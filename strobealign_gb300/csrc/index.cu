@@ -189,7 +189,7 @@ __global__ void k_extent(const RefRandstrobe* rs, uint64_t n, unsigned int* out)
 
 inline unsigned grid_for(uint64_t n, unsigned block) {
     uint64_t g = (n + block - 1) / block;
-    if (g > 152ULL * 64) g = 152ULL * 64;
+    if (g > sm_count() * 64) g = sm_count() * 64;
     return (unsigned)(g == 0 ? 1 : g);
 }
 

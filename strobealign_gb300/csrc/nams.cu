@@ -1378,7 +1378,7 @@ __global__ void k_nam_anchor_gather(uint64_t total_nams, const uint64_t* src, co
 
 inline unsigned warps_grid(uint64_t items) {
     uint64_t blocks = (items + WARPS_PER_BLOCK - 1) / WARPS_PER_BLOCK;
-    if (blocks > 152ULL * 32) blocks = 152ULL * 32;
+    if (blocks > sm_count() * 32) blocks = sm_count() * 32;
     return (unsigned)(blocks ? blocks : 1);
 }
 
@@ -1433,9 +1433,14 @@ void run_seeding_noalloc(const SeedParams& sp, const uint8_t* seq, const uint64_
         throw Error(SA_ERR_INVALID, "batch has " + std::to_string(total) + " bases; the allocation-free seeding "
                                     "entry point takes at most " +
                                         std::to_string((uint64_t)SA_RANDSTROBES_NOALLOC_MAX_BASES));
-    // scratch address per device, looked up on the first call on that device
+    // scratch address per device and CUDA context, looked up by the first call on that
+    // device in that context (a context created anew, e.g. after cudaDeviceReset,
+    // looks it up again instead of using a stale address)
     constexpr int MAX_DEVICES = 64;
+    using CtxGetCurrent = int (*)(void**);  // cuCtxGetCurrent(CUcontext*)
     static std::mutex mu;
+    static CtxGetCurrent ctx_current = nullptr;
+    static void* scratch_ctx[MAX_DEVICES] = {};
     static uint8_t* scratch[MAX_DEVICES] = {};
     int dev = 0;
     SA_CUDA(cudaGetDevice(&dev));
@@ -1443,11 +1448,27 @@ void run_seeding_noalloc(const SeedParams& sp, const uint8_t* seq, const uint64_
     uint8_t* base;
     {
         std::lock_guard<std::mutex> g(mu);
-        if (!scratch[dev]) {
-            // loads the kernel too, so that later calls only launch
+        if (!ctx_current) {
+            cudaDriverEntryPointQueryResult q{};
+            SA_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", reinterpret_cast<void**>(&ctx_current), 12000,
+                                                     cudaEnableDefault, &q));
+            if (q != cudaDriverEntryPointSuccess || !ctx_current)
+                throw Error(SA_ERR_CUDA, "cuCtxGetCurrent is not available");
+        }
+        void* ctx = nullptr;
+        if (ctx_current(&ctx) != 0) throw Error(SA_ERR_CUDA, "cuCtxGetCurrent failed");
+        if (!ctx || !scratch[dev] || scratch_ctx[dev] != ctx) {
+            // binds (or creates) the device's primary context and loads the kernel, so
+            // that later calls only launch
             cudaFuncAttributes fa;
             SA_CUDA(cudaFuncGetAttributes(&fa, k_seed<true>));
-            SA_CUDA(cudaGetSymbolAddress((void**)&scratch[dev], g_seed_scratch));
+            if (ctx_current(&ctx) != 0 || !ctx) throw Error(SA_ERR_CUDA, "no current CUDA context");
+        }
+        if (!scratch[dev] || scratch_ctx[dev] != ctx) {
+            uint8_t* p = nullptr;
+            SA_CUDA(cudaGetSymbolAddress((void**)&p, g_seed_scratch));
+            scratch[dev] = p;
+            scratch_ctx[dev] = ctx;
         }
         base = scratch[dev];
     }
@@ -1575,7 +1596,7 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     SA_CUDA(cudaMemsetAsync(ws.nam_seg_count.p, 0, 2 * (size_t)n * sizeof(uint32_t), st));
     const uint64_t chain_units = (uint64_t)n_list[2] + ((uint64_t)n_list[0] + NG - 1) / NG;
     const unsigned chain_grid = (unsigned)std::max<uint64_t>(
-        1, std::min<uint64_t>((chain_units + CHAIN_WARPS - 1) / CHAIN_WARPS, 152ULL * 64));
+        1, std::min<uint64_t>((chain_units + CHAIN_WARPS - 1) / CHAIN_WARPS, sm_count() * 64));
     if (cfg.nam_anchors) {
         ws.anc_sparse.reserve(3 * total_anchors + 1);
         ws.anc_start.reserve(total_anchors + 1);
@@ -1657,7 +1678,7 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
         SA_CUDA(cudaStreamSynchronize(st));
         ws.nam_anc.reserve(tot + 1);
         if (total_nams)
-            k_nam_anchor_gather<<<(unsigned)std::min<uint64_t>((total_nams + 255) / 256, 152 * 16), 256, 0, st>>>(
+            k_nam_anchor_gather<<<(unsigned)std::min<uint64_t>((total_nams + 255) / 256, sm_count() * 16), 256, 0, st>>>(
                 total_nams, ws.nam_anc_src.p, ws.nam_anc_off.p, ws.anc_sparse.p, ws.nam_anc.p);
         launches += 3;
         ws.last_total_nam_anchors = tot;

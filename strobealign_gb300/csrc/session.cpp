@@ -108,7 +108,17 @@ Session::Session(const sa_index* idx, const sa_refs* refs, const sa_chaining_par
     pcfg_.rg_id = rg_id_;
     pcfg_.has_rg = mp.rg_id != nullptr;
     pcfg_.k = idx->sp.k;
-    if (cfg_.max_inflight_bases == 0) cfg_.max_inflight_bases = 1ull << 30;
+    // memory-based admission: the arena and the lanes' workspaces come out of the free
+    // device memory, less a reserve kept for everything else on the device
+    size_t mem_free = 0, mem_total = 0;
+    SA_CUDA(cudaMemGetInfo(&mem_free, &mem_total));
+    reserve_ = cfg_.device_reserve_bytes ? cfg_.device_reserve_bytes
+                                         : std::max<uint64_t>(2ull << 30, (uint64_t)mem_total / 20);
+    if (cfg_.max_inflight_bases == 0) {
+        // an eighth of what is usable, the rest left to the NAM and extension workspaces
+        const uint64_t usable = mem_free > reserve_ ? (uint64_t)mem_free - reserve_ : 0;
+        cfg_.max_inflight_bases = std::min<uint64_t>(1ull << 33, std::max<uint64_t>(1ull << 24, usable / 8));
+    }
     const uint64_t slots = cfg_.max_inflight_bases / 32 + 65536;
     arena_seq_.reserve(cfg_.max_inflight_bases + 16);
     arena_off_.reserve(slots);
@@ -303,6 +313,13 @@ bool Session::wait(uint64_t ticket, int64_t timeout_ms, std::unique_ptr<Request>
         return false;
     auto it = live_.find(ticket);
     if (it == live_.end()) throw Error(SA_ERR_CANCELLED, "request was cancelled");
+    if (it->second->state == 3 && it->second->users > 0) {
+        // a failed request: wait for the threads still reading its records
+        Request* rq = it->second.get();
+        cv_done_.wait(lk, [&] { return rq->users == 0; });
+        it = live_.find(ticket);
+        if (it == live_.end()) throw Error(SA_ERR_CANCELLED, "request was cancelled");
+    }
     if (it->second->state == 3) {
         const std::string msg = it->second->error;
         const int32_t code = it->second->error_code ? it->second->error_code : SA_ERR_INVALID;
@@ -374,16 +391,49 @@ void Session::admitter(AdmitLane& lane) {
             return seq_alloc_.largest_free() >= std::max<uint64_t>(q.total_bases, 1) &&
                    off_alloc_.largest_free() >= q.n_reads + 1;
         };
-        cv_admit_.wait(lk, [&] { return broken_ || stop_ || (!queue_.empty() && fits(*queue_.front())); });
+        // device memory for the lane's NAM workspace to grow to `bases` (other lanes'
+        // admissions in progress count as taken)
+        auto growth = [&](uint64_t bases) {
+            return bases > lane.ws_bases ? (bases - lane.ws_bases) * NAM_BYTES_PER_BASE : 0;
+        };
+        auto mem_ok = [&](uint64_t bases) {
+            const uint64_t need = growth(bases);
+            if (!need) return true;
+            size_t f = 0, t = 0;
+            if (cudaMemGetInfo(&f, &t) != cudaSuccess) return false;
+            return (uint64_t)f >= reserve_ + pending_growth_ + need;
+        };
+        // free device memory can grow without a notification (another allocation on the
+        // device ends), so the wait polls
+        cv_admit_.wait_for(lk, std::chrono::milliseconds(20),
+                           [&] { return broken_ || stop_ || (!queue_.empty() && fits(*queue_.front())); });
         if (broken_ || stop_) break;
+        if (queue_.empty() || !fits(*queue_.front())) continue;
+        if (!mem_ok(queue_.front()->total_bases)) {
+            if (inflight_ == 0 && admitting_ == 0) {
+                // nothing in flight will free memory: refuse the request
+                std::unique_ptr<Request> rq = std::move(queue_.front());
+                queue_.pop_front();
+                rq->state = 3;
+                rq->error = "admission refused: the request's " + std::to_string(rq->total_bases) +
+                            " bases need more device memory than is free beyond the reserve";
+                rq->error_code = SA_ERR_BUSY;
+                refused_++;
+                live_[rq->id] = std::move(rq);
+                cv_done_.notify_all();
+            }
+            continue;
+        }
         // one NAM pipeline for the queued requests at the front, up to a read budget (the
-        // fixed cost of a pipeline run is paid once), all single-end or all paired-end
+        // fixed cost of a pipeline run is paid once) and to the device memory free for the
+        // workspace, all single-end or all paired-end
         group.clear();
-        uint64_t group_reads = 0;
+        uint64_t group_reads = 0, group_bases = 0;
         const bool paired = queue_.front()->paired;
         while (!queue_.empty() && (group.empty() || (queue_.front()->paired == paired &&
                                                      group_reads + queue_.front()->n_reads <= admit_group_reads_ &&
-                                                     fits(*queue_.front())))) {
+                                                     fits(*queue_.front()) &&
+                                                     mem_ok(group_bases + queue_.front()->total_bases)))) {
             std::unique_ptr<Request> rq = std::move(queue_.front());
             queue_.pop_front();
             Request* r = rq.get();
@@ -395,8 +445,18 @@ void Session::admitter(AdmitLane& lane) {
             live_[r->id] = std::move(rq);
             group.push_back(r);
             group_reads += r->n_reads;
+            group_bases += r->total_bases;
         }
+        const uint64_t grow = growth(group_bases);
+        pending_growth_ += grow;
+        lane.ws_bases = std::max(lane.ws_bases, group_bases);
         admitting_++;
+        for (Request* r : group) r->users++;
+        auto release_group = [&]() {  // with mu_ held
+            pending_growth_ -= grow;  // allocated by now (or failed)
+            for (Request* r : group)
+                if (--r->users == 0 && r->state == 3) cv_done_.notify_all();
+        };
         lk.unlock();
         try {
             const auto ta = std::chrono::steady_clock::now();
@@ -409,11 +469,13 @@ void Session::admitter(AdmitLane& lane) {
         } catch (const std::exception& e) {
             lk.lock();
             admitting_--;
+            release_group();
             fail_all(e.what(), dynamic_cast<const Error*>(&e) ? static_cast<const Error&>(e).code : SA_ERR_CUDA);
             return;
         }
         lk.lock();
         admitting_--;
+        release_group();
         for (Request* r : group) {
             if (r->chunks.empty()) {
                 lk.unlock();
@@ -672,6 +734,7 @@ void Session::worker() {
         const bool first = !r->seeded[item.second];
         r->seeded[item.second] = 1;
         running_++;
+        r->users++;
         lk.unlock();
         std::string err;
         try {
@@ -683,6 +746,7 @@ void Session::worker() {
         }
         lk.lock();
         running_--;
+        if (--r->users == 0 && r->state == 3) cv_done_.notify_all();
         if (r->state == 3) continue;  // failed meanwhile
         if (!err.empty()) {
             fail_all("internal: " + err, SA_ERR_INVALID);

@@ -73,6 +73,10 @@ struct Request {
     uint32_t waves = 0;
     uint64_t h2d_bytes = 0, d2h_bytes = 0;  // this request's share of the transfers
     int state = 0;  // 0 queued, 1 admitted, 2 done, 3 failed
+    // threads reading the request's records outside the session lock (admission lanes,
+    // policy workers); a failed request's wait returns only once this is 0, so that a
+    // caller's borrowed buffers are no longer read when it frees them
+    int users = 0;
     std::string error;
     int32_t error_code = 0;
     std::chrono::steady_clock::time_point t_submit, t_admit, t_done;
@@ -80,7 +84,8 @@ struct Request {
 };
 
 struct SessionConfig {
-    uint64_t max_inflight_bases = 1ull << 30;
+    uint64_t max_inflight_bases = 0;      // 0 = sized from free device memory
+    uint64_t device_reserve_bytes = 0;    // 0 = max(2 GiB, 5% of the device)
     uint32_t max_inflight_requests = 0;  // 0 = no limit
     uint32_t policy_threads = 0;         // 0 = all host threads
     uint32_t admission_streams = 2;      // requests admitted concurrently (NAM pipelines in flight)
@@ -93,6 +98,7 @@ struct SessionConfig {
 struct AdmitLane {
     cudaStream_t st = nullptr;
     NamWorkspace nws;
+    uint64_t ws_bases = 0;  // bases the lane's NAM workspace has grown to (admission estimate)
     PinnedBuf<uint8_t> h_seq;
     PinnedBuf<uint64_t> h_off;
     std::vector<uint64_t> h_goff;
@@ -115,6 +121,13 @@ class Session {
     // success the request is released and its output moved out.
     bool wait(uint64_t ticket, int64_t timeout_ms, std::unique_ptr<Request>& out);
     uint64_t in_flight() const;
+    // device read arena (bases) and the device memory admission leaves free
+    uint64_t arena_bases() const { return cfg_.max_inflight_bases; }
+    uint64_t reserve_bytes() const { return reserve_; }
+    uint64_t refused() const { return refused_; }
+    // NAM workspace bytes per base of an admitted group (estimate: syncmers 12,
+    // randstrobes 48, hits 32, anchor counts 8, anchors and chaining state)
+    static constexpr uint64_t NAM_BYTES_PER_BASE = 160;
     const std::vector<ContigInfo>& contigs() const { return contigs_; }
 
   private:
@@ -161,6 +174,9 @@ class Session {
     uint64_t waiting_jobs_ = 0;
     unsigned running_ = 0;
     uint64_t next_id_ = 1;
+    uint64_t reserve_ = 0;         // device memory admission keeps free
+    uint64_t pending_growth_ = 0;  // workspace growth of groups being admitted (not yet allocated)
+    uint64_t refused_ = 0;         // requests refused for lack of device memory
     uint32_t inflight_ = 0;
     bool stop_ = false;
     bool workers_stop_ = false;

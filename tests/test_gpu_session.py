@@ -85,6 +85,38 @@ def test_session_admission_limits(setup):
         s.close()
 
 
+def test_session_admission_by_free_device_memory(setup):
+    # admission is bounded by the device memory free beyond the reserve: with a reserve
+    # that leaves a few hundred MB, requests are admitted in small groups and map to the
+    # same bytes; with a reserve above the free memory, nothing can ever be admitted and
+    # the request is refused (SA_ERR_BUSY) instead of waiting forever
+    import torch
+    sa, refs, idx, r1, r2 = setup
+    reqs = _requests(sa, r1, r2)
+    want = _alone(sa, refs, idx, reqs, use_ssw=1)
+    free, _ = torch.cuda.mem_get_info()
+    s = sa.Session(idx, refs, use_ssw=1, device_reserve_bytes=max(1, free - (400 << 20)))
+    info = s.info
+    assert info["device_reserve_bytes"] == max(1, free - (400 << 20))
+    assert (1 << 24) <= info["arena_bases"] <= (1 << 33)
+    tickets = [s.submit(x, y) for x, y in reqs]
+    for i, t in enumerate(tickets):
+        assert s.wait(t)[0] == want[i], f"request {i} differs under a reduced reserve"
+    assert s.info["refused_requests"] == 0
+    s.close()
+    s = sa.Session(idx, refs, use_ssw=1, device_reserve_bytes=free + (64 << 30))
+    t = s.submit(*reqs[0])
+    with pytest.raises(sa.SaError) as e:
+        s.wait(t)
+    assert e.value.code == -9  # SA_ERR_BUSY
+    assert s.info["refused_requests"] == 1
+    s.close()
+    # the default: the arena from free memory, and the reserve at least 2 GiB
+    s = sa.Session(idx, refs)
+    assert s.info["device_reserve_bytes"] >= (2 << 30) and s.info["arena_bases"] >= (1 << 24)
+    s.close()
+
+
 def test_session_rejects_oversized_and_unknown(setup):
     sa, refs, idx, r1, r2 = setup
     s = sa.Session(idx, refs, use_ssw=1, max_inflight_bases=100_000)

@@ -36,13 +36,18 @@ def test_version_and_defaults_without_gpu():
     m = sa.mapping_defaults()
     assert (m.max_tries, m.rescue_distance, m.match, m.mismatch, m.gap_open, m.gap_extend, m.end_bonus) == \
         (20, 100, 2, 8, 12, 1, 10)
-    # session defaults: 2^30-base arena, two admission lanes, batches copied at submit
+    # session defaults: arena and reserve sized from free device memory at creation,
+    # two admission lanes, batches copied at submit
     from strobealign_gb300 import _lib as L
     sp = L.SessionParams()
     sa.lib().sa_session_params_default(ctypes.byref(sp))
     assert (sp.max_inflight_bases, sp.max_inflight_requests, sp.policy_threads, sp.admission_streams,
-            sp.borrow_inputs) == (1 << 30, 0, 0, 2, 0)
-    assert ctypes.sizeof(L.SessionParams) == 24
+            sp.borrow_inputs, sp.device_reserve_bytes) == (0, 0, 0, 2, 0, 0)
+    assert ctypes.sizeof(L.SessionParams) == 32
+    # batch schedule defaults: four NAM parts, overlapped
+    sc = L.ScheduleParams()
+    sa.lib().sa_schedule_params_default(ctypes.byref(sc))
+    assert (sc.parts, sc.overlap, sc.wave_min_jobs, sc.max_wave_jobs) == (4, 1, 32768, 262144)
 
 
 def test_synthetic_generator_is_deterministic():
