@@ -155,6 +155,7 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
         PrepRec p{};
         p.read = jb.read;
         p.qlen = L;
+        p.diag = NO_DIAG;
         p.ref_id = jb.ref_id;
         r.valid = 0;
         if (jb.kind == JOB_EXTEND_FAST || jb.kind == JOB_EXTEND_FULL) {
@@ -202,6 +203,7 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
                 if (we > clen) we = clen;
                 p.wstart = ws;
                 p.wlen = (uint32_t)(we - ws);
+                p.diag = prs - ws;
                 // Aligner::align returns None for reference segments over 2000 (src/aligner.rs:83-86)
                 p.type = (jb.use_ssw && p.wlen <= 2000 && L > 0) ? 2 : 0;
                 if (!jb.use_ssw) {
@@ -1278,6 +1280,60 @@ __device__ __forceinline__ EndPos wave_pass(bool run, const uint8_t* q, int qlen
     return run ? res : z;
 }
 
+// A lower bound of the score ssw.c's striped passes reach (in either striping), from
+// the NAM's diagonal: the best local path over diagonals d0 - 4 .. d0 + 3 with at most
+// one gap of up to 3 bases, one diagonal per thread of the group (all 32 threads
+// enter).  Such a path is a lower bound of the passes' H: every H takes the diagonal
+// term; a gap entered from a cell reached diagonally is counted by E (computed from H
+// before the lazy-F raise, which already holds the diagonal term) or by F (exact after
+// the lazy-F loop); only a path that goes F then E could be missed, and none is used.
+// When the bound reaches 255 - bias, the byte pass must overflow, so the task can run
+// its word pass directly with the same results.  Returns the group's bound (0 when the
+// group does not run).
+__device__ __forceinline__ int wave_diag_bound(bool run, const uint8_t* q, int qlen, const uint8_t* r, int rlen,
+                                               int d0, const AlignScores& sc, int gl) {
+    constexpr int NEG = -(1 << 28);
+    const int go = sc.gap_open, ge = sc.gap_extend, mat = sc.match, mis = -(int)sc.mismatch;
+    const int rows = __reduce_max_sync(FULLM, run ? qlen : 0);
+    const int delta = d0 + gl - 4;
+    int A = NEG, B = NEG, best = 0;
+    int h1 = NEG, h2 = NEG, h3 = NEG;  // A on this diagonal 1, 2, 3 rows back (h1 = A(i - 1))
+    for (int i = 0; i < rows; i++) {
+        const bool in = run && i < qlen;
+        const int j = i + delta;
+        int s = NEG;
+        if (in && j >= 0 && j < rlen) {
+            const int qc = c_ssw_code[q[i]], rc = c_ssw_code[r[j]];
+            s = (qc == rc && qc < 4) ? mat : mis;
+        }
+        // entries into this diagonal after one gap: deletion from a lower diagonal
+        // (lane - g, row i - 1), insertion from a higher one (lane + g, row i - 1 - g)
+        const int d1 = __shfl_up_sync(FULLM, h1, 1, WV_T), d2 = __shfl_up_sync(FULLM, h1, 2, WV_T),
+                  d3 = __shfl_up_sync(FULLM, h1, 3, WV_T);
+        const int i1 = __shfl_down_sync(FULLM, h2, 1, WV_T), i2 = __shfl_down_sync(FULLM, h3, 2, WV_T);
+        int x = NEG;
+        if (gl >= 1) x = max(x, d1 - go);
+        if (gl >= 2) x = max(x, d2 - go - ge);
+        if (gl >= 3) x = max(x, d3 - go - 2 * ge);
+        if (gl + 1 < WV_T) x = max(x, i1 - go);
+        if (gl + 2 < WV_T) x = max(x, i2 - go - ge);
+        if (s == NEG) {
+            A = NEG;
+            B = NEG;
+        } else {
+            A = max(A, 0) + s;
+            B = max(B, x) + s;
+            best = max(best, max(A, B));
+        }
+        h3 = h2;
+        h2 = h1;
+        h1 = A;
+    }
+#pragma unroll
+    for (int o = WV_T / 2; o; o >>= 1) best = max(best, __shfl_xor_sync(FULLM, best, o, WV_T));
+    return run ? best : 0;
+}
+
 // ssw_align's end searches with wave_pass for tasks of reads up to 8 * NMAX nt, in
 // the longest-first order of k_ssw: each warp takes four consecutive tasks (one per
 // group of eight threads) and runs the forward byte pass, the forward word pass of the
@@ -1314,12 +1370,20 @@ __global__ void __launch_bounds__(128, 4) k_ssw_wave(SswTask* tasks, const uint3
             q = arena + pr.arena_off;
         }
         const uint8_t* r = q + qlen;
+        // a byte pass that must overflow is skipped: the word pass alone gives the same
+        // results (the task's diagonal bound reaches 255 - bias)
+        const uint32_t d0 = have ? prep[tasks[ti].job].diag : NO_DIAG;
+        const bool try_bound = have && d0 != NO_DIAG && qlen * (int)sc.match >= 255 - bias;
+        bool certain = false;
+        if (__any_sync(FULLM, try_bound))
+            certain = wave_diag_bound(try_bound, q, qlen, r, wlen, (int)d0, sc, gl) >= 255 - bias;
         // forward: byte, word on overflow (ext/ssw/ssw.c:840-862)
-        EndPos e = wave_pass<NMAX, true>(have, q, qlen, false, r, wlen, false, false, 0, sc, bias, prof, gl, gm);
-        const bool word = have && e.score == 255;
+        EndPos e = wave_pass<NMAX, true>(have && !certain, q, qlen, false, r, wlen, false, false, 0, sc, bias, prof, gl,
+                                         gm);
+        const bool word = have && (certain || e.score == 255);
         const EndPos ew = wave_pass<NMAX, false>(word, q, qlen, false, r, wlen, false, false, 0, sc, bias, prof, gl,
                                                  gm);
-        unsigned long long c_fb = (unsigned long long)qlen * e.cols, c_fw = 0, c_rb = 0, c_rw = 0;
+        unsigned long long c_fb = certain ? 0 : (unsigned long long)qlen * e.cols, c_fw = 0, c_rb = 0, c_rw = 0;
         if (word) {
             e = ew;
             c_fw = (unsigned long long)qlen * e.cols;

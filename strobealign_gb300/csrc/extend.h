@@ -23,8 +23,11 @@ struct PrepRec {
     uint64_t cigar_off;   // first op of this job's CIGAR
     uint64_t h_off;       // banded-DP scratch (ints)
     uint32_t cigar_cap;
-    uint32_t pad_;
+    // SSW task of a NAM extension: the window column of query position 0 on the NAM's
+    // diagonal (NO_DIAG for rescue and stage tasks)
+    uint32_t diag;
 };
+constexpr uint32_t NO_DIAG = 0xffffffffu;
 
 // SSW task state (ext/ssw/ssw.c:818-922 results).
 struct SswTask {

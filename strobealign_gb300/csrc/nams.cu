@@ -847,15 +847,17 @@ __device__ void chain_extract(const uint64_t* dedup, const float* dp, const uint
 
 // The read orientations that have anchors (only the better orientation of a read gets
 // anchors, src/chainer.rs:205-216, so about half are empty), for k_chain4: those with
-// at most CHAIN_GROUP_MAX anchors in `list` (increasing within each warp's 32), taken
-// four per warp, the others in `long_list`, one per warp.  The ranges of those with
+// at most CHAIN_GROUP_MAX anchors in `list`, taken eight per warp, the others in
+// `long_list`, one per warp; key / long_key receive their anchor counts (the lists
+// are then ordered by them).  The ranges of those with
 // more than CHAIN_SORT_SMALL anchors go to sort_begin / sort_end for a segmented sort;
 // k_chain4 sorts the others itself.  n_list: [0] listed, [1] sort ranges, [2] long.
 constexpr uint32_t CHAIN_SORT_SMALL = 256;
 constexpr uint32_t CHAIN_GROUP_MAX = 96;
 
 __global__ void k_seg_list(const uint64_t* seg_count, const uint64_t* seg_off, uint32_t nseg, uint32_t* list,
-                           uint32_t* long_list, uint32_t* n_list, uint64_t* sort_begin, uint64_t* sort_end) {
+                           uint32_t* long_list, uint32_t* n_list, uint64_t* sort_begin, uint64_t* sort_end,
+                           uint32_t* key, uint32_t* long_key) {
     const uint32_t lane = lane_id();
     const uint32_t step = gridDim.x * blockDim.x;
     for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < nseg; base += step) {
@@ -870,8 +872,14 @@ __global__ void k_seg_list(const uint64_t* seg_count, const uint64_t* seg_off, u
         as = __shfl_sync(FULL, as, 0);
         ab = __shfl_sync(FULL, ab, 0);
         al = __shfl_sync(FULL, al, 0);
-        if (shrt) list[as + __popc(bs & lanemask_lt())] = sg;
-        if (lng) long_list[al + __popc(bl & lanemask_lt())] = sg;
+        if (shrt) {
+            list[as + __popc(bs & lanemask_lt())] = sg;
+            key[as + __popc(bs & lanemask_lt())] = (uint32_t)cnt;
+        }
+        if (lng) {
+            long_list[al + __popc(bl & lanemask_lt())] = sg;
+            long_key[al + __popc(bl & lanemask_lt())] = cnt < 0xffffffffull ? (uint32_t)cnt : 0xffffffffu;
+        }
         if (big) {
             const uint32_t k = ab + __popc(bb & lanemask_lt());
             const uint64_t o = seg_off[sg];
@@ -998,6 +1006,141 @@ __device__ __forceinline__ void chain_candidates(uint32_t j, bool in, const uint
         }
     }
 }
+
+// The lookback DP of collinear_chaining (src/chainer.rs:85-180) over anchors [c0, c1)
+// of one read orientation (its anchors at dedup[b ..]) by the whole warp: 32
+// predecessors per step, the early-break rules as a prefix max over the lanes.
+// Predecessors never go below c0 (earlier anchors lie max_ref_gap or more behind, or
+// on another reference, and end the reference's scan without contributing).  With
+// recheck, (best_score, best_index, best_key) is the running best over all anchors
+// before c0 and is updated as the reference updates it (strict >); without, the
+// best-index re-check (:150-165) is left out.
+template <bool RING>
+__device__ void warp_chain_range(const uint64_t* dedup, float* dp, uint32_t* pred, uint64_t b, uint32_t c0, uint32_t c1,
+                                 uint32_t max_ref_gap, const ChainCtx& cc, const AnchorPack& ap, uint64_t* ring_key,
+                                 float* ring_dp, bool recheck, float& best_score, uint32_t& best_index,
+                                 uint64_t& best_key) {
+    const uint32_t lane = lane_id();
+    const uint64_t qmask = (1ULL << ap.qbits) - 1, pmask = (1ULL << ap.pbits) - 1;
+    const float kf = __uint2float_rn(cc.k);
+    uint64_t next_key = c0 < c1 ? dedup[b + c0] : 0;
+    for (uint32_t i = c0; i < c1; i++) {
+        const uint64_t ki = next_key;
+        if (i + 1 < c1) next_key = dedup[b + i + 1];
+        const uint32_t ri = (uint32_t)(ki >> (ap.pbits + ap.qbits)), rsi = (uint32_t)((ki >> ap.qbits) & pmask),
+                       qi = (uint32_t)(ki & qmask);
+        uint32_t lookup_end = i > cc.cp.max_lookback ? i - cc.cp.max_lookback : 0;
+        if (lookup_end < c0) lookup_end = c0;
+        float cur = kf;
+        uint32_t cur_pred = 0xffffffffu;
+        bool stop = false;
+        for (uint32_t base = 0; !stop && base < i - lookup_end; base += 32) {
+            const uint32_t t = base + lane;
+            const bool in = t < i - lookup_end;
+            const uint32_t j = i - 1 - t;
+            bool hard, valid, diag;
+            float val;
+            chain_candidates<RING>(j, in, dedup, dp, b, ring_key, ring_dp, ri, rsi, qi, max_ref_gap, cc, ap, hard,
+                                   valid, diag, val);
+            const uint32_t hb = __ballot_sync(FULL, hard);
+            const uint32_t lim = hb ? (uint32_t)(__ffs(hb) - 1) : 32;
+            if (lane >= lim) valid = false;
+            float incl = valid ? val : -INFINITY;
+            for (int d = 1; d < 32; d <<= 1) {
+                const float y = __shfl_up_sync(FULL, incl, d);
+                if (lane >= (uint32_t)d) incl = fmaxf(incl, y);
+            }
+            float excl = __shfl_up_sync(FULL, incl, 1);
+            if (lane == 0) excl = -INFINITY;
+            const bool upd = valid && val >= fmaxf(cur, excl);
+            const uint32_t ub = __ballot_sync(FULL, upd);
+            const uint32_t sb = __ballot_sync(FULL, upd && diag);
+            uint32_t reach = lim;
+            if (sb) {
+                reach = (uint32_t)__ffs(sb);
+                stop = true;
+            }
+            if (hb) stop = true;
+            const uint32_t um = ub & (reach >= 32 ? FULL : ((1u << reach) - 1));
+            if (um) {
+                const uint32_t last = 31 - __clz(um);
+                cur = __shfl_sync(FULL, val, last);
+                cur_pred = i - 1 - (base + last);
+            }
+        }
+        if (recheck && best_index != 0xffffffffu) {
+            const uint64_t kb = best_key;
+            const uint32_t rb = (uint32_t)(kb >> (ap.pbits + ap.qbits)), rsb = (uint32_t)((kb >> ap.qbits) & pmask),
+                           qb = (uint32_t)(kb & qmask);
+            if (rb == ri && qi > qb) {
+                const uint32_t dq = qi - qb, dr = rsi - rsb;
+                const uint32_t mx = dq > dr ? dq : dr, mn = dq < dr ? dq : dr;
+                if (dr < max_ref_gap && dr > 0 && !ratio_above(mx, mn, cc)) {
+                    const float ns = __fadd_rn(best_score, chain_score(dq, dr, cc));
+                    if (ns > cur) {
+                        cur = ns;
+                        cur_pred = best_index;
+                    }
+                }
+            }
+        }
+        if (lane == 0) {
+            dp[b + i] = cur;
+            pred[b + i] = cur_pred;
+            if (RING) {
+                ring_key[i & 63] = ki;
+                ring_dp[i & 63] = cur;
+            }
+        }
+        if (recheck && cur > best_score) {
+            best_score = cur;
+            best_index = i;
+            best_key = ki;
+        }
+        if (!recheck && cur > best_score) best_score = cur;  // the range's maximum
+        __syncwarp();
+    }
+}
+
+// The same for a small cluster [c0, c1) by one thread, without the re-check; returns
+// the cluster's maximum.
+__device__ float lane_chain_range(const uint64_t* dedup, float* dp, uint32_t* pred, uint64_t b, uint32_t c0,
+                                  uint32_t c1, uint32_t max_ref_gap, const ChainCtx& cc, const AnchorPack& ap) {
+    const uint64_t qmask = (1ULL << ap.qbits) - 1, pmask = (1ULL << ap.pbits) - 1;
+    const float kf = __uint2float_rn(cc.k);
+    float mx = 0.0f;
+    for (uint32_t i = c0; i < c1; i++) {
+        const uint64_t ki = dedup[b + i];
+        const uint32_t rsi = (uint32_t)((ki >> ap.qbits) & pmask), qi = (uint32_t)(ki & qmask);
+        uint32_t lookup_end = i > cc.cp.max_lookback ? i - cc.cp.max_lookback : 0;
+        if (lookup_end < c0) lookup_end = c0;
+        float cur = kf;
+        uint32_t cur_pred = 0xffffffffu;
+        for (uint32_t j = i; j-- > lookup_end;) {
+            // one reference within a cluster: the reference's ref_id break cannot fire
+            const uint64_t kj = dedup[b + j];
+            const uint32_t rsj = (uint32_t)((kj >> ap.qbits) & pmask), qj = (uint32_t)(kj & qmask);
+            if (qi < qj) continue;
+            const uint32_t dq = qi - qj, dr = rsi - rsj;
+            if (dr >= max_ref_gap) break;
+            const uint32_t a = dq > dr ? dq : dr, m = dq < dr ? dq : dr;
+            if (ratio_above(a, m, cc)) continue;
+            const float ns = __fadd_rn(dp[b + j], chain_score(dq, dr, cc));
+            if (ns >= cur) {
+                cur = ns;
+                cur_pred = j;
+                if (dq == dr) break;
+            }
+        }
+        dp[b + i] = cur;
+        pred[b + i] = cur_pred;
+        if (cur > mx) mx = cur;
+    }
+    return mx;
+}
+
+// Anchors per cluster above which a cluster is scored by the whole warp
+constexpr uint32_t CHAIN_LANE_CLUSTER_MAX = 48;
 
 template <bool RING>
 __global__ void __launch_bounds__(32 * CHAIN_WARPS, 8) k_chain4(const uint64_t* __restrict__ off, uint32_t n, const uint64_t* seg_off,
@@ -1160,7 +1303,16 @@ __global__ void __launch_bounds__(32 * CHAIN_WARPS, 8) k_chain4(const uint64_t* 
             const float bs = __shfl_sync(FULL, best_score, (lane % NG) * CG);
             if (lane < NG) my_best = bs;
         } else {
-            // the whole warp per orientation
+            // the whole warp per orientation.  Anchors sorted by (reference, position)
+            // fall into clusters: a new one starts where the reference changes or the
+            // position jumps by max_ref_gap or more.  A predecessor scan never crosses
+            // into an earlier cluster, so every cluster's DP depends on the others only
+            // through the best-index re-check, which can fire only once the cluster
+            // holds the running best (a strict maximum over all earlier anchors).  The
+            // clusters are scored at once without the re-check (small ones a thread
+            // each, large ones by the warp); then, in order, each cluster whose maximum
+            // beats the running best of the clusters before it is scored again with
+            // the re-check, and the running best is carried on.  The others are final.
             uint64_t* ring_key = ring_key_s + (RING ? wib * NG * 64 : 0);
             float* ring_dp = ring_dp_s + (RING ? wib * NG * 64 : 0);
             for (uint32_t q = 0; q < NG; q++) {
@@ -1169,85 +1321,79 @@ __global__ void __launch_bounds__(32 * CHAIN_WARPS, 8) k_chain4(const uint64_t* 
                 if (sg == NONE || N == 0) continue;
                 const uint32_t read_len = (uint32_t)(off[(sg >> 1) + 1] - off[sg >> 1]);
                 const uint32_t max_ref_gap = cc.cp.max_ref_gap ? cc.cp.max_ref_gap : read_len;
+                // cluster starts (aux[b ..]), maxima (aux[T + b ..]) and large clusters
+                // (aux[2T + b ..]); chain_extract reuses the three after the DP
+                uint32_t* cstart = aux + b;
+                float* cmax = reinterpret_cast<float*>(aux + total_anchors + b);
+                uint32_t* cbig = aux + 2 * total_anchors + b;
+                uint32_t C = 0;
+                for (uint32_t c = 0; c < N; c += 32) {
+                    const uint32_t i = c + lane;
+                    bool st = false;
+                    if (i < N) {
+                        if (i == 0) {
+                            st = true;
+                        } else {
+                            const uint64_t ki = dedup[b + i], kp = dedup[b + i - 1];
+                            st = (ki >> (ap.pbits + ap.qbits)) != (kp >> (ap.pbits + ap.qbits)) ||
+                                 (uint32_t)((ki >> ap.qbits) & pmask) - (uint32_t)((kp >> ap.qbits) & pmask) >=
+                                     max_ref_gap;
+                        }
+                    }
+                    const uint32_t bal = __ballot_sync(FULL, st);
+                    if (st) cstart[C + __popc(bal & lanemask_lt())] = i;
+                    C += __popc(bal);
+                }
+                __syncwarp();
+                // scoring without the re-check: small clusters a thread each
+                uint32_t nbig = 0;
+                for (uint32_t c0 = 0; c0 < C; c0 += 32) {
+                    const uint32_t c = c0 + lane;
+                    bool big = false;
+                    if (c < C) {
+                        const uint32_t lo = cstart[c], hi = c + 1 < C ? cstart[c + 1] : N;
+                        big = hi - lo > CHAIN_LANE_CLUSTER_MAX;
+                        if (!big) cmax[c] = lane_chain_range(dedup, dp, pred, b, lo, hi, max_ref_gap, cc, ap);
+                    }
+                    const uint32_t bal = __ballot_sync(FULL, big);
+                    if (big) cbig[nbig + __popc(bal & lanemask_lt())] = c;
+                    nbig += __popc(bal);
+                }
+                __syncwarp();
+                // large clusters by the warp
+                for (uint32_t x = 0; x < nbig; x++) {
+                    const uint32_t c = cbig[x];
+                    const uint32_t lo = cstart[c], hi = c + 1 < C ? cstart[c + 1] : N;
+                    float mx = 0.0f;
+                    uint32_t bi = 0xffffffffu;
+                    uint64_t bk = 0;
+                    warp_chain_range<RING>(dedup, dp, pred, b, lo, hi, max_ref_gap, cc, ap, ring_key, ring_dp, false,
+                                           mx, bi, bk);
+                    if (lane == 0) cmax[c] = mx;
+                    __syncwarp();
+                }
+                __syncwarp();
+                // in order: clusters whose maximum beats the running best, scored again
                 float best_score = 0.0f;
                 uint32_t best_index = 0xffffffffu;
                 uint64_t best_key = 0;
-                uint64_t next_key = dedup[b];
-                for (uint32_t i = 0; i < N; i++) {
-                    const uint64_t ki = next_key;
-                    if (i + 1 < N) next_key = dedup[b + i + 1];
-                    const uint32_t ri = (uint32_t)(ki >> (ap.pbits + ap.qbits)),
-                                   rsi = (uint32_t)((ki >> ap.qbits) & pmask), qi = (uint32_t)(ki & qmask);
-                    const uint32_t lookup_end = i > cc.cp.max_lookback ? i - cc.cp.max_lookback : 0;
-                    float cur = kf;
-                    uint32_t cur_pred = 0xffffffffu;
-                    bool stop = false;
-                    for (uint32_t base = 0; !stop && base < i - lookup_end; base += 32) {
-                        const uint32_t t = base + lane;
-                        const bool in = t < i - lookup_end;
-                        const uint32_t j = i - 1 - t;
-                        bool hard, valid, diag;
-                        float val;
-                        chain_candidates<RING>(j, in, dedup, dp, b, ring_key, ring_dp, ri, rsi, qi, max_ref_gap, cc,
-                                               ap, hard, valid, diag, val);
-                        const uint32_t hb = __ballot_sync(FULL, hard);
-                        const uint32_t lim = hb ? (uint32_t)(__ffs(hb) - 1) : 32;
-                        if (lane >= lim) valid = false;
-                        float incl = valid ? val : -INFINITY;
-                        for (int d = 1; d < 32; d <<= 1) {
-                            const float y = __shfl_up_sync(FULL, incl, d);
-                            if (lane >= (uint32_t)d) incl = fmaxf(incl, y);
-                        }
-                        float excl = __shfl_up_sync(FULL, incl, 1);
-                        if (lane == 0) excl = -INFINITY;
-                        const bool upd = valid && val >= fmaxf(cur, excl);
-                        const uint32_t ub = __ballot_sync(FULL, upd);
-                        const uint32_t sb = __ballot_sync(FULL, upd && diag);
-                        uint32_t reach = lim;
-                        if (sb) {
-                            reach = (uint32_t)__ffs(sb);
-                            stop = true;
-                        }
-                        if (hb) stop = true;
-                        const uint32_t um = ub & (reach >= 32 ? FULL : ((1u << reach) - 1));
-                        if (um) {
-                            const uint32_t last = 31 - __clz(um);
-                            cur = __shfl_sync(FULL, val, last);
-                            cur_pred = i - 1 - (base + last);
-                        }
+                for (uint32_t c0 = 0; c0 < C; c0 += 32) {
+                    const uint32_t c = c0 + lane;
+                    const float m = c < C ? cmax[c] : -INFINITY;
+                    uint32_t from = 0;
+                    for (;;) {
+                        const bool rec = c < C && lane >= from && (best_index == 0xffffffffu || m > best_score);
+                        const uint32_t bal = __ballot_sync(FULL, rec);
+                        if (!bal) break;
+                        const uint32_t l = __ffs(bal) - 1, cc0 = c0 + l;
+                        const uint32_t lo = cstart[cc0], hi = cc0 + 1 < C ? cstart[cc0 + 1] : N;
+                        warp_chain_range<RING>(dedup, dp, pred, b, lo, hi, max_ref_gap, cc, ap, ring_key, ring_dp,
+                                               true, best_score, best_index, best_key);
+                        from = l + 1;
                     }
-                    if (best_index != 0xffffffffu) {
-                        const uint64_t kb = best_key;
-                        const uint32_t rb = (uint32_t)(kb >> (ap.pbits + ap.qbits)),
-                                       rsb = (uint32_t)((kb >> ap.qbits) & pmask), qb = (uint32_t)(kb & qmask);
-                        if (rb == ri && qi > qb) {
-                            const uint32_t dq = qi - qb, dr = rsi - rsb;
-                            const uint32_t mx = dq > dr ? dq : dr, mn = dq < dr ? dq : dr;
-                            if (dr < max_ref_gap && dr > 0 && !ratio_above(mx, mn, cc)) {
-                                const float ns = __fadd_rn(best_score, chain_score(dq, dr, cc));
-                                if (ns > cur) {
-                                    cur = ns;
-                                    cur_pred = best_index;
-                                }
-                            }
-                        }
-                    }
-                    if (lane == 0) {
-                        dp[b + i] = cur;
-                        pred[b + i] = cur_pred;
-                        if (RING) {
-                            ring_key[i & 63] = ki;
-                            ring_dp[i & 63] = cur;
-                        }
-                    }
-                    if (cur > best_score) {
-                        best_score = cur;
-                        best_index = i;
-                        best_key = ki;
-                    }
-                    __syncwarp();
                 }
                 if (lane == q) my_best = best_score;
+                __syncwarp();
             }
         }
         __syncwarp();
@@ -1539,9 +1685,13 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     ws.sort_end.reserve(2 * (size_t)n);
     uint32_t* const long_list = ws.seg_list.p + 2 * (size_t)n;
     uint32_t* const list_counts = ws.seg_list.p + 4 * (size_t)n;
+    ws.seg_key.reserve(4 * (size_t)n);
+    ws.seg_key_alt.reserve(4 * (size_t)n);
+    ws.seg_sorted.reserve(4 * (size_t)n);
     SA_CUDA(cudaMemsetAsync(list_counts, 0, 12, st));
     k_seg_list<<<warps_grid((2 * (uint64_t)n + 31) / 32), 32 * WARPS_PER_BLOCK, 0, st>>>(
-        ws.seg_count.p, ws.seg_off.p, 2 * n, ws.seg_list.p, long_list, list_counts, ws.sort_begin.p, ws.sort_end.p);
+        ws.seg_count.p, ws.seg_off.p, 2 * n, ws.seg_list.p, long_list, list_counts, ws.sort_begin.p, ws.sort_end.p,
+        ws.seg_key.p, ws.seg_key.p + 2 * (size_t)n);
     launches++;
     uint64_t total_anchors = 0;
     uint32_t n_list[3] = {0, 0, 0};
@@ -1568,6 +1718,36 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
                                            st);
         kt->end(st);
         launches++;
+    }
+    // read orientations by anchor count, largest first: the eight orientations of a
+    // grouped warp then have similar counts (the warp runs as many steps as its largest
+    // one), and the long orientations start first
+    const uint32_t* short_list = ws.seg_list.p;
+    const uint32_t* long_sorted = long_list;
+    {
+        size_t tmp = 0, t2 = 0;
+        if (n_list[0] > 1)
+            cub::DeviceRadixSort::SortPairsDescending(nullptr, tmp, ws.seg_key.p, ws.seg_key_alt.p, ws.seg_list.p,
+                                                      ws.seg_sorted.p, (int64_t)n_list[0], 0, 8, st);
+        if (n_list[2] > 1)
+            cub::DeviceRadixSort::SortPairsDescending(nullptr, t2, ws.seg_key.p, ws.seg_key_alt.p, ws.seg_list.p,
+                                                      ws.seg_sorted.p, (int64_t)n_list[2], 0, 32, st);
+        ws.cub_tmp.reserve(std::max(tmp, t2));
+        kt->begin(KS_NAMS_OTHER, st);
+        if (n_list[0] > 1) {
+            cub::DeviceRadixSort::SortPairsDescending(ws.cub_tmp.p, tmp, ws.seg_key.p, ws.seg_key_alt.p,
+                                                      ws.seg_list.p, ws.seg_sorted.p, (int64_t)n_list[0], 0, 8, st);
+            short_list = ws.seg_sorted.p;
+            launches++;
+        }
+        if (n_list[2] > 1) {
+            const size_t o = 2 * (size_t)n;
+            cub::DeviceRadixSort::SortPairsDescending(ws.cub_tmp.p, t2, ws.seg_key.p + o, ws.seg_key_alt.p + o,
+                                                      long_list, ws.seg_sorted.p + o, (int64_t)n_list[2], 0, 32, st);
+            long_sorted = ws.seg_sorted.p + o;
+            launches++;
+        }
+        kt->end(st);
     }
     ws.dp.reserve(total_anchors);
     ws.pred.reserve(total_anchors);
@@ -1605,12 +1785,12 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
         k_chain4<true><<<chain_grid, 32 * CHAIN_WARPS, 0, st>>>(
             ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p,
             total_anchors, ap, cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
-            cfg.nam_anchors ? ws.anc_start.p : nullptr, ws.seg_list.p, n_list[0], long_list, n_list[2]);
+            cfg.nam_anchors ? ws.anc_start.p : nullptr, short_list, n_list[0], long_sorted, n_list[2]);
     else
         k_chain4<false><<<chain_grid, 32 * CHAIN_WARPS, 0, st>>>(
             ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p,
             total_anchors, ap, cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
-            cfg.nam_anchors ? ws.anc_start.p : nullptr, ws.seg_list.p, n_list[0], long_list, n_list[2]);
+            cfg.nam_anchors ? ws.anc_start.p : nullptr, short_list, n_list[0], long_sorted, n_list[2]);
     kt->end(st);
     launches++;
     ws.nam_count.reserve((size_t)n + 1);

@@ -50,6 +50,8 @@ struct NamWorkspace {
     // read orientations with anchors (2n slots), their count in slot 2n and the count of
     // those sorted by the segmented sort in slot 2n + 1; that sort's ranges
     DevBuf<uint32_t> seg_list;
+    // seg_list's anchor counts, and the lists ordered by them (descending) for k_chain4
+    DevBuf<uint32_t> seg_key, seg_key_alt, seg_sorted;
     DevBuf<uint64_t> sort_begin, sort_end;
     DevBuf<uint64_t> long_begin, long_end;
     // with NamConfig::nam_anchors: the anchors of each NAM's chain, last to first
