@@ -298,7 +298,14 @@ def parity_leg(g, r1, r2, rl, idx, gpu_sam: bytes, use_ssw: bool, threads: int) 
         first = {"byte": k, "line": line, "gpu": gpu_sam[lo:gpu_sam.find(b"\n", k)][:300].decode(errors="replace"),
                  "oracle": want[lo:want.find(b"\n", k)][:300].decode(errors="replace")}
     reads = len(r1) * (2 if r2 is not None else 1)
+    # the lookup roofline's algorithmic bytes: distinct 32-byte index sectors the
+    # reference's lookups read per read, counted by the oracle on a sample
+    m = min(len(r1), 20000)
+    sec = [o.lookup_sectors(_prefix(x, m)) for x in (r1, r2) if x is not None]
+    sectors = {"sample_reads": sum(x["reads"] for x in sec), "dir_sectors": sum(x["dir_sectors"] for x in sec),
+               "table_sectors": sum(x["table_sectors"] for x in sec), "randstrobes": sum(x["randstrobes"] for x in sec)}
     parity = {"reads": reads, "records": len(r1), "sam_bytes": len(gpu_sam), "identical": same, "first_diff": first,
+              "lookup_sectors": sectors,
               "index_identical": index_same, "index": {"bits": bits, "filter_cutoff": cutoff, "randstrobes": n},
               "oracle_index_s": round(o.build_seconds, 2), "oracle_map_s": round(sec, 2),
               "leg_s": round(time.perf_counter() - t0, 1)}
@@ -533,7 +540,10 @@ def main():
     dom = max(modelled, key=lambda k: modelled[k][0]) if modelled else None
     shares = {k: round(v[0] / total_ms, 4) for k, v in kern.items() if total_ms and v[0] > 0}
     counts = {k: int(st[k]) for k in ("n_bases", "n_randstrobes", "n_anchor_total")}
-    roofline, rooflines = roofline_for(dom, kern, cells, peaks, clk.summary(), counts, args.steps) if dom else (None, {})
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    lookup = (parity or {}).get("lookup_sectors")
+    roofline, rooflines = roofline_for(dom, kern, cells, peaks, clk.summary(), counts, args.steps, sms, n_reads,
+                                       lookup) if dom else (None, {})
     reads_gb = int(R1.seq_offsets[-1]) * (2 if R2 is not None else 1) / 1e9
     out = {
         "metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": ws, "steps": args.steps,
@@ -582,26 +592,42 @@ def main():
 ALGO_BYTES = {
     # read bases in; per randstrobe out: hash, reverse-complement hash, start, end
     "seed": lambda c: c["n_bases"] + 24 * c["n_randstrobes"],
-    # per randstrobe probe: the bucket-directory pair (16 B) and one 32-byte table sector,
-    # and the hit record out (position, info, count: 16 B)
-    "hits": lambda c: 64 * c["n_randstrobes"],
 }
 # stages reported as anchors per second (no HBM or ALU roofline model)
-ANCHOR_RATE = ("anchors", "sort", "chain")
+ANCHOR_RATE = ("sort", "chain")
 
 
-def roofline_for(dom, kern, cells, peaks, clocks, counts, steps) -> dict:
+def roofline_for(dom, kern, cells, peaks, clocks, counts, steps, sms, n_reads, lookup=None) -> dict:
     """Roofline of every timed stage, and of the dominant one.
 
-    Seeding and the index lookups are framed against HBM bandwidth with their
-    algorithmic bytes per launch (ALGO_BYTES, from the batch's counts); the anchor walk,
-    the anchor sort and chaining as anchors per second.  Extension (the SSW kernel k_sw:
-    byte pass, word reruns of the byte overflows, reverse passes) is integer-ALU bound:
-    its unit is one SSW call of |query| x |reference window| canonical cells, against
-    152 SMs x 128 INT32 lanes x SM clock / 11 ops per cell; the cells the passes
-    actually computed are reported beside it."""
+    Seeding is framed against HBM bandwidth with its algorithmic bytes per launch
+    (ALGO_BYTES, from the batch's counts).  The index lookups (the probe, hit and anchor
+    kernels) are framed against HBM random 32-byte sectors: their algorithmic bytes are
+    the distinct index sectors the reference's lookups read per read (the oracle counts
+    them on a sample of the batch, `lookup`), 32 bytes each; without the sample, 64
+    bytes per randstrobe.  The anchor sort and chaining are reported as anchors per
+    second.  Extension (the SSW kernels: byte pass, word passes of the byte overflows,
+    reverse passes) is integer-ALU bound: its unit is one SSW call of |query| x
+    |reference window| canonical cells, against SMs x 128 INT32 lanes x SM clock / 11
+    ops per cell; the cells the passes actually computed are reported beside it."""
     hbm = peaks.get("hbm_gbs", 6800.0)
     out = {}
+    lk = [kern.get(k, [0.0, 0]) for k in ("hits", "anchors")]
+    if lk[0][1]:
+        ms = lk[0][0] + lk[1][0]
+        if lookup and lookup.get("sample_reads"):
+            per_read = 32.0 * (lookup["dir_sectors"] + lookup["table_sectors"]) / lookup["sample_reads"]
+            model = (f"{per_read / 32:.1f} distinct 32-byte index sectors per read (oracle count over "
+                     f"{lookup['sample_reads']} reads of the batch) x 32 B")
+        else:
+            per_read = 64.0 * counts["n_randstrobes"] / max(1, n_reads)
+            model = "64 B per randstrobe probe (no oracle sample)"
+        total = per_read * n_reads * steps
+        achieved = total / (ms / 1000.0) / 1e9 if ms else 0.0
+        out["lookup"] = {"kernel": "k_probe + k_hits + k_anchors", "bound": "hbm (random 32-byte sectors)",
+                         "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                         "avg_launch_ms": ms / max(1, lk[0][1]), "launches": lk[0][1] + lk[1][1],
+                         "algorithmic_bytes_per_read": per_read, "model": model}
     for st, f in ALGO_BYTES.items():
         if st not in kern or not kern[st][1]:
             continue
@@ -623,15 +649,15 @@ def roofline_for(dom, kern, cells, peaks, clocks, counts, steps) -> dict:
         n = kern.get("sw_byte", [0.0, 0])[1] + kern.get("sw_word", [0.0, 0])[1]
         sec = ms / 1000.0
         clock = (clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)) * 1e6
-        peak_gcups = 152 * 128 * clock / 11 / 1e9
+        peak_gcups = sms * 128 * clock / 11 / 1e9
         achieved = cells.get("canonical", 0) / sec / 1e9 if sec else 0.0
         computed = sum(v for k, v in cells.items() if k != "canonical")
         out["sw"] = {"kernel": "k_ssw (byte, word, reverse passes)", "bound": "int32", "achieved": achieved,
                      "peak": peak_gcups, "unit": "GCUPS", "frac": achieved / peak_gcups, "traffic": None,
                      "avg_launch_ms": ms / max(n, 1), "launches": n,
                      "computed_gcups": computed / sec / 1e9 if sec else 0.0, "cells": cells,
-                     "peak_source": "152 SMs x 128 INT32 lanes x median SM clock under load / 11 ops per cell"}
-    key = "sw" if dom in ("sw_byte", "sw_word") else dom
+                     "peak_source": f"{sms} SMs x 128 INT32 lanes x median SM clock under load / 11 ops per cell"}
+    key = "sw" if dom in ("sw_byte", "sw_word") else "lookup" if dom == "hits" else dom
     head = dict(out.get(key) or {"kernel": dom, "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s",
                                  "frac": None, "traffic": None})
     head["stage"] = dom

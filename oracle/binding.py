@@ -43,6 +43,8 @@ def lib() -> C.CDLL:
     L.ora_map_batch.argtypes = [C.c_void_p, C.POINTER(ReadBatch), C.POINTER(ReadBatch), C.POINTER(MapOpts),
                                 C.POINTER(C.c_void_p), C.POINTER(C.c_size_t), C.POINTER(C.c_double)]
     L.ora_output_free.argtypes = [C.c_void_p]
+    L.ora_lookup_sectors.restype = C.c_int32
+    L.ora_lookup_sectors.argtypes = [C.c_void_p, C.POINTER(ReadBatch), C.c_int32, C.c_uint32, C.POINTER(C.c_uint64)]
     return L
 
 
@@ -111,6 +113,16 @@ class OracleIndex:
         finally:
             lib().ora_output_free(out)
         return data, sec.value
+
+    def lookup_sectors(self, reads, mcs: int = 0, rescue_distance: int = 100) -> dict:
+        """Distinct 32-byte index sectors the reference's lookups read per read, summed
+        over a ReadSet-like batch: directory, table, and the randstrobes probed."""
+        keep: list = []
+        b = _batch(reads.seq, reads.offsets, reads.names, reads.name_offsets, None, keep)
+        out = (C.c_uint64 * 3)()
+        lib().ora_lookup_sectors(self.h, C.byref(b), mcs, rescue_distance, out)
+        return {"reads": len(reads), "dir_sectors": int(out[0]), "table_sectors": int(out[1]),
+                "randstrobes": int(out[2])}
 
     def __del__(self):
         if getattr(self, "h", None):

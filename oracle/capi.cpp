@@ -422,4 +422,29 @@ int32_t ora_has_shared_substring(const char* read, size_t rl, const char* ref, s
     return has_shared_substring(std::string(read, rl), std::string(ref, fl), k) ? 1 : 0;
 }
 
+// The index sectors the lookups of get_nams_by_chaining read (32-byte sectors, distinct
+// per read; src/index.rs:127-338, src/hit.rs, src/chainer.rs:304-384): out[0] directory
+// sectors, out[1] table sectors, out[2] randstrobes probed, summed over the reads.
+int32_t ora_lookup_sectors(void* h, const ora_read_batch* b, int32_t mcs, uint32_t rescue_distance, uint64_t* out) {
+    auto* o = (OraIndex*)h;
+    std::vector<uint64_t> sec;
+    const uint64_t dir_lo = (uint64_t)(uintptr_t)o->index.bucket_starts.data() >> 5;
+    const uint64_t dir_hi = (uint64_t)(uintptr_t)(o->index.bucket_starts.data() + o->index.bucket_starts.size()) >> 5;
+    out[0] = out[1] = out[2] = 0;
+    ChainingParameters cp;
+    for (size_t i = 0; i < b->n; i++) {
+        std::string seq(b->seq + b->seq_offsets[i], b->seq_offsets[i + 1] - b->seq_offsets[i]);
+        NamDetails nd;
+        sec.clear();
+        g_sectors = &sec;
+        get_nams_by_chaining(seq, o->index, cp, rescue_distance, (Mcs)mcs, nd);
+        g_sectors = nullptr;
+        std::sort(sec.begin(), sec.end());
+        sec.erase(std::unique(sec.begin(), sec.end()), sec.end());
+        for (uint64_t x : sec) (x >= dir_lo && x <= dir_hi ? out[0] : out[1])++;
+        out[2] += nd.n_randstrobes;
+    }
+    return 0;
+}
+
 }  // extern "C"

@@ -8,12 +8,15 @@
 
 namespace oracle {
 
+thread_local std::vector<uint64_t>* g_sectors = nullptr;
+
 // src/partition.rs:27-88: a lower bound on a monotone predicate
 template <class P>
 static size_t partition_point(const RefRandstrobe* s, size_t n, P pred) {
     size_t lo = 0, hi = n;
     while (lo < hi) {
         size_t mid = lo + (hi - lo) / 2;
+        touch(s + mid);
         if (pred(s[mid])) lo = mid + 1;
         else hi = mid;
     }
@@ -24,6 +27,8 @@ static size_t partition_point(const RefRandstrobe* s, size_t n, P pred) {
 size_t Index::get_masked_from(uint64_t hash, uint64_t mask, size_t start_position, bool has_start) const {
     uint64_t masked = hash & mask;
     size_t top_n = (size_t)(hash >> (64 - bits));
+    if (!has_start) touch(&bucket_starts[top_n]);
+    touch(&bucket_starts[top_n + 1]);
     size_t ps = has_start ? start_position : (size_t)bucket_starts[top_n];
     size_t pe = (size_t)bucket_starts[top_n + 1];
     if (ps >= pe) return SIZE_MAX;
@@ -31,6 +36,7 @@ size_t Index::get_masked_from(uint64_t hash, uint64_t mask, size_t start_positio
     const RefRandstrobe* b = randstrobes.data() + ps;
     if (len < 4) {
         for (size_t i = 0; i < len; i++) {
+            touch(b + i);
             uint64_t h = b[i].hash() & mask;
             if (h == masked) return ps + i;
             if (h > masked) return SIZE_MAX;
@@ -38,19 +44,23 @@ size_t Index::get_masked_from(uint64_t hash, uint64_t mask, size_t start_positio
         return SIZE_MAX;
     }
     size_t pos = partition_point(b, len, [&](const RefRandstrobe& r) { return (r.hash() & mask) < masked; });
+    if (pos < len) touch(b + pos);
     if (pos < len && (b[pos].hash() & mask) == masked) return ps + pos;
     return SIZE_MAX;
 }
 
 // src/index.rs:272-295
 size_t Index::get_count(size_t position, uint64_t mask) const {
+    touch(&randstrobes[position]);
     uint64_t key = randstrobes[position].hash();
     uint64_t masked = key & mask;
     size_t top_n = (size_t)(key >> (64 - bits));
+    touch(&bucket_starts[top_n + 1]);
     size_t pe = (size_t)bucket_starts[top_n + 1];
     if (pe - position < 8) {
         size_t count = 1;
         for (size_t p = position + 1; p < pe; p++) {
+            touch(&randstrobes[p]);
             if ((randstrobes[p].hash() & mask) == masked) count++;
             else break;
         }
@@ -69,7 +79,11 @@ size_t Index::get_count_full(size_t pos, uint64_t hash_revcomp) const {
 
 // src/index.rs:298-307 (the guard uses the index's own filter_cutoff)
 bool Index::is_too_frequent_forward(size_t pos, size_t cutoff) const {
-    if (pos + filter_cutoff < randstrobes.size()) return randstrobes[pos].hash() == randstrobes[pos + cutoff].hash();
+    if (pos + filter_cutoff < randstrobes.size()) {
+        touch(&randstrobes[pos]);
+        touch(&randstrobes[pos + cutoff]);
+        return randstrobes[pos].hash() == randstrobes[pos + cutoff].hash();
+    }
     return false;
 }
 
@@ -87,6 +101,10 @@ bool Index::is_too_frequent(size_t pos, size_t cutoff, uint64_t hash_revcomp) co
 
 // src/index.rs:325-337
 bool Index::is_too_frequent_partial(size_t pos, size_t cutoff) const {
+    if (pos + cutoff < randstrobes.size()) {
+        touch(&randstrobes[pos]);
+        touch(&randstrobes[pos + cutoff]);
+    }
     if (pos + cutoff < randstrobes.size())
         return (randstrobes[pos].hash() & params.main_hash_mask) ==
                (randstrobes[pos + cutoff].hash() & params.main_hash_mask);
@@ -231,6 +249,7 @@ std::vector<Anchor> hits_to_anchors(const std::vector<Hit>& hits, const Index& i
             uint64_t fh = idx.randstrobes[e].hash_offset & idx.params.forward_main_hash_mask;
             for (size_t i = e; i < idx.randstrobes.size(); i++) {
                 const RefRandstrobe& r = idx.randstrobes[i];
+                touch(&r);
                 if ((r.hash_offset & idx.params.forward_main_hash_mask) != fh) break;
                 a.push_back(Anchor{r.ref_index, r.position, h.query_start});
             }
@@ -239,6 +258,7 @@ std::vector<Anchor> hits_to_anchors(const std::vector<Hit>& hits, const Index& i
             uint64_t fh = idx.randstrobes[h.position].hash();
             for (size_t i = h.position; i < idx.randstrobes.size(); i++) {
                 const RefRandstrobe& r = idx.randstrobes[i];
+                touch(&r);
                 if (r.hash() != fh) break;
                 size_t ref_start = r.position;
                 size_t ref_end = ref_start + r.offset() + k;

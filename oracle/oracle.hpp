@@ -75,6 +75,13 @@ void randstrobes_query(const std::string& seq, const SeedingParameters& p,
                        std::vector<QueryRandstrobe> out[2]);
 
 // ---------------------------------------------------------------- index
+// Measurement hook (bench.py's lookup roofline): while g_sectors points to a vector,
+// every index array element the lookups read appends its 32-byte sector address.
+extern thread_local std::vector<uint64_t>* g_sectors;
+inline void touch(const void* p) {
+    if (g_sectors) g_sectors->push_back((uint64_t)(uintptr_t)p >> 5);
+}
+
 // src/index.rs:15-110
 constexpr uint64_t REF_RANDSTROBE_HASH_MASK = 0xFFFFFFFFFFFFFF00ULL;
 struct RefRandstrobe {

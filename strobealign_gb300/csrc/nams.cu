@@ -1345,12 +1345,13 @@ __global__ void __launch_bounds__(32 * CHAIN_WARPS, 8) k_chain4(const uint64_t* 
                     C += __popc(bal);
                 }
                 __syncwarp();
-                // scoring without the re-check: small clusters a thread each
+                // scoring without the re-check: small clusters a thread each (the first
+                // cluster always holds the running best, so it is scored only below)
                 uint32_t nbig = 0;
                 for (uint32_t c0 = 0; c0 < C; c0 += 32) {
                     const uint32_t c = c0 + lane;
                     bool big = false;
-                    if (c < C) {
+                    if (c < C && c > 0) {
                         const uint32_t lo = cstart[c], hi = c + 1 < C ? cstart[c + 1] : N;
                         big = hi - lo > CHAIN_LANE_CLUSTER_MAX;
                         if (!big) cmax[c] = lane_chain_range(dedup, dp, pred, b, lo, hi, max_ref_gap, cc, ap);
@@ -1379,7 +1380,7 @@ __global__ void __launch_bounds__(32 * CHAIN_WARPS, 8) k_chain4(const uint64_t* 
                 uint64_t best_key = 0;
                 for (uint32_t c0 = 0; c0 < C; c0 += 32) {
                     const uint32_t c = c0 + lane;
-                    const float m = c < C ? cmax[c] : -INFINITY;
+                    const float m = c < C && c > 0 ? cmax[c] : -INFINITY;
                     uint32_t from = 0;
                     for (;;) {
                         const bool rec = c < C && lane >= from && (best_index == 0xffffffffu || m > best_score);

@@ -410,7 +410,13 @@ void Session::admitter(AdmitLane& lane) {
         if (broken_ || stop_) break;
         if (queue_.empty() || !fits(*queue_.front())) continue;
         if (!mem_ok(queue_.front()->total_bases)) {
-            if (inflight_ == 0 && admitting_ == 0) {
+            // a lane whose workspace already holds the request takes it instead
+            bool other = false;
+            for (auto& l : lanes_) other = other || l->ws_bases >= queue_.front()->total_bases;
+            if (other) {
+                cv_admit_.notify_all();
+                cv_admit_.wait_for(lk, std::chrono::milliseconds(20));  // releases the lock meanwhile
+            } else if (inflight_ == 0 && admitting_ == 0) {
                 // nothing in flight will free memory: refuse the request
                 std::unique_ptr<Request> rq = std::move(queue_.front());
                 queue_.pop_front();
@@ -421,6 +427,11 @@ void Session::admitter(AdmitLane& lane) {
                 refused_++;
                 live_[rq->id] = std::move(rq);
                 cv_done_.notify_all();
+            } else {
+                // memory frees as admissions and requests in flight finish: wait (the
+                // lock is released meanwhile; the predicate wait above would return at
+                // once and spin with it held)
+                cv_admit_.wait_for(lk, std::chrono::milliseconds(20));
             }
             continue;
         }
