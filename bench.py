@@ -301,9 +301,10 @@ def parity_leg(g, r1, r2, rl, idx, gpu_sam: bytes, use_ssw: bool, threads: int) 
     # the lookup roofline's algorithmic bytes: distinct 32-byte index sectors the
     # reference's lookups read per read, counted by the oracle on a sample
     m = min(len(r1), 20000)
-    sec = [o.lookup_sectors(_prefix(x, m)) for x in (r1, r2) if x is not None]
-    sectors = {"sample_reads": sum(x["reads"] for x in sec), "dir_sectors": sum(x["dir_sectors"] for x in sec),
-               "table_sectors": sum(x["table_sectors"] for x in sec), "randstrobes": sum(x["randstrobes"] for x in sec)}
+    cnt = [o.lookup_sectors(_prefix(x, m)) for x in (r1, r2) if x is not None]
+    sectors = {"sample_reads": sum(x["reads"] for x in cnt), "dir_sectors": sum(x["dir_sectors"] for x in cnt),
+               "table_sectors": sum(x["table_sectors"] for x in cnt),
+               "randstrobes": sum(x["randstrobes"] for x in cnt)}
     parity = {"reads": reads, "records": len(r1), "sam_bytes": len(gpu_sam), "identical": same, "first_diff": first,
               "lookup_sectors": sectors,
               "index_identical": index_same, "index": {"bits": bits, "filter_cutoff": cutoff, "randstrobes": n},
