@@ -1042,6 +1042,13 @@ __device__ void warp_chain_range(const uint64_t* dedup, float* dp, uint32_t* pre
             float val;
             chain_candidates<RING>(j, in, dedup, dp, b, ring_key, ring_dp, ri, rsi, qi, max_ref_gap, cc, ap, hard,
                                    valid, diag, val);
+            // the common case: the first candidate updates and lies on the same diagonal,
+            // which ends the scan (the prefix max below would find the same)
+            if (__ballot_sync(FULL, lane == 0 && valid && diag && val >= cur)) {
+                cur = __shfl_sync(FULL, val, 0);
+                cur_pred = i - 1 - base;
+                break;
+            }
             const uint32_t hb = __ballot_sync(FULL, hard);
             const uint32_t lim = hb ? (uint32_t)(__ffs(hb) - 1) : 32;
             if (lane >= lim) valid = false;
@@ -1142,13 +1149,153 @@ __device__ float lane_chain_range(const uint64_t* dedup, float* dp, uint32_t* pr
 // Anchors per cluster above which a cluster is scored by the whole warp
 constexpr uint32_t CHAIN_LANE_CLUSTER_MAX = 48;
 
+// Sort (orientations up to CHAIN_SORT_SMALL anchors, whose keys are still unsorted in
+// the dedup buffer) or take the segmented sort's output, and deduplicate
+// (src/chainer.rs:228-229) the anchors [b, e) of one read orientation into
+// dedup[b ..]; returns the count.  The whole warp.
+__device__ __forceinline__ uint32_t orientation_dedup(const uint64_t* sorted, uint64_t* dedup, uint64_t b, uint64_t e) {
+    const uint32_t lane = lane_id();
+    const uint32_t cnt = (uint32_t)(e - b);
+    if (cnt <= CHAIN_SORT_SMALL) {
+        if (cnt <= 32) return warp_sort_dedup<1>(dedup + b, cnt);
+        if (cnt <= 64) return warp_sort_dedup<2>(dedup + b, cnt);
+        if (cnt <= 128) return warp_sort_dedup<4>(dedup + b, cnt);
+        return warp_sort_dedup<8>(dedup + b, cnt);
+    }
+    uint32_t N = 0;
+    for (uint64_t c = b; c < e; c += 32) {
+        const uint64_t i = c + lane;
+        bool keep = false;
+        uint64_t key = 0;
+        if (i < e) {
+            key = sorted[i];
+            keep = i == b || sorted[i - 1] != key;
+        }
+        const uint32_t bal = __ballot_sync(FULL, keep);
+        if (keep) dedup[b + N + __popc(bal & lanemask_lt())] = key;
+        N += __popc(bal);
+    }
+    return N;
+}
+
+// Long read orientations (more than CHAIN_GROUP_MAX anchors), before k_chain4.  Anchors
+// sorted by (reference, position) fall into clusters: a new one starts where the
+// reference changes or the position jumps by max_ref_gap or more.  A predecessor scan
+// never crosses into an earlier cluster (the reference's scan breaks there or skips
+// without contributing), so a cluster's DP depends on the others only through the
+// best-index re-check (src/chainer.rs:150-165), which can fire only once the cluster
+// holds the running best, a strict maximum over all earlier anchors.  So the clusters
+// are scored at once without the re-check, here, and k_chain4 then scores again, in
+// order, each cluster whose maximum beats the running best of the clusters before it
+// (with the re-check, carrying the running best on); the others are final.
+//
+// k_chain_long_prep: a warp per long orientation u: the dedup, the cluster starts
+// (aux[b ..]), and the clusters of up to CHAIN_LANE_CLUSTER_MAX anchors scored a
+// thread each (maxima at aux[T + b ..] as floats); the larger ones (except the first,
+// which k_chain4 scores with the re-check anyway) are queued as (u, cluster) items for
+// k_chain_big, a warp each.  long_n[u] / long_c[u]: anchors after dedup, clusters.
+__global__ void __launch_bounds__(128) k_chain_long_prep(const uint64_t* __restrict__ off, const uint64_t* seg_off,
+                                                         const uint64_t* sorted, uint64_t* dedup, float* dp,
+                                                         uint32_t* pred, uint32_t* aux, uint64_t total_anchors,
+                                                         AnchorPack ap, ChainCtx cc, const uint32_t* long_list,
+                                                         uint32_t n_long, uint32_t* long_n, uint32_t* long_c,
+                                                         uint32_t* big_items, uint32_t* n_big) {
+    const uint32_t lane = lane_id();
+    const uint64_t pmask = (1ULL << ap.pbits) - 1;
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t u = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; u < n_long; u += nwarps) {
+        const uint32_t sg = long_list[u];
+        const uint64_t b = seg_off[sg], e = seg_off[sg + 1];
+        const uint32_t N = orientation_dedup(sorted, dedup, b, e);
+        __syncwarp();
+        const uint32_t read_len = (uint32_t)(off[(sg >> 1) + 1] - off[sg >> 1]);
+        const uint32_t max_ref_gap = cc.cp.max_ref_gap ? cc.cp.max_ref_gap : read_len;
+        uint32_t* cstart = aux + b;
+        float* cmax = reinterpret_cast<float*>(aux + total_anchors + b);
+        uint32_t C = 0;
+        for (uint32_t c = 0; c < N; c += 32) {
+            const uint32_t i = c + lane;
+            bool st = false;
+            if (i < N) {
+                if (i == 0) {
+                    st = true;
+                } else {
+                    const uint64_t ki = dedup[b + i], kp = dedup[b + i - 1];
+                    st = (ki >> (ap.pbits + ap.qbits)) != (kp >> (ap.pbits + ap.qbits)) ||
+                         (uint32_t)((ki >> ap.qbits) & pmask) - (uint32_t)((kp >> ap.qbits) & pmask) >= max_ref_gap;
+                }
+            }
+            const uint32_t bal = __ballot_sync(FULL, st);
+            if (st) cstart[C + __popc(bal & lanemask_lt())] = i;
+            C += __popc(bal);
+        }
+        __syncwarp();
+        for (uint32_t c0 = 0; c0 < C; c0 += 32) {
+            const uint32_t c = c0 + lane;
+            bool big = false;
+            if (c < C && c > 0) {
+                const uint32_t lo = cstart[c], hi = c + 1 < C ? cstart[c + 1] : N;
+                big = hi - lo > CHAIN_LANE_CLUSTER_MAX;
+                if (!big) cmax[c] = lane_chain_range(dedup, dp, pred, b, lo, hi, max_ref_gap, cc, ap);
+            }
+            const uint32_t bal = __ballot_sync(FULL, big);
+            uint32_t at = 0;
+            if (lane == 0 && bal) at = atomicAdd(n_big, (uint32_t)__popc(bal));
+            at = __shfl_sync(FULL, at, 0);
+            if (big) {
+                const uint32_t x = at + __popc(bal & lanemask_lt());
+                big_items[2 * x] = u;
+                big_items[2 * x + 1] = c;
+            }
+        }
+        if (lane == 0) {
+            long_n[u] = N;
+            long_c[u] = C;
+        }
+        __syncwarp();
+    }
+}
+
+// The queued large clusters, a warp each, without the re-check (their maxima into
+// aux[T + b + cluster]).
+template <bool RING>
+__global__ void __launch_bounds__(128) k_chain_big(const uint64_t* __restrict__ off, const uint64_t* seg_off,
+                                                   const uint64_t* dedup, float* dp, uint32_t* pred, uint32_t* aux,
+                                                   uint64_t total_anchors, AnchorPack ap, ChainCtx cc,
+                                                   const uint32_t* long_list, const uint32_t* long_n,
+                                                   const uint32_t* long_c, const uint32_t* big_items,
+                                                   const uint32_t* n_big) {
+    __shared__ uint64_t ring_key_s[RING ? 4 * 64 : 1];
+    __shared__ float ring_dp_s[RING ? 4 * 64 : 1];
+    const uint32_t lane = lane_id(), wib = threadIdx.x / 32;
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
+    const uint32_t nb = *n_big;
+    for (uint32_t x = blockIdx.x * (blockDim.x / 32) + wib; x < nb; x += nwarps) {
+        const uint32_t u = big_items[2 * x], c = big_items[2 * x + 1];
+        const uint32_t sg = long_list[u], N = long_n[u], C = long_c[u];
+        const uint64_t b = seg_off[sg];
+        const uint32_t* cstart = aux + b;
+        const uint32_t lo = cstart[c], hi = c + 1 < C ? cstart[c + 1] : N;
+        const uint32_t read_len = (uint32_t)(off[(sg >> 1) + 1] - off[sg >> 1]);
+        const uint32_t max_ref_gap = cc.cp.max_ref_gap ? cc.cp.max_ref_gap : read_len;
+        float mx = 0.0f;
+        uint32_t bi = 0xffffffffu;
+        uint64_t bk = 0;
+        warp_chain_range<RING>(dedup, dp, pred, b, lo, hi, max_ref_gap, cc, ap, ring_key_s + (RING ? wib * 64 : 0),
+                               ring_dp_s + (RING ? wib * 64 : 0), false, mx, bi, bk);
+        if (lane == 0) reinterpret_cast<float*>(aux + total_anchors + b)[c] = mx;
+        __syncwarp();
+    }
+}
+
 template <bool RING>
 __global__ void __launch_bounds__(32 * CHAIN_WARPS, 8) k_chain4(const uint64_t* __restrict__ off, uint32_t n, const uint64_t* seg_off,
                                                 const uint64_t* sorted, uint64_t* dedup, float* dp, uint32_t* pred,
                                                 uint32_t* aux, uint64_t total_anchors, AnchorPack ap, ChainCtx cc,
                                                 NamRec* nam_out, uint32_t* nam_seg_count, uint64_t* anc_out,
                                                 uint64_t* anc_start, const uint32_t* seg_list, uint32_t n_list,
-                                                const uint32_t* long_list, uint32_t n_long) {
+                                                const uint32_t* long_list, uint32_t n_long, const uint32_t* long_n,
+                                                const uint32_t* long_c) {
     __shared__ uint32_t hist[CHAIN_WARPS * 256];
     __shared__ uint64_t ring_key_s[RING ? CHAIN_WARPS * NG * 64 : 1];
     __shared__ float ring_dp_s[RING ? CHAIN_WARPS * NG * 64 : 1];
@@ -1170,35 +1317,15 @@ __global__ void __launch_bounds__(32 * CHAIN_WARPS, 8) k_chain4(const uint64_t* 
             const uint32_t l = NG * (u - n_long) + lane;
             if (lane < NG && l < n_list) my_sg = seg_list[l];
         }
-        // dedup (src/chainer.rs:228-229), one orientation after the other
+        // dedup (src/chainer.rs:228-229), one orientation after the other; the long
+        // orientations were deduplicated by k_chain_long_prep
         uint32_t my_n = 0;
         uint64_t my_b = 0;
         for (uint32_t q = 0; q < NG; q++) {
             const uint32_t sg = __shfl_sync(FULL, my_sg, q);
             if (sg == NONE) continue;
             const uint64_t b = seg_off[sg], e = seg_off[sg + 1];
-            uint32_t N = 0;
-            const uint32_t cnt = (uint32_t)(e - b);
-            if (cnt <= CHAIN_SORT_SMALL) {
-                // the orientation's keys, still unsorted in the dedup buffer: sort them here
-                if (cnt <= 32) N = warp_sort_dedup<1>(dedup + b, cnt);
-                else if (cnt <= 64) N = warp_sort_dedup<2>(dedup + b, cnt);
-                else if (cnt <= 128) N = warp_sort_dedup<4>(dedup + b, cnt);
-                else N = warp_sort_dedup<8>(dedup + b, cnt);
-            } else {
-                for (uint64_t c = b; c < e; c += 32) {
-                    const uint64_t i = c + lane;
-                    bool keep = false;
-                    uint64_t key = 0;
-                    if (i < e) {
-                        key = sorted[i];
-                        keep = i == b || sorted[i - 1] != key;
-                    }
-                    const uint32_t bal = __ballot_sync(FULL, keep);
-                    if (keep) dedup[b + N + __popc(bal & lanemask_lt())] = key;
-                    N += __popc(bal);
-                }
-            }
+            const uint32_t N = u < n_long ? long_n[u] : orientation_dedup(sorted, dedup, b, e);
             if (lane == q) {
                 my_n = N;
                 my_b = b;
@@ -1303,16 +1430,9 @@ __global__ void __launch_bounds__(32 * CHAIN_WARPS, 8) k_chain4(const uint64_t* 
             const float bs = __shfl_sync(FULL, best_score, (lane % NG) * CG);
             if (lane < NG) my_best = bs;
         } else {
-            // the whole warp per orientation.  Anchors sorted by (reference, position)
-            // fall into clusters: a new one starts where the reference changes or the
-            // position jumps by max_ref_gap or more.  A predecessor scan never crosses
-            // into an earlier cluster, so every cluster's DP depends on the others only
-            // through the best-index re-check, which can fire only once the cluster
-            // holds the running best (a strict maximum over all earlier anchors).  The
-            // clusters are scored at once without the re-check (small ones a thread
-            // each, large ones by the warp); then, in order, each cluster whose maximum
-            // beats the running best of the clusters before it is scored again with
-            // the re-check, and the running best is carried on.  The others are final.
+            // a long orientation (k_chain_long_prep and k_chain_big scored its clusters
+            // without the re-check): the clusters whose maximum beats the running best,
+            // in order, again with the re-check
             uint64_t* ring_key = ring_key_s + (RING ? wib * NG * 64 : 0);
             float* ring_dp = ring_dp_s + (RING ? wib * NG * 64 : 0);
             for (uint32_t q = 0; q < NG; q++) {
@@ -1321,59 +1441,9 @@ __global__ void __launch_bounds__(32 * CHAIN_WARPS, 8) k_chain4(const uint64_t* 
                 if (sg == NONE || N == 0) continue;
                 const uint32_t read_len = (uint32_t)(off[(sg >> 1) + 1] - off[sg >> 1]);
                 const uint32_t max_ref_gap = cc.cp.max_ref_gap ? cc.cp.max_ref_gap : read_len;
-                // cluster starts (aux[b ..]), maxima (aux[T + b ..]) and large clusters
-                // (aux[2T + b ..]); chain_extract reuses the three after the DP
-                uint32_t* cstart = aux + b;
-                float* cmax = reinterpret_cast<float*>(aux + total_anchors + b);
-                uint32_t* cbig = aux + 2 * total_anchors + b;
-                uint32_t C = 0;
-                for (uint32_t c = 0; c < N; c += 32) {
-                    const uint32_t i = c + lane;
-                    bool st = false;
-                    if (i < N) {
-                        if (i == 0) {
-                            st = true;
-                        } else {
-                            const uint64_t ki = dedup[b + i], kp = dedup[b + i - 1];
-                            st = (ki >> (ap.pbits + ap.qbits)) != (kp >> (ap.pbits + ap.qbits)) ||
-                                 (uint32_t)((ki >> ap.qbits) & pmask) - (uint32_t)((kp >> ap.qbits) & pmask) >=
-                                     max_ref_gap;
-                        }
-                    }
-                    const uint32_t bal = __ballot_sync(FULL, st);
-                    if (st) cstart[C + __popc(bal & lanemask_lt())] = i;
-                    C += __popc(bal);
-                }
-                __syncwarp();
-                // scoring without the re-check: small clusters a thread each (the first
-                // cluster always holds the running best, so it is scored only below)
-                uint32_t nbig = 0;
-                for (uint32_t c0 = 0; c0 < C; c0 += 32) {
-                    const uint32_t c = c0 + lane;
-                    bool big = false;
-                    if (c < C && c > 0) {
-                        const uint32_t lo = cstart[c], hi = c + 1 < C ? cstart[c + 1] : N;
-                        big = hi - lo > CHAIN_LANE_CLUSTER_MAX;
-                        if (!big) cmax[c] = lane_chain_range(dedup, dp, pred, b, lo, hi, max_ref_gap, cc, ap);
-                    }
-                    const uint32_t bal = __ballot_sync(FULL, big);
-                    if (big) cbig[nbig + __popc(bal & lanemask_lt())] = c;
-                    nbig += __popc(bal);
-                }
-                __syncwarp();
-                // large clusters by the warp
-                for (uint32_t x = 0; x < nbig; x++) {
-                    const uint32_t c = cbig[x];
-                    const uint32_t lo = cstart[c], hi = c + 1 < C ? cstart[c + 1] : N;
-                    float mx = 0.0f;
-                    uint32_t bi = 0xffffffffu;
-                    uint64_t bk = 0;
-                    warp_chain_range<RING>(dedup, dp, pred, b, lo, hi, max_ref_gap, cc, ap, ring_key, ring_dp, false,
-                                           mx, bi, bk);
-                    if (lane == 0) cmax[c] = mx;
-                    __syncwarp();
-                }
-                __syncwarp();
+                const uint32_t* cstart = aux + b;
+                const float* cmax = reinterpret_cast<const float*>(aux + total_anchors + b);
+                const uint32_t C = long_c[u];
                 // in order: clusters whose maximum beats the running best, scored again
                 float best_score = 0.0f;
                 uint32_t best_index = 0xffffffffu;
@@ -1782,16 +1852,38 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
         ws.anc_sparse.reserve(3 * total_anchors + 1);
         ws.anc_start.reserve(total_anchors + 1);
     }
+    // long orientations: dedup, clusters and their first scoring, before k_chain4
+    uint32_t* const long_n = ws.seg_key_alt.p;
+    uint32_t* const long_c = ws.seg_key_alt.p + 2 * (size_t)n;
+    if (n_list[2]) {
+        const uint64_t cap = total_anchors / (CHAIN_LANE_CLUSTER_MAX + 1) + 1;
+        ws.chain_big.reserve(2 * cap + 2);
+        SA_CUDA(cudaMemsetAsync(ws.chain_big.p, 0, 4, st));
+        const unsigned pgrid = (unsigned)std::min<uint64_t>(((uint64_t)n_list[2] + 3) / 4, sm_count() * 16);
+        k_chain_long_prep<<<pgrid, 128, 0, st>>>(ws.off.p, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p,
+                                                 ws.pred.p, ws.aux.p, total_anchors, ap, cc, long_sorted, n_list[2],
+                                                 long_n, long_c, ws.chain_big.p + 2, ws.chain_big.p);
+        const unsigned bgrid = (unsigned)(sm_count() * 8);
+        if (cfg.cp.max_lookback < 64)
+            k_chain_big<true><<<bgrid, 128, 0, st>>>(ws.off.p, ws.seg_off.p, ws.anchors.p, ws.dp.p, ws.pred.p,
+                                                     ws.aux.p, total_anchors, ap, cc, long_sorted, long_n, long_c,
+                                                     ws.chain_big.p + 2, ws.chain_big.p);
+        else
+            k_chain_big<false><<<bgrid, 128, 0, st>>>(ws.off.p, ws.seg_off.p, ws.anchors.p, ws.dp.p, ws.pred.p,
+                                                      ws.aux.p, total_anchors, ap, cc, long_sorted, long_n, long_c,
+                                                      ws.chain_big.p + 2, ws.chain_big.p);
+        launches += 2;
+    }
     if (cfg.cp.max_lookback < 64)
         k_chain4<true><<<chain_grid, 32 * CHAIN_WARPS, 0, st>>>(
             ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p,
             total_anchors, ap, cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
-            cfg.nam_anchors ? ws.anc_start.p : nullptr, short_list, n_list[0], long_sorted, n_list[2]);
+            cfg.nam_anchors ? ws.anc_start.p : nullptr, short_list, n_list[0], long_sorted, n_list[2], long_n, long_c);
     else
         k_chain4<false><<<chain_grid, 32 * CHAIN_WARPS, 0, st>>>(
             ws.off.p, n, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p, ws.pred.p, ws.aux.p,
             total_anchors, ap, cc, ws.nam_scratch.p, ws.nam_seg_count.p, cfg.nam_anchors ? ws.anc_sparse.p : nullptr,
-            cfg.nam_anchors ? ws.anc_start.p : nullptr, short_list, n_list[0], long_sorted, n_list[2]);
+            cfg.nam_anchors ? ws.anc_start.p : nullptr, short_list, n_list[0], long_sorted, n_list[2], long_n, long_c);
     kt->end(st);
     launches++;
     ws.nam_count.reserve((size_t)n + 1);

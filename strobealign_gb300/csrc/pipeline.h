@@ -52,6 +52,9 @@ struct NamWorkspace {
     DevBuf<uint32_t> seg_list;
     // seg_list's anchor counts, and the lists ordered by them (descending) for k_chain4
     DevBuf<uint32_t> seg_key, seg_key_alt, seg_sorted;
+    // long orientations' large clusters queued for k_chain_big: [0] count, then
+    // (orientation, cluster) pairs
+    DevBuf<uint32_t> chain_big;
     DevBuf<uint64_t> sort_begin, sort_end;
     DevBuf<uint64_t> long_begin, long_end;
     // with NamConfig::nam_anchors: the anchors of each NAM's chain, last to first
