@@ -80,6 +80,8 @@ def parse(argv=None):
                     help="reference arm: records per step (0 = four 1 Mnt chunks per host thread)")
     ap.add_argument("--aux-steps", type=int, default=3, help="steps of the plain and batched host-buffer passes")
     ap.add_argument("--no-served", action="store_true", help="skip the served and latency passes (profiling runs)")
+    ap.add_argument("--tune", type=int, default=1, help="1: autotune the mapper on a calibration sample first")
+    ap.add_argument("--tune-records", type=int, default=500_000, help="records in the calibration sample")
     return ap.parse_args(argv)
 
 
@@ -195,6 +197,12 @@ def _slice(rs, a: int, b: int):
     o, no = rs.offsets, rs.name_offsets
     return syn.ReadSet(rs.seq[int(o[a]):int(o[b])], o[a:b + 1] - o[a], rs.names[int(no[a]):int(no[b])],
                        no[a:b + 1] - no[a], rs.qual[int(o[a]):int(o[b])] if rs.qual is not None else None)
+
+
+def _calib(rs, n: int):
+    """Reads.from_arrays arguments for the first n records of a ReadSet."""
+    p = _prefix(rs, n)
+    return p.seq, p.offsets, p.names, p.name_offsets, p.qual
 
 
 def oracle_index(g, read_length: int, threads: int):
@@ -426,6 +434,19 @@ def main():
     R2 = sa.Reads.from_arrays(r2.seq, r2.offsets, r2.names, r2.name_offsets, r2.qual) if r2 is not None else None
     n_reads = (2 if r2 is not None else 1) * len(R1)
     mapper = sa.Mapper(index, refs, use_ssw=1 if use_ssw else 0)
+    # the autotuner on a calibration sample of the workload (output-invariant knobs);
+    # its choice stays in the mapper for the timed passes
+    tune = None
+    if args.tune:
+        m = min(len(R1), args.tune_records)
+        c1 = sa.Reads.from_arrays(*_calib(r1, m))
+        c2 = sa.Reads.from_arrays(*_calib(r2, m)) if r2 is not None else None
+        t0 = time.time()
+        tune = mapper.autotune(c1, c2, rounds=2)
+        calib_reads = m * (2 if r2 is not None else 1)
+        tune.update(sample_records=m, tune_s=round(time.time() - t0, 1),
+                    default_reads_per_s=calib_reads / tune["seconds_default"],
+                    tuned_reads_per_s=calib_reads / tune["seconds_tuned"])
     mapper.upload(R1, R2)
 
     def barrier():
@@ -574,6 +595,7 @@ def main():
                                                "vs_batched_e2e": served / batched_e2e,
                                                "latency_open_loop": lat},
         "gpu_launches": launches,
+        "tuning": tune,
         "stage_share": shares,
         # wall seconds per step: NAM pipeline (GPU), extension waves (GPU, incl. job
         # upload and result download), host policy between and after waves

@@ -462,6 +462,38 @@ typedef struct {
 void sa_schedule_params_default(sa_schedule_params* p);
 int32_t sa_mapper_set_schedule(sa_mapper* m, const sa_schedule_params* p);
 
+/* Tuning knobs of a mapper, chosen by sa_mapper_autotune.  No counterpart in the
+ * reference; output bytes never depend on them.
+ *   parts, wave_min_jobs, max_wave_jobs  as in sa_schedule_params
+ *   ssw_wave_max_qlen       SSW tasks of reads up to this length (at most 192) run on
+ *                           the lane-wavefront kernel, longer ones a warp per task
+ *   chain_lane_cluster_max  clusters of a long read orientation's anchors up to this
+ *                           size are chained by one thread, larger ones by a warp */
+typedef struct {
+    uint32_t parts;
+    uint64_t wave_min_jobs;
+    uint64_t max_wave_jobs;
+    uint32_t ssw_wave_max_qlen;
+    uint32_t chain_lane_cluster_max;
+} sa_tuning;
+typedef struct {
+    sa_tuning chosen;
+    double seconds_default; /* the calibration batch under the defaults (median of rounds) */
+    double seconds_tuned;   /* under the chosen knobs */
+    uint32_t trials;
+} sa_tune_report;
+void sa_tuning_default(sa_tuning* t);
+int32_t sa_mapper_set_tuning(sa_mapper* m, const sa_tuning* t);
+int32_t sa_mapper_get_tuning(const sa_mapper* m, sa_tuning* t);
+/* Autotuner: uploads the calibration batch (it stays uploaded, replacing any earlier
+ * one), maps it under the default knobs, then tries a short list of values for one
+ * knob after another (coordinate descent; each trial the median of `rounds` maps, a
+ * change kept only when 2% faster), checks that every trial writes the same bytes
+ * (SA_ERR_INVALID otherwise) and applies the choice to the mapper.  The batch should
+ * have the shape of the workload (read lengths, genome). */
+int32_t sa_mapper_autotune(sa_mapper* m, const sa_read_batch* r1, const sa_read_batch* r2, uint32_t rounds,
+                           sa_tune_report* out);
+
 /* SAM header (src/io/sam.rs:176-200); cmd_line NULL omits the @PG line. */
 int32_t sa_sam_header(const sa_refs* refs, const char* cmd_line, const char* rg_id, const char* const* rg_fields,
                       size_t n_rg_fields, sa_output* out);

@@ -509,6 +509,30 @@ class Mapper:
             sp.max_wave_jobs = max_wave_jobs
         L.check(lib().sa_mapper_set_schedule(self.h, C.byref(sp)))
 
+    def tuning(self) -> dict:
+        t = L.Tuning()
+        L.check(lib().sa_mapper_get_tuning(self.h, C.byref(t)))
+        return {f: int(getattr(t, f)) for f, _ in L.Tuning._fields_}
+
+    def set_tuning(self, **kw) -> None:
+        t = L.Tuning()
+        L.check(lib().sa_mapper_get_tuning(self.h, C.byref(t)))
+        for k, v in kw.items():
+            setattr(t, k, v)
+        L.check(lib().sa_mapper_set_tuning(self.h, C.byref(t)))
+
+    def autotune(self, r1: Reads, r2: Reads | None = None, rounds: int = 2) -> dict:
+        """sa_mapper_autotune on a calibration batch (it stays uploaded): the chosen knobs
+        and the batch's time under the defaults and under them."""
+        rep = L.TuneReport()
+        self._b1 = r1.c()
+        self._b2 = r2.c() if r2 is not None else None
+        self._keep = (r1, r2)
+        L.check(lib().sa_mapper_autotune(self.h, C.byref(self._b1), C.byref(self._b2) if self._b2 is not None else None,
+                                         rounds, C.byref(rep)))
+        return {"chosen": {f: int(getattr(rep.chosen, f)) for f, _ in L.Tuning._fields_},
+                "seconds_default": rep.seconds_default, "seconds_tuned": rep.seconds_tuned, "trials": rep.trials}
+
     def abundances(self) -> np.ndarray:
         n = len(self.refs)
         out = np.zeros(n, dtype=np.float64)

@@ -90,6 +90,15 @@ class ScheduleParams(C.Structure):
     _fields_ = [("parts", u32), ("overlap", u32), ("wave_min_jobs", u64), ("max_wave_jobs", u64)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("parts", u32), ("wave_min_jobs", u64), ("max_wave_jobs", u64), ("ssw_wave_max_qlen", u32),
+                ("chain_lane_cluster_max", u32)]
+
+
+class TuneReport(C.Structure):
+    _fields_ = [("chosen", Tuning), ("seconds_default", f64), ("seconds_tuned", f64), ("trials", u32)]
+
+
 class RequestStats(C.Structure):
     _fields_ = [("seconds_queued", f64), ("seconds_service", f64), ("seconds_total", f64), ("n_reads", u64),
                 ("n_waves", u32), ("h2d_bytes", u64), ("d2h_bytes", u64)]
@@ -161,6 +170,10 @@ SIGNATURES = {
     "sa_piecewise_batch": (i32, [P(MappingParams), u32, sz, vp, P(u64), vp, P(u64), P(u32), P(u64),
                                  P(StageAlignment), P(u32), sz]),
     "sa_mapper_set_schedule": (i32, [vp, P(ScheduleParams)]),
+    "sa_tuning_default": (None, [P(Tuning)]),
+    "sa_mapper_set_tuning": (i32, [vp, P(Tuning)]),
+    "sa_mapper_get_tuning": (i32, [vp, P(Tuning)]),
+    "sa_mapper_autotune": (i32, [vp, P(ReadBatch), P(ReadBatch), u32, P(TuneReport)]),
 }
 
 _lib = None

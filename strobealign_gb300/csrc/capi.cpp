@@ -447,6 +447,57 @@ int32_t sa_mapper_set_schedule(sa_mapper* m, const sa_schedule_params* p) {
     SA_CATCH
 }
 
+static void tuning_to_c(const Mapper::Tuning& t, sa_tuning* o) {
+    o->parts = t.parts;
+    o->wave_min_jobs = t.wave_min_jobs;
+    o->max_wave_jobs = t.max_wave_jobs;
+    o->ssw_wave_max_qlen = t.wave_qmax;
+    o->chain_lane_cluster_max = t.chain_lane_max;
+}
+
+void sa_tuning_default(sa_tuning* t) {
+    if (t) tuning_to_c(Mapper::Tuning(), t);
+}
+
+int32_t sa_mapper_set_tuning(sa_mapper* m, const sa_tuning* t) {
+    SA_TRY
+    require(m && t, "null argument");
+    require(t->parts >= 1 && t->max_wave_jobs >= 1 && t->wave_min_jobs >= 1, "tuning values must be positive");
+    require(t->ssw_wave_max_qlen >= 1 && t->ssw_wave_max_qlen <= 192, "ssw_wave_max_qlen must be in 1..192");
+    require(t->chain_lane_cluster_max >= 1 && t->chain_lane_cluster_max <= 4096,
+            "chain_lane_cluster_max must be in 1..4096");
+    Mapper::Tuning x;
+    x.parts = t->parts;
+    x.wave_min_jobs = t->wave_min_jobs;
+    x.max_wave_jobs = t->max_wave_jobs;
+    x.wave_qmax = t->ssw_wave_max_qlen;
+    x.chain_lane_max = t->chain_lane_cluster_max;
+    m->m->set_tuning(x);
+    return SA_OK;
+    SA_CATCH
+}
+
+int32_t sa_mapper_get_tuning(const sa_mapper* m, sa_tuning* t) {
+    SA_TRY
+    require(m && t, "null argument");
+    tuning_to_c(m->m->tuning(), t);
+    return SA_OK;
+    SA_CATCH
+}
+
+int32_t sa_mapper_autotune(sa_mapper* m, const sa_read_batch* r1, const sa_read_batch* r2, uint32_t rounds,
+                           sa_tune_report* out) {
+    SA_TRY
+    require(m && r1 && out, "null argument");
+    const Mapper::TuneReport rep = m->m->autotune(r1, r2, rounds);
+    tuning_to_c(rep.chosen, &out->chosen);
+    out->seconds_default = rep.seconds_default;
+    out->seconds_tuned = rep.seconds_tuned;
+    out->trials = rep.trials;
+    return SA_OK;
+    SA_CATCH
+}
+
 int32_t sa_mapper_get_stats(const sa_mapper* m, sa_mapper_stats* out) {
     SA_TRY
     require(m && out, "null argument");

@@ -2870,10 +2870,11 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
 #define SA_SSW(RM)                                                                                              \
     k_ssw<RM><<<(unsigned)blocks, tpb, (size_t)wpb * 5 * 32 * ((RM + 3) / 4) * 4, st>>>(                       \
         ws.tasks.p, ws.order.p, n_tasks, ws.prep.p, ws.arena.p, sc, bias, ws.counters.p, ws.counters.p + 21, \
-        (uint32_t)(8 * WAVE_NMAX))
-            // tasks of reads up to 192 nt: eight threads per task; the longer ones of a batch
-            // of mixed lengths a warp per task, in a launch before
-            if (max_qlen > 8 * WAVE_NMAX) {
+        wave_qmax)
+            // tasks of reads up to wave_qmax (at most 192) nt: eight threads per task; the
+            // longer ones of a batch of mixed lengths a warp per task, in a launch before
+            const uint32_t wave_qmax = std::min<uint32_t>(ws.wave_qmax, 8 * WAVE_NMAX);
+            if (max_qlen > wave_qmax) {
                 if (rmax == 4) SA_SSW(4);
                 else if (rmax == 8) SA_SSW(8);
                 else SA_SSW(16);
@@ -2885,8 +2886,7 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
                 if (wblocks > sm_count() * 16) wblocks = sm_count() * 16;
                 const size_t smem = (size_t)wpb * 5 * ((WAVE_NMAX + 7) / 8) * 32 * sizeof(uint4);
                 k_ssw_wave<WAVE_NMAX><<<(unsigned)wblocks, tpb, smem, st>>>(
-                    ws.tasks.p, ws.order.p, n_tasks, ws.prep.p, ws.arena.p, sc, bias, ws.counters.p,
-                    (uint32_t)(8 * WAVE_NMAX));
+                    ws.tasks.p, ws.order.p, n_tasks, ws.prep.p, ws.arena.p, sc, bias, ws.counters.p, wave_qmax);
             }
 #undef SA_SSW
             kt->end(st);

@@ -70,6 +70,9 @@ struct ExtWorkspace {
     PodArray<ExtResult> h_results;
     PodArray<uint32_t> h_cigar;
     uint64_t total_cigar = 0;
+    // tuning (output-invariant): SSW tasks of reads up to wave_qmax nt (at most 192) run
+    // on the lane-wavefront kernel, longer ones a warp per task
+    uint32_t wave_qmax = 192;
     uint64_t cells[5] = {0, 0, 0, 0, 0};  // SW cells: canonical, then computed forward byte / word, reverse byte / word
 };
 

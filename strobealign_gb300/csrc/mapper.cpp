@@ -118,6 +118,7 @@ void Mapper::part_nams(Part& p, uint32_t& launches) {
     cfg.mcs = mp_.mcs_strategy;
     cfg.rescue_distance = mp_.rescue_distance;
     cfg.nam_anchors = single_end_piecewise_ && !bv_.paired;
+    cfg.chain_lane_max = chain_lane_max_;
     pws_.seq.reserve(total + 16);
     pws_.off.reserve((size_t)n + 1);
     h_poff_.reserve((size_t)n + 1);
@@ -672,6 +673,81 @@ void Mapper::map_uploaded(sa_output* out) {
         stats_.kernel_ms[i] = i < KS_COUNT ? kt_.ms[i] + kt_nam_.ms[i] : 0.0;
         stats_.kernel_launches[i] = i < KS_COUNT ? kt_.launches[i] + kt_nam_.launches[i] : 0;
     }
+}
+
+void Mapper::set_tuning(const Tuning& t) {
+    set_parts(t.parts);
+    set_wave_min_jobs(std::max<uint64_t>(1, t.wave_min_jobs));
+    set_max_wave_jobs(t.max_wave_jobs);
+    ews_.wave_qmax = std::max<uint32_t>(1, t.wave_qmax);
+    chain_lane_max_ = std::max<uint32_t>(1, t.chain_lane_max);
+}
+
+Mapper::Tuning Mapper::tuning() const {
+    Tuning t;
+    t.parts = parts_target_;
+    t.wave_min_jobs = wave_min_jobs_;
+    t.max_wave_jobs = max_wave_jobs_;
+    t.wave_qmax = ews_.wave_qmax;
+    t.chain_lane_max = chain_lane_max_;
+    return t;
+}
+
+Mapper::TuneReport Mapper::autotune(const sa_read_batch* r1, const sa_read_batch* r2, uint32_t rounds) {
+    rounds = std::max<uint32_t>(1, rounds);
+    const bool saved_overlap = overlap_;
+    overlap_ = true;
+    upload(r1, r2);
+    std::vector<char> want;
+    TuneReport rep;
+    auto run = [&](const Tuning& t) {
+        set_tuning(t);
+        std::vector<double> secs;
+        for (uint32_t r = 0; r < rounds; r++) {
+            sa_output o{};
+            const auto t0 = std::chrono::steady_clock::now();
+            map_uploaded(&o);
+            secs.push_back(std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+            const bool same = want.size() == o.len && (o.len == 0 || std::memcmp(want.data(), o.data, o.len) == 0);
+            release_output(o.data);
+            if (!same) throw Error(SA_ERR_INVALID, "internal: tuning changed the output bytes");
+        }
+        rep.trials++;
+        std::sort(secs.begin(), secs.end());
+        return secs[secs.size() / 2];
+    };
+    Tuning best;  // the defaults
+    set_tuning(best);
+    {
+        sa_output o{};
+        map_uploaded(&o);  // warm-up, and the bytes every trial must reproduce
+        want.assign(o.data, o.data + o.len);
+        release_output(o.data);
+    }
+    double best_s = run(best);
+    rep.seconds_default = best_s;
+    auto knob = [&](auto field, std::initializer_list<uint64_t> values) {
+        for (uint64_t v : values) {
+            Tuning t = best;
+            if ((uint64_t)(t.*field) == v) continue;
+            t.*field = (std::remove_reference_t<decltype(t.*field)>)v;
+            const double sec = run(t);
+            if (sec < 0.98 * best_s) {
+                best = t;
+                best_s = sec;
+            }
+        }
+    };
+    knob(&Tuning::parts, {2, 8, 16});
+    knob(&Tuning::max_wave_jobs, {65536, 131072, 524288});
+    knob(&Tuning::wave_min_jobs, {8192, 131072});
+    if (max_qlen_ > 128) knob(&Tuning::wave_qmax, {128, 160});
+    knob(&Tuning::chain_lane_max, {16, 128});
+    set_tuning(best);
+    overlap_ = saved_overlap;
+    rep.chosen = best;
+    rep.seconds_tuned = best_s;
+    return rep;
 }
 
 }  // namespace sa

@@ -45,6 +45,24 @@ class Mapper {
     // alternate, every waiting request goes into the waves before any chunk resumes,
     // and the output is gathered after the last chunk
     void set_overlap(bool on) { overlap_ = on; }
+    // output-invariant knobs the autotuner chooses
+    struct Tuning {
+        uint32_t parts = 4;
+        uint64_t wave_min_jobs = 32768, max_wave_jobs = 262144;
+        uint32_t wave_qmax = 192, chain_lane_max = 48;
+    };
+    struct TuneReport {
+        Tuning chosen;
+        double seconds_default = 0, seconds_tuned = 0;
+        uint32_t trials = 0;
+    };
+    void set_tuning(const Tuning& t);
+    Tuning tuning() const;
+    // Times the batch under the default knobs, then one knob after another over a short
+    // list of values (coordinate descent, each trial the median of `rounds` maps), keeps a
+    // change only when it is 2% faster, checks that every trial writes the same bytes,
+    // and applies the choice.  The batch stays uploaded.
+    TuneReport autotune(const sa_read_batch* r1, const sa_read_batch* r2, uint32_t rounds);
 
   private:
     // One NAM-pipeline part of a batch: a run of whole chunks with their reads' NAMs on
@@ -81,6 +99,7 @@ class Mapper {
     uint64_t wave_min_jobs_ = 32768;
     uint64_t max_wave_jobs_ = 262144;
     bool overlap_ = true;
+    uint32_t chain_lane_max_ = 48;
     bool trace_ = false;
 
     const sa_index* idx_;

@@ -1146,8 +1146,6 @@ __device__ float lane_chain_range(const uint64_t* dedup, float* dp, uint32_t* pr
     return mx;
 }
 
-// Anchors per cluster above which a cluster is scored by the whole warp
-constexpr uint32_t CHAIN_LANE_CLUSTER_MAX = 48;
 
 // Sort (orientations up to CHAIN_SORT_SMALL anchors, whose keys are still unsorted in
 // the dedup buffer) or take the segmented sort's output, and deduplicate
@@ -1190,7 +1188,7 @@ __device__ __forceinline__ uint32_t orientation_dedup(const uint64_t* sorted, ui
 // (with the re-check, carrying the running best on); the others are final.
 //
 // k_chain_long_prep: a warp per long orientation u: the dedup, the cluster starts
-// (aux[b ..]), and the clusters of up to CHAIN_LANE_CLUSTER_MAX anchors scored a
+// (aux[b ..]), and the clusters of up to lane_max anchors scored a
 // thread each (maxima at aux[T + b ..] as floats); the larger ones (except the first,
 // which k_chain4 scores with the re-check anyway) are queued as (u, cluster) items for
 // k_chain_big, a warp each.  long_n[u] / long_c[u]: anchors after dedup, clusters.
@@ -1199,7 +1197,7 @@ __global__ void __launch_bounds__(128) k_chain_long_prep(const uint64_t* __restr
                                                          uint32_t* pred, uint32_t* aux, uint64_t total_anchors,
                                                          AnchorPack ap, ChainCtx cc, const uint32_t* long_list,
                                                          uint32_t n_long, uint32_t* long_n, uint32_t* long_c,
-                                                         uint32_t* big_items, uint32_t* n_big) {
+                                                         uint32_t* big_items, uint32_t* n_big, uint32_t lane_max) {
     const uint32_t lane = lane_id();
     const uint64_t pmask = (1ULL << ap.pbits) - 1;
     const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
@@ -1235,7 +1233,7 @@ __global__ void __launch_bounds__(128) k_chain_long_prep(const uint64_t* __restr
             bool big = false;
             if (c < C && c > 0) {
                 const uint32_t lo = cstart[c], hi = c + 1 < C ? cstart[c + 1] : N;
-                big = hi - lo > CHAIN_LANE_CLUSTER_MAX;
+                big = hi - lo > lane_max;
                 if (!big) cmax[c] = lane_chain_range(dedup, dp, pred, b, lo, hi, max_ref_gap, cc, ap);
             }
             const uint32_t bal = __ballot_sync(FULL, big);
@@ -1856,13 +1854,14 @@ uint32_t run_nam_pipeline(const DevIndex& ix, const DevRefs& refs, const NamConf
     uint32_t* const long_n = ws.seg_key_alt.p;
     uint32_t* const long_c = ws.seg_key_alt.p + 2 * (size_t)n;
     if (n_list[2]) {
-        const uint64_t cap = total_anchors / (CHAIN_LANE_CLUSTER_MAX + 1) + 1;
+        const uint32_t lane_max = std::max<uint32_t>(1, cfg.chain_lane_max);
+        const uint64_t cap = total_anchors / (lane_max + 1) + 1;
         ws.chain_big.reserve(2 * cap + 2);
         SA_CUDA(cudaMemsetAsync(ws.chain_big.p, 0, 4, st));
         const unsigned pgrid = (unsigned)std::min<uint64_t>(((uint64_t)n_list[2] + 3) / 4, sm_count() * 16);
         k_chain_long_prep<<<pgrid, 128, 0, st>>>(ws.off.p, ws.seg_off.p, ws.anchors_sorted.p, ws.anchors.p, ws.dp.p,
                                                  ws.pred.p, ws.aux.p, total_anchors, ap, cc, long_sorted, n_list[2],
-                                                 long_n, long_c, ws.chain_big.p + 2, ws.chain_big.p);
+                                                 long_n, long_c, ws.chain_big.p + 2, ws.chain_big.p, lane_max);
         const unsigned bgrid = (unsigned)(sm_count() * 8);
         if (cfg.cp.max_lookback < 64)
             k_chain_big<true><<<bgrid, 128, 0, st>>>(ws.off.p, ws.seg_off.p, ws.anchors.p, ws.dp.p, ws.pred.p,

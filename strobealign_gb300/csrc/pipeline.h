@@ -73,6 +73,9 @@ struct NamConfig {
     uint32_t mcs;
     uint32_t rescue_distance;
     bool nam_anchors = false;  // also keep each NAM's chain anchors (single-end piecewise extension)
+    // tuning (output-invariant): clusters of a long read orientation up to this many
+    // anchors are scored by one thread, larger ones by a warp
+    uint32_t chain_lane_max = 48;
 };
 
 // Runs seeding -> hits -> rescue -> anchors -> sort -> chaining -> NAM compaction for

@@ -331,6 +331,30 @@ def test_plain_schedule_matches_batched_engine(sa, synth):
             assert outs[0] == want, _first_diff(outs[0], want)
 
 
+def test_tuning_knobs_do_not_change_output(sa, synth, repeats):
+    # every tuning knob at an extreme: all clusters of long read orientations chained a
+    # warp each (or a thread each), SSW tasks of reads over 64 nt a warp each, one part,
+    # tiny waves; and the autotuner's choice -- all write the oracle's bytes
+    for d in (synth, repeats):
+        refs, idx = _index(sa, d["fa"])
+        r1 = sa.Reads.from_file(d["f1"])
+        r2 = sa.Reads.from_file(d["f2"])
+        want = run_oracle_cli(["--no-PG", d["fa"], d["f1"], d["f2"]])[len(sa.sam_header(refs)):]
+        for kw in (dict(chain_lane_cluster_max=1), dict(chain_lane_cluster_max=4096),
+                   dict(ssw_wave_max_qlen=64, parts=1, max_wave_jobs=300, wave_min_jobs=1)):
+            m = sa.Mapper(idx, refs)
+            m.set_tuning(**kw)
+            got = m.map(r1, r2)
+            assert got == want, (kw, _first_diff(got, want))
+        m = sa.Mapper(idx, refs)
+        rep = m.autotune(r1, r2, rounds=1)
+        assert rep["trials"] >= 5 and rep["seconds_tuned"] <= rep["seconds_default"] * 1.0001
+        assert m.tuning() == rep["chosen"]
+        assert m.map_uploaded() == want
+    with pytest.raises(sa.SaError):
+        sa.Mapper(idx, refs).set_tuning(ssw_wave_max_qlen=500)
+
+
 def test_synthetic_paired_end_small_chunks_matches_oracle(sa, synth):
     # many chunks: the per-chunk RNG and insert-size restarts are exercised
     want = run_oracle_cli(["--no-PG", "--chunk-size=20000", synth["fa"], synth["f1"], synth["f2"]])
