@@ -157,7 +157,8 @@ typedef struct {
     const uint64_t* comment_offsets;
 } sa_read_batch;
 
-/* Parse a FASTQ/FASTA read file (src/io/fastq.rs:19-100) into an owned batch. */
+/* Parse a FASTQ/FASTA read file (src/io/fastq.rs:19-100) into an owned batch; gzip
+ * when the name ends in ".gz" (src/io/xopen.rs:9-20), "-" for standard input. */
 typedef struct sa_reads sa_reads;
 int32_t sa_reads_from_file(const char* path, sa_reads** out);
 int32_t sa_reads_view(const sa_reads* reads, sa_read_batch* view);
@@ -493,6 +494,33 @@ int32_t sa_mapper_get_tuning(const sa_mapper* m, sa_tuning* t);
  * have the shape of the workload (read lengths, genome). */
 int32_t sa_mapper_autotune(sa_mapper* m, const sa_read_batch* r1, const sa_read_batch* r2, uint32_t rounds,
                            sa_tune_report* out);
+
+/* ---------------------------------------------------------------- file to file
+ * The reference CLI's read → map → write loop (src/main.rs:555-700): a reader thread
+ * parses reads1 (and reads2 for paired-end; pairs end with the shorter file, as zip
+ * pairs them) into batches of whole chunks, the calling thread maps each batch, and a
+ * writer thread appends the outputs to out_path in input order, so parsing, mapping and
+ * writing overlap.  Inputs are FASTQ or FASTA, gzip when the name ends in ".gz" (every
+ * member, src/io/xopen.rs:9-20), "-" for standard input; out_path "-" is standard
+ * output.  The bytes written are header followed by what sa_map_batch returns for all
+ * records at once; in abundance mode the per-contig table ("name\tabundance" with six
+ * decimals, src/main.rs:990-1001) of the mapper's accumulated abundances follows. */
+typedef struct {
+    uint64_t batch_bases;  /* nucleotides per mapped batch, rounded up to whole chunks (0: 2^29) */
+    uint32_t read_ahead;   /* parsed batches queued ahead of the mapper (0: 2) */
+    int32_t append;        /* 1: append to out_path instead of truncating it */
+    const char* header;    /* bytes written first (the SAM header); may be NULL */
+    size_t header_len;
+} sa_stream_params;
+typedef struct {
+    uint64_t n_reads, n_records, n_mapped, n_batches;
+    uint64_t bytes_in;     /* bytes read from the input files (compressed size for .gz) */
+    uint64_t bytes_out;
+    double seconds_total, seconds_map, seconds_wait_input;
+} sa_stream_stats;
+void sa_stream_params_default(sa_stream_params* p);
+int32_t sa_map_files(sa_mapper* m, const char* reads1, const char* reads2, const char* out_path,
+                     const sa_stream_params* p, sa_stream_stats* stats);
 
 /* SAM header (src/io/sam.rs:176-200); cmd_line NULL omits the @PG line. */
 int32_t sa_sam_header(const sa_refs* refs, const char* cmd_line, const char* rg_id, const char* const* rg_fields,

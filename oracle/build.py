@@ -3,8 +3,11 @@
 * oracle/_build/sa_oracle       -- CLI: the reference's mapping path restated in C++
 * oracle/_build/liboracle.so    -- the same code behind ctypes entry points (capi.cpp)
 * oracle/_ref/libssw_ref.so     -- the reference's own ext/ssw/ssw.c compiled from where
-                                   it lies in the reference tree, only when that tree is
-                                   present (used to fuzz the SSW restatement)
+                                   it lies in the reference tree, only when a tree is named
+                                   (argument, or STROBEALIGN_REFERENCE in the environment);
+                                   used to fuzz the SSW restatement
+
+    python oracle/build.py [REFERENCE_TREE]
 
 All objects are compiled with -ffp-contract=off so f32/f64 expressions round as
 the reference's Rust code does.
@@ -21,7 +24,13 @@ BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
 SOURCES = ["seeding.cpp", "nams.cpp", "ssw.cpp", "mapper.cpp", "piecewise.cpp", "io.cpp", "driver.cpp"]
 FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-Wall"]
-REFERENCE_TREE = Path(os.environ.get("STROBEALIGN_REFERENCE", "/root/reference"))
+
+
+def reference_tree(tree: str | os.PathLike | None = None) -> Path | None:
+    """The strobealign source checkout to compile ext/ssw/ssw.c from: the argument, else
+    STROBEALIGN_REFERENCE; None when neither names one."""
+    t = tree if tree is not None else os.environ.get("STROBEALIGN_REFERENCE")
+    return Path(t) if t else None
 
 
 def cli_path() -> Path:
@@ -42,7 +51,7 @@ def _run(cmd):
         raise RuntimeError(f"oracle build failed: {' '.join(map(str, cmd))}\n{r.stdout}\n{r.stderr}")
 
 
-def build(force: bool = False) -> None:
+def build(force: bool = False, reference: str | os.PathLike | None = None) -> None:
     BUILD.mkdir(exist_ok=True)
     srcs = [HERE / s for s in SOURCES]
     deps = srcs + [HERE / "oracle.hpp", HERE / "main.cpp", HERE / "capi.cpp"]
@@ -62,13 +71,15 @@ def build(force: bool = False) -> None:
         _run(["g++", *FLAGS, "-o", str(cli_path()), *core, str(BUILD / "main.o"), "-lpthread"])
     if force or jobs or not lib_path().exists() or lib_path().stat().st_mtime < newest:
         _run(["g++", *FLAGS, "-shared", "-o", str(lib_path()), *core, str(BUILD / "capi.o"), "-lpthread"])
-    ssw = REFERENCE_TREE / "ext" / "ssw" / "ssw.c"
-    if ssw.exists():
+    tree = reference_tree(reference)
+    ssw = tree / "ext" / "ssw" / "ssw.c" if tree is not None else None
+    if ssw is not None and ssw.exists():
         REF_OUT.mkdir(exist_ok=True)
         if force or not ref_ssw_path().exists():
             _run(["gcc", "-O2", "-fPIC", "-shared", "-o", str(ref_ssw_path()), str(ssw), "-lm"])
 
 
 if __name__ == "__main__":
-    build(force=True)
+    import sys
+    build(force=True, reference=sys.argv[1] if len(sys.argv) > 1 else None)
     print(cli_path(), lib_path(), ref_ssw_path() if ref_ssw_path().exists() else "(no reference tree)")

@@ -19,6 +19,7 @@ back to the CPU.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -532,6 +533,25 @@ class Mapper:
                                          rounds, C.byref(rep)))
         return {"chosen": {f: int(getattr(rep.chosen, f)) for f, _ in L.Tuning._fields_},
                 "seconds_default": rep.seconds_default, "seconds_tuned": rep.seconds_tuned, "trials": rep.trials}
+
+    def map_files(self, reads1: str, reads2: str | None, out: str, header: bytes = b"", batch_bases: int = 0,
+                  read_ahead: int = 0, append: bool = False) -> dict:
+        """sa_map_files: reads1 (and reads2) mapped into the file out, parsing, mapping and
+        writing overlapped; header (the SAM header) is written first.  Returns the stream
+        statistics."""
+        p = L.StreamParams()
+        lib().sa_stream_params_default(C.byref(p))
+        if batch_bases:
+            p.batch_bases = batch_bases
+        if read_ahead:
+            p.read_ahead = read_ahead
+        p.append = int(append)
+        p.header = header or None
+        p.header_len = len(header)
+        st = L.StreamStats()
+        L.check(lib().sa_map_files(self.h, os.fsencode(reads1), os.fsencode(reads2) if reads2 else None,
+                                   os.fsencode(out), C.byref(p), C.byref(st)))
+        return {f: getattr(st, f) for f, _ in L.StreamStats._fields_}
 
     def abundances(self) -> np.ndarray:
         n = len(self.refs)

@@ -99,6 +99,15 @@ class TuneReport(C.Structure):
     _fields_ = [("chosen", Tuning), ("seconds_default", f64), ("seconds_tuned", f64), ("trials", u32)]
 
 
+class StreamParams(C.Structure):
+    _fields_ = [("batch_bases", u64), ("read_ahead", u32), ("append", i32), ("header", cp), ("header_len", sz)]
+
+
+class StreamStats(C.Structure):
+    _fields_ = [("n_reads", u64), ("n_records", u64), ("n_mapped", u64), ("n_batches", u64), ("bytes_in", u64),
+                ("bytes_out", u64), ("seconds_total", f64), ("seconds_map", f64), ("seconds_wait_input", f64)]
+
+
 class RequestStats(C.Structure):
     _fields_ = [("seconds_queued", f64), ("seconds_service", f64), ("seconds_total", f64), ("n_reads", u64),
                 ("n_waves", u32), ("h2d_bytes", u64), ("d2h_bytes", u64)]
@@ -174,6 +183,8 @@ SIGNATURES = {
     "sa_mapper_set_tuning": (i32, [vp, P(Tuning)]),
     "sa_mapper_get_tuning": (i32, [vp, P(Tuning)]),
     "sa_mapper_autotune": (i32, [vp, P(ReadBatch), P(ReadBatch), u32, P(TuneReport)]),
+    "sa_stream_params_default": (None, [P(StreamParams)]),
+    "sa_map_files": (i32, [vp, cp, cp, cp, P(StreamParams), P(StreamStats)]),
 }
 
 _lib = None

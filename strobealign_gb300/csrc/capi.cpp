@@ -8,6 +8,7 @@
 
 #include "mapper.h"
 #include "session.h"
+#include "stream.h"
 
 namespace sa {
 
@@ -443,6 +444,42 @@ int32_t sa_mapper_set_schedule(sa_mapper* m, const sa_schedule_params* p) {
     m->m->set_overlap(p->overlap != 0);
     m->m->set_wave_min_jobs(p->wave_min_jobs ? p->wave_min_jobs : 32768);
     m->m->set_max_wave_jobs(p->max_wave_jobs ? p->max_wave_jobs : 262144);
+    return SA_OK;
+    SA_CATCH
+}
+
+void sa_stream_params_default(sa_stream_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->batch_bases = (uint64_t)1 << 29;
+    p->read_ahead = 2;
+}
+
+int32_t sa_map_files(sa_mapper* m, const char* reads1, const char* reads2, const char* out_path,
+                     const sa_stream_params* p, sa_stream_stats* stats) {
+    SA_TRY
+    require(m && reads1 && out_path, "null argument");
+    StreamConfig cfg;
+    if (p) {
+        cfg.batch_bases = p->batch_bases;
+        cfg.read_ahead = p->read_ahead ? p->read_ahead : 2;
+        cfg.append = p->append != 0;
+        cfg.header = p->header;
+        cfg.header_len = p->header ? p->header_len : 0;
+    }
+    const std::string r2 = reads2 ? reads2 : "";
+    const StreamResult r = map_files(*m->m, reads1, reads2 ? &r2 : nullptr, out_path, cfg);
+    if (stats) {
+        stats->n_reads = r.reads;
+        stats->n_records = r.records;
+        stats->n_mapped = r.mapped;
+        stats->n_batches = r.batches;
+        stats->bytes_in = r.bytes_in;
+        stats->bytes_out = r.bytes_out;
+        stats->seconds_total = r.seconds_total;
+        stats->seconds_map = r.seconds_map;
+        stats->seconds_wait_input = r.seconds_wait_input;
+    }
     return SA_OK;
     SA_CATCH
 }

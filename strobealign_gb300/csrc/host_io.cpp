@@ -1,13 +1,198 @@
 // Host-side inputs: reference contigs (2-bit PackedSeq form) and read batches.
 // FASTA: src/io/fasta.rs:116-165; FASTQ: src/io/fastq.rs:19-100; headers split
-// as src/io/mod.rs:33-40; wildcard bases encoded as src/packed_seq.rs:50-92.
-#include "host_state.h"
+// as src/io/mod.rs:33-40; wildcard bases encoded as src/packed_seq.rs:50-92; gzip
+// inputs as src/io/xopen.rs:9-20.
+#include "host_input.h"
 
+#include <dlfcn.h>
+#include <fcntl.h>
+#include <unistd.h>
+
+#include <cerrno>
 #include <cmath>
 #include <cstring>
-#include <fstream>
+#include <mutex>
 
 namespace sa {
+
+// ---------------------------------------------------------------- gzip through zlib
+// zlib's z_stream as its public header lays it out (identical on LP64 x86-64 and
+// aarch64); the library is opened by name, so no zlib header is needed to build.
+struct ZStream {
+    const unsigned char* next_in;
+    unsigned avail_in;
+    unsigned long total_in;
+    unsigned char* next_out;
+    unsigned avail_out;
+    unsigned long total_out;
+    const char* msg;
+    void* state;
+    void* zalloc;
+    void* zfree;
+    void* opaque;
+    int data_type;
+    unsigned long adler;
+    unsigned long reserved;
+};
+
+namespace {
+constexpr int Z_OK_ = 0, Z_STREAM_END_ = 1, Z_BUF_ERROR_ = -5, Z_NO_FLUSH_ = 0;
+
+struct Zlib {
+    int (*inflate_init2)(ZStream*, int, const char*, int) = nullptr;
+    int (*inflate)(ZStream*, int) = nullptr;
+    int (*inflate_end)(ZStream*) = nullptr;
+    int (*inflate_reset)(ZStream*) = nullptr;
+    const char* (*version)() = nullptr;
+    std::string error;
+};
+
+const Zlib& zlib() {
+    static Zlib z;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* h = dlopen("libz.so.1", RTLD_NOW | RTLD_LOCAL);
+        if (!h) h = dlopen("libz.so", RTLD_NOW | RTLD_LOCAL);
+        if (!h) {
+            z.error = "gzip input needs zlib (libz.so.1), which could not be loaded";
+            return;
+        }
+        z.inflate_init2 = (int (*)(ZStream*, int, const char*, int))dlsym(h, "inflateInit2_");
+        z.inflate = (int (*)(ZStream*, int))dlsym(h, "inflate");
+        z.inflate_end = (int (*)(ZStream*))dlsym(h, "inflateEnd");
+        z.inflate_reset = (int (*)(ZStream*))dlsym(h, "inflateReset");
+        z.version = (const char* (*)())dlsym(h, "zlibVersion");
+        if (!z.inflate_init2 || !z.inflate || !z.inflate_end || !z.inflate_reset || !z.version)
+            z.error = "libz.so.1 lacks the inflate entry points";
+    });
+    return z;
+}
+
+bool ends_with(const std::string& s, const char* suffix) {
+    const size_t n = std::strlen(suffix);
+    return s.size() >= n && s.compare(s.size() - n, n, suffix) == 0;
+}
+}  // namespace
+
+struct ByteSource::Gz {
+    ZStream zs{};
+    std::vector<unsigned char> in;
+    bool input_end = false, member_done = false, any_input = false, open = false;
+    ~Gz() {
+        if (open) zlib().inflate_end(&zs);
+    }
+};
+
+ByteSource::ByteSource(const std::string& path) : path_(path) {
+    if (path == "-") {
+        fd_ = 0;
+    } else {
+        fd_ = ::open(path.c_str(), O_RDONLY | O_CLOEXEC);
+        if (fd_ < 0) throw Error(SA_ERR_IO, "cannot open " + path + ": " + std::strerror(errno));
+        own_fd_ = true;
+    }
+    if (path != "-" && ends_with(path, ".gz")) {
+        const Zlib& z = zlib();
+        if (!z.error.empty()) {
+            ::close(fd_);
+            throw Error(SA_ERR_IO, path + ": " + z.error);
+        }
+        gz_ = std::make_unique<Gz>();
+        gz_->in.resize((size_t)1 << 20);
+        // window bits 15 + 16: gzip members only
+        if (z.inflate_init2(&gz_->zs, 15 + 16, z.version(), (int)sizeof(ZStream)) != Z_OK_) {
+            ::close(fd_);
+            throw Error(SA_ERR_IO, path + ": zlib inflateInit2 failed");
+        }
+        gz_->open = true;
+    }
+}
+
+ByteSource::~ByteSource() {
+    gz_.reset();
+    if (own_fd_ && fd_ >= 0) ::close(fd_);
+}
+
+size_t ByteSource::read_file(char* dst, size_t n) {
+    for (;;) {
+        const ssize_t k = ::read(fd_, dst, n);
+        if (k >= 0) {
+            raw_ += (uint64_t)k;
+            return (size_t)k;
+        }
+        if (errno != EINTR) throw Error(SA_ERR_IO, "read error on " + path_ + ": " + std::strerror(errno));
+    }
+}
+
+size_t ByteSource::read(char* dst, size_t n) {
+    if (!gz_) return read_file(dst, n);
+    Gz& g = *gz_;
+    const Zlib& z = zlib();
+    if (n > ((size_t)1 << 30)) n = (size_t)1 << 30;
+    for (;;) {
+        if (g.zs.avail_in == 0 && !g.input_end) {
+            const size_t k = read_file(reinterpret_cast<char*>(g.in.data()), g.in.size());
+            if (k == 0) g.input_end = true;
+            else g.any_input = true;
+            g.zs.next_in = g.in.data();
+            g.zs.avail_in = (unsigned)k;
+        }
+        if (g.member_done) {
+            // the next member starts right after this one; the input ends after a member
+            if (g.zs.avail_in == 0) return 0;
+            z.inflate_reset(&g.zs);
+            g.member_done = false;
+        }
+        if (!g.any_input) return 0;  // an empty file holds no records
+        g.zs.next_out = reinterpret_cast<unsigned char*>(dst);
+        g.zs.avail_out = (unsigned)n;
+        const int rc = z.inflate(&g.zs, Z_NO_FLUSH_);
+        const size_t produced = n - g.zs.avail_out;
+        if (rc == Z_STREAM_END_) {
+            g.member_done = true;
+        } else if (rc == Z_BUF_ERROR_) {
+            if (g.input_end && g.zs.avail_in == 0 && produced == 0)
+                throw Error(SA_ERR_FORMAT, path_ + ": unexpected end of gzip data");
+        } else if (rc != Z_OK_) {
+            throw Error(SA_ERR_FORMAT, path_ + ": invalid gzip data" + (g.zs.msg ? std::string(" (") + g.zs.msg + ")" : ""));
+        } else if (produced == 0 && g.input_end && g.zs.avail_in == 0) {
+            throw Error(SA_ERR_FORMAT, path_ + ": unexpected end of gzip data");
+        }
+        if (produced) return produced;
+    }
+}
+
+// ---------------------------------------------------------------- lines
+LineReader::LineReader(const std::string& path) : src_(path), buf_((size_t)4 << 20) {}
+
+bool LineReader::fill() {
+    if (eof_) return false;
+    if (pos_ < end_) return true;
+    pos_ = 0;
+    end_ = src_.read(buf_.data(), buf_.size());
+    if (end_ == 0) eof_ = true;
+    return end_ > 0;
+}
+
+int LineReader::peek() {
+    if (pos_ >= end_ && !fill()) return -1;
+    return (unsigned char)buf_[pos_];
+}
+
+size_t LineReader::read_line(std::string& out) {
+    size_t total = 0;
+    for (;;) {
+        if (pos_ >= end_ && !fill()) return total;
+        const char* b = buf_.data() + pos_;
+        const size_t avail = end_ - pos_;
+        const char* nl = static_cast<const char*>(std::memchr(b, '\n', avail));
+        const size_t take = nl ? (size_t)(nl - b) + 1 : avail;
+        out.append(b, take);
+        pos_ += take;
+        total += take;
+        if (nl) return total;
+    }
+}
 
 static std::string trim_end(const std::string& s) {
     size_t e = s.size();
@@ -63,13 +248,14 @@ static void validate_names(const std::vector<Contig>& cs) {
 }
 
 void load_fasta(const std::string& path, std::vector<Contig>& out) {
-    std::ifstream f(path, std::ios::binary);
-    if (!f) throw Error(SA_ERR_IO, "cannot open " + path);
+    LineReader f(path);
     std::string line;
     bool have = false;
     Contig cur;
-    while (std::getline(f, line)) {
-        if (!line.empty() && line[0] == '>') {
+    for (;;) {
+        line.clear();
+        if (!f.read_line(line)) break;
+        if (line[0] == '>') {
             if (have) out.push_back(std::move(cur));
             cur = Contig();
             std::string c;
@@ -114,62 +300,117 @@ static void push_str(std::string& buf, std::vector<uint64_t>& off, const std::st
     off.push_back(buf.size());
 }
 
-void load_reads(const std::string& path, ReadStore& rs) {
-    std::ifstream f(path, std::ios::binary);
-    if (!f) throw Error(SA_ERR_IO, "cannot open " + path);
+void reset_read_store(ReadStore& rs, bool has_qual) {
     rs = ReadStore();
     rs.seq_off.push_back(0);
     rs.name_off.push_back(0);
     rs.comment_off.push_back(0);
-    int first = f.peek();
-    if (first == '>') {
-        std::string line, name, comment, seq;
-        bool have = false, hc = false;
-        auto flush = [&]() {
-            push_str(rs.seq, rs.seq_off, seq);
-            push_str(rs.names, rs.name_off, name);
-            push_str(rs.comments, rs.comment_off, hc ? comment : std::string());
-            rs.has_comment.push_back(hc);
-            seq.clear();
-        };
-        while (std::getline(f, line)) {
-            if (!line.empty() && line[0] == '>') {
-                if (have) flush();
-                split_header(line.substr(1), name, comment, hc);
-                have = true;
-            } else {
-                std::string t = trim_end(line);
-                for (char& c : t) c = (char)toupper((unsigned char)c);
-                seq += t;
-            }
-        }
-        if (have) flush();
+    rs.has_qual = has_qual;
+}
+
+void split_read_store(ReadStore& rs, size_t from, ReadStore& tail) {
+    const size_t n = read_store_size(rs);
+    reset_read_store(tail, rs.has_qual);
+    if (from >= n) return;
+    const uint64_t s0 = rs.seq_off[from], n0 = rs.name_off[from], c0 = rs.comment_off[from];
+    tail.seq.assign(rs.seq, s0, std::string::npos);
+    if (rs.has_qual) tail.qual.assign(rs.qual, s0, std::string::npos);
+    tail.names.assign(rs.names, n0, std::string::npos);
+    tail.comments.assign(rs.comments, c0, std::string::npos);
+    for (size_t i = from + 1; i <= n; i++) {
+        tail.seq_off.push_back(rs.seq_off[i] - s0);
+        tail.name_off.push_back(rs.name_off[i] - n0);
+        tail.comment_off.push_back(rs.comment_off[i] - c0);
+    }
+    tail.has_comment.assign(rs.has_comment.begin() + (ptrdiff_t)from, rs.has_comment.end());
+    rs.seq.resize(s0);
+    if (rs.has_qual) rs.qual.resize(s0);
+    rs.names.resize(n0);
+    rs.comments.resize(c0);
+    rs.seq_off.resize(from + 1);
+    rs.name_off.resize(from + 1);
+    rs.comment_off.resize(from + 1);
+    rs.has_comment.resize(from);
+}
+
+ReadParser::ReadParser(const std::string& path) : in_(path) {
+    fasta_ = in_.peek() == '>';
+    if (fasta_) have_header_ = in_.read_line(header_) > 0;
+}
+
+// Vec::pop of the line end, then a '\r' (src/io/fastq.rs:62-66)
+static void drop_line_end(std::string& s) {
+    if (!s.empty()) s.pop_back();
+    if (!s.empty() && s.back() == '\r') s.pop_back();
+}
+
+size_t ReadParser::parse(ReadStore& rs, size_t max_records) {
+    size_t n = 0;
+    if (fasta_) {
         rs.has_qual = false;
-        return;
+        while (n < max_records && have_header_) {
+            bool hc = false;
+            split_header(header_.substr(1), name_, comment_, hc);
+            seq_.clear();
+            have_header_ = false;
+            for (;;) {
+                line_.clear();
+                if (!in_.read_line(line_)) break;
+                if (line_[0] == '>') {
+                    header_.swap(line_);
+                    have_header_ = true;
+                    break;
+                }
+                std::string t = trim_end(line_);
+                for (char& c : t) c = (char)toupper((unsigned char)c);
+                seq_ += t;
+            }
+            push_str(rs.seq, rs.seq_off, seq_);
+            push_str(rs.names, rs.name_off, name_);
+            push_str(rs.comments, rs.comment_off, hc ? comment_ : std::string());
+            rs.has_comment.push_back(hc);
+            n++;
+        }
+        return n;
     }
     rs.has_qual = true;
     rs.qual_off_unused = 0;
-    std::string l1, l2, l3, l4, name, comment;
-    bool hc;
-    while (std::getline(f, l1)) {
-        if (l1.empty() || l1[0] != '@') throw Error(SA_ERR_FORMAT, "FASTQ record must start with '@'");
-        split_header(l1.substr(1), name, comment, hc);
-        if (name.empty()) throw Error(SA_ERR_FORMAT, "Record identifier is empty");
-        if (name.size() >= 2 && (name.compare(name.size() - 2, 2, "/1") == 0 || name.compare(name.size() - 2, 2, "/2") == 0))
-            name.resize(name.size() - 2);
-        std::getline(f, l2);
-        std::getline(f, l3);
-        std::getline(f, l4);
-        if (!l2.empty() && l2.back() == '\r') l2.pop_back();
-        if (!l4.empty() && l4.back() == '\r') l4.pop_back();
-        if (l2.size() != l4.size()) throw Error(SA_ERR_FORMAT, "sequence and quality lengths differ in " + name);
-        for (char& c : l2) c = (char)toupper((unsigned char)c);
-        push_str(rs.seq, rs.seq_off, l2);
-        rs.qual += l4;
-        push_str(rs.names, rs.name_off, name);
-        push_str(rs.comments, rs.comment_off, hc ? comment : std::string());
+    while (n < max_records) {
+        line_.clear();
+        if (!in_.read_line(line_)) break;
+        if (line_[0] != '@') throw Error(SA_ERR_FORMAT, "FASTQ record must start with '@'");
+        bool hc = false;
+        split_header(line_.substr(1), name_, comment_, hc);
+        if (name_.empty()) throw Error(SA_ERR_FORMAT, "Record identifier is empty");
+        if (name_.size() >= 2 &&
+            (name_.compare(name_.size() - 2, 2, "/1") == 0 || name_.compare(name_.size() - 2, 2, "/2") == 0))
+            name_.resize(name_.size() - 2);
+        seq_.clear();
+        in_.read_line(seq_);
+        drop_line_end(seq_);
+        line_.clear();
+        in_.read_line(line_);
+        qual_.clear();
+        in_.read_line(qual_);
+        drop_line_end(qual_);
+        if (seq_.size() != qual_.size())
+            throw Error(SA_ERR_FORMAT, "Found " + std::to_string(seq_.size()) + " nucleotides but " +
+                                           std::to_string(qual_.size()) + " quality values in record '" + name_ + "'");
+        for (char& c : seq_) c = (char)toupper((unsigned char)c);
+        push_str(rs.seq, rs.seq_off, seq_);
+        rs.qual += qual_;
+        push_str(rs.names, rs.name_off, name_);
+        push_str(rs.comments, rs.comment_off, hc ? comment_ : std::string());
         rs.has_comment.push_back(hc);
+        n++;
     }
+    return n;
+}
+
+void load_reads(const std::string& path, ReadStore& rs) {
+    ReadParser p(path);
+    reset_read_store(rs, !p.fasta());
+    p.parse(rs, SIZE_MAX);
 }
 
 }  // namespace sa

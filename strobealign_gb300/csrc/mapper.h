@@ -18,6 +18,8 @@ class Mapper {
     void upload(const sa_read_batch* r1, const sa_read_batch* r2);
     void map_uploaded(sa_output* out);
     const sa_mapper_stats& stats() const { return stats_; }
+    const sa_mapping_params& mapping_params() const { return mp_; }
+    const std::vector<ContigInfo>& contigs() const { return contigs_; }
     const std::vector<double>& abundances() const { return abundances_; }
     std::vector<uint64_t> contig_lengths() const {
         std::vector<uint64_t> v;

@@ -35,7 +35,9 @@ GOLDEN_COMMANDS = {
 
 
 def main() -> None:
-    src = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference") / "tests"
+    if len(sys.argv) != 2:
+        sys.exit("usage: fetch_reference_fixtures.py REFERENCE_TREE (the strobealign source checkout)")
+    src = Path(sys.argv[1]) / "tests"
     dst = Path(__file__).resolve().parent
     for name in FILES:
         shutil.copyfile(src / name, dst / name)

@@ -1,0 +1,102 @@
+"""Input files without a GPU: gzip (single and multi-member, src/io/xopen.rs:9-20) reads
+the same records as the plain file, FASTA reads and references load from .gz, and
+broken inputs fail with an error (src/io/fastq.rs:37-86) instead of a crash."""
+import gzip
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+
+@pytest.fixture(scope="module")
+def sa():
+    import strobealign_gb300 as sa
+    sa.lib()
+    return sa
+
+
+def _same(a, b):
+    assert len(a) == len(b)
+    assert a.seq == b.seq and a.names == b.names and a.qual == b.qual and a.comments == b.comments
+    assert np.array_equal(a.seq_offsets, b.seq_offsets) and np.array_equal(a.name_offsets, b.name_offsets)
+    assert np.array_equal(a.comment_offsets, b.comment_offsets)
+
+
+def _members(data: bytes, parts: int) -> bytes:
+    cut = [len(data) * i // parts for i in range(parts + 1)]
+    return b"".join(gzip.compress(data[cut[i]:cut[i + 1]], compresslevel=1 + i % 9) for i in range(parts))
+
+
+@pytest.mark.parametrize("name", ["phix.1.fastq", "phix.tags.fastq", "interleaved.fq"])
+def test_gzip_fastq_matches_plain(sa, tmp_path, name):
+    src = GOLDEN / name
+    plain = sa.Reads.from_file(str(src))
+    assert len(plain) > 0
+    one = tmp_path / (name + ".gz")
+    one.write_bytes(gzip.compress(src.read_bytes()))
+    _same(plain, sa.Reads.from_file(str(one)))
+    # several members, split anywhere (inside records and lines)
+    multi = tmp_path / ("multi." + name + ".gz")
+    multi.write_bytes(_members(src.read_bytes(), 7))
+    _same(plain, sa.Reads.from_file(str(multi)))
+
+
+def test_gzip_fasta_reads_and_references(sa, tmp_path):
+    src = GOLDEN / "phix.fasta"
+    gz = tmp_path / "phix.fasta.gz"
+    gz.write_bytes(_members(src.read_bytes(), 3))
+    _same(sa.Reads.from_file(str(src)), sa.Reads.from_file(str(gz)))
+    a, b = sa.References.from_fasta(str(src)), sa.References.from_fasta(str(gz))
+    assert len(a) == len(b) and a.total_length == b.total_length > 5000
+
+
+def test_fasta_reads_multiline_lowercase(sa, tmp_path):
+    f = tmp_path / "r.fa"
+    f.write_bytes(b">r1 first read\nacgt\nACGN\n\n>r2\nTTTT\r\n>r3\n")
+    r = sa.Reads.from_file(str(f))
+    assert len(r) == 3 and r.qual is None
+    assert r.seq == b"ACGTACGNTTTT" and list(r.seq_offsets) == [0, 8, 12, 12]
+    assert r.names == b"r1r2r3" and r.comments == b"first read"
+
+
+def test_fastq_record_rules(sa, tmp_path):
+    f = tmp_path / "r.fq"
+    f.write_bytes(b"@a/1 c1\nacgt\n+\nIIII\n@b/2\nGG\r\n+\nII\r\n@c/3\nA\n+\nI\n")
+    r = sa.Reads.from_file(str(f))
+    assert r.names == b"abc/3" and r.seq == b"ACGTGGA" and r.qual == b"IIIIIII" and r.comments == b"c1"
+
+
+@pytest.mark.parametrize("body,msg", [
+    (b"@a\nACGT\n+\nIII\n", "quality"),
+    (b"a\nACGT\n+\nIIII\n", "'@'"),
+    (b"@\nACGT\n+\nIIII\n", "identifier"),
+    # no newline after the last quality line: its last byte goes as the line end
+    (b"@a\nACGT\n+\nIIII", "quality"),
+])
+def test_fastq_errors(sa, tmp_path, body, msg):
+    f = tmp_path / "bad.fq"
+    f.write_bytes(body)
+    with pytest.raises(sa.SaError, match=msg):
+        sa.Reads.from_file(str(f))
+
+
+def test_gzip_errors(sa, tmp_path):
+    data = gzip.compress((GOLDEN / "phix.1.fastq").read_bytes())
+    t = tmp_path / "trunc.fq.gz"
+    t.write_bytes(data[: len(data) // 2])
+    with pytest.raises(sa.SaError, match="gzip"):
+        sa.Reads.from_file(str(t))
+    c = tmp_path / "corrupt.fq.gz"
+    c.write_bytes(data[:20] + bytes(b ^ 0x5A for b in data[20:200]) + data[200:])
+    with pytest.raises(sa.SaError):
+        sa.Reads.from_file(str(c))
+    g = tmp_path / "garbage.fq.gz"
+    g.write_bytes(data + b"not a gzip member")
+    with pytest.raises(sa.SaError, match="gzip"):
+        sa.Reads.from_file(str(g))
+    e = tmp_path / "empty.fq.gz"
+    e.write_bytes(b"")
+    assert len(sa.Reads.from_file(str(e))) == 0
+    with pytest.raises(sa.SaError, match="cannot open"):
+        sa.Reads.from_file(str(tmp_path / "missing.fq.gz"))
