@@ -80,8 +80,11 @@ def parse(argv=None):
                     help="reference arm: records per step (0 = four 1 Mnt chunks per host thread)")
     ap.add_argument("--aux-steps", type=int, default=3, help="steps of the plain and batched host-buffer passes")
     ap.add_argument("--no-served", action="store_true", help="skip the served and latency passes (profiling runs)")
+    ap.add_argument("--stream-pairs", type=int, default=2_000_000,
+                    help="records of the file-to-file leg (FASTQ and FASTQ.gz through sa_map_files); 0: skip")
     ap.add_argument("--tune", type=int, default=1, help="1: autotune the mapper on a calibration sample first")
-    ap.add_argument("--tune-records", type=int, default=500_000, help="records in the calibration sample")
+    ap.add_argument("--tune-records", type=int, default=0,
+                    help="records in the calibration sample (0: the whole batch; the best knobs depend on its size)")
     return ap.parse_args(argv)
 
 
@@ -333,6 +336,60 @@ def parity_leg(g, r1, r2, rl, idx, gpu_sam: bytes, use_ssw: bool, threads: int) 
     return parity, cpu
 
 
+def stream_leg(sa, mapper, refs, r1, r2, pairs: int) -> dict:
+    """File to file: the first `pairs` records written as FASTQ (and gzip level 1), then
+    mapped into a SAM file by sa_map_files (parsing, mapping and writing overlapped);
+    the file's bytes are checked against the SAM header plus sa_map_batch's output for
+    the same records."""
+    import gzip
+    import hashlib
+    import shutil
+    import threading
+    n = min(pairs, len(r1))
+    d = tempfile.mkdtemp(prefix="sa_stream_")
+    try:
+        files = [os.path.join(d, "r1.fq")] + ([os.path.join(d, "r2.fq")] if r2 is not None else [])
+        sets = [_prefix(r1, n)] + ([_prefix(r2, n)] if r2 is not None else [])
+        t = time.time()
+        for f, rs in zip(files, sets):
+            rs.write_fastq(f)
+
+        def gz(src):
+            with open(src, "rb") as fi, gzip.open(src + ".gz", "wb", compresslevel=1) as fo:
+                shutil.copyfileobj(fi, fo, 16 << 20)
+        ths = [threading.Thread(target=gz, args=(f,)) for f in files]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        write_s = time.time() - t
+        c1 = sa.Reads.from_arrays(*_calib(r1, n))
+        c2 = sa.Reads.from_arrays(*_calib(r2, n)) if r2 is not None else None
+        hdr = sa.sam_header(refs)
+        want = hashlib.sha256(hdr + mapper.map(c1, c2)).hexdigest()
+        del c1, c2
+        out = {"records": n, "input_bytes": {"plain": sum(os.path.getsize(f) for f in files),
+                                             "gzip": sum(os.path.getsize(f + ".gz") for f in files)},
+               "write_inputs_s": round(write_s, 1), "unit": "reads/s"}
+        for kind, ext in (("plain", ""), ("gzip", ".gz")):
+            o = os.path.join(d, "out.sam")
+            t = time.time()
+            st = mapper.map_files(files[0] + ext, files[1] + ext if len(files) > 1 else None, o, header=hdr)
+            sec = time.time() - t
+            h = hashlib.sha256()
+            with open(o, "rb") as f:
+                for blk in iter(lambda: f.read(64 << 20), b""):
+                    h.update(blk)
+            os.remove(o)
+            out[kind] = {"reads_per_s": st["n_reads"] / sec, "seconds": round(sec, 3),
+                         "seconds_map": round(st["seconds_map"], 3),
+                         "seconds_wait_input": round(st["seconds_wait_input"], 3), "batches": st["n_batches"],
+                         "sam_bytes": st["bytes_out"], "identical": h.hexdigest() == want}
+        return out
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
 def slowest_rank(pg, seconds: float, device: str = "cpu") -> float:
     """Max over ranks of a rank's wall time (the job's time); identity without a process group."""
     if pg is None:
@@ -438,11 +495,11 @@ def main():
     # its choice stays in the mapper for the timed passes
     tune = None
     if args.tune:
-        m = min(len(R1), args.tune_records)
-        c1 = sa.Reads.from_arrays(*_calib(r1, m))
-        c2 = sa.Reads.from_arrays(*_calib(r2, m)) if r2 is not None else None
+        m = min(len(R1), args.tune_records or len(R1))
+        c1 = sa.Reads.from_arrays(*_calib(r1, m)) if m < len(R1) else R1
+        c2 = (sa.Reads.from_arrays(*_calib(r2, m)) if m < len(R1) else R2) if r2 is not None else None
         t0 = time.time()
-        tune = mapper.autotune(c1, c2, rounds=2)
+        tune = mapper.autotune(c1, c2, rounds=1 if m == len(R1) else 2)
         calib_reads = m * (2 if r2 is not None else 1)
         tune.update(sample_records=m, tune_s=round(time.time() - t0, 1),
                     default_reads_per_s=calib_reads / tune["seconds_default"],
@@ -549,6 +606,12 @@ def main():
             del gpu_sam
         except Exception as e:  # reported, never fatal for the GPU line
             parity = {"identical": None, "error": f"{type(e).__name__}: {str(e)[:300]}"}
+    stream = None
+    if rank == 0 and args.stream_pairs:
+        try:
+            stream = stream_leg(sa, mapper, refs, r1, r2, args.stream_pairs)
+        except Exception as e:  # reported, never fatal for the GPU line
+            stream = {"error": f"{type(e).__name__}: {str(e)[:300]}"}
     if rank != 0:
         pg.destroy_process_group()
         return
@@ -579,6 +642,9 @@ def main():
                                  "device, NAM parts overlapped with the policy and extension waves",
                    "e2e_form": "served: the same records as requests of log-uniform 1..100k pairs through "
                                "sa_session submit/wait from host buffers, continuous batching",
+                   "stream_form": "file to file: the first stream-pairs records as FASTQ and as FASTQ.gz (level 1) "
+                                  "mapped into a SAM file by sa_map_files (reader, mapper and writer threads "
+                                  "overlapped), bytes checked against sa_map_batch",
                    "plain_form": "stage-synchronous: sa_map_batch from host buffers with overlap = 0 (NAM parts "
                                  "one after another, then policy and extension waves taking turns)",
                    "aux_steps": aux, "requests_per_step": len(reqs), "sam_bytes_per_step": sam_bytes,
@@ -595,6 +661,7 @@ def main():
                                                "vs_batched_e2e": served / batched_e2e,
                                                "latency_open_loop": lat},
         "gpu_launches": launches,
+        "stream": stream,
         "tuning": tune,
         "stage_share": shares,
         # wall seconds per step: NAM pipeline (GPU), extension waves (GPU, incl. job

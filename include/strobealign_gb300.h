@@ -469,13 +469,19 @@ int32_t sa_mapper_set_schedule(sa_mapper* m, const sa_schedule_params* p);
  *   ssw_wave_max_qlen       SSW tasks of reads up to this length (at most 192) run on
  *                           the lane-wavefront kernel, longer ones a warp per task
  *   chain_lane_cluster_max  clusters of a long read orientation's anchors up to this
- *                           size are chained by one thread, larger ones by a warp */
+ *                           size are chained by one thread, larger ones by a warp
+ *   l2_fetch_bytes          the context's L2 fetch granularity for DRAM reads
+ *                           (cudaLimitMaxL2FetchGranularity: 32, 64 or 128; 0 keeps the
+ *                           value the context had when the mapper was created).  It is a
+ *                           limit of the calling process's CUDA context on the mapper's
+ *                           device, so it applies to every kernel of the process. */
 typedef struct {
     uint32_t parts;
     uint64_t wave_min_jobs;
     uint64_t max_wave_jobs;
     uint32_t ssw_wave_max_qlen;
     uint32_t chain_lane_cluster_max;
+    uint32_t l2_fetch_bytes;
 } sa_tuning;
 typedef struct {
     sa_tuning chosen;

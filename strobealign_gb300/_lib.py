@@ -92,7 +92,7 @@ class ScheduleParams(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("parts", u32), ("wave_min_jobs", u64), ("max_wave_jobs", u64), ("ssw_wave_max_qlen", u32),
-                ("chain_lane_cluster_max", u32)]
+                ("chain_lane_cluster_max", u32), ("l2_fetch_bytes", u32)]
 
 
 class TuneReport(C.Structure):

@@ -490,6 +490,7 @@ static void tuning_to_c(const Mapper::Tuning& t, sa_tuning* o) {
     o->max_wave_jobs = t.max_wave_jobs;
     o->ssw_wave_max_qlen = t.wave_qmax;
     o->chain_lane_cluster_max = t.chain_lane_max;
+    o->l2_fetch_bytes = t.l2_fetch;
 }
 
 void sa_tuning_default(sa_tuning* t) {
@@ -503,12 +504,15 @@ int32_t sa_mapper_set_tuning(sa_mapper* m, const sa_tuning* t) {
     require(t->ssw_wave_max_qlen >= 1 && t->ssw_wave_max_qlen <= 192, "ssw_wave_max_qlen must be in 1..192");
     require(t->chain_lane_cluster_max >= 1 && t->chain_lane_cluster_max <= 4096,
             "chain_lane_cluster_max must be in 1..4096");
+    require(t->l2_fetch_bytes == 0 || t->l2_fetch_bytes == 32 || t->l2_fetch_bytes == 64 || t->l2_fetch_bytes == 128,
+            "l2_fetch_bytes must be 0, 32, 64 or 128");
     Mapper::Tuning x;
     x.parts = t->parts;
     x.wave_min_jobs = t->wave_min_jobs;
     x.max_wave_jobs = t->max_wave_jobs;
     x.wave_qmax = t->ssw_wave_max_qlen;
     x.chain_lane_max = t->chain_lane_cluster_max;
+    x.l2_fetch = t->l2_fetch_bytes;
     m->m->set_tuning(x);
     return SA_OK;
     SA_CATCH

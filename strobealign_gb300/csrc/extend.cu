@@ -1580,21 +1580,22 @@ __global__ void __launch_bounds__(128) k_band_warp(SswTask* tasks, uint32_t n_ta
         const int rl = tk.ref_end1 - tk.ref_begin1 + 1, ql = tk.read_end1 - tk.read_begin1 + 1;
         const int len = rl > ql ? rl : ql;
         int bw = (rl > ql ? rl - ql : ql - rl) + 1;
-        // band doubling (ext/ssw/ssw.c:626-660)
+        // band doubling (ext/ssw/ssw.c:626-660).  Every pass records its direction bits:
+        // the doubling ends on the width it ran last, so the last pass's bits are the
+        // ones the traceback reads and no pass is repeated to record them.
         bool fallback = false;
         int mx = 0;
+        uint32_t* rowbits = reinterpret_cast<uint32_t*>(hscratch + p.h_off);
         do {
             if (bw > 15) {
                 fallback = true;
                 break;
             }
-            mx = band_pass_warp(r + tk.ref_begin1, q + tk.read_begin1, rl, ql, bw, sc, nullptr);
+            mx = band_pass_warp(r + tk.ref_begin1, q + tk.read_begin1, rl, ql, bw, sc, rowbits);
             bw *= 2;
         } while (mx < tk.score1 && bw <= len);
         if (fallback) continue;  // raw_off stays RAW_FALLBACK
         bw /= 2;
-        uint32_t* rowbits = reinterpret_cast<uint32_t*>(hscratch + p.h_off);
-        band_pass_warp(r + tk.ref_begin1, q + tk.read_begin1, rl, ql, bw, sc, rowbits);
         __syncwarp();
         if (lane == 0) {
             // traceback (ext/ssw/ssw.c:680-753) over the flat direction array of
@@ -1602,22 +1603,28 @@ __global__ void __launch_bounds__(128) k_band_warp(SswTask* tasks, uint32_t n_ta
             uint32_t* c = rowbits + 4 * (size_t)ql;
             const int width_d = 2 * bw + 1;
             const int64_t dsize = (int64_t)width_d * ql * 3;
-            auto dir_at = [&](int64_t at) -> int {
-                const int row = (int)(at / (3 * width_d));
-                const int rem = (int)(at % (3 * width_d));
-                const int k = rem / 3, w = rem % 3;
+            // the row's four direction words, loaded when the walk enters a row
+            int cached = -1;
+            uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
+            auto dir_of = [&](int row, int k, int w) -> int {
                 const int x = row - bw > 0 ? row - bw : 0;
                 const int end = rl - 1 < row + bw ? rl - 1 : row + bw;
                 if (k > end - x) return 0;  // not written by the pass
-                const uint32_t* rb = rowbits + 4 * (size_t)row;
-                const int dde = (rb[0] >> k) & 1 ? 3 : 2;
-                const int ddf = (rb[1] >> k) & 1 ? 5 : 4;
+                if (row != cached) {
+                    const uint32_t* rb = rowbits + 4 * (size_t)row;
+                    w0 = rb[0];
+                    w1 = rb[1];
+                    w2 = rb[2];
+                    w3 = rb[3];
+                    cached = row;
+                }
+                const int dde = (w0 >> k) & 1 ? 3 : 2;
+                const int ddf = (w1 >> k) & 1 ? 5 : 4;
                 if (w == 0) return dde;
                 if (w == 1) return ddf;
-                return (rb[2] >> k) & 1 ? 1 : ((rb[3] >> k) & 1 ? dde : ddf);
+                return (w2 >> k) & 1 ? 1 : ((w3 >> k) & 1 ? dde : ddf);
             };
             int i = ql - 1, j = rl - 1, e = 0, which = 2;
-            int64_t line = (int64_t)width_d * i * 3;
             char op = 'M', prev = 'M';
             uint32_t nc = 0;
             const uint32_t cap = (uint32_t)(rl + ql + 4);
@@ -1627,15 +1634,24 @@ __global__ void __launch_bounds__(128) k_band_warp(SswTask* tasks, uint32_t n_ta
             };
             while (i >= 0 && j > 0) {
                 const int x = i - bw > 0 ? i - bw : 0;
-                const int64_t at = line + (int64_t)(j - x) * 3 + which;
-                if (at < 0 || at >= dsize) {
-                    fail = true;
-                    break;
+                const int k = j - x;
+                int d;
+                if (k >= 0 && k < width_d) {
+                    d = dir_of(i, k, which);  // the flat index falls in row i
+                } else {
+                    // the flat index (row i, band column k) runs into a neighbouring row
+                    const int64_t at = (int64_t)width_d * i * 3 + (int64_t)k * 3 + which;
+                    if (at < 0 || at >= dsize) {
+                        fail = true;
+                        break;
+                    }
+                    const int rem = (int)(at % (3 * width_d));
+                    d = dir_of((int)(at / (3 * width_d)), rem / 3, rem % 3);
                 }
-                switch (dir_at(at)) {
-                    case 1: --i; --j; which = 2; line -= width_d * 3; op = 'M'; break;
-                    case 2: --i; which = 0; line -= width_d * 3; op = 'I'; break;
-                    case 3: --i; which = 2; line -= width_d * 3; op = 'I'; break;
+                switch (d) {
+                    case 1: --i; --j; which = 2; op = 'M'; break;
+                    case 2: --i; which = 0; op = 'I'; break;
+                    case 3: --i; which = 2; op = 'I'; break;
                     case 4: --j; which = 1; op = 'D'; break;
                     case 5: --j; which = 2; op = 'D'; break;
                     default: fail = true;

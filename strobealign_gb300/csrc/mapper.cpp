@@ -23,6 +23,10 @@ namespace sa {
 Mapper::Mapper(const sa_index* idx, const sa_refs* refs, const sa_chaining_params& cp, const sa_mapping_params& mp)
     : idx_(idx), refs_(refs), cp_(cp), mp_(mp) {
     if (mp.rg_id) rg_id_ = mp.rg_id;
+    if (cudaDeviceGetLimit(&l2_fetch_default_, cudaLimitMaxL2FetchGranularity) != cudaSuccess) {
+        l2_fetch_default_ = 0;
+        cudaGetLastError();
+    }
     // SA_TRACE_WAVES=1: one line per extension wave on stderr
     const char* tr = std::getenv("SA_TRACE_WAVES");
     trace_ = tr && *tr && *tr != '0';
@@ -72,6 +76,8 @@ Mapper::Mapper(const sa_index* idx, const sa_refs* refs, const sa_chaining_param
 }
 
 Mapper::~Mapper() {
+    // the fetch granularity is the context's: give back the value found at construction
+    if (l2_fetch_ && l2_fetch_default_) cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, l2_fetch_default_);
     if (st_) cudaStreamDestroy(st_);
     if (stn_) cudaStreamDestroy(stn_);
 }
@@ -681,6 +687,11 @@ void Mapper::set_tuning(const Tuning& t) {
     set_max_wave_jobs(t.max_wave_jobs);
     ews_.wave_qmax = std::max<uint32_t>(1, t.wave_qmax);
     chain_lane_max_ = std::max<uint32_t>(1, t.chain_lane_max);
+    if (t.l2_fetch != l2_fetch_) {
+        const size_t v = t.l2_fetch ? t.l2_fetch : l2_fetch_default_;
+        if (v) SA_CUDA(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, v));
+        l2_fetch_ = t.l2_fetch;
+    }
 }
 
 Mapper::Tuning Mapper::tuning() const {
@@ -690,6 +701,7 @@ Mapper::Tuning Mapper::tuning() const {
     t.max_wave_jobs = max_wave_jobs_;
     t.wave_qmax = ews_.wave_qmax;
     t.chain_lane_max = chain_lane_max_;
+    t.l2_fetch = l2_fetch_;
     return t;
 }
 
@@ -700,6 +712,9 @@ Mapper::TuneReport Mapper::autotune(const sa_read_batch* r1, const sa_read_batch
     upload(r1, r2);
     std::vector<char> want;
     TuneReport rep;
+    // SA_TRACE_TUNE=1: one line per trial on stderr
+    const char* tt = std::getenv("SA_TRACE_TUNE");
+    const bool trace_tune = tt && *tt && *tt != '0';
     auto run = [&](const Tuning& t) {
         set_tuning(t);
         std::vector<double> secs;
@@ -714,6 +729,10 @@ Mapper::TuneReport Mapper::autotune(const sa_read_batch* r1, const sa_read_batch
         }
         rep.trials++;
         std::sort(secs.begin(), secs.end());
+        if (trace_tune)
+            std::fprintf(stderr, "sa_tune parts=%u wave_min=%llu wave_max=%llu wave_qmax=%u chain_lane=%u l2=%u s=%.4f\n",
+                         t.parts, (unsigned long long)t.wave_min_jobs, (unsigned long long)t.max_wave_jobs, t.wave_qmax,
+                         t.chain_lane_max, t.l2_fetch, secs[secs.size() / 2]);
         return secs[secs.size() / 2];
     };
     Tuning best;  // the defaults
@@ -743,6 +762,7 @@ Mapper::TuneReport Mapper::autotune(const sa_read_batch* r1, const sa_read_batch
     knob(&Tuning::wave_min_jobs, {8192, 131072});
     if (max_qlen_ > 128) knob(&Tuning::wave_qmax, {128, 160});
     knob(&Tuning::chain_lane_max, {16, 128});
+    knob(&Tuning::l2_fetch, {32, 64, 128});
     set_tuning(best);
     overlap_ = saved_overlap;
     rep.chosen = best;

@@ -52,6 +52,7 @@ class Mapper {
         uint32_t parts = 4;
         uint64_t wave_min_jobs = 32768, max_wave_jobs = 262144;
         uint32_t wave_qmax = 192, chain_lane_max = 48;
+        uint32_t l2_fetch = 0;  // 0: the context's value at construction
     };
     struct TuneReport {
         Tuning chosen;
@@ -102,6 +103,8 @@ class Mapper {
     uint64_t max_wave_jobs_ = 262144;
     bool overlap_ = true;
     uint32_t chain_lane_max_ = 48;
+    uint32_t l2_fetch_ = 0;           // applied by set_tuning (0: untouched)
+    size_t l2_fetch_default_ = 0;     // the context's limit at construction
     bool trace_ = false;
 
     const sa_index* idx_;

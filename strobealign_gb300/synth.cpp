@@ -19,6 +19,8 @@
 // strands; substitutions at `sub` per base, insertions/deletions of 1-3 bases
 // (geometric, p = 1/2, truncated) at `indel` per base, the read cut back to its
 // length; a `rescue_fraction` of pairs has one mate with 15% extra substitutions.
+#include <string>
+#include <cstdio>
 #include <algorithm>
 #include <atomic>
 #include <cstdint>
@@ -368,6 +370,40 @@ int32_t syn_reads(uint64_t seed, const uint8_t* genome, const uint64_t* starts, 
         if (paired) std::vector<uint8_t>().swap(out2[b]);
     });
     return 0;
+}
+
+// Records [0, n) as FASTQ ("@name", sequence, "+", quality; qual NULL writes 'I' for
+// every base) to path; 0 on success, -1 on an I/O error.
+int32_t syn_write_fastq(const char* path, uint64_t n, const uint8_t* seq, const uint64_t* off, const uint8_t* names,
+                        const uint64_t* name_off, const uint8_t* qual) {
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return -1;
+    std::vector<char> buf;
+    buf.reserve((size_t)8 << 20);
+    bool ok = true;
+    std::string fill;
+    for (uint64_t i = 0; i < n && ok; i++) {
+        const uint64_t a = off[i], b = off[i + 1];
+        buf.push_back('@');
+        buf.insert(buf.end(), names + name_off[i], names + name_off[i + 1]);
+        buf.push_back('\n');
+        buf.insert(buf.end(), seq + a, seq + b);
+        buf.insert(buf.end(), {'\n', '+', '\n'});
+        if (qual) {
+            buf.insert(buf.end(), qual + a, qual + b);
+        } else {
+            if (fill.size() < b - a) fill.assign(b - a, 'I');
+            buf.insert(buf.end(), fill.begin(), fill.begin() + (ptrdiff_t)(b - a));
+        }
+        buf.push_back('\n');
+        if (buf.size() >= ((size_t)8 << 20)) {
+            ok = std::fwrite(buf.data(), 1, buf.size(), f) == buf.size();
+            buf.clear();
+        }
+    }
+    if (ok && !buf.empty()) ok = std::fwrite(buf.data(), 1, buf.size(), f) == buf.size();
+    if (std::fclose(f) != 0) ok = false;
+    return ok ? 0 : -1;
 }
 
 }  // extern "C"

@@ -55,6 +55,9 @@ def _native() -> C.CDLL:
     lib.syn_reads.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32,
                               C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_char, C.c_void_p,
                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]
+    lib.syn_write_fastq.restype = C.c_int32
+    lib.syn_write_fastq.argtypes = [C.c_char_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_char_p, C.c_void_p,
+                                    C.c_char_p]
     return lib
 
 
@@ -101,10 +104,13 @@ class ReadSet:
         return n, s
 
     def write_fastq(self, path: str) -> None:
-        with open(path, "wb") as f:
-            for i in range(len(self)):
-                n, s = self.record(i)
-                f.write(b"@" + n.encode() + b"\n" + s + b"\n+\n" + b"I" * len(s) + b"\n")
+        """FASTQ with 'I' for every quality (synth.cpp syn_write_fastq)."""
+        seq = np.ascontiguousarray(self.seq, dtype=np.uint8)
+        off = np.ascontiguousarray(self.offsets, dtype=np.uint64)
+        no = np.ascontiguousarray(self.name_offsets, dtype=np.uint64)
+        if _native().syn_write_fastq(os.fsencode(path), len(self), seq.ctypes.data, off.ctypes.data, bytes(self.names),
+                                     no.ctypes.data, None) != 0:
+            raise OSError(f"cannot write {path}")
 
 
 def _genome_arrays(genome: Genome):

@@ -341,7 +341,8 @@ def test_tuning_knobs_do_not_change_output(sa, synth, repeats):
         r2 = sa.Reads.from_file(d["f2"])
         want = run_oracle_cli(["--no-PG", d["fa"], d["f1"], d["f2"]])[len(sa.sam_header(refs)):]
         for kw in (dict(chain_lane_cluster_max=1), dict(chain_lane_cluster_max=4096),
-                   dict(ssw_wave_max_qlen=64, parts=1, max_wave_jobs=300, wave_min_jobs=1)):
+                   dict(ssw_wave_max_qlen=64, parts=1, max_wave_jobs=300, wave_min_jobs=1),
+                   dict(l2_fetch_bytes=32), dict(l2_fetch_bytes=128)):
             m = sa.Mapper(idx, refs)
             m.set_tuning(**kw)
             got = m.map(r1, r2)
@@ -353,6 +354,14 @@ def test_tuning_knobs_do_not_change_output(sa, synth, repeats):
         assert m.map_uploaded() == want
     with pytest.raises(sa.SaError):
         sa.Mapper(idx, refs).set_tuning(ssw_wave_max_qlen=500)
+    with pytest.raises(sa.SaError):
+        sa.Mapper(idx, refs).set_tuning(l2_fetch_bytes=48)
+    # a mapper gives the context's fetch granularity back when it is set to 0
+    m = sa.Mapper(idx, refs)
+    m.set_tuning(l2_fetch_bytes=32)
+    assert m.tuning()["l2_fetch_bytes"] == 32
+    m.set_tuning(l2_fetch_bytes=0)
+    assert m.tuning()["l2_fetch_bytes"] == 0
 
 
 def test_synthetic_paired_end_small_chunks_matches_oracle(sa, synth):
