@@ -683,6 +683,16 @@ ALGO_BYTES = {
     # read bases in; per randstrobe out: hash, reverse-complement hash, start, end
     "seed": lambda c: c["n_bases"] + 24 * c["n_randstrobes"],
 }
+# DRAM bytes (read + write) the kernels moved in one ncu capture of the human-shaped
+# workload at 1/10 scale (profiles/dram_traffic_nam_and_extension_kernels_human_scale0.1.md),
+# per unit of work; a full-scale launch's traffic is this times the units it processes
+# (the kernels touch the index at random, so the bytes grow with the reads).
+NCU_DRAM = {
+    "lookup": (24.8e3, "read"),     # k_probe 11.8 KB + k_anchors (two passes) 11.2 KB + k_hits 1.7 KB
+    "seed": (2.46e3, "read"),       # k_seed: 349 MB read + 882 MB written per 500k reads
+    "sw": (0.012, "canonical cell"),  # k_ssw_wave: 8.9 MB per launch of 7.4e8 canonical cells
+}
+NCU_DRAM_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, 1/10-scale capture, scaled by units per launch"
 # stages reported as anchors per second (no HBM or ALU roofline model)
 ANCHOR_RATE = ("sort", "chain")
 
@@ -715,7 +725,9 @@ def roofline_for(dom, kern, cells, peaks, clocks, counts, steps, sms, n_reads, l
         total = per_read * n_reads * steps
         achieved = total / (ms / 1000.0) / 1e9 if ms else 0.0
         out["lookup"] = {"kernel": "k_probe + k_hits + k_anchors", "bound": "hbm (random 32-byte sectors)",
-                         "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                         "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": NCU_DRAM["lookup"][0] * n_reads * steps / max(1, lk[0][1]),
+                         "traffic_source": NCU_DRAM_SOURCE,
                          "avg_launch_ms": ms / max(1, lk[0][1]), "launches": lk[0][1] + lk[1][1],
                          "algorithmic_bytes_per_read": per_read, "model": model}
     for st, f in ALGO_BYTES.items():
@@ -725,8 +737,10 @@ def roofline_for(dom, kern, cells, peaks, clocks, counts, steps, sms, n_reads, l
         sec = ms / 1000.0
         per_launch = f(counts) * steps / n
         achieved = per_launch * n / sec / 1e9
+        traffic = NCU_DRAM[st][0] * n_reads * steps / n if st in NCU_DRAM else None
         out[st] = {"kernel": st, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                   "frac": achieved / hbm, "traffic": None, "avg_launch_ms": ms / n, "launches": n,
+                   "frac": achieved / hbm, "traffic": traffic, "traffic_source": NCU_DRAM_SOURCE,
+                   "avg_launch_ms": ms / n, "launches": n,
                    "algorithmic_bytes_per_launch": per_launch}
     for st in ANCHOR_RATE:
         if st in kern and kern[st][1]:
@@ -743,7 +757,9 @@ def roofline_for(dom, kern, cells, peaks, clocks, counts, steps, sms, n_reads, l
         achieved = cells.get("canonical", 0) / sec / 1e9 if sec else 0.0
         computed = sum(v for k, v in cells.items() if k != "canonical")
         out["sw"] = {"kernel": "k_ssw (byte, word, reverse passes)", "bound": "int32", "achieved": achieved,
-                     "peak": peak_gcups, "unit": "GCUPS", "frac": achieved / peak_gcups, "traffic": None,
+                     "peak": peak_gcups, "unit": "GCUPS", "frac": achieved / peak_gcups,
+                     "traffic": NCU_DRAM["sw"][0] * cells.get("canonical", 0) / max(n, 1),
+                     "traffic_source": NCU_DRAM_SOURCE,
                      "avg_launch_ms": ms / max(n, 1), "launches": n,
                      "computed_gcups": computed / sec / 1e9 if sec else 0.0, "cells": cells,
                      "peak_source": f"{sms} SMs x 128 INT32 lanes x median SM clock under load / 11 ops per cell"}

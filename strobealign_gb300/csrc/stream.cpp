@@ -6,6 +6,7 @@
 // with a batch of many chunks as the unit handed to the GPU.
 #include "stream.h"
 
+#include <algorithm>
 #include <atomic>
 #include <cerrno>
 #include <condition_variable>
@@ -143,7 +144,6 @@ StreamResult map_files(Mapper& m, const std::string& reads1, const std::string* 
             auto pend = std::make_unique<InBatch>();
             reset_read_store(pend->r1, !p1->fasta());
             if (p2) reset_read_store(pend->r2, !p2->fasta());
-            const size_t step = 1 << 16;
             bool at_end = false;
             while (true) {
                 // parse until the pending records hold a batch's bases and one whole chunk
@@ -154,6 +154,12 @@ StreamResult map_files(Mapper& m, const std::string& reads1, const std::string* 
                         cut = whole_chunks(pend->r1, p2 ? &pend->r2 : nullptr, chunk_size, at_end);
                         if (cut > 0 || at_end) break;
                     }
+                    // records to parse next: about what the batch still lacks, at the
+                    // mean record length so far (150 nt per mate before the first)
+                    const size_t have = read_store_size(pend->r1);
+                    const double per_rec = have ? (double)bases / (double)have : (p2 ? 300.0 : 150.0);
+                    const double lack = bases < batch_bases ? (double)(batch_bases - bases) : (double)chunk_size;
+                    const size_t step = (size_t)std::min(65536.0, std::max(256.0, lack / per_rec + 1.0));
                     size_t k1 = 0, k2 = 0;
                     if (p2) {
                         std::exception_ptr e2;
