@@ -755,14 +755,29 @@ def roofline_for(dom, kern, cells, peaks, clocks, counts, steps, sms, n_reads, l
         clock = (clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)) * 1e6
         peak_gcups = sms * 128 * clock / 11 / 1e9
         achieved = cells.get("canonical", 0) / sec / 1e9 if sec else 0.0
-        computed = sum(v for k, v in cells.items() if k != "canonical")
+        computed = sum(cells.get(k, 0) for k in ("forward_byte", "forward_word", "reverse_byte", "reverse_word"))
+        sw_cells = {k: v for k, v in cells.items() if not k.startswith("band_")}
         out["sw"] = {"kernel": "k_ssw (byte, word, reverse passes)", "bound": "int32", "achieved": achieved,
                      "peak": peak_gcups, "unit": "GCUPS", "frac": achieved / peak_gcups,
                      "traffic": NCU_DRAM["sw"][0] * cells.get("canonical", 0) / max(n, 1),
                      "traffic_source": NCU_DRAM_SOURCE,
                      "avg_launch_ms": ms / max(n, 1), "launches": n,
-                     "computed_gcups": computed / sec / 1e9 if sec else 0.0, "cells": cells,
+                     "computed_gcups": computed / sec / 1e9 if sec else 0.0, "cells": sw_cells,
                      "peak_source": f"{sms} SMs x 128 INT32 lanes x median SM clock under load / 11 ops per cell"}
+    if kern.get("banded_traceback", [0, 0])[1] and cells.get("band_canonical"):
+        # banded_sw (ext/ssw/ssw.c:598-769): the final pass's band cells per second, the
+        # same integer-ALU model as SSW; the doubling passes' cells beside it
+        ms, n = kern["banded_traceback"]
+        sec = ms / 1000.0
+        clock = (clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)) * 1e6
+        peak_gcups = sms * 128 * clock / 11 / 1e9
+        achieved = cells["band_canonical"] / sec / 1e9 if sec else 0.0
+        out["band"] = {"kernel": "k_band_warp + k_band_width_wide + k_band_trace_wide", "bound": "int32",
+                       "achieved": achieved, "peak": peak_gcups, "unit": "GCUPS", "frac": achieved / peak_gcups,
+                       "traffic": None, "avg_launch_ms": ms / max(n, 1), "launches": n,
+                       "computed_gcups": cells.get("band_computed", 0) / sec / 1e9 if sec else 0.0,
+                       "cells": {"canonical": cells["band_canonical"], "computed": cells.get("band_computed", 0)},
+                       "peak_source": f"{sms} SMs x 128 INT32 lanes x median SM clock under load / 11 ops per cell"}
     key = "sw" if dom in ("sw_byte", "sw_word") else "lookup" if dom == "hits" else dom
     head = dict(out.get(key) or {"kernel": dom, "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s",
                                  "frac": None, "traffic": None})

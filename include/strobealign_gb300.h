@@ -428,6 +428,9 @@ typedef struct {
     /* work counts of the NAM stages: read bases, randstrobes (both orientations; one
      * index probe each), anchors */
     uint64_t n_bases, n_randstrobes, n_anchor_total;
+    /* banded traceback cells (banded_sw, ext/ssw/ssw.c:598-769): [0] every pass of the
+     * band doubling, [1] the final pass, (2bw+1)-wide band rows clipped to the window */
+    uint64_t band_cells[2];
 } sa_mapper_stats;
 int32_t sa_mapper_get_stats(const sa_mapper* m, sa_mapper_stats* out);
 /* Record CUDA events around each stage's launches (off by default). */

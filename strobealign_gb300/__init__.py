@@ -487,6 +487,8 @@ class Mapper:
         d["kernel_launches"] = {n: s.kernel_launches[i] for i, n in enumerate(L.KERNEL_SLOTS)}
         d["sw_cells"] = dict(zip(("canonical", "forward_byte", "forward_word", "reverse_byte", "reverse_word"),
                                  list(s.sw_cells)))
+        d["sw_cells"].update(band_computed=int(s.band_cells[0]), band_canonical=int(s.band_cells[1]))
+        d.pop("band_cells", None)
         return d
 
     def set_profiling(self, on: bool = True) -> None:

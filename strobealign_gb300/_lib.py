@@ -118,7 +118,7 @@ class MapperStats(C.Structure):
                 ("seconds_policy", f64), ("seconds_total", f64), ("n_jobs", u64), ("n_waves", u64),
                 ("n_launches", u64), ("h2d_bytes", u64), ("d2h_bytes", u64), ("n_nams", u64), ("n_anchors", u64),
                 ("kernel_ms", f64 * 16), ("kernel_launches", u64 * 16), ("sw_cells", u64 * 5),
-                ("n_bases", u64), ("n_randstrobes", u64), ("n_anchor_total", u64)]
+                ("n_bases", u64), ("n_randstrobes", u64), ("n_anchor_total", u64), ("band_cells", u64 * 2)]
 
 
 KERNEL_SLOTS = ["seed", "hits", "anchors", "sort", "chain", "nams_other", "prepare", "fill", "sw_byte", "sw_word",

@@ -1563,6 +1563,28 @@ __device__ int band_pass_warp(const uint8_t* ref, const uint8_t* read, int rl, i
     return mx;
 }
 
+// Cells of one banded pass (the band's cells of every row), warp-collective
+__device__ __forceinline__ uint64_t band_cells(int rl, int ql, int bw) {
+    const int lane = threadIdx.x & 31;
+    uint32_t c = 0;
+    for (int i = lane; i < ql; i += 32) {
+        const int x = i - bw > 0 ? i - bw : 0;
+        const int end = rl - 1 < i + bw ? rl - 1 : i + bw;
+        if (end >= x) c += (uint32_t)(end - x + 1);
+    }
+    for (int d = 16; d > 0; d >>= 1) c += __shfl_xor_sync(FULLM, c, d);
+    return c;
+}
+
+// banded cells at counters[24..27] (u64): every pass's, and the final pass's
+__device__ __forceinline__ void count_band_cells(uint32_t* counters, uint64_t computed, uint64_t canonical) {
+    unsigned long long* bc = reinterpret_cast<unsigned long long*>(counters + 24);
+    if ((threadIdx.x & 31) == 0) {
+        if (computed) atomicAdd(bc, (unsigned long long)computed);
+        if (canonical) atomicAdd(bc + 1, (unsigned long long)canonical);
+    }
+}
+
 __global__ void __launch_bounds__(128) k_band_warp(SswTask* tasks, uint32_t n_tasks, const PrepRec* prep,
                                                    const uint8_t* arena, int32_t* hscratch, AlignScores sc,
                                                    uint32_t* counters) {
@@ -1585,6 +1607,7 @@ __global__ void __launch_bounds__(128) k_band_warp(SswTask* tasks, uint32_t n_ta
         // ones the traceback reads and no pass is repeated to record them.
         bool fallback = false;
         int mx = 0;
+        uint64_t computed = 0;
         uint32_t* rowbits = reinterpret_cast<uint32_t*>(hscratch + p.h_off);
         do {
             if (bw > 15) {
@@ -1592,10 +1615,15 @@ __global__ void __launch_bounds__(128) k_band_warp(SswTask* tasks, uint32_t n_ta
                 break;
             }
             mx = band_pass_warp(r + tk.ref_begin1, q + tk.read_begin1, rl, ql, bw, sc, rowbits);
+            computed += band_cells(rl, ql, bw);
             bw *= 2;
         } while (mx < tk.score1 && bw <= len);
-        if (fallback) continue;  // raw_off stays RAW_FALLBACK
+        if (fallback) {
+            count_band_cells(counters, computed, 0);
+            continue;  // raw_off stays RAW_FALLBACK
+        }
         bw /= 2;
+        count_band_cells(counters, computed, band_cells(rl, ql, bw));
         __syncwarp();
         if (lane == 0) {
             // traceback (ext/ssw/ssw.c:680-753) over the flat direction array of
@@ -1892,15 +1920,18 @@ __global__ void __launch_bounds__(32) k_band_width_wide(SswTask* tasks, const ui
         int bw = (rl > ql ? rl - ql : ql - rl) + 1;
         int mx = 0;
         bool fail = false;
+        uint64_t computed = 0;
         do {
             if (2 * bw + 4 > maxc) {
                 fail = true;
                 break;
             }
             mx = band_pass_wide(r + tk.ref_begin1, q + tk.read_begin1, rl, ql, bw, sc, band_smem, maxc, nullptr, 0);
+            computed += band_cells(rl, ql, bw);
             bw *= 2;
         } while (mx < tk.score1 && bw <= len);
         bw /= 2;
+        count_band_cells(counters, computed, 0);
         if (lane == 0) {
             tk.band_width = bw;
             if (fail) tk.flag = 1;
@@ -1935,6 +1966,10 @@ __global__ void __launch_bounds__(32) k_band_trace_wide(SswTask* tasks, const ui
         const int nch = (2 * bw + 1 + 31) / 32;
         uint32_t* rowbits = reinterpret_cast<uint32_t*>(dir + dir_off[ti]);
         band_pass_wide(r + tk.ref_begin1, q + tk.read_begin1, rl, ql, bw, sc, band_smem, maxc, rowbits, nch);
+        {
+            const uint64_t cells = band_cells(rl, ql, bw);
+            count_band_cells(counters, cells, cells);
+        }
         __syncwarp();
         if (lane == 0) {
             uint32_t nc = 0;
@@ -2735,7 +2770,7 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
     ws.prep.reserve(n);
     ws.sizes.reserve(3 * ((size_t)n + 1));
     ws.offs.reserve(3 * ((size_t)n + 1));
-    ws.counters.reserve(24);
+    ws.counters.reserve(28);
     if (n == 0) {
         ws.h_results.clear();
         ws.h_cigar.clear();
@@ -2743,7 +2778,7 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
     }
     uint64_t* sz[3] = {ws.sizes.p, ws.sizes.p + n + 1, ws.sizes.p + 2 * ((size_t)n + 1)};
     uint64_t* of[3] = {ws.offs.p, ws.offs.p + n + 1, ws.offs.p + 2 * ((size_t)n + 1)};
-    SA_CUDA(cudaMemsetAsync(ws.counters.p, 0, 24 * sizeof(uint32_t), st));
+    SA_CUDA(cudaMemsetAsync(ws.counters.p, 0, 28 * sizeof(uint32_t), st));
     kt->begin(KS_PREPARE, st);
     ws.rescue_list.reserve(n);
     k_prepare<<<grid1(n), 256, 0, st>>>(ws.jobs.p, n, seq, off, refs, k, raw_refs, raw_off, ws.results.p, ws.prep.p,
@@ -3008,6 +3043,7 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
                             st));
     if (used) SA_CUDA(cudaMemcpyAsync(ws.h_cigar.data(), ws.raw.p, used * 4, cudaMemcpyDeviceToHost, st));
     SA_CUDA(cudaMemcpyAsync(ws.cells, ws.counters.p + 8, 5 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    SA_CUDA(cudaMemcpyAsync(ws.cells + 5, ws.counters.p + 24, 2 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
     SA_CUDA(cudaStreamSynchronize(st));
     tot[1] = used;
     ws.total_cigar = tot[1];

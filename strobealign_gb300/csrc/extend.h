@@ -53,7 +53,7 @@ struct ExtWorkspace {
     DevBuf<uint32_t> cigar;
     DevBuf<int32_t> hscratch;
     DevBuf<SswTask> tasks;
-    DevBuf<uint32_t> counters;  // [0] n_tasks [1] n_word [2] n_rev_byte [3] n_rev_word [4] n_rescue, u64 cells at [8]
+    DevBuf<uint32_t> counters;  // [0] n_tasks [1] n_word [2] n_rev_byte [3] n_rev_word [4] n_rescue, u64 cells at [8], u64 band cells at [24]
     DevBuf<uint32_t> rescue_list;
     DevBuf<uint32_t> list_word, list_rev_byte, list_rev_word;
     DevBuf<uint32_t> order;  // task order of the fused SSW kernel
@@ -73,7 +73,9 @@ struct ExtWorkspace {
     // tuning (output-invariant): SSW tasks of reads up to wave_qmax nt (at most 192) run
     // on the lane-wavefront kernel, longer ones a warp per task
     uint32_t wave_qmax = 192;
-    uint64_t cells[5] = {0, 0, 0, 0, 0};  // SW cells: canonical, then computed forward byte / word, reverse byte / word
+    // SW cells: canonical, then computed forward byte / word, reverse byte / word; then
+    // banded cells: every pass's, and the final pass's
+    uint64_t cells[7] = {0, 0, 0, 0, 0, 0, 0};
 };
 
 // Runs jobs (already in ws.jobs, n of them) against the reads in nws.seq/nws.off.

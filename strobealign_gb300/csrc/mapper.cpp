@@ -190,7 +190,7 @@ std::shared_ptr<const WaveResults> Mapper::run_wave(const ExtJob* jobs, uint32_t
     launches += run_extension(refs_view_, nws_, idx_->sp.k, sc, nj, ews_, max_qlen, st_, &kt_,
                               anchor_words ? ews_.anchors.p : nullptr, max_anchors);
     d2h_bytes_ += (size_t)nj * sizeof(ExtResult) + ews_.total_cigar * 4;
-    for (int c = 0; c < 5; c++) sw_cells_[c] += ews_.cells[c];
+    for (int c = 0; c < 7; c++) sw_cells_[c] += ews_.cells[c];
     std::swap(w->results, ews_.h_results);
     std::swap(w->cigar, ews_.h_cigar);
     jobs_run_ += nj;
@@ -496,7 +496,7 @@ void Mapper::map_uploaded(sa_output* out) {
     t_ext_ = 0;
     kt_.reset();
     kt_nam_.reset();
-    for (int c = 0; c < 5; c++) sw_cells_[c] = 0;
+    for (int c = 0; c < 7; c++) sw_cells_[c] = 0;
     // chunks (src/main.rs:591-604), cut on the uploaded read offsets (record j's bases
     // are off[rpr * (j + 1)] - off[rpr * j])
     std::vector<ChunkState> chunks;
@@ -675,6 +675,7 @@ void Mapper::map_uploaded(sa_output* out) {
     kt_.collect();
     kt_nam_.collect();
     for (int c = 0; c < 5; c++) stats_.sw_cells[c] = sw_cells_[c];
+    for (int c = 0; c < 2; c++) stats_.band_cells[c] = sw_cells_[5 + c];
     for (int i = 0; i < 16; i++) {
         stats_.kernel_ms[i] = i < KS_COUNT ? kt_.ms[i] + kt_nam_.ms[i] : 0.0;
         stats_.kernel_launches[i] = i < KS_COUNT ? kt_.launches[i] + kt_nam_.launches[i] : 0;

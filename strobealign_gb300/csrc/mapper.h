@@ -97,7 +97,7 @@ class Mapper {
     sa_mapper_stats stats_{};
     double t_ext_ = 0;
     KernelTimers kt_, kt_nam_;
-    uint64_t sw_cells_[5] = {0, 0, 0, 0, 0};
+    uint64_t sw_cells_[7] = {0, 0, 0, 0, 0, 0, 0};  // SW cells, then banded cells
     unsigned policy_threads_ = std::max(1u, std::thread::hardware_concurrency());
     uint64_t wave_min_jobs_ = 32768;
     uint64_t max_wave_jobs_ = 262144;
