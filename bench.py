@@ -568,6 +568,15 @@ def main():
     mapper.set_schedule(overlap=False)
     mapper.map(R1, R2, copy=False)  # warm-up of the plain form
     plain_e2e, plain_h2d, plain_d2h, plain_waves, plain_launches = host_pass(aux)
+    # one more plain map with the stage timers on: in the plain form no NAM part runs
+    # beside the extension waves, so these are each kernel's times alone on the GPU
+    mapper.set_profiling(True)
+    mapper.map(R1, R2, copy=False)
+    st_iso = mapper.stats()
+    mapper.set_profiling(False)
+    kern_iso = {k: [v, int(st_iso["kernel_launches"][k])] for k, v in st_iso["kernel_ms"].items()}
+    cells_iso = {k: int(v) for k, v in st_iso["sw_cells"].items()}
+    counts_iso = {k: int(st_iso[k]) for k in ("n_bases", "n_randstrobes", "n_anchor_total")}
     mapper.set_schedule()
     # served: the same records as a stream of requests (log-uniform 1..100k pairs), each
     # its own chunk stream, through one session with continuous batching
@@ -629,6 +638,8 @@ def main():
     lookup = (parity or {}).get("lookup_sectors")
     roofline, rooflines = roofline_for(dom, kern, cells, peaks, clk.summary(), counts, args.steps, sms, n_reads,
                                        lookup) if dom else (None, {})
+    _, rooflines_iso = roofline_for(dom, kern_iso, cells_iso, peaks, clk.summary(), counts_iso, 1, sms, n_reads,
+                                    lookup) if dom else (None, {})
     reads_gb = int(R1.seq_offsets[-1]) * (2 if R2 is not None else 1) / 1e9
     out = {
         "metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": ws, "steps": args.steps,
@@ -669,6 +680,9 @@ def main():
         "phases_s": {k.replace("seconds_", ""): round(v, 4) for k, v in phases.items()},
         "roofline": roofline,
         "rooflines": rooflines,
+        # the same stages timed in one plain (stage-synchronous) map, each kernel alone on
+        # the GPU: the kernels' own rates, without the NAM stream sharing the SMs
+        "rooflines_isolated": rooflines_iso,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
     }

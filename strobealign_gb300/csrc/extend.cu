@@ -1099,6 +1099,7 @@ __global__ void __launch_bounds__(128, RMAX <= 4 ? 5 : 1) k_ssw(SswTask* tasks, 
 // 16-byte word, laid out [code][word][lane] per warp.
 constexpr int WV_T = 8;      // threads per task
 constexpr int WAVE_NMAX = 24;  // rows per thread: reads up to 8 * 24 = 192 nt
+constexpr int WAVE_NMAX_SHORT = 20;  // reads up to 160 nt: fewer registers, five blocks per SM
 constexpr int WV_SCALE = 8;  // log2 of the score scale (rows < 256)
 
 struct WaveScores {
@@ -1339,7 +1340,7 @@ __device__ __forceinline__ int wave_diag_bound(bool run, const uint8_t* q, int q
 // group of eight threads) and runs the forward byte pass, the forward word pass of the
 // tasks that overflowed, then the reverse passes in each task's mode.
 template <int NMAX>
-__global__ void __launch_bounds__(128, 4) k_ssw_wave(SswTask* tasks, const uint32_t* order, uint32_t n_tasks,
+__global__ void __launch_bounds__(128, NMAX <= 20 ? 5 : 4) k_ssw_wave(SswTask* tasks, const uint32_t* order, uint32_t n_tasks,
                                                       const PrepRec* prep, const uint8_t* arena, AlignScores sc,
                                                       int bias, uint32_t* counters, uint32_t qmax) {
     constexpr int NW = (NMAX + 7) / 8;
@@ -2935,9 +2936,16 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
                 const uint64_t per_block = (uint64_t)wpb * (32 / WV_T);  // tasks per block and round
                 uint64_t wblocks = ((uint64_t)n_tasks + per_block - 1) / per_block;
                 if (wblocks > sm_count() * 16) wblocks = sm_count() * 16;
-                const size_t smem = (size_t)wpb * 5 * ((WAVE_NMAX + 7) / 8) * 32 * sizeof(uint4);
-                k_ssw_wave<WAVE_NMAX><<<(unsigned)wblocks, tpb, smem, st>>>(
-                    ws.tasks.p, ws.order.p, n_tasks, ws.prep.p, ws.arena.p, sc, bias, ws.counters.p, wave_qmax);
+                // the kernel's row arrays sized for the longest read it takes
+                const bool short_reads = std::min<uint32_t>(max_qlen, wave_qmax) <= 8 * WAVE_NMAX_SHORT;
+                const int nmax = short_reads ? WAVE_NMAX_SHORT : WAVE_NMAX;
+                const size_t smem = (size_t)wpb * 5 * ((nmax + 7) / 8) * 32 * sizeof(uint4);
+                if (short_reads)
+                    k_ssw_wave<WAVE_NMAX_SHORT><<<(unsigned)wblocks, tpb, smem, st>>>(
+                        ws.tasks.p, ws.order.p, n_tasks, ws.prep.p, ws.arena.p, sc, bias, ws.counters.p, wave_qmax);
+                else
+                    k_ssw_wave<WAVE_NMAX><<<(unsigned)wblocks, tpb, smem, st>>>(
+                        ws.tasks.p, ws.order.p, n_tasks, ws.prep.p, ws.arena.p, sc, bias, ws.counters.p, wave_qmax);
             }
 #undef SA_SSW
             kt->end(st);
