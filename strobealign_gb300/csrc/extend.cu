@@ -1586,6 +1586,248 @@ __device__ __forceinline__ void count_band_cells(uint32_t* counters, uint64_t co
     }
 }
 
+// banded_sw's traceback (ext/ssw/ssw.c:680-753) by one thread over the direction bits
+// of the last pass: words(row, w0, w1, w2, w3) gives row `row`'s bits for band index k
+// (E opened, F opened, H from the diagonal, E over F).  The library walks a flat
+// (2bw+1) x 3-byte-per-row array, so an index that leaves a row reads the neighbouring
+// row's entries, or 0 where the pass wrote nothing; the walk does the same.  Writes the
+// CIGAR (reversed into order) to c; false when the walk fails or c is too small.
+template <class Words>
+__device__ bool band_trace_thread(Words words, int rl, int ql, int bw, uint32_t* c, uint32_t cap, uint32_t& nc) {
+    const int width_d = 2 * bw + 1;
+    const int64_t dsize = (int64_t)width_d * ql * 3;
+    // the row's four direction words, loaded when the walk enters a row
+    int cached = -1;
+    uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
+    auto dir_of = [&](int row, int k, int w) -> int {
+        const int x = row - bw > 0 ? row - bw : 0;
+        const int end = rl - 1 < row + bw ? rl - 1 : row + bw;
+        if (k > end - x) return 0;  // not written by the pass
+        if (row != cached) {
+            words(row, w0, w1, w2, w3);
+            cached = row;
+        }
+        const int dde = (w0 >> k) & 1 ? 3 : 2;
+        const int ddf = (w1 >> k) & 1 ? 5 : 4;
+        if (w == 0) return dde;
+        if (w == 1) return ddf;
+        return (w2 >> k) & 1 ? 1 : ((w3 >> k) & 1 ? dde : ddf);
+    };
+    int i = ql - 1, j = rl - 1, e = 0, which = 2;
+    char op = 'M', prev = 'M';
+    nc = 0;
+    auto enc = [](int l, char o) -> uint32_t { return ((uint32_t)l << 4) | (o == 'M' ? 0u : o == 'I' ? 1u : 2u); };
+    while (i >= 0 && j > 0) {
+        const int x = i - bw > 0 ? i - bw : 0;
+        const int k = j - x;
+        int d;
+        if (k >= 0 && k < width_d) {
+            d = dir_of(i, k, which);  // the flat index falls in row i
+        } else {
+            // the flat index (row i, band column k) runs into a neighbouring row
+            const int64_t at = (int64_t)width_d * i * 3 + (int64_t)k * 3 + which;
+            if (at < 0 || at >= dsize) return false;
+            const int rem = (int)(at % (3 * width_d));
+            d = dir_of((int)(at / (3 * width_d)), rem / 3, rem % 3);
+        }
+        switch (d) {
+            case 1: --i; --j; which = 2; op = 'M'; break;
+            case 2: --i; which = 0; op = 'I'; break;
+            case 3: --i; which = 2; op = 'I'; break;
+            case 4: --j; which = 1; op = 'D'; break;
+            case 5: --j; which = 2; op = 'D'; break;
+            default: return false;
+        }
+        if (op == prev) ++e;
+        else {
+            if (nc >= cap) return false;
+            c[nc++] = enc(e, prev);
+            prev = op;
+            e = 1;
+        }
+    }
+    if (nc + 2 > cap) return false;
+    if (op == 'M') c[nc++] = enc(e + 1, op);
+    else {
+        c[nc++] = enc(e, op);
+        c[nc++] = enc(1, 'M');
+    }
+    for (uint32_t a = 0, b = nc - 1; a < b; a++, b--) {
+        const uint32_t tmp = c[a];
+        c[a] = c[b];
+        c[b] = tmp;
+    }
+    return true;
+}
+
+// banded_sw's pass (ext/ssw/ssw.c:614-676) for band width BW by one thread.  The
+// library's h_b, e_b and h_c (indices u = 1 .. 2BW+1 for the band's cells, 0 and the
+// edge held at 0) are register arrays: cell j of row i is band index k = j - x
+// (x = max(0, i - BW)), u = k + 1, and the previous row's cell j sits at k + 1 + sh
+// (sh = 1 once the band has started to slide), so every index is a constant of the
+// unrolled loop.  The reference's codes of the band's columns slide along in
+// registers.  The row's direction bits go to rows[2i] (bits k: E opened; 16 + k: F
+// opened) and rows[2i + 1] (bits k: H from the diagonal; 16 + k: E over F) when rows is
+// set.  Returns the maximum; cells counts the band's cells.
+template <int BW>
+__device__ int band_pass_thread(const uint8_t* ref, const uint8_t* read, int rl, int ql, const AlignScores& sc,
+                                uint32_t* rows, uint64_t& cells) {
+    constexpr int K = 2 * BW + 1;  // band cells per row
+    constexpr int W = K + 2;       // the library's width
+    const int gO = sc.gap_open, gE = sc.gap_extend;
+    int hb[W], eb[W], hc[W], rc[K];
+#pragma unroll
+    for (int t = 0; t < W; t++) {
+        hb[t] = 0;
+        eb[t] = 0;
+        hc[t] = 0;
+    }
+    // codes of columns x .. end of row 0
+    const int end0 = rl - 1 < BW ? rl - 1 : BW;
+#pragma unroll
+    for (int k = 0; k < K; k++) rc[k] = k <= end0 ? c_ssw_code[ref[k]] : 4;
+    int mx = 0, prev_end = end0;
+    for (int i = 0; i < ql; i++) {
+        const int x = i - BW > 0 ? i - BW : 0;
+        const int sh = i - BW > 0 ? 1 : 0;  // x - max(0, i - 1 - BW)
+        const int end = rl - 1 < i + BW ? rl - 1 : i + BW;
+        const int n = end - x + 1;
+        if (i > 0) {
+            // slide the column codes to this row's band
+            if (sh) {
+#pragma unroll
+                for (int k = 0; k + 1 < K; k++) rc[k] = rc[k + 1];
+            }
+            if (end > prev_end) {
+                const int code = c_ssw_code[ref[end]];
+#pragma unroll
+                for (int k = 0; k < K; k++)
+                    if (k == n - 1) rc[k] = code;
+            }
+            prev_end = end;
+        }
+        const int edge = end + 1 < W - 1 ? end + 1 : W - 1;
+#pragma unroll
+        for (int t = 1; t < W; t++)
+            if (t == edge) {
+                hb[t] = 0;
+                eb[t] = 0;
+            }
+        hb[0] = eb[0] = hc[0] = 0;
+        const int qcode = c_ssw_code[read[i]];
+        int f = 0;
+        uint32_t d0 = 0, d1 = 0;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            if (k < n) {
+                const int he = sh ? hb[k + 2 < W ? k + 2 : W - 1] : hb[k + 1];
+                const int ee = sh ? eb[k + 2 < W ? k + 2 : W - 1] : eb[k + 1];
+                const int hd = sh ? hb[k + 1] : hb[k];
+                int t1 = i == 0 ? -gO : he - gO;
+                int t2 = i == 0 ? -gE : ee - gE;
+                const int E = t1 > t2 ? t1 : t2;
+                eb[k + 1] = E;
+                d0 |= (uint32_t)(t1 > t2) << k;
+                t1 = hc[k] - gO;
+                t2 = f - gE;
+                f = t1 > t2 ? t1 : t2;
+                d0 |= (uint32_t)(t1 > t2) << (16 + k);
+                const int e1 = E > 0 ? E : 0, f1 = f > 0 ? f : 0;
+                t1 = e1 > f1 ? e1 : f1;
+                t2 = hd + mat_score(rc[k], qcode, sc);
+                const int H = t1 > t2 ? t1 : t2;
+                hc[k + 1] = H;
+                if (H > mx) mx = H;
+                d1 |= (uint32_t)(t1 <= t2) << k;
+                d1 |= (uint32_t)(e1 > f1) << (16 + k);
+            }
+        }
+#pragma unroll
+        for (int t = 1; t < W - 1; t++)
+            if (t <= n) hb[t] = hc[t];
+        cells += (uint64_t)(n > 0 ? n : 0);
+        if (rows) {
+            rows[2 * i] = d0;
+            rows[2 * i + 1] = d1;
+        }
+    }
+    return mx;
+}
+
+constexpr int BAND_THREAD_MAX_BW = 5;  // bands up to 11 cells a thread per task
+
+// banded_sw (ext/ssw/ssw.c:598-769) a thread per task while the band width stays at
+// most BAND_THREAD_MAX_BW (the band of an alignment without indels is 3 cells wide, so
+// a warp per task left most lanes idle).  A task whose doubling goes past that is left
+// for k_band_warp (raw_off stays RAW_FALLBACK), which starts its doubling over.
+__global__ void __launch_bounds__(128) k_band_small(SswTask* tasks, uint32_t n_tasks, const PrepRec* prep,
+                                                    const uint8_t* arena, int32_t* hscratch, AlignScores sc,
+                                                    uint32_t* counters) {
+    uint64_t computed = 0, canonical = 0;
+    for (uint32_t ti = blockIdx.x * blockDim.x + threadIdx.x; ti < n_tasks; ti += gridDim.x * blockDim.x) {
+        SswTask tk = tasks[ti];
+        if (tk.ref_begin1 < 0 || tk.read_begin1 < 0) continue;
+        const PrepRec p = prep[tk.job];
+        const uint8_t* q = arena + p.arena_off + tk.read_begin1;
+        const uint8_t* r = arena + p.arena_off + p.qlen + tk.ref_begin1;
+        const int rl = tk.ref_end1 - tk.ref_begin1 + 1, ql = tk.read_end1 - tk.read_begin1 + 1;
+        const int len = rl > ql ? rl : ql;
+        int bw = (rl > ql ? rl - ql : ql - rl) + 1;
+        if (bw > BAND_THREAD_MAX_BW) continue;
+        // rows in the task's scratch as k_band_warp keeps them, the CIGAR after them
+        uint32_t* rows = reinterpret_cast<uint32_t*>(hscratch + p.h_off);
+        int mx = 0;
+        bool small = true;
+        uint64_t cells = 0;
+        do {
+            if (bw > BAND_THREAD_MAX_BW) {
+                small = false;
+                break;
+            }
+            cells = 0;
+            switch (bw) {
+                case 1: mx = band_pass_thread<1>(r, q, rl, ql, sc, rows, cells); break;
+                case 2: mx = band_pass_thread<2>(r, q, rl, ql, sc, rows, cells); break;
+                case 3: mx = band_pass_thread<3>(r, q, rl, ql, sc, rows, cells); break;
+                case 4: mx = band_pass_thread<4>(r, q, rl, ql, sc, rows, cells); break;
+                default: mx = band_pass_thread<5>(r, q, rl, ql, sc, rows, cells); break;
+            }
+            computed += cells;
+            bw *= 2;
+        } while (mx < tk.score1 && bw <= len);
+        if (!small) continue;  // raw_off stays RAW_FALLBACK: k_band_warp takes it
+        bw /= 2;
+        canonical += cells;
+        uint32_t* c = rows + 4 * (size_t)ql;
+        uint32_t nc = 0;
+        const bool ok = band_trace_thread(
+            [&](int row, uint32_t& w0, uint32_t& w1, uint32_t& w2, uint32_t& w3) {
+                const uint32_t a = rows[2 * row], b = rows[2 * row + 1];
+                w0 = a & 0xffffu;
+                w1 = a >> 16;
+                w2 = b & 0xffffu;
+                w3 = b >> 16;
+            },
+            rl, ql, bw, c, (uint32_t)(rl + ql + 4), nc);
+        tk.band_width = bw;
+        if (!ok) {
+            tk.flag = 1;
+            tk.raw_len = 0;
+        } else {
+            tk.raw_len = nc;
+        }
+        tk.raw_off = (uint64_t)p.h_off + 4 * (uint64_t)ql;
+        tasks[ti] = tk;
+    }
+    // the cells of this thread's tasks, one atomic per warp
+    unsigned long long cs = computed, cn = canonical;
+    for (int d = 16; d > 0; d >>= 1) {
+        cs += __shfl_xor_sync(FULLM, cs, d);
+        cn += __shfl_xor_sync(FULLM, cn, d);
+    }
+    count_band_cells(counters, cs, cn);
+}
+
 __global__ void __launch_bounds__(128) k_band_warp(SswTask* tasks, uint32_t n_tasks, const PrepRec* prep,
                                                    const uint8_t* arena, int32_t* hscratch, AlignScores sc,
                                                    uint32_t* counters) {
@@ -1596,7 +1838,8 @@ __global__ void __launch_bounds__(128) k_band_warp(SswTask* tasks, uint32_t n_ta
         ti = __shfl_sync(FULLM, ti, 0);
         if (ti >= n_tasks) break;
         SswTask tk = tasks[ti];
-        if (tk.ref_begin1 < 0 || tk.read_begin1 < 0) continue;
+        // skip the tasks k_band_small finished
+        if (tk.ref_begin1 < 0 || tk.read_begin1 < 0 || tk.raw_off != RAW_FALLBACK) continue;
         const PrepRec p = prep[tk.job];
         const uint8_t* q = arena + p.arena_off;
         const uint8_t* r = q + p.qlen;
@@ -1627,94 +1870,23 @@ __global__ void __launch_bounds__(128) k_band_warp(SswTask* tasks, uint32_t n_ta
         count_band_cells(counters, computed, band_cells(rl, ql, bw));
         __syncwarp();
         if (lane == 0) {
-            // traceback (ext/ssw/ssw.c:680-753) over the flat direction array of
-            // (2bw+1) x 3 bytes per row
+            // traceback over the four ballot words per row the passes recorded
             uint32_t* c = rowbits + 4 * (size_t)ql;
-            const int width_d = 2 * bw + 1;
-            const int64_t dsize = (int64_t)width_d * ql * 3;
-            // the row's four direction words, loaded when the walk enters a row
-            int cached = -1;
-            uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
-            auto dir_of = [&](int row, int k, int w) -> int {
-                const int x = row - bw > 0 ? row - bw : 0;
-                const int end = rl - 1 < row + bw ? rl - 1 : row + bw;
-                if (k > end - x) return 0;  // not written by the pass
-                if (row != cached) {
+            uint32_t nc = 0;
+            const bool ok = band_trace_thread(
+                [&](int row, uint32_t& w0, uint32_t& w1, uint32_t& w2, uint32_t& w3) {
                     const uint32_t* rb = rowbits + 4 * (size_t)row;
                     w0 = rb[0];
                     w1 = rb[1];
                     w2 = rb[2];
                     w3 = rb[3];
-                    cached = row;
-                }
-                const int dde = (w0 >> k) & 1 ? 3 : 2;
-                const int ddf = (w1 >> k) & 1 ? 5 : 4;
-                if (w == 0) return dde;
-                if (w == 1) return ddf;
-                return (w2 >> k) & 1 ? 1 : ((w3 >> k) & 1 ? dde : ddf);
-            };
-            int i = ql - 1, j = rl - 1, e = 0, which = 2;
-            char op = 'M', prev = 'M';
-            uint32_t nc = 0;
-            const uint32_t cap = (uint32_t)(rl + ql + 4);
-            bool fail = false;
-            auto enc = [](int l, char o) -> uint32_t {
-                return ((uint32_t)l << 4) | (o == 'M' ? 0u : o == 'I' ? 1u : 2u);
-            };
-            while (i >= 0 && j > 0) {
-                const int x = i - bw > 0 ? i - bw : 0;
-                const int k = j - x;
-                int d;
-                if (k >= 0 && k < width_d) {
-                    d = dir_of(i, k, which);  // the flat index falls in row i
-                } else {
-                    // the flat index (row i, band column k) runs into a neighbouring row
-                    const int64_t at = (int64_t)width_d * i * 3 + (int64_t)k * 3 + which;
-                    if (at < 0 || at >= dsize) {
-                        fail = true;
-                        break;
-                    }
-                    const int rem = (int)(at % (3 * width_d));
-                    d = dir_of((int)(at / (3 * width_d)), rem / 3, rem % 3);
-                }
-                switch (d) {
-                    case 1: --i; --j; which = 2; op = 'M'; break;
-                    case 2: --i; which = 0; op = 'I'; break;
-                    case 3: --i; which = 2; op = 'I'; break;
-                    case 4: --j; which = 1; op = 'D'; break;
-                    case 5: --j; which = 2; op = 'D'; break;
-                    default: fail = true;
-                }
-                if (fail) break;
-                if (op == prev) ++e;
-                else {
-                    if (nc >= cap) {
-                        fail = true;
-                        break;
-                    }
-                    c[nc++] = enc(e, prev);
-                    prev = op;
-                    e = 1;
-                }
-            }
-            if (!fail) {
-                if (nc + 2 > cap) fail = true;
-                else if (op == 'M') c[nc++] = enc(e + 1, op);
-                else {
-                    c[nc++] = enc(e, op);
-                    c[nc++] = enc(1, 'M');
-                }
-            }
+                },
+                rl, ql, bw, c, (uint32_t)(rl + ql + 4), nc);
             tk.band_width = bw;
-            if (fail) {
+            if (!ok) {
                 tk.flag = 1;
                 tk.raw_len = 0;
             } else {
-                for (uint32_t a = 0, b = nc - 1; a < b; a++, b--) {
-                    const uint32_t tmp = c[a];
-                    c[a] = c[b];
-                    c[b] = tmp;
-                }
                 tk.raw_len = nc;
             }
             tk.raw_off = (uint64_t)p.h_off + 4 * (uint64_t)ql;
@@ -2972,6 +3144,10 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
             kt->begin(KS_BAND, st);
             uint64_t blocks = ((uint64_t)n_tasks + 3) / 4;
             if (blocks > sm_count() * 16) blocks = sm_count() * 16;
+            uint64_t tblocks = ((uint64_t)n_tasks + 127) / 128;
+            if (tblocks > sm_count() * 16) tblocks = sm_count() * 16;
+            k_band_small<<<(unsigned)tblocks, 128, 0, st>>>(ws.tasks.p, n_tasks, ws.prep.p, ws.arena.p,
+                                                             ws.hscratch.p, sc, ws.counters.p);
             k_band_warp<<<(unsigned)blocks, 128, 0, st>>>(ws.tasks.p, n_tasks, ws.prep.p, ws.arena.p, ws.hscratch.p,
                                                           sc, ws.counters.p);
             kt->end(st);

@@ -3,8 +3,10 @@
 #pragma once
 #include "host_state.h"
 
+#include <atomic>
 #include <memory>
 #include <string>
+#include <string_view>
 #include <vector>
 
 namespace sa {
@@ -25,10 +27,11 @@ class ByteSource {
 
   private:
     size_t read_file(char* dst, size_t n);
+    size_t inflate_some(char* dst, size_t n);  // gzip: the next decoded bytes, 0 at the end
     std::string path_;
     int fd_ = -1;
     bool own_fd_ = false;
-    uint64_t raw_ = 0;
+    std::atomic<uint64_t> raw_{0};
     struct Gz;
     std::unique_ptr<Gz> gz_;
 };
@@ -37,9 +40,10 @@ class ByteSource {
 class LineReader {
   public:
     explicit LineReader(const std::string& path);
-    // appends the next line, with its '\n' when it has one, to out; returns the bytes
-    // appended, 0 at the end of the input
-    size_t read_line(std::string& out);
+    // the next line without its '\n' as a view that stays valid until the next call;
+    // newline tells whether the line ended with '\n' (not at the end of the input);
+    // false at the end of the input
+    bool next(std::string_view& line, bool& newline);
     int peek();  // the next byte, -1 at the end
     const ByteSource& source() const { return src_; }
 
@@ -49,6 +53,7 @@ class LineReader {
     std::vector<char> buf_;
     size_t pos_ = 0, end_ = 0;
     bool eof_ = false;
+    std::string spill_;  // a line that crosses the end of the buffer
 };
 
 // Incremental read parser: FASTA when the first byte is '>' (src/io/reads.rs:121-132),
@@ -66,9 +71,8 @@ class ReadParser {
   private:
     LineReader in_;
     bool fasta_ = false;
-    std::string line_, header_;  // FASTA: the next record's header line, read ahead
+    std::string header_;  // FASTA: the next record's header line, read ahead
     bool have_header_ = false;
-    std::string name_, comment_, seq_, qual_;
 };
 
 // An empty store (offset arrays holding their leading 0)

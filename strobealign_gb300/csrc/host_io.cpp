@@ -8,10 +8,15 @@
 #include <fcntl.h>
 #include <unistd.h>
 
+#include <algorithm>
 #include <cerrno>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
+#include <exception>
 #include <mutex>
+#include <thread>
 
 namespace sa {
 
@@ -74,11 +79,31 @@ bool ends_with(const std::string& s, const char* suffix) {
 }
 }  // namespace
 
+// gzip decoding runs on a thread of its own, a few blocks ahead of the reader, so that
+// inflating and parsing overlap
 struct ByteSource::Gz {
     ZStream zs{};
     std::vector<unsigned char> in;
     bool input_end = false, member_done = false, any_input = false, open = false;
+    // decoded blocks handed to read(): at most kAhead queued
+    static constexpr size_t kBlock = (size_t)4 << 20, kAhead = 4;
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<std::vector<char>> ready, spare;
+    bool done = false, stop = false;
+    std::exception_ptr err;
+    std::vector<char> cur;  // the block read() is taking bytes from
+    size_t cur_pos = 0;
     ~Gz() {
+        if (worker.joinable()) {
+            {
+                std::lock_guard<std::mutex> g(mu);
+                stop = true;
+            }
+            cv.notify_all();
+            worker.join();
+        }
         if (open) zlib().inflate_end(&zs);
     }
 };
@@ -126,6 +151,76 @@ size_t ByteSource::read_file(char* dst, size_t n) {
 
 size_t ByteSource::read(char* dst, size_t n) {
     if (!gz_) return read_file(dst, n);
+    Gz& g = *gz_;
+    if (!g.worker.joinable() && !g.done) {
+        g.worker = std::thread([this] {
+            Gz& w = *gz_;
+            try {
+                for (;;) {
+                    std::vector<char> blk;
+                    {
+                        std::unique_lock<std::mutex> l(w.mu);
+                        w.cv.wait(l, [&] { return w.stop || w.ready.size() < Gz::kAhead; });
+                        if (w.stop) return;
+                        if (!w.spare.empty()) {
+                            blk.swap(w.spare.front());
+                            w.spare.pop_front();
+                        }
+                    }
+                    blk.resize(Gz::kBlock);
+                    size_t got = 0;
+                    while (got < blk.size()) {
+                        const size_t k = inflate_some(blk.data() + got, blk.size() - got);
+                        if (k == 0) break;
+                        got += k;
+                    }
+                    blk.resize(got);
+                    std::lock_guard<std::mutex> l(w.mu);
+                    if (got) w.ready.push_back(std::move(blk));
+                    if (got < Gz::kBlock) {
+                        w.done = true;
+                        w.cv.notify_all();
+                        return;
+                    }
+                    w.cv.notify_all();
+                }
+            } catch (...) {
+                std::lock_guard<std::mutex> l(w.mu);
+                w.err = std::current_exception();
+                w.done = true;
+                w.cv.notify_all();
+            }
+        });
+    }
+    size_t out = 0;
+    while (out < n) {
+        if (g.cur_pos >= g.cur.size()) {
+            std::unique_lock<std::mutex> l(g.mu);
+            if (!g.cur.empty()) {
+                g.cur.clear();
+                g.spare.push_back(std::move(g.cur));
+                g.cur = std::vector<char>();
+            }
+            g.cur_pos = 0;
+            g.cv.wait(l, [&] { return !g.ready.empty() || g.done; });
+            if (g.ready.empty()) {
+                if (g.err) std::rethrow_exception(g.err);
+                break;  // the end of the input
+            }
+            g.cur.swap(g.ready.front());
+            g.ready.pop_front();
+            g.cv.notify_all();
+        }
+        const size_t take = std::min(n - out, g.cur.size() - g.cur_pos);
+        std::memcpy(dst + out, g.cur.data() + g.cur_pos, take);
+        g.cur_pos += take;
+        out += take;
+        if (out) break;  // hand back what is there
+    }
+    return out;
+}
+
+size_t ByteSource::inflate_some(char* dst, size_t n) {
     Gz& g = *gz_;
     const Zlib& z = zlib();
     if (n > ((size_t)1 << 30)) n = (size_t)1 << 30;
@@ -179,22 +274,37 @@ int LineReader::peek() {
     return (unsigned char)buf_[pos_];
 }
 
-size_t LineReader::read_line(std::string& out) {
-    size_t total = 0;
-    for (;;) {
-        if (pos_ >= end_ && !fill()) return total;
-        const char* b = buf_.data() + pos_;
-        const size_t avail = end_ - pos_;
-        const char* nl = static_cast<const char*>(std::memchr(b, '\n', avail));
-        const size_t take = nl ? (size_t)(nl - b) + 1 : avail;
-        out.append(b, take);
-        pos_ += take;
-        total += take;
-        if (nl) return total;
+bool LineReader::next(std::string_view& line, bool& newline) {
+    if (pos_ >= end_ && !fill()) return false;
+    const char* b = buf_.data() + pos_;
+    const char* nl = static_cast<const char*>(std::memchr(b, '\n', end_ - pos_));
+    if (nl) {
+        line = std::string_view(b, (size_t)(nl - b));
+        pos_ += line.size() + 1;
+        newline = true;
+        return true;
     }
+    // the line runs past the buffer: gather it
+    spill_.assign(b, end_ - pos_);
+    pos_ = end_;
+    newline = false;
+    while (fill()) {
+        const char* c = buf_.data() + pos_;
+        const char* n2 = static_cast<const char*>(std::memchr(c, '\n', end_ - pos_));
+        const size_t take = n2 ? (size_t)(n2 - c) : end_ - pos_;
+        spill_.append(c, take);
+        pos_ += take;
+        if (n2) {
+            pos_++;
+            newline = true;
+            break;
+        }
+    }
+    line = spill_;
+    return true;
 }
 
-static std::string trim_end(const std::string& s) {
+static std::string_view trim_end_view(std::string_view s) {
     size_t e = s.size();
     while (e > 0 && (s[e - 1] == ' ' || s[e - 1] == '\t' || s[e - 1] == '\n' || s[e - 1] == '\r' ||
                      s[e - 1] == '\f' || s[e - 1] == '\v'))
@@ -202,12 +312,14 @@ static std::string trim_end(const std::string& s) {
     return s.substr(0, e);
 }
 
-static void split_header(const std::string& h, std::string& name, std::string& comment, bool& has_comment) {
-    std::string t = trim_end(h);
-    size_t p = t.find_first_of(" \t");
-    if (p == std::string::npos) {
+// split_header on a view: name up to the first blank, the comment after it
+static void split_header_view(std::string_view h, std::string_view& name, std::string_view& comment,
+                              bool& has_comment) {
+    const std::string_view t = trim_end_view(h);
+    const size_t p = t.find_first_of(" \t");
+    if (p == std::string_view::npos) {
         name = t;
-        comment.clear();
+        comment = std::string_view();
         has_comment = false;
     } else {
         name = t.substr(0, p);
@@ -249,23 +361,21 @@ static void validate_names(const std::vector<Contig>& cs) {
 
 void load_fasta(const std::string& path, std::vector<Contig>& out) {
     LineReader f(path);
-    std::string line;
-    bool have = false;
+    std::string_view line;
+    bool nl = false, have = false;
     Contig cur;
-    for (;;) {
-        line.clear();
-        if (!f.read_line(line)) break;
-        if (line[0] == '>') {
+    while (f.next(line, nl)) {
+        if (!line.empty() && line[0] == '>') {
             if (have) out.push_back(std::move(cur));
             cur = Contig();
-            std::string c;
+            std::string_view name, c;
             bool hc;
-            split_header(line.substr(1), cur.name, c, hc);
+            split_header_view(line.substr(1), name, c, hc);
+            cur.name.assign(name);
             have = true;
         } else if (have) {
-            std::string t = trim_end(line);
-            for (char ch : t) cur.push((uint8_t)ch);
-        } else if (!trim_end(line).empty()) {
+            for (char ch : trim_end_view(line)) cur.push((uint8_t)ch);
+        } else if (!trim_end_view(line).empty()) {
             throw Error(SA_ERR_FORMAT, "FASTA file must start with '>'");
         }
     }
@@ -293,11 +403,6 @@ uint32_t pick_bits(const std::vector<Contig>& cs, const SeedParams& p) {
     if (lg < 9) lg = 9;
     if (lg > 32) lg = 32;
     return lg - 1;
-}
-
-static void push_str(std::string& buf, std::vector<uint64_t>& off, const std::string& s) {
-    buf += s;
-    off.push_back(buf.size());
 }
 
 void reset_read_store(ReadStore& rs, bool has_qual) {
@@ -335,40 +440,63 @@ void split_read_store(ReadStore& rs, size_t from, ReadStore& tail) {
 
 ReadParser::ReadParser(const std::string& path) : in_(path) {
     fasta_ = in_.peek() == '>';
-    if (fasta_) have_header_ = in_.read_line(header_) > 0;
+    if (fasta_) {
+        std::string_view h;
+        bool nl;
+        have_header_ = in_.next(h, nl);
+        if (have_header_) header_.assign(h);
+    }
 }
 
-// Vec::pop of the line end, then a '\r' (src/io/fastq.rs:62-66)
-static void drop_line_end(std::string& s) {
-    if (!s.empty()) s.pop_back();
-    if (!s.empty() && s.back() == '\r') s.pop_back();
+namespace {
+struct UpperTable {
+    char t[256];
+    UpperTable() {
+        for (int c = 0; c < 256; c++) t[c] = (char)toupper(c);
+    }
+};
+const UpperTable kUpper;
+
+// appends s upper-cased to out
+void append_upper(std::string& out, std::string_view s) {
+    const size_t o = out.size();
+    out.append(s);
+    char* p = &out[o];
+    for (size_t i = 0; i < s.size(); i++) p[i] = kUpper.t[(unsigned char)p[i]];
 }
+
+// the sequence / quality line as read_until and Vec::pop leave it (src/io/fastq.rs:61-76):
+// the last byte goes (the '\n', or a real byte at the end of the input), then a '\r'
+std::string_view fastq_line(std::string_view l, bool newline) {
+    if (!newline && !l.empty()) l.remove_suffix(1);
+    if (!l.empty() && l.back() == '\r') l.remove_suffix(1);
+    return l;
+}
+}  // namespace
 
 size_t ReadParser::parse(ReadStore& rs, size_t max_records) {
     size_t n = 0;
+    std::string_view line, name, comment;
+    bool nl = false, hc = false;
     if (fasta_) {
         rs.has_qual = false;
         while (n < max_records && have_header_) {
-            bool hc = false;
-            split_header(header_.substr(1), name_, comment_, hc);
-            seq_.clear();
+            split_header_view(std::string_view(header_).substr(1), name, comment, hc);
+            rs.names.append(name);
+            rs.name_off.push_back(rs.names.size());
+            rs.comments.append(hc ? comment : std::string_view());
+            rs.comment_off.push_back(rs.comments.size());
+            rs.has_comment.push_back(hc);
             have_header_ = false;
-            for (;;) {
-                line_.clear();
-                if (!in_.read_line(line_)) break;
-                if (line_[0] == '>') {
-                    header_.swap(line_);
+            while (in_.next(line, nl)) {
+                if (!line.empty() && line[0] == '>') {
+                    header_.assign(line);
                     have_header_ = true;
                     break;
                 }
-                std::string t = trim_end(line_);
-                for (char& c : t) c = (char)toupper((unsigned char)c);
-                seq_ += t;
+                append_upper(rs.seq, trim_end_view(line));
             }
-            push_str(rs.seq, rs.seq_off, seq_);
-            push_str(rs.names, rs.name_off, name_);
-            push_str(rs.comments, rs.comment_off, hc ? comment_ : std::string());
-            rs.has_comment.push_back(hc);
+            rs.seq_off.push_back(rs.seq.size());
             n++;
         }
         return n;
@@ -376,31 +504,40 @@ size_t ReadParser::parse(ReadStore& rs, size_t max_records) {
     rs.has_qual = true;
     rs.qual_off_unused = 0;
     while (n < max_records) {
-        line_.clear();
-        if (!in_.read_line(line_)) break;
-        if (line_[0] != '@') throw Error(SA_ERR_FORMAT, "FASTQ record must start with '@'");
-        bool hc = false;
-        split_header(line_.substr(1), name_, comment_, hc);
-        if (name_.empty()) throw Error(SA_ERR_FORMAT, "Record identifier is empty");
-        if (name_.size() >= 2 &&
-            (name_.compare(name_.size() - 2, 2, "/1") == 0 || name_.compare(name_.size() - 2, 2, "/2") == 0))
-            name_.resize(name_.size() - 2);
-        seq_.clear();
-        in_.read_line(seq_);
-        drop_line_end(seq_);
-        line_.clear();
-        in_.read_line(line_);
-        qual_.clear();
-        in_.read_line(qual_);
-        drop_line_end(qual_);
-        if (seq_.size() != qual_.size())
-            throw Error(SA_ERR_FORMAT, "Found " + std::to_string(seq_.size()) + " nucleotides but " +
-                                           std::to_string(qual_.size()) + " quality values in record '" + name_ + "'");
-        for (char& c : seq_) c = (char)toupper((unsigned char)c);
-        push_str(rs.seq, rs.seq_off, seq_);
-        rs.qual += qual_;
-        push_str(rs.names, rs.name_off, name_);
-        push_str(rs.comments, rs.comment_off, hc ? comment_ : std::string());
+        if (!in_.next(line, nl)) break;
+        if (line.empty() || line[0] != '@') throw Error(SA_ERR_FORMAT, "FASTQ record must start with '@'");
+        split_header_view(line.substr(1), name, comment, hc);
+        if (name.empty()) throw Error(SA_ERR_FORMAT, "Record identifier is empty");
+        if (name.size() >= 2 && name[name.size() - 2] == '/' && (name.back() == '1' || name.back() == '2'))
+            name.remove_suffix(2);
+        // the views die with the next line: keep the name now
+        const size_t name0 = rs.names.size(), comment0 = rs.comments.size();
+        rs.names.append(name);
+        rs.comments.append(hc ? comment : std::string_view());
+        std::string_view seq;
+        if (in_.next(line, nl)) seq = fastq_line(line, nl);
+        else seq = std::string_view();
+        const size_t seq0 = rs.seq.size();
+        append_upper(rs.seq, seq);
+        const size_t L = rs.seq.size() - seq0;
+        std::string_view plus;
+        bool nl2;
+        in_.next(plus, nl2);
+        std::string_view qual;
+        if (in_.next(line, nl)) qual = fastq_line(line, nl);
+        else qual = std::string_view();
+        if (L != qual.size()) {
+            const std::string nm = rs.names.substr(name0);
+            rs.names.resize(name0);
+            rs.comments.resize(comment0);
+            rs.seq.resize(seq0);
+            throw Error(SA_ERR_FORMAT, "Found " + std::to_string(L) + " nucleotides but " +
+                                           std::to_string(qual.size()) + " quality values in record '" + nm + "'");
+        }
+        rs.qual.append(qual);
+        rs.seq_off.push_back(rs.seq.size());
+        rs.name_off.push_back(rs.names.size());
+        rs.comment_off.push_back(rs.comments.size());
         rs.has_comment.push_back(hc);
         n++;
     }

@@ -144,6 +144,20 @@ StreamResult map_files(Mapper& m, const std::string& reads1, const std::string* 
             auto pend = std::make_unique<InBatch>();
             reset_read_store(pend->r1, !p1->fasta());
             if (p2) reset_read_store(pend->r2, !p2->fasta());
+            // room for a batch up front: the stores then grow without copying
+            const uint64_t per_file = (p2 ? batch_bases / 2 : batch_bases) + (batch_bases >> 4);
+            auto reserve = [&](ReadStore& rs, size_t records) {
+                rs.seq.reserve(per_file);
+                if (rs.has_qual) rs.qual.reserve(per_file);
+                rs.seq_off.reserve(records + 1);
+                rs.name_off.reserve(records + 1);
+                rs.comment_off.reserve(records + 1);
+                rs.has_comment.reserve(records);
+                rs.names.reserve(records * 16);
+            };
+            size_t rec_est = (size_t)std::min<uint64_t>(per_file / 100 + 1024, (uint64_t)1 << 24);
+            reserve(pend->r1, rec_est);
+            if (p2) reserve(pend->r2, rec_est);
             bool at_end = false;
             while (true) {
                 // parse until the pending records hold a batch's bases and one whole chunk
@@ -197,6 +211,9 @@ StreamResult map_files(Mapper& m, const std::string& reads1, const std::string* 
                 auto next = std::make_unique<InBatch>();
                 split_read_store(pend->r1, cut, next->r1);
                 if (p2) split_read_store(pend->r2, cut, next->r2);
+                rec_est = std::max<size_t>(rec_est, n + n / 8);
+                reserve(next->r1, rec_est);
+                if (p2) reserve(next->r2, rec_est);
                 if (!inq.push(std::move(pend))) break;
                 pend = std::move(next);
                 if (at_end && read_store_size(pend->r1) == 0) break;
