@@ -40,16 +40,6 @@ __device__ __forceinline__ uint8_t read_char(const uint8_t* s, uint32_t L, uint3
     return rc ? c_comp[s[L - 1 - i]] : s[i];
 }
 
-// Nam::is_consistent (src/nam.rs:49-69) for a NAM in the given orientation
-__device__ bool nam_consistent(const DevRefs& R, const uint8_t* s, uint32_t L, uint32_t ref_id, uint32_t rs,
-                               uint32_t re, uint32_t qs, uint32_t qe, bool rc, uint32_t k) {
-    for (uint32_t i = 0; i < k; i++)
-        if (ref_base(R, ref_id, rs + i) != read_char(s, L, qs + i, rc)) return false;
-    for (uint32_t i = 0; i < k; i++)
-        if (ref_base(R, ref_id, re - k + i) != read_char(s, L, qe - k + i, rc)) return false;
-    return true;
-}
-
 // has_shared_substring (src/mapper.rs:1157-1168), warp per rescue job: the
 // window's substrings of length 2k/3 go into a shared-memory hash set (2-bit
 // codes, the window read straight from the packed reference), then every read
@@ -142,12 +132,42 @@ __global__ void __launch_bounds__(64) k_rescue_filter(const uint32_t* __restrict
     }
 }
 
+// Nam::is_consistent (src/nam.rs:49-69) by a warp: lane i < k compares base i of both
+// ends (k < 32)
+__device__ __forceinline__ bool warp_nam_consistent(const DevRefs& R, const uint8_t* s, uint32_t L, uint32_t ref_id,
+                                                    uint32_t rs, uint32_t re, uint32_t qs, uint32_t qe, bool rc,
+                                                    uint32_t k) {
+    const uint32_t lane = threadIdx.x & 31;
+    bool ok = true;
+    if (lane < k) {
+        ok = ref_base(R, ref_id, rs + lane) == read_char(s, L, qs + lane, rc) &&
+             ref_base(R, ref_id, re - k + lane) == read_char(s, L, qe - k + lane, rc);
+    }
+    return __all_sync(FULLM, ok);
+}
+
+// Mismatches of the read against the reference from ref_start, by a warp
+__device__ __forceinline__ uint32_t warp_hamming(const DevRefs& R, const uint8_t* s, uint32_t L, uint32_t ref_id,
+                                                 uint32_t ref_start, bool rc) {
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t hd = 0;
+    for (uint32_t c = 0; c < L; c += 32) {
+        const uint32_t i = c + lane;
+        const bool mm = i < L && ref_base(R, ref_id, ref_start + i) != read_char(s, L, i, rc);
+        hd += __popc(__ballot_sync(FULLM, mm));
+    }
+    return hd;
+}
+
+// A warp per job (all lanes hold the job; the base comparisons are spread over them)
 __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict__ seq,
                           const uint64_t* __restrict__ off, DevRefs R, uint32_t k, const uint8_t* raw_refs,
                           const uint64_t* raw_off, ExtResult* res, PrepRec* prep, uint64_t* sz_arena,
                           uint64_t* sz_cigar, uint64_t* sz_h, uint32_t* rescue_list, uint32_t* n_rescue,
                           uint32_t* max_pw_window) {
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) / 32; t < n; t += nwarps) {
         ExtJob jb = jobs[t];
         const uint8_t* s = seq + off[jb.read];
         const uint32_t L = (uint32_t)(off[jb.read + 1] - off[jb.read]);
@@ -161,11 +181,11 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
         if (jb.kind == JOB_EXTEND_FAST || jb.kind == JOB_EXTEND_FULL) {
             uint32_t qs = jb.query_start, qe = jb.query_end;
             bool rc = jb.is_revcomp;
-            bool cons = nam_consistent(R, s, L, jb.ref_id, jb.ref_start, jb.ref_end, qs, qe, rc, k);
+            bool cons = warp_nam_consistent(R, s, L, jb.ref_id, jb.ref_start, jb.ref_end, qs, qe, rc, k);
             bool flipped = false;
             if (!cons && jb.kind == JOB_EXTEND_FULL) {
                 uint32_t q2s = L - qe, q2e = L - qs;
-                if (nam_consistent(R, s, L, jb.ref_id, jb.ref_start, jb.ref_end, q2s, q2e, !rc, k)) {
+                if (warp_nam_consistent(R, s, L, jb.ref_id, jb.ref_start, jb.ref_end, q2s, q2e, !rc, k)) {
                     rc = !rc;
                     qs = q2s;
                     qe = q2e;
@@ -186,8 +206,7 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
             uint32_t pre = (uint32_t)(pre64 < clen ? pre64 : clen);
             bool hamming = false;
             if ((uint64_t)prs + L == pre && cons) {
-                uint32_t hd = 0;
-                for (uint32_t i = 0; i < L; i++) hd += ref_base(R, jb.ref_id, prs + i) != read_char(s, L, i, rc);
+                const uint32_t hd = warp_hamming(R, s, L, jb.ref_id, prs, rc);
                 if (__fdiv_rn(__uint2float_rn(hd), __uint2float_rn(L)) < 0.05f) hamming = true;
             }
             if (hamming) {
@@ -217,7 +236,7 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
                     p.wstart = ds;
                     p.wlen = de > ds ? (uint32_t)(de - ds) : 0;
                     p.type = (cons && jb.anc_n > 0 && L > 0) ? 3 : 0;
-                    if (p.type == 3) atomicMax(max_pw_window, p.wlen);
+                    if (p.type == 3 && lane == 0) atomicMax(max_pw_window, p.wlen);
                 }
             }
         } else if (jb.kind == JOB_RESCUE) {
@@ -229,7 +248,7 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
             p.wlen = jb.ref_end - jb.ref_start;
             // extended only if has_shared_substring holds (k_rescue_filter)
             p.type = (p.wlen <= 2000 && L > 0) ? 2 : 0;
-            if (p.type == 2) rescue_list[atomicAdd(n_rescue, 1u)] = t;
+            if (p.type == 2 && lane == 0) rescue_list[atomicAdd(n_rescue, 1u)] = t;
         } else {  // JOB_ALIGN: raw reference bytes
             p.rc = 0;
             p.wstart = 0;
@@ -249,11 +268,13 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
             hs = 3 * (2 * len + 8);
         }
         p.cigar_cap = (uint32_t)cap;
-        res[t] = r;
-        prep[t] = p;
-        sz_arena[t] = ab;
-        sz_cigar[t] = cap;
-        sz_h[t] = hs;
+        if (lane == 0) {
+            res[t] = r;
+            prep[t] = p;
+            sz_arena[t] = ab;
+            sz_cigar[t] = cap;
+            sz_h[t] = hs;
+        }
     }
 }
 
@@ -320,62 +341,111 @@ __device__ __forceinline__ uint32_t hamming_cigar(EQ eq, uint32_t bs, uint32_t b
     return mm;
 }
 
-// Thread per job: the Hamming path (hamming_align, src/aligner.rs:181-259), or the
-// SSW / piecewise job's query and reference window bytes copied into the arena.
-__global__ void k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict__ seq, const uint64_t* __restrict__ off,
-                       DevRefs R, const uint8_t* raw_refs, const uint64_t* raw_off, AlignScores sc, PrepRec* prep,
-                       const uint64_t* off_arena, const uint64_t* off_cigar, const uint64_t* off_h, uint8_t* arena,
-                       uint32_t* cigar, ExtResult* res, SswTask* tasks, uint32_t* counters, uint32_t* pw_list) {
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+// The =/X CIGAR of [bs, be) from a match bit array (hamming_align, src/aligner.rs:233-248),
+// a run of equal bits at a time; returns the mismatches.
+__device__ __forceinline__ uint32_t hamming_cigar_bits(const uint32_t* bits, uint32_t bs, uint32_t be, CigarWriter& w) {
+    uint32_t mm = 0;
+    uint32_t i = bs;
+    while (i < be) {
+        const bool e = (bits[i >> 5] >> (i & 31)) & 1;
+        // the end of the run of e starting at i
+        uint32_t j = i;
+        for (;;) {
+            const uint32_t word = e ? ~bits[j >> 5] : bits[j >> 5];
+            const uint32_t m = word & (0xffffffffu << (j & 31));
+            if (m) {
+                j = (j & ~31u) + (uint32_t)(__ffs(m) - 1);
+                break;
+            }
+            j = (j & ~31u) + 32;
+            if (j >= be) break;
+        }
+        if (j > be) j = be;
+        const uint32_t len = j - i;
+        if (!e) mm += len;
+        w.push(e ? 7u : 8u, len);
+        i = j;
+    }
+    w.finish();
+    return mm;
+}
+
+// A warp per job: the Hamming path (hamming_align, src/aligner.rs:181-259) from a match
+// bit array the lanes build (32 bases per ballot), or the SSW / piecewise job's query
+// and reference window bytes copied into the arena by all lanes.
+constexpr uint32_t FILL_WARPS = 8;
+__global__ void __launch_bounds__(32 * FILL_WARPS) k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict__ seq,
+                                                          const uint64_t* __restrict__ off, DevRefs R,
+                                                          const uint8_t* raw_refs, const uint64_t* raw_off,
+                                                          AlignScores sc, PrepRec* prep, const uint64_t* off_arena,
+                                                          const uint64_t* off_cigar, const uint64_t* off_h,
+                                                          uint8_t* arena, uint32_t* cigar, ExtResult* res,
+                                                          SswTask* tasks, uint32_t* counters, uint32_t* pw_list) {
+    __shared__ uint32_t bits_s[FILL_WARPS][MAX_READ_LEN / 32];
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t* bits = bits_s[threadIdx.x / 32];
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) / 32; t < n; t += nwarps) {
         PrepRec p = prep[t];
         p.arena_off = off_arena[t];
         p.cigar_off = off_cigar[t];
         p.h_off = off_h[t];
-        prep[t] = p;
+        if (lane == 0) prep[t] = p;
         const uint8_t* s = seq + off[p.read];
         const uint32_t L = p.qlen;
         if (p.type == 1) {
             // hamming_align (src/aligner.rs:181-259)
-            auto eq = [&](uint32_t i) { return read_char(s, L, i, p.rc) == ref_base(R, p.ref_id, p.wstart + i); };
-            uint32_t bs, be;
-            const int32_t best = highest_scoring_segment(eq, L, sc, bs, be);
-            CigarWriter w{cigar + p.cigar_off, 0, p.cigar_cap, false};
-            const uint32_t mm = hamming_cigar(eq, bs, be, w);
-            ExtResult r = res[t];
-            r.valid = w.overflow ? 0 : 1;
-            r.score = (uint32_t)best;
-            r.edit_distance = mm;
-            r.ref_start = p.wstart + bs;
-            r.length = be - bs;
-            r.soft_clip_left = bs;
-            r.soft_clip_right = L - be;
-            r.cigar_offset = (uint32_t)p.cigar_off;
-            r.cigar_len = w.n;
-            res[t] = r;
-        } else if (p.type == 3) {
-            uint8_t* q = arena + p.arena_off;
-            for (uint32_t i = 0; i < L; i++) q[i] = read_char(s, L, i, p.rc);
-            uint8_t* w = q + L;
-            for (uint32_t i = 0; i < p.wlen; i++) w[i] = ref_base(R, p.ref_id, p.wstart + i);
-            pw_list[atomicAdd(&counters[19], 1u)] = t;
-        } else if (p.type == 2) {
-            uint8_t* q = arena + p.arena_off;
-            for (uint32_t i = 0; i < L; i++) q[i] = read_char(s, L, i, p.rc);
-            uint8_t* w = q + L;
-            if (jobs[t].kind == JOB_ALIGN) {
-                const uint8_t* rr = raw_refs + raw_off[p.ref_id];
-                for (uint32_t i = 0; i < p.wlen; i++) w[i] = rr[i];
-            } else {
-                for (uint32_t i = 0; i < p.wlen; i++) w[i] = ref_base(R, p.ref_id, p.wstart + i);
+            const uint32_t nw = (L + 31) / 32;
+            for (uint32_t w = 0; w < nw; w++) {
+                const uint32_t i = 32 * w + lane;
+                const bool eq = i < L && read_char(s, L, i, p.rc) == ref_base(R, p.ref_id, p.wstart + i);
+                const uint32_t m = __ballot_sync(FULLM, eq);
+                if (lane == 0) bits[w] = m;
             }
-            uint32_t ti = atomicAdd(&counters[0], 1u);
-            atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8), (unsigned long long)L * p.wlen);
-            SswTask tk{};
-            tk.job = t;
-            tk.raw_off = RAW_FALLBACK;
-            tk.ref_begin1 = -1;
-            tk.read_begin1 = -1;
-            tasks[ti] = tk;
+            __syncwarp();
+            if (lane == 0) {
+                auto eq = [&](uint32_t i) { return (bool)((bits[i >> 5] >> (i & 31)) & 1); };
+                uint32_t bs, be;
+                const int32_t best = highest_scoring_segment(eq, L, sc, bs, be);
+                CigarWriter w{cigar + p.cigar_off, 0, p.cigar_cap, false};
+                const uint32_t mm = hamming_cigar_bits(bits, bs, be, w);
+                ExtResult r = res[t];
+                r.valid = w.overflow ? 0 : 1;
+                r.score = (uint32_t)best;
+                r.edit_distance = mm;
+                r.ref_start = p.wstart + bs;
+                r.length = be - bs;
+                r.soft_clip_left = bs;
+                r.soft_clip_right = L - be;
+                r.cigar_offset = (uint32_t)p.cigar_off;
+                r.cigar_len = w.n;
+                res[t] = r;
+            }
+            __syncwarp();
+        } else if (p.type == 2 || p.type == 3) {
+            uint8_t* q = arena + p.arena_off;
+            for (uint32_t i = lane; i < L; i += 32) q[i] = read_char(s, L, i, p.rc);
+            uint8_t* w = q + L;
+            if (p.type == 2 && jobs[t].kind == JOB_ALIGN) {
+                const uint8_t* rr = raw_refs + raw_off[p.ref_id];
+                for (uint32_t i = lane; i < p.wlen; i += 32) w[i] = rr[i];
+            } else {
+                for (uint32_t i = lane; i < p.wlen; i += 32) w[i] = ref_base(R, p.ref_id, p.wstart + i);
+            }
+            if (lane == 0) {
+                if (p.type == 3) {
+                    pw_list[atomicAdd(&counters[19], 1u)] = t;
+                } else {
+                    uint32_t ti = atomicAdd(&counters[0], 1u);
+                    atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8), (unsigned long long)L * p.wlen);
+                    SswTask tk{};
+                    tk.job = t;
+                    tk.raw_off = RAW_FALLBACK;
+                    tk.ref_begin1 = -1;
+                    tk.read_begin1 = -1;
+                    tasks[ti] = tk;
+                }
+            }
         }
     }
 }
@@ -1762,7 +1832,7 @@ constexpr int BAND_THREAD_MAX_BW = 5;  // bands up to 11 cells a thread per task
 // for k_band_warp (raw_off stays RAW_FALLBACK), which starts its doubling over.
 __global__ void __launch_bounds__(128) k_band_small(SswTask* tasks, uint32_t n_tasks, const PrepRec* prep,
                                                     const uint8_t* arena, int32_t* hscratch, AlignScores sc,
-                                                    uint32_t* counters) {
+                                                    uint32_t* counters, uint32_t* warp_list) {
     uint64_t computed = 0, canonical = 0;
     for (uint32_t ti = blockIdx.x * blockDim.x + threadIdx.x; ti < n_tasks; ti += gridDim.x * blockDim.x) {
         SswTask tk = tasks[ti];
@@ -1773,7 +1843,10 @@ __global__ void __launch_bounds__(128) k_band_small(SswTask* tasks, uint32_t n_t
         const int rl = tk.ref_end1 - tk.ref_begin1 + 1, ql = tk.read_end1 - tk.read_begin1 + 1;
         const int len = rl > ql ? rl : ql;
         int bw = (rl > ql ? rl - ql : ql - rl) + 1;
-        if (bw > BAND_THREAD_MAX_BW) continue;
+        if (bw > BAND_THREAD_MAX_BW) {
+            warp_list[atomicAdd(&counters[28], 1u)] = ti;
+            continue;
+        }
         // rows in the task's scratch as k_band_warp keeps them, the CIGAR after them
         uint32_t* rows = reinterpret_cast<uint32_t*>(hscratch + p.h_off);
         int mx = 0;
@@ -1795,7 +1868,10 @@ __global__ void __launch_bounds__(128) k_band_small(SswTask* tasks, uint32_t n_t
             computed += cells;
             bw *= 2;
         } while (mx < tk.score1 && bw <= len);
-        if (!small) continue;  // raw_off stays RAW_FALLBACK: k_band_warp takes it
+        if (!small) {  // raw_off stays RAW_FALLBACK: k_band_warp takes it
+            warp_list[atomicAdd(&counters[28], 1u)] = ti;
+            continue;
+        }
         bw /= 2;
         canonical += cells;
         uint32_t* c = rows + 4 * (size_t)ql;
@@ -1828,15 +1904,17 @@ __global__ void __launch_bounds__(128) k_band_small(SswTask* tasks, uint32_t n_t
     count_band_cells(counters, cs, cn);
 }
 
-__global__ void __launch_bounds__(128) k_band_warp(SswTask* tasks, uint32_t n_tasks, const PrepRec* prep,
+__global__ void __launch_bounds__(128) k_band_warp(SswTask* tasks, const uint32_t* list, const PrepRec* prep,
                                                    const uint8_t* arena, int32_t* hscratch, AlignScores sc,
-                                                   uint32_t* counters) {
+                                                   uint32_t* counters, uint32_t* wide_list) {
     const int lane = threadIdx.x & 31;
+    const uint32_t n_list = counters[28];  // the tasks k_band_small left
     for (;;) {
-        uint32_t ti = 0;
-        if (lane == 0) ti = atomicAdd(&counters[6], 1u);
-        ti = __shfl_sync(FULLM, ti, 0);
-        if (ti >= n_tasks) break;
+        uint32_t li = 0;
+        if (lane == 0) li = atomicAdd(&counters[6], 1u);
+        li = __shfl_sync(FULLM, li, 0);
+        if (li >= n_list) break;
+        const uint32_t ti = list[li];
         SswTask tk = tasks[ti];
         // skip the tasks k_band_small finished
         if (tk.ref_begin1 < 0 || tk.read_begin1 < 0 || tk.raw_off != RAW_FALLBACK) continue;
@@ -1864,6 +1942,7 @@ __global__ void __launch_bounds__(128) k_band_warp(SswTask* tasks, uint32_t n_ta
         } while (mx < tk.score1 && bw <= len);
         if (fallback) {
             count_band_cells(counters, computed, 0);
+            if (lane == 0) wide_list[atomicAdd(&counters[29], 1u)] = ti;
             continue;  // raw_off stays RAW_FALLBACK
         }
         bw /= 2;
@@ -2066,25 +2145,23 @@ __device__ bool band_traceback(const uint32_t* rowbits, int nch, int rl, int ql,
 
 // Band width search of the tasks k_band_warp left (raw_off == RAW_FALLBACK), warp
 // per task; sizes their direction (ballot words) and CIGAR slices.
-__global__ void __launch_bounds__(32) k_band_width_wide(SswTask* tasks, const uint32_t* n_tasks_ptr, const PrepRec* prep,
+// Over the tasks k_band_warp left (wide_list); dir_size and raw_size are zero for the
+// others.
+__global__ void __launch_bounds__(32) k_band_width_wide(SswTask* tasks, const uint32_t* n_tasks_ptr,
+                                                        const uint32_t* wide_list, const PrepRec* prep,
                                                         const uint8_t* arena, AlignScores sc, int maxc,
                                                         uint64_t* dir_size, uint64_t* raw_size, uint32_t* counters) {
     extern __shared__ int band_smem[];
     const int lane = threadIdx.x & 31;
     const uint32_t n = *n_tasks_ptr;
     for (;;) {
-        uint32_t ti = 0;
-        if (lane == 0) ti = atomicAdd(&counters[7], 1u);
-        ti = __shfl_sync(FULLM, ti, 0);
-        if (ti >= n) break;
+        uint32_t li = 0;
+        if (lane == 0) li = atomicAdd(&counters[7], 1u);
+        li = __shfl_sync(FULLM, li, 0);
+        if (li >= n) break;
+        const uint32_t ti = wide_list[li];
         SswTask tk = tasks[ti];
-        if (tk.ref_begin1 < 0 || tk.read_begin1 < 0 || tk.raw_off != RAW_FALLBACK) {
-            if (lane == 0) {
-                dir_size[ti] = 0;
-                raw_size[ti] = 0;
-            }
-            continue;
-        }
+        if (tk.ref_begin1 < 0 || tk.read_begin1 < 0 || tk.raw_off != RAW_FALLBACK) continue;
         const PrepRec p = prep[tk.job];
         const uint8_t* q = arena + p.arena_off;
         const uint8_t* r = q + p.qlen;
@@ -2117,7 +2194,8 @@ __global__ void __launch_bounds__(32) k_band_width_wide(SswTask* tasks, const ui
     }
 }
 
-__global__ void __launch_bounds__(32) k_band_trace_wide(SswTask* tasks, const uint32_t* n_tasks_ptr, const PrepRec* prep,
+__global__ void __launch_bounds__(32) k_band_trace_wide(SswTask* tasks, const uint32_t* n_tasks_ptr,
+                                                        const uint32_t* wide_list, const PrepRec* prep,
                                                         const uint8_t* arena, AlignScores sc, int maxc,
                                                         const uint64_t* dir_off, uint8_t* dir,
                                                         const uint64_t* raw_off, uint32_t* raw, uint32_t* counters) {
@@ -2125,10 +2203,11 @@ __global__ void __launch_bounds__(32) k_band_trace_wide(SswTask* tasks, const ui
     const int lane = threadIdx.x & 31;
     const uint32_t n = *n_tasks_ptr;
     for (;;) {
-        uint32_t ti = 0;
-        if (lane == 0) ti = atomicAdd(&counters[18], 1u);
-        ti = __shfl_sync(FULLM, ti, 0);
-        if (ti >= n) break;
+        uint32_t li = 0;
+        if (lane == 0) li = atomicAdd(&counters[18], 1u);
+        li = __shfl_sync(FULLM, li, 0);
+        if (li >= n) break;
+        const uint32_t ti = wide_list[li];
         SswTask tk = tasks[ti];
         if (tk.ref_begin1 < 0 || tk.read_begin1 < 0 || tk.raw_off != RAW_FALLBACK || tk.flag == 1) continue;
         const PrepRec p = prep[tk.job];
@@ -2943,7 +3022,7 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
     ws.prep.reserve(n);
     ws.sizes.reserve(3 * ((size_t)n + 1));
     ws.offs.reserve(3 * ((size_t)n + 1));
-    ws.counters.reserve(28);
+    ws.counters.reserve(32);
     if (n == 0) {
         ws.h_results.clear();
         ws.h_cigar.clear();
@@ -2951,10 +3030,11 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
     }
     uint64_t* sz[3] = {ws.sizes.p, ws.sizes.p + n + 1, ws.sizes.p + 2 * ((size_t)n + 1)};
     uint64_t* of[3] = {ws.offs.p, ws.offs.p + n + 1, ws.offs.p + 2 * ((size_t)n + 1)};
-    SA_CUDA(cudaMemsetAsync(ws.counters.p, 0, 28 * sizeof(uint32_t), st));
+    SA_CUDA(cudaMemsetAsync(ws.counters.p, 0, 32 * sizeof(uint32_t), st));
     kt->begin(KS_PREPARE, st);
     ws.rescue_list.reserve(n);
-    k_prepare<<<grid1(n), 256, 0, st>>>(ws.jobs.p, n, seq, off, refs, k, raw_refs, raw_off, ws.results.p, ws.prep.p,
+    k_prepare<<<grid1((uint64_t)n * 32), 256, 0, st>>>(ws.jobs.p, n, seq, off, refs, k, raw_refs, raw_off,
+                                                        ws.results.p, ws.prep.p,
                                         sz[0], sz[1], sz[2], ws.rescue_list.p, ws.counters.p + 4,
                                         ws.counters.p + 20);
     {
@@ -2992,7 +3072,8 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
     ws.list_rev_word.reserve(n);
     kt->begin(KS_FILL, st);
     ws.pw_list.reserve(n);
-    k_fill<<<grid1(n), 256, 0, st>>>(ws.jobs.p, n, seq, off, refs, raw_refs, raw_off, sc, ws.prep.p, of[0], of[1],
+    k_fill<<<grid1((uint64_t)n * 32, 32 * FILL_WARPS), 32 * FILL_WARPS, 0, st>>>(
+        ws.jobs.p, n, seq, off, refs, raw_refs, raw_off, sc, ws.prep.p, of[0], of[1],
                                      of[2], ws.arena.p, ws.cigar.p, ws.results.p, ws.tasks.p, ws.counters.p,
                                      ws.pw_list.p);
     kt->end(st);
@@ -3146,10 +3227,12 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
             if (blocks > sm_count() * 16) blocks = sm_count() * 16;
             uint64_t tblocks = ((uint64_t)n_tasks + 127) / 128;
             if (tblocks > sm_count() * 16) tblocks = sm_count() * 16;
+            ws.band_list.reserve(n_tasks);
+            ws.wide_list.reserve(n_tasks);
             k_band_small<<<(unsigned)tblocks, 128, 0, st>>>(ws.tasks.p, n_tasks, ws.prep.p, ws.arena.p,
-                                                             ws.hscratch.p, sc, ws.counters.p);
-            k_band_warp<<<(unsigned)blocks, 128, 0, st>>>(ws.tasks.p, n_tasks, ws.prep.p, ws.arena.p, ws.hscratch.p,
-                                                          sc, ws.counters.p);
+                                                             ws.hscratch.p, sc, ws.counters.p, ws.band_list.p);
+            k_band_warp<<<(unsigned)blocks, 128, 0, st>>>(ws.tasks.p, ws.band_list.p, ws.prep.p, ws.arena.p,
+                                                          ws.hscratch.p, sc, ws.counters.p, ws.wide_list.p);
             kt->end(st);
             launches++;
         }
@@ -3172,8 +3255,11 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
                                              (int)band_smem));
                 attr_smem = (int)band_smem;
             }
-            k_band_width_wide<<<band_blocks, 32, band_smem, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p, sc,
-                                                                 maxc, ws.dir_size.p, ws.raw_size.p, ws.counters.p);
+            SA_CUDA(cudaMemsetAsync(ws.dir_size.p, 0, (size_t)n_tasks * 8, st));
+            SA_CUDA(cudaMemsetAsync(ws.raw_size.p, 0, (size_t)n_tasks * 8, st));
+            k_band_width_wide<<<band_blocks, 32, band_smem, st>>>(ws.tasks.p, ws.counters.p + 29, ws.wide_list.p,
+                                                                 ws.prep.p, ws.arena.p, sc, maxc, ws.dir_size.p,
+                                                                 ws.raw_size.p, ws.counters.p);
         } else {
             k_band_width<<<grid1(n_tasks, 128), 128, 0, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p,
                                                               ws.hscratch.p, sc, ws.dir_size.p, ws.raw_size.p);
@@ -3194,9 +3280,9 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
         SA_CUDA(cudaMemsetAsync(ws.dir.p, 0, dtot + 16, st));
         kt->begin(KS_BAND, st);
         if (wide)
-            k_band_trace_wide<<<band_blocks, 32, band_smem, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p, sc,
-                                                                 maxc, ws.dir_off.p, ws.dir.p, ws.raw_off.p, ws.raw.p,
-                                                                 ws.counters.p);
+            k_band_trace_wide<<<band_blocks, 32, band_smem, st>>>(ws.tasks.p, ws.counters.p + 29, ws.wide_list.p,
+                                                                 ws.prep.p, ws.arena.p, sc, maxc, ws.dir_off.p,
+                                                                 ws.dir.p, ws.raw_off.p, ws.raw.p, ws.counters.p);
         else
             k_band_trace<<<grid1(n_tasks, 128), 128, 0, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p,
                                                               ws.hscratch.p, sc, ws.dir_off.p, ws.dir.p, ws.raw_off.p,
