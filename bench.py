@@ -476,6 +476,8 @@ def main():
         pg = dist
     import strobealign_gb300 as sa
 
+    # the device's integer instruction rate: the Smith-Waterman rooflines' denominator
+    alu = sa.measure_int_alu()
     t = time.time()
     g, r1, r2, read_length = workload(args.scale, args.workload, args.pairs)
     gen_s = time.time() - t
@@ -647,9 +649,9 @@ def main():
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     lookup = (parity or {}).get("lookup_sectors")
     roofline, rooflines = roofline_for(dom, kern, cells, peaks, clk.summary(), counts, args.steps, sms, n_reads,
-                                       lookup) if dom else (None, {})
+                                       lookup, alu) if dom else (None, {})
     _, rooflines_iso = roofline_for(dom, kern_iso, cells_iso, peaks, clk.summary(), counts_iso, 1, sms, n_reads,
-                                    lookup) if dom else (None, {})
+                                    lookup, alu) if dom else (None, {})
     reads_gb = int(R1.seq_offsets[-1]) * (2 if R2 is not None else 1) / 1e9
     out = {
         "metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": ws, "steps": args.steps,
@@ -694,6 +696,7 @@ def main():
         # the same stages timed in one plain (stage-synchronous) map, each kernel alone on
         # the GPU: the kernels' own rates, without the NAM stream sharing the SMs
         "rooflines_isolated": rooflines_iso,
+        "int_alu": alu,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
     }
@@ -722,7 +725,7 @@ NCU_DRAM_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, 1/10-scale 
 ANCHOR_RATE = ("sort", "chain")
 
 
-def roofline_for(dom, kern, cells, peaks, clocks, counts, steps, sms, n_reads, lookup=None) -> dict:
+def roofline_for(dom, kern, cells, peaks, clocks, counts, steps, sms, n_reads, lookup=None, alu=None) -> dict:
     """Roofline of every timed stage, and of the dominant one.
 
     Seeding is framed against HBM bandwidth with its algorithmic bytes per launch
@@ -773,12 +776,21 @@ def roofline_for(dom, kern, cells, peaks, clocks, counts, steps, sms, n_reads, l
             out[st] = {"kernel": st, "bound": "issue/latency", "achieved": counts["n_anchor_total"] * steps / (ms / 1e3),
                        "peak": None, "unit": "anchors/s", "frac": None, "traffic": None, "avg_launch_ms": ms / n,
                        "launches": n}
+    # the integer-ALU denominator: the device's measured add-then-max rate / 11
+    # instructions per cell when measured, else SMs x 128 lanes x clock / 11
+    clock = (clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)) * 1e6
+    model_gcups = sms * 128 * clock / 11 / 1e9
+    if alu and alu.get("viaddmax_per_s"):
+        peak_gcups = alu["viaddmax_per_s"] / 11 / 1e9
+        peak_source = ("measured add-then-max instruction rate (sa_measure_int_alu, all SMs) / 11 instructions "
+                       "per cell")
+    else:
+        peak_gcups = model_gcups
+        peak_source = f"{sms} SMs x 128 INT32 lanes x median SM clock under load / 11 ops per cell"
     if kern.get("sw_byte", [0, 0])[1]:
         ms = kern.get("sw_byte", [0.0, 0])[0] + kern.get("sw_word", [0.0, 0])[0]
         n = kern.get("sw_byte", [0.0, 0])[1] + kern.get("sw_word", [0.0, 0])[1]
         sec = ms / 1000.0
-        clock = (clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)) * 1e6
-        peak_gcups = sms * 128 * clock / 11 / 1e9
         achieved = cells.get("canonical", 0) / sec / 1e9 if sec else 0.0
         computed = sum(cells.get(k, 0) for k in ("forward_byte", "forward_word", "reverse_byte", "reverse_word"))
         sw_cells = {k: v for k, v in cells.items() if not k.startswith("band_")}
@@ -788,21 +800,19 @@ def roofline_for(dom, kern, cells, peaks, clocks, counts, steps, sms, n_reads, l
                      "traffic_source": NCU_DRAM_SOURCE,
                      "avg_launch_ms": ms / max(n, 1), "launches": n,
                      "computed_gcups": computed / sec / 1e9 if sec else 0.0, "cells": sw_cells,
-                     "peak_source": f"{sms} SMs x 128 INT32 lanes x median SM clock under load / 11 ops per cell"}
+                     "peak_source": peak_source, "model_peak_gcups": model_gcups}
     if kern.get("banded_traceback", [0, 0])[1] and cells.get("band_canonical"):
         # banded_sw (ext/ssw/ssw.c:598-769): the final pass's band cells per second, the
         # same integer-ALU model as SSW; the doubling passes' cells beside it
         ms, n = kern["banded_traceback"]
         sec = ms / 1000.0
-        clock = (clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)) * 1e6
-        peak_gcups = sms * 128 * clock / 11 / 1e9
         achieved = cells["band_canonical"] / sec / 1e9 if sec else 0.0
-        out["band"] = {"kernel": "k_band_warp + k_band_width_wide + k_band_trace_wide", "bound": "int32",
+        out["band"] = {"kernel": "k_band_small + k_band_warp + k_band_width_wide + k_band_trace_wide", "bound": "int32",
                        "achieved": achieved, "peak": peak_gcups, "unit": "GCUPS", "frac": achieved / peak_gcups,
                        "traffic": None, "avg_launch_ms": ms / max(n, 1), "launches": n,
                        "computed_gcups": cells.get("band_computed", 0) / sec / 1e9 if sec else 0.0,
                        "cells": {"canonical": cells["band_canonical"], "computed": cells.get("band_computed", 0)},
-                       "peak_source": f"{sms} SMs x 128 INT32 lanes x median SM clock under load / 11 ops per cell"}
+                       "peak_source": peak_source}
     key = "sw" if dom in ("sw_byte", "sw_word") else "lookup" if dom == "hits" else dom
     head = dict(out.get(key) or {"kernel": dom, "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s",
                                  "frac": None, "traffic": None})

@@ -531,6 +531,14 @@ void sa_stream_params_default(sa_stream_params* p);
 int32_t sa_map_files(sa_mapper* m, const char* reads1, const char* reads2, const char* out_path,
                      const sa_stream_params* p, sa_stream_stats* stats);
 
+/* ---------------------------------------------------------------- measurement
+ * Integer-ALU instruction rate of the current device, measured by a kernel of eight
+ * independent chains per thread over every SM (the median of five launches):
+ * out[0] add-then-max instructions per second (the fused form the SSW and banded
+ * kernels use), out[1] max and xor instructions per second.  The denominator of the
+ * Smith-Waterman rooflines; no reference counterpart. */
+int32_t sa_measure_int_alu(double* out);
+
 /* SAM header (src/io/sam.rs:176-200); cmd_line NULL omits the @PG line. */
 int32_t sa_sam_header(const sa_refs* refs, const char* cmd_line, const char* rg_id, const char* const* rg_fields,
                       size_t n_rg_fields, sa_output* out);

@@ -646,6 +646,13 @@ class Session:
         self.close()
 
 
+def measure_int_alu() -> dict:
+    """sa_measure_int_alu: the device's integer instruction rates (per second)."""
+    out = (C.c_double * 2)()
+    L.check(lib().sa_measure_int_alu(out))
+    return {"viaddmax_per_s": out[0], "max_xor_per_s": out[1]}
+
+
 def sam_header(refs: References, cmd_line: str | None = None, rg_id: str | None = None,
                rg_fields: list[str] = ()) -> bytes:
     o = L.Output()

@@ -183,6 +183,7 @@ SIGNATURES = {
     "sa_mapper_set_tuning": (i32, [vp, P(Tuning)]),
     "sa_mapper_get_tuning": (i32, [vp, P(Tuning)]),
     "sa_mapper_autotune": (i32, [vp, P(ReadBatch), P(ReadBatch), u32, P(TuneReport)]),
+    "sa_measure_int_alu": (i32, [P(f64)]),
     "sa_stream_params_default": (None, [P(StreamParams)]),
     "sa_map_files": (i32, [vp, cp, cp, cp, P(StreamParams), P(StreamStats)]),
 }

@@ -2342,17 +2342,60 @@ __global__ void k_band_trace(SswTask* tasks, const uint32_t* n_tasks_ptr, const 
 }
 
 // SswAligner::align (src/ssw.rs:156-188) + Aligner::align end bonus (src/aligner.rs:92-148)
-__global__ void k_finalize(const SswTask* tasks, const uint32_t* n_tasks_ptr, const PrepRec* prep, const uint8_t* arena,
-                           const uint64_t* raw_off, const uint32_t* raw, const int32_t* hscratch, AlignScores sc,
-                           uint32_t* cigar, ExtResult* res) {
+// A warp per task: the base comparisons of the front and back extensions and of the
+// CIGAR's M runs are made 32 at a time by ballot; lane 0 turns each mask into =/X runs.
+// Mismatches among the first cnt positions from (qa, ra), by the warp
+__device__ __forceinline__ uint32_t warp_mismatches(const uint8_t* q, const uint8_t* rf, uint32_t qa, uint32_t ra,
+                                                    uint32_t cnt, int step) {
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t mm = 0;
+    for (uint32_t c = 0; c < cnt; c += 32) {
+        const uint32_t t = c + lane;
+        const bool x = t < cnt && q[(int64_t)qa + step * (int64_t)t] != rf[(int64_t)ra + step * (int64_t)t];
+        mm += __popc(__ballot_sync(FULLM, x));
+    }
+    return mm;
+}
+
+// =/X runs of q[qa, qa + len) against rf[ra, ...) pushed by lane 0; returns the mismatches
+__device__ __forceinline__ uint32_t warp_eq_runs(const uint8_t* q, const uint8_t* rf, uint32_t qa, uint32_t ra,
+                                                 uint32_t len, CigarWriter& w) {
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t mm = 0;
+    for (uint32_t c = 0; c < len; c += 32) {
+        const uint32_t t = c + lane;
+        const uint32_t m = __ballot_sync(FULLM, t < len && q[qa + t] == rf[ra + t]);
+        const uint32_t cnt = len - c < 32 ? len - c : 32;
+        const uint32_t valid = cnt == 32 ? 0xffffffffu : ((1u << cnt) - 1);
+        mm += __popc(~m & valid);
+        if (lane == 0) {
+            uint32_t pos = 0;
+            while (pos < cnt) {
+                const bool e = (m >> pos) & 1;
+                const uint32_t x = (e ? ~m : m) & valid & (0xffffffffu << pos);
+                const uint32_t stop = x ? (uint32_t)(__ffs(x) - 1) : cnt;
+                w.push(e ? 7u : 8u, stop - pos);
+                pos = stop;
+            }
+        }
+    }
+    return mm;
+}
+
+__global__ void __launch_bounds__(128) k_finalize(const SswTask* tasks, const uint32_t* n_tasks_ptr,
+                                                  const PrepRec* prep, const uint8_t* arena, const uint64_t* raw_off,
+                                                  const uint32_t* raw, const int32_t* hscratch, AlignScores sc,
+                                                  uint32_t* cigar, ExtResult* res) {
+    const uint32_t lane = threadIdx.x & 31;
     const uint32_t n = *n_tasks_ptr;
-    for (uint32_t ti = blockIdx.x * blockDim.x + threadIdx.x; ti < n; ti += gridDim.x * blockDim.x) {
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t ti = (blockIdx.x * blockDim.x + threadIdx.x) / 32; ti < n; ti += nwarps) {
         const SswTask tk = tasks[ti];
         const PrepRec p = prep[tk.job];
         ExtResult r = res[tk.job];
         r.valid = 0;
         if (tk.ref_begin1 < 0 || tk.read_begin1 < 0 || tk.flag != 0) {
-            res[tk.job] = r;
+            if (lane == 0) res[tk.job] = r;
             continue;
         }
         const uint8_t* q = arena + p.arena_off;
@@ -2363,7 +2406,6 @@ __global__ void k_finalize(const SswTask* tasks, const uint32_t* n_tasks_ptr, co
         // M -> =/X over the aligned segments; reject walks past them (the reference panics there)
         const uint32_t* rw = tk.raw_off == RAW_FALLBACK ? raw + raw_off[ti]
                                                         : reinterpret_cast<const uint32_t*>(hscratch) + tk.raw_off;
-        uint32_t ed = 0;
         bool bad = false;
         {
             uint32_t qi = qs, ri = rs;
@@ -2378,42 +2420,33 @@ __global__ void k_finalize(const SswTask* tasks, const uint32_t* n_tasks_ptr, co
             }
         }
         if (bad) {
-            res[tk.job] = r;
+            if (lane == 0) res[tk.job] = r;
             continue;
         }
-        // front extension (src/aligner.rs:92-118)
-        uint32_t fq = qs, fr = rs;
-        int32_t fscore = score;
-        uint32_t fed = 0;
-        while (fq > 0 && fr > 0) {
-            fq--;
-            fr--;
-            if (q[fq] == rf[fr]) fscore += sc.match;
-            else { fscore -= sc.mismatch; fed++; }
-        }
-        bool take_front = fq == 0 && fscore + (int32_t)sc.end_bonus > score;
+        // front extension (src/aligner.rs:92-118): ungapped to the left while both
+        // sequences last
+        const uint32_t fm = qs < rs ? qs : rs;
+        const uint32_t fed = warp_mismatches(q, rf, qs - 1, rs - 1, fm, -1);
+        const uint32_t fq = qs - fm, fr = rs - fm;
+        const int32_t fscore = score + (int32_t)sc.match * (int32_t)(fm - fed) - (int32_t)sc.mismatch * (int32_t)fed;
+        const bool take_front = fq == 0 && fscore + (int32_t)sc.end_bonus > score;
         CigarWriter w{cigar + p.cigar_off, 0, p.cigar_cap, false};
-        if (take_front && qs > 0) {
-            for (uint32_t a = fq; a < qs; a++) w.push(q[a] == rf[fr + (a - fq)] ? 7u : 8u, 1);
-        }
+        if (take_front && qs > 0) warp_eq_runs(q, rf, fq, fr, qs - fq, w);
+        uint32_t ed = 0;
         {
             uint32_t qi = qs, ri = rs;
             for (uint32_t a = 0; a < tk.raw_len; a++) {
                 uint32_t op = rw[a] & 15, l = rw[a] >> 4;
                 if (op == 0) {
-                    for (uint32_t b = 0; b < l; b++) {
-                        bool eq = q[qi] == rf[ri];
-                        ed += !eq;
-                        w.push(eq ? 7u : 8u, 1);
-                        qi++;
-                        ri++;
-                    }
+                    ed += warp_eq_runs(q, rf, qi, ri, l, w);
+                    qi += l;
+                    ri += l;
                 } else if (op == 1) {
-                    w.push(1, l);
+                    if (lane == 0) w.push(1, l);
                     ed += l;
                     qi += l;
                 } else {
-                    w.push(2, l);
+                    if (lane == 0) w.push(2, l);
                     ed += l;
                     ri += l;
                 }
@@ -2428,35 +2461,32 @@ __global__ void k_finalize(const SswTask* tasks, const uint32_t* n_tasks_ptr, co
             edits = ed + fed;
         }
         // back extension (src/aligner.rs:120-148)
-        uint32_t bq = qe, br = re;
-        int32_t bscore = score;
-        uint32_t bed = edits;
-        while (bq < qlen && br < rlen) {
-            if (q[bq] == rf[br]) bscore += sc.match;
-            else { bscore -= sc.mismatch; bed++; }
-            bq++;
-            br++;
-        }
+        const uint32_t bm = qlen - qe < rlen - re ? qlen - qe : rlen - re;
+        const uint32_t bmm = warp_mismatches(q, rf, qe, re, bm, 1);
+        const uint32_t bq = qe + bm, br = re + bm;
+        const int32_t bscore = score + (int32_t)sc.match * (int32_t)(bm - bmm) - (int32_t)sc.mismatch * (int32_t)bmm;
+        const uint32_t bed = edits + bmm;
         uint32_t a_qe = qe, a_re = re;
         if (bq == qlen && bscore + (int32_t)sc.end_bonus > score) {
-            if (qe < qlen)
-                for (uint32_t a = qe; a < bq; a++) w.push(q[a] == rf[re + (a - qe)] ? 7u : 8u, 1);
+            if (qe < qlen) warp_eq_runs(q, rf, qe, re, bq - qe, w);
             a_qe = qlen;
             a_re = br;
             score = bscore + (int32_t)sc.end_bonus;
             edits = bed;
         }
-        w.finish();
-        r.valid = w.overflow ? 0 : 1;
-        r.score = (uint32_t)score;
-        r.edit_distance = edits;
-        r.ref_start = p.wstart + a_rs;
-        r.length = a_re - a_rs;
-        r.soft_clip_left = a_qs;
-        r.soft_clip_right = qlen - a_qe;
-        r.cigar_offset = (uint32_t)p.cigar_off;
-        r.cigar_len = w.n;
-        res[tk.job] = r;
+        if (lane == 0) {
+            w.finish();
+            r.valid = w.overflow ? 0 : 1;
+            r.score = (uint32_t)score;
+            r.edit_distance = edits;
+            r.ref_start = p.wstart + a_rs;
+            r.length = a_re - a_rs;
+            r.soft_clip_left = a_qs;
+            r.soft_clip_right = qlen - a_qe;
+            r.cigar_offset = (uint32_t)p.cigar_off;
+            r.cigar_len = w.n;
+            res[tk.job] = r;
+        }
     }
 }
 
@@ -3289,8 +3319,8 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
                                                               ws.raw.p);
         kt->end(st);
         kt->begin(KS_FINALIZE, st);
-        // one warp per block: a wave's few thousand SSW tasks spread over all SMs
-        k_finalize<<<grid1(n_tasks, 32), 32, 0, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p,
+        // a warp per task
+        k_finalize<<<grid1((uint64_t)n_tasks * 32, 128), 128, 0, st>>>(ws.tasks.p, ws.counters.p, ws.prep.p, ws.arena.p,
                                                         ws.raw_off.p, ws.raw.p, ws.hscratch.p, sc, ws.cigar.p,
                                                         ws.results.p);
         kt->end(st);
