@@ -132,42 +132,50 @@ __global__ void __launch_bounds__(64) k_rescue_filter(const uint32_t* __restrict
     }
 }
 
-// Nam::is_consistent (src/nam.rs:49-69) by a warp: lane i < k compares base i of both
-// ends (k < 32)
-__device__ __forceinline__ bool warp_nam_consistent(const DevRefs& R, const uint8_t* s, uint32_t L, uint32_t ref_id,
-                                                    uint32_t rs, uint32_t re, uint32_t qs, uint32_t qe, bool rc,
-                                                    uint32_t k) {
-    const uint32_t lane = threadIdx.x & 31;
-    bool ok = true;
-    if (lane < k) {
-        ok = ref_base(R, ref_id, rs + lane) == read_char(s, L, qs + lane, rc) &&
-             ref_base(R, ref_id, re - k + lane) == read_char(s, L, qe - k + lane, rc);
-    }
-    return __all_sync(FULLM, ok);
+// 2-bit codes of the reference bases [pos, pos + 32) of contig c (pos inside the contig;
+// the word after a contig's last is its padding word)
+__device__ __forceinline__ uint64_t ref_codes32(const DevRefs& R, uint32_t c, uint64_t pos) {
+    const uint64_t* W = R.words + R.word_off[c];
+    const uint64_t a = pos >> 5;
+    const uint32_t sh = (uint32_t)(pos & 31) * 2;
+    const uint64_t w0 = __ldg(W + a);
+    return sh ? (w0 >> sh) | (__ldg(W + a + 1) << (64 - sh)) : w0;
 }
 
-// Mismatches of the read against the reference from ref_start, by a warp
-__device__ __forceinline__ uint32_t warp_hamming(const DevRefs& R, const uint8_t* s, uint32_t L, uint32_t ref_id,
-                                                 uint32_t ref_start, bool rc) {
-    const uint32_t lane = threadIdx.x & 31;
+// "ACGT"[code]
+__device__ __forceinline__ uint8_t code_char(uint32_t code) { return (uint8_t)(0x54474341u >> (8 * code)); }
+
+// Mismatches of read positions [qs, qs + cnt) (cnt <= 32) against the reference from pos
+__device__ __forceinline__ uint32_t mismatches32(const DevRefs& R, uint32_t c, uint64_t pos, const uint8_t* s,
+                                                 uint32_t L, uint32_t qs, uint32_t cnt, bool rc) {
+    const uint64_t v = ref_codes32(R, c, pos);
+    uint32_t mm = 0;
+    for (uint32_t b = 0; b < cnt; b++) mm += read_char(s, L, qs + b, rc) != code_char((uint32_t)(v >> (2 * b)) & 3);
+    return mm;
+}
+
+// Nam::is_consistent (src/nam.rs:49-69): the k-mers at both ends of the NAM match (k < 32)
+__device__ __forceinline__ bool nam_consistent(const DevRefs& R, const uint8_t* s, uint32_t L, uint32_t ref_id,
+                                               uint32_t rs, uint32_t re, uint32_t qs, uint32_t qe, bool rc,
+                                               uint32_t k) {
+    return mismatches32(R, ref_id, rs, s, L, qs, k, rc) == 0 && mismatches32(R, ref_id, re - k, s, L, qe - k, k, rc) == 0;
+}
+
+// Mismatches of the read against the reference from ref_start
+__device__ __forceinline__ uint32_t hamming_distance(const DevRefs& R, const uint8_t* s, uint32_t L, uint32_t ref_id,
+                                                     uint32_t ref_start, bool rc) {
     uint32_t hd = 0;
-    for (uint32_t c = 0; c < L; c += 32) {
-        const uint32_t i = c + lane;
-        const bool mm = i < L && ref_base(R, ref_id, ref_start + i) != read_char(s, L, i, rc);
-        hd += __popc(__ballot_sync(FULLM, mm));
-    }
+    for (uint32_t c = 0; c < L; c += 32) hd += mismatches32(R, ref_id, (uint64_t)ref_start + c, s, L, c, L - c < 32 ? L - c : 32, rc);
     return hd;
 }
 
-// A warp per job (all lanes hold the job; the base comparisons are spread over them)
+// Thread per job; the reference bases come 32 at a time from the packed words
 __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict__ seq,
                           const uint64_t* __restrict__ off, DevRefs R, uint32_t k, const uint8_t* raw_refs,
                           const uint64_t* raw_off, ExtResult* res, PrepRec* prep, uint64_t* sz_arena,
                           uint64_t* sz_cigar, uint64_t* sz_h, uint32_t* rescue_list, uint32_t* n_rescue,
                           uint32_t* max_pw_window) {
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
-    for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) / 32; t < n; t += nwarps) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         ExtJob jb = jobs[t];
         const uint8_t* s = seq + off[jb.read];
         const uint32_t L = (uint32_t)(off[jb.read + 1] - off[jb.read]);
@@ -181,11 +189,11 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
         if (jb.kind == JOB_EXTEND_FAST || jb.kind == JOB_EXTEND_FULL) {
             uint32_t qs = jb.query_start, qe = jb.query_end;
             bool rc = jb.is_revcomp;
-            bool cons = warp_nam_consistent(R, s, L, jb.ref_id, jb.ref_start, jb.ref_end, qs, qe, rc, k);
+            bool cons = nam_consistent(R, s, L, jb.ref_id, jb.ref_start, jb.ref_end, qs, qe, rc, k);
             bool flipped = false;
             if (!cons && jb.kind == JOB_EXTEND_FULL) {
                 uint32_t q2s = L - qe, q2e = L - qs;
-                if (warp_nam_consistent(R, s, L, jb.ref_id, jb.ref_start, jb.ref_end, q2s, q2e, !rc, k)) {
+                if (nam_consistent(R, s, L, jb.ref_id, jb.ref_start, jb.ref_end, q2s, q2e, !rc, k)) {
                     rc = !rc;
                     qs = q2s;
                     qe = q2e;
@@ -206,7 +214,7 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
             uint32_t pre = (uint32_t)(pre64 < clen ? pre64 : clen);
             bool hamming = false;
             if ((uint64_t)prs + L == pre && cons) {
-                const uint32_t hd = warp_hamming(R, s, L, jb.ref_id, prs, rc);
+                const uint32_t hd = hamming_distance(R, s, L, jb.ref_id, prs, rc);
                 if (__fdiv_rn(__uint2float_rn(hd), __uint2float_rn(L)) < 0.05f) hamming = true;
             }
             if (hamming) {
@@ -236,7 +244,7 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
                     p.wstart = ds;
                     p.wlen = de > ds ? (uint32_t)(de - ds) : 0;
                     p.type = (cons && jb.anc_n > 0 && L > 0) ? 3 : 0;
-                    if (p.type == 3 && lane == 0) atomicMax(max_pw_window, p.wlen);
+                    if (p.type == 3) atomicMax(max_pw_window, p.wlen);
                 }
             }
         } else if (jb.kind == JOB_RESCUE) {
@@ -248,7 +256,7 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
             p.wlen = jb.ref_end - jb.ref_start;
             // extended only if has_shared_substring holds (k_rescue_filter)
             p.type = (p.wlen <= 2000 && L > 0) ? 2 : 0;
-            if (p.type == 2 && lane == 0) rescue_list[atomicAdd(n_rescue, 1u)] = t;
+            if (p.type == 2) rescue_list[atomicAdd(n_rescue, 1u)] = t;
         } else {  // JOB_ALIGN: raw reference bytes
             p.rc = 0;
             p.wstart = 0;
@@ -268,13 +276,11 @@ __global__ void k_prepare(const ExtJob* jobs, uint32_t n, const uint8_t* __restr
             hs = 3 * (2 * len + 8);
         }
         p.cigar_cap = (uint32_t)cap;
-        if (lane == 0) {
-            res[t] = r;
-            prep[t] = p;
-            sz_arena[t] = ab;
-            sz_cigar[t] = cap;
-            sz_h[t] = hs;
-        }
+        res[t] = r;
+        prep[t] = p;
+        sz_arena[t] = ab;
+        sz_cigar[t] = cap;
+        sz_h[t] = hs;
     }
 }
 
@@ -370,76 +376,93 @@ __device__ __forceinline__ uint32_t hamming_cigar_bits(const uint32_t* bits, uin
     return mm;
 }
 
-// A warp per job: the Hamming path (hamming_align, src/aligner.rs:181-259) from a match
-// bit array the lanes build (32 bases per ballot), or the SSW / piecewise job's query
-// and reference window bytes copied into the arena by all lanes.
-constexpr uint32_t FILL_WARPS = 8;
-__global__ void __launch_bounds__(32 * FILL_WARPS) k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict__ seq,
-                                                          const uint64_t* __restrict__ off, DevRefs R,
-                                                          const uint8_t* raw_refs, const uint64_t* raw_off,
-                                                          AlignScores sc, PrepRec* prep, const uint64_t* off_arena,
-                                                          const uint64_t* off_cigar, const uint64_t* off_h,
-                                                          uint8_t* arena, uint32_t* cigar, ExtResult* res,
-                                                          SswTask* tasks, uint32_t* counters, uint32_t* pw_list) {
-    __shared__ uint32_t bits_s[FILL_WARPS][MAX_READ_LEN / 32];
+// A warp takes 32 consecutive jobs, a lane each.  Hamming jobs (hamming_align,
+// src/aligner.rs:181-259) run on their lane: the match bits of the read against the
+// reference, 32 bases per pair of packed reference words, then the best segment and its
+// =/X runs from the bits.  The SSW / piecewise jobs' query and reference window bytes are
+// copied into the arena by the whole warp, one job after another.
+__global__ void __launch_bounds__(256) k_fill(const ExtJob* jobs, uint32_t n, const uint8_t* __restrict__ seq,
+                                              const uint64_t* __restrict__ off, DevRefs R, const uint8_t* raw_refs,
+                                              const uint64_t* raw_off, AlignScores sc, PrepRec* prep,
+                                              const uint64_t* off_arena, const uint64_t* off_cigar,
+                                              const uint64_t* off_h, uint8_t* arena, uint32_t* cigar, ExtResult* res,
+                                              SswTask* tasks, uint32_t* counters, uint32_t* pw_list) {
     const uint32_t lane = threadIdx.x & 31;
-    uint32_t* bits = bits_s[threadIdx.x / 32];
     const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
-    for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) / 32; t < n; t += nwarps) {
-        PrepRec p = prep[t];
-        p.arena_off = off_arena[t];
-        p.cigar_off = off_cigar[t];
-        p.h_off = off_h[t];
-        if (lane == 0) prep[t] = p;
-        const uint8_t* s = seq + off[p.read];
-        const uint32_t L = p.qlen;
-        if (p.type == 1) {
-            // hamming_align (src/aligner.rs:181-259)
+    for (uint32_t b0 = (blockIdx.x * blockDim.x + threadIdx.x) / 32 * 32; b0 < n; b0 += nwarps * 32) {
+        const uint32_t t = b0 + lane;
+        PrepRec p{};
+        uint64_t s_off = 0;
+        bool align_raw = false;
+        if (t < n) {
+            p = prep[t];
+            p.arena_off = off_arena[t];
+            p.cigar_off = off_cigar[t];
+            p.h_off = off_h[t];
+            prep[t] = p;
+            s_off = off[p.read];
+            align_raw = p.type == 2 && jobs[t].kind == JOB_ALIGN;
+        }
+        if (t < n && p.type == 1) {
+            const uint8_t* s = seq + s_off;
+            const uint32_t L = p.qlen;
+            uint32_t bits[MAX_READ_LEN / 32];
             const uint32_t nw = (L + 31) / 32;
             for (uint32_t w = 0; w < nw; w++) {
-                const uint32_t i = 32 * w + lane;
-                const bool eq = i < L && read_char(s, L, i, p.rc) == ref_base(R, p.ref_id, p.wstart + i);
-                const uint32_t m = __ballot_sync(FULLM, eq);
-                if (lane == 0) bits[w] = m;
+                const uint64_t v = ref_codes32(R, p.ref_id, (uint64_t)p.wstart + 32 * w);
+                const uint32_t cnt = L - 32 * w < 32 ? L - 32 * w : 32;
+                uint32_t m = 0;
+                for (uint32_t b = 0; b < cnt; b++)
+                    m |= (uint32_t)(read_char(s, L, 32 * w + b, p.rc) == code_char((uint32_t)(v >> (2 * b)) & 3)) << b;
+                bits[w] = m;
             }
-            __syncwarp();
-            if (lane == 0) {
-                auto eq = [&](uint32_t i) { return (bool)((bits[i >> 5] >> (i & 31)) & 1); };
-                uint32_t bs, be;
-                const int32_t best = highest_scoring_segment(eq, L, sc, bs, be);
-                CigarWriter w{cigar + p.cigar_off, 0, p.cigar_cap, false};
-                const uint32_t mm = hamming_cigar_bits(bits, bs, be, w);
-                ExtResult r = res[t];
-                r.valid = w.overflow ? 0 : 1;
-                r.score = (uint32_t)best;
-                r.edit_distance = mm;
-                r.ref_start = p.wstart + bs;
-                r.length = be - bs;
-                r.soft_clip_left = bs;
-                r.soft_clip_right = L - be;
-                r.cigar_offset = (uint32_t)p.cigar_off;
-                r.cigar_len = w.n;
-                res[t] = r;
-            }
-            __syncwarp();
-        } else if (p.type == 2 || p.type == 3) {
-            uint8_t* q = arena + p.arena_off;
-            for (uint32_t i = lane; i < L; i += 32) q[i] = read_char(s, L, i, p.rc);
+            auto eq = [&](uint32_t i) { return (bool)((bits[i >> 5] >> (i & 31)) & 1); };
+            uint32_t bs, be;
+            const int32_t best = highest_scoring_segment(eq, L, sc, bs, be);
+            CigarWriter cw{cigar + p.cigar_off, 0, p.cigar_cap, false};
+            const uint32_t mm = hamming_cigar_bits(bits, bs, be, cw);
+            ExtResult r = res[t];
+            r.valid = cw.overflow ? 0 : 1;
+            r.score = (uint32_t)best;
+            r.edit_distance = mm;
+            r.ref_start = p.wstart + bs;
+            r.length = be - bs;
+            r.soft_clip_left = bs;
+            r.soft_clip_right = L - be;
+            r.cigar_offset = (uint32_t)p.cigar_off;
+            r.cigar_len = cw.n;
+            res[t] = r;
+        }
+        // the copies, a job at a time by the whole warp
+        uint32_t todo = __ballot_sync(FULLM, t < n && (p.type == 2 || p.type == 3));
+        while (todo) {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const uint32_t jt = b0 + (uint32_t)src;
+            const uint64_t aoff = __shfl_sync(FULLM, (unsigned long long)p.arena_off, src);
+            const uint64_t so = __shfl_sync(FULLM, (unsigned long long)s_off, src);
+            const uint32_t L = __shfl_sync(FULLM, p.qlen, src), rcf = __shfl_sync(FULLM, p.rc, src);
+            const uint32_t wlen = __shfl_sync(FULLM, p.wlen, src), wstart = __shfl_sync(FULLM, p.wstart, src);
+            const uint32_t ref_id = __shfl_sync(FULLM, p.ref_id, src), type = __shfl_sync(FULLM, p.type, src);
+            const bool raw = __shfl_sync(FULLM, align_raw, src);
+            const uint8_t* s = seq + so;
+            uint8_t* q = arena + aoff;
+            for (uint32_t i = lane; i < L; i += 32) q[i] = read_char(s, L, i, rcf);
             uint8_t* w = q + L;
-            if (p.type == 2 && jobs[t].kind == JOB_ALIGN) {
-                const uint8_t* rr = raw_refs + raw_off[p.ref_id];
-                for (uint32_t i = lane; i < p.wlen; i += 32) w[i] = rr[i];
+            if (raw) {
+                const uint8_t* rr = raw_refs + raw_off[ref_id];
+                for (uint32_t i = lane; i < wlen; i += 32) w[i] = rr[i];
             } else {
-                for (uint32_t i = lane; i < p.wlen; i += 32) w[i] = ref_base(R, p.ref_id, p.wstart + i);
+                for (uint32_t i = lane; i < wlen; i += 32) w[i] = ref_base(R, ref_id, (uint64_t)wstart + i);
             }
-            if (lane == 0) {
-                if (p.type == 3) {
-                    pw_list[atomicAdd(&counters[19], 1u)] = t;
+            if (lane == (uint32_t)src) {
+                if (type == 3) {
+                    pw_list[atomicAdd(&counters[19], 1u)] = jt;
                 } else {
                     uint32_t ti = atomicAdd(&counters[0], 1u);
-                    atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8), (unsigned long long)L * p.wlen);
+                    atomicAdd(reinterpret_cast<unsigned long long*>(counters + 8), (unsigned long long)L * wlen);
                     SswTask tk{};
-                    tk.job = t;
+                    tk.job = jt;
                     tk.raw_off = RAW_FALLBACK;
                     tk.ref_begin1 = -1;
                     tk.read_begin1 = -1;
@@ -3063,8 +3086,7 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
     SA_CUDA(cudaMemsetAsync(ws.counters.p, 0, 32 * sizeof(uint32_t), st));
     kt->begin(KS_PREPARE, st);
     ws.rescue_list.reserve(n);
-    k_prepare<<<grid1((uint64_t)n * 32), 256, 0, st>>>(ws.jobs.p, n, seq, off, refs, k, raw_refs, raw_off,
-                                                        ws.results.p, ws.prep.p,
+    k_prepare<<<grid1(n), 256, 0, st>>>(ws.jobs.p, n, seq, off, refs, k, raw_refs, raw_off, ws.results.p, ws.prep.p,
                                         sz[0], sz[1], sz[2], ws.rescue_list.p, ws.counters.p + 4,
                                         ws.counters.p + 20);
     {
@@ -3102,7 +3124,7 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
     ws.list_rev_word.reserve(n);
     kt->begin(KS_FILL, st);
     ws.pw_list.reserve(n);
-    k_fill<<<grid1((uint64_t)n * 32, 32 * FILL_WARPS), 32 * FILL_WARPS, 0, st>>>(
+    k_fill<<<grid1(n), 256, 0, st>>>(
         ws.jobs.p, n, seq, off, refs, raw_refs, raw_off, sc, ws.prep.p, of[0], of[1],
                                      of[2], ws.arena.p, ws.cigar.p, ws.results.p, ws.tasks.p, ws.counters.p,
                                      ws.pw_list.p);
