@@ -1849,27 +1849,49 @@ __device__ int band_pass_thread(const uint8_t* ref, const uint8_t* read, int rl,
 
 constexpr int BAND_THREAD_MAX_BW = 5;  // bands up to 11 cells a thread per task
 
+// Tasks by starting band width |rl - ql| + 1: bucket b (1 .. BAND_THREAD_MAX_BW) holds
+// its tasks at buckets[b * n_tasks ..] and their count at bucket_n[b]; wider ones go
+// straight to k_band_warp's list.  k_band_small then runs the buckets in turn, so the
+// threads of a warp share their band width (one template instance per warp).
+__global__ void k_band_bucket(const SswTask* tasks, uint32_t n_tasks, uint32_t* buckets, uint32_t* bucket_n,
+                              uint32_t* warp_list, uint32_t* counters) {
+    for (uint32_t ti = blockIdx.x * blockDim.x + threadIdx.x; ti < n_tasks; ti += gridDim.x * blockDim.x) {
+        const SswTask tk = tasks[ti];
+        if (tk.ref_begin1 < 0 || tk.read_begin1 < 0) continue;
+        const int rl = tk.ref_end1 - tk.ref_begin1 + 1, ql = tk.read_end1 - tk.read_begin1 + 1;
+        const int bw = (rl > ql ? rl - ql : ql - rl) + 1;
+        if (bw > BAND_THREAD_MAX_BW) warp_list[atomicAdd(&counters[28], 1u)] = ti;
+        else buckets[(size_t)bw * n_tasks + atomicAdd(&bucket_n[bw], 1u)] = ti;
+    }
+}
+
 // banded_sw (ext/ssw/ssw.c:598-769) a thread per task while the band width stays at
 // most BAND_THREAD_MAX_BW (the band of an alignment without indels is 3 cells wide, so
 // a warp per task left most lanes idle).  A task whose doubling goes past that is left
 // for k_band_warp (raw_off stays RAW_FALLBACK), which starts its doubling over.
 __global__ void __launch_bounds__(128) k_band_small(SswTask* tasks, uint32_t n_tasks, const PrepRec* prep,
                                                     const uint8_t* arena, int32_t* hscratch, AlignScores sc,
-                                                    uint32_t* counters, uint32_t* warp_list) {
+                                                    uint32_t* counters, uint32_t* warp_list, const uint32_t* buckets,
+                                                    const uint32_t* bucket_n) {
     uint64_t computed = 0, canonical = 0;
-    for (uint32_t ti = blockIdx.x * blockDim.x + threadIdx.x; ti < n_tasks; ti += gridDim.x * blockDim.x) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t bucket = 1, i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (;;) {
+        // the next task: bucket by bucket, the threads striding through each
+        while (bucket <= (uint32_t)BAND_THREAD_MAX_BW && i >= bucket_n[bucket]) {
+            i -= bucket_n[bucket];
+            bucket++;
+        }
+        if (bucket > (uint32_t)BAND_THREAD_MAX_BW) break;
+        const uint32_t ti = buckets[(size_t)bucket * n_tasks + i];
+        i += stride;
         SswTask tk = tasks[ti];
-        if (tk.ref_begin1 < 0 || tk.read_begin1 < 0) continue;
         const PrepRec p = prep[tk.job];
         const uint8_t* q = arena + p.arena_off + tk.read_begin1;
         const uint8_t* r = arena + p.arena_off + p.qlen + tk.ref_begin1;
         const int rl = tk.ref_end1 - tk.ref_begin1 + 1, ql = tk.read_end1 - tk.read_begin1 + 1;
         const int len = rl > ql ? rl : ql;
         int bw = (rl > ql ? rl - ql : ql - rl) + 1;
-        if (bw > BAND_THREAD_MAX_BW) {
-            warp_list[atomicAdd(&counters[28], 1u)] = ti;
-            continue;
-        }
         // rows in the task's scratch as k_band_warp keeps them, the CIGAR after them
         uint32_t* rows = reinterpret_cast<uint32_t*>(hscratch + p.h_off);
         int mx = 0;
@@ -3281,8 +3303,14 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
             if (tblocks > sm_count() * 16) tblocks = sm_count() * 16;
             ws.band_list.reserve(n_tasks);
             ws.wide_list.reserve(n_tasks);
+            ws.band_buckets.reserve((size_t)(BAND_THREAD_MAX_BW + 1) * n_tasks + 8);
+            uint32_t* bucket_n = ws.band_buckets.p + (size_t)(BAND_THREAD_MAX_BW + 1) * n_tasks;
+            SA_CUDA(cudaMemsetAsync(bucket_n, 0, 8 * sizeof(uint32_t), st));
+            k_band_bucket<<<grid1(n_tasks), 256, 0, st>>>(ws.tasks.p, n_tasks, ws.band_buckets.p, bucket_n,
+                                                          ws.band_list.p, ws.counters.p);
             k_band_small<<<(unsigned)tblocks, 128, 0, st>>>(ws.tasks.p, n_tasks, ws.prep.p, ws.arena.p,
-                                                             ws.hscratch.p, sc, ws.counters.p, ws.band_list.p);
+                                                             ws.hscratch.p, sc, ws.counters.p, ws.band_list.p,
+                                                             ws.band_buckets.p, bucket_n);
             k_band_warp<<<(unsigned)blocks, 128, 0, st>>>(ws.tasks.p, ws.band_list.p, ws.prep.p, ws.arena.p,
                                                           ws.hscratch.p, sc, ws.counters.p, ws.wide_list.p);
             kt->end(st);

@@ -54,6 +54,7 @@ struct ExtWorkspace {
     DevBuf<int32_t> hscratch;
     DevBuf<SswTask> tasks;
     DevBuf<uint32_t> band_list, wide_list;  // tasks left by k_band_small / by k_band_warp
+    DevBuf<uint32_t> band_buckets;          // tasks by starting band width, then the counts
     DevBuf<uint32_t> counters;  // [0] n_tasks [1] n_word [2] n_rev_byte [3] n_rev_word [4] n_rescue, u64 cells at [8], u64 band cells at [24], band list sizes at [28] and [29]
     DevBuf<uint32_t> rescue_list;
     DevBuf<uint32_t> list_word, list_rev_byte, list_rev_word;
