@@ -845,6 +845,99 @@ __device__ void chain_extract(const uint64_t* dedup, const float* dp, const uint
     __syncwarp();
 }
 
+// extract_chains (src/chainer.rs:386-449) for the eight orientations of a grouped warp at
+// once: group g (lanes 4g .. 4g+3) collects its orientation's candidates, and its first
+// lane orders them (insertion into the sorted list: a stable sort by score, descending)
+// and walks the chains, so the eight walks' dependent loads overlap instead of running
+// one orientation after another.  nmax bounds every group's anchor count; sg == ~0u
+// marks a group without an orientation.
+__device__ void group_chain_extract(const uint64_t* dedup, const float* dp, const uint32_t* pred, uint32_t* aux,
+                                    uint64_t total_anchors, uint64_t b, uint32_t N, uint32_t nmax, uint32_t sg,
+                                    float best_score, const AnchorPack& ap, const ChainCtx& cc, NamRec* nam_out,
+                                    uint32_t* nam_seg_count, uint64_t* anc_out, uint64_t* anc_start) {
+    const uint32_t lane = lane_id(), gl = lane % 4, gsh = lane - gl;
+    const uint64_t qmask = (1ULL << ap.qbits) - 1, pmask = (1ULL << ap.pbits) - 1;
+    const bool has = sg != 0xffffffffu && N > 0;
+    const float valid_score = __fmul_rn(best_score, cc.cp.valid_score_threshold);
+    uint32_t* cand = aux + b;
+    uint32_t* sorted_c = aux + total_anchors + b;
+    uint32_t* used = aux + 2 * total_anchors + b;
+    uint32_t M = 0;
+    for (uint32_t c = 0; c < nmax; c += 4) {
+        const uint32_t i = c + gl;
+        const bool in = has && i < N;
+        const bool take = in && dp[b + i] >= valid_score;
+        const uint32_t bal = (__ballot_sync(FULL, take) >> gsh) & 15u;
+        if (take) cand[M + __popc(bal & ((1u << gl) - 1))] = i;
+        if (in) used[i] = 0;
+        M += __popc(bal);
+    }
+    __syncwarp();
+    if (has && gl == 0) {
+        // candidates arrive in anchor order; each goes after every entry scoring at least
+        // as much, so equal scores keep anchor order
+        for (uint32_t t = 0; t < M; t++) {
+            const uint32_t ci = cand[t];
+            const float sc = dp[b + ci];
+            uint32_t pos = t;
+            while (pos > 0 && dp[b + sorted_c[pos - 1]] < sc) {
+                sorted_c[pos] = sorted_c[pos - 1];
+                pos--;
+            }
+            sorted_c[pos] = ci;
+        }
+        uint32_t nn = 0;
+        NamRec* outp = nam_out + b;
+        uint64_t* ao = anc_out ? anc_out + 3 * b : nullptr;
+        uint32_t acur = 0;
+        for (uint32_t c = 0; c < M; c++) {
+            const uint32_t i = sorted_c[c];
+            if (used[i]) continue;
+            uint32_t j = i;
+            bool overlaps = false;
+            uint32_t nanch = 1;
+            const uint64_t ki = dedup[b + i];
+            if (ao) ao[acur] = ki;
+            uint32_t matching = cc.k;
+            uint32_t cov = (uint32_t)((ki >> ap.qbits) & pmask);
+            while (pred[b + j] != 0xffffffffu) {
+                j = pred[b + j];
+                if (used[j]) {
+                    overlaps = true;
+                    break;
+                }
+                const uint64_t kj = dedup[b + j];
+                if (ao) ao[acur + nanch] = kj;
+                nanch++;
+                used[j] = 1;
+                const uint32_t rsj = (uint32_t)((kj >> ap.qbits) & pmask);
+                const uint32_t d = cov > rsj ? cov - rsj : 0;
+                matching += d < cc.k ? d : cc.k;
+                cov = rsj;
+            }
+            if (overlaps) continue;
+            const uint64_t kf2 = dedup[b + j];
+            NamRec nr;
+            nr.nam_id = nn;
+            nr.query_start = (uint32_t)(kf2 & qmask);
+            nr.query_end = (uint32_t)(ki & qmask) + cc.k;
+            nr.ref_start = (uint32_t)((kf2 >> ap.qbits) & pmask);
+            nr.ref_end = (uint32_t)((ki >> ap.qbits) & pmask) + cc.k;
+            nr.matching_bases = matching;
+            nr.ref_id = (uint32_t)(ki >> (ap.pbits + ap.qbits));
+            nr.score = __fadd_rn(dp[b + i], __fmul_rn(__uint2float_rn(nanch), cc.cp.matches_weight));
+            nr.is_revcomp = sg & 1;
+            nr.n_anchors = nanch;
+            if (anc_start) anc_start[b + nn] = 3 * b + acur;
+            acur += nanch;
+            outp[nn++] = nr;
+        }
+        nam_seg_count[sg] = nn;
+    }
+    if (sg != 0xffffffffu && N == 0 && gl == 0) nam_seg_count[sg] = 0;
+    __syncwarp();
+}
+
 // The read orientations that have anchors (only the better orientation of a read gets
 // anchors, src/chainer.rs:205-216, so about half are empty), for k_chain4: those with
 // at most CHAIN_GROUP_MAX anchors in `list`, taken eight per warp, the others in
@@ -1427,6 +1520,11 @@ __global__ void __launch_bounds__(32 * CHAIN_WARPS, 8) k_chain4(const uint64_t* 
             }
             const float bs = __shfl_sync(FULL, best_score, (lane % NG) * CG);
             if (lane < NG) my_best = bs;
+            // the eight extractions side by side, a group each
+            __syncwarp();
+            group_chain_extract(dedup, dp, pred, aux, total_anchors, b, N, nmax, sg, best_score, ap, cc, nam_out,
+                                nam_seg_count, anc_out, anc_start);
+            continue;
         } else {
             // a long orientation (k_chain_long_prep and k_chain_big scored its clusters
             // without the re-check): the clusters whose maximum beats the running best,
