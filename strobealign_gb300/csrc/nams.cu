@@ -794,6 +794,17 @@ __device__ void chain_extract(const uint64_t* dedup, const float* dp, const uint
         warp_radix_sort_desc(cand, sorted_c, M, dp + b, hist);
     }
     __syncwarp();
+    // the walk's used flags: a bit each in the warp's shared counters (free after the
+    // sort) when they fit, else the global array
+    const bool bits = N <= 32 * 256;
+    if (bits)
+        for (uint32_t w = lane; w < (N + 31) / 32; w += 32) hist[w] = 0;
+    __syncwarp();
+    auto is_used = [&](uint32_t j) -> bool { return bits ? (hist[j >> 5] >> (j & 31)) & 1 : used[j] != 0; };
+    auto set_used = [&](uint32_t j) {
+        if (bits) hist[j >> 5] |= 1u << (j & 31);
+        else used[j] = 1;
+    };
     if (lane == 0) {
         uint32_t nn = 0;
         NamRec* outp = nam_out + b;
@@ -804,7 +815,7 @@ __device__ void chain_extract(const uint64_t* dedup, const float* dp, const uint
         uint32_t acur = 0;
         for (uint32_t c = 0; c < M; c++) {
             uint32_t i = sorted_c[c];
-            if (used[i]) continue;
+            if (is_used(i)) continue;
             uint32_t j = i;
             bool overlaps = false;
             uint32_t nanch = 1;
@@ -814,10 +825,10 @@ __device__ void chain_extract(const uint64_t* dedup, const float* dp, const uint
             uint32_t cov = (uint32_t)((ki >> ap.qbits) & pmask);
             while (pred[b + j] != 0xffffffffu) {
                 j = pred[b + j];
-                if (used[j]) { overlaps = true; break; }
+                if (is_used(j)) { overlaps = true; break; }
                 if (ao) ao[acur + nanch] = dedup[b + j];
                 nanch++;
-                used[j] = 1;
+                set_used(j);
                 uint32_t rsj = (uint32_t)((dedup[b + j] >> ap.qbits) & pmask);
                 uint32_t d = cov > rsj ? cov - rsj : 0;
                 matching += d < cc.k ? d : cc.k;
@@ -861,7 +872,6 @@ __device__ void group_chain_extract(const uint64_t* dedup, const float* dp, cons
     const float valid_score = __fmul_rn(best_score, cc.cp.valid_score_threshold);
     uint32_t* cand = aux + b;
     uint32_t* sorted_c = aux + total_anchors + b;
-    uint32_t* used = aux + 2 * total_anchors + b;
     uint32_t M = 0;
     for (uint32_t c = 0; c < nmax; c += 4) {
         const uint32_t i = c + gl;
@@ -869,10 +879,21 @@ __device__ void group_chain_extract(const uint64_t* dedup, const float* dp, cons
         const bool take = in && dp[b + i] >= valid_score;
         const uint32_t bal = (__ballot_sync(FULL, take) >> gsh) & 15u;
         if (take) cand[M + __popc(bal & ((1u << gl) - 1))] = i;
-        if (in) used[i] = 0;
         M += __popc(bal);
     }
     __syncwarp();
+    // used flags of the group's anchors (at most CHAIN_GROUP_MAX = 96) in three words
+    uint32_t u0 = 0, u1 = 0, u2 = 0;
+    auto is_used = [&](uint32_t j) -> bool {
+        const uint32_t w = j < 32 ? u0 : j < 64 ? u1 : u2;
+        return (w >> (j & 31)) & 1;
+    };
+    auto set_used = [&](uint32_t j) {
+        const uint32_t m = 1u << (j & 31);
+        if (j < 32) u0 |= m;
+        else if (j < 64) u1 |= m;
+        else u2 |= m;
+    };
     if (has && gl == 0) {
         // candidates arrive in anchor order; each goes after every entry scoring at least
         // as much, so equal scores keep anchor order
@@ -892,7 +913,7 @@ __device__ void group_chain_extract(const uint64_t* dedup, const float* dp, cons
         uint32_t acur = 0;
         for (uint32_t c = 0; c < M; c++) {
             const uint32_t i = sorted_c[c];
-            if (used[i]) continue;
+            if (is_used(i)) continue;
             uint32_t j = i;
             bool overlaps = false;
             uint32_t nanch = 1;
@@ -902,14 +923,14 @@ __device__ void group_chain_extract(const uint64_t* dedup, const float* dp, cons
             uint32_t cov = (uint32_t)((ki >> ap.qbits) & pmask);
             while (pred[b + j] != 0xffffffffu) {
                 j = pred[b + j];
-                if (used[j]) {
+                if (is_used(j)) {
                     overlaps = true;
                     break;
                 }
                 const uint64_t kj = dedup[b + j];
                 if (ao) ao[acur + nanch] = kj;
                 nanch++;
-                used[j] = 1;
+                set_used(j);
                 const uint32_t rsj = (uint32_t)((kj >> ap.qbits) & pmask);
                 const uint32_t d = cov > rsj ? cov - rsj : 0;
                 matching += d < cc.k ? d : cc.k;
@@ -1110,12 +1131,20 @@ __device__ __forceinline__ void chain_candidates(uint32_t j, bool in, const uint
 // best-index re-check (:150-165) is left out.
 template <bool RING>
 __device__ void warp_chain_range(const uint64_t* dedup, float* dp, uint32_t* pred, uint64_t b, uint32_t c0, uint32_t c1,
-                                 uint32_t max_ref_gap, const ChainCtx& cc, const AnchorPack& ap, uint64_t* ring_key,
-                                 float* ring_dp, bool recheck, float& best_score, uint32_t& best_index,
-                                 uint64_t& best_key) {
+                                 uint32_t floor, uint32_t max_ref_gap, const ChainCtx& cc, const AnchorPack& ap,
+                                 uint64_t* ring_key, float* ring_dp, bool recheck, float& best_score,
+                                 uint32_t& best_index, uint64_t& best_key) {
     const uint32_t lane = lane_id();
     const uint64_t qmask = (1ULL << ap.qbits) - 1, pmask = (1ULL << ap.pbits) - 1;
     const float kf = __uint2float_rn(cc.k);
+    if (RING && c0 > floor) {
+        // resuming inside a cluster: the ring takes the anchors before c0 from memory
+        for (uint32_t j = (c0 - floor > 64 ? c0 - 64 : floor) + lane; j < c0; j += 32) {
+            ring_key[j & 63] = dedup[b + j];
+            ring_dp[j & 63] = dp[b + j];
+        }
+        __syncwarp();
+    }
     uint64_t next_key = c0 < c1 ? dedup[b + c0] : 0;
     for (uint32_t i = c0; i < c1; i++) {
         const uint64_t ki = next_key;
@@ -1123,7 +1152,7 @@ __device__ void warp_chain_range(const uint64_t* dedup, float* dp, uint32_t* pre
         const uint32_t ri = (uint32_t)(ki >> (ap.pbits + ap.qbits)), rsi = (uint32_t)((ki >> ap.qbits) & pmask),
                        qi = (uint32_t)(ki & qmask);
         uint32_t lookup_end = i > cc.cp.max_lookback ? i - cc.cp.max_lookback : 0;
-        if (lookup_end < c0) lookup_end = c0;
+        if (lookup_end < floor) lookup_end = floor;
         float cur = kf;
         uint32_t cur_pred = 0xffffffffu;
         bool stop = false;
@@ -1202,6 +1231,82 @@ __device__ void warp_chain_range(const uint64_t* dedup, float* dp, uint32_t* pre
     }
 }
 
+// The first anchor of [lo, hi) (one cluster) where the best-index re-check
+// (src/chainer.rs:150-165) would change the DP values dp holds from scoring the cluster
+// without it; hi when there is none.  Up to that anchor both scorings agree, so the
+// running best (best_score / best_index / best_key, strict > updates as the reference
+// makes them) is a prefix maximum, taken 32 anchors at a time by a shuffle scan; the
+// re-check's test runs on every anchor at once.  On return the running best is the one
+// before the returned anchor.
+__device__ uint32_t recheck_first_fire(const uint64_t* dedup, const float* dp, uint64_t b, uint32_t lo, uint32_t hi,
+                                       uint32_t max_ref_gap, const ChainCtx& cc, const AnchorPack& ap,
+                                       float& best_score, uint32_t& best_index, uint64_t& best_key) {
+    const uint32_t lane = lane_id();
+    const uint64_t qmask = (1ULL << ap.qbits) - 1, pmask = (1ULL << ap.pbits) - 1;
+    for (uint32_t c = lo; c < hi; c += 32) {
+        const uint32_t i = c + lane;
+        const bool in = i < hi;
+        const float d = in ? dp[b + i] : -INFINITY;
+        const uint64_t k = in ? dedup[b + i] : 0;
+        // inclusive prefix (maximum, first index reaching it) over the lanes
+        float pv = d;
+        uint32_t pi = i;
+        for (uint32_t s = 1; s < 32; s <<= 1) {
+            const float v2 = __shfl_up_sync(FULL, pv, s);
+            const uint32_t i2 = __shfl_up_sync(FULL, pi, s);
+            if (lane >= s && v2 >= pv) {
+                pv = v2;
+                pi = i2;
+            }
+        }
+        // the running best before anchor i: the carry, then lanes < lane
+        float ev = __shfl_up_sync(FULL, pv, 1);
+        uint32_t ei = __shfl_up_sync(FULL, pi, 1);
+        if (lane == 0) ev = -INFINITY;
+        float bs = best_score;
+        uint32_t bi = best_index;
+        bool from_chunk = false;
+        if (ev > bs) {
+            bs = ev;
+            bi = ei;
+            from_chunk = true;
+        }
+        const uint64_t kc = __shfl_sync(FULL, k, from_chunk ? ei - c : 0);
+        const uint64_t bk = from_chunk ? kc : best_key;
+        bool fire = false;
+        if (in && bi != 0xffffffffu) {
+            const uint32_t ri = (uint32_t)(k >> (ap.pbits + ap.qbits)), rsi = (uint32_t)((k >> ap.qbits) & pmask),
+                           qi = (uint32_t)(k & qmask);
+            const uint32_t rb = (uint32_t)(bk >> (ap.pbits + ap.qbits)), rsb = (uint32_t)((bk >> ap.qbits) & pmask),
+                           qb = (uint32_t)(bk & qmask);
+            if (rb == ri && qi > qb) {
+                const uint32_t dq = qi - qb, dr = rsi - rsb;
+                const uint32_t mx = dq > dr ? dq : dr, mn = dq < dr ? dq : dr;
+                if (dr < max_ref_gap && dr > 0 && !ratio_above(mx, mn, cc))
+                    fire = __fadd_rn(bs, chain_score(dq, dr, cc)) > d;
+            }
+        }
+        const uint32_t fb = __ballot_sync(FULL, fire);
+        if (fb) {
+            const int f = __ffs(fb) - 1;
+            best_score = __shfl_sync(FULL, bs, f);
+            best_index = __shfl_sync(FULL, bi, f);
+            best_key = __shfl_sync(FULL, bk, f);
+            return c + (uint32_t)f;
+        }
+        // the whole chunk: carry its maximum on
+        const float v31 = __shfl_sync(FULL, pv, 31);
+        const uint32_t i31 = __shfl_sync(FULL, pi, 31);
+        const uint64_t k31 = __shfl_sync(FULL, k, (i31 - c) & 31);
+        if (v31 > best_score) {
+            best_score = v31;
+            best_index = i31;
+            best_key = k31;
+        }
+    }
+    return hi;
+}
+
 // The same for a small cluster [c0, c1) by one thread, without the re-check; returns
 // the cluster's maximum.
 __device__ float lane_chain_range(const uint64_t* dedup, float* dp, uint32_t* pred, uint64_t b, uint32_t c0,
@@ -1276,15 +1381,17 @@ __device__ __forceinline__ uint32_t orientation_dedup(const uint64_t* sorted, ui
 // without contributing), so a cluster's DP depends on the others only through the
 // best-index re-check (src/chainer.rs:150-165), which can fire only once the cluster
 // holds the running best, a strict maximum over all earlier anchors.  So the clusters
-// are scored at once without the re-check, here, and k_chain4 then scores again, in
-// order, each cluster whose maximum beats the running best of the clusters before it
-// (with the re-check, carrying the running best on); the others are final.
+// are scored at once without the re-check, here, and k_chain4 then takes, in order, each
+// cluster whose maximum beats the running best of the clusters before it, finds the
+// first anchor where the re-check fires and scores again from there (carrying the
+// running best on); the others are final.
 //
 // k_chain_long_prep: a warp per long orientation u: the dedup, the cluster starts
-// (aux[b ..]), and the clusters of up to lane_max anchors scored a
-// thread each (maxima at aux[T + b ..] as floats); the larger ones (except the first,
-// which k_chain4 scores with the re-check anyway) are queued as (u, cluster) items for
+// (aux[b ..]), and the clusters of up to lane_max anchors scored a thread each (maxima
+// at aux[T + b ..] as floats); the larger ones are queued as (u, cluster) items for
 // k_chain_big, a warp each.  long_n[u] / long_c[u]: anchors after dedup, clusters.
+// k_chain4 then checks each record cluster for the first anchor where the re-check
+// fires (recheck_first_fire) and scores again from there only.
 __global__ void __launch_bounds__(128) k_chain_long_prep(const uint64_t* __restrict__ off, const uint64_t* seg_off,
                                                          const uint64_t* sorted, uint64_t* dedup, float* dp,
                                                          uint32_t* pred, uint32_t* aux, uint64_t total_anchors,
@@ -1324,7 +1431,7 @@ __global__ void __launch_bounds__(128) k_chain_long_prep(const uint64_t* __restr
         for (uint32_t c0 = 0; c0 < C; c0 += 32) {
             const uint32_t c = c0 + lane;
             bool big = false;
-            if (c < C && c > 0) {
+            if (c < C) {
                 const uint32_t lo = cstart[c], hi = c + 1 < C ? cstart[c + 1] : N;
                 big = hi - lo > lane_max;
                 if (!big) cmax[c] = lane_chain_range(dedup, dp, pred, b, lo, hi, max_ref_gap, cc, ap);
@@ -1372,8 +1479,9 @@ __global__ void __launch_bounds__(128) k_chain_big(const uint64_t* __restrict__ 
         float mx = 0.0f;
         uint32_t bi = 0xffffffffu;
         uint64_t bk = 0;
-        warp_chain_range<RING>(dedup, dp, pred, b, lo, hi, max_ref_gap, cc, ap, ring_key_s + (RING ? wib * 64 : 0),
-                               ring_dp_s + (RING ? wib * 64 : 0), false, mx, bi, bk);
+        warp_chain_range<RING>(dedup, dp, pred, b, lo, hi, lo, max_ref_gap, cc, ap,
+                               ring_key_s + (RING ? wib * 64 : 0), ring_dp_s + (RING ? wib * 64 : 0), false, mx, bi,
+                               bk);
         if (lane == 0) reinterpret_cast<float*>(aux + total_anchors + b)[c] = mx;
         __syncwarp();
     }
@@ -1554,8 +1662,13 @@ __global__ void __launch_bounds__(32 * CHAIN_WARPS, 8) k_chain4(const uint64_t* 
                         if (!bal) break;
                         const uint32_t l = __ffs(bal) - 1, cc0 = c0 + l;
                         const uint32_t lo = cstart[cc0], hi = cc0 + 1 < C ? cstart[cc0 + 1] : N;
-                        warp_chain_range<RING>(dedup, dp, pred, b, lo, hi, max_ref_gap, cc, ap, ring_key, ring_dp,
-                                               true, best_score, best_index, best_key);
+                        // the values scored without the re-check stand up to the first
+                        // anchor where it would fire; only the rest is scored again
+                        const uint32_t i0 = recheck_first_fire(dedup, dp, b, lo, hi, max_ref_gap, cc, ap, best_score,
+                                                               best_index, best_key);
+                        if (i0 < hi)
+                            warp_chain_range<RING>(dedup, dp, pred, b, i0, hi, lo, max_ref_gap, cc, ap, ring_key,
+                                                   ring_dp, true, best_score, best_index, best_key);
                         from = l + 1;
                     }
                 }
