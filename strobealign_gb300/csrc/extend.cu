@@ -2847,12 +2847,15 @@ __global__ void __launch_bounds__(32) k_piecewise(const uint32_t* __restrict__ l
             const int qd = cqs - pqe, rd = crs - prre;
             if (rd > 0 && qd > 0) {
                 if (rd == qd) {
-                    // hamming_align_global, taken if it scores above 85% of all matches
-                    const int hsc = hamming_global_score(q + pqe, dref + prre, qd, sc);
+                    // hamming_align_global, taken if it scores above 85% of all matches;
+                    // the comparisons 32 at a time by ballot
+                    const int gmm = (int)warp_mismatches(q, dref, (uint32_t)pqe, (uint32_t)prre, (uint32_t)qd, 1);
+                    const int hraw = (int)sc.match * (qd - gmm) - (int)sc.mismatch * gmm;
+                    const int hsc = hraw > 0 ? hraw : 0;
                     const uint32_t thr = (uint32_t)ceilf(__fmul_rn((float)qd, 0.85f));
                     if (hsc > 0 && (uint32_t)hsc > (uint32_t)sc.match * thr) {
                         score += hsc;
-                        for (int x = 0; x < qd; x++) push(q[pqe + x] == dref[prre + x] ? 7u : 8u, 1);
+                        warp_eq_runs(q, dref, (uint32_t)pqe, (uint32_t)prre, (uint32_t)qd, w);
                         score += K * (int)sc.match;
                         push(7, K);
                         continue;
