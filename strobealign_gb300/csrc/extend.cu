@@ -2778,16 +2778,23 @@ __device__ __forceinline__ int hamming_global_score(const uint8_t* q, const uint
     return hs > 0 ? hs : 0;
 }
 
+// The DP rows of a piece live in shared memory when the piece is at most smem_w - 1
+// columns wide (PW_SMEM_W: small enough that 32 single-warp blocks fit on an SM), else in
+// the block's slice of global scratch.
+constexpr uint32_t PW_SMEM_W = 256;
 __global__ void __launch_bounds__(32) k_piecewise(const uint32_t* __restrict__ list, const uint32_t* n_list_ptr,
                                                   const ExtJob* jobs, const PrepRec* prep, const uint8_t* arena,
                                                   const uint32_t* __restrict__ anchors, AlignScores sc, uint32_t k,
                                                   uint8_t* scratch, uint64_t cells_bytes, uint64_t ops_bytes,
-                                                  uint32_t* cigar, ExtResult* res, uint32_t* counters) {
+                                                  uint64_t rows_bytes, uint32_t smem_w, uint32_t* cigar,
+                                                  ExtResult* res, uint32_t* counters) {
     extern __shared__ int pw_rows[];
     const int lane = threadIdx.x & 31;
     const uint32_t n_list = *n_list_ptr;
-    uint8_t* dirs = scratch + (size_t)blockIdx.x * (cells_bytes + ops_bytes);
+    uint8_t* dirs = scratch + (size_t)blockIdx.x * (cells_bytes + ops_bytes + rows_bytes);
     uint8_t* ops = dirs + cells_bytes;
+    int* grows = reinterpret_cast<int*>(ops + ops_bytes);
+    auto rows_for = [&](int m) { return (uint32_t)m + 1 <= smem_w ? pw_rows : grows; };
     for (;;) {
         uint32_t li = 0;
         if (lane == 0) li = atomicAdd(&counters[22], 1u);
@@ -2823,7 +2830,7 @@ __global__ void __launch_bounds__(32) k_piecewise(const uint32_t* __restrict__ l
         int pre_qs, pre_rs, score;
         if (fqs > 0 && frs > 0) {
             const int rs = frs > fqs + padding ? frs - (fqs + padding) : 0;
-            const PwPiece pc = pw_dp<true, true>(q, fqs, dref + rs, frs - rs, sc, pw_rows, dirs, ops);
+            const PwPiece pc = pw_dp<true, true>(q, fqs, dref + rs, frs - rs, sc, rows_for(frs - rs), dirs, ops);
             if (pc.score == 0) {
                 pre_qs = fqs;
                 pre_rs = frs;
@@ -2861,7 +2868,7 @@ __global__ void __launch_bounds__(32) k_piecewise(const uint32_t* __restrict__ l
                         continue;
                     }
                 }
-                const PwPiece pc = pw_dp<false, false>(q + pqe, qd, dref + prre, rd, sc, pw_rows, dirs, ops);
+                const PwPiece pc = pw_dp<false, false>(q + pqe, qd, dref + prre, rd, sc, rows_for(rd), dirs, ops);
                 score += pc.score;
                 for (int x = pc.nops; x-- > 0;) push(ops[x], 1);
                 score += K * (int)sc.match;
@@ -2892,7 +2899,8 @@ __global__ void __launch_bounds__(32) k_piecewise(const uint32_t* __restrict__ l
         if (lqe < L && lre < RL) {
             const int qlen2 = L - lqe;
             const int re = lre + qlen2 + padding < RL ? lre + qlen2 + padding : RL;
-            const PwPiece pc = pw_dp<true, false>(q + lqe, qlen2, dref + lre, re - lre, sc, pw_rows, dirs, ops);
+            const PwPiece pc = pw_dp<true, false>(q + lqe, qlen2, dref + lre, re - lre, sc, rows_for(re - lre), dirs,
+                                                  ops);
             if (pc.score == 0) {
                 post_qe = lqe;
                 post_re = lre;
@@ -3161,11 +3169,15 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
         auto a16 = [](uint64_t x) { return (x + 15) & ~(uint64_t)15; };
         const uint64_t cells = a16(((uint64_t)max_qlen + 1) * ((uint64_t)max_pw_window + 1));
         const uint64_t opsb = a16((uint64_t)max_qlen + max_pw_window + 8) + a16(8ull * (max_anchors + 1));
-        // single-warp blocks, up to 16 per SM: the per-job work is mostly serial (anchor
-        // pruning, gap checks, traceback pushes), so more resident warps hide its latency
-        const unsigned blocks = (unsigned)std::min<uint64_t>(n, sm_count() * 16);
-        ws.pw_scratch.reserve((cells + opsb) * blocks);
-        const size_t smem = 16 * ((size_t)max_pw_window + 2);
+        // single-warp blocks, 28 per SM (the registers of 28 fit): the per-job work is
+        // mostly serial (anchor pruning, gap checks, traceback pushes, a row at a time), so
+        // more resident warps hide its latency; the rows of wide pieces go to global
+        // scratch so that the shared rows stay small
+        const unsigned blocks = (unsigned)std::min<uint64_t>(n, sm_count() * 28);
+        const uint64_t rowsb = a16(16ull * ((uint64_t)max_pw_window + 2));
+        ws.pw_scratch.reserve((cells + opsb + rowsb) * blocks);
+        const uint32_t smem_w = (uint32_t)std::min<uint64_t>((uint64_t)max_pw_window + 2, PW_SMEM_W);
+        const size_t smem = 16 * (size_t)smem_w;
         static size_t attr = 0;
         if (smem > attr) {
             SA_CUDA(cudaFuncSetAttribute(k_piecewise, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -3173,8 +3185,8 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
         }
         kt->begin(KS_EXT_OTHER, st);
         k_piecewise<<<blocks, 32, smem, st>>>(ws.pw_list.p, ws.counters.p + 19, ws.jobs.p, ws.prep.p, ws.arena.p,
-                                              anchors, sc, k, ws.pw_scratch.p, cells, opsb, ws.cigar.p, ws.results.p,
-                                              ws.counters.p);
+                                              anchors, sc, k, ws.pw_scratch.p, cells, opsb, rowsb, smem_w,
+                                              ws.cigar.p, ws.results.p, ws.counters.p);
         kt->end(st);
         launches++;
     }
@@ -3556,13 +3568,14 @@ void stage_piecewise(uint32_t n, const uint8_t* q, const uint64_t* qo, const uin
     const uint64_t cells = a16((max_q + 1) * (max_w + 1));
     const uint64_t opsb = a16(max_q + max_w + 8) + a16(8ull * (max_a + 1));
     const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(n, 1024));
-    d_scratch.reserve((cells + opsb) * blocks);
-    const size_t smem = 16 * ((size_t)max_w + 2);
-    if (smem > 48 * 1024)
-        SA_CUDA(cudaFuncSetAttribute(k_piecewise, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const uint64_t rowsb = a16(16ull * (max_w + 2));
+    d_scratch.reserve((cells + opsb + rowsb) * blocks);
+    const uint32_t smem_w = (uint32_t)std::min<uint64_t>(max_w + 2, PW_SMEM_W);
+    const size_t smem = 16 * (size_t)smem_w;
     if (n)
         k_piecewise<<<blocks, 32, smem, st>>>(d_list.p, d_counters.p + 19, d_jobs.p, d_prep.p, d_arena.p, d_anc.p, sc,
-                                              k, d_scratch.p, cells, opsb, d_cigar.p, d_res.p, d_counters.p);
+                                              k, d_scratch.p, cells, opsb, rowsb, smem_w, d_cigar.p, d_res.p,
+                                              d_counters.p);
     SA_CUDA(cudaGetLastError());
     std::vector<ExtResult> res(std::max<uint32_t>(n, 1));
     std::vector<uint32_t> hc(cig + 1);
