@@ -437,14 +437,14 @@ int32_t sa_mapper_get_stats(const sa_mapper* m, sa_mapper_stats* out);
 int32_t sa_mapper_set_profiling(sa_mapper* m, int32_t enable);
 /* Parts a large batch is cut into (runs of whole chunks, at least 4 chunks each): the
  * NAM pipeline of one part runs while the earlier parts are extended and written.
- * Output bytes do not depend on it.  Default 4; batches of more than 2^27 bases get
+ * Output bytes do not depend on it.  Default 8; batches of more than 2^27 bases get
  * as many parts as hold at most 2^27 bases each. */
 int32_t sa_mapper_set_parts(sa_mapper* m, uint32_t parts);
 
 /* How a batch is scheduled on the device and the host.  No counterpart in the
  * reference (it maps chunks on CPU threads); output bytes never depend on it.
  *   parts          NAM-pipeline parts (runs of whole chunks, at least 4 chunks each);
- *                  0 = 4.  Batches of more than 2^27 bases get more parts, so that a
+ *                  0 = 8.  Batches of more than 2^27 bases get more parts, so that a
  *                  part holds at most 2^27 bases.  With overlap, part p + 1's pipeline
  *                  runs while earlier parts are extended.
  *   overlap        1 (default): continuous batching -- policy threads run the chunks

@@ -498,10 +498,11 @@ class Mapper:
         """NAM-pipeline parts a large batch is cut into (output does not depend on it)."""
         L.check(lib().sa_mapper_set_parts(self.h, parts))
 
-    def set_schedule(self, parts: int = 4, overlap: bool = True, wave_min_jobs: int = 0,
+    def set_schedule(self, parts: int = 0, overlap: bool = True, wave_min_jobs: int = 0,
                      max_wave_jobs: int = 0) -> None:
         """Batch scheduling (sa_mapper_set_schedule); output bytes do not depend on it.
-        overlap=False with parts=1 is the plain, stage-synchronous form."""
+        parts=0 takes the library's default (8); overlap=False is the plain,
+        stage-synchronous form."""
         sp = L.ScheduleParams()
         lib().sa_schedule_params_default(C.byref(sp))
         sp.parts = parts

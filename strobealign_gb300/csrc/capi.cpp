@@ -430,7 +430,7 @@ int32_t sa_mapper_set_parts(sa_mapper* m, uint32_t parts) {
 
 void sa_schedule_params_default(sa_schedule_params* p) {
     if (!p) return;
-    p->parts = 4;
+    p->parts = 8;
     p->overlap = 1;
     p->wave_min_jobs = 32768;
     p->max_wave_jobs = 262144;
@@ -440,7 +440,7 @@ int32_t sa_mapper_set_schedule(sa_mapper* m, const sa_schedule_params* p) {
     SA_TRY
     require(m && p, "null argument");
     require(p->overlap <= 1, "overlap must be 0 or 1");
-    m->m->set_parts(p->parts ? p->parts : 4);
+    m->m->set_parts(p->parts ? p->parts : 8);
     m->m->set_overlap(p->overlap != 0);
     m->m->set_wave_min_jobs(p->wave_min_jobs ? p->wave_min_jobs : 32768);
     m->m->set_max_wave_jobs(p->max_wave_jobs ? p->max_wave_jobs : 262144);

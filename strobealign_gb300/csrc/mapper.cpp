@@ -758,7 +758,7 @@ Mapper::TuneReport Mapper::autotune(const sa_read_batch* r1, const sa_read_batch
             }
         }
     };
-    knob(&Tuning::parts, {2, 8, 16});
+    knob(&Tuning::parts, {2, 4, 16});
     knob(&Tuning::max_wave_jobs, {65536, 131072, 524288});
     knob(&Tuning::wave_min_jobs, {8192, 131072});
     if (max_qlen_ > 128) knob(&Tuning::wave_qmax, {128, 160});

@@ -49,7 +49,7 @@ class Mapper {
     void set_overlap(bool on) { overlap_ = on; }
     // output-invariant knobs the autotuner chooses
     struct Tuning {
-        uint32_t parts = 4;
+        uint32_t parts = 8;
         uint64_t wave_min_jobs = 32768, max_wave_jobs = 262144;
         uint32_t wave_qmax = 192, chain_lane_max = 48;
         uint32_t l2_fetch = 0;  // 0: the context's value at construction
@@ -129,7 +129,7 @@ class Mapper {
     PinnedBuf<ExtJob> h_jobs_;
     std::vector<std::unique_ptr<Part>> parts_;  // grow-only; pinned buffers reused across batches
     size_t n_parts_ = 0;
-    uint32_t parts_target_ = 4;
+    uint32_t parts_target_ = 8;
     NamWorkspace pws_;            // NAM pipeline buffers of one part
     PinnedBuf<uint64_t> h_poff_;  // a part's local read offsets
     double t_nams_ = 0;

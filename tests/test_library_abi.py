@@ -44,10 +44,10 @@ def test_version_and_defaults_without_gpu():
     assert (sp.max_inflight_bases, sp.max_inflight_requests, sp.policy_threads, sp.admission_streams,
             sp.borrow_inputs, sp.device_reserve_bytes) == (0, 0, 0, 2, 0, 0)
     assert ctypes.sizeof(L.SessionParams) == 32
-    # batch schedule defaults: four NAM parts, overlapped
+    # batch schedule defaults: eight NAM parts, overlapped
     sc = L.ScheduleParams()
     sa.lib().sa_schedule_params_default(ctypes.byref(sc))
-    assert (sc.parts, sc.overlap, sc.wave_min_jobs, sc.max_wave_jobs) == (4, 1, 32768, 262144)
+    assert (sc.parts, sc.overlap, sc.wave_min_jobs, sc.max_wave_jobs) == (8, 1, 32768, 262144)
 
 
 def test_synthetic_generator_is_deterministic():
