@@ -125,8 +125,13 @@ StreamResult map_files(Mapper& m, const std::string& reads1, const std::string* 
         out = std::fopen(out_path.c_str(), cfg.append ? "ab" : "wb");
         if (!out) throw Error(SA_ERR_IO, "cannot open " + out_path + " for writing: " + std::strerror(errno));
     }
-    std::vector<char> obuf((size_t)8 << 20);
-    std::setvbuf(out, obuf.data(), _IOFBF, obuf.size());
+    // a large buffer for a file this call opened (standard output keeps its own: a
+    // buffer installed there would outlive this call)
+    std::vector<char> obuf;
+    if (out != stdout) {
+        obuf.resize((size_t)8 << 20);
+        std::setvbuf(out, obuf.data(), _IOFBF, obuf.size());
+    }
     auto close_out = [&]() {
         if (out && out != stdout) std::fclose(out);
         else if (out) std::fflush(out);
