@@ -137,6 +137,14 @@ StreamResult map_files(Mapper& m, const std::string& reads1, const std::string* 
         else if (out) std::fflush(out);
         out = nullptr;
     };
+    // closes the file on any early exit, before its buffer goes
+    struct OutGuard {
+        std::FILE*& f;
+        ~OutGuard() {
+            if (f && f != stdout) std::fclose(f);
+            else if (f) std::fflush(f);
+        }
+    } guard{out};
 
     StreamResult res;
     BoundedQueue<std::unique_ptr<InBatch>> inq(cfg.read_ahead ? cfg.read_ahead : 2);
