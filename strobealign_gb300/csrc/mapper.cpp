@@ -707,6 +707,19 @@ Mapper::Tuning Mapper::tuning() const {
 }
 
 Mapper::TuneReport Mapper::autotune(const sa_read_batch* r1, const sa_read_batch* r2, uint32_t rounds) {
+    const Tuning before = tuning();
+    const bool saved_overlap = overlap_;
+    try {
+        return autotune_run(r1, r2, rounds);
+    } catch (...) {
+        // a failed tuning leaves the mapper as it found it
+        overlap_ = saved_overlap;
+        set_tuning(before);
+        throw;
+    }
+}
+
+Mapper::TuneReport Mapper::autotune_run(const sa_read_batch* r1, const sa_read_batch* r2, uint32_t rounds) {
     rounds = std::max<uint32_t>(1, rounds);
     const bool saved_overlap = overlap_;
     overlap_ = true;

@@ -68,6 +68,11 @@ class Mapper {
     TuneReport autotune(const sa_read_batch* r1, const sa_read_batch* r2, uint32_t rounds);
 
   private:
+    TuneReport autotune_run(const sa_read_batch* r1, const sa_read_batch* r2, uint32_t rounds);
+
+  public:
+
+  private:
     // One NAM-pipeline part of a batch: a run of whole chunks with their reads' NAMs on
     // the host, and the part's own read view and result store (read and record indices
     // local to the part).  The NAM pipeline of part p + 1 runs while the chunks of

@@ -100,3 +100,19 @@ def test_gzip_errors(sa, tmp_path):
     assert len(sa.Reads.from_file(str(e))) == 0
     with pytest.raises(sa.SaError, match="cannot open"):
         sa.Reads.from_file(str(tmp_path / "missing.fq.gz"))
+
+
+def test_reads_from_standard_input(tmp_path):
+    # "-" reads standard input (src/io/xopen.rs:11-12)
+    import subprocess
+    import sys
+    from conftest import ROOT
+    src = GOLDEN / "phix.1.fastq"
+    code = ("import sys; sys.path.insert(0, %r); import strobealign_gb300 as sa; r = sa.Reads.from_file('-'); "
+            "print(len(r), len(r.seq))" % str(ROOT))
+    with open(src, "rb") as f:
+        out = subprocess.run([sys.executable, "-c", code], stdin=f, capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    import strobealign_gb300 as sa
+    want = sa.Reads.from_file(str(src))
+    assert out.stdout.split() == [str(len(want)), str(len(want.seq))]
