@@ -18,6 +18,8 @@
 //               extension of Aligner::align
 #include <cub/cub.cuh>
 
+#include <type_traits>
+
 #include "extend.h"
 
 namespace sa {
@@ -1198,10 +1200,15 @@ constexpr int WV_SCALE = 8;  // log2 of the score scale (rows < 256)
 struct WaveScores {
     int gO, gE;  // scaled
 };
+// the default gap penalties (12, 1) as constants: the per-row offsets of the lazy-F
+// raise become immediates and the penalties leave the registers
+struct DefaultWaveScores {
+    static constexpr int gO = 12 << WV_SCALE, gE = 1 << WV_SCALE;
+};
 
-template <int N, bool BYTE>
+template <int N, bool BYTE, class WS>
 __device__ __forceinline__ EndPos wave_loop(const uint8_t* r, int rlen, bool r_rev, int qlen, bool check_term,
-                                            int terminate, int bias, WaveScores ws, const uint4* prof, int gl,
+                                            int terminate, int bias, WS ws, const uint4* prof, int gl,
                                             unsigned m, bool run) {
     constexpr int NW = (N + 7) / 8;
     int H[N], E[N];
@@ -1316,7 +1323,7 @@ __device__ __forceinline__ EndPos wave_loop(const uint8_t* r, int rlen, bool r_r
 // per thread.  All 32 threads enter together.  When the running groups share N, the
 // warp runs them in lockstep (full-warp shuffles and votes); otherwise each group runs
 // on its own with its own mask.
-template <int NMAX, bool BYTE>
+template <int NMAX, bool BYTE, bool DEF>
 __device__ __forceinline__ EndPos wave_pass(bool run, const uint8_t* q, int qlen, bool q_rev, const uint8_t* r, int rlen,
                             bool r_rev, bool check_term, int terminate, const AlignScores& sc, int bias, uint4* prof,
                             int gl, unsigned gm) {
@@ -1356,13 +1363,15 @@ __device__ __forceinline__ EndPos wave_pass(bool run, const uint8_t* q, int qlen
                 prof[(b * nw + w) * 32] = make_uint4(v[0], v[1], v[2], v[3]);
             }
     }
-    const WaveScores ws{(int)sc.gap_open << WV_SCALE, (int)sc.gap_extend << WV_SCALE};
+    using WS = std::conditional_t<DEF, DefaultWaveScores, WaveScores>;
+    WS ws{};
+    if constexpr (!DEF) ws = WaveScores{(int)sc.gap_open << WV_SCALE, (int)sc.gap_extend << WV_SCALE};
     EndPos res = z;
     // byte mode: N is even, so the odd cases are never taken there
 #define SA_WV(K)                                                                                                 \
     case K:                                                                                                      \
         if constexpr (K <= NMAX && (!BYTE || K % 2 == 0))                                                        \
-            res = wave_loop<K, BYTE>(r, rlen, r_rev, qlen, check_term, terminate, bias, ws, prof, gl, m, run);   \
+            res = wave_loop<K, BYTE, WS>(r, rlen, r_rev, qlen, check_term, terminate, bias, ws, prof, gl, m, run); \
         break;
     switch (NN) {
         SA_WV(1) SA_WV(2) SA_WV(3) SA_WV(4) SA_WV(5) SA_WV(6) SA_WV(7) SA_WV(8)
@@ -1432,7 +1441,7 @@ __device__ __forceinline__ int wave_diag_bound(bool run, const uint8_t* q, int q
 // the longest-first order of k_ssw: each warp takes four consecutive tasks (one per
 // group of eight threads) and runs the forward byte pass, the forward word pass of the
 // tasks that overflowed, then the reverse passes in each task's mode.
-template <int NMAX>
+template <int NMAX, bool DEF>
 __global__ void __launch_bounds__(128, NMAX <= 20 ? 5 : 4) k_ssw_wave(SswTask* tasks, const uint32_t* order, uint32_t n_tasks,
                                                       const PrepRec* prep, const uint8_t* arena, AlignScores sc,
                                                       int bias, uint32_t* counters, uint32_t qmax) {
@@ -1472,10 +1481,10 @@ __global__ void __launch_bounds__(128, NMAX <= 20 ? 5 : 4) k_ssw_wave(SswTask* t
         if (__any_sync(FULLM, try_bound))
             certain = wave_diag_bound(try_bound, q, qlen, r, wlen, (int)d0, sc, gl) >= 255 - bias;
         // forward: byte, word on overflow (ext/ssw/ssw.c:840-862)
-        EndPos e = wave_pass<NMAX, true>(have && !certain, q, qlen, false, r, wlen, false, false, 0, sc, bias, prof, gl,
+        EndPos e = wave_pass<NMAX, true, DEF>(have && !certain, q, qlen, false, r, wlen, false, false, 0, sc, bias, prof, gl,
                                          gm);
         const bool word = have && (certain || e.score == 255);
-        const EndPos ew = wave_pass<NMAX, false>(word, q, qlen, false, r, wlen, false, false, 0, sc, bias, prof, gl,
+        const EndPos ew = wave_pass<NMAX, false, DEF>(word, q, qlen, false, r, wlen, false, false, 0, sc, bias, prof, gl,
                                                  gm);
         unsigned long long c_fb = certain ? 0 : (unsigned long long)qlen * e.cols, c_fw = 0, c_rb = 0, c_rw = 0;
         if (word) {
@@ -1484,9 +1493,9 @@ __global__ void __launch_bounds__(128, NMAX <= 20 ? 5 : 4) k_ssw_wave(SswTask* t
         }
         // reverse pass over read[0..=read_end1] and ref[0..=ref_end1] (ext/ssw/ssw.c:870-888)
         const bool rev = have && e.ref >= 0;
-        const EndPos bb = wave_pass<NMAX, true>(rev && !word, q, e.read + 1, true, r, e.ref + 1, true, true, e.score,
+        const EndPos bb = wave_pass<NMAX, true, DEF>(rev && !word, q, e.read + 1, true, r, e.ref + 1, true, true, e.score,
                                                 sc, bias, prof, gl, gm);
-        const EndPos bw = wave_pass<NMAX, false>(rev && word, q, e.read + 1, true, r, e.ref + 1, true, true, e.score,
+        const EndPos bw = wave_pass<NMAX, false, DEF>(rev && word, q, e.read + 1, true, r, e.ref + 1, true, true, e.score,
                                                  sc, bias, prof, gl, gm);
         EndPos b = word ? bw : bb;
         if (!rev) {
@@ -3282,12 +3291,15 @@ uint32_t run_extension_raw(const DevRefs& refs, const uint8_t* seq, const uint64
                 const bool short_reads = std::min<uint32_t>(max_qlen, wave_qmax) <= 8 * WAVE_NMAX_SHORT;
                 const int nmax = short_reads ? WAVE_NMAX_SHORT : WAVE_NMAX;
                 const size_t smem = (size_t)wpb * 5 * ((nmax + 7) / 8) * 32 * sizeof(uint4);
-                if (short_reads)
-                    k_ssw_wave<WAVE_NMAX_SHORT><<<(unsigned)wblocks, tpb, smem, st>>>(
-                        ws.tasks.p, ws.order.p, n_tasks, ws.prep.p, ws.arena.p, sc, bias, ws.counters.p, wave_qmax);
-                else
-                    k_ssw_wave<WAVE_NMAX><<<(unsigned)wblocks, tpb, smem, st>>>(
-                        ws.tasks.p, ws.order.p, n_tasks, ws.prep.p, ws.arena.p, sc, bias, ws.counters.p, wave_qmax);
+                const bool def_gaps = sc.gap_open == 12 && sc.gap_extend == 1;
+#define SA_SSWW(NM, DF)                                                                                      \
+    k_ssw_wave<NM, DF><<<(unsigned)wblocks, tpb, smem, st>>>(ws.tasks.p, ws.order.p, n_tasks, ws.prep.p,   \
+                                                             ws.arena.p, sc, bias, ws.counters.p, wave_qmax)
+                if (short_reads && def_gaps) SA_SSWW(WAVE_NMAX_SHORT, true);
+                else if (short_reads) SA_SSWW(WAVE_NMAX_SHORT, false);
+                else if (def_gaps) SA_SSWW(WAVE_NMAX, true);
+                else SA_SSWW(WAVE_NMAX, false);
+#undef SA_SSWW
             }
 #undef SA_SSW
             kt->end(st);
