@@ -524,24 +524,6 @@ void best_scoring_nam_pairs(const std::vector<NamRec>& n1, const std::vector<Nam
     stable_sort_small(pairs, [](const NamPair& a, const NamPair& b) { return a.score > b.score; });
 }
 
-void add_details(Details& a, const Details& b) {
-    a.nam.full_not_found += b.nam.full_not_found;
-    a.nam.full_filtered += b.nam.full_filtered;
-    a.nam.full_found += b.nam.full_found;
-    a.nam.partial_not_found += b.nam.partial_not_found;
-    a.nam.partial_filtered += b.nam.partial_filtered;
-    a.nam.partial_found += b.nam.partial_found;
-    a.nam.rescued += b.nam.rescued;
-    a.nam.n_randstrobes += b.nam.n_randstrobes;
-    a.nam.n_anchors += b.nam.n_anchors;
-    a.nam.n_nams += b.nam.n_nams;
-    a.inconsistent_nams += b.inconsistent_nams;
-    a.mate_rescue += b.mate_rescue;
-    a.tried_alignment += b.tried_alignment;
-    a.gapped += b.gapped;
-    a.best_alignments += b.best_alignments;
-}
-
 }  // namespace
 
 // Per-thread buffers of one record's evaluation, reused across records
