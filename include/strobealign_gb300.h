@@ -163,6 +163,12 @@ typedef struct sa_reads sa_reads;
 int32_t sa_reads_from_file(const char* path, sa_reads** out);
 int32_t sa_reads_view(const sa_reads* reads, sa_read_batch* view);
 void sa_reads_free(sa_reads* reads);
+/* The records InterleavedIterator forms from reads in file order (src/io/reads.rs:68-113):
+ * a read and the next one are a pair when their names are equal, any other read is
+ * single-end.  first_read[r] = record r's first read, for r < *n_records, then
+ * first_read[*n_records] = reads->n; capacity entries (reads->n + 1 suffice). */
+int32_t sa_reads_pair_interleaved(const sa_read_batch* reads, uint32_t* first_read, size_t capacity,
+                                  size_t* n_records);
 
 /* ---------------------------------------------------------------- stage entry points */
 /* randstrobes_query (src/seeding/mod.rs:19-75) for every read of the batch.
@@ -331,6 +337,13 @@ typedef struct {
  * a batch that starts at the beginning of an input reproduces the reference's
  * output bytes for those records.  r2 = NULL for single-end. */
 int32_t sa_map_batch(sa_mapper* m, const sa_read_batch* r1, const sa_read_batch* r2, sa_output* out);
+/* Map one batch of mixed single-end and paired-end records, as --interleaved reads them
+ * (src/main.rs:580-581, InterleavedIterator src/io/reads.rs:68-113): reads in file order,
+ * a read and the next one a pair (r1, r2) when their names are equal, any other read a
+ * single-end record.  Chunks count both mates of a pair; each record is mapped as
+ * sa_map_batch maps its kind, with the chunk's RNG and insert-size estimate shared
+ * between the kinds (src/main.rs:873-988). */
+int32_t sa_map_batch_interleaved(sa_mapper* m, const sa_read_batch* reads, sa_output* out);
 void sa_output_free(sa_output* out);
 /* Abundances accumulated over all batches (--aemb), one per contig, already
  * divided by the contig length as output_abundances does (src/main.rs:990-1001). */
@@ -520,6 +533,8 @@ typedef struct {
     int32_t append;        /* 1: append to out_path instead of truncating it */
     const char* header;    /* bytes written first (the SAM header); may be NULL */
     size_t header_len;
+    int32_t interleaved;   /* 1: reads1 holds mixed single-end and paired records (reads2 NULL),
+                              paired as sa_map_batch_interleaved pairs them */
 } sa_stream_params;
 typedef struct {
     uint64_t n_reads, n_records, n_mapped, n_batches;

@@ -42,6 +42,9 @@ def lib() -> C.CDLL:
     L.ora_map_batch.restype = C.c_int32
     L.ora_map_batch.argtypes = [C.c_void_p, C.POINTER(ReadBatch), C.POINTER(ReadBatch), C.POINTER(MapOpts),
                                 C.POINTER(C.c_void_p), C.POINTER(C.c_size_t), C.POINTER(C.c_double)]
+    L.ora_map_interleaved.restype = C.c_int32
+    L.ora_map_interleaved.argtypes = [C.c_void_p, C.POINTER(ReadBatch), C.POINTER(MapOpts), C.POINTER(C.c_void_p),
+                                      C.POINTER(C.c_size_t), C.POINTER(C.c_double)]
     L.ora_output_free.argtypes = [C.c_void_p]
     L.ora_lookup_sectors.restype = C.c_int32
     L.ora_lookup_sectors.argtypes = [C.c_void_p, C.POINTER(ReadBatch), C.c_int32, C.c_uint32, C.POINTER(C.c_uint64)]
@@ -58,6 +61,16 @@ def _batch(seq: np.ndarray, offsets: np.ndarray, names: bytes, name_offsets: np.
     b = ReadBatch(len(off) - 1, seq.ctypes.data, off.ctypes.data, C.addressof(qb) if qb is not None else None,
                   C.addressof(nb), noff.ctypes.data)
     return b
+
+
+def _take_output(out: C.c_void_p, n: C.c_size_t) -> bytes:
+    """The bytes of an oracle output buffer, which is then freed."""
+    try:
+        m = n.value
+        return (C.string_at(out.value, m) if m < (1 << 31) else
+                np.ctypeslib.as_array((C.c_uint8 * m).from_address(out.value)).tobytes()) if m else b""
+    finally:
+        lib().ora_output_free(out)
 
 
 class OracleIndex:
@@ -99,20 +112,31 @@ class OracleIndex:
         keep: list = []
         b1 = _batch(r1.seq, r1.offsets, r1.names, r1.name_offsets, r1.qual, keep)
         b2 = _batch(r2.seq, r2.offsets, r2.names, r2.name_offsets, r2.qual, keep) if r2 is not None else None
-        o = MapOpts(mode, max_secondary, 0.5, 100, 20, 0, 1, 1 if use_ssw else 0, 1 if eqx else 0,
-                    1 if details else 0, chunk_size, threads or self.threads)
+        o = self._opts(mode, threads, chunk_size, eqx, use_ssw, max_secondary, details)
         out, n, sec = C.c_void_p(), C.c_size_t(), C.c_double()
         r = lib().ora_map_batch(self.h, C.byref(b1), C.byref(b2) if b2 is not None else None, C.byref(o),
                                 C.byref(out), C.byref(n), C.byref(sec))
         if r != 0:
             raise RuntimeError(f"ora_map_batch failed ({r})")
-        try:
-            m = n.value
-            data = (C.string_at(out.value, m) if m < (1 << 31) else
-                    np.ctypeslib.as_array((C.c_uint8 * m).from_address(out.value)).tobytes()) if m else b""
-        finally:
-            lib().ora_output_free(out)
-        return data, sec.value
+        return _take_output(out, n), sec.value
+
+    def map_interleaved(self, reads, mode: int = 0, threads: int = 0, chunk_size: int = 1_000_000,
+                        eqx: bool = False, use_ssw: bool = False, max_secondary: int = 0,
+                        details: bool = False) -> tuple[bytes, float]:
+        """As map_batch for one ReadSet-like batch in file order, consecutive records with
+        equal names mapped as pairs and the others as single-end reads (--interleaved)."""
+        keep: list = []
+        b = _batch(reads.seq, reads.offsets, reads.names, reads.name_offsets, reads.qual, keep)
+        o = self._opts(mode, threads, chunk_size, eqx, use_ssw, max_secondary, details)
+        out, n, sec = C.c_void_p(), C.c_size_t(), C.c_double()
+        r = lib().ora_map_interleaved(self.h, C.byref(b), C.byref(o), C.byref(out), C.byref(n), C.byref(sec))
+        if r != 0:
+            raise RuntimeError(f"ora_map_interleaved failed ({r})")
+        return _take_output(out, n), sec.value
+
+    def _opts(self, mode, threads, chunk_size, eqx, use_ssw, max_secondary, details) -> MapOpts:
+        return MapOpts(mode, max_secondary, 0.5, 100, 20, 0, 1, 1 if use_ssw else 0, 1 if eqx else 0,
+                       1 if details else 0, chunk_size, threads or self.threads)
 
     def lookup_sectors(self, reads, mcs: int = 0, rescue_distance: int = 100) -> dict:
         """Distinct 32-byte index sectors the reference's lookups read per read, summed

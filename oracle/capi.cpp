@@ -176,12 +176,32 @@ static void records_from(const ora_read_batch* b, std::vector<SequenceRecord>& o
 // ora_output_free) receives the records' SAM / PAF bytes without a header, or for mode
 // 2 the per-contig abundances (f64, divided by contig length) as raw bytes;
 // *seconds = the mapping time (record conversion excluded).
+static int32_t map_in_memory(OraIndex* o, const std::vector<SequenceRecord>& a, const std::vector<SequenceRecord>* b,
+                             const std::vector<uint8_t>* has_mate, const ora_map_opts* opt, char** out,
+                             size_t* out_len, double* seconds);
+
 int32_t ora_map_batch(void* h, const ora_read_batch* r1, const ora_read_batch* r2, const ora_map_opts* opt,
                       char** out, size_t* out_len, double* seconds) {
-    auto* o = (OraIndex*)h;
     std::vector<SequenceRecord> a, b;
     records_from(r1, a, opt->threads);
     if (r2) records_from(r2, b, opt->threads);
+    return map_in_memory((OraIndex*)h, a, r2 ? &b : nullptr, nullptr, opt, out, out_len, seconds);
+}
+
+// As ora_map_batch for one batch of records in file order, paired as --interleaved pairs
+// them (src/io/reads.rs:68-113): mixed single-end and paired-end records.
+int32_t ora_map_interleaved(void* h, const ora_read_batch* reads, const ora_map_opts* opt, char** out,
+                            size_t* out_len, double* seconds) {
+    std::vector<SequenceRecord> flat, a, b;
+    std::vector<uint8_t> has_mate;
+    records_from(reads, flat, opt->threads);
+    pair_interleaved(std::move(flat), a, b, has_mate);
+    return map_in_memory((OraIndex*)h, a, &b, &has_mate, opt, out, out_len, seconds);
+}
+
+static int32_t map_in_memory(OraIndex* o, const std::vector<SequenceRecord>& a, const std::vector<SequenceRecord>* b,
+                             const std::vector<uint8_t>* has_mate, const ora_map_opts* opt, char** out,
+                             size_t* out_len, double* seconds) {
     Context ctx;
     ctx.refs = &o->refs;
     ctx.index = &o->index;
@@ -196,8 +216,8 @@ int32_t ora_map_batch(void* h, const ora_read_batch* r1, const ora_read_batch* r
     ctx.so.details = opt->details != 0;
     auto t0 = std::chrono::steady_clock::now();
     std::vector<double> ab;
-    std::vector<std::string> outs = map_records(ctx, a, r2 ? &b : nullptr, (MapMode)opt->mode,
-                                                std::max<uint32_t>(opt->threads, 1), opt->chunk_size, &ab);
+    std::vector<std::string> outs = map_records(ctx, a, b, (MapMode)opt->mode, std::max<uint32_t>(opt->threads, 1),
+                                                opt->chunk_size, &ab, has_mate);
     if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (opt->mode == 2) {
         *out_len = ab.size() * sizeof(double);

@@ -3,11 +3,13 @@
 // (:591-604, chunk = records until the nucleotide count exceeds chunk_size), a fresh
 // Rng::with_seed(0) and InsertSizeDistribution per chunk (:878-879), output in chunk
 // order (:653-667) and the abundance table (:990-1001).  Chunks run on -t threads
-// (driver.cpp), and so does the index build.
+// (driver.cpp), and so does the index build.  --interleaved pairs consecutive records
+// of one file by name (src/io/reads.rs:68-113).
 //
 //   sa_oracle [options] ref.fa reads1.fq [reads2.fq]
 #include "oracle.hpp"
 
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cstdio>
@@ -23,7 +25,7 @@ namespace {
 struct Args {
     size_t threads = 1, chunk_size = 1000000;
     bool map_only = false, aemb = false, eqx = false, no_pg = false, only_mapped = false, details = false;
-    bool fastq_comments = false, use_ssw = false;
+    bool fastq_comments = false, use_ssw = false, interleaved = false;
     std::string rg_id;
     bool has_rg_id = false;
     std::vector<std::string> rg;
@@ -63,6 +65,7 @@ bool parse(int argc, char** argv, Args& a, std::string& err) {
         else if (key == "--details") a.details = true;
         else if (key == "-C") a.fastq_comments = true;
         else if (key == "--ssw") a.use_ssw = true;
+        else if (key == "--interleaved") a.interleaved = true;
         else if (key == "--rg-id") { a.rg_id = next(); a.has_rg_id = true; }
         else if (key == "--rg") a.rg.push_back(next());
         else if (key == "-N") a.max_secondary = std::stoul(next());
@@ -106,13 +109,21 @@ int main(int argc, char** argv) {
     if (refs.empty()) { std::fprintf(stderr, "error: No sequences found in the reference FASTA\n"); return 1; }
     std::vector<SequenceRecord> r1, r2;
     if (!read_fastq_file(a.pos[1], r1, err)) { std::fprintf(stderr, "error: %s\n", err.c_str()); return 1; }
-    bool paired = a.pos.size() > 2;
-    if (paired && !read_fastq_file(a.pos[2], r2, err)) { std::fprintf(stderr, "error: %s\n", err.c_str()); return 1; }
+    if (a.interleaved && a.pos.size() > 2) { std::fprintf(stderr, "error: --interleaved takes one reads file\n"); return 2; }
+    bool paired = a.pos.size() > 2 || a.interleaved;
+    if (a.pos.size() > 2 && !read_fastq_file(a.pos[2], r2, err)) { std::fprintf(stderr, "error: %s\n", err.c_str()); return 1; }
     size_t read_length = a.read_length;
     if (!a.has_read_length) {
+        // estimate_read_length over the first 500 records of the first file (src/main.rs:351)
         size_t s = 0, n = 0;
         for (size_t i = 0; i < r1.size() && i < 500; i++) { s += r1[i].seq.size(); n++; }
         read_length = n ? s / n : 0;
+    }
+    std::vector<uint8_t> has_mate;
+    if (a.interleaved) {
+        std::vector<SequenceRecord> flat;
+        flat.swap(r1);
+        pair_interleaved(std::move(flat), r1, r2, has_mate);
     }
     SeedingParameters sp = SeedingParameters::from_read_length(read_length);
     auto t0 = std::chrono::steady_clock::now();
@@ -140,7 +151,8 @@ int main(int argc, char** argv) {
     size_t nt = std::max<size_t>(a.threads, 1);
     size_t n = paired ? std::min(r1.size(), r2.size()) : r1.size();
     std::vector<double> tot;
-    std::vector<std::string> outs = map_records(ctx, r1, paired ? &r2 : nullptr, mode, nt, a.chunk_size, &tot);
+    std::vector<std::string> outs = map_records(ctx, r1, paired ? &r2 : nullptr, mode, nt, a.chunk_size, &tot,
+                                                a.interleaved ? &has_mate : nullptr);
     auto t2 = std::chrono::steady_clock::now();
 
     FILE* fo = a.output.empty() ? stdout : std::fopen(a.output.c_str(), "wb");
@@ -162,7 +174,8 @@ int main(int argc, char** argv) {
         double ti = std::chrono::duration<double>(t1 - t0).count();
         double tm = std::chrono::duration<double>(t2 - t1).count();
         std::fprintf(stderr, "oracle_timing index_s=%.6f map_s=%.6f reads=%zu threads=%zu\n", ti, tm,
-                     paired ? 2 * n : n, nt);
+                     a.interleaved ? n + (size_t)std::count(has_mate.begin(), has_mate.end(), 1) : paired ? 2 * n : n,
+                     nt);
     }
     return 0;
 }

@@ -318,11 +318,21 @@ void abundances_paired_end_read(const SequenceRecord& r1, const SequenceRecord& 
 // Chunk driver of src/main.rs:591-604,873-988 (driver.cpp): per-chunk output strings in
 // chunk order; abundances (if requested) summed over threads, not yet divided by length.
 enum class MapMode { Sam = 0, Paf = 1, Abundance = 2 };
+// has_mate (mixed input; may be null): record i is a pair only where has_mate[i] != 0,
+// else single-end, its r2 entry unused.
 std::vector<std::pair<size_t, size_t>> chunk_ranges(const std::vector<SequenceRecord>& r1,
-                                                    const std::vector<SequenceRecord>* r2, size_t chunk_size);
+                                                    const std::vector<SequenceRecord>* r2, size_t chunk_size,
+                                                    const std::vector<uint8_t>* has_mate = nullptr);
 std::vector<std::string> map_records(const Context& ctx, const std::vector<SequenceRecord>& r1,
                                      const std::vector<SequenceRecord>* r2, MapMode mode, size_t threads,
-                                     size_t chunk_size, std::vector<double>* abundances);
+                                     size_t chunk_size, std::vector<double>* abundances,
+                                     const std::vector<uint8_t>* has_mate = nullptr);
+// InterleavedIterator (src/io/reads.rs:68-113): a record and the next one form a pair
+// when their names are equal; otherwise the first is single-end and the second starts
+// the next record.  r1 / r2 / has_mate are aligned per record (r2[i] empty where
+// has_mate[i] == 0).
+void pair_interleaved(std::vector<SequenceRecord>&& records, std::vector<SequenceRecord>& r1,
+                      std::vector<SequenceRecord>& r2, std::vector<uint8_t>& has_mate);
 
 // Piecewise single-end extension (src/piecewisealigner.rs); block-aligner restated.
 // One DP piece: kind 0 global_alignment, 1 xdrop GlobalStartLocalEnd, 2 xdrop

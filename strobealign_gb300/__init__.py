@@ -233,6 +233,15 @@ class Reads:
     def __len__(self):
         return len(self.seq_offsets) - 1
 
+    def interleaved_records(self) -> np.ndarray:
+        """sa_reads_pair_interleaved: each record's first read, then the read count (a
+        record of two reads is a pair, of one read single-end)."""
+        out = np.zeros(len(self) + 1, dtype=np.uint32)
+        n = C.c_size_t()
+        b = self.c()
+        L.check(lib().sa_reads_pair_interleaved(C.byref(b), _p(out, C.c_uint32), len(out), C.byref(n)))
+        return out[:n.value + 1].copy()
+
     def c(self) -> L.ReadBatch:
         b = L.ReadBatch()
         self._bufs = [self.seq, self.names, self.qual, self.comments]
@@ -459,6 +468,20 @@ class Mapper:
         finally:
             lib().sa_output_free(C.byref(o))
 
+    def map_interleaved(self, reads: Reads, copy: bool = True):
+        """sa_map_batch_interleaved: reads in file order, consecutive reads with equal
+        names mapped as pairs and the others as single-end records."""
+        o = L.Output()
+        b = reads.c()
+        L.check(lib().sa_map_batch_interleaved(self.h, C.byref(b), C.byref(o)))
+        try:
+            data = _bytes(o.data, o.len) if copy else o.len
+            self.last = dict(n_reads=o.n_reads, n_mapped=o.n_mapped, n_waves=o.n_waves,
+                             n_gpu_launches=o.n_gpu_launches)
+            return data
+        finally:
+            lib().sa_output_free(C.byref(o))
+
     def upload(self, r1: Reads, r2: Reads | None = None) -> None:
         """Copy a batch to the device; map it with map_uploaded()."""
         self._b1 = r1.c()
@@ -538,10 +561,10 @@ class Mapper:
                 "seconds_default": rep.seconds_default, "seconds_tuned": rep.seconds_tuned, "trials": rep.trials}
 
     def map_files(self, reads1: str, reads2: str | None, out: str, header: bytes = b"", batch_bases: int = 0,
-                  read_ahead: int = 0, append: bool = False) -> dict:
+                  read_ahead: int = 0, append: bool = False, interleaved: bool = False) -> dict:
         """sa_map_files: reads1 (and reads2) mapped into the file out, parsing, mapping and
-        writing overlapped; header (the SAM header) is written first.  Returns the stream
-        statistics."""
+        writing overlapped; header (the SAM header) is written first; interleaved: reads1
+        holds mixed single-end and paired records.  Returns the stream statistics."""
         p = L.StreamParams()
         lib().sa_stream_params_default(C.byref(p))
         if batch_bases:
@@ -549,6 +572,7 @@ class Mapper:
         if read_ahead:
             p.read_ahead = read_ahead
         p.append = int(append)
+        p.interleaved = int(interleaved)
         p.header = header or None
         p.header_len = len(header)
         st = L.StreamStats()

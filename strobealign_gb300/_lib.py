@@ -100,7 +100,8 @@ class TuneReport(C.Structure):
 
 
 class StreamParams(C.Structure):
-    _fields_ = [("batch_bases", u64), ("read_ahead", u32), ("append", i32), ("header", cp), ("header_len", sz)]
+    _fields_ = [("batch_bases", u64), ("read_ahead", u32), ("append", i32), ("header", cp), ("header_len", sz),
+                ("interleaved", i32)]
 
 
 class StreamStats(C.Structure):
@@ -155,6 +156,7 @@ SIGNATURES = {
     "sa_reads_from_file": (i32, [cp, P(vp)]),
     "sa_reads_view": (i32, [vp, P(ReadBatch)]),
     "sa_reads_free": (None, [vp]),
+    "sa_reads_pair_interleaved": (i32, [P(ReadBatch), vp, sz, P(sz)]),
     "sa_randstrobes_batch": (i32, [vp, P(ReadBatch), P(QueryRandstrobe), sz, P(u64), P(u32)]),
     "sa_randstrobes_device_noalloc": (i32, [vp, vp, vp, u32, u64, vp, vp, vp, vp, vp, vp]),
     "sa_nams_batch": (i32, [vp, P(ChainingParams), P(MappingParams), P(ReadBatch), P(Nam), sz, P(u64), P(u32),
@@ -163,6 +165,7 @@ SIGNATURES = {
     "sa_mapper_create": (i32, [vp, vp, P(ChainingParams), P(MappingParams), P(vp)]),
     "sa_mapper_free": (None, [vp]),
     "sa_map_batch": (i32, [vp, P(ReadBatch), P(ReadBatch), P(Output)]),
+    "sa_map_batch_interleaved": (i32, [vp, P(ReadBatch), P(Output)]),
     "sa_output_free": (None, [P(Output)]),
     "sa_mapper_abundances": (i32, [vp, P(f64), sz]),
     "sa_sam_header": (i32, [vp, cp, cp, P(cp), sz, P(Output)]),

@@ -1,11 +1,13 @@
 // C ABI (include/strobealign_gb300.h).  Every entry point converts exceptions into
 // status codes; none aborts.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
 
+#include "host_input.h"
 #include "mapper.h"
 #include "session.h"
 #include "stream.h"
@@ -343,6 +345,20 @@ int32_t sa_reads_view(const sa_reads* reads, sa_read_batch* v) {
 
 void sa_reads_free(sa_reads* reads) { delete reads; }
 
+int32_t sa_reads_pair_interleaved(const sa_read_batch* reads, uint32_t* first_read, size_t capacity,
+                                  size_t* n_records) {
+    SA_TRY
+    require(reads && first_read && n_records, "null argument");
+    require(reads->n < UINT32_MAX, "batch too large");
+    std::vector<uint32_t> rr;
+    pair_records_by_name(*reads, true, rr);
+    require(rr.size() <= capacity, "output too small");
+    std::copy(rr.begin(), rr.end(), first_read);
+    *n_records = rr.size() - 1;
+    return SA_OK;
+    SA_CATCH
+}
+
 int32_t sa_mapper_create(const sa_index* idx, const sa_refs* refs, const sa_chaining_params* cp,
                          const sa_mapping_params* mp, sa_mapper** out) {
     SA_TRY
@@ -373,6 +389,15 @@ int32_t sa_map_batch(sa_mapper* m, const sa_read_batch* r1, const sa_read_batch*
     require(m && r1 && out, "null argument");
     std::memset(out, 0, sizeof(*out));
     m->m->map(r1, r2, out);
+    return SA_OK;
+    SA_CATCH
+}
+
+int32_t sa_map_batch_interleaved(sa_mapper* m, const sa_read_batch* reads, sa_output* out) {
+    SA_TRY
+    require(m && reads && out, "null argument");
+    std::memset(out, 0, sizeof(*out));
+    m->m->map_interleaved(reads, out);
     return SA_OK;
     SA_CATCH
 }
@@ -466,7 +491,9 @@ int32_t sa_map_files(sa_mapper* m, const char* reads1, const char* reads2, const
         cfg.append = p->append != 0;
         cfg.header = p->header;
         cfg.header_len = p->header ? p->header_len : 0;
+        cfg.interleaved = p->interleaved != 0;
     }
+    require(!(cfg.interleaved && reads2), "interleaved input takes one reads file");
     const std::string r2 = reads2 ? reads2 : "";
     const StreamResult r = map_files(*m->m, reads1, reads2 ? &r2 : nullptr, out_path, cfg);
     if (stats) {

@@ -75,6 +75,13 @@ class ReadParser {
     bool have_header_ = false;
 };
 
+// Records of reads in file order as InterleavedIterator forms them (src/io/reads.rs:
+// 68-113): a read and the next one are a pair when their names are equal, any other read
+// is single-end.  rec_read gets each record's first read and then the number of reads the
+// records cover (records + 1 entries).  Unless at_end, a last read without a successor
+// is left out: the next read of the input may be its mate.
+void pair_records_by_name(const sa_read_batch& reads, bool at_end, std::vector<uint32_t>& rec_read);
+
 // An empty store (offset arrays holding their leading 0)
 void reset_read_store(ReadStore& rs, bool has_qual);
 inline size_t read_store_size(const ReadStore& rs) { return rs.seq_off.empty() ? 0 : rs.seq_off.size() - 1; }

@@ -406,6 +406,22 @@ uint32_t pick_bits(const std::vector<Contig>& cs, const SeedParams& p) {
     return lg - 1;
 }
 
+void pair_records_by_name(const sa_read_batch& reads, bool at_end, std::vector<uint32_t>& rec_read) {
+    const size_t n = reads.n;
+    rec_read.clear();
+    rec_read.reserve(n + 1);
+    auto name = [&](size_t i) {
+        return std::string_view(reads.names + reads.name_offsets[i], reads.name_offsets[i + 1] - reads.name_offsets[i]);
+    };
+    size_t i = 0;
+    while (i < n) {
+        if (i + 1 == n && !at_end) break;
+        rec_read.push_back((uint32_t)i);
+        i += i + 1 < n && name(i) == name(i + 1) ? 2 : 1;
+    }
+    rec_read.push_back((uint32_t)i);
+}
+
 void reset_read_store(ReadStore& rs, bool has_qual) {
     rs = ReadStore();
     rs.seq_off.push_back(0);

@@ -15,6 +15,7 @@
 #include <mutex>
 #include <thread>
 
+#include "host_input.h"
 #include "host_util.h"
 #include "mapper.h"
 
@@ -123,7 +124,7 @@ void Mapper::part_nams(Part& p, uint32_t& launches) {
                          cp_.max_ref_gap, cp_.matches_weight, cp_.max_diagonal_ratio};
     cfg.mcs = mp_.mcs_strategy;
     cfg.rescue_distance = mp_.rescue_distance;
-    cfg.nam_anchors = single_end_piecewise_ && !bv_.paired;
+    cfg.nam_anchors = single_end_piecewise_ && (!bv_.paired || bv_.rec_read);
     cfg.chain_lane_max = chain_lane_max_;
     pws_.seq.reserve(total + 16);
     pws_.off.reserve((size_t)n + 1);
@@ -197,6 +198,24 @@ std::shared_ptr<const WaveResults> Mapper::run_wave(const ExtJob* jobs, uint32_t
     return w;
 }
 
+namespace {
+ReadView read_view(const sa_read_batch* b, uint64_t i) {
+    ReadView v;
+    v.seq = b->seq + b->seq_offsets[i];
+    v.len = (uint32_t)(b->seq_offsets[i + 1] - b->seq_offsets[i]);
+    v.qual = b->qual ? b->qual + b->seq_offsets[i] : nullptr;
+    v.name = b->names + b->name_offsets[i];
+    v.name_len = (uint32_t)(b->name_offsets[i + 1] - b->name_offsets[i]);
+    v.comment = nullptr;
+    v.comment_len = 0;
+    if (b->comments && b->comment_offsets && b->comment_offsets[i + 1] > b->comment_offsets[i]) {
+        v.comment = b->comments + b->comment_offsets[i];
+        v.comment_len = (uint32_t)(b->comment_offsets[i + 1] - b->comment_offsets[i]);
+    }
+    return v;
+}
+}  // namespace
+
 void Mapper::upload(const sa_read_batch* r1, const sa_read_batch* r2) {
     auto t0 = std::chrono::steady_clock::now();
     const bool paired = r2 != nullptr;
@@ -204,22 +223,9 @@ void Mapper::upload(const sa_read_batch* r1, const sa_read_batch* r2) {
     const uint64_t nrec = r1->n;
     bv_ = BatchView();
     bv_.paired = paired;
+    rec_read_.clear();
     reads_.resize(paired ? 2 * nrec : nrec);
-    auto view = [](const sa_read_batch* b, uint64_t i) {
-        ReadView v;
-        v.seq = b->seq + b->seq_offsets[i];
-        v.len = (uint32_t)(b->seq_offsets[i + 1] - b->seq_offsets[i]);
-        v.qual = b->qual ? b->qual + b->seq_offsets[i] : nullptr;
-        v.name = b->names + b->name_offsets[i];
-        v.name_len = (uint32_t)(b->name_offsets[i + 1] - b->name_offsets[i]);
-        v.comment = nullptr;
-        v.comment_len = 0;
-        if (b->comments && b->comment_offsets && b->comment_offsets[i + 1] > b->comment_offsets[i]) {
-            v.comment = b->comments + b->comment_offsets[i];
-            v.comment_len = (uint32_t)(b->comment_offsets[i + 1] - b->comment_offsets[i]);
-        }
-        return v;
-    };
+    auto view = read_view;
     parallel_ranges(nrec, policy_threads_, [&](uint64_t a, uint64_t b) {
         for (uint64_t i = a; i < b; i++) {
             if (paired) {
@@ -238,6 +244,38 @@ void Mapper::upload(const sa_read_batch* r1, const sa_read_batch* r2) {
     SA_CUDA(cudaStreamSynchronize(st_));
     have_batch_ = true;
     stats_.seconds_upload = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void Mapper::upload_interleaved(const sa_read_batch* reads) {
+    auto t0 = std::chrono::steady_clock::now();
+    const uint64_t n = reads->n;
+    if (n >= UINT32_MAX) throw Error(SA_ERR_INVALID, "batch too large");
+    bv_ = BatchView();
+    reads_.resize(n);
+    parallel_ranges(n, policy_threads_, [&](uint64_t a, uint64_t b) {
+        for (uint64_t i = a; i < b; i++) reads_[i] = read_view(reads, i);
+    });
+    pair_records_by_name(*reads, true, rec_read_);
+    bv_.rec_read = rec_read_.data();
+    max_qlen_ = 1;
+    bv_.reads = ReadSpan{reads_.data(), reads_.size()};
+    for (auto& r : reads_) max_qlen_ = std::max(max_qlen_, r.len);
+    h2d_bytes_ = 0;
+    upload_reads(bv_.reads);
+    SA_CUDA(cudaStreamSynchronize(st_));
+    have_batch_ = true;
+    stats_.seconds_upload = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void Mapper::map_interleaved(const sa_read_batch* reads, sa_output* out) {
+    auto t0 = std::chrono::steady_clock::now();
+    upload_interleaved(reads);
+    uint64_t h2d = h2d_bytes_;
+    double tu = stats_.seconds_upload;
+    map_uploaded(out);
+    stats_.seconds_upload = tu;
+    stats_.h2d_bytes += h2d;
+    stats_.seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
 void Mapper::map(const sa_read_batch* r1, const sa_read_batch* r2, sa_output* out) {
@@ -488,7 +526,10 @@ void Mapper::map_uploaded(sa_output* out) {
     t_map0_ = t0;
     BatchView& bv = bv_;
     const bool paired = bv.paired;
-    const uint64_t nrec = paired ? bv.reads.size() / 2 : bv.reads.size();
+    const bool mixed = bv.rec_read != nullptr;
+    const uint64_t nrec = mixed ? rec_read_.size() - 1 : paired ? bv.reads.size() / 2 : bv.reads.size();
+    // record j's first read (for j = nrec: the read count)
+    auto first_read = [&](uint64_t j) -> uint64_t { return mixed ? rec_read_[j] : paired ? 2 * j : j; };
     uint32_t launches = 0;
     h2d_bytes_ = 0;
     d2h_bytes_ = 0;
@@ -498,17 +539,16 @@ void Mapper::map_uploaded(sa_output* out) {
     kt_nam_.reset();
     for (int c = 0; c < 7; c++) sw_cells_[c] = 0;
     // chunks (src/main.rs:591-604), cut on the uploaded read offsets (record j's bases
-    // are off[rpr * (j + 1)] - off[rpr * j])
+    // are off[first_read(j + 1)] - off[first_read(j)])
     std::vector<ChunkState> chunks;
     chunks.reserve(total_bases_ / (mp_.chunk_size + 1) + 2);
     const uint64_t* off = h_off_.p;
-    const uint64_t step = paired ? 2 : 1;
     for (uint64_t i = 0; i < nrec;) {
         uint64_t j = i;
-        const uint64_t base = off[step * i];
+        const uint64_t base = off[first_read(i)];
         while (j < nrec) {
             j++;
-            if (off[step * j] - base > mp_.chunk_size) break;
+            if (off[first_read(j)] - base > mp_.chunk_size) break;
         }
         ChunkState cs;
         cs.first = cs.next = i;
@@ -523,7 +563,6 @@ void Mapper::map_uploaded(sa_output* out) {
     // parts: runs of whole chunks (at least 4 chunks each), so that chunk semantics and
     // output order are those of the whole batch; read and record indices inside a part
     // are local to it
-    const uint32_t rpr = paired ? 2 : 1;
     const size_t nchunks = chunks.size();
     // at least parts_target_ parts, and enough that a part holds at most
     // MAX_PART_BASES bases (the NAM workspace takes about 100 bytes per base)
@@ -542,10 +581,14 @@ void Mapper::map_uploaded(sa_output* out) {
         p.chunk_hi = c1;
         p.rec_lo = c0 < nchunks ? chunks[c0].first : nrec;
         p.rec_hi = c1 > 0 && c1 <= nchunks ? chunks[c1 - 1].end : p.rec_lo;
-        p.read_lo = (uint32_t)(rpr * p.rec_lo);
-        p.read_hi = (uint32_t)(rpr * p.rec_hi);
+        p.read_lo = (uint32_t)first_read(p.rec_lo);
+        p.read_hi = (uint32_t)first_read(p.rec_hi);
         p.bv = BatchView();
         p.bv.paired = paired;
+        if (mixed) {
+            p.bv.rec_read = rec_read_.data() + p.rec_lo;
+            p.bv.rec_read_base = p.read_lo;
+        }
         p.bv.reads = ReadSpan{reads_.data() + p.read_lo, (size_t)(p.read_hi - p.read_lo)};
         p.store.reset(p.read_hi - p.read_lo);
         p.n_nams = 0;

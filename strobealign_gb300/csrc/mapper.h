@@ -16,6 +16,10 @@ class Mapper {
     ~Mapper();
     void map(const sa_read_batch* r1, const sa_read_batch* r2, sa_output* out);
     void upload(const sa_read_batch* r1, const sa_read_batch* r2);
+    // mixed input: one batch of reads in file order, a read and the next one a pair when
+    // their names are equal, any other read single-end (src/io/reads.rs:68-113)
+    void map_interleaved(const sa_read_batch* reads, sa_output* out);
+    void upload_interleaved(const sa_read_batch* reads);
     void map_uploaded(sa_output* out);
     const sa_mapper_stats& stats() const { return stats_; }
     const sa_mapping_params& mapping_params() const { return mp_; }
@@ -97,6 +101,9 @@ class Mapper {
     uint32_t schedule(std::vector<ChunkState>& chunks, uint32_t& launches, uint32_t& nam_launches);
     PodArray<ReadView> reads_;  // the uploaded batch's read views (device read order)
     BatchView bv_;
+    // mixed input: record r's reads are rec_read_[r] .. rec_read_[r + 1] (n + 1 entries);
+    // empty for uniform batches
+    std::vector<uint32_t> rec_read_;
     bool have_batch_ = false;
     uint32_t max_qlen_ = 1;
     sa_mapper_stats stats_{};

@@ -620,7 +620,7 @@ ExtJob Policy::nam_job(uint32_t read, const NamRec& cur, uint32_t kind) const {
     j.query_end = n.query_end;
     j.is_revcomp = n.is_revcomp;
     // paired-end extension always uses SSW (src/mapper.rs:860-870); single-end follows --ssw
-    j.use_ssw = (bv_->paired || cfg_.mp.use_ssw) ? 1 : 0;
+    j.use_ssw = (pe_ || cfg_.mp.use_ssw) ? 1 : 0;
     j.nam = (uint32_t)(f != e ? f - b : 0);
     return j;
 }
@@ -776,7 +776,7 @@ std::vector<NamRec> Policy::sorted_nams(uint32_t read, Rng& rng) const {
 // ------------------------------------------------------------------ single end
 // src/mapper.rs:349-528
 bool Policy::se_record(uint64_t rec, Rng& rng, OutBuf& out, uint64_t& mapped) {
-    const uint32_t read = (uint32_t)rec;
+    const uint32_t read = bv_->first_read(rec);
     const ReadView& rv = bv_->reads[read];
     std::vector<NamRec>& nams = sc_->nams[0];
     sorted_nams(read, rng, nams);
@@ -864,7 +864,7 @@ bool Policy::se_record(uint64_t rec, Rng& rng, OutBuf& out, uint64_t& mapped) {
 // ------------------------------------------------------------------ paired end
 // src/mapper.rs:624-1091
 bool Policy::pe_record(uint64_t rec, Rng& rng, InsertSize& isd, OutBuf& out, uint64_t& mapped) {
-    const uint32_t rd[2] = {(uint32_t)(2 * rec), (uint32_t)(2 * rec + 1)};
+    const uint32_t rd[2] = {bv_->first_read(rec), bv_->first_read(rec) + 1};
     const ReadView* rv[2] = {&bv_->reads[rd[0]], &bv_->reads[rd[1]]};
     Details det[2];
     std::vector<NamRec>(&nams)[2] = sc_->nams;
@@ -1358,13 +1358,14 @@ int best_paired_location(const std::vector<NamPairM>& pairs, const std::vector<N
 
 // src/maponly.rs:18-52
 void Policy::paf_se(uint64_t rec, Rng& rng, OutBuf& out) {
-    std::vector<NamRec> nams = sorted_nams((uint32_t)rec, rng);
-    if (!nams.empty()) paf_line(*this, nams[0], bv_->reads[rec], 0, mapping_quality(nams), out);
+    const uint32_t read = bv_->first_read(rec);
+    std::vector<NamRec> nams = sorted_nams(read, rng);
+    if (!nams.empty()) paf_line(*this, nams[0], bv_->reads[read], 0, mapping_quality(nams), out);
 }
 
 // src/maponly.rs:114-195
 void Policy::paf_pe(uint64_t rec, Rng& rng, InsertSize& isd, OutBuf& out) {
-    uint32_t a = (uint32_t)(2 * rec), b = a + 1;
+    uint32_t a = bv_->first_read(rec), b = a + 1;
     std::vector<NamRec> n1 = unsorted_nams(*bv_, a), n2 = unsorted_nams(*bv_, b);
     if (n1.empty() && n2.empty()) return;
     std::vector<NamPairM> pairs = nam_pairs_maponly(n1, n2, isd.mu, isd.sigma, bv_->details[a].both_orientations,
@@ -1382,16 +1383,17 @@ void Policy::paf_pe(uint64_t rec, Rng& rng, InsertSize& isd, OutBuf& out) {
 
 // src/maponly.rs:57-78
 void Policy::aemb_se(uint64_t rec, Rng& rng) {
-    std::vector<NamRec> nams = sorted_nams((uint32_t)rec, rng);
+    const uint32_t read = bv_->first_read(rec);
+    std::vector<NamRec> nams = sorted_nams(read, rng);
     size_t nb = 0;
     while (nb < nams.size() && nams[nb].score == nams[0].score) nb++;
-    double w = (double)bv_->reads[rec].len / (double)nb;
+    double w = (double)bv_->reads[read].len / (double)nb;
     for (size_t i = 0; i < nb; i++) add_abundance(nams[i].ref_id, w);
 }
 
 // src/maponly.rs:198-261
 void Policy::aemb_pe(uint64_t rec, Rng& rng, InsertSize& isd) {
-    uint32_t a = (uint32_t)(2 * rec), b = a + 1;
+    uint32_t a = bv_->first_read(rec), b = a + 1;
     std::vector<NamRec> n1 = unsorted_nams(*bv_, a), n2 = unsorted_nams(*bv_, b);
     if (n1.empty() && n2.empty()) return;
     std::vector<NamPairM> pairs = nam_pairs_maponly(n1, n2, isd.mu, isd.sigma, bv_->details[a].both_orientations,
@@ -1433,10 +1435,11 @@ void Policy::seed_requests(ChunkState& cs) {
             if (c.timing) cs.seconds_seed += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         }
     } acc{cfg_, cs, t0};
-    const bool paired = bv_->paired;
     for (uint64_t rec = cs.first; rec < cs.end; rec++) {
+        const bool paired = bv_->rec_paired(rec);
+        pe_ = paired;
         for (int m = 0; m < (paired ? 2 : 1); m++) {
-            uint32_t read = paired ? (uint32_t)(2 * rec + m) : (uint32_t)rec;
+            const uint32_t read = bv_->first_read(rec) + m;
             const NamRec* n = bv_->nams + bv_->nam_off[read];
             size_t c = bv_->nam_off[read + 1] - bv_->nam_off[read];
             if (!c) continue;
@@ -1461,16 +1464,18 @@ void Policy::run_chunk(ChunkState& cs) {
     const auto t_run = timing ? now() : std::chrono::steady_clock::time_point();
     cs.runs++;
     // false: the record stopped on a missing result
+    // a record with a mate is a pair (src/main.rs:886-985 matches on r2)
     auto one = [&](uint64_t rec, Rng& rng, InsertSize& isd, OutBuf& out, uint64_t& mapped) -> bool {
+        pe_ = bv_->rec_paired(rec);
         switch (cfg_.mp.mode) {
             case SA_MODE_SAM:
-                return bv_->paired ? pe_record(rec, rng, isd, out, mapped) : se_record(rec, rng, out, mapped);
+                return pe_ ? pe_record(rec, rng, isd, out, mapped) : se_record(rec, rng, out, mapped);
             case SA_MODE_PAF:
-                if (bv_->paired) paf_pe(rec, rng, isd, out);
+                if (pe_) paf_pe(rec, rng, isd, out);
                 else paf_se(rec, rng, out);
                 return true;
             default:
-                if (bv_->paired) aemb_pe(rec, rng, isd);
+                if (pe_) aemb_pe(rec, rng, isd);
                 else aemb_se(rec, rng);
                 return true;
         }
@@ -1529,8 +1534,9 @@ void Policy::run_chunk(ChunkState& cs) {
                     // room for the captured records (SEQ and QUAL plus the fixed fields)
                     uint64_t est = 0;
                     for (uint64_t rec = cs.next + 1; rec < cs.end; rec++) {
-                        if (bv_->paired) est += 2ull * (bv_->reads[2 * rec].len + bv_->reads[2 * rec + 1].len) + 320;
-                        else est += 2ull * bv_->reads[rec].len + 160;
+                        const uint32_t r0 = bv_->first_read(rec);
+                        if (bv_->rec_paired(rec)) est += 2ull * (bv_->reads[r0].len + bv_->reads[r0 + 1].len) + 320;
+                        else est += 2ull * bv_->reads[r0].len + 160;
                     }
                     cs.spec_out.reserve(est);
                 }

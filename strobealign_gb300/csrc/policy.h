@@ -146,6 +146,16 @@ struct BatchView {
     const uint64_t* nam_off = nullptr;
     const NamDetailsRec* details = nullptr;
     bool paired = false;
+    // mixed input (interleaved files, src/io/reads.rs:68-113): record r's reads are
+    // rec_read[r] - rec_read_base up to rec_read[r + 1] - rec_read_base, one read
+    // (single-end) or two (a pair); null: every record is a pair (paired) or every
+    // record one read
+    const uint32_t* rec_read = nullptr;
+    uint32_t rec_read_base = 0;
+    uint32_t first_read(uint64_t rec) const {
+        return rec_read ? rec_read[rec] - rec_read_base : (uint32_t)(paired ? 2 * rec : rec);
+    }
+    bool rec_paired(uint64_t rec) const { return rec_read ? rec_read[rec + 1] - rec_read[rec] == 2 : paired; }
     // single-end piecewise extension: chain anchors of NAM t (index into nams) are the
     // packed keys nam_anc[nam_anc_off[t] .. nam_anc_off[t + 1]), last to first
     const uint64_t* nam_anc_off = nullptr;
@@ -274,6 +284,7 @@ class Policy {
     ResultStore* store_;
     ChunkState* cur_ = nullptr;
     bool speculative_ = false;
+    bool pe_ = false;  // the record being evaluated is a pair (its extensions use SSW)
     struct Scratch;
     std::unique_ptr<Scratch> sc_;
     void add_abundance(uint32_t ref_id, double w) {

@@ -25,6 +25,7 @@ namespace {
 
 struct InBatch {
     ReadStore r1, r2;
+    size_t records = 0;  // interleaved input: records (single-end or pairs) of r1's reads
 };
 
 template <class T>
@@ -107,6 +108,34 @@ size_t whole_chunks(const ReadStore& a, const ReadStore* b, uint64_t chunk_size,
     return cut;
 }
 
+// Interleaved input: as whole_chunks over the records pair_records_by_name forms from the
+// pending reads; returns the cut in reads and sets records to the records before it.
+size_t whole_chunks_interleaved(const ReadStore& a, uint64_t chunk_size, bool at_end, std::vector<uint32_t>& rec_read,
+                                size_t& records) {
+    const sa_read_batch v = view_of(a);
+    pair_records_by_name(v, at_end, rec_read);
+    const size_t n = rec_read.size() - 1;
+    auto off = [&](size_t j) { return a.seq_off[rec_read[j]]; };
+    size_t cut = 0;
+    for (size_t i = 0; i < n;) {
+        size_t j = i;
+        const uint64_t base = off(i);
+        bool full = false;
+        while (j < n) {
+            j++;
+            if (off(j) - base > chunk_size) {
+                full = true;
+                break;
+            }
+        }
+        if (!full && !at_end) break;
+        cut = j;
+        i = j;
+    }
+    records = cut;
+    return rec_read[cut];
+}
+
 }  // namespace
 
 StreamResult map_files(Mapper& m, const std::string& reads1, const std::string* reads2, const std::string& out_path,
@@ -172,13 +201,19 @@ StreamResult map_files(Mapper& m, const std::string& reads1, const std::string* 
             reserve(pend->r1, rec_est);
             if (p2) reserve(pend->r2, rec_est);
             bool at_end = false;
+            std::vector<uint32_t> rec_read;
             while (true) {
                 // parse until the pending records hold a batch's bases and one whole chunk
-                size_t cut = 0;
+                size_t cut = 0, records = 0;
                 for (;;) {
                     const uint64_t bases = pend->r1.seq.size() + (p2 ? pend->r2.seq.size() : 0);
                     if (at_end || bases >= batch_bases) {
-                        cut = whole_chunks(pend->r1, p2 ? &pend->r2 : nullptr, chunk_size, at_end);
+                        if (cfg.interleaved) {
+                            cut = whole_chunks_interleaved(pend->r1, chunk_size, at_end, rec_read, records);
+                        } else {
+                            cut = whole_chunks(pend->r1, p2 ? &pend->r2 : nullptr, chunk_size, at_end);
+                            records = cut;
+                        }
                         if (cut > 0 || at_end) break;
                     }
                     // records to parse next: about what the batch still lacks, at the
@@ -221,6 +256,7 @@ StreamResult map_files(Mapper& m, const std::string& reads1, const std::string* 
                 }
                 const size_t n = read_store_size(pend->r1);
                 if (n == 0) break;
+                pend->records = records;
                 auto next = std::make_unique<InBatch>();
                 split_read_store(pend->r1, cut, next->r1);
                 if (p2) split_read_store(pend->r2, cut, next->r2);
@@ -270,9 +306,10 @@ StreamResult map_files(Mapper& m, const std::string& reads1, const std::string* 
             const sa_read_batch v2 = p2 ? view_of(b->r2) : sa_read_batch{};
             sa_output o{};
             const auto tm = std::chrono::steady_clock::now();
-            m.map(&v1, p2 ? &v2 : nullptr, &o);
+            if (cfg.interleaved) m.map_interleaved(&v1, &o);
+            else m.map(&v1, p2 ? &v2 : nullptr, &o);
             res.seconds_map += since(tm);
-            res.records += v1.n;
+            res.records += b->records;
             res.reads += o.n_reads;
             res.mapped += o.n_mapped;
             res.batches++;

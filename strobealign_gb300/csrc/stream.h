@@ -12,6 +12,7 @@ struct StreamConfig {
     bool append = false;       // append to the output file instead of truncating it
     const char* header = nullptr;
     size_t header_len = 0;
+    bool interleaved = false;  // reads1 holds mixed single-end and paired records
 };
 
 struct StreamResult {
