@@ -57,6 +57,10 @@ typedef struct {
 
 /* SeedingParameters::new(read_length) (src/seeding/parameters.rs:181-221). */
 int32_t sa_seeding_params_from_read_length(size_t read_length, sa_seeding_params* out);
+/* estimate_read_length over the first 500 records of a read file (src/main.rs:351,
+ * :1003-1012): the mean sequence length, rounded down; 0 for an empty file.  Plain or
+ * gzip FASTQ/FASTA; standard input ("-") is refused, since its records would be used up. */
+int32_t sa_estimate_read_length(const char* path, size_t* out);
 
 /* ChainingParameters (src/chainer.rs:16-44), MappingParameters (src/mapper.rs:31-55),
  * Scores (src/aligner.rs:11-30) and SAM output options (src/mapper.rs:87-112). */

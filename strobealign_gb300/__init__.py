@@ -678,6 +678,13 @@ def measure_int_alu() -> dict:
     return {"viaddmax_per_s": out[0], "max_xor_per_s": out[1]}
 
 
+def estimate_read_length(path: str) -> int:
+    """sa_estimate_read_length: mean length of the first 500 records of a read file."""
+    n = C.c_size_t()
+    L.check(lib().sa_estimate_read_length(os.fsencode(path), C.byref(n)))
+    return n.value
+
+
 def sam_header(refs: References, cmd_line: str | None = None, rg_id: str | None = None,
                rg_fields: list[str] = ()) -> bytes:
     o = L.Output()

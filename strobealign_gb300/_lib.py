@@ -157,6 +157,7 @@ SIGNATURES = {
     "sa_reads_view": (i32, [vp, P(ReadBatch)]),
     "sa_reads_free": (None, [vp]),
     "sa_reads_pair_interleaved": (i32, [P(ReadBatch), vp, sz, P(sz)]),
+    "sa_estimate_read_length": (i32, [cp, P(sz)]),
     "sa_randstrobes_batch": (i32, [vp, P(ReadBatch), P(QueryRandstrobe), sz, P(u64), P(u32)]),
     "sa_randstrobes_device_noalloc": (i32, [vp, vp, vp, u32, u64, vp, vp, vp, vp, vp, vp]),
     "sa_nams_batch": (i32, [vp, P(ChainingParams), P(MappingParams), P(ReadBatch), P(Nam), sz, P(u64), P(u32),

@@ -345,6 +345,19 @@ int32_t sa_reads_view(const sa_reads* reads, sa_read_batch* v) {
 
 void sa_reads_free(sa_reads* reads) { delete reads; }
 
+int32_t sa_estimate_read_length(const char* path, size_t* out) {
+    SA_TRY
+    require(path && out, "null argument");
+    require(std::string(path) != "-", "the read length of standard input cannot be estimated");
+    ReadParser parser(path);
+    ReadStore rs;
+    reset_read_store(rs, !parser.fasta());
+    const size_t n = parser.parse(rs, 500);
+    *out = n ? (size_t)(rs.seq_off[n] / n) : 0;
+    return SA_OK;
+    SA_CATCH
+}
+
 int32_t sa_reads_pair_interleaved(const sa_read_batch* reads, uint32_t* first_read, size_t capacity,
                                   size_t* n_records) {
     SA_TRY

@@ -116,3 +116,23 @@ def test_reads_from_standard_input(tmp_path):
     import strobealign_gb300 as sa
     want = sa.Reads.from_file(str(src))
     assert out.stdout.split() == [str(len(want)), str(len(want.seq))]
+
+
+def test_estimate_read_length(tmp_path):
+    # src/main.rs:1042-1046: the first 500 records of phix.1.fastq give 289
+    import strobealign_gb300 as sa
+    assert sa.estimate_read_length(str(GOLDEN / "phix.1.fastq")) == 289
+    data = (GOLDEN / "phix.1.fastq").read_bytes()
+    (tmp_path / "r.fq.gz").write_bytes(gzip.compress(data))
+    assert sa.estimate_read_length(str(tmp_path / "r.fq.gz")) == 289
+    # only the first 500 records count; the mean is rounded down
+    rec = [b"@r%d\n%s\n+\n%s\n" % (i, b"A" * (10 if i < 500 else 1000), b"I" * (10 if i < 500 else 1000))
+           for i in range(600)]
+    (tmp_path / "long.fq").write_bytes(b"".join(rec))
+    assert sa.estimate_read_length(str(tmp_path / "long.fq")) == 10
+    (tmp_path / "odd.fa").write_bytes(b">a\nACG\n>b\nACGTAC\n")
+    assert sa.estimate_read_length(str(tmp_path / "odd.fa")) == 4
+    (tmp_path / "empty.fq").write_bytes(b"")
+    assert sa.estimate_read_length(str(tmp_path / "empty.fq")) == 0
+    with pytest.raises(sa.SaError, match="standard input"):
+        sa.estimate_read_length("-")
