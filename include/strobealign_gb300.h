@@ -109,6 +109,12 @@ int32_t sa_refs_from_buffers(size_t n_contigs, const char* const* names, const c
                              const size_t* lens, sa_refs** out);
 size_t sa_refs_count(const sa_refs* refs);
 size_t sa_refs_total_length(const sa_refs* refs);
+/* Contig i's name (NUL-terminated, owned by refs) and length in bases. */
+int32_t sa_refs_contig(const sa_refs* refs, size_t i, const char** name, uint64_t* length);
+/* PackedSeq::decode (src/packed_seq.rs:103-126): bases [start, end) of contig i as ASCII
+ * A/C/G/T into out (end - start bytes; a wildcard base decodes to its pseudo-random
+ * 2-bit value, src/packed_seq.rs:50-59). */
+int32_t sa_refs_decode(const sa_refs* refs, size_t i, uint64_t start, uint64_t end, char* out);
 /* SyncmerParameters::pick_bits (src/indexer.rs:294-300). */
 uint32_t sa_refs_pick_bits(const sa_refs* refs, const sa_seeding_params* p);
 void sa_refs_free(sa_refs* refs);

@@ -9,10 +9,11 @@
 
 namespace oracle {
 
+// trim_ascii_end: space, tab, line feed, form feed and carriage return (not vertical tab)
 static std::string trim_end(const std::string& s) {
     size_t e = s.size();
     while (e > 0 && (s[e - 1] == ' ' || s[e - 1] == '\t' || s[e - 1] == '\n' || s[e - 1] == '\r' ||
-                     s[e - 1] == '\f' || s[e - 1] == '\v'))
+                     s[e - 1] == '\f'))
         e--;
     return s.substr(0, e);
 }

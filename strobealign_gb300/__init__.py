@@ -98,6 +98,20 @@ class References:
     def total_length(self) -> int:
         return lib().sa_refs_total_length(self.h)
 
+    def contig(self, i: int) -> tuple[str, int]:
+        """sa_refs_contig: (name, length) of contig i."""
+        name, n = C.c_char_p(), C.c_uint64()
+        L.check(lib().sa_refs_contig(self.h, i, C.byref(name), C.byref(n)))
+        return name.value.decode(), n.value
+
+    def decode(self, i: int, start: int = 0, end: int | None = None) -> bytes:
+        """sa_refs_decode: bases [start, end) of contig i as A/C/G/T."""
+        if end is None:
+            end = self.contig(i)[1]
+        buf = C.create_string_buffer(max(end - start, 1))
+        L.check(lib().sa_refs_decode(self.h, i, start, end, buf))
+        return buf.raw[:end - start]
+
     def pick_bits(self, params: SeedingParameters) -> int:
         return lib().sa_refs_pick_bits(self.h, C.byref(params.c))
 

@@ -144,6 +144,8 @@ SIGNATURES = {
     "sa_refs_from_buffers": (i32, [sz, P(cp), P(cp), P(sz), P(vp)]),
     "sa_refs_count": (sz, [vp]),
     "sa_refs_total_length": (sz, [vp]),
+    "sa_refs_contig": (i32, [vp, sz, P(cp), P(u64)]),
+    "sa_refs_decode": (i32, [vp, sz, u64, u64, vp]),
     "sa_refs_pick_bits": (u32, [vp, P(SeedingParams)]),
     "sa_refs_free": (None, [vp]),
     "sa_index_build": (i32, [vp, P(SeedingParams), i32, f64, P(vp)]),

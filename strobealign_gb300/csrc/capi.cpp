@@ -167,6 +167,28 @@ int32_t sa_refs_from_buffers(size_t n, const char* const* names, const char* con
 
 size_t sa_refs_count(const sa_refs* refs) { return refs ? refs->contigs.size() : 0; }
 size_t sa_refs_total_length(const sa_refs* refs) { return refs ? refs->total_len : 0; }
+
+int32_t sa_refs_contig(const sa_refs* refs, size_t i, const char** name, uint64_t* length) {
+    SA_TRY
+    require(refs && name && length, "null argument");
+    require(i < refs->contigs.size(), "contig index out of range");
+    *name = refs->contigs[i].name.c_str();
+    *length = refs->contigs[i].len;
+    return SA_OK;
+    SA_CATCH
+}
+
+int32_t sa_refs_decode(const sa_refs* refs, size_t i, uint64_t start, uint64_t end, char* out) {
+    SA_TRY
+    require(refs && (out || start == end), "null argument");
+    require(i < refs->contigs.size(), "contig index out of range");
+    const Contig& c = refs->contigs[i];
+    require(start <= end && end <= c.len, "range outside the contig");
+    static const char kBase[4] = {'A', 'C', 'G', 'T'};
+    for (uint64_t p = start; p < end; p++) out[p - start] = kBase[c.bits(p)];
+    return SA_OK;
+    SA_CATCH
+}
 uint32_t sa_refs_pick_bits(const sa_refs* refs, const sa_seeding_params* p) {
     return pick_bits(refs->contigs, to_seed_params(*p));
 }

@@ -305,10 +305,56 @@ bool LineReader::next(std::string_view& line, bool& newline) {
     return true;
 }
 
+// Lines the reference reads into a String (read_line) must be UTF-8, or the read fails
+// with an I/O error: every line of a FASTA file, and a FASTQ record's header lines.
+// RFC 3629 well-formedness (no overlong forms, no surrogates, nothing above U+10FFFF).
+static bool utf8_ok(std::string_view s) {
+    const auto* p = reinterpret_cast<const unsigned char*>(s.data());
+    const size_t n = s.size();
+    size_t i = 0;
+    while (i < n) {
+        // ASCII runs, eight bytes at a time
+        while (i + 8 <= n) {
+            uint64_t w;
+            std::memcpy(&w, p + i, 8);
+            if (w & 0x8080808080808080ULL) break;
+            i += 8;
+        }
+        if (i >= n) break;
+        const unsigned c = p[i];
+        if (c < 0x80) {
+            i++;
+            continue;
+        }
+        size_t len;
+        unsigned lo = 0x80, hi = 0xBF;  // range of the second byte
+        if (c >= 0xC2 && c <= 0xDF) len = 2;
+        else if (c == 0xE0) len = 3, lo = 0xA0;
+        else if (c >= 0xE1 && c <= 0xEC) len = 3;
+        else if (c == 0xED) len = 3, hi = 0x9F;
+        else if (c >= 0xEE && c <= 0xEF) len = 3;
+        else if (c == 0xF0) len = 4, lo = 0x90;
+        else if (c >= 0xF1 && c <= 0xF3) len = 4;
+        else if (c == 0xF4) len = 4, hi = 0x8F;
+        else return false;
+        if (i + len > n) return false;
+        if (p[i + 1] < lo || p[i + 1] > hi) return false;
+        for (size_t k = 2; k < len; k++)
+            if (p[i + k] < 0x80 || p[i + k] > 0xBF) return false;
+        i += len;
+    }
+    return true;
+}
+
+static void require_utf8(std::string_view line) {
+    if (!utf8_ok(line)) throw Error(SA_ERR_FORMAT, "stream did not contain valid UTF-8");
+}
+
+// trim_ascii_end: space, tab, line feed, form feed and carriage return (not vertical tab)
 static std::string_view trim_end_view(std::string_view s) {
     size_t e = s.size();
     while (e > 0 && (s[e - 1] == ' ' || s[e - 1] == '\t' || s[e - 1] == '\n' || s[e - 1] == '\r' ||
-                     s[e - 1] == '\f' || s[e - 1] == '\v'))
+                     s[e - 1] == '\f'))
         e--;
     return s.substr(0, e);
 }
@@ -366,6 +412,7 @@ void load_fasta(const std::string& path, std::vector<Contig>& out) {
     bool nl = false, have = false;
     Contig cur;
     while (f.next(line, nl)) {
+        require_utf8(line);
         if (!line.empty() && line[0] == '>') {
             if (have) out.push_back(std::move(cur));
             cur = Contig();
@@ -461,7 +508,10 @@ ReadParser::ReadParser(const std::string& path) : in_(path) {
         std::string_view h;
         bool nl;
         have_header_ = in_.next(h, nl);
-        if (have_header_) header_.assign(h);
+        if (have_header_) {
+            require_utf8(h);
+            header_.assign(h);
+        }
     }
 }
 
@@ -502,6 +552,7 @@ size_t ReadParser::parse(ReadStore& rs, size_t max_records) {
             rs.has_comment.push_back(hc);
             have_header_ = false;
             while (in_.next(line, nl)) {
+                require_utf8(line);
                 if (!line.empty() && line[0] == '>') {
                     header_.assign(line);
                     have_header_ = true;
@@ -518,6 +569,7 @@ size_t ReadParser::parse(ReadStore& rs, size_t max_records) {
     rs.qual_off_unused = 0;
     while (n < max_records) {
         if (!in_.next(line, nl)) break;
+        require_utf8(line);
         if (line.empty() || line[0] != '@') throw Error(SA_ERR_FORMAT, "FASTQ record must start with '@'");
         split_header_view(line.substr(1), name, comment, hc);
         if (name.empty()) throw Error(SA_ERR_FORMAT, "Record identifier is empty");
@@ -535,7 +587,7 @@ size_t ReadParser::parse(ReadStore& rs, size_t max_records) {
         const size_t L = rs.seq.size() - seq0;
         std::string_view plus;
         bool nl2;
-        in_.next(plus, nl2);
+        if (in_.next(plus, nl2)) require_utf8(plus);
         std::string_view qual;
         if (in_.next(line, nl)) qual = fastq_line(line, nl);
         else qual = std::string_view();

@@ -136,3 +136,107 @@ def test_estimate_read_length(tmp_path):
     assert sa.estimate_read_length(str(tmp_path / "empty.fq")) == 0
     with pytest.raises(sa.SaError, match="standard input"):
         sa.estimate_read_length("-")
+
+
+# The reference's own reader unit tests (src/io/fasta.rs:174-306, src/io/fastq.rs:97-120,
+# src/io/mod.rs:40-58) on the library's readers.
+
+def _refs(sa, tmp_path, data: bytes):
+    f = tmp_path / "ref.fa"
+    f.write_bytes(data)
+    return sa.References.from_fasta(str(f))
+
+
+def test_reference_fasta_phix(sa):
+    r = sa.References.from_fasta(str(GOLDEN / "phix.fasta"))
+    assert len(r) == 1 and r.contig(0) == ("NC_001422.1", 5386)
+    assert r.decode(0, 0, 5) == b"GAGTT"
+
+
+def test_reference_fasta_parse(sa, tmp_path):
+    r = _refs(sa, tmp_path, b">ref1 a comment\nacgt\n\n>ref2\naacc\ngg\n\ntt\n>empty\n>empty_at_end_of_file")
+    assert [r.contig(i)[0] for i in range(len(r))] == ["ref1", "ref2", "empty", "empty_at_end_of_file"]
+    assert [r.decode(i) for i in range(len(r))] == [b"ACGT", b"AACCGGTT", b"", b""]
+
+
+@pytest.mark.parametrize("data,names", [
+    (b"><>;abc\nAAAA\n>abc\nCCCC\n", ["<>;abc", "abc"]),
+    (b">ab c\nACGT\n>de\tf\nACGT\n", ["ab", "de"]),
+])
+def test_reference_fasta_names(sa, tmp_path, data, names):
+    r = _refs(sa, tmp_path, data)
+    assert [r.contig(i)[0] for i in range(len(r))] == names
+
+
+@pytest.mark.parametrize("data", [
+    b">name\x08\n",               # a control character in the name
+    b">\x00x80\nACGT\n",           # a NUL in the name
+    b">abc\nAAAA\n>abc\nCCCC\n",   # duplicate names
+    b"bla",                        # no '>' first
+    b">a\nAC\xffGT\n",             # not UTF-8 (read_line fails)
+])
+def test_reference_fasta_errors(sa, tmp_path, data):
+    with pytest.raises(sa.SaError):
+        _refs(sa, tmp_path, data)
+
+
+def test_reference_fasta_error_on_fastq(sa):
+    with pytest.raises(sa.SaError):
+        sa.References.from_fasta(str(GOLDEN / "phix.1.fastq"))
+
+
+def test_reference_fasta_wildcards_and_blanks(sa, tmp_path):
+    # a vertical tab is not ASCII whitespace to trim_ascii_end: it stays, as a wildcard
+    # base; a two-byte UTF-8 character is two wildcard bases; each wildcard takes the
+    # value encode_wildcard gives its position (src/packed_seq.rs:50-59)
+    r = _refs(sa, tmp_path, b">a\nAC\x0b\nG\xc3\xa9NT \t\r\n")
+    assert r.contig(0) == ("a", 8)
+
+    def wild(pos):
+        h = (pos * 0x9E3779B97F4A7C15) & (2 ** 64 - 1)
+        return b"ACGT"[(h ^ (h >> 30)) & 3:][:1]
+
+    assert r.decode(0) == b"AC" + wild(2) + b"G" + wild(4) + wild(5) + wild(6) + b"T"
+
+
+def test_fasta_reads_reference_cases(sa, tmp_path):
+    r = sa.Reads.from_file(str(GOLDEN / "phix.fasta"))
+    assert len(r) == 1 and r.names == b"NC_001422.1" and len(r.seq) == 5386 and r.seq[:5] == b"GAGTT"
+    f = tmp_path / "only_name.fa"
+    f.write_bytes(b">name\n")
+    r = sa.Reads.from_file(str(f))
+    assert len(r) == 1 and r.names == b"name" and r.seq == b""
+    f = tmp_path / "upper.fa"
+    f.write_bytes(b">name\r\nacgt\n>name2\nTgCa")
+    r = sa.Reads.from_file(str(f))
+    assert r.names == b"namename2" and list(r.name_offsets) == [0, 4, 9]
+    assert r.seq == b"ACGTTGCA" and list(r.seq_offsets) == [0, 4, 8]
+    f = tmp_path / "empty.fa"
+    f.write_bytes(b"")
+    assert len(sa.Reads.from_file(str(f))) == 0
+    f = tmp_path / "bad.fa"
+    f.write_bytes(b">a\nACGT\n>b\xfe\nACGT\n")
+    with pytest.raises(sa.SaError, match="UTF-8"):
+        sa.Reads.from_file(str(f))
+
+
+def test_fastq_reference_cases(sa, tmp_path):
+    f = tmp_path / "start.fq"
+    f.write_bytes(b"@a\nA\n+\n#\n>b")
+    with pytest.raises(sa.SaError):
+        sa.Reads.from_file(str(f))
+    # split_header: "id comment", "id comment ", "id", "id ", "id  "
+    f = tmp_path / "hdr.fq"
+    f.write_bytes(b"@id comment\nA\n+\nI\n@id comment \nA\n+\nI\n@id\nA\n+\nI\n@id \nA\n+\nI\n@id  \nA\n+\nI\n")
+    r = sa.Reads.from_file(str(f))
+    assert r.names == b"id" * 5 and r.comments == b"comment" * 2 and list(r.comment_offsets) == [0, 7, 14, 14, 14, 14]
+    # a vertical tab is kept in the name; bytes that are not UTF-8 are fine in sequence and
+    # quality lines (read as bytes) but not in the header (read as a String)
+    f = tmp_path / "vt.fq"
+    f.write_bytes(b"@id\x0b\nA\xffC\n+\nI\xfeI\n")
+    r = sa.Reads.from_file(str(f))
+    assert r.names == b"id\x0b" and r.seq == b"A\xffC" and r.qual == b"I\xfeI"
+    f = tmp_path / "bad.fq"
+    f.write_bytes(b"@a\nACGT\n+\nIIII\n@b\xc0\xaf\nACGT\n+\nIIII\n")
+    with pytest.raises(sa.SaError, match="UTF-8"):
+        sa.Reads.from_file(str(f))
