@@ -31,8 +31,15 @@ def test_version_and_defaults_without_gpu():
     p = sa.SeedingParameters.from_read_length(150)
     assert (p.k, p.s, p.w_min, p.w_max, p.max_dist) == (20, 16, 5, 11, 80)
     assert p.main_hash_mask == 0xFFFFFFFFFC000000 and p.partial_orientation_pos == 25
+    # src/seeding/parameters.rs:334-373: read length 251 takes the 250 profile
     p = sa.SeedingParameters.from_read_length(251)
-    assert (p.k, p.s, p.w_min, p.w_max, p.max_dist) == (22, 18, 6, 16, 180)
+    assert (p.k, p.s, p.w_min, p.w_max, p.max_dist, p.q) == (22, 18, 6, 16, 180, 255)
+    assert p.main_hash_mask == 0xFFFFFFFFFC000000 and p.partial_orientation_pos == 25
+    assert p.forward_main_hash_mask == 0xFFFFFFFFFC000000 | (1 << 25)
+    # :376-383: read lengths next to a profile's take its parameters
+    fields = [f for f, _ in type(p.c)._fields_]
+    as_tuple = lambda rl: tuple(getattr(sa.SeedingParameters.from_read_length(rl).c, f) for f in fields)
+    assert as_tuple(149) == as_tuple(150) == as_tuple(151)
     m = sa.mapping_defaults()
     assert (m.max_tries, m.rescue_distance, m.match, m.mismatch, m.gap_open, m.gap_extend, m.end_bonus) == \
         (20, 100, 2, 8, 12, 1, 10)
