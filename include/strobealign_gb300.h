@@ -402,6 +402,10 @@ int32_t sa_session_create(const sa_index* idx, const sa_refs* refs, const sa_cha
 /* Copies the batch (or, with borrow_inputs, refers to it) and queues it; r2 = NULL for
  * single-end.  SA_ERR_INVALID if the request can never fit in the arena. */
 int32_t sa_session_submit(sa_session* s, const sa_read_batch* r1, const sa_read_batch* r2, uint64_t* ticket);
+/* As sa_session_submit for mixed single-end and paired records in file order, paired by
+ * name as sa_map_batch_interleaved pairs them; the output equals sa_map_batch_interleaved
+ * on the same records alone. */
+int32_t sa_session_submit_interleaved(sa_session* s, const sa_read_batch* reads, uint64_t* ticket);
 /* *done = 1 once the request's output is ready. */
 int32_t sa_session_poll(sa_session* s, uint64_t ticket, int32_t* done);
 /* Waits up to timeout_ms (< 0: no limit; SA_ERR_TIMEOUT when it runs out) and

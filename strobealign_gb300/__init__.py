@@ -647,6 +647,16 @@ class Session:
             self._borrowed[t.value] = (r1, r2, b1, b2)
         return t.value
 
+    def submit_interleaved(self, reads: Reads) -> int:
+        """sa_session_submit_interleaved: mixed single-end and paired records in file
+        order, paired by name."""
+        b = reads.c()
+        t = C.c_uint64()
+        L.check(lib().sa_session_submit_interleaved(self.h, C.byref(b), C.byref(t)))
+        if self.borrow:
+            self._borrowed[t.value] = (reads, None, b, None)
+        return t.value
+
     @property
     def info(self) -> dict:
         """The device read arena (bases) and memory reserve the session chose, and the

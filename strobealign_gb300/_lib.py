@@ -131,6 +131,7 @@ SIGNATURES = {
     "sa_session_params_default": (None, [P(SessionParams)]),
     "sa_session_create": (i32, [vp, vp, P(ChainingParams), P(MappingParams), P(SessionParams), P(vp)]),
     "sa_session_submit": (i32, [vp, P(ReadBatch), P(ReadBatch), P(u64)]),
+    "sa_session_submit_interleaved": (i32, [vp, P(ReadBatch), P(u64)]),
     "sa_session_poll": (i32, [vp, u64, P(i32)]),
     "sa_session_wait": (i32, [vp, u64, i64, P(Output), P(RequestStats), P(f64), sz]),
     "sa_session_free": (None, [vp]),

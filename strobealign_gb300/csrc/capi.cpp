@@ -966,6 +966,14 @@ int32_t sa_session_submit(sa_session* s, const sa_read_batch* r1, const sa_read_
     SA_CATCH
 }
 
+int32_t sa_session_submit_interleaved(sa_session* s, const sa_read_batch* reads, uint64_t* ticket) {
+    SA_TRY
+    require(s && reads && ticket, "null argument");
+    *ticket = s->s->submit(reads, nullptr, true);
+    return SA_OK;
+    SA_CATCH
+}
+
 int32_t sa_session_poll(sa_session* s, uint64_t ticket, int32_t* done) {
     SA_TRY
     require(s && done, "null argument");

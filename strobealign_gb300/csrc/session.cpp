@@ -11,6 +11,7 @@
 #include <cstdlib>
 #include <cstring>
 
+#include "host_input.h"
 #include "host_util.h"
 #include "session.h"
 
@@ -161,8 +162,10 @@ Session::~Session() {
         if (l->st) cudaStreamDestroy(l->st);
 }
 
-uint64_t Session::submit(const sa_read_batch* r1, const sa_read_batch* r2) {
+uint64_t Session::submit(const sa_read_batch* r1, const sa_read_batch* r2, bool interleaved) {
     if (!r1) throw Error(SA_ERR_INVALID, "null read batch");
+    if (interleaved && r2) throw Error(SA_ERR_INVALID, "interleaved input takes one read batch");
+    if (interleaved && r1->n >= UINT32_MAX) throw Error(SA_ERR_INVALID, "batch too large");
     const bool paired = r2 != nullptr;
     if (paired && r2->n != r1->n) throw Error(SA_ERR_INVALID, "r1 and r2 batches differ in size");
     auto r = std::make_unique<Request>();
@@ -268,6 +271,13 @@ uint64_t Session::submit(const sa_read_batch* r1, const sa_read_batch* r2) {
     });
     r->seq_off[r->n_reads] = so;
     r->total_bases = so;
+    if (interleaved) {
+        // the reads stay in file order; records pair them by name (src/io/reads.rs:68-113)
+        pair_records_by_name(*r1, true, r->rec_read);
+        r->mixed = true;
+        r->nrec = r->rec_read.size() - 1;
+        r->bv.rec_read = r->rec_read.data();
+    }
     if (r->total_bases > seq_alloc_.capacity() || r->n_reads + 1 > off_alloc_.capacity())
         throw Error(SA_ERR_INVALID, "request larger than the session's in-flight capacity (" +
                                         std::to_string(seq_alloc_.capacity()) + " bases)");
@@ -437,11 +447,11 @@ void Session::admitter(AdmitLane& lane) {
         }
         // one NAM pipeline for the queued requests at the front, up to a read budget (the
         // fixed cost of a pipeline run is paid once) and to the device memory free for the
-        // workspace, all single-end or all paired-end
+        // workspace, all of one kind (single-end, paired-end or mixed)
         group.clear();
         uint64_t group_reads = 0, group_bases = 0;
-        const bool paired = queue_.front()->paired;
-        while (!queue_.empty() && (group.empty() || (queue_.front()->paired == paired &&
+        const int kind = queue_.front()->kind();
+        while (!queue_.empty() && (group.empty() || (queue_.front()->kind() == kind &&
                                                      group_reads + queue_.front()->n_reads <= admit_group_reads_ &&
                                                      fits(*queue_.front()) &&
                                                      mem_ok(group_bases + queue_.front()->total_bases)))) {
@@ -514,8 +524,8 @@ void Session::admit_group(const std::vector<Request*>& group, AdmitLane& lane) {
         bases += r->total_bases;
     }
     const uint32_t n = (uint32_t)n64;
-    const bool paired = group[0]->paired;
-    const bool nam_anchors = !paired && mp_.mode == SA_MODE_SAM && !mp_.use_ssw;
+    // single-end records (in a single-end or mixed group) extend piecewise on the NAMs' anchors
+    const bool nam_anchors = group[0]->kind() != 1 && mp_.mode == SA_MODE_SAM && !mp_.use_ssw;
     if (n > 0) {
         lane.h_seq.reserve(bases + 16);
         lane.h_off.reserve((size_t)n + 1);
@@ -631,7 +641,8 @@ void Session::admit_group(const std::vector<Request*>& group, AdmitLane& lane) {
         for (uint64_t i = 0; i < r.nrec;) {
             uint64_t nt = 0, j = i;
             while (j < r.nrec) {
-                nt += r.bv.reads[paired ? 2 * j : j].len + (paired ? r.bv.reads[2 * j + 1].len : 0);
+                const uint32_t f = r.bv.first_read(j);
+                nt += r.bv.reads[f].len + (r.bv.rec_paired(j) ? r.bv.reads[f + 1].len : 0);
                 j++;
                 if (nt > mp_.chunk_size) break;
             }

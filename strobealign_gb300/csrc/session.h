@@ -43,6 +43,12 @@ class RangeAllocator {
 struct Request {
     uint64_t id = 0;
     bool paired = false;
+    // mixed single-end and paired records (interleaved input): reads in file order,
+    // record r's reads from rec_read[r] to rec_read[r + 1]
+    bool mixed = false;
+    std::vector<uint32_t> rec_read;
+    // admission groups share one NAM pipeline configuration: single-end, paired, mixed
+    int kind() const { return mixed ? 2 : paired ? 1 : 0; }
     // owned copies of the records (empty when the session borrows the caller's batch)
     RawBytes seq, qual, names, comments;
     // sequences in device read order (mates interleaved) with per-read offsets;
@@ -114,7 +120,7 @@ class Session {
     Session(const sa_index* idx, const sa_refs* refs, const sa_chaining_params& cp, const sa_mapping_params& mp,
             const SessionConfig& sc);
     ~Session();
-    uint64_t submit(const sa_read_batch* r1, const sa_read_batch* r2);
+    uint64_t submit(const sa_read_batch* r1, const sa_read_batch* r2, bool interleaved = false);
     // 1 done, 0 not yet; throws for an unknown ticket
     int poll(uint64_t ticket);
     // Waits up to timeout_ms (< 0: no limit).  Returns false on timeout.  On

@@ -2,7 +2,8 @@
 interleaved input map mixed single-end and paired-end records (paired by name as
 src/io/reads.rs:68-113 pairs them) to the oracle's --interleaved bytes; phiX mates
 interleaved in one file give the reference's paired-end golden; a streamed mixed file
-gives the bytes of one batch."""
+gives the bytes of one batch; a serving session's mixed requests give the mapper's
+bytes."""
 import gzip
 import random
 
@@ -128,3 +129,23 @@ def test_map_files_interleaved_takes_one_file(mixed):
     m = sa.Mapper(s["idx"], s["refs"])
     with pytest.raises(sa.SaError, match="one reads file"):
         m.map_files(s["f"], s["f"], str(s["dir"] / "x.sam"), interleaved=True)
+
+
+@pytest.mark.parametrize("kw", [dict(eqx=1), dict(use_ssw=1, chunk_size=30_000, borrow_inputs=True)])
+def test_session_interleaved_requests(mixed, kw):
+    # mixed requests beside paired-end and single-end ones: each request's bytes equal
+    # the mapper's on the same records alone
+    s, sa = mixed, mixed["sa"]
+    kw = dict(kw)
+    borrow = kw.pop("borrow_inputs", False)
+    reads = sa.Reads.from_file(s["f"])
+    r1 = sa.Reads.from_file(str(s["dir"] / "r1.fq"))
+    r2 = sa.Reads.from_file(str(s["dir"] / "r2.fq"))
+    se = sa.Reads.from_file(str(s["dir"] / "se.fq"))
+    m = sa.Mapper(s["idx"], s["refs"], **kw)
+    want = [m.map_interleaved(reads), m.map(r1, r2), m.map(se), m.map_interleaved(reads)]
+    sess = sa.Session(s["idx"], s["refs"], borrow_inputs=borrow, **kw)
+    tickets = [sess.submit_interleaved(reads), sess.submit(r1, r2), sess.submit(se), sess.submit_interleaved(reads)]
+    got = [sess.wait(t)[0] for t in tickets]
+    for i, (g, w) in enumerate(zip(got, want)):
+        assert g == w, f"request {i} differs: " + _first_diff(g, w)
