@@ -173,6 +173,15 @@ typedef struct sa_reads sa_reads;
 int32_t sa_reads_from_file(const char* path, sa_reads** out);
 int32_t sa_reads_view(const sa_reads* reads, sa_read_batch* view);
 void sa_reads_free(sa_reads* reads);
+/* A read file read in batches, as the reference's record iterator yields records
+ * (src/io/reads.rs:121-132 over FastqReader / FastaReader): sa_read_file_next parses up
+ * to max_records more records into a new owned batch (release with sa_reads_free); a
+ * batch of 0 records marks the end of the input.  Same formats and rules as
+ * sa_reads_from_file. */
+typedef struct sa_read_file sa_read_file;
+int32_t sa_read_file_open(const char* path, sa_read_file** out);
+int32_t sa_read_file_next(sa_read_file* f, size_t max_records, sa_reads** out);
+void sa_read_file_close(sa_read_file* f);
 /* The records InterleavedIterator forms from reads in file order (src/io/reads.rs:68-113):
  * a read and the next one are a pair when their names are equal, any other read is
  * single-end.  first_read[r] = record r's first read, for r < *n_records, then

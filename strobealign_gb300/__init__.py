@@ -188,6 +188,25 @@ class StrobemerIndex:
             self.h = C.c_void_p()
 
 
+class ReadFile:
+    """sa_read_file_*: a read file read in batches (next(n) gives up to n more records,
+    an empty batch at the end)."""
+
+    def __init__(self, path: str):
+        self.h = C.c_void_p()
+        L.check(lib().sa_read_file_open(os.fsencode(path), C.byref(self.h)))
+
+    def next(self, max_records: int) -> "Reads":
+        h = C.c_void_p()
+        L.check(lib().sa_read_file_next(self.h, max_records, C.byref(h)))
+        return Reads._take(h)
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().sa_read_file_close(self.h)
+            self.h = C.c_void_p()
+
+
 @dataclass
 class Reads:
     """A batch of reads as concatenated buffers (the C ABI's sa_read_batch)."""
@@ -229,6 +248,11 @@ class Reads:
     def from_file(cls, path: str) -> "Reads":
         h = C.c_void_p()
         L.check(lib().sa_reads_from_file(str(path).encode(), C.byref(h)))
+        return cls._take(h)
+
+    @classmethod
+    def _take(cls, h: C.c_void_p) -> "Reads":
+        """A copy of an owned sa_reads batch, which is then freed."""
         try:
             v = L.ReadBatch()
             L.check(lib().sa_reads_view(h, C.byref(v)))

@@ -159,6 +159,9 @@ SIGNATURES = {
     "sa_reads_from_file": (i32, [cp, P(vp)]),
     "sa_reads_view": (i32, [vp, P(ReadBatch)]),
     "sa_reads_free": (None, [vp]),
+    "sa_read_file_open": (i32, [cp, P(vp)]),
+    "sa_read_file_next": (i32, [vp, sz, P(vp)]),
+    "sa_read_file_close": (None, [vp]),
     "sa_reads_pair_interleaved": (i32, [P(ReadBatch), vp, sz, P(sz)]),
     "sa_estimate_read_length": (i32, [cp, P(sz)]),
     "sa_randstrobes_batch": (i32, [vp, P(ReadBatch), P(QueryRandstrobe), sz, P(u64), P(u32)]),

@@ -349,6 +349,33 @@ int32_t sa_reads_from_file(const char* path, sa_reads** out) {
     SA_CATCH
 }
 
+struct sa_read_file {
+    std::unique_ptr<ReadParser> parser;
+};
+
+int32_t sa_read_file_open(const char* path, sa_read_file** out) {
+    SA_TRY
+    require(path && out, "null argument");
+    auto f = std::make_unique<sa_read_file>();
+    f->parser = std::make_unique<ReadParser>(path);
+    *out = f.release();
+    return SA_OK;
+    SA_CATCH
+}
+
+int32_t sa_read_file_next(sa_read_file* f, size_t max_records, sa_reads** out) {
+    SA_TRY
+    require(f && out, "null argument");
+    auto r = std::make_unique<sa_reads>();
+    reset_read_store(r->store, !f->parser->fasta());
+    f->parser->parse(r->store, max_records);
+    *out = r.release();
+    return SA_OK;
+    SA_CATCH
+}
+
+void sa_read_file_close(sa_read_file* f) { delete f; }
+
 int32_t sa_reads_view(const sa_reads* reads, sa_read_batch* v) {
     SA_TRY
     require(reads && v, "null argument");
