@@ -627,6 +627,13 @@ static void deduplicate_scored_pairs(std::vector<ScoredAlignmentPair>& p) {
     p.resize(j);
 }
 
+// src/mapper.rs:1360-1369: the pairs that share the first (best) score of a sorted list
+static size_t count_best_alignment_pairs(const std::vector<ScoredAlignmentPair>& p) {
+    size_t nb = 0;
+    while (nb < p.size() && p[nb].score == p[0].score) nb++;
+    return nb;
+}
+
 // src/mapper.rs:778-1014 (returns true for the Proper fast path)
 static bool extend_paired_seeds(const Context& ctx, std::vector<Nam> nams[2], const Read& read1, const Read& read2,
                                 size_t k, Details det[2], const InsertSizeDistribution& isd, Alignment proper[2],
@@ -801,9 +808,7 @@ std::string align_paired_end_read(const SequenceRecord& r1, const SequenceRecord
         std::stable_sort(pairs.begin(), pairs.end(),
                          [](const ScoredAlignmentPair& a, const ScoredAlignmentPair& b) { return a.score > b.score; });
         deduplicate_scored_pairs(pairs);
-        size_t nb = 0;
-        if (!pairs.empty())
-            while (nb < pairs.size() && pairs[nb].score == pairs[0].score) nb++;
+        const size_t nb = count_best_alignment_pairs(pairs);
         det[0].best_alignments = nb;
         det[1].best_alignments = nb;
         if (nb > 1) {
@@ -1043,3 +1048,50 @@ void abundances_paired_end_read(const SequenceRecord& r1, const SequenceRecord& 
 }
 
 }  // namespace oracle
+
+// Hooks for the reference's unit tests of the pair helpers (src/mapper.rs tests
+// is_proper_pair_*, deduplicate_scored_pairs_works, count_best_alignment_pairs_works)
+extern "C" {
+
+int32_t ora_is_proper_pair(uint64_t ref1, uint64_t start1, int32_t rc1, uint64_t ref2, uint64_t start2, int32_t rc2,
+                           float mu, float sigma) {
+    oracle::Alignment a, b;
+    a.reference_id = ref1;
+    a.ref_start = start1;
+    a.is_revcomp = rc1 != 0;
+    b.reference_id = ref2;
+    b.ref_start = start2;
+    b.is_revcomp = rc2 != 0;
+    return oracle::is_proper_pair(a, b, mu, sigma) ? 1 : 0;
+}
+
+// n pairs: score, then per mate present / reference / start (ref_start < 0: absent);
+// deduplicated in place; returns how many are left and their scores in out_score
+size_t ora_deduplicate_scored_pairs(size_t n, const double* score, const int64_t* ref1, const int64_t* start1,
+                                    const int64_t* ref2, const int64_t* start2, double* out_score) {
+    std::vector<oracle::ScoredAlignmentPair> v(n);
+    for (size_t i = 0; i < n; i++) {
+        v[i].score = score[i];
+        if (start1[i] >= 0) {
+            v[i].a1 = oracle::Alignment();
+            v[i].a1->reference_id = (size_t)ref1[i];
+            v[i].a1->ref_start = (size_t)start1[i];
+        }
+        if (start2[i] >= 0) {
+            v[i].a2 = oracle::Alignment();
+            v[i].a2->reference_id = (size_t)ref2[i];
+            v[i].a2->ref_start = (size_t)start2[i];
+        }
+    }
+    oracle::deduplicate_scored_pairs(v);
+    for (size_t i = 0; i < v.size(); i++) out_score[i] = v[i].score;
+    return v.size();
+}
+
+size_t ora_count_best_alignment_pairs(size_t n, const double* score) {
+    std::vector<oracle::ScoredAlignmentPair> v(n);
+    for (size_t i = 0; i < n; i++) v[i].score = score[i];
+    return oracle::count_best_alignment_pairs(v);
+}
+
+}  // extern "C"

@@ -336,3 +336,41 @@ def test_stage_entry_points_reject_bad_input(sa):
         sa.piecewise_batch(["ACGTACGTAC"], ["ACGTACGTAC"], [[]], 5)  # no anchors
     with pytest.raises(sa.SaError):
         sa.hamming_batch(["ACGT"], ["ACGT"], [2])
+
+
+def test_oracle_pair_helpers():
+    # src/mapper.rs tests: is_proper_pair_within_distance, _rev_within_distance,
+    # _incompatible, _too_far (mu 300, sigma 50), deduplicate_scored_pairs_works,
+    # count_best_alignment_pairs_works
+    lib = oracle()
+    lib.ora_is_proper_pair.restype = C.c_int32
+    lib.ora_is_proper_pair.argtypes = [C.c_uint64, C.c_uint64, C.c_int32, C.c_uint64, C.c_uint64, C.c_int32,
+                                       C.c_float, C.c_float]
+    proper = lambda a, b: lib.ora_is_proper_pair(a[0], a[1], a[2], b[0], b[1], b[2], 300.0, 50.0) == 1
+    assert proper((0, 100, False), (0, 350, True))
+    assert proper((0, 350, True), (0, 100, False))
+    assert not proper((0, 100, False), (0, 350, False))
+    assert not proper((0, 100, False), (0, 10_000, True))
+    d = C.POINTER(C.c_double)
+    i64 = C.POINTER(C.c_int64)
+    lib.ora_deduplicate_scored_pairs.restype = C.c_size_t
+    lib.ora_deduplicate_scored_pairs.argtypes = [C.c_size_t, d, i64, i64, i64, i64, d]
+
+    def dedup(rows):
+        n = len(rows)
+        arr = lambda k, t: (t * n)(*[r[k] for r in rows])
+        out = (C.c_double * max(n, 1))()
+        m = lib.ora_deduplicate_scored_pairs(n, arr(0, C.c_double), arr(1, C.c_int64), arr(2, C.c_int64),
+                                             arr(3, C.c_int64), arr(4, C.c_int64), out)
+        return list(out[:m])
+
+    assert dedup([(733.0, 0, 1906, 0, 123), (724.0, 0, 1906, 0, 123)]) == [733.0]
+    # consecutive duplicates only, compared with the last kept pair; an absent mate
+    # matches only an absent mate
+    assert dedup([(9.0, 0, 5, 0, 9), (8.0, 0, 5, 0, 9), (7.0, 0, 6, 0, 9), (6.0, 0, 5, 0, 9),
+                  (5.0, 0, 5, -1, -1), (4.0, 0, 5, -1, -1)]) == [9.0, 7.0, 6.0, 5.0]
+    lib.ora_count_best_alignment_pairs.restype = C.c_size_t
+    lib.ora_count_best_alignment_pairs.argtypes = [C.c_size_t, d]
+    best = lambda s: lib.ora_count_best_alignment_pairs(len(s), (C.c_double * max(len(s), 1))(*s))
+    assert [best([]), best([10.0]), best([10.0, 10.0]), best([10.0, 10.0, 5.0]), best([10.0, 5.0, 5.0])] == \
+        [0, 1, 2, 2, 1]
