@@ -455,6 +455,7 @@ uint32_t pick_bits(const std::vector<Contig>& cs, const SeedParams& p) {
 
 void pair_records_by_name(const sa_read_batch& reads, bool at_end, std::vector<uint32_t>& rec_read) {
     const size_t n = reads.n;
+    if (n >= UINT32_MAX) throw Error(SA_ERR_INVALID, "batch too large");
     rec_read.clear();
     rec_read.reserve(n + 1);
     auto name = [&](size_t i) {
