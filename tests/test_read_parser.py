@@ -9,7 +9,6 @@ missing last newline and lines longer than the reader's buffer."""
 import gzip
 import random
 
-import numpy as np
 import pytest
 
 
@@ -197,3 +196,26 @@ def test_read_file_errors(tmp_path):
         sa.ReadFile(str(tmp_path / "missing.fq"))
     (tmp_path / "e.fq").write_bytes(b"")
     assert len(sa.ReadFile(str(tmp_path / "e.fq")).next(10)) == 0
+
+
+def test_header_utf8_rule_matches_python(tmp_path):
+    # a header line the reference reads into a String fails exactly when it is not UTF-8
+    import strobealign_gb300 as sa
+    rnd = random.Random(21)
+    alphabet = [0x41, 0x7F, 0x80, 0xBF, 0xC0, 0xC1, 0xC2, 0xDF, 0xE0, 0xED, 0xEF, 0xF0, 0xF4, 0xF5, 0xFF, 0x9F,
+                0xA0, 0x8F, 0x90]
+    path = tmp_path / "h.fq"
+    for _ in range(400):
+        body = bytes(rnd.choice(alphabet) for _ in range(rnd.randint(1, 6)))
+        head = b"@a" + body
+        path.write_bytes(head + b"\nA\n+\nI\n")
+        try:
+            head.decode("utf-8")
+            ok = True
+        except UnicodeDecodeError:
+            ok = False
+        if ok:
+            assert len(sa.Reads.from_file(str(path))) == 1
+        else:
+            with pytest.raises(sa.SaError, match="UTF-8"):
+                sa.Reads.from_file(str(path))
