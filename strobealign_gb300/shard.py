@@ -23,6 +23,16 @@ def record_lengths(offsets1: np.ndarray, offsets2: np.ndarray | None = None) -> 
     return n
 
 
+def interleaved_record_lengths(seq_offsets: np.ndarray, first_read: np.ndarray) -> np.ndarray:
+    """Nucleotides per record of interleaved input (a single read or a pair), from the
+    reads' offsets and each record's first read (Reads.interleaved_records: record r is
+    reads first_read[r] .. first_read[r + 1]); a record range [a, b) is then the reads
+    [first_read[a], first_read[b])."""
+    o = np.asarray(seq_offsets, dtype=np.int64)
+    f = np.asarray(first_read, dtype=np.int64)
+    return o[f[1:]] - o[f[:-1]]
+
+
 def chunk_starts(lengths: np.ndarray, chunk_size: int = 1_000_000) -> np.ndarray:
     """Record index of every chunk start, then the record count: a chunk takes records
     until its nucleotides exceed chunk_size (the record that crosses is its last)."""

@@ -99,3 +99,75 @@ def test_two_gloo_ranks_reproduce_the_single_process_bytes():
     g, r1, r2 = _data()
     want = OracleIndex(g.names, g.seqs, 150, threads=1).map_batch(r1, r2, chunk_size=CHUNK, threads=1)[0]
     assert got == want
+
+
+def _interleaved_data():
+    # a mixed file's reads in order: pairs (mates with one name) and single reads
+    from strobealign_gb300 import synthetic as syn
+    g, r1, r2 = _data()
+    se = syn.make_single_end(73, g, 700, (60, 300), 0.01, 0.002)
+    seqs, names = [], []
+    rnd = np.random.default_rng(74)
+    i = j = 0
+    while i < len(r1) or j < len(se):
+        if j == len(se) or (i < len(r1) and rnd.random() < 0.6):
+            for rs in (r1, r2):
+                n, s = rs.record(i)
+                names.append(n)
+                seqs.append(s)
+            i += 1
+        else:
+            n, s = se.record(j)
+            names.append(n)
+            seqs.append(s)
+            j += 1
+    return g, names, seqs
+
+
+def _read_set(names, seqs):
+    from strobealign_gb300 import synthetic as syn
+    off = np.zeros(len(seqs) + 1, dtype=np.uint64)
+    off[1:] = np.cumsum([len(s) for s in seqs])
+    no = np.zeros(len(names) + 1, dtype=np.uint64)
+    no[1:] = np.cumsum([len(n) for n in names])
+    seq = np.frombuffer(b"".join(seqs), dtype=np.uint8)
+    return syn.ReadSet(seq, off, "".join(names).encode(), no, b"I" * int(off[-1]))
+
+
+def _rank_interleaved(rank, world, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from oracle.binding import OracleIndex
+    from strobealign_gb300 import Reads, shard
+    g, names, seqs = _interleaved_data()
+    first = Reads.from_lists(names, seqs).interleaved_records()
+    off = np.concatenate([[0], np.cumsum([len(s) for s in seqs])])
+    a, b = shard.shard_ranges(shard.interleaved_record_lengths(off, first), world, CHUNK)[rank]
+    ra, rb = int(first[a]), int(first[b])
+    idx = OracleIndex(g.names, g.seqs, 150, threads=1)
+    mine = idx.map_interleaved(_read_set(names[ra:rb], seqs[ra:rb]), chunk_size=CHUNK, threads=1)[0] \
+        if rb > ra else b""
+    out = shard.gather_in_order(mine, rank, world, dist)
+    q.put((rank, (a, b), out))
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_reproduce_the_single_process_bytes_interleaved():
+    # mixed single-end and paired records: ranges of whole records, pairs never split
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_interleaved, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted(q.get(timeout=300) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    (_, rng0, got), (_, rng1, none) = out
+    assert none is None and rng0[1] == rng1[0] > 0
+    from oracle.binding import OracleIndex
+    g, names, seqs = _interleaved_data()
+    want = OracleIndex(g.names, g.seqs, 150, threads=1).map_interleaved(_read_set(names, seqs), chunk_size=CHUNK,
+                                                                        threads=1)[0]
+    assert got == want
